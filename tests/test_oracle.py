@@ -1,0 +1,116 @@
+"""The CPU oracle against the reference: tables, golden fixtures, digests, and (where the
+reference was compiled here) a direct comparison on seeded fields."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import cpu_libs
+from tmc_gb300 import volumes as V
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def _load_small():
+    z = np.load(os.path.join(GOLDEN, "golden.npz"))
+    names = sorted({k.split("__")[0] for k in z.files})
+    return z, names
+
+
+def _vol_from(z, name):
+    meta = z[f"{name}__meta"]
+    return V.Volume(z[f"{name}__field"], origin=tuple(meta[1:4]), spacing=tuple(meta[4:7]), iso=float(meta[0])), \
+        int(meta[7]), int(meta[8])
+
+
+def test_tables_match_reference():
+    """Packed tables (tmc_gb300/csrc/mc_tables.h) equal the reference tables
+    (mc/MarchingCubes.h e_pattern/t_ambig/t_pattern, cpp_dmc/LookupTables.h r_pattern)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "gen_tables", os.path.join(cpu_libs.ROOT, "tmc_gb300", "csrc", "gen_tables.py"))
+    g = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(g)
+    ref = json.load(open(os.path.join(GOLDEN, "ref_tables.json")))
+    assert [g.edge_mask(c) for c in range(256)] == ref["mc_e_pattern"]
+    assert [105 if g.ambiguous(c) else c for c in range(256)] == ref["mc_t_ambig"] == ref["dmc_t_ambig"]
+    # the header must be what the generator writes today
+    hdr = open(os.path.join(cpu_libs.ROOT, "tmc_gb300", "csrc", "mc_tables.h")).read()
+    for c in range(256):
+        row = ref["mc_t_pattern"][16 * c: 16 * c + 16]
+        n = next((i for i in range(0, 16, 3) if row[i] == -1), 15) // 3
+        word = n
+        for t in range(n):
+            for k in range(3):
+                word |= (row[3 * t + k] & 0xF) << (4 + 4 * (3 * t + k))
+        assert f"0x{word:016x}ull" in hdr
+    # every unambiguous r_pattern contour is the rule contour rotated to its start edge
+    rp = ref["dmc_r_pattern"]
+    for c in range(256):
+        if g.ambiguous(c) or rp[17 * c] == 0:
+            continue
+        mine = g.contours(c)[0]
+        want = rp[17 * c + 2: 17 * c + 2 + rp[17 * c + 1]]
+        r = mine.index(want[0])
+        assert mine[r:] + mine[:r] == want
+
+
+@pytest.mark.parametrize("name", _load_small()[1])
+def test_oracle_golden_small(oracle, name):
+    z, _ = _load_small()
+    vol, simp, flip = _vol_from(z, name)
+    out = oracle.dmc(vol, simp, flip) if name.endswith(("_dmc", "_simplify", "_flip")) else oracle.tmc(vol)
+    for k in [k.split("__")[1] for k in z.files if k.startswith(name + "__")]:
+        if k in ("field", "meta"):
+            continue
+        np.testing.assert_array_equal(out[k], z[f"{name}__{k}"], err_msg=f"{name}:{k}")
+
+
+def _digest_cases():
+    return sorted(json.load(open(os.path.join(GOLDEN, "digests.json"))).items())
+
+
+@pytest.mark.parametrize("name,case", _digest_cases(), ids=[n for n, _ in _digest_cases()])
+def test_oracle_digests(oracle, name, case):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    vol = mg.make_volume(case["recipe"])
+    assert _digest(vol.data) == case["field"], "field generation differs on this platform"
+    out = oracle.dmc(vol, case["simplify"], case["flip"]) if case["algo"] == "dmc" else oracle.tmc(vol)
+    for k, d in case["digests"].items():
+        assert out[k].size == case["sizes"][k], f"{name}:{k} size"
+        assert _digest(out[k]) == d, f"{name}:{k}"
+
+
+@pytest.mark.skipif(not cpu_libs.ref_available(), reason="reference not compiled here (make -C oracle ref)")
+@pytest.mark.parametrize("seed", [101, 102, 103])
+def test_oracle_vs_reference_random(oracle, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = [int(x) for x in rng.integers(9, 30, size=3)]
+    d = V.upsampled_noise(max(n), rng, coarse=5)[: n[2], : n[1], : n[0]].copy()
+    vol = V.Volume(d, spacing=(0.1, 0.2, 0.15), origin=(0.5, -1.0, 2.0), iso=float(rng.uniform(-0.2, 0.2)))
+    ref = cpu_libs.RefLib()
+    for simp in (0, 1):
+        a, b = oracle.dmc(vol, simp, seed & 1), ref.dmc(vol, simp, seed & 1)
+        for k in a:
+            np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    a, b = oracle.tmc(vol), ref.tmc(vol)
+    for k in b:
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
+def test_oracle_empty_volume(oracle):
+    """A field entirely above the isovalue gives an empty mesh (the reference's dualMC crashes on
+    an empty mesh with simplification on; the oracle returns empty arrays)."""
+    vol = V.Volume(np.ones((8, 9, 10), np.float32), spacing=(1, 1, 1), iso=0.0)
+    out = oracle.dmc(vol, 1, 0)
+    assert out["v"].size == 0 and out["q"].size == 0
+    assert oracle.tmc(vol)["t"].size == 0
