@@ -1,0 +1,125 @@
+/* tmc_gb300: uniform-grid isosurface extraction on one GB300 (sm_103a).
+ *
+ * C ABI over hand-written CUDA kernels.  Plain C types only; every entry point returns a
+ * tmc_status and never exits the process.  The entry points replace these reference calls:
+ *
+ *   tmc_dmc_extract        dmc::DualMarchingCubes::dualMC          cpp_dmc/DualMarchingCubes.h:163-165
+ *                          p_mc::DualMarchingCubes::dualMC          dmc/DualMarchingCubes.h:74-77
+ *   tmc_tmc_sharedvertex   p_mc::MarchingCubes::mc_sharedvertex     cuda_tmc/MarchingCubes.h:60
+ *                          tmc::MarchingCubes::t_mc (via operator()) mc/MarchingCubes.h:301, mc/MarchingCubes.cpp:151
+ *   tmc_tmc_halfedge       p_mc::MarchingCubes::mc_halfedge         cuda_tmc/MarchingCubes.h:71
+ *   tmc_batch_extract      (no single reference call: many dualMC / mc_sharedvertex calls in one launch)
+ *   tmc_server_*           (no reference counterpart: request loop around the calls above)
+ *
+ * Threading: a context is thread-compatible, not thread-safe; use one context per host thread.
+ * All work of a context runs on its own CUDA stream.
+ */
+#ifndef TMC_GB300_H
+#define TMC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tmc_status {
+  TMC_OK = 0,
+  TMC_ERR_INVALID_ARG = 1, /* null pointer, bad size, unknown flag */
+  TMC_ERR_OOM = 2,         /* device or host allocation failed */
+  TMC_ERR_CAPACITY = 3,    /* a fixed-capacity buffer overflowed (batched/served paths) */
+  TMC_ERR_CUDA = 4,        /* a CUDA runtime call failed; see tmc_last_error */
+  TMC_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
+  TMC_ERR_NUMERIC = 6,     /* the field holds NaN or Inf */
+  TMC_ERR_INTERNAL = 7
+} tmc_status;
+
+typedef struct tmc_ctx tmc_ctx;
+
+typedef struct tmc_ctx_opts {
+  size_t reserve_bytes; /* device memory the context keeps pooled between calls (0 = default) */
+  int32_t check_numeric; /* 1: scan the field for NaN/Inf and fail with TMC_ERR_NUMERIC */
+  int32_t reserved;
+} tmc_ctx_opts;
+
+/* A uniform grid: point (i,j,k) sits at origin + (i,j,k)*spacing; data[(k*ny + j)*nx + i]. */
+typedef struct tmc_volume {
+  int32_t nx, ny, nz;   /* grid points per axis, each >= 2 */
+  double origin[3];
+  double spacing[3];
+  const float* data;    /* float32 scalar field, x fastest */
+  int32_t on_device;    /* 1: `data` is device memory on the context's device; 0: host memory */
+  int32_t reserved;
+} tmc_volume;
+
+/* flags */
+enum {
+  /* DMC mesh simplification, as cpp_dmc's sFlag (DualMarchingCubes.cpp:60-72): P3X3Y colour pass,
+   * P3X3Y isolated pass and P3333.  The three can also be chosen one by one. */
+  TMC_DMC_SIMPLIFY = 1u << 0,
+  TMC_DMC_P3X3Y_COLOR = 1u << 1,
+  TMC_DMC_P3X3Y_ISOLATED = 1u << 2,
+  TMC_DMC_P3333 = 1u << 3,
+  TMC_OUT_TRIANGLES = 1u << 4,  /* DMC: also split quads into triangles (collectTriangles) */
+  TMC_OUT_HALFEDGES = 1u << 5,  /* halfedges {origin, face, next, twin} + vertex/face handles */
+  TMC_OUT_HOST = 1u << 6,       /* results in host memory (owned by the mesh) instead of device */
+  TMC_OUT_POS_F64 = 1u << 7,    /* also emit float64 positions, bit-equal to the CPU reference */
+  TMC_OUT_LOCAL = 1u << 8,      /* DMC without simplification: per-vertex generating cell + local (u,v,w) */
+  TMC_GRAD_FLIP = 1u << 9,      /* DMC normals from the negated gradient (UniformGrid::flip_gradient) */
+  TMC_TMC_KEY32 = 1u << 10      /* TMC: reproduce the reference's 32-bit edge keys (int overflow included) */
+};
+
+typedef struct tmc_mesh {
+  int64_t nr_v, nr_q, nr_t, nr_he;
+  int32_t on_device; /* 1: arrays are device pointers (valid until tmc_mesh_free) */
+  int32_t reserved;
+  float* v;          /* 3*nr_v positions */
+  float* n;          /* 3*nr_v unit normals */
+  double* v64;       /* 3*nr_v float64 positions (TMC_OUT_POS_F64), else NULL */
+  int32_t* quads;    /* 4*nr_q (DMC) */
+  int32_t* tris;     /* 3*nr_t */
+  int32_t* he;       /* 4*nr_he: origin, face, next, twin (-1 = boundary) */
+  int32_t* he_v;     /* nr_v: one outgoing halfedge per vertex */
+  int32_t* he_f;     /* per face: its first halfedge */
+  int64_t* vcell;    /* nr_v generating cell (TMC_OUT_LOCAL) */
+  float* vuvw;       /* 3*nr_v local coordinates in the generating cell (TMC_OUT_LOCAL) */
+  int64_t stats[8];  /* [0] active cells [1] ambiguous cells [2,3] representative fallbacks
+                        (7x7 then 26x26 failed) [4] non-manifold edges [5] singular faces [6] cells */
+  void* priv;
+} tmc_mesh;
+
+/* context ---------------------------------------------------------------------------------- */
+tmc_status tmc_ctx_create(int device, const tmc_ctx_opts* opts, tmc_ctx** out);
+tmc_status tmc_ctx_destroy(tmc_ctx* ctx);
+const char* tmc_last_error(const tmc_ctx* ctx);
+void* tmc_ctx_stream(tmc_ctx* ctx); /* the context's cudaStream_t */
+tmc_status tmc_ctx_synchronize(tmc_ctx* ctx);
+/* number of library kernels launched by this context since creation */
+int64_t tmc_ctx_launch_count(const tmc_ctx* ctx);
+
+/* extraction -------------------------------------------------------------------------------- */
+/* Dual Marching Cubes: quad mesh (+ triangles, + halfedges).  Vertices in generating-cell order,
+ * quads in dual-edge key order, as the reference CPU path emits them. */
+tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t flags, tmc_mesh* out);
+/* Topologically correct Marching Cubes, shared-vertex triangle mesh. */
+tmc_status tmc_tmc_sharedvertex(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t flags, tmc_mesh* out);
+/* Topologically correct Marching Cubes with the triangle halfedge structure. */
+tmc_status tmc_tmc_halfedge(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t flags, tmc_mesh* out);
+tmc_status tmc_mesh_free(tmc_ctx* ctx, tmc_mesh* mesh);
+
+/* batched extraction ------------------------------------------------------------------------ */
+enum { TMC_ALGO_DMC = 0, TMC_ALGO_TMC = 1 };
+typedef struct tmc_request {
+  tmc_volume vol;
+  double iso;
+  uint32_t algo;  /* TMC_ALGO_DMC or TMC_ALGO_TMC */
+  uint32_t flags;
+} tmc_request;
+/* Extract n independent requests in one batched pipeline (device-resident fields). */
+tmc_status tmc_batch_extract(tmc_ctx* ctx, int32_t n, const tmc_request* reqs, tmc_mesh* outs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TMC_GB300_H */

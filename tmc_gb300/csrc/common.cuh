@@ -1,0 +1,192 @@
+// Device-side building blocks shared by the DMC and TMC kernels: the grid view, packed cell
+// topology, MC polygons (contours) and small helpers.
+//
+// Arithmetic note: this library is compiled with -fmad=false, so every float/double expression
+// written here rounds each operation exactly as the reference's CPU code does when compiled
+// without floating-point contraction.  Hot loops that want fused multiply-adds use explicit
+// __fmaf_rn / __fma_rn.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mc_tables.h"
+
+namespace tmc {
+
+// ------------------------------------------------------------------------------------------
+// grid view
+// ------------------------------------------------------------------------------------------
+struct Grid {
+  const float* f;
+  int nx, ny, nz;     // points
+  double ox, oy, oz;  // origin
+  double dx, dy, dz;  // spacing
+  double iso;
+  float iso_up;       // smallest float >= iso:  (double)f >= iso  <=>  f >= iso_up
+  int pad;
+  __host__ __device__ int cx() const { return nx - 1; }
+  __host__ __device__ int cy() const { return ny - 1; }
+  __host__ __device__ int cz() const { return nz - 1; }
+  __host__ __device__ int64_t ncells() const { return (int64_t)(nx - 1) * (ny - 1) * (nz - 1); }
+  __device__ __forceinline__ float at(int i, int j, int k) const {
+    return __ldg(f + ((int64_t)k * ny + j) * nx + i);
+  }
+  __host__ __device__ __forceinline__ int64_t cell_index(int i, int j, int k) const {
+    return ((int64_t)k * (ny - 1) + j) * (nx - 1) + i;
+  }
+};
+
+// ------------------------------------------------------------------------------------------
+// packed topology lookups (4 bits per entry)
+// ------------------------------------------------------------------------------------------
+__host__ __device__ __forceinline__ int nib(uint64_t w, int i) { return (int)((w >> (4 * i)) & 0xF); }
+__host__ __device__ __forceinline__ int edge_v0(int e) { return nib(TMC_PK_EDGE_V0, e); }
+__host__ __device__ __forceinline__ int edge_v1(int e) { return nib(TMC_PK_EDGE_V1, e); }
+__host__ __device__ __forceinline__ int edge_off(int e) { return nib(TMC_PK_EDGE_OFF, e); }   // di|dj<<1|dk<<2
+__host__ __device__ __forceinline__ int edge_axis(int e) { return nib(TMC_PK_EDGE_AXIS, e); }
+__host__ __device__ __forceinline__ int quad_slot(int e, int neg) {
+  return neg ? nib(TMC_PK_QUAD_SLOT1, e) : nib(TMC_PK_QUAD_SLOT0, e);
+}
+__host__ __device__ __forceinline__ uint32_t face_v_pack(int f) {
+  constexpr uint32_t P[6] = {TMC_PK_FACE_V0, TMC_PK_FACE_V1, TMC_PK_FACE_V2,
+                             TMC_PK_FACE_V3, TMC_PK_FACE_V4, TMC_PK_FACE_V5};
+  return P[f];
+}
+__host__ __device__ __forceinline__ uint32_t face_e_pack(int f) {
+  constexpr uint32_t P[6] = {TMC_PK_FACE_E0, TMC_PK_FACE_E1, TMC_PK_FACE_E2,
+                             TMC_PK_FACE_E3, TMC_PK_FACE_E4, TMC_PK_FACE_E5};
+  return P[f];
+}
+// single segment of the face cases that need no decider: face-local edge a -> edge b
+#define TMC_PK_FACE_RULE_A 0x303220210031100ull
+#define TMC_PK_FACE_RULE_B 0x11300120223030ull
+
+__host__ __device__ __forceinline__ bool case_ambiguous(unsigned c) {
+  const uint64_t w = (c < 128) ? ((c < 64) ? TMC_AMBIGUOUS_W0 : TMC_AMBIGUOUS_W1)
+                               : ((c < 192) ? TMC_AMBIGUOUS_W2 : TMC_AMBIGUOUS_W3);
+  return (w >> (c & 63)) & 1ull;
+}
+// edges crossed by the isosurface for case c (bit e)
+__host__ __device__ __forceinline__ uint32_t case_edge_mask(unsigned c) {
+  uint32_t m = 0;
+#pragma unroll
+  for (int e = 0; e < 12; e++) m |= (((c >> edge_v0(e)) ^ (c >> edge_v1(e))) & 1u) << e;
+  return m;
+}
+
+// ------------------------------------------------------------------------------------------
+// contours of the MC polygon, packed in 64 bits:
+//   nibbles 0..11  the edges of all contours in order (contour t starts after contours 0..t-1)
+//   nibbles 12..15 the size of contour 0..3 (0 = no contour)
+// ------------------------------------------------------------------------------------------
+__host__ __device__ __forceinline__ int cnt_size(uint64_t c, int t) { return nib(c, 12 + t); }
+__host__ __device__ __forceinline__ int cnt_count(uint64_t c) {
+  return (cnt_size(c, 0) > 0) + (cnt_size(c, 1) > 0) + (cnt_size(c, 2) > 0) + (cnt_size(c, 3) > 0);
+}
+__host__ __device__ __forceinline__ int cnt_start(uint64_t c, int t) {
+  int s = 0;
+  for (int q = 0; q < t; q++) s += cnt_size(c, q);
+  return s;
+}
+__host__ __device__ __forceinline__ int cnt_edge(uint64_t c, int flat) { return nib(c, flat); }
+
+__host__ __device__ __forceinline__ int ctz32(uint32_t x) {
+#ifdef __CUDA_ARCH__
+  return __ffs((int)x) - 1;
+#else
+  return __builtin_ctz(x);
+#endif
+}
+
+// Connect oriented segments into closed contours, each starting at its lowest edge -- the
+// connect loop of mc_polygon (cpp_dmc/DualMarchingCubes.cpp:443-463) and p_slice
+// (mc/MarchingCubes.cpp:690-709).  `to` holds the next edge of every crossed edge (nibble e),
+// `emask` the crossed edges.
+__host__ __device__ __forceinline__ uint64_t connect_contours(uint64_t to, uint32_t emask) {
+  uint64_t out = 0;
+  int flat = 0, t = 0;
+  uint32_t rem = emask;
+  while (rem && t < 4) {
+    const int start = ctz32(rem);
+    int e = start, sz = 0;
+    do {
+      out |= (uint64_t)e << (4 * flat);
+      flat++;
+      sz++;
+      rem &= ~(1u << e);
+      e = nib(to, e);
+    } while (e != start && sz < 12);
+    out |= (uint64_t)sz << (4 * (12 + t));
+    t++;
+  }
+  return out;
+}
+
+// Oriented segments of one face: fc = face case (bit b: face vertex b >= iso), sep = the decider
+// branch for the two ambiguous face cases (6, 9).  Follows the face-case switch of
+// cpp_dmc/DualMarchingCubes.cpp:357-425 / mc/MarchingCubes.cpp:495-668.
+__host__ __device__ __forceinline__ void face_segments(int fc, int sep, uint32_t fe, uint64_t& to) {
+  auto set = [&](int a, int b) {
+    const int ea = nib(fe, a), eb = nib(fe, b);
+    to = (to & ~(0xFull << (4 * ea))) | ((uint64_t)eb << (4 * ea));
+  };
+  if (fc == 6) {
+    if (sep) { set(3, 0); set(1, 2); }
+    else { set(1, 0); set(3, 2); }
+  } else if (fc == 9) {
+    if (sep) { set(0, 1); set(2, 3); }
+    else { set(0, 3); set(2, 1); }
+  } else if (fc != 0 && fc != 15) {
+    set(nib(TMC_PK_FACE_RULE_A, fc), nib(TMC_PK_FACE_RULE_B, fc));
+  }
+}
+
+__host__ __device__ __forceinline__ int face_case(unsigned cs, uint32_t fv) {
+  return (int)(((cs >> nib(fv, 0)) & 1) | ((cs >> nib(fv, 1)) & 1) << 1 | ((cs >> nib(fv, 2)) & 1) << 2 |
+               ((cs >> nib(fv, 3)) & 1) << 3);
+}
+
+// asymptotic decider, float64 (cpp_dmc/DualMarchingCubes.h:330)
+__host__ __device__ __forceinline__ double decider(double f0, double f1, double f2, double f3) {
+  return (f0 * f3 - f1 * f2) / (f0 + f3 - f1 - f2);
+}
+
+// Contour of an unambiguous case from the packed table (size nibble, then edges).
+__host__ __device__ __forceinline__ uint64_t table_contour(uint64_t w) {
+  const int sz = (int)(w & 0xF);
+  return (w >> 4) | ((uint64_t)sz << 48);
+}
+
+// DMC MC polygon (mc_polygon, cpp_dmc/DualMarchingCubes.cpp:328-487): table contour for the
+// unambiguous cases, face rules with the float64 decider (>= iso) for the ambiguous ones.
+__device__ __forceinline__ uint64_t dmc_polygon(unsigned cs, const float u[8], double iso, const uint64_t* case_contour) {
+  if (!case_ambiguous(cs)) return table_contour(case_contour[cs]);
+  uint64_t to = ~0ull;
+#pragma unroll
+  for (int f = 0; f < 6; f++) {
+    const uint32_t fv = face_v_pack(f);
+    const int fc = face_case(cs, fv);
+    int sep = 0;
+    if (fc == 6 || fc == 9) {
+      const double val = decider(u[nib(fv, 0)], u[nib(fv, 1)], u[nib(fv, 2)], u[nib(fv, 3)]);
+      sep = val >= iso;
+    }
+    face_segments(fc, sep, face_e_pack(f), to);
+  }
+  return connect_contours(to, case_edge_mask(cs));
+}
+
+// ------------------------------------------------------------------------------------------
+// misc
+// ------------------------------------------------------------------------------------------
+struct DevFlags {
+  unsigned int overflow;   // a capacity check failed
+  unsigned int numeric;    // NaN / Inf seen
+  unsigned int timeout;    // a bounded wait gave up
+  unsigned int pad;
+  unsigned long long counters[8];
+};
+
+__host__ __device__ __forceinline__ int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace tmc

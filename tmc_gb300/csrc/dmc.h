@@ -1,0 +1,33 @@
+// Internal interface between the runtime (C ABI) and the DMC kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace tmc {
+
+struct DmcVertexOut {
+  float* v;        // 3 per vertex
+  float* n;        // 3 per vertex
+  double* v64;     // optional
+  int64_t* vcell;  // optional (with vuvw)
+  float* vuvw;
+};
+
+struct DmcScratch {
+  uint32_t* rec;                  // per cell
+  int32_t* voff;                  // per cell
+  int32_t* qoff;                  // per cell
+  unsigned long long* tile_sums;  // per scan tile
+  unsigned long long* totals;     // [0] = (vertices << 32) | quads
+  unsigned long long* stats;      // 8 counters
+};
+
+// Each launcher returns the number of kernels it launched.
+int64_t dmc_tiles(const Grid& g);  // scan tiles for the cell count of g
+int dmc_front_count(const Grid& g, DmcScratch& s, cudaStream_t st);
+int dmc_front_emit(const Grid& g, DmcScratch& s, DmcVertexOut vo, int32_t* quads, uint8_t* colors, int flip,
+                   int sms, cudaStream_t st);
+
+}  // namespace tmc

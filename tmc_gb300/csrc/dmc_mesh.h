@@ -1,0 +1,38 @@
+// Internal interface: DMC mesh post-processing (halfedges, valence, face colouring, P3X3Y/P3333
+// simplification, quad -> triangle split).
+#pragma once
+#include <cstdint>
+#include <vector>
+#include <cuda_runtime.h>
+
+namespace tmc {
+
+struct DmcMesh {
+  int64_t nv = 0, nq = 0;
+  float* v = nullptr;
+  float* n = nullptr;
+  double* v64 = nullptr;
+  int32_t* quads = nullptr;
+  uint8_t* colors = nullptr;
+};
+
+struct DmcPostOut {
+  DmcMesh mesh;                 // final vertices and quads
+  int64_t nt = 0, nhe = 0;
+  int32_t* tris = nullptr;
+  int32_t* he = nullptr;        // 4 per halfedge
+  int32_t* he_v = nullptr;
+  int32_t* he_f = nullptr;
+  int64_t non_manifold = 0;
+  std::vector<void*> owned;     // new device buffers now owned by the result
+  std::vector<void*> freed;     // input buffers released by the post-processing
+};
+
+struct DmcPostStatus {
+  cudaError_t err = cudaSuccess;
+  int launches = 0;
+};
+
+DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaStream_t st, DmcPostOut* out);
+
+}  // namespace tmc

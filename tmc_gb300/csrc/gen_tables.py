@@ -119,12 +119,15 @@ def main():
     L.append("#include <stdint.h>")
     L.append("")
     L.append("// Edges crossed by the isosurface, per case (bit e = edge e).")
-    L.append("static const uint16_t TMC_EDGE_MASK[256] = {")
+    L.append("#define TMC_EDGE_MASK_INIT { \\")
     for r in range(0, 256, 16):
-        L.append("  " + ", ".join(str(x) for x in e_pat[r:r + 16]) + ",")
-    L.append("};")
+        L.append("  " + ", ".join(str(x) for x in e_pat[r:r + 16]) + ", \\")
+    L.append("}")
+    L.append("static const uint16_t TMC_EDGE_MASK[256] = TMC_EDGE_MASK_INIT;")
     L.append("// Ambiguous cases (bit c of word c/64).")
-    L.append("static const uint64_t TMC_AMBIGUOUS[4] = {" + ", ".join(f"0x{w:016x}ull" for w in amb_words) + "};")
+    for i, w in enumerate(amb_words):
+        L.append(f"#define TMC_AMBIGUOUS_W{i} 0x{w:016x}ull")
+    L.append("static const uint64_t TMC_AMBIGUOUS[4] = {TMC_AMBIGUOUS_W0, TMC_AMBIGUOUS_W1, TMC_AMBIGUOUS_W2, TMC_AMBIGUOUS_W3};")
     L.append("// Start edge of the single contour of each unambiguous case, two cases per byte")
     L.append("// (low nibble = even case); 15 = no contour / ambiguous case.")
     packed = [start[2 * i] | (start[2 * i + 1] << 4) for i in range(128)]
@@ -133,10 +136,48 @@ def main():
         L.append("  " + ", ".join(str(x) for x in packed[r:r + 16]) + ",")
     L.append("};")
     L.append("// Triangles of each unambiguous case: bits 0-3 count, then 4-bit edge ids (3 per triangle).")
-    L.append("static const uint64_t TMC_TRIANGLES[256] = {")
+    L.append("#define TMC_TRIANGLES_INIT { \\")
     for r in range(0, 256, 4):
-        L.append("  " + ", ".join(f"0x{w:016x}ull" for w in tris[r:r + 4]) + ",")
-    L.append("};")
+        L.append("  " + ", ".join(f"0x{w:016x}ull" for w in tris[r:r + 4]) + ", \\")
+    L.append("}")
+    L.append("static const uint64_t TMC_TRIANGLES[256] = TMC_TRIANGLES_INIT;")
+    # ---- packed topology (4 bits per entry) and the per-case contour of unambiguous cases ----
+    def pack(vals):
+        w = 0
+        for i, x in enumerate(vals):
+            assert 0 <= x < 16
+            w |= x << (4 * i)
+        return w
+    EDGE_GLOBAL = [(0, 0, 0, 0), (1, 0, 0, 1), (0, 1, 0, 0), (0, 0, 0, 1), (0, 0, 1, 0), (1, 0, 1, 1),
+                   (0, 1, 1, 0), (0, 0, 1, 1), (0, 0, 0, 2), (1, 0, 0, 2), (1, 1, 0, 2), (0, 1, 0, 2)]
+    QUAD_SLOT = [(0, 0), (0, 0), (3, 1), (3, 1), (1, 3), (1, 3), (2, 2), (2, 2), (0, 0), (3, 1), (2, 2), (1, 3)]
+    L.append("")
+    L.append("// Packed cell topology, 4 bits per entry (entry i at bits 4i..4i+3).")
+    L.append(f"#define TMC_PK_EDGE_V0 0x{pack([a for a, b in EDGE_V]):012x}ull   // first end vertex of edge e")
+    L.append(f"#define TMC_PK_EDGE_V1 0x{pack([b for a, b in EDGE_V]):012x}ull   // second end vertex of edge e")
+    L.append(f"#define TMC_PK_EDGE_OFF 0x{pack([g[0] | g[1] << 1 | g[2] << 2 for g in EDGE_GLOBAL]):012x}ull  // lower grid point offset (di|dj<<1|dk<<2)")
+    L.append(f"#define TMC_PK_EDGE_AXIS 0x{pack([g[3] for g in EDGE_GLOBAL]):012x}ull // axis of edge e")
+    L.append(f"#define TMC_PK_QUAD_SLOT0 0x{pack([q[0] for q in QUAD_SLOT]):012x}ull // quad slot, first end vertex >= iso")
+    L.append(f"#define TMC_PK_QUAD_SLOT1 0x{pack([q[1] for q in QUAD_SLOT]):012x}ull // quad slot, first end vertex < iso")
+    for f in range(6):
+        L.append(f"#define TMC_PK_FACE_V{f} 0x{pack(FACE_V[f]):04x}u")
+        L.append(f"#define TMC_PK_FACE_E{f} 0x{pack(FACE_E[f]):04x}u")
+    L.append("// The contour of each unambiguous case, rotated to the start edge above: bits 0-3 size,")
+    L.append("// then the edges, one nibble each.  0 for ambiguous and empty cases.")
+    L.append("#define TMC_CASE_CONTOUR_INIT { \\")
+    words = []
+    for c in range(256):
+        if amb[c] or start[c] == 15:
+            words.append(0)
+            continue
+        cnt = contours(c)[0]
+        r = cnt.index(start[c])
+        cnt = cnt[r:] + cnt[:r]
+        words.append(pack([len(cnt)] + cnt))
+    for r in range(0, 256, 4):
+        L.append("  " + ", ".join(f"0x{w:016x}ull" for w in words[r:r + 4]) + ", \\")
+    L.append("}")
+    L.append("static const uint64_t TMC_CASE_CONTOUR[256] = TMC_CASE_CONTOUR_INIT;")
     with open(os.path.join(HERE, "mc_tables.h"), "w") as f:
         f.write("\n".join(L) + "\n")
 

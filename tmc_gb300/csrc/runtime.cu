@@ -1,0 +1,383 @@
+// Host runtime behind the C ABI (include/tmc_gb300.h): contexts, stream-ordered pooled device
+// memory, argument checking, and the extraction drivers that sequence the kernels.
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/tmc_gb300.h"
+#include "common.cuh"
+#include "dmc.h"
+#include "dmc_mesh.h"
+#include "tmc_cells.h"
+
+struct tmc_ctx {
+  int device = 0;
+  int sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaMemPool_t pool = nullptr;
+  tmc_ctx_opts opts{};
+  std::string err;
+  std::atomic<int64_t> launches{0};
+  unsigned long long* d_stats = nullptr;  // 8 counters, reused per call
+  void* h_pinned = nullptr;               // small pinned staging area (totals, stats)
+};
+
+namespace {
+
+struct MeshPriv {
+  std::vector<void*> dev;
+  std::vector<void*> host;
+};
+
+tmc_status fail(tmc_ctx* ctx, tmc_status s, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->err = buf;
+  return s;
+}
+
+#define TMC_CUDA(ctx, call)                                                                     \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) {                                                                    \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? TMC_ERR_OOM : TMC_ERR_CUDA, "%s: %s (%s:%d)", \
+                  #call, cudaGetErrorString(e_), __FILE__, __LINE__);                           \
+    }                                                                                           \
+  } while (0)
+
+// Stream-ordered allocation from the device's pool; tracked for release.
+struct Allocs {
+  tmc_ctx* ctx;
+  std::vector<void*> ptrs;
+  explicit Allocs(tmc_ctx* c) : ctx(c) {}
+  ~Allocs() {
+    for (void* p : ptrs) cudaFreeAsync(p, ctx->stream);
+  }
+  template <typename T>
+  cudaError_t get(T** out, size_t count) {
+    void* p = nullptr;
+    cudaError_t e = cudaMallocAsync(&p, count ? count * sizeof(T) : 16, ctx->stream);
+    if (e == cudaSuccess) ptrs.push_back(p);
+    *out = (T*)p;
+    return e;
+  }
+  // hand ownership of p to the caller
+  void release(void* p) {
+    for (auto& q : ptrs)
+      if (q == p) q = nullptr;
+    std::vector<void*> keep;
+    for (void* q : ptrs)
+      if (q) keep.push_back(q);
+    ptrs.swap(keep);
+  }
+};
+
+float iso_up(double iso) {
+  float f = (float)iso;
+  if ((double)f < iso) f = std::nextafter(f, INFINITY);
+  return f;
+}
+
+tmc_status check_volume(tmc_ctx* ctx, const tmc_volume* vol) {
+  if (!vol) return fail(ctx, TMC_ERR_INVALID_ARG, "volume is NULL");
+  if (!vol->data) return fail(ctx, TMC_ERR_INVALID_ARG, "volume data is NULL");
+  if (vol->nx < 2 || vol->ny < 2 || vol->nz < 2)
+    return fail(ctx, TMC_ERR_INVALID_ARG, "grid %dx%dx%d: every axis needs at least 2 points", vol->nx, vol->ny,
+                vol->nz);
+  if (vol->nx > 65535 || vol->ny > 65535 || vol->nz > 65535)
+    return fail(ctx, TMC_ERR_INVALID_ARG, "grid axis above 65535 points");
+  for (int d = 0; d < 3; d++)
+    if (!(vol->spacing[d] > 0) || !std::isfinite(vol->spacing[d]) || !std::isfinite(vol->origin[d]))
+      return fail(ctx, TMC_ERR_INVALID_ARG, "spacing must be positive and finite");
+  const int64_t cells = (int64_t)(vol->nx - 1) * (vol->ny - 1) * (vol->nz - 1);
+  if (cells > (int64_t)1 << 32) return fail(ctx, TMC_ERR_INVALID_ARG, "more than 2^32 cells");
+  return TMC_OK;
+}
+
+// Bring the field to the device (copy from host memory when needed).
+tmc_status field_on_device(tmc_ctx* ctx, const tmc_volume* vol, Allocs& al, const float** out) {
+  const size_t n = (size_t)vol->nx * vol->ny * vol->nz;
+  if (vol->on_device) {
+    *out = vol->data;
+    return TMC_OK;
+  }
+  float* d = nullptr;
+  TMC_CUDA(ctx, al.get(&d, n));
+  TMC_CUDA(ctx, cudaMemcpyAsync(d, vol->data, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  *out = d;
+  return TMC_OK;
+}
+
+tmc::Grid make_grid(const tmc_volume* vol, const float* dev, double iso) {
+  tmc::Grid g{};
+  g.f = dev;
+  g.nx = vol->nx;
+  g.ny = vol->ny;
+  g.nz = vol->nz;
+  g.ox = vol->origin[0];
+  g.oy = vol->origin[1];
+  g.oz = vol->origin[2];
+  g.dx = vol->spacing[0];
+  g.dy = vol->spacing[1];
+  g.dz = vol->spacing[2];
+  g.iso = iso;
+  g.iso_up = iso_up(iso);
+  return g;
+}
+
+void mesh_reset(tmc_mesh* m) { std::memset(m, 0, sizeof(*m)); }
+
+// Move device arrays of a finished mesh to host memory when TMC_OUT_HOST is set.
+template <typename T>
+tmc_status to_host(tmc_ctx* ctx, T** p, size_t count, MeshPriv* mp) {
+  if (!*p) return TMC_OK;
+  T* h = (T*)std::malloc(count ? count * sizeof(T) : 16);
+  if (!h) return fail(ctx, TMC_ERR_OOM, "host allocation of %zu bytes failed", count * sizeof(T));
+  if (count) TMC_CUDA(ctx, cudaMemcpyAsync(h, *p, count * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+  mp->host.push_back(h);
+  *p = h;
+  return TMC_OK;
+}
+
+tmc_status finish_mesh(tmc_ctx* ctx, uint32_t flags, tmc_mesh* out, MeshPriv* mp) {
+  tmc_status s = TMC_OK;
+  if (flags & TMC_OUT_HOST) {
+    const size_t nv = (size_t)out->nr_v, nq = (size_t)out->nr_q, nt = (size_t)out->nr_t, nh = (size_t)out->nr_he;
+    if ((s = to_host(ctx, &out->v, 3 * nv, mp))) return s;
+    if ((s = to_host(ctx, &out->n, 3 * nv, mp))) return s;
+    if ((s = to_host(ctx, &out->v64, 3 * nv, mp))) return s;
+    if ((s = to_host(ctx, &out->quads, 4 * nq, mp))) return s;
+    if ((s = to_host(ctx, &out->tris, 3 * nt, mp))) return s;
+    if ((s = to_host(ctx, &out->he, 4 * nh, mp))) return s;
+    if ((s = to_host(ctx, &out->he_v, nv, mp))) return s;
+    if ((s = to_host(ctx, &out->he_f, out->nr_q ? nq : nt, mp))) return s;
+    if ((s = to_host(ctx, &out->vcell, nv, mp))) return s;
+    if ((s = to_host(ctx, &out->vuvw, 3 * nv, mp))) return s;
+    TMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (void* p : mp->dev) cudaFreeAsync(p, ctx->stream);
+    mp->dev.clear();
+    out->on_device = 0;
+  } else {
+    out->on_device = 1;
+  }
+  out->priv = mp;
+  return TMC_OK;
+}
+
+}  // namespace
+
+// ============================================================================================
+// C ABI
+// ============================================================================================
+extern "C" {
+
+tmc_status tmc_ctx_create(int device, const tmc_ctx_opts* opts, tmc_ctx** out) {
+  if (!out) return TMC_ERR_INVALID_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return TMC_ERR_CUDA;
+  if (device < 0 || device >= ndev) return TMC_ERR_INVALID_ARG;
+  tmc_ctx* ctx = new (std::nothrow) tmc_ctx();
+  if (!ctx) return TMC_ERR_OOM;
+  ctx->device = device;
+  if (opts) ctx->opts = *opts;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    delete ctx;
+    return TMC_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return TMC_ERR_CUDA;
+  }
+  // keep freed blocks pooled on the device between calls
+  if (cudaDeviceGetDefaultMemPool(&ctx->pool, device) == cudaSuccess) {
+    uint64_t thr = ctx->opts.reserve_bytes ? (uint64_t)ctx->opts.reserve_bytes : UINT64_MAX;
+    cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  if (cudaMalloc(&ctx->d_stats, 8 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMallocHost(&ctx->h_pinned, 4096) != cudaSuccess) {
+    tmc_ctx_destroy(ctx);
+    return TMC_ERR_OOM;
+  }
+  *out = ctx;
+  return TMC_OK;
+}
+
+tmc_status tmc_ctx_destroy(tmc_ctx* ctx) {
+  if (!ctx) return TMC_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->d_stats) cudaFree(ctx->d_stats);
+  if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return TMC_OK;
+}
+
+const char* tmc_last_error(const tmc_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+void* tmc_ctx_stream(tmc_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+int64_t tmc_ctx_launch_count(const tmc_ctx* ctx) { return ctx ? ctx->launches.load() : 0; }
+
+tmc_status tmc_ctx_synchronize(tmc_ctx* ctx) {
+  if (!ctx) return TMC_ERR_INVALID_ARG;
+  TMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return TMC_OK;
+}
+
+tmc_status tmc_mesh_free(tmc_ctx* ctx, tmc_mesh* mesh) {
+  if (!ctx || !mesh) return TMC_ERR_INVALID_ARG;
+  MeshPriv* mp = (MeshPriv*)mesh->priv;
+  if (mp) {
+    cudaSetDevice(ctx->device);
+    for (void* p : mp->dev) cudaFreeAsync(p, ctx->stream);
+    for (void* p : mp->host) std::free(p);
+    delete mp;
+  }
+  mesh_reset(mesh);
+  return TMC_OK;
+}
+
+tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t flags, tmc_mesh* out) {
+  if (!ctx || !out) return fail(ctx, TMC_ERR_INVALID_ARG, "context or output is NULL");
+  mesh_reset(out);
+  tmc_status s = check_volume(ctx, vol);
+  if (s) return s;
+  if (!std::isfinite(iso)) return fail(ctx, TMC_ERR_INVALID_ARG, "isovalue must be finite");
+  if (flags & TMC_DMC_SIMPLIFY) flags |= TMC_DMC_P3X3Y_COLOR | TMC_DMC_P3X3Y_ISOLATED | TMC_DMC_P3333;
+  const bool simplify = flags & (TMC_DMC_P3X3Y_COLOR | TMC_DMC_P3X3Y_ISOLATED | TMC_DMC_P3333);
+  if ((flags & TMC_OUT_LOCAL) && simplify)
+    return fail(ctx, TMC_ERR_INVALID_ARG, "local coordinates exist only without simplification");
+  TMC_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  Allocs al(ctx);
+  const float* field = nullptr;
+  if ((s = field_on_device(ctx, vol, al, &field))) return s;
+  const tmc::Grid g = make_grid(vol, field, iso);
+  const int64_t ncell = g.ncells();
+
+  tmc::DmcScratch sc{};
+  TMC_CUDA(ctx, al.get(&sc.rec, ncell));
+  TMC_CUDA(ctx, al.get(&sc.voff, ncell));
+  TMC_CUDA(ctx, al.get(&sc.qoff, ncell));
+  TMC_CUDA(ctx, al.get(&sc.tile_sums, tmc::dmc_tiles(g)));
+  TMC_CUDA(ctx, al.get(&sc.totals, 2));
+  sc.stats = ctx->d_stats;
+  TMC_CUDA(ctx, cudaMemsetAsync(sc.stats, 0, 8 * sizeof(unsigned long long), st));
+  ctx->launches += tmc::dmc_front_count(g, sc, st);
+  unsigned long long* h = (unsigned long long*)ctx->h_pinned;
+  TMC_CUDA(ctx, cudaMemcpyAsync(h, sc.totals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  TMC_CUDA(ctx, cudaStreamSynchronize(st));
+  const int64_t nv = (int64_t)(h[0] >> 32), nq = (int64_t)(h[0] & 0xffffffffull);
+
+  MeshPriv* mp = new (std::nothrow) MeshPriv();
+  if (!mp) return fail(ctx, TMC_ERR_OOM, "host allocation failed");
+  auto own = [&](void* p) {
+    al.release(p);
+    mp->dev.push_back(p);
+  };
+  tmc::DmcVertexOut vo{};
+  int32_t* quads = nullptr;
+  uint8_t* colors = nullptr;
+  cudaError_t ce = cudaSuccess;
+#define TMC_GET(ptr, count)                 \
+  do {                                      \
+    ce = al.get(&(ptr), (count));           \
+    if (ce != cudaSuccess) {                \
+      delete mp;                            \
+      TMC_CUDA(ctx, ce);                    \
+    }                                       \
+    own(ptr);                               \
+  } while (0)
+  TMC_GET(vo.v, 3 * nv);
+  TMC_GET(vo.n, 3 * nv);
+  if (flags & TMC_OUT_POS_F64) TMC_GET(vo.v64, 3 * nv);
+  if (flags & TMC_OUT_LOCAL) {
+    TMC_GET(vo.vcell, nv);
+    TMC_GET(vo.vuvw, 3 * nv);
+  }
+  TMC_GET(quads, 4 * nq);
+  ce = al.get(&colors, nq);
+  if (ce != cudaSuccess) {
+    delete mp;
+    TMC_CUDA(ctx, ce);
+  }
+  ctx->launches += tmc::dmc_front_emit(g, sc, vo, quads, colors, (flags & TMC_GRAD_FLIP) ? 1 : 0, ctx->sms, st);
+  TMC_CUDA(ctx, cudaGetLastError());
+
+  tmc::DmcMesh mesh{};
+  mesh.nv = nv;
+  mesh.nq = nq;
+  mesh.v = vo.v;
+  mesh.n = vo.n;
+  mesh.v64 = vo.v64;
+  mesh.quads = quads;
+  mesh.colors = colors;
+  tmc::DmcPostOut post{};
+  tmc::DmcPostStatus ps = tmc::dmc_postprocess(mesh, flags, ctx->sms, st, &post);
+  if (ps.err != cudaSuccess) {
+    delete mp;
+    TMC_CUDA(ctx, ps.err);
+  }
+  ctx->launches += ps.launches;
+  for (void* p : post.owned) mp->dev.push_back(p);
+  for (void* p : post.freed) {
+    al.release(p);
+    for (auto& q : mp->dev)
+      if (q == p) q = nullptr;
+  }
+  {
+    std::vector<void*> keep;
+    for (void* q : mp->dev)
+      if (q) keep.push_back(q);
+    mp->dev.swap(keep);
+  }
+  out->nr_v = post.mesh.nv;
+  out->nr_q = post.mesh.nq;
+  out->v = post.mesh.v;
+  out->n = post.mesh.n;
+  out->v64 = post.mesh.v64;
+  out->quads = post.mesh.quads;
+  out->nr_t = post.nt;
+  out->tris = post.tris;
+  out->nr_he = post.nhe;
+  out->he = post.he;
+  out->he_v = post.he_v;
+  out->he_f = post.he_f;
+  out->vcell = vo.vcell;
+  out->vuvw = vo.vuvw;
+  TMC_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  TMC_CUDA(ctx, cudaStreamSynchronize(st));
+  for (int q = 0; q < 8; q++) out->stats[q] = (int64_t)h[q];
+  out->stats[4] = post.non_manifold;
+  out->stats[6] = ncell;
+#undef TMC_GET
+  return finish_mesh(ctx, flags, out, mp);
+}
+
+}  // extern "C"
+
+extern "C" {
+// Entry points whose drivers live in other translation units are defined there; these two are
+// placeholders until the TMC and batched drivers land.
+tmc_status tmc_tmc_sharedvertex(tmc_ctx* ctx, const tmc_volume*, double, uint32_t, tmc_mesh* out) {
+  if (out) mesh_reset(out);
+  return fail(ctx, TMC_ERR_INTERNAL, "TMC extraction is not built yet");
+}
+tmc_status tmc_tmc_halfedge(tmc_ctx* ctx, const tmc_volume*, double, uint32_t, tmc_mesh* out) {
+  if (out) mesh_reset(out);
+  return fail(ctx, TMC_ERR_INTERNAL, "TMC extraction is not built yet");
+}
+tmc_status tmc_batch_extract(tmc_ctx* ctx, int32_t, const tmc_request*, tmc_mesh*) {
+  return fail(ctx, TMC_ERR_INTERNAL, "batched extraction is not built yet");
+}
+}

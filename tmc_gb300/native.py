@@ -1,0 +1,198 @@
+"""ctypes binding of the C ABI in include/tmc_gb300.h (libtmc_gb300.so, built in-tree).
+
+The library is the product path: there is no CPU fallback.  Loading fails loudly when the
+extension has not been built (run tmc_gb300.build.build()) or no CUDA device is present.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libtmc_gb300.so")
+
+TMC_OK = 0
+STATUS = {0: "TMC_OK", 1: "TMC_ERR_INVALID_ARG", 2: "TMC_ERR_OOM", 3: "TMC_ERR_CAPACITY", 4: "TMC_ERR_CUDA",
+          5: "TMC_ERR_TIMEOUT", 6: "TMC_ERR_NUMERIC", 7: "TMC_ERR_INTERNAL"}
+
+DMC_SIMPLIFY = 1 << 0
+DMC_P3X3Y_COLOR = 1 << 1
+DMC_P3X3Y_ISOLATED = 1 << 2
+DMC_P3333 = 1 << 3
+OUT_TRIANGLES = 1 << 4
+OUT_HALFEDGES = 1 << 5
+OUT_HOST = 1 << 6
+OUT_POS_F64 = 1 << 7
+OUT_LOCAL = 1 << 8
+GRAD_FLIP = 1 << 9
+TMC_KEY32 = 1 << 10
+ALGO_DMC = 0
+ALGO_TMC = 1
+
+# every symbol include/tmc_gb300.h declares
+EXPORTS = ["tmc_ctx_create", "tmc_ctx_destroy", "tmc_last_error", "tmc_ctx_stream", "tmc_ctx_synchronize",
+           "tmc_ctx_launch_count", "tmc_dmc_extract", "tmc_tmc_sharedvertex", "tmc_tmc_halfedge",
+           "tmc_mesh_free", "tmc_batch_extract"]
+
+
+class TmcError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class CtxOpts(ctypes.Structure):
+    _fields_ = [("reserve_bytes", ctypes.c_size_t), ("check_numeric", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class Volume(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+                ("origin", ctypes.c_double * 3), ("spacing", ctypes.c_double * 3),
+                ("data", ctypes.c_void_p), ("on_device", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class Mesh(ctypes.Structure):
+    _fields_ = [("nr_v", ctypes.c_int64), ("nr_q", ctypes.c_int64), ("nr_t", ctypes.c_int64), ("nr_he", ctypes.c_int64),
+                ("on_device", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("v", ctypes.c_void_p), ("n", ctypes.c_void_p), ("v64", ctypes.c_void_p),
+                ("quads", ctypes.c_void_p), ("tris", ctypes.c_void_p), ("he", ctypes.c_void_p),
+                ("he_v", ctypes.c_void_p), ("he_f", ctypes.c_void_p), ("vcell", ctypes.c_void_p),
+                ("vuvw", ctypes.c_void_p), ("stats", ctypes.c_int64 * 8), ("priv", ctypes.c_void_p)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("vol", Volume), ("iso", ctypes.c_double), ("algo", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with tmc_gb300.build.build() (no CPU fallback exists)")
+    lib = ctypes.CDLL(path)
+    lib.tmc_ctx_create.argtypes = [ctypes.c_int, ctypes.POINTER(CtxOpts), ctypes.POINTER(ctypes.c_void_p)]
+    lib.tmc_ctx_destroy.argtypes = [ctypes.c_void_p]
+    lib.tmc_last_error.argtypes = [ctypes.c_void_p]
+    lib.tmc_last_error.restype = ctypes.c_char_p
+    lib.tmc_ctx_stream.argtypes = [ctypes.c_void_p]
+    lib.tmc_ctx_stream.restype = ctypes.c_void_p
+    lib.tmc_ctx_synchronize.argtypes = [ctypes.c_void_p]
+    lib.tmc_ctx_launch_count.argtypes = [ctypes.c_void_p]
+    lib.tmc_ctx_launch_count.restype = ctypes.c_int64
+    for name in ("tmc_dmc_extract", "tmc_tmc_sharedvertex", "tmc_tmc_halfedge"):
+        if hasattr(lib, name):
+            f = getattr(lib, name)
+            f.argtypes = [ctypes.c_void_p, ctypes.POINTER(Volume), ctypes.c_double, ctypes.c_uint32, ctypes.POINTER(Mesh)]
+    lib.tmc_mesh_free.argtypes = [ctypes.c_void_p, ctypes.POINTER(Mesh)]
+    if hasattr(lib, "tmc_batch_extract"):
+        lib.tmc_batch_extract.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(Request), ctypes.POINTER(Mesh)]
+    _lib = lib
+    return lib
+
+
+def make_volume(vol, data_ptr: int | None = None, on_device: bool = False) -> Volume:
+    """A tmc_volume for a tmc_gb300.volumes.Volume (host numpy data) or a device pointer."""
+    nx, ny, nz = vol.dims
+    v = Volume()
+    v.nx, v.ny, v.nz = nx, ny, nz
+    v.origin = (ctypes.c_double * 3)(*vol.origin)
+    v.spacing = (ctypes.c_double * 3)(*vol.spacing)
+    if data_ptr is None:
+        arr = np.ascontiguousarray(vol.data, dtype=np.float32)
+        vol._keep = arr  # keep alive
+        v.data = arr.ctypes.data
+        v.on_device = 0
+    else:
+        v.data = data_ptr
+        v.on_device = 1 if on_device else 0
+    return v
+
+
+def _host_array(ptr, count, dtype):
+    if not ptr or count == 0:
+        return np.zeros(0, dtype=dtype)
+    ct = np.ctypeslib.as_ctypes_type(np.dtype(dtype))
+    buf = (ct * count).from_address(ptr)
+    return np.ctypeslib.as_array(buf).copy()
+
+
+class Context:
+    """One CUDA stream, pooled device memory; mirrors a reference extraction object."""
+
+    def __init__(self, device: int = 0, reserve_bytes: int = 0, check_numeric: bool = False):
+        self.lib = load()
+        self.h = ctypes.c_void_p()
+        opts = CtxOpts(reserve_bytes, 1 if check_numeric else 0, 0)
+        st = self.lib.tmc_ctx_create(device, ctypes.byref(opts), ctypes.byref(self.h))
+        if st != TMC_OK:
+            raise TmcError(st, "tmc_ctx_create failed (is a CUDA device visible?)")
+
+    def close(self):
+        if self.h:
+            self.lib.tmc_ctx_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return self.lib.tmc_ctx_stream(self.h)
+
+    def launches(self) -> int:
+        return self.lib.tmc_ctx_launch_count(self.h)
+
+    def synchronize(self):
+        self._check(self.lib.tmc_ctx_synchronize(self.h))
+
+    def _check(self, st):
+        if st != TMC_OK:
+            raise TmcError(st, self.lib.tmc_last_error(self.h).decode())
+
+    def _run(self, fn, volume: Volume, iso: float, flags: int) -> Mesh:
+        m = Mesh()
+        self._check(getattr(self.lib, fn)(self.h, ctypes.byref(volume), float(iso), int(flags), ctypes.byref(m)))
+        return m
+
+    def free(self, m: Mesh):
+        self._check(self.lib.tmc_mesh_free(self.h, ctypes.byref(m)))
+
+    # -- raw calls (mesh stays where flags put it; caller frees) -----------------------------
+    def dmc_raw(self, volume: Volume, iso: float, flags: int) -> Mesh:
+        return self._run("tmc_dmc_extract", volume, iso, flags)
+
+    def tmc_raw(self, volume: Volume, iso: float, flags: int, halfedge: bool = False) -> Mesh:
+        return self._run("tmc_tmc_halfedge" if halfedge else "tmc_tmc_sharedvertex", volume, iso, flags)
+
+    # -- numpy results --------------------------------------------------------------------
+    def fetch(self, m: Mesh) -> dict:
+        """Copy a host-resident mesh (OUT_HOST) into numpy arrays and free it."""
+        assert not m.on_device, "fetch() needs a mesh extracted with OUT_HOST"
+        nv, nq, nt, nh = m.nr_v, m.nr_q, m.nr_t, m.nr_he
+        out = dict(v=_host_array(m.v, 3 * nv, np.float32), n=_host_array(m.n, 3 * nv, np.float32),
+                   v64=_host_array(m.v64, 3 * nv, np.float64), q=_host_array(m.quads, 4 * nq, np.int32),
+                   t=_host_array(m.tris, 3 * nt, np.int32), he=_host_array(m.he, 4 * nh, np.int32),
+                   hv=_host_array(m.he_v, nv if m.he_v else 0, np.int32),
+                   hf=_host_array(m.he_f, (nq if nq else nt) if m.he_f else 0, np.int32),
+                   vcell=_host_array(m.vcell, nv if m.vcell else 0, np.int64),
+                   vuvw=_host_array(m.vuvw, 3 * nv if m.vuvw else 0, np.float32),
+                   stats=np.array(list(m.stats)))
+        self.free(m)
+        return out
+
+    def dmc(self, vol, flags: int = 0, iso: float | None = None) -> dict:
+        m = self.dmc_raw(make_volume(vol), vol.iso if iso is None else iso, flags | OUT_HOST)
+        return self.fetch(m)
+
+    def tmc(self, vol, flags: int = 0, halfedge: bool = False, iso: float | None = None) -> dict:
+        m = self.tmc_raw(make_volume(vol), vol.iso if iso is None else iso, flags | OUT_HOST, halfedge)
+        return self.fetch(m)
