@@ -1,0 +1,369 @@
+"""Benchmark: uniform-grid isosurface extraction on one GB300 (replicas on N GPUs).
+
+Workload (default): the 512^3 dense-ambiguity field -- a 33^3 grid of U[-1,1] values (seeded)
+trilinearly upsampled to 512^3 plus 0.02*N(0,1) per voxel, isovalue 0 -- extracted each step
+with TMC (shared-vertex triangles) and with DMC (halfedges, triangles, P3X3Y colour + isolated +
+P3333 simplification).  Synthetic data (no datasets exist for this path).  The field (512 MiB) is
+larger than L2, so no L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  `value` is device-resident throughput (field already in HBM); `e2e` is the
+same metric through the C ABI with host buffers (field copied in, mesh copied out every step).
+Cells per step = 2 * 511^3 (each extraction visits every cell once).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gcells/s"
+N = 512
+SEED = 1
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------------------------------------
+# clocks during the timed region
+# ------------------------------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) > 8:
+                for i, nm in enumerate(names):
+                    if r[5 + i].lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+# ------------------------------------------------------------------------------------------------
+# our arm
+# ------------------------------------------------------------------------------------------------
+def algorithmic_bytes(stage: str, sizes: dict, cells: int, voxels: int) -> float:
+    """Algorithmic bytes of one launch of a stage: field read once (4 B/voxel) for the classifying
+    kernels, emitted mesh bytes for the emitting kernels (24 B/vertex, 16 B/quad, 12 B/triangle);
+    scratch, hash tables and re-reads excluded."""
+    if stage in ("tmc_classify", "dmc_classify"):
+        return 4.0 * voxels
+    if stage == "tmc_emit":
+        return 24.0 * sizes["tmc_v"] + 12.0 * sizes["tmc_t"]
+    if stage == "dmc_vertex":
+        return 24.0 * sizes["dmc_front_v"]
+    if stage == "dmc_quad":
+        return 16.0 * sizes["dmc_front_q"]
+    return 0.0
+
+
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    from tmc_gb300 import native, volumes
+    try:
+        native.load()
+    except RuntimeError:
+        from tmc_gb300 import build
+        build.build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    vol = volumes.noise_volume(N, seed=SEED + rank)
+    cells = vol.cells
+    voxels = vol.data.size
+    ctx = native.Context(local)
+    dev = torch.from_numpy(vol.data).cuda()
+    vdev = native.make_volume(vol, dev.data_ptr(), on_device=True)
+    host = torch.from_numpy(vol.data).pin_memory()
+    vhost = native.make_volume(vol, host.data_ptr(), on_device=False)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    dmc_flags = native.DMC_SIMPLIFY | native.OUT_HALFEDGES | native.OUT_TRIANGLES
+
+    def step(v, extra=0):
+        mt = ctx.tmc_raw(v, vol.iso, extra)
+        md = ctx.dmc_raw(v, vol.iso, dmc_flags | extra)
+        return mt, md
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    for _ in range(args.warmup):
+        mt, md = step(vdev)
+        ctx.free(mt)
+        ctx.free(md)
+    sizes = {"tmc_v": mt.nr_v, "tmc_t": mt.nr_t, "dmc_v": md.nr_v, "dmc_q": md.nr_q}
+    # ---- device-resident timed region ----
+    barrier()
+    l0 = ctx.launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            mt, md = step(vdev)
+            ctx.free(mt)
+            ctx.free(md)
+        e1.record(stream)
+        barrier()
+    launches = ctx.launches() - l0
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    ms_step = ms / args.steps
+    value = world * 2 * cells * args.steps / (ms * 1e-3) / 1e9
+    # ---- end to end through the C ABI with host buffers ----
+    for _ in range(1):
+        mt, md = step(vhost, native.OUT_HOST)
+        ctx.free(mt)
+        ctx.free(md)
+    barrier()
+    d2h = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        mt, md = step(vhost, native.OUT_HOST)
+        d2h = (24 * mt.nr_v + 12 * mt.nr_t) + (24 * md.nr_v + 16 * md.nr_q + 12 * md.nr_t + 16 * md.nr_he +
+                                                 4 * md.nr_v + 4 * md.nr_q)
+        ctx.free(mt)
+        ctx.free(md)
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e = world * 2 * cells * args.steps / e2e_s / 1e9
+    # ---- per-stage profile (separate pass, not timed above) ----
+    ctx.set_profiling(True)
+    m = ctx.dmc_raw(vdev, vol.iso, native.OUT_LOCAL)  # front end alone, for its mesh sizes
+    sizes["dmc_front_v"], sizes["dmc_front_q"] = m.nr_v, m.nr_q
+    ctx.free(m)
+    ctx.set_profiling(True)
+    for _ in range(2):
+        mt, md = step(vdev)
+        ctx.free(mt)
+        ctx.free(md)
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    total_ms = sum(v[0] for v in prof.values())
+    dom = max(prof.items(), key=lambda kv: kv[1][0])
+    dom_name, (dom_ms, dom_cnt) = dom
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    avg_ms = dom_ms / max(dom_cnt, 1)
+    algo = algorithmic_bytes(dom_name, sizes, cells, voxels)
+    achieved = algo / (avg_ms * 1e-3) / 1e9 if algo else 0.0
+    stages = {k: {"ms_per_step": round(v[0] / 2, 4), "share": round(v[0] / total_ms, 4)} for k, v in prof.items()}
+    # memory-bound classifier, reported beside the dominant kernel
+    cls = {}
+    for st in ("tmc_classify", "dmc_classify"):
+        if st in prof:
+            a = prof[st][0] / prof[st][1]
+            cls[st] = {"ms": round(a, 4), "achieved_gbs": round(4.0 * voxels / (a * 1e-3) / 1e9, 1),
+                       "frac": round(4.0 * voxels / (a * 1e-3) / 1e9 / peak, 4)}
+    out = {
+        "metric": METRIC, "value": round(value, 4), "unit": "Gcells/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "512^3 noise field (33^3 U[-1,1] upsampled + 0.02 N(0,1)), isovalue 0: TMC shared-vertex"
+                               " + DMC halfedge/triangles with P3X3Y+P3333 simplification per step",
+                   "grid": [N, N, N], "cells_per_step": 2 * cells, "seed": SEED,
+                   "l2": "inputs larger than L2 (512 MiB field)", "parallelism": f"replicas x{world}"},
+        "mesh": sizes,
+        "e2e": {"value": round(e2e, 4), "unit": "Gcells/s", "h2d_bytes_per_step": 2 * 4 * voxels,
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "algorithmic_bytes_per_launch": algo, "avg_launch_ms": round(avg_ms, 4),
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s"},
+        "classify_roofline": cls,
+        "stages": stages,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_port(vol)
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return out if rank == 0 else None
+
+
+def _sample_slab(vol, z0, nz):
+    from tmc_gb300 import volumes
+    d = vol.data[z0:z0 + nz].copy()
+    return volumes.Volume(d, origin=(vol.origin[0], vol.origin[1], vol.origin[2] + z0 * vol.spacing[2]),
+                          spacing=vol.spacing, iso=vol.iso)
+
+
+def cpu_baseline_port(vol, planes=24):
+    """The oracle (a single-threaded C restatement of the reference CPU path) on a bounded sample
+    of the same field: a slab of `planes` z-planes, TMC + DMC with simplification."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from cpu_libs import OracleLib
+    o = OracleLib()
+    s = _sample_slab(vol, 200, planes)
+    t0 = time.perf_counter()
+    o.tmc(s)
+    o.dmc(s, 1)
+    dt = time.perf_counter() - t0
+    cells = 2 * s.cells
+    return {"value": round(cells / dt / 1e9, 6), "unit": "Gcells/s", "cores": 1, "kind": "port",
+            "sample": f"z-slab of {planes} planes ({s.dims[0]}x{s.dims[1]}x{s.dims[2]}) of the same field, "
+                      f"TMC + DMC(simplify), {dt:.2f} s"}
+
+
+# ------------------------------------------------------------------------------------------------
+# reference arm: the reference's own CPU implementation on the host cores
+# ------------------------------------------------------------------------------------------------
+def _ref_worker(a):
+    path, z0, nz, kind = a
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from tmc_gb300 import volumes
+    import cpu_libs
+    data = np.load(path, mmap_mode="r")
+    n = data.shape[2]
+    d = np.ascontiguousarray(data[z0:z0 + nz])
+    vol = volumes.Volume(d, origin=(-1.0, -1.0, -1.0 + z0 * 2.0 / (n - 1)), spacing=(2.0 / (n - 1),) * 3, iso=0.0)
+    lib = cpu_libs.RefLib() if kind == "reference" else cpu_libs.OracleLib()
+    t0 = time.perf_counter()
+    lib.tmc(vol)
+    lib.dmc(vol, 1)
+    return time.perf_counter() - t0, 2 * vol.cells
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    import multiprocessing as mp
+
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import cpu_libs
+    from tmc_gb300 import volumes
+    kind = "reference" if cpu_libs.ref_available() else "port"
+    if kind == "port":
+        try:
+            cpu_libs.OracleLib()
+        except Exception as e:
+            return {"impl": "reference", "unavailable": f"oracle could not be built: {e}"}
+    vol = volumes.noise_volume(N, seed=SEED)
+    path = "/dev/shm/tmc_bench_field.npy" if os.path.isdir("/dev/shm") else os.path.join(ROOT, "_bench_field.npy")
+    np.save(path, vol.data)
+    cores = os.cpu_count() or 1
+    planes = 12
+    jobs = [(path, (w * 37) % (N - planes), planes, kind) for w in range(cores)]
+    with mp.get_context("spawn").Pool(cores) as pool:
+        for _ in range(args.warmup):
+            pool.map(_ref_worker, jobs[: max(1, cores // 4)])
+        t0 = time.perf_counter()
+        cells = 0
+        for _ in range(args.steps):
+            for dt, c in pool.map(_ref_worker, jobs):
+                cells += c
+        wall = time.perf_counter() - t0
+    try:
+        os.remove(path)
+    except OSError:
+        pass
+    value = cells / wall / 1e9
+    ms_step = wall / args.steps * 1e3
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": "Gcells/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "512^3 noise field, isovalue 0: TMC shared-vertex + DMC with P3X3Y+P3333 "
+                                   "simplification, per step one z-slab sample per host core",
+                       "grid": [N, N, N], "sample_planes": planes},
+            "cpu_baseline": {"value": round(value, 6), "unit": "Gcells/s", "cores": cores, "kind": kind,
+                             "sample": f"{cores} slabs of {planes} z-planes of the 512^3 field per step, "
+                                       f"one process per core (the CPU path is single-threaded)"},
+            "e2e": {"value": round(value, 6), "unit": "Gcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        out = run_ours(args, rank, world, local)
+    if out is not None and rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -97,6 +97,12 @@ void* tmc_ctx_stream(tmc_ctx* ctx); /* the context's cudaStream_t */
 tmc_status tmc_ctx_synchronize(tmc_ctx* ctx);
 /* number of library kernels launched by this context since creation */
 int64_t tmc_ctx_launch_count(const tmc_ctx* ctx);
+/* Per-stage device timing with CUDA events on the context stream (the counterpart of the
+ * reference's CTimer stage report, dmc/CTimer.h:123-190).  Enabling resets the totals. */
+tmc_status tmc_ctx_set_profiling(tmc_ctx* ctx, int on);
+/* Copies up to `max` stages: names (32 chars each), accumulated milliseconds and event counts.
+ * Returns the number of stages, or -1. */
+int32_t tmc_ctx_profile_read(tmc_ctx* ctx, int32_t max, char* names, double* ms, int64_t* counts);
 
 /* extraction -------------------------------------------------------------------------------- */
 /* Dual Marching Cubes: quad mesh (+ triangles, + halfedges).  Vertices in generating-cell order,

@@ -371,28 +371,28 @@ static uint64_t he_key(int v0, int v1) {
 
 typedef struct { int* he; int* hv; int* hf; int nq; int nv; } hmesh;
 
-static void halfedges(int nr_v, const int* quads, int nr_q, hmesh* h) {
+static void halfedges_p(int nr_v, const int* quads, int P, int nr_q, hmesh* h) {
   h->nq = nr_q; h->nv = nr_v;
-  h->he = (int*)malloc((size_t)5 * 4 * nr_q * sizeof(int) + 1);
+  h->he = (int*)malloc((size_t)5 * P * nr_q * sizeof(int) + 1);
   h->hv = (int*)malloc((size_t)nr_v * sizeof(int) + 1);
   h->hf = (int*)malloc((size_t)nr_q * sizeof(int) + 1);
   for (int v = 0; v < nr_v; v++) h->hv[v] = INVALID;
-  hkey* keys = (hkey*)malloc((size_t)4 * nr_q * sizeof(hkey) + 1);
+  hkey* keys = (hkey*)malloc((size_t)P * nr_q * sizeof(hkey) + 1);
   for (int i = 0; i < nr_q; i++) {
-    const int* q = quads + 4 * i;
-    for (int r = 0; r < 4; r++) {
-      int* e = h->he + 5 * (4 * i + r);
-      e[0] = q[r]; e[1] = i; e[2] = 4 * i + (r + 1) % 4; e[3] = INVALID; e[4] = MANIFOLD;
+    const int* q = quads + P * i;
+    for (int r = 0; r < P; r++) {
+      int* e = h->he + 5 * (P * i + r);
+      e[0] = q[r]; e[1] = i; e[2] = P * i + (r + 1) % P; e[3] = INVALID; e[4] = MANIFOLD;
     }
-    h->hf[i] = 4 * i;
-    for (int r = 0; r < 4; r++) h->hv[q[r]] = 4 * i + r;
-    for (int r = 0; r < 4; r++) { keys[4 * i + r].key = he_key(q[r], q[(r + 1) % 4]); keys[4 * i + r].he = 4 * i + r; }
+    h->hf[i] = P * i;
+    for (int r = 0; r < P; r++) h->hv[q[r]] = P * i + r;
+    for (int r = 0; r < P; r++) { keys[P * i + r].key = he_key(q[r], q[(r + 1) % P]); keys[P * i + r].he = P * i + r; }
   }
-  qsort(keys, (size_t)4 * nr_q, sizeof(hkey), cmp_hkey);
+  qsort(keys, (size_t)P * nr_q, sizeof(hkey), cmp_hkey);
 #define HE(x) (h->he + 5 * (size_t)(x))
-  for (size_t s = 0; s < (size_t)4 * nr_q;) {
+  for (size_t s = 0; s < (size_t)P * nr_q;) {
     size_t t = s;
-    while (t < (size_t)4 * nr_q && keys[t].key == keys[s].key) t++;
+    while (t < (size_t)P * nr_q && keys[t].key == keys[s].key) t++;
     const int c = (int)(t - s);
     if (c == 1) {
       HE(keys[s].he)[3] = INVALID;
@@ -422,6 +422,7 @@ static void halfedges(int nr_v, const int* quads, int nr_q, hmesh* h) {
 #undef HE
   free(keys);
 }
+static void halfedges(int nr_v, const int* quads, int nr_q, hmesh* h) { halfedges_p(nr_v, quads, 4, nr_q, h); }
 static void hmesh_free(hmesh* h) { free(h->he); free(h->hv); free(h->hf); }
 
 #define HE(h, x) ((h)->he + 5 * (size_t)(x))
@@ -785,4 +786,20 @@ void oracle_dmc_color_valence(int nr_v, int nr_q, const int* quads, int* colors_
   memcpy(valence_out, vV, (size_t)nr_v * sizeof(int));
   free(vV);
   hmesh_free(&h);
+}
+
+/* Halfedges of a triangle (P = 3) or quad (P = 4) mesh with the rules of halfedges()
+ * (cpp_dmc/DualMarchingCubes.cpp:488-671); used as the oracle of the TMC halfedge output, whose
+ * reference kernel (cuda_tmc/MarchingCubes.cu:2284-2336) registers only the first edge of each
+ * triangle. he5: 5 ints per halfedge. */
+int64_t oracle_halfedges(const int* faces, int P, int nr_f, int nr_v, int* he5, int* hv, int* hf) {
+  hmesh h;
+  halfedges_p(nr_v, faces, P, nr_f, &h);
+  memcpy(he5, h.he, (size_t)5 * P * nr_f * sizeof(int));
+  memcpy(hv, h.hv, (size_t)nr_v * sizeof(int));
+  memcpy(hf, h.hf, (size_t)nr_f * sizeof(int));
+  int64_t nm = 0;
+  for (int64_t e = 0; e < (int64_t)P * nr_f; e++) nm += h.he[5 * e + 4] != 0;
+  hmesh_free(&h);
+  return nm;
 }

@@ -110,6 +110,18 @@ class OracleLib(_Lib):
         self.lib.oracle_dmc_color_valence(int(nv), int(q.size // 4), _p(q), _p(col), _p(val))
         return col, val
 
+    def halfedges(self, faces, P, nv):
+        """Halfedges of a P-gon mesh with the reference's halfedges() rules: he (5 per halfedge:
+        origin, face, next, twin, flag), hv, hf."""
+        f = np.ascontiguousarray(faces, dtype=np.int32)
+        nf = f.size // P
+        he = np.zeros(5 * P * nf, np.int32)
+        hv = np.zeros(nv, np.int32)
+        hf = np.zeros(nf, np.int32)
+        self.lib.oracle_halfedges.restype = ctypes.c_int64
+        self.lib.oracle_halfedges(_p(f), int(P), int(nf), int(nv), _p(he), _p(hv), _p(hf))
+        return dict(he=he, hv=hv, hf=hf)
+
 
 class RefLib(_Lib):
     prefix = "ref"

@@ -18,7 +18,7 @@ def lib():
 
 def declared():
     hdr = open(os.path.join(ROOT, "include", "tmc_gb300.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:tmc_status|const char\*|void\*|int64_t)\s+(tmc_\w+)\(", hdr, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:tmc_status|const char\*|void\*|int64_t|int32_t)\s+(tmc_\w+)\(", hdr, re.M)))
 
 
 def test_header_declares_entry_points():

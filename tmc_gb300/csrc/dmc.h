@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "profiler.h"
 
 namespace tmc {
 
@@ -26,8 +27,8 @@ struct DmcScratch {
 
 // Each launcher returns the number of kernels it launched.
 int64_t dmc_tiles(const Grid& g);  // scan tiles for the cell count of g
-int dmc_front_count(const Grid& g, DmcScratch& s, cudaStream_t st);
+int dmc_front_count(const Grid& g, DmcScratch& s, cudaStream_t st, Prof* prof = nullptr);
 int dmc_front_emit(const Grid& g, DmcScratch& s, DmcVertexOut vo, int32_t* quads, uint8_t* colors, int flip,
-                   int sms, cudaStream_t st);
+                   int sms, cudaStream_t st, Prof* prof = nullptr);
 
 }  // namespace tmc

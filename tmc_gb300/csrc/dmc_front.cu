@@ -481,10 +481,14 @@ __global__ void __launch_bounds__(128) dmc_quad_kernel(Grid g, const uint32_t* r
 // ------------------------------------------------------------------------------------------
 // host-side launches
 // ------------------------------------------------------------------------------------------
-int dmc_front_count(const Grid& g, DmcScratch& s, cudaStream_t st) {
+int dmc_front_count(const Grid& g, DmcScratch& s, cudaStream_t st, Prof* prof) {
   const int64_t n = g.ncells();
   const int64_t tiles = ceil_div(n, kScanTile);
-  dmc_classify_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(g, s.rec, s.tile_sums, s.stats);
+  {
+    Stage t(prof, "dmc_classify", st);
+    dmc_classify_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(g, s.rec, s.tile_sums, s.stats);
+  }
+  Stage t(prof, "dmc_scan", st);
   scan_tile_sums_kernel<<<1, 1024, 0, st>>>(s.tile_sums, tiles, s.totals);
   dmc_offsets_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(n, s.rec, s.tile_sums, s.voff, s.qoff);
   return 3;
@@ -493,10 +497,14 @@ int dmc_front_count(const Grid& g, DmcScratch& s, cudaStream_t st) {
 int64_t dmc_tiles(const Grid& g) { return ceil_div(g.ncells(), kScanTile); }
 
 int dmc_front_emit(const Grid& g, DmcScratch& s, DmcVertexOut vo, int32_t* quads, uint8_t* colors, int flip,
-                   int sms, cudaStream_t st) {
+                   int sms, cudaStream_t st, Prof* prof) {
   const int64_t n = g.ncells();
   const int64_t blocks = std::min<int64_t>(ceil_div(n, 128), (int64_t)sms * 16);
-  dmc_vertex_kernel<<<(unsigned)blocks, 128, 0, st>>>(g, s.rec, s.voff, vo, flip, s.stats);
+  {
+    Stage t(prof, "dmc_vertex", st);
+    dmc_vertex_kernel<<<(unsigned)blocks, 128, 0, st>>>(g, s.rec, s.voff, vo, flip, s.stats);
+  }
+  Stage t(prof, "dmc_quad", st);
   dmc_quad_kernel<<<(unsigned)blocks, 128, 0, st>>>(g, s.rec, s.voff, s.qoff, quads, colors);
   return 2;
 }

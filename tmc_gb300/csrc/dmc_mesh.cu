@@ -1,15 +1,622 @@
+// DMC mesh post-processing on the GPU: face colouring, vertex valence, P3X3Y simplification
+// (colour pass and isolated pass), P3333 simplification, final halfedges and the quad -> triangle
+// split.  Follows cpp_dmc/DualMarchingCubes.cpp:488-1460 step by step; every sequential loop of
+// the reference is shown to be order-independent (or made so) where it is parallelised:
+//
+//  * colorFaces (:714-844): faces are reduced class by class (inherited colours 5..23, then the
+//    faces whose inherited colour is 4).  Inherited colour = 3*parity(lower grid point) + axis,
+//    and two faces sharing an edge come from two grid edges of one grid face, so they never share
+//    an inherited colour: inside one class no face reads another face's new colour.  One launch
+//    per class.
+//  * mergeVertices3X3Y (:916-1094): a merge reads valence >= 5 vertices and writes valence-3
+//    vertices, so reads never see writes.  Several faces writing the same vertex resolve to the
+//    highest face index (the reference's last write), via atomicMax claims.
+//  * mark3333 (:1189-1322): marked faces cannot be adjacent and their vertices have valence 3, so
+//    no vertex is written twice; the neighbour flags are idempotent.
+//  * removal passes: order-preserving compaction through prefix sums.
+#include <cmath>
+
 #include "../../include/tmc_gb300.h"
 #include "dmc_mesh.h"
+#include "halfedges.h"
+#include "scan.cuh"
 
 namespace tmc {
 
-DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaStream_t st, DmcPostOut* out) {
-  (void)sms;
-  (void)st;
+namespace {
+
+inline unsigned grid_for(int64_t n, int sms) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)sms * 8));
+}
+
+#define FOR_EACH(i, n) for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
+
+__device__ __forceinline__ int he_twin(const int32_t* he, int64_t h) { return he[5 * h + 3]; }
+__device__ __forceinline__ int he_face(const int32_t* he, int64_t h) { return he[5 * h + 1]; }
+__device__ __forceinline__ int he_origin(const int32_t* he, int64_t h) { return he[5 * h]; }
+__device__ __forceinline__ int he_flag(const int32_t* he, int64_t h) { return he[5 * h + 4]; }
+
+// collectNeighbors (cpp_dmc/DualMarchingCubes.cpp:673-702); halfedge r of face f is 4f + r
+__device__ __forceinline__ void neighbors(const int32_t* he, int64_t f, int n[4]) {
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    const int t = he_twin(he, 4 * f + r);
+    n[r] = (t != -1) ? he_face(he, t) : -1;
+  }
+}
+
+// isNonManifold (:874-885)
+__device__ __forceinline__ bool non_manifold(const int32_t* he, int64_t f) {
+  return he_flag(he, 4 * f) == 1 || he_flag(he, 4 * f + 1) == 1 || he_flag(he, 4 * f + 2) == 1 ||
+         he_flag(he, 4 * f + 3) == 1;
+}
+
+// ---------------------------------------------------------------------------------------------
+// colouring
+// ---------------------------------------------------------------------------------------------
+// class of an inherited colour: 0..18 for colours 5..23, 19 for colour 4, -1 otherwise
+__device__ __forceinline__ int color_class(int c) { return c > 4 ? c - 5 : (c == 4 ? 19 : -1); }
+
+__global__ void color_count_kernel(const uint8_t* col, int64_t nq, int32_t* cnt) {
+  FOR_EACH(f, nq) {
+    const int k = color_class(col[f]);
+    if (k >= 0) atomicAdd(cnt + k, 1);
+  }
+}
+
+__global__ void color_offsets_kernel(const int32_t* cnt, int32_t* off, int32_t* cursor) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    int s = 0;
+    for (int k = 0; k < 20; k++) {
+      off[k] = s;
+      cursor[k] = s;
+      s += cnt[k];
+    }
+    off[20] = s;
+  }
+}
+
+__global__ void color_scatter_kernel(const uint8_t* col, int64_t nq, int32_t* cursor, int32_t* list) {
+  FOR_EACH(f, nq) {
+    const int k = color_class(col[f]);
+    if (k >= 0) list[atomicAdd(cursor + k, 1)] = (int32_t)f;
+  }
+}
+
+__global__ void color_reduce_kernel(const int32_t* he, uint8_t* col, const int32_t* list, const int32_t* off, int k,
+                                    int lim) {
+  const int64_t b = off[k], e = off[k + 1];
+  FOR_EACH(idx, e - b) {
+    const int f = list[b + idx];
+    int n[4], nc[4];
+    neighbors(he, f, n);
+#pragma unroll
+    for (int r = 0; r < 4; r++) nc[r] = (n[r] != -1) ? (int)col[n[r]] : -1;
+    for (int c = 0; c <= lim; c++) {
+      if (nc[0] != c && nc[1] != c && nc[2] != c && nc[3] != c) {
+        col[f] = (uint8_t)c;
+        break;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// valence and patterns
+// ---------------------------------------------------------------------------------------------
+// vertexValence (:847-871)
+__global__ void valence_kernel(const int32_t* he, int64_t nh, int32_t* val) {
+  FOR_EACH(h, nh) {
+    atomicAdd(val + he_origin(he, h), 1);
+    if (he_twin(he, h) == -1) atomicAdd(val + he_origin(he, he[5 * h + 2]), 1);
+  }
+}
+
+// mark3X3Y (:889-913)
+__global__ void mark3x3y_kernel(const int32_t* q, int64_t nq, const int32_t* val, uint8_t* p) {
+  FOR_EACH(f, nq) {
+    const int a = val[q[4 * f]], b = val[q[4 * f + 1]], c = val[q[4 * f + 2]], d = val[q[4 * f + 3]];
+    p[f] = (a == 3 && b >= 5 && c == 3 && d >= 5) || (a >= 5 && b == 3 && c >= 5 && d == 3);
+  }
+}
+
+// mergeVertices3X3Y, both variants (:916-1094): decide removal, claim written vertices
+__global__ void merge_claim_kernel(const int32_t* he, int64_t nq, const uint8_t* p, const int32_t* val,
+                                   const uint8_t* col, int color_pass, uint8_t* branch, int32_t* own_pos,
+                                   int32_t* own_rm) {
+  FOR_EACH(f, nq) {
+    branch[f] = 0;
+    if (!p[f]) continue;
+    int n[4];
+    neighbors(he, f, n);
+    if (color_pass) {
+      bool bad = false;
+      for (int r = 0; r < 4; r++) {
+        if (n[r] >= 0 && non_manifold(he, n[r])) bad = true;
+        if (n[r] < 0) bad = true;
+      }
+      if (bad) continue;
+      const int c = col[f];
+      bool ok = true;
+      for (int r = 0; r < 4; r++)
+        if (p[n[r]] && (int)col[n[r]] <= c) ok = false;
+      if (!ok) continue;
+    } else {
+      bool skip = false;
+      for (int r = 0; r < 4; r++)
+        if (n[r] != -1 && non_manifold(he, n[r])) skip = true;
+      for (int r = 0; r < 4; r++)
+        if (n[r] != -1 && p[n[r]]) skip = true;
+      if (skip) continue;
+    }
+    const int v0 = he_origin(he, 4 * f), v1 = he_origin(he, 4 * f + 1), v2 = he_origin(he, 4 * f + 2),
+              v3 = he_origin(he, 4 * f + 3);
+    const int a = val[v0], b = val[v1], c2 = val[v2], d = val[v3];
+    if (a == 3 && b >= 5 && c2 == 3 && d >= 5) {
+      branch[f] = 1;
+      atomicMax(own_pos + v0, (int32_t)f);
+      atomicMax(own_rm + v2, (int32_t)f);
+    } else if (a >= 5 && b == 3 && c2 >= 5 && d == 3) {
+      branch[f] = 2;
+      atomicMax(own_pos + v1, (int32_t)f);
+      atomicMax(own_rm + v3, (int32_t)f);
+    }
+  }
+}
+
+__device__ __forceinline__ void midpoint(double* v64, float* v, float* n, int dst, int a, int b) {
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const double x = v64[3 * (int64_t)a + d] + 0.5 * (v64[3 * (int64_t)b + d] - v64[3 * (int64_t)a + d]);
+    v64[3 * (int64_t)dst + d] = x;
+    v[3 * (int64_t)dst + d] = (float)x;
+  }
+  double m[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const double na = n[3 * (int64_t)a + d], nb = n[3 * (int64_t)b + d];
+    m[d] = na + 0.5 * (nb - na);
+  }
+  const double s = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+#pragma unroll
+  for (int d = 0; d < 3; d++) n[3 * (int64_t)dst + d] = (float)(m[d] / s);
+}
+
+__global__ void merge_apply_kernel(const int32_t* he, int64_t nq, const uint8_t* branch, const int32_t* own_pos,
+                                   const int32_t* own_rm, double* v64, float* v, float* n, uint8_t* vm_first,
+                                   int32_t* vm_second, uint8_t* em) {
+  FOR_EACH(f, nq) {
+    em[f] = branch[f] != 0;
+    if (!branch[f]) continue;
+    const int v0 = he_origin(he, 4 * f), v1 = he_origin(he, 4 * f + 1), v2 = he_origin(he, 4 * f + 2),
+              v3 = he_origin(he, 4 * f + 3);
+    if (branch[f] == 1) {
+      if (own_pos[v0] == f) midpoint(v64, v, n, v0, v1, v3);
+      vm_first[v2] = 1;
+      if (own_rm[v2] == f) vm_second[v2] = v0;
+    } else {
+      if (own_pos[v1] == f) midpoint(v64, v, n, v1, v0, v2);
+      vm_first[v3] = 1;
+      if (own_rm[v3] == f) vm_second[v3] = v1;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// compaction helpers
+// ---------------------------------------------------------------------------------------------
+__global__ void invert_flags_kernel(const uint8_t* in, int64_t n, uint8_t* out) {
+  FOR_EACH(i, n) out[i] = !in[i];
+}
+
+// removeVertices3X3Y / removeVertices3333 (:1096-1112, :1324-1338): kept vertices move to their
+// new index, which becomes their map entry
+__global__ void gather_vertices_kernel(const uint8_t* keep, const int32_t* idx, int64_t nv, const double* v64,
+                                       const float* v, const float* n, double* v64o, float* vo, float* no,
+                                       int32_t* map) {
+  FOR_EACH(i, nv) {
+    if (!keep[i]) continue;
+    const int64_t o = idx[i];
+    for (int d = 0; d < 3; d++) {
+      v64o[3 * o + d] = v64[3 * i + d];
+      vo[3 * o + d] = v[3 * i + d];
+      no[3 * o + d] = n[3 * i + d];
+    }
+    map[i] = (int32_t)o;
+  }
+}
+
+// removeQuadrilaterals3X3Y (:1114-1137)
+__global__ void gather_quads_3x3y_kernel(const uint8_t* em, const int32_t* idx, int64_t nq, const int32_t* q,
+                                         const uint8_t* vm_first, const int32_t* vm_second, int32_t* qo) {
+  FOR_EACH(f, nq) {
+    if (em[f]) continue;
+    const int64_t o = idx[f];
+    for (int r = 0; r < 4; r++) {
+      const int x = q[4 * f + r];
+      qo[4 * o + r] = vm_first[x] ? vm_second[vm_second[x]] : vm_second[x];
+    }
+  }
+}
+
+// mark3333 (:1189-1322)
+__global__ void mark3333_kernel(const int32_t* he, int64_t nq, const int32_t* val, uint8_t* p3, uint8_t* rflag,
+                                uint8_t* vm0, int32_t* vm1) {
+  FOR_EACH(f, nq) {
+    if (non_manifold(he, f)) continue;
+    int vq[4], fo[4], vo[4];
+    for (int r = 0; r < 4; r++) vq[r] = he_origin(he, 4 * f + r);
+    if (val[vq[0]] != 3 || val[vq[1]] != 3 || val[vq[2]] != 3 || val[vq[3]] != 3) continue;
+    bool boundary = false;
+    for (int r = 0; r < 4; r++) {
+      const int twin = he_twin(he, 4 * f + r);
+      if (twin == -1) {
+        boundary = true;
+        break;
+      }
+      fo[r] = he_face(he, twin);
+      const int nx = he[5 * (int64_t)he[5 * (int64_t)twin + 2] + 2];
+      vo[r] = he_origin(he, nx);
+    }
+    if (boundary) continue;
+    bool nm = false;
+    for (int r = 0; r < 4; r++)
+      if (non_manifold(he, fo[r])) nm = true;
+    if (nm) continue;
+    const int a = val[vo[0]], b = val[vo[1]], c = val[vo[2]], d = val[vo[3]];
+    if ((a == 3 && b == 3) || (b == 3 && c == 3) || (c == 3 && d == 3) || (d == 3 && a == 3)) continue;
+    if (a == 3 || b == 3 || c == 3 || d == 3) continue;
+    if (a == 4 && b == 4 && c == 4 && d == 4) continue;
+    for (int r = 0; r < 4; r++) {
+      vm0[vq[r]] = 1;
+      vm1[vq[r]] = vo[r];
+    }
+    p3[f] = 1;
+    for (int r = 0; r < 4; r++) rflag[fo[r]] = 1;
+  }
+}
+
+// removeQuadrilaterals3333 (:1340-1382)
+__global__ void gather_quads_3333_kernel(const uint8_t* rflag, const int32_t* idx, int64_t nq, const int32_t* q,
+                                         const uint8_t* p3, const int32_t* vm1, const int32_t* vm2, int32_t* qo) {
+  FOR_EACH(f, nq) {
+    if (rflag[f]) continue;
+    const int64_t o = idx[f];
+    for (int r = 0; r < 4; r++) {
+      const int x = q[4 * f + r];
+      qo[4 * o + r] = p3[f] ? vm2[vm1[x]] : vm2[x];
+    }
+  }
+}
+
+__global__ void fill_i32_kernel(int32_t* p, int64_t n, int32_t v) {
+  FOR_EACH(i, n) p[i] = v;
+}
+
+// ---------------------------------------------------------------------------------------------
+// quad -> triangles (collectTriangles, :1387-1460; minAngle, DualMarchingCubes.h:746-756)
+// ---------------------------------------------------------------------------------------------
+// float acos rounded once from the float64 result: correctly rounded in all but vanishingly rare
+// cases (the host library's acosf is not, so splits decided by a 1-ulp tie may differ)
+__device__ __forceinline__ float acos_f(float x) { return (float)acos((double)x); }
+
+__device__ __forceinline__ double min_angle(const double* p0, const double* p1, const double* p2) {
+  auto dist = [](const double* a, const double* b) {
+    const double d = (a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]);
+    return sqrt(d);
+  };
+  const float a = dist(p0, p1);
+  const float b = dist(p1, p2);
+  const float c = dist(p2, p0);
+  const float A = acos_f((b * b + c * c - a * a) / (2 * b * c));
+  const float B = acos_f((a * a + c * c - b * b) / (2 * a * c));
+  const float C = acos_f((b * b + a * a - c * c) / (2 * b * a));
+  const float mAB = (B < A) ? B : A;
+  return (C < mAB) ? C : mAB;
+}
+
+__global__ void triangles_kernel(const int32_t* q, int64_t nq, const double* v64, int32_t* t) {
+  FOR_EACH(i, nq) {
+    const int v0 = q[4 * i], v1 = q[4 * i + 1], v2 = q[4 * i + 2], v3 = q[4 * i + 3];
+    const double *P0 = v64 + 3 * (int64_t)v0, *P1 = v64 + 3 * (int64_t)v1, *P2 = v64 + 3 * (int64_t)v2,
+                 *P3 = v64 + 3 * (int64_t)v3;
+    double a1 = min_angle(P0, P1, P2);
+    double a2 = min_angle(P0, P2, P3);
+    const double b1 = a2 < a1 ? a2 : a1, b2 = a1 < a2 ? a2 : a1;
+    a1 = min_angle(P1, P3, P0);
+    a2 = min_angle(P1, P2, P3);
+    const double c1 = a2 < a1 ? a2 : a1, c2 = a1 < a2 ? a2 : a1;
+    int32_t* o = t + 6 * i;
+    if (b1 < c1 || (b1 == c1 && b2 <= c2)) {
+      o[0] = v1; o[1] = v3; o[2] = v0; o[3] = v1; o[4] = v2; o[5] = v3;
+    } else {
+      o[0] = v0; o[1] = v1; o[2] = v2; o[3] = v0; o[4] = v2; o[5] = v3;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// driver helpers
+// ---------------------------------------------------------------------------------------------
+struct Pool {
+  cudaStream_t st;
+  std::vector<void*> temp;
+  cudaError_t err = cudaSuccess;
+  template <typename T>
+  T* get(int64_t n) {
+    void* p = nullptr;
+    if (err != cudaSuccess) return nullptr;
+    err = cudaMallocAsync(&p, (size_t)std::max<int64_t>(n, 4) * sizeof(T), st);
+    if (err == cudaSuccess) temp.push_back(p);
+    return (T*)p;
+  }
+  void drop(void* p) {
+    for (auto& q : temp)
+      if (q == p) q = nullptr;
+  }
+  ~Pool() {
+    for (void* p : temp)
+      if (p) cudaFreeAsync(p, st);
+  }
+};
+
+struct HeWork {
+  int32_t* he5 = nullptr;
+  int32_t* hv = nullptr;
+  int32_t* hf = nullptr;
+  HeTable t{};
+  int32_t* slot = nullptr;
+  unsigned long long* hv_key = nullptr;
+  unsigned long long* nm = nullptr;
+  unsigned* ovf = nullptr;
+};
+
+}  // namespace
+
+DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaStream_t st, DmcPostOut* out,
+                              Prof* prof) {
   DmcPostStatus s;
   out->mesh = in;
-  if (flags & (TMC_DMC_P3X3Y_COLOR | TMC_DMC_P3X3Y_ISOLATED | TMC_DMC_P3333 | TMC_OUT_TRIANGLES | TMC_OUT_HALFEDGES))
-    s.err = cudaErrorNotSupported;
+  const bool c3x3y = flags & TMC_DMC_P3X3Y_COLOR, i3x3y = flags & TMC_DMC_P3X3Y_ISOLATED,
+             p3333 = flags & TMC_DMC_P3333, want_t = flags & TMC_OUT_TRIANGLES, want_he = flags & TMC_OUT_HALFEDGES;
+  if (!(c3x3y || i3x3y || p3333 || want_t || want_he)) return s;
+  Pool pool{st};
+  const int64_t NV = std::max<int64_t>(in.nv, 1), NQ = std::max<int64_t>(in.nq, 1);
+  unsigned long long* h_cnt = nullptr;
+  if ((s.err = cudaMallocHost(&h_cnt, 4 * sizeof(unsigned long long))) != cudaSuccess) return s;
+
+  // working mesh (double buffered)
+  DmcMesh cur = in;
+  HeWork hw;
+  hw.he5 = pool.get<int32_t>(5 * 4 * NQ);
+  hw.hv = pool.get<int32_t>(NV);
+  hw.hf = pool.get<int32_t>(NQ);
+  hw.t.size = he_table_size(4 * NQ);
+  hw.t.keys = pool.get<unsigned long long>(hw.t.size);
+  hw.t.count = pool.get<int32_t>(hw.t.size);
+  hw.t.ids = pool.get<int32_t>(4 * hw.t.size);
+  hw.slot = pool.get<int32_t>(4 * NQ);
+  hw.hv_key = pool.get<unsigned long long>(NV);
+  hw.nm = pool.get<unsigned long long>(2);
+  hw.ovf = pool.get<unsigned>(2);
+  unsigned long long* tiles = pool.get<unsigned long long>(scan_tiles(4 * NQ) + 2);
+  unsigned long long* total = pool.get<unsigned long long>(2);
+  if (pool.err) {
+    s.err = pool.err;
+    cudaFreeHost(h_cnt);
+    return s;
+  }
+  auto halfedges = [&](const DmcMesh& m) {
+    Stage tm(prof, "dmc_halfedges", st);
+    cudaMemsetAsync(hw.nm, 0, 2 * sizeof(unsigned long long), st);
+    HeOut ho{hw.he5, hw.hv, hw.hf};
+    s.launches += build_halfedges(m.quads, 4, m.nq, m.nv, ho, hw.t, hw.slot, hw.hv_key, hw.nm, hw.ovf, sms, st);
+  };
+  auto read_total = [&]() -> int64_t {
+    cudaMemcpyAsync(h_cnt, total, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    return (int64_t)h_cnt[0];
+  };
+
+  const bool simplify = c3x3y || i3x3y || p3333;
+  int32_t* val = nullptr;
+  uint8_t *p = nullptr, *branch = nullptr, *vm_first = nullptr, *em = nullptr, *keep = nullptr;
+  int32_t *own_pos = nullptr, *own_rm = nullptr, *vm_second = nullptr, *idx = nullptr;
+  if (simplify) {
+    val = pool.get<int32_t>(NV);
+    p = pool.get<uint8_t>(NQ);
+    branch = pool.get<uint8_t>(NQ);
+    vm_first = pool.get<uint8_t>(NV);
+    em = pool.get<uint8_t>(NQ);
+    keep = pool.get<uint8_t>(std::max(NV, NQ));
+    own_pos = pool.get<int32_t>(NV);
+    own_rm = pool.get<int32_t>(NV);
+    vm_second = pool.get<int32_t>(NV);
+    idx = pool.get<int32_t>(std::max(NV, NQ));
+    if (pool.err) {
+      s.err = pool.err;
+      cudaFreeHost(h_cnt);
+      return s;
+    }
+  }
+  // new output buffers replace the input ones after each compaction
+  auto new_vertices = [&](int64_t nv, DmcMesh& m) {
+    m.v64 = nullptr;
+    cudaError_t e;
+    void *a = nullptr, *b = nullptr, *c = nullptr;
+    if ((e = cudaMallocAsync(&a, std::max<int64_t>(nv, 1) * 3 * sizeof(double), st)) != cudaSuccess) return e;
+    if ((e = cudaMallocAsync(&b, std::max<int64_t>(nv, 1) * 3 * sizeof(float), st)) != cudaSuccess) return e;
+    if ((e = cudaMallocAsync(&c, std::max<int64_t>(nv, 1) * 3 * sizeof(float), st)) != cudaSuccess) return e;
+    m.v64 = (double*)a;
+    m.v = (float*)b;
+    m.n = (float*)c;
+    return cudaSuccess;
+  };
+  auto retire = [&](void* ptr) {
+    if (!ptr) return;
+    bool mine = false;
+    for (auto& q : out->owned)
+      if (q == ptr) {
+        q = nullptr;
+        mine = true;
+      }
+    if (!mine) out->freed.push_back(ptr);
+    cudaFreeAsync(ptr, st);
+  };
+  auto adopt = [&](void* ptr) { out->owned.push_back(ptr); };
+
+  const unsigned gq = grid_for(NQ, sms), gv = grid_for(NV, sms);
+  // ---- P3X3Y: colour pass, then isolated pass (simplify3X3Y, :1139-1182) ----
+  for (int pass = 0; pass < 2; pass++) {
+    if ((pass == 0 && !c3x3y) || (pass == 1 && !i3x3y)) continue;
+    if (cur.nq == 0) break;
+    halfedges(cur);
+    if (pass == 0) {
+      Stage tm(prof, "dmc_color", st);
+      int32_t* cnt = pool.get<int32_t>(24);
+      int32_t* off = pool.get<int32_t>(24);
+      int32_t* cursor = pool.get<int32_t>(24);
+      int32_t* list = pool.get<int32_t>(NQ);
+      if (pool.err) break;
+      cudaMemsetAsync(cnt, 0, 24 * sizeof(int32_t), st);
+      color_count_kernel<<<gq, 256, 0, st>>>(cur.colors, cur.nq, cnt);
+      color_offsets_kernel<<<1, 32, 0, st>>>(cnt, off, cursor);
+      color_scatter_kernel<<<gq, 256, 0, st>>>(cur.colors, cur.nq, cursor, list);
+      s.launches += 3;
+      for (int k = 0; k < 19; k++) color_reduce_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.colors, list, off, k, 4);
+      color_reduce_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.colors, list, off, 19, 3);
+      s.launches += 20;
+    }
+    Stage tm(prof, "dmc_p3x3y", st);
+    cudaMemsetAsync(val, 0, cur.nv * sizeof(int32_t), st);
+    valence_kernel<<<grid_for(4 * cur.nq, sms), 256, 0, st>>>(hw.he5, 4 * cur.nq, val);
+    mark3x3y_kernel<<<gq, 256, 0, st>>>(cur.quads, cur.nq, val, p);
+    fill_i32_kernel<<<gv, 256, 0, st>>>(own_pos, cur.nv, -1);
+    fill_i32_kernel<<<gv, 256, 0, st>>>(own_rm, cur.nv, -1);
+    fill_i32_kernel<<<gv, 256, 0, st>>>(vm_second, cur.nv, -1);
+    cudaMemsetAsync(vm_first, 0, cur.nv, st);
+    merge_claim_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.nq, p, val, cur.colors, pass == 0, branch, own_pos, own_rm);
+    merge_apply_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.nq, branch, own_pos, own_rm, cur.v64, cur.v, cur.n, vm_first,
+                                           vm_second, em);
+    s.launches += 8;
+    // remove vertices
+    invert_flags_kernel<<<gv, 256, 0, st>>>(vm_first, cur.nv, keep);
+    s.launches += 1 + scan_flags(keep, cur.nv, idx, tiles, total, st);
+    const int64_t nv2 = read_total();
+    DmcMesh nx = cur;
+    if ((s.err = new_vertices(nv2, nx)) != cudaSuccess) break;
+    adopt(nx.v64);
+    adopt(nx.v);
+    adopt(nx.n);
+    gather_vertices_kernel<<<gv, 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.v, cur.n, nx.v64, nx.v, nx.n,
+                                                vm_second);
+    // remove quads
+    invert_flags_kernel<<<gq, 256, 0, st>>>(em, cur.nq, keep);
+    s.launches += 2 + scan_flags(keep, cur.nq, idx, tiles, total, st);
+    const int64_t nq2 = read_total();
+    void* qn = nullptr;
+    if ((s.err = cudaMallocAsync(&qn, std::max<int64_t>(nq2, 1) * 4 * sizeof(int32_t), st)) != cudaSuccess) break;
+    adopt(qn);
+    gather_quads_3x3y_kernel<<<gq, 256, 0, st>>>(keep, idx, cur.nq, cur.quads, vm_first, vm_second, (int32_t*)qn);
+    s.launches += 1;
+    // the inherited colours are only read by the colour pass; they are not carried along
+    retire(cur.v64);
+    retire(cur.v);
+    retire(cur.n);
+    retire(cur.quads);
+    nx.nv = nv2;
+    nx.nq = nq2;
+    nx.quads = (int32_t*)qn;
+    cur = nx;
+  }
+  // ---- P3333 (simplify3333, :1362-1385) ----
+  if (s.err == cudaSuccess && p3333 && cur.nq > 0) {
+    halfedges(cur);
+    Stage tm(prof, "dmc_p3333", st);
+    uint8_t* p3 = p;
+    uint8_t* rflag = em;
+    uint8_t* vm0 = vm_first;
+    int32_t* vm1 = own_pos;
+    int32_t* vm2 = vm_second;
+    cudaMemsetAsync(val, 0, cur.nv * sizeof(int32_t), st);
+    valence_kernel<<<grid_for(4 * cur.nq, sms), 256, 0, st>>>(hw.he5, 4 * cur.nq, val);
+    cudaMemsetAsync(p3, 0, cur.nq, st);
+    cudaMemsetAsync(rflag, 0, cur.nq, st);
+    cudaMemsetAsync(vm0, 0, cur.nv, st);
+    fill_i32_kernel<<<gv, 256, 0, st>>>(vm1, cur.nv, -1);
+    fill_i32_kernel<<<gv, 256, 0, st>>>(vm2, cur.nv, -1);
+    mark3333_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.nq, val, p3, rflag, vm0, vm1);
+    invert_flags_kernel<<<gv, 256, 0, st>>>(vm0, cur.nv, keep);
+    s.launches += 5 + scan_flags(keep, cur.nv, idx, tiles, total, st);
+    const int64_t nv2 = read_total();
+    DmcMesh nx = cur;
+    if ((s.err = new_vertices(nv2, nx)) == cudaSuccess) {
+      adopt(nx.v64);
+      adopt(nx.v);
+      adopt(nx.n);
+      gather_vertices_kernel<<<gv, 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.v, cur.n, nx.v64, nx.v, nx.n, vm2);
+      invert_flags_kernel<<<gq, 256, 0, st>>>(rflag, cur.nq, keep);
+      s.launches += 2 + scan_flags(keep, cur.nq, idx, tiles, total, st);
+      const int64_t nq2 = read_total();
+      void* qn = nullptr;
+      if ((s.err = cudaMallocAsync(&qn, std::max<int64_t>(nq2, 1) * 4 * sizeof(int32_t), st)) == cudaSuccess) {
+        adopt(qn);
+        gather_quads_3333_kernel<<<gq, 256, 0, st>>>(rflag, idx, cur.nq, cur.quads, p3, vm1, vm2, (int32_t*)qn);
+        s.launches += 1;
+        retire(cur.v64);
+        retire(cur.v);
+        retire(cur.n);
+        retire(cur.quads);
+        nx.nv = nv2;
+        nx.nq = nq2;
+        nx.quads = (int32_t*)qn;
+        cur = nx;
+      }
+    }
+  }
+  // ---- final halfedges and triangles ----
+  if (s.err == cudaSuccess && want_he) {
+    halfedges(cur);
+    void *he4 = nullptr, *hv = nullptr, *hf = nullptr;
+    if ((s.err = cudaMallocAsync(&he4, std::max<int64_t>(4 * cur.nq, 1) * 4 * sizeof(int32_t), st)) == cudaSuccess &&
+        (s.err = cudaMallocAsync(&hv, std::max<int64_t>(cur.nv, 1) * sizeof(int32_t), st)) == cudaSuccess &&
+        (s.err = cudaMallocAsync(&hf, std::max<int64_t>(cur.nq, 1) * sizeof(int32_t), st)) == cudaSuccess) {
+      adopt(he4);
+      adopt(hv);
+      adopt(hf);
+      s.launches += pack_halfedges4(hw.he5, 4 * cur.nq, (int32_t*)he4, sms, st);
+      cudaMemcpyAsync(hv, hw.hv, cur.nv * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+      cudaMemcpyAsync(hf, hw.hf, cur.nq * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+      cudaMemcpyAsync(h_cnt + 1, hw.nm, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+      cudaStreamSynchronize(st);
+      out->non_manifold = (int64_t)h_cnt[1];
+      out->nhe = 4 * cur.nq;
+      out->he = (int32_t*)he4;
+      out->he_v = (int32_t*)hv;
+      out->he_f = (int32_t*)hf;
+    }
+  }
+  if (s.err == cudaSuccess && want_t) {
+    void* tr = nullptr;
+    if ((s.err = cudaMallocAsync(&tr, std::max<int64_t>(2 * cur.nq, 1) * 3 * sizeof(int32_t), st)) == cudaSuccess) {
+      adopt(tr);
+      Stage tm(prof, "dmc_triangles", st);
+      triangles_kernel<<<grid_for(cur.nq, sms), 256, 0, st>>>(cur.quads, cur.nq, cur.v64, (int32_t*)tr);
+      s.launches += 1;
+      out->nt = 2 * cur.nq;
+      out->tris = (int32_t*)tr;
+    }
+  }
+  {
+    std::vector<void*> keepv;
+    for (void* q : out->owned)
+      if (q) keepv.push_back(q);
+    out->owned.swap(keepv);
+  }
+  if (s.err == cudaSuccess) s.err = cudaGetLastError();
+  cudaStreamSynchronize(st);
+  cudaFreeHost(h_cnt);
+  out->mesh = cur;
   return s;
 }
 

@@ -5,6 +5,8 @@
 #include <vector>
 #include <cuda_runtime.h>
 
+#include "profiler.h"
+
 namespace tmc {
 
 struct DmcMesh {
@@ -33,6 +35,7 @@ struct DmcPostStatus {
   int launches = 0;
 };
 
-DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaStream_t st, DmcPostOut* out);
+DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaStream_t st, DmcPostOut* out,
+                              Prof* prof = nullptr);
 
 }  // namespace tmc

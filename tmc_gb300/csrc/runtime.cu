@@ -14,6 +14,8 @@
 #include "common.cuh"
 #include "dmc.h"
 #include "dmc_mesh.h"
+#include "halfedges.h"
+#include "profiler.h"
 #include "tmc_cells.h"
 
 struct tmc_ctx {
@@ -26,6 +28,7 @@ struct tmc_ctx {
   std::atomic<int64_t> launches{0};
   unsigned long long* d_stats = nullptr;  // 8 counters, reused per call
   void* h_pinned = nullptr;               // small pinned staging area (totals, stats)
+  tmc::Prof prof;                         // stage timings (off unless enabled)
 };
 
 namespace {
@@ -234,6 +237,33 @@ tmc_status tmc_ctx_synchronize(tmc_ctx* ctx) {
   return TMC_OK;
 }
 
+tmc_status tmc_ctx_set_profiling(tmc_ctx* ctx, int on) {
+  if (!ctx) return TMC_ERR_INVALID_ARG;
+  TMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->prof.collect();
+  ctx->prof.on = on != 0;
+  ctx->prof.acc.clear();
+  return TMC_OK;
+}
+
+int32_t tmc_ctx_profile_read(tmc_ctx* ctx, int32_t max, char* names, double* ms, int64_t* counts) {
+  if (!ctx) return -1;
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return -1;
+  ctx->prof.collect();
+  int32_t i = 0;
+  for (auto& kv : ctx->prof.acc) {
+    if (i >= max) break;
+    if (names) {
+      std::strncpy(names + 32 * i, kv.first.c_str(), 31);
+      names[32 * i + 31] = 0;
+    }
+    if (ms) ms[i] = kv.second.first;
+    if (counts) counts[i] = kv.second.second;
+    i++;
+  }
+  return i;
+}
+
 tmc_status tmc_mesh_free(tmc_ctx* ctx, tmc_mesh* mesh) {
   if (!ctx || !mesh) return TMC_ERR_INVALID_ARG;
   MeshPriv* mp = (MeshPriv*)mesh->priv;
@@ -273,7 +303,7 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   TMC_CUDA(ctx, al.get(&sc.totals, 2));
   sc.stats = ctx->d_stats;
   TMC_CUDA(ctx, cudaMemsetAsync(sc.stats, 0, 8 * sizeof(unsigned long long), st));
-  ctx->launches += tmc::dmc_front_count(g, sc, st);
+  ctx->launches += tmc::dmc_front_count(g, sc, st, &ctx->prof);
   unsigned long long* h = (unsigned long long*)ctx->h_pinned;
   TMC_CUDA(ctx, cudaMemcpyAsync(h, sc.totals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   TMC_CUDA(ctx, cudaStreamSynchronize(st));
@@ -300,7 +330,9 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   } while (0)
   TMC_GET(vo.v, 3 * nv);
   TMC_GET(vo.n, 3 * nv);
-  if (flags & TMC_OUT_POS_F64) TMC_GET(vo.v64, 3 * nv);
+  // simplification and the triangle split work on float64 positions, as the reference does
+  const bool need_f64 = (flags & (TMC_OUT_POS_F64 | TMC_OUT_TRIANGLES)) || simplify;
+  if (need_f64) TMC_GET(vo.v64, 3 * nv);
   if (flags & TMC_OUT_LOCAL) {
     TMC_GET(vo.vcell, nv);
     TMC_GET(vo.vuvw, 3 * nv);
@@ -311,7 +343,8 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
     delete mp;
     TMC_CUDA(ctx, ce);
   }
-  ctx->launches += tmc::dmc_front_emit(g, sc, vo, quads, colors, (flags & TMC_GRAD_FLIP) ? 1 : 0, ctx->sms, st);
+  ctx->launches += tmc::dmc_front_emit(g, sc, vo, quads, colors, (flags & TMC_GRAD_FLIP) ? 1 : 0, ctx->sms, st,
+                                       &ctx->prof);
   TMC_CUDA(ctx, cudaGetLastError());
 
   tmc::DmcMesh mesh{};
@@ -323,7 +356,7 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   mesh.quads = quads;
   mesh.colors = colors;
   tmc::DmcPostOut post{};
-  tmc::DmcPostStatus ps = tmc::dmc_postprocess(mesh, flags, ctx->sms, st, &post);
+  tmc::DmcPostStatus ps = tmc::dmc_postprocess(mesh, flags, ctx->sms, st, &post, &ctx->prof);
   if (ps.err != cudaSuccess) {
     delete mp;
     TMC_CUDA(ctx, ps.err);
@@ -346,6 +379,18 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   out->v = post.mesh.v;
   out->n = post.mesh.n;
   out->v64 = post.mesh.v64;
+  if (out->v64 && !(flags & TMC_OUT_POS_F64)) {
+    for (auto& q : mp->dev)
+      if (q == out->v64) q = nullptr;
+    {
+      std::vector<void*> keep;
+      for (void* q : mp->dev)
+        if (q) keep.push_back(q);
+      mp->dev.swap(keep);
+    }
+    cudaFreeAsync(out->v64, st);
+    out->v64 = nullptr;
+  }
   out->quads = post.mesh.quads;
   out->nr_t = post.nt;
   out->tris = post.tris;
@@ -358,6 +403,7 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   TMC_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   TMC_CUDA(ctx, cudaStreamSynchronize(st));
   for (int q = 0; q < 8; q++) out->stats[q] = (int64_t)h[q];
+  ctx->prof.collect();
   out->stats[4] = post.non_manifold;
   out->stats[6] = ncell;
 #undef TMC_GET
@@ -366,16 +412,118 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
 
 }  // extern "C"
 
-extern "C" {
-// Entry points whose drivers live in other translation units are defined there; these two are
-// placeholders until the TMC and batched drivers land.
-tmc_status tmc_tmc_sharedvertex(tmc_ctx* ctx, const tmc_volume*, double, uint32_t, tmc_mesh* out) {
-  if (out) mesh_reset(out);
-  return fail(ctx, TMC_ERR_INTERNAL, "TMC extraction is not built yet");
+namespace {
+
+// TMC extraction driver shared by the shared-vertex and halfedge entry points.
+tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t flags, tmc_mesh* out, bool halfedge) {
+  if (!ctx || !out) return fail(ctx, TMC_ERR_INVALID_ARG, "context or output is NULL");
+  mesh_reset(out);
+  tmc_status s = check_volume(ctx, vol);
+  if (s) return s;
+  if (!std::isfinite(iso)) return fail(ctx, TMC_ERR_INVALID_ARG, "isovalue must be finite");
+  if (flags & (TMC_DMC_SIMPLIFY | TMC_DMC_P3X3Y_COLOR | TMC_DMC_P3X3Y_ISOLATED | TMC_DMC_P3333 | TMC_OUT_LOCAL))
+    return fail(ctx, TMC_ERR_INVALID_ARG, "DMC-only flag given to a TMC extraction");
+  if (halfedge) flags |= TMC_OUT_HALFEDGES;
+  TMC_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  Allocs al(ctx);
+  const float* field = nullptr;
+  if ((s = field_on_device(ctx, vol, al, &field))) return s;
+  const tmc::Grid g = make_grid(vol, field, iso);
+  const int64_t ncell = g.ncells();
+  tmc::TmcScratch sc{};
+  TMC_CUDA(ctx, al.get(&sc.rec, ncell));
+  TMC_CUDA(ctx, al.get(&sc.voff, ncell));
+  TMC_CUDA(ctx, al.get(&sc.toff, ncell));
+  TMC_CUDA(ctx, al.get(&sc.tile_sums, tmc::tmc_tiles(g)));
+  TMC_CUDA(ctx, al.get(&sc.totals, 2));
+  sc.stats = ctx->d_stats;
+  TMC_CUDA(ctx, cudaMemsetAsync(sc.stats, 0, 8 * sizeof(unsigned long long), st));
+  ctx->launches += tmc::tmc_count(g, sc, st, &ctx->prof);
+  unsigned long long* h = (unsigned long long*)ctx->h_pinned;
+  TMC_CUDA(ctx, cudaMemcpyAsync(h, sc.totals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  TMC_CUDA(ctx, cudaStreamSynchronize(st));
+  const int64_t nv = (int64_t)(h[0] >> 32), nt = (int64_t)(h[0] & 0xffffffffull);
+
+  MeshPriv* mp = new (std::nothrow) MeshPriv();
+  if (!mp) return fail(ctx, TMC_ERR_OOM, "host allocation failed");
+  cudaError_t ce = cudaSuccess;
+#define TMC_OWN(ptr, count)                 \
+  do {                                      \
+    ce = al.get(&(ptr), (count));           \
+    if (ce != cudaSuccess) {                \
+      delete mp;                            \
+      TMC_CUDA(ctx, ce);                    \
+    }                                       \
+    al.release(ptr);                        \
+    mp->dev.push_back(ptr);                 \
+  } while (0)
+  tmc::TmcVertexOut vo{};
+  int32_t* tris = nullptr;
+  TMC_OWN(vo.v, 3 * nv);
+  TMC_OWN(vo.n, 3 * nv);
+  if (flags & TMC_OUT_POS_F64) TMC_OWN(vo.v64, 3 * nv);
+  TMC_OWN(tris, 3 * nt);
+  ctx->launches += tmc::tmc_emit(g, sc, vo, tris, ctx->sms, st, &ctx->prof);
+  TMC_CUDA(ctx, cudaGetLastError());
+  out->nr_v = nv;
+  out->nr_t = nt;
+  out->v = vo.v;
+  out->n = vo.n;
+  out->v64 = vo.v64;
+  out->tris = tris;
+  int64_t non_manifold = 0;
+  if (flags & TMC_OUT_HALFEDGES) {
+    const int64_t nh = 3 * nt;
+    tmc::HeTable t{};
+    t.size = tmc::he_table_size(nh);
+    int32_t *he5 = nullptr, *slot = nullptr, *he4 = nullptr, *hv = nullptr, *hf = nullptr;
+    unsigned long long *hv_key = nullptr, *nm = nullptr;
+    unsigned* ovf = nullptr;
+    TMC_CUDA(ctx, al.get(&t.keys, t.size));
+    TMC_CUDA(ctx, al.get(&t.count, t.size));
+    TMC_CUDA(ctx, al.get(&t.ids, 4 * t.size));
+    TMC_CUDA(ctx, al.get(&he5, 5 * nh));
+    TMC_CUDA(ctx, al.get(&slot, nh));
+    TMC_CUDA(ctx, al.get(&hv_key, nv));
+    TMC_CUDA(ctx, al.get(&nm, 2));
+    TMC_CUDA(ctx, al.get(&ovf, 2));
+    TMC_CUDA(ctx, cudaMemsetAsync(nm, 0, 2 * sizeof(unsigned long long), st));
+    TMC_CUDA(ctx, cudaMemsetAsync(ovf, 0, 2 * sizeof(unsigned), st));
+    TMC_OWN(he4, 4 * nh);
+    TMC_OWN(hv, nv);
+    TMC_OWN(hf, nt);
+    tmc::HeOut ho{he5, hv, hf};
+    tmc::Stage stage(&ctx->prof, "tmc_halfedges", st);
+    ctx->launches += tmc::build_halfedges(tris, 3, nt, nv, ho, t, slot, hv_key, nm, ovf, ctx->sms, st);
+    ctx->launches += tmc::pack_halfedges4(he5, nh, he4, ctx->sms, st);
+    TMC_CUDA(ctx, cudaGetLastError());
+    TMC_CUDA(ctx, cudaMemcpyAsync(h + 8, nm, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    TMC_CUDA(ctx, cudaStreamSynchronize(st));
+    non_manifold = (int64_t)h[8];
+    out->nr_he = nh;
+    out->he = he4;
+    out->he_v = hv;
+    out->he_f = hf;
+  }
+#undef TMC_OWN
+  TMC_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  TMC_CUDA(ctx, cudaStreamSynchronize(st));
+  for (int q = 0; q < 8; q++) out->stats[q] = (int64_t)h[q];
+  ctx->prof.collect();
+  out->stats[4] = non_manifold;
+  out->stats[6] = ncell;
+  return finish_mesh(ctx, flags, out, mp);
 }
-tmc_status tmc_tmc_halfedge(tmc_ctx* ctx, const tmc_volume*, double, uint32_t, tmc_mesh* out) {
-  if (out) mesh_reset(out);
-  return fail(ctx, TMC_ERR_INTERNAL, "TMC extraction is not built yet");
+
+}  // namespace
+
+extern "C" {
+tmc_status tmc_tmc_sharedvertex(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t flags, tmc_mesh* out) {
+  return tmc_extract(ctx, vol, iso, flags, out, false);
+}
+tmc_status tmc_tmc_halfedge(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t flags, tmc_mesh* out) {
+  return tmc_extract(ctx, vol, iso, flags, out, true);
 }
 tmc_status tmc_batch_extract(tmc_ctx* ctx, int32_t, const tmc_request*, tmc_mesh*) {
   return fail(ctx, TMC_ERR_INTERNAL, "batched extraction is not built yet");

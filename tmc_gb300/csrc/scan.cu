@@ -30,3 +30,56 @@ __global__ void scan_tile_sums_kernel(unsigned long long* sums, int64_t ntiles, 
 }
 
 }  // namespace tmc
+
+namespace tmc {
+
+// Generic compaction scan of 0/1 flags (one byte each): out[i] = number of set flags before i.
+__global__ void __launch_bounds__(kScanThreads) flag_tile_sum_kernel(const uint8_t* flags, int64_t n,
+                                                                    unsigned long long* tile_sums) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  unsigned long long s = 0;
+  for (int q = 0; q < kScanItems; q++) {
+    const int64_t i = base + (int64_t)q * kScanThreads + threadIdx.x;
+    if (i < n) s += flags[i] != 0;
+  }
+  unsigned long long tot;
+  block_exclusive_scan<unsigned long long>(s, &tot);
+  if (threadIdx.x == 0) tile_sums[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kScanThreads) flag_offsets_kernel(const uint8_t* flags, int64_t n,
+                                                                   const unsigned long long* tile_off, int32_t* out) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  const int64_t mine = base + (int64_t)threadIdx.x * kScanItems;
+  uint8_t f[kScanItems];
+  unsigned long long s = 0;
+#pragma unroll
+  for (int q = 0; q < kScanItems; q++) {
+    f[q] = (mine + q < n) ? (flags[mine + q] != 0) : 0;
+    s += f[q];
+  }
+  unsigned long long tot;
+  unsigned long long pre = block_exclusive_scan<unsigned long long>(s, &tot) + tile_off[blockIdx.x];
+#pragma unroll
+  for (int q = 0; q < kScanItems; q++) {
+    if (mine + q < n) out[mine + q] = (int32_t)pre;
+    pre += f[q];
+  }
+}
+
+int64_t scan_tiles(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
+
+int scan_flags(const uint8_t* flags, int64_t n, int32_t* out, unsigned long long* tile_sums,
+               unsigned long long* total, cudaStream_t st) {
+  const int64_t tiles = scan_tiles(n);
+  if (tiles == 0) {
+    cudaMemsetAsync(total, 0, sizeof(unsigned long long), st);
+    return 0;
+  }
+  flag_tile_sum_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(flags, n, tile_sums);
+  scan_tile_sums_kernel<<<1, 1024, 0, st>>>(tile_sums, tiles, total);
+  flag_offsets_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(flags, n, tile_sums, out);
+  return 3;
+}
+
+}  // namespace tmc

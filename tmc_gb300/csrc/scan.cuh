@@ -51,4 +51,10 @@ struct Pair {
 // sums holds `ntiles` 64-bit packed pairs; totals[0..1] get the grand totals as 64-bit.
 __global__ void scan_tile_sums_kernel(unsigned long long* sums, int64_t ntiles, unsigned long long* totals);
 
+// Device-wide compaction scan of byte flags; tile_sums needs scan_tiles(n) words.  Returns the
+// number of kernels launched.
+int64_t scan_tiles(int64_t n);
+int scan_flags(const uint8_t* flags, int64_t n, int32_t* out, unsigned long long* tile_sums,
+               unsigned long long* total, cudaStream_t st);
+
 }  // namespace tmc

@@ -1,1 +1,638 @@
+// Topologically correct Marching Cubes (TMC) on the GPU, emitted in the reference's order.
+//
+// Order.  The reference CPU path t_mc (mc/MarchingCubes.cpp:151-317) walks cells in grid order
+// and creates a vertex for a crossed edge the first time a cell touches it (std::map keyed by the
+// global edge), in edge order 0..11, followed by the cell's inner vertices (p_slice,
+// :323-1299); triangles are appended cell by cell.  The first cell touching an edge is the
+// lowest-index cell around it, so each cell "owns" a fixed subset of its edges (those whose lower
+// neighbours across the edge do not exist).  Hence
+//   vertex index   = #vertices of earlier cells + rank among the cell's owned edges (or inner)
+//   triangle index = #triangles of earlier cells + rank in the cell
+// both exclusive prefix sums over cells; a triangle corner on an edge owned by a neighbour reads
+// that neighbour's record.  No hash table, no atomics, deterministic output.
+//
+// Kernels:
+//   tmc_classify_kernel  per-cell record: owned crossed edges, inner vertex and triangle counts
+//                        (ambiguous cells run the full p_slice logic in counting mode)
+//   tmc_offsets_kernel   in-tile scan -> per-cell vertex / triangle offsets
+//   tmc_emit_kernel      vertices (edge and inner) and triangles
+#include "scan.cuh"
 #include "tmc_cells.h"
+
+namespace tmc {
+
+__constant__ uint64_t c_tmc_tris[256] = TMC_TRIANGLES_INIT;
+
+// per-cell record
+//   bits 0-11  owned crossed edges
+//   bits 12-14 inner vertices (0, 1 or 6)
+//   bits 15-20 triangles
+//   bit 21     ambiguous case
+//   bit 22     a singular face the reference cannot triangulate (cell emits no triangle)
+__device__ __forceinline__ uint32_t trec_owned(uint32_t r) { return r & 0xFFF; }
+__device__ __forceinline__ int trec_inner(uint32_t r) { return (r >> 12) & 7; }
+__device__ __forceinline__ int trec_ntri(uint32_t r) { return (r >> 15) & 63; }
+__device__ __forceinline__ int trec_nv(uint32_t r) { return __popc(trec_owned(r)) + trec_inner(r); }
+
+__device__ __forceinline__ void tcell_ijk(const Grid& g, int64_t c, int& i, int& j, int& k) {
+  const int64_t cx = g.nx - 1, cy = g.ny - 1;
+  i = (int)(c % cx);
+  const int64_t r = c / cx;
+  j = (int)(r % cy);
+  k = (int)(r / cy);
+}
+
+__device__ __forceinline__ void tload_corners(const Grid& g, int i, int j, int k, float u[8]) {
+  const float* p = g.f + ((int64_t)k * g.ny + j) * g.nx + i;
+  const int64_t sy = g.nx, sz = (int64_t)g.nx * g.ny;
+  u[0] = __ldg(p);
+  u[1] = __ldg(p + 1);
+  u[2] = __ldg(p + sy);
+  u[3] = __ldg(p + sy + 1);
+  u[4] = __ldg(p + sz);
+  u[5] = __ldg(p + sz + 1);
+  u[6] = __ldg(p + sz + sy);
+  u[7] = __ldg(p + sz + sy + 1);
+}
+
+// Edges a cell creates first: across the edge, along each other axis, the cell either sits on the
+// far side of the edge (offset 1) or no lower neighbour exists (index 0).
+__device__ __forceinline__ uint32_t owned_edges(int i, int j, int k) {
+  uint32_t m = 0;
+#pragma unroll
+  for (int e = 0; e < 12; e++) {
+    const int off = edge_off(e), ax = edge_axis(e);
+    bool own = true;
+    if (ax != 0) own = own && (((off >> 0) & 1) || i == 0);
+    if (ax != 1) own = own && (((off >> 1) & 1) || j == 0);
+    if (ax != 2) own = own && (((off >> 2) & 1) || k == 0);
+    m |= (uint32_t)own << e;
+  }
+  return m;
+}
+
+// Owner cell of local edge e of cell (i,j,k) and the edge's local index there.
+__device__ __forceinline__ void edge_owner(int i, int j, int k, int e, int& oi, int& oj, int& ok, int& oe) {
+  const int off = edge_off(e), ax = edge_axis(e);
+  const int gi = i + (off & 1), gj = j + ((off >> 1) & 1), gk = k + ((off >> 2) & 1);
+  oi = (ax == 0) ? gi : (gi > 0 ? gi - 1 : 0);
+  oj = (ax == 1) ? gj : (gj > 0 ? gj - 1 : 0);
+  ok = (ax == 2) ? gk : (gk > 0 ? gk - 1 : 0);
+  const int o = (gi - oi) | ((gj - oj) << 1) | ((gk - ok) << 2);  // offset of the edge in the owner
+  // local edge with that offset and axis
+#pragma unroll
+  for (int q = 0; q < 12; q++)
+    if (edge_axis(q) == ax && edge_off(q) == o) oe = q;
+}
+
+// ------------------------------------------------------------------------------------------
+// cell geometry in float64 for the ambiguous path
+// ------------------------------------------------------------------------------------------
+// UGrid::gradient (mc/MarchingCubes.cpp:1451-1509): one-sided differences on the border
+__device__ __forceinline__ void tmc_point_gradient(const Grid& g, int i, int j, int k, double out[3]) {
+  if (i == 0) out[0] = ((double)g.at(i + 1, j, k) - (double)g.at(i, j, k)) / g.dx;
+  else if (i == g.nx - 1) out[0] = ((double)g.at(i, j, k) - (double)g.at(i - 1, j, k)) / g.dx;
+  else out[0] = ((double)g.at(i + 1, j, k) - (double)g.at(i - 1, j, k)) / (2 * g.dx);
+  if (j == 0) out[1] = ((double)g.at(i, j + 1, k) - (double)g.at(i, j, k)) / g.dy;
+  else if (j == g.ny - 1) out[1] = ((double)g.at(i, j, k) - (double)g.at(i, j - 1, k)) / g.dy;
+  else out[1] = ((double)g.at(i, j + 1, k) - (double)g.at(i, j - 1, k)) / (2 * g.dy);
+  if (k == 0) out[2] = ((double)g.at(i, j, k + 1) - (double)g.at(i, j, k)) / g.dz;
+  else if (k == g.nz - 1) out[2] = ((double)g.at(i, j, k) - (double)g.at(i, j, k - 1)) / g.dz;
+  else out[2] = ((double)g.at(i, j, k + 1) - (double)g.at(i, j, k - 1)) / (2 * g.dz);
+}
+
+__device__ __forceinline__ void cell_trilinear3(const double q[8][3], double u, double v, double w, double out[3]) {
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+    out[d] = (1 - w) * ((1 - v) * (q[0][d] + u * (q[1][d] - q[0][d])) + v * (q[2][d] + u * (q[3][d] - q[2][d]))) +
+             w * ((1 - v) * (q[4][d] + u * (q[5][d] - q[4][d])) + v * (q[6][d] + u * (q[7][d] - q[6][d])));
+}
+
+// e_vert (mc/MarchingCubes.cpp:902-911): local coordinate d of the point on edge e
+__device__ __forceinline__ double e_vert(const double ecoord[12], int e, int d) {
+  return (edge_axis(e) == d) ? ecoord[e] : (double)((edge_off(e) >> d) & 1);
+}
+
+struct TriSink {
+  int32_t* out;  // 3 per triangle, NULL when counting
+  int n;
+  __device__ __forceinline__ void put(int a, int b, int c) {
+    if (out) {
+      out[3 * n] = a;
+      out[3 * n + 1] = b;
+      out[3 * n + 2] = c;
+    }
+    n++;
+  }
+};
+
+struct AmbResult {
+  int inner;     // inner vertices created
+  bool error;    // singular face without a valid triangulation
+};
+
+// p_slice after the edge vertices (mc/MarchingCubes.cpp:418-1296), float64 throughout.
+// vid[e]: global index of the vertex on crossed edge e; ibase: index of the first inner vertex.
+// When `geo` is set, inner vertices are written there (positions/normals).
+struct InnerOut {
+  float* v;
+  float* n;
+  double* v64;
+};
+
+__device__ AmbResult p_slice_dev(unsigned ic, const double F[8], double iso, const double ecoord[12],
+                                 const int32_t vid[12], int32_t ibase, TriSink& tri, const double (*P)[3],
+                                 const double (*N)[3], const InnerOut* geo) {
+  AmbResult res{0, false};
+  uint64_t to = ~0ull;
+  int f_flag = 0;
+#pragma unroll 1
+  for (int f = 0; f < 6; f++) {
+    const uint32_t fv = face_v_pack(f), fe = face_e_pack(f);
+    const double f0 = F[nib(fv, 0)], f1 = F[nib(fv, 1)], f2 = F[nib(fv, 2)], f3 = F[nib(fv, 3)];
+    int fc = 0;
+    if (f0 >= iso) fc |= 1;
+    if (f1 >= iso) fc |= 2;
+    if (f2 >= iso) fc |= 4;
+    if (f3 >= iso) fc |= 8;
+    int sep = 0;
+    if (fc == 6 || fc == 9) {
+      const double val = decider(f0, f1, f2, f3);
+      if (val > iso) sep = 1;
+      else if (val < iso) sep = 0;
+      else {
+        f_flag |= 1 << f;
+        const unsigned e_flag = 0x218;
+        double ec0 = ecoord[nib(fe, 0)], ec1 = ecoord[nib(fe, 1)], ec2 = ecoord[nib(fe, 2)], ec3 = ecoord[nib(fe, 3)];
+        if ((e_flag >> (f * 2)) & 1) { ec0 = 1 - ec0; ec2 = 1 - ec2; }
+        if ((e_flag >> (f * 2)) & 2) { ec1 = 1 - ec1; ec3 = 1 - ec3; }
+        const bool c1 = (ec1 < ec3 && ec0 > ec2), c2 = (ec1 > ec3 && ec0 < ec2);
+        if (!c1 && !c2) {
+          res.error = true;
+          return res;
+        }
+        sep = (fc == 6) ? (c1 ? 0 : 1) : (c1 ? 1 : 0);
+      }
+    }
+    face_segments(fc, sep, fe, to);
+  }
+  const uint64_t c = connect_contours(to, case_edge_mask(ic));
+  const int cnt = cnt_count(c);
+
+  // inner-ambiguity quadratic (:715-795)
+  double ui[2] = {0, 0}, vi[2] = {0, 0}, wi[2] = {0, 0};
+  unsigned q_sol = 0;
+  const double a = (F[0] - F[1]) * (-F[6] + F[7] + F[4] - F[5]) - (F[4] - F[5]) * (-F[2] + F[3] + F[0] - F[1]);
+  const double b = (iso - F[0]) * (-F[6] + F[7] + F[4] - F[5]) + (F[0] - F[1]) * (F[6] - F[4]) -
+                   (iso - F[4]) * (-F[2] + F[3] + F[0] - F[1]) - (F[4] - F[5]) * (F[2] - F[0]);
+  const double cc = (iso - F[0]) * (F[6] - F[4]) - (iso - F[4]) * (F[2] - F[0]);
+  double d = b * b - 4 * a * cc;
+  if (d > 0) {
+    d = sqrt(d);
+    ui[0] = (-b - d) / (2 * a);
+    ui[1] = (-b + d) / (2 * a);
+    double g1 = F[0] * (1 - ui[0]) + F[1] * ui[0];
+    double g2 = F[2] * (1 - ui[0]) + F[3] * ui[0];
+    vi[0] = (iso - g1) / (g2 - g1);
+    if (isnan(vi[0]) || isinf(vi[0])) vi[0] = -1.f;
+    g1 = F[0] * (1 - ui[1]) + F[1] * ui[1];
+    g2 = F[2] * (1 - ui[1]) + F[3] * ui[1];
+    vi[1] = (iso - g1) / (g2 - g1);
+    if (isnan(vi[1]) || isinf(vi[1])) vi[1] = -1.f;
+    g1 = F[0] * (1 - ui[0]) + F[1] * ui[0];
+    g2 = F[4] * (1 - ui[0]) + F[5] * ui[0];
+    wi[0] = (iso - g1) / (g2 - g1);
+    if (isnan(wi[0]) || isinf(wi[0])) wi[0] = -1.f;
+    g1 = F[0] * (1 - ui[1]) + F[1] * ui[1];
+    g2 = F[4] * (1 - ui[1]) + F[5] * ui[1];
+    wi[1] = (iso - g1) / (g2 - g1);
+    if (isnan(wi[1]) || isinf(wi[1])) wi[1] = -1.f;
+    if (f_flag & 1) { if (wi[0] < wi[1]) wi[0] = 0; else wi[1] = 0; }
+    if (f_flag & 2) { if (wi[0] > wi[1]) wi[1] = 1; else wi[1] = 1; }
+    if (f_flag & 4) { if (vi[0] < vi[1]) vi[0] = 0; else vi[1] = 0; }
+    if (f_flag & 8) { if (vi[0] > vi[1]) vi[0] = 1; else vi[1] = 1; }
+    if (f_flag & 16) { if (ui[0] < ui[1]) ui[0] = 0; else ui[1] = 0; }
+    if (f_flag & 32) { if (ui[0] > ui[1]) ui[0] = 1; else ui[1] = 1; }
+    if (0 < ui[0] && ui[0] < 1) q_sol |= 1;
+    if (0 < ui[1] && ui[1] < 1) q_sol |= 2;
+    if (0 < vi[0] && vi[0] < 1) q_sol |= 4;
+    if (0 < vi[1] && vi[1] < 1) q_sol |= 8;
+    if (0 < wi[0] && wi[0] < 1) q_sol |= 16;
+    if (0 < wi[1] && wi[1] < 1) q_sol |= 32;
+  }
+
+  if (__popc(q_sol) == 6) {
+    // tunnel or 12-vertex contour: inner hexagon (:831-1083)
+    const double hvt[6][3] = {{ui[0], vi[0], wi[0]}, {ui[0], vi[0], wi[1]}, {ui[1], vi[0], wi[1]},
+                              {ui[1], vi[1], wi[1]}, {ui[1], vi[1], wi[0]}, {ui[0], vi[1], wi[0]}};
+    int not_tunnel = 0xF;
+    if (cnt == 3) {
+      const double uc_min = (ui[0] < ui[1]) ? ui[0] : ui[1];
+      const double uc_max = (ui[0] < ui[1]) ? ui[1] : ui[0];
+      int flat = 0;
+      for (int t = 0; t < cnt; t++) {
+        const int sz = cnt_size(c, t);
+        if (sz == 3) {
+          double umin = 2, umax = -2;
+          const int e0 = cnt_edge(c, flat), e1 = cnt_edge(c, flat + 1), e2 = cnt_edge(c, flat + 2);
+          const double u_e0 = e_vert(ecoord, e0, 0), u_e1 = e_vert(ecoord, e1, 0), u_e2 = e_vert(ecoord, e2, 0);
+          umin = (u_e0 < umin) ? u_e0 : umin;
+          umin = (u_e1 < umin) ? u_e1 : umin;
+          umin = (u_e2 < umin) ? u_e2 : umin;
+          umax = (u_e0 > umax) ? u_e0 : umax;
+          umax = (u_e1 > umax) ? u_e1 : umax;
+          umax = (u_e2 > umax) ? u_e1 : umax;  // the reference keeps u_e1 here
+          if (uc_min > umax || uc_max < umin) {
+            not_tunnel = t;
+            tri.put(vid[e0], vid[e1], vid[e2]);
+          }
+        }
+        flat += sz;
+      }
+    }
+    if (geo) {
+      for (int s = 0; s < 6; s++) {
+        double hp[3], hn[3];
+        cell_trilinear3(P, hvt[s][0], hvt[s][1], hvt[s][2], hp);
+        cell_trilinear3(N, hvt[s][0], hvt[s][1], hvt[s][2], hn);
+        const double factor = sqrt(hn[0] * hn[0] + hn[1] * hn[1] + hn[2] * hn[2]);
+        const int64_t o = 3 * (int64_t)(ibase + s);
+        for (int q = 0; q < 3; q++) {
+          geo->v[o + q] = (float)hp[q];
+          geo->n[o + q] = (float)(hn[q] / factor);
+          if (geo->v64) geo->v64[o + q] = hp[q];
+        }
+      }
+    }
+    res.inner = 6;
+    unsigned char tcon[12];
+    int flat = 0;
+    for (int t = 0; t < cnt; t++) {
+      const int sz = cnt_size(c, t);
+      if (not_tunnel != t) {
+        for (int r = 0; r < sz; r++) {
+          unsigned idx = (unsigned)-1;
+          double dist = 1000.;
+          const int ci = cnt_edge(c, flat + r);
+          const double ue = e_vert(ecoord, ci, 0), ve = e_vert(ecoord, ci, 1), we = e_vert(ecoord, ci, 2);
+          for (int s = 0; s < 6; s++) {
+            const double uval = ue - hvt[s][0], vval = ve - hvt[s][1], wval = we - hvt[s][2];
+            const double val = uval * uval + vval * vval + wval * wval;
+            if (dist > val) {
+              idx = (unsigned)s;
+              dist = val;
+            }
+          }
+          tcon[ci] = (unsigned char)idx;
+        }
+        for (int r = 0; r < sz; r++) {
+          const int tid1 = cnt_edge(c, flat + r), tid2 = cnt_edge(c, flat + (r + 1) % sz);
+          const int cid1 = tcon[tid1], cid2 = tcon[tid2];
+          const int rr = (cid1 - cid2) < 0 ? cid2 - cid1 : cid1 - cid2;
+          const int dst = rr > 2 ? 6 - rr : rr;
+          if (dst == 0) {
+            tri.put(vid[tid1], vid[tid2], ibase + cid1);
+          } else if (dst == 1) {
+            double l1 = 0, l2 = 0;
+            {
+              const double a0 = e_vert(ecoord, tid1, 0) - hvt[cid2][0], a1 = e_vert(ecoord, tid1, 1) - hvt[cid2][1],
+                           a2 = e_vert(ecoord, tid1, 2) - hvt[cid2][2];
+              l1 = a0 * a0 + a1 * a1 + a2 * a2;
+              const double b0 = e_vert(ecoord, tid2, 0) - hvt[cid1][0], b1 = e_vert(ecoord, tid2, 1) - hvt[cid1][1],
+                           b2 = e_vert(ecoord, tid2, 2) - hvt[cid1][2];
+              l2 = b0 * b0 + b1 * b1 + b2 * b2;
+            }
+            if (l1 < l2) {
+              tri.put(vid[tid1], vid[tid2], ibase + cid2);
+              tri.put(vid[tid1], ibase + cid2, ibase + cid1);
+            } else {
+              tri.put(vid[tid1], vid[tid2], ibase + cid1);
+              tri.put(vid[tid2], ibase + cid2, ibase + cid1);
+            }
+          } else if (dst == 2) {
+            const int dmax = (cid1 > cid2) ? cid1 : cid2, dmin = (cid1 < cid2) ? cid1 : cid2;
+            const int cidm = ((dmax + 2) % 6 == dmin) ? (dmax + 1) % 6 : (dmax + dmin) / 2;
+            tri.put(vid[tid1], vid[tid2], ibase + cidm);
+            tri.put(vid[tid1], ibase + cidm, ibase + cid1);
+            tri.put(vid[tid2], ibase + cid2, ibase + cidm);
+          }
+        }
+      }
+      flat += sz;
+    }
+    if (cnt == 1) {
+      const bool s_ = decider(F[0], F[1], F[2], F[3]) <= iso;
+      const bool of_ = (wi[1] < wi[0]) ? s_ : !s_;
+      const int t0 = ibase, t1 = ibase + 1, t2 = ibase + 2, t3 = ibase + 3, t4 = ibase + 4, t5 = ibase + 5;
+      if (!of_) {
+        tri.put(t0, t2, t1); tri.put(t2, t4, t3); tri.put(t0, t5, t4); tri.put(t0, t4, t2);
+      } else {
+        tri.put(t0, t1, t2); tri.put(t2, t3, t4); tri.put(t0, t4, t5); tri.put(t0, t2, t4);
+      }
+    }
+    return res;
+  }
+  // no tunnel
+  const unsigned nr_u = ((q_sol & 0x5) == 0x5) + ((q_sol & 0xA) == 0xA);
+  const unsigned nr_v = ((q_sol & 0x11) == 0x11) + ((q_sol & 0x22) == 0x22);
+  const unsigned nr_w = ((q_sol & 0x18) == 0x18) + ((q_sol & 0x24) == 0x24);
+  const unsigned nr_t = nr_u + nr_v + nr_w;
+  if (nr_t == nr_u || nr_t == nr_v || nr_t == nr_w) {
+    int flat = 0;
+    for (int t = 0; t < cnt; t++) {
+      const int sz = cnt_size(c, t);
+      int e[6];
+      for (int q = 0; q < 6; q++) e[q] = (q < sz) ? vid[cnt_edge(c, flat + q)] : -1;
+      switch (sz) {
+        case 3: tri.put(e[0], e[1], e[2]); break;
+        case 4: tri.put(e[0], e[1], e[2]); tri.put(e[0], e[2], e[3]); break;
+        case 5: tri.put(e[0], e[1], e[2]); tri.put(e[0], e[2], e[3]); tri.put(e[0], e[3], e[4]); break;
+        case 6:
+          tri.put(e[0], e[1], e[3]); tri.put(e[1], e[2], e[3]); tri.put(e[0], e[3], e[4]); tri.put(e[0], e[4], e[5]);
+          break;
+        default: break;
+      }
+      flat += sz;
+    }
+    return res;
+  }
+  // saddle points: one inner vertex (:1178-1296)
+  const unsigned fs00 = q_sol & 1, fs01 = (q_sol >> 1) & 1, fs10 = (q_sol >> 2) & 1, fs11 = (q_sol >> 3) & 1,
+                 fs20 = (q_sol >> 4) & 1, fs21 = (q_sol >> 5) & 1;
+  const unsigned fc1 = fs00 * fs10 + fs01 * fs11;
+  const unsigned fc2 = fs00 * fs20 + fs01 * fs21;
+  const unsigned fc3 = fs10 * fs21 + fs11 * fs20;
+  const unsigned c_faces = fc1 + fc2 + fc3;
+  double uc = 0, vc = 0, wc = 0;
+  if (c_faces == 2) {
+    if (fc1 == 0) {
+      uc = fs00 * ui[0] + fs01 * ui[1]; vc = fs10 * vi[0] + fs11 * vi[1]; wc = fs10 * wi[1] + fs11 * wi[0];
+    } else if (fc2 == 0) {
+      uc = fs00 * ui[0] + fs01 * ui[1]; vc = fs00 * vi[0] + fs01 * vi[1]; wc = fs00 * wi[1] + fs01 * wi[0];
+    } else if (fc3 == 0) {
+      uc = fs10 * ui[0] + fs11 * ui[1]; vc = fs10 * vi[0] + fs11 * vi[1]; wc = fs10 * wi[0] + fs11 * wi[1];
+    }
+  } else if (c_faces == 3) {
+    uc = (fs00 * ui[0] + fs01 * ui[1]) / (int)(fs00 + fs01);
+    vc = (fs10 * vi[0] + fs11 * vi[1]) / (int)(fs10 + fs11);
+    wc = (fs20 * wi[0] + fs21 * wi[1]) / (int)(fs20 + fs21);
+  } else if (c_faces == 4) {
+    const unsigned nu = fs00 + fs01, nv = fs10 + fs11, nw = fs20 + fs21;
+    if (nw == 1) {
+      uc = fs20 * ui[0] + fs21 * ui[1]; vc = fs21 * vi[0] + fs20 * vi[1]; wc = fs20 * wi[0] + fs21 * wi[1];
+    } else if (nv == 1) {
+      uc = fs10 * ui[0] + fs11 * ui[1]; vc = fs10 * vi[0] + fs11 * vi[1]; wc = fs11 * wi[0] + fs10 * wi[1];
+    } else if (nu == 1) {
+      uc = fs00 * ui[0] + fs01 * ui[1]; vc = fs00 * vi[0] + fs01 * vi[1]; wc = fs00 * wi[0] + fs01 * wi[1];
+    }
+  }
+  bool pt_used = false;
+  int flat = 0;
+  for (int t = 0; t < cnt; t++) {
+    const int sz = cnt_size(c, t);
+    if (sz == 3) {
+      tri.put(vid[cnt_edge(c, flat)], vid[cnt_edge(c, flat + 1)], vid[cnt_edge(c, flat + 2)]);
+    } else {
+      pt_used = true;
+      for (int r = 0; r < sz; r++) tri.put(vid[cnt_edge(c, flat + r)], vid[cnt_edge(c, flat + (r + 1) % sz)], ibase);
+    }
+    flat += sz;
+  }
+  if (pt_used) {
+    res.inner = 1;
+    if (geo) {
+      double ip[3], in[3];
+      cell_trilinear3(P, uc, vc, wc, ip);
+      cell_trilinear3(N, uc, vc, wc, in);
+      const double factor = sqrt(in[0] * in[0] + in[1] * in[1] + in[2] * in[2]);
+      const int64_t o = 3 * (int64_t)ibase;
+      for (int q = 0; q < 3; q++) {
+        geo->v[o + q] = (float)ip[q];
+        geo->n[o + q] = (float)(in[q] / factor);
+        if (geo->v64) geo->v64[o + q] = ip[q];
+      }
+    }
+  }
+  return res;
+}
+
+// corner data of an ambiguous cell in float64: values, positions, normals, edge parameters
+struct AmbCell {
+  double F[8];
+  double P[8][3];
+  double N[8][3];
+  double ec[12];
+};
+
+__device__ void load_amb_cell(const Grid& g, int i, int j, int k, const float u[8], uint32_t emask, AmbCell& a,
+                              bool geometry) {
+#pragma unroll
+  for (int q = 0; q < 8; q++) a.F[q] = u[q];
+  for (int e = 0; e < 12; e++) {
+    a.ec[e] = 0;
+    if (emask & (1u << e)) {
+      const int v0 = edge_v0(e), v1 = edge_v1(e);
+      a.ec[e] = (g.iso - a.F[v0]) / (a.F[v1] - a.F[v0]);
+    }
+  }
+  if (geometry) {
+    for (int q = 0; q < 8; q++) {
+      const int ii = i + (q & 1), jj = j + ((q >> 1) & 1), kk = k + ((q >> 2) & 1);
+      a.P[q][0] = g.ox + ii * g.dx;
+      a.P[q][1] = g.oy + jj * g.dy;
+      a.P[q][2] = g.oz + kk * g.dz;
+      tmc_point_gradient(g, ii, jj, kk, a.N[q]);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// kernels
+// ------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kScanThreads) tmc_classify_kernel(Grid g, uint32_t* rec,
+                                                                   unsigned long long* tile_sums,
+                                                                   unsigned long long* stats) {
+  const int64_t n = g.ncells();
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  unsigned long long local = 0, act = 0, amb = 0, sing = 0;
+  for (int s = 0; s < kScanItems; s++) {
+    const int64_t c = base + (int64_t)s * kScanThreads + threadIdx.x;
+    if (c >= n) break;
+    int i, j, k;
+    tcell_ijk(g, c, i, j, k);
+    float u[8];
+    tload_corners(g, i, j, k, u);
+    unsigned cs = 0;
+#pragma unroll
+    for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
+    uint32_t r = 0;
+    if (cs != 0 && cs != 255) {
+      const uint32_t em = case_edge_mask(cs);
+      r = em & owned_edges(i, j, k);
+      if (!case_ambiguous(cs)) {
+        r |= (uint32_t)(c_tmc_tris[cs] & 0xF) << 15;
+      } else {
+        AmbCell a;
+        load_amb_cell(g, i, j, k, u, em, a, false);
+        int32_t vid[12];
+        for (int e = 0; e < 12; e++) vid[e] = 0;
+        TriSink ts{nullptr, 0};
+        const AmbResult ar = p_slice_dev(cs, a.F, g.iso, a.ec, vid, 0, ts, a.P, a.N, nullptr);
+        r |= (uint32_t)ar.inner << 12 | (uint32_t)ts.n << 15 | (1u << 21) | (ar.error ? (1u << 22) : 0u);
+        amb++;
+        sing += ar.error;
+      }
+      act++;
+    }
+    rec[c] = r;
+    local += ((unsigned long long)trec_nv(r) << 32) | (unsigned long long)trec_ntri(r);
+  }
+  unsigned long long tot;
+  block_exclusive_scan<unsigned long long>(local, &tot);
+  if (threadIdx.x == 0) tile_sums[blockIdx.x] = tot;
+  for (int o = 16; o; o >>= 1) {
+    act += __shfl_down_sync(0xffffffffu, act, o);
+    amb += __shfl_down_sync(0xffffffffu, amb, o);
+    sing += __shfl_down_sync(0xffffffffu, sing, o);
+  }
+  if ((threadIdx.x & 31) == 0 && (act | amb | sing)) {
+    atomicAdd(stats + 0, act);
+    atomicAdd(stats + 1, amb);
+    atomicAdd(stats + 5, sing);
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) tmc_offsets_kernel(int64_t n, const uint32_t* rec,
+                                                                  const unsigned long long* tile_off,
+                                                                  int32_t* voff, int32_t* toff) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  uint32_t r[kScanItems];
+  unsigned long long local = 0;
+  const int64_t mine = base + (int64_t)threadIdx.x * kScanItems;
+#pragma unroll
+  for (int s = 0; s < kScanItems; s++) {
+    r[s] = (mine + s < n) ? rec[mine + s] : 0u;
+    local += ((unsigned long long)trec_nv(r[s]) << 32) | (unsigned long long)trec_ntri(r[s]);
+  }
+  unsigned long long tot;
+  unsigned long long pre = block_exclusive_scan<unsigned long long>(local, &tot) + tile_off[blockIdx.x];
+#pragma unroll
+  for (int s = 0; s < kScanItems; s++) {
+    if (mine + s < n) {
+      voff[mine + s] = (int32_t)(pre >> 32);
+      toff[mine + s] = (int32_t)(pre & 0xffffffffull);
+    }
+    pre += ((unsigned long long)trec_nv(r[s]) << 32) | (unsigned long long)trec_ntri(r[s]);
+  }
+}
+
+// edge vertex: interpolation as t_mc (mc/MarchingCubes.cpp:241-254), float64
+__device__ __forceinline__ void edge_vertex_f64(const Grid& g, int i, int j, int k, int e, const float u[8],
+                                                const TmcVertexOut& out, int32_t idx) {
+  const int v0 = edge_v0(e), v1 = edge_v1(e);
+  const double F0 = u[v0], F1 = u[v1];
+  const double l = (g.iso - F0) / (F1 - F0);
+  const int i0 = i + (v0 & 1), j0 = j + ((v0 >> 1) & 1), k0 = k + ((v0 >> 2) & 1);
+  const int i1 = i + (v1 & 1), j1 = j + ((v1 >> 1) & 1), k1 = k + ((v1 >> 2) & 1);
+  const double p0[3] = {g.ox + i0 * g.dx, g.oy + j0 * g.dy, g.oz + k0 * g.dz};
+  const double p1[3] = {g.ox + i1 * g.dx, g.oy + j1 * g.dy, g.oz + k1 * g.dz};
+  double n0[3], n1[3];
+  tmc_point_gradient(g, i0, j0, k0, n0);
+  tmc_point_gradient(g, i1, j1, k1, n1);
+  double ip[3], in[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) ip[d] = (1 - l) * p0[d] + l * p1[d];
+#pragma unroll
+  for (int d = 0; d < 3; d++) in[d] = (1 - l) * n0[d] + l * n1[d];
+  const double nl = sqrt(in[0] * in[0] + in[1] * in[1] + in[2] * in[2]);
+  const int64_t o = 3 * (int64_t)idx;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    out.v[o + d] = (float)ip[d];
+    out.n[o + d] = (float)(in[d] / nl);
+    if (out.v64) out.v64[o + d] = ip[d];
+  }
+}
+
+__global__ void __launch_bounds__(128) tmc_emit_kernel(Grid g, const uint32_t* rec, const int32_t* voff,
+                                                       const int32_t* toff, TmcVertexOut out, int32_t* tris) {
+  const int64_t n = g.ncells();
+  for (int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; cell < n;
+       cell += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t r = rec[cell];
+    if (r == 0) continue;
+    int i, j, k;
+    tcell_ijk(g, cell, i, j, k);
+    float u[8];
+    tload_corners(g, i, j, k, u);
+    unsigned cs = 0;
+#pragma unroll
+    for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
+    const uint32_t em = case_edge_mask(cs);
+    const uint32_t own = trec_owned(r);
+    const int32_t vbase = voff[cell];
+    // owned edge vertices, in edge order
+    int32_t vid[12];
+    int rank = 0;
+    for (int e = 0; e < 12; e++) {
+      vid[e] = -1;
+      if (!(em & (1u << e))) continue;
+      if (own & (1u << e)) {
+        vid[e] = vbase + rank;
+        edge_vertex_f64(g, i, j, k, e, u, out, vid[e]);
+        rank++;
+      } else {
+        int oi, oj, ok, oe = 0;
+        edge_owner(i, j, k, e, oi, oj, ok, oe);
+        const int64_t oc = g.cell_index(oi, oj, ok);
+        const uint32_t orec = rec[oc];
+        vid[e] = voff[oc] + __popc(trec_owned(orec) & ((1u << oe) - 1u));
+      }
+    }
+    TriSink ts{tris + 3 * (int64_t)toff[cell], 0};
+    if (!((r >> 21) & 1)) {
+      // unambiguous: table triangles with reversed winding (t_mc, mc/MarchingCubes.cpp:276-294)
+      const uint64_t tw = c_tmc_tris[cs];
+      const int nt = (int)(tw & 0xF);
+      for (int t = 0; t < nt; t++) {
+        const int e0 = (int)((tw >> (4 + 12 * t)) & 0xF), e1 = (int)((tw >> (8 + 12 * t)) & 0xF),
+                  e2 = (int)((tw >> (12 + 12 * t)) & 0xF);
+        ts.put(vid[e2], vid[e1], vid[e0]);
+      }
+    } else if (!((r >> 22) & 1)) {
+      AmbCell a;
+      load_amb_cell(g, i, j, k, u, em, a, true);
+      InnerOut io{out.v, out.n, out.v64};
+      p_slice_dev(cs, a.F, g.iso, a.ec, vid, vbase + rank, ts, a.P, a.N, &io);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// host-side launches
+// ------------------------------------------------------------------------------------------
+int64_t tmc_tiles(const Grid& g) { return ceil_div(g.ncells(), kScanTile); }
+
+int tmc_count(const Grid& g, TmcScratch& s, cudaStream_t st, Prof* prof) {
+  const int64_t n = g.ncells();
+  const int64_t tiles = tmc_tiles(g);
+  {
+    Stage t(prof, "tmc_classify", st);
+    tmc_classify_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(g, s.rec, s.tile_sums, s.stats);
+  }
+  Stage t(prof, "tmc_scan", st);
+  scan_tile_sums_kernel<<<1, 1024, 0, st>>>(s.tile_sums, tiles, s.totals);
+  tmc_offsets_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(n, s.rec, s.tile_sums, s.voff, s.toff);
+  return 3;
+}
+
+int tmc_emit(const Grid& g, TmcScratch& s, TmcVertexOut vo, int32_t* tris, int sms, cudaStream_t st,
+             Prof* prof) {
+  Stage t(prof, "tmc_emit", st);
+  const int64_t n = g.ncells();
+  const int64_t blocks = std::min<int64_t>(ceil_div(n, 128), (int64_t)sms * 16);
+  tmc_emit_kernel<<<(unsigned)blocks, 128, 0, st>>>(g, s.rec, s.voff, s.toff, vo, tris);
+  return 1;
+}
+
+}  // namespace tmc

@@ -4,3 +4,28 @@
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "profiler.h"
+
+namespace tmc {
+
+struct TmcVertexOut {
+  float* v;
+  float* n;
+  double* v64;  // optional
+};
+
+struct TmcScratch {
+  uint32_t* rec;
+  int32_t* voff;
+  int32_t* toff;
+  unsigned long long* tile_sums;
+  unsigned long long* totals;
+  unsigned long long* stats;
+};
+
+int64_t tmc_tiles(const Grid& g);
+int tmc_count(const Grid& g, TmcScratch& s, cudaStream_t st, Prof* prof = nullptr);
+int tmc_emit(const Grid& g, TmcScratch& s, TmcVertexOut vo, int32_t* tris, int sms, cudaStream_t st,
+             Prof* prof = nullptr);
+
+}  // namespace tmc

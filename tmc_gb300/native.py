@@ -33,7 +33,7 @@ ALGO_TMC = 1
 
 # every symbol include/tmc_gb300.h declares
 EXPORTS = ["tmc_ctx_create", "tmc_ctx_destroy", "tmc_last_error", "tmc_ctx_stream", "tmc_ctx_synchronize",
-           "tmc_ctx_launch_count", "tmc_dmc_extract", "tmc_tmc_sharedvertex", "tmc_tmc_halfedge",
+           "tmc_ctx_launch_count", "tmc_ctx_set_profiling", "tmc_ctx_profile_read", "tmc_dmc_extract", "tmc_tmc_sharedvertex", "tmc_tmc_halfedge",
            "tmc_mesh_free", "tmc_batch_extract"]
 
 
@@ -90,6 +90,10 @@ def load(path: str = LIB_PATH):
             f = getattr(lib, name)
             f.argtypes = [ctypes.c_void_p, ctypes.POINTER(Volume), ctypes.c_double, ctypes.c_uint32, ctypes.POINTER(Mesh)]
     lib.tmc_mesh_free.argtypes = [ctypes.c_void_p, ctypes.POINTER(Mesh)]
+    lib.tmc_ctx_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.tmc_ctx_profile_read.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_char_p,
+                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]
+    lib.tmc_ctx_profile_read.restype = ctypes.c_int32
     if hasattr(lib, "tmc_batch_extract"):
         lib.tmc_batch_extract.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(Request), ctypes.POINTER(Mesh)]
     _lib = lib
@@ -150,6 +154,22 @@ class Context:
 
     def launches(self) -> int:
         return self.lib.tmc_ctx_launch_count(self.h)
+
+    def set_profiling(self, on: bool):
+        self._check(self.lib.tmc_ctx_set_profiling(self.h, 1 if on else 0))
+
+    def profile(self) -> dict:
+        """{stage: (total_ms, count)} accumulated since profiling was enabled."""
+        n = 64
+        names = ctypes.create_string_buffer(32 * n)
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_int64 * n)()
+        k = self.lib.tmc_ctx_profile_read(self.h, n, names, ms, cnt)
+        out = {}
+        for i in range(max(k, 0)):
+            nm = names.raw[32 * i: 32 * i + 32].split(b"\0")[0].decode()
+            out[nm] = (ms[i], cnt[i])
+        return out
 
     def synchronize(self):
         self._check(self.lib.tmc_ctx_synchronize(self.h))
