@@ -213,10 +213,14 @@ __global__ void invert_flags_kernel(const uint8_t* in, int64_t n, uint8_t* out) 
 // new index, which becomes their map entry
 __global__ void gather_vertices_kernel(const uint8_t* keep, const int32_t* idx, int64_t nv, const double* v64,
                                        const float* v, const float* n, double* v64o, float* vo, float* no,
-                                       int32_t* map) {
+                                       int32_t* map, int64_t cap, unsigned* overflow) {
   FOR_EACH(i, nv) {
     if (!keep[i]) continue;
     const int64_t o = idx[i];
+    if (o < 0 || o >= cap) {
+      atomicAdd(overflow, 1u);
+      continue;
+    }
     for (int d = 0; d < 3; d++) {
       v64o[3 * o + d] = v64[3 * i + d];
       vo[3 * o + d] = v[3 * i + d];
@@ -228,10 +232,15 @@ __global__ void gather_vertices_kernel(const uint8_t* keep, const int32_t* idx, 
 
 // removeQuadrilaterals3X3Y (:1114-1137)
 __global__ void gather_quads_3x3y_kernel(const uint8_t* em, const int32_t* idx, int64_t nq, const int32_t* q,
-                                         const uint8_t* vm_first, const int32_t* vm_second, int32_t* qo) {
+                                         const uint8_t* vm_first, const int32_t* vm_second, int32_t* qo, int64_t cap,
+                                         unsigned* overflow) {
   FOR_EACH(f, nq) {
     if (em[f]) continue;
     const int64_t o = idx[f];
+    if (o < 0 || o >= cap) {
+      atomicAdd(overflow, 1u);
+      continue;
+    }
     for (int r = 0; r < 4; r++) {
       const int x = q[4 * f + r];
       qo[4 * o + r] = vm_first[x] ? vm_second[vm_second[x]] : vm_second[x];
@@ -278,10 +287,15 @@ __global__ void mark3333_kernel(const int32_t* he, int64_t nq, const int32_t* va
 
 // removeQuadrilaterals3333 (:1340-1382)
 __global__ void gather_quads_3333_kernel(const uint8_t* rflag, const int32_t* idx, int64_t nq, const int32_t* q,
-                                         const uint8_t* p3, const int32_t* vm1, const int32_t* vm2, int32_t* qo) {
+                                         const uint8_t* p3, const int32_t* vm1, const int32_t* vm2, int32_t* qo,
+                                         int64_t cap, unsigned* overflow) {
   FOR_EACH(f, nq) {
     if (rflag[f]) continue;
     const int64_t o = idx[f];
+    if (o < 0 || o >= cap) {
+      atomicAdd(overflow, 1u);
+      continue;
+    }
     for (int r = 0; r < 4; r++) {
       const int x = q[4 * f + r];
       qo[4 * o + r] = p3[f] ? vm2[vm1[x]] : vm2[x];
@@ -400,6 +414,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   hw.nm = pool.get<unsigned long long>(2);
   hw.ovf = pool.get<unsigned>(2);
   unsigned long long* tiles = pool.get<unsigned long long>(scan_tiles(4 * NQ) + 2);
+  if (hw.ovf) cudaMemsetAsync(hw.ovf, 0, 2 * sizeof(unsigned), st);
   unsigned long long* total = pool.get<unsigned long long>(2);
   if (pool.err) {
     s.err = pool.err;
@@ -509,7 +524,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     adopt(nx.v);
     adopt(nx.n);
     gather_vertices_kernel<<<gv, 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.v, cur.n, nx.v64, nx.v, nx.n,
-                                                vm_second);
+                                                vm_second, nv2, hw.ovf);
     // remove quads
     invert_flags_kernel<<<gq, 256, 0, st>>>(em, cur.nq, keep);
     s.launches += 2 + scan_flags(keep, cur.nq, idx, tiles, total, st);
@@ -517,7 +532,8 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     void* qn = nullptr;
     if ((s.err = cudaMallocAsync(&qn, std::max<int64_t>(nq2, 1) * 4 * sizeof(int32_t), st)) != cudaSuccess) break;
     adopt(qn);
-    gather_quads_3x3y_kernel<<<gq, 256, 0, st>>>(keep, idx, cur.nq, cur.quads, vm_first, vm_second, (int32_t*)qn);
+    gather_quads_3x3y_kernel<<<gq, 256, 0, st>>>(em, idx, cur.nq, cur.quads, vm_first, vm_second, (int32_t*)qn,
+                                                  nq2, hw.ovf);
     s.launches += 1;
     // the inherited colours are only read by the colour pass; they are not carried along
     retire(cur.v64);
@@ -554,14 +570,16 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
       adopt(nx.v64);
       adopt(nx.v);
       adopt(nx.n);
-      gather_vertices_kernel<<<gv, 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.v, cur.n, nx.v64, nx.v, nx.n, vm2);
+      gather_vertices_kernel<<<gv, 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.v, cur.n, nx.v64, nx.v, nx.n, vm2,
+                                                  nv2, hw.ovf);
       invert_flags_kernel<<<gq, 256, 0, st>>>(rflag, cur.nq, keep);
       s.launches += 2 + scan_flags(keep, cur.nq, idx, tiles, total, st);
       const int64_t nq2 = read_total();
       void* qn = nullptr;
       if ((s.err = cudaMallocAsync(&qn, std::max<int64_t>(nq2, 1) * 4 * sizeof(int32_t), st)) == cudaSuccess) {
         adopt(qn);
-        gather_quads_3333_kernel<<<gq, 256, 0, st>>>(rflag, idx, cur.nq, cur.quads, p3, vm1, vm2, (int32_t*)qn);
+        gather_quads_3333_kernel<<<gq, 256, 0, st>>>(rflag, idx, cur.nq, cur.quads, p3, vm1, vm2, (int32_t*)qn, nq2,
+                                                      hw.ovf);
         s.launches += 1;
         retire(cur.v64);
         retire(cur.v);
