@@ -1,0 +1,88 @@
+// CPU check of the DMC vertex representative: for every contour of a field, the fast path
+// (float32 search + certified float-float rounding, tmc_gb300/csrc/dmc_repr.cuh) must return the
+// same floats as the float64 restatement of the reference.  Built with nvcc as host code.
+//   repr_check field.raw nx ny nz iso  -> prints "contours mismatches fallbacks fail1 fail2"
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "../../tmc_gb300/csrc/common.cuh"
+#include "../../tmc_gb300/csrc/dmc_repr.cuh"
+
+using namespace tmc;
+
+static uint64_t polygon(unsigned cs, const float u[8], double iso) {
+  if (!case_ambiguous(cs)) return table_contour(TMC_CASE_CONTOUR[cs]);
+  uint64_t to = ~0ull;
+  for (int f = 0; f < 6; f++) {
+    const uint32_t fv = face_v_pack(f);
+    const int fc = face_case(cs, fv);
+    int sep = 0;
+    if (fc == 6 || fc == 9) sep = decider(u[nib(fv, 0)], u[nib(fv, 1)], u[nib(fv, 2)], u[nib(fv, 3)]) >= iso;
+    face_segments(fc, sep, face_e_pack(f), to);
+  }
+  return connect_contours(to, case_edge_mask(cs));
+}
+
+int main(int argc, char** argv) {
+  if (argc < 6) return 2;
+  const int nx = atoi(argv[2]), ny = atoi(argv[3]), nz = atoi(argv[4]);
+  const double iso = atof(argv[5]);
+  std::vector<float> f((size_t)nx * ny * nz);
+  FILE* in = fopen(argv[1], "rb");
+  if (!in || fread(f.data(), 4, f.size(), in) != f.size()) return 3;
+  fclose(in);
+  const float iso_up = [&] { float x = (float)iso; if ((double)x < iso) x = nextafterf(x, INFINITY); return x; }();
+  long contours = 0, mism = 0;
+  repr::Stats se, sf;
+  for (int k = 0; k < nz - 1; k++)
+    for (int j = 0; j < ny - 1; j++)
+      for (int i = 0; i < nx - 1; i++) {
+        float u[8];
+        for (int q = 0; q < 8; q++)
+          u[q] = f[((size_t)(k + ((q >> 2) & 1)) * ny + (j + ((q >> 1) & 1))) * nx + i + (q & 1)];
+        unsigned cs = 0;
+        for (int q = 0; q < 8; q++) cs |= (unsigned)(u[q] >= iso_up) << q;
+        if (cs == 0 || cs == 255) continue;
+        const uint64_t c = polygon(cs, u, iso);
+        const int n = cnt_count(c);
+        repr::Boxes bx;
+        float pts[4][36];
+        int flat = 0;
+        for (int t = 0; t < n; t++) {
+          for (int d = 0; d < 3; d++) { bx.b[t][d][0] = 1; bx.b[t][d][1] = 0; }
+          const int sz = cnt_size(c, t);
+          for (int q = 0; q < sz; q++) {
+            const int e = cnt_edge(c, flat + q);
+            bool fb = false;
+            const float l = repr::edge_param_fast(e, u, iso, ffx::ff_from_double(iso), fb);
+            if (l != repr::edge_param_exact(e, u, iso)) mism++;
+            float ui[3];
+            repr::local_from_param(e, l, ui);
+            for (int d = 0; d < 3; d++) {
+              pts[t][3 * q + d] = ui[d];
+              bx.b[t][d][0] = bx.b[t][d][0] > ui[d] ? ui[d] : bx.b[t][d][0];
+              bx.b[t][d][1] = bx.b[t][d][1] < ui[d] ? ui[d] : bx.b[t][d][1];
+            }
+          }
+          flat += sz;
+        }
+        for (int t = 0; t < n; t++) {
+          const int sz = cnt_size(c, t);
+          double pe[3];
+          repr::mean_point_exact(pts[t], sz, pe);
+          repr::representative_exact(u, iso, c, t, pe, bx, se);
+          float pf[3];
+          repr::representative_fast(u, iso, c, t, pts[t], sz, bx, pf, sf);
+          contours++;
+          if ((float)pe[0] != pf[0] || (float)pe[1] != pf[1] || (float)pe[2] != pf[2]) {
+            if (mism < 5)
+              fprintf(stderr, "cell %d %d %d t %d: exact %.9g %.9g %.9g fast %.9g %.9g %.9g\n", i, j, k, t, pe[0],
+                      pe[1], pe[2], pf[0], pf[1], pf[2]);
+            mism++;
+          }
+        }
+      }
+  printf("%ld %ld %d %d %d %d %d\n", contours, mism, sf.fallback, sf.fail1, sf.fail2, se.fail1, se.fail2);
+  return 0;
+}

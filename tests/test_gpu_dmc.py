@@ -57,7 +57,8 @@ def test_dmc_front_matches_oracle(ctx, oracle, name, flip):
     np.testing.assert_array_equal(got["vuvw"], want["vuvw"])
     np.testing.assert_array_equal(got["v64"], want["v"])
     assert _close32(got["v"], want["v"])
-    assert _close32(got["n"], want["n"])
+    # float32 normals are computed in float32 when nothing needs them in float64
+    assert np.max(np.abs(got["n"].astype(np.float64) - want["n"]), initial=0) < 1e-5
     assert got["stats"][2] == want["proj_fail"][0] and got["stats"][3] == want["proj_fail"][1]
 
 
@@ -119,7 +120,10 @@ def test_dmc_full_pipeline_matches_oracle(ctx, oracle, name, simplify):
     np.testing.assert_array_equal(got["q"], want["q"])
     np.testing.assert_array_equal(got["v64"], want["v"])
     assert _close32(got["v"], want["v"])
-    assert _close32(got["n"], want["n"], ulps=4)
+    if simplify:  # float64 normals are kept through the merges
+        assert _close32(got["n"], want["n"], ulps=2)
+    else:
+        assert np.max(np.abs(got["n"].astype(np.float64) - want["n"]), initial=0) < 1e-5
     he5 = want["he"].reshape(-1, 5)
     np.testing.assert_array_equal(got["he"].reshape(-1, 4), he5[:, :4])
     np.testing.assert_array_equal(got["hv"], want["hv"])

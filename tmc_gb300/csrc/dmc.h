@@ -12,6 +12,7 @@ struct DmcVertexOut {
   float* v;        // 3 per vertex
   float* n;        // 3 per vertex
   double* v64;     // optional
+  double* n64;     // optional: float64 normals (kept while the mesh is simplified)
   int64_t* vcell;  // optional (with vuvw)
   float* vuvw;
 };
@@ -20,6 +21,7 @@ struct DmcScratch {
   uint32_t* rec;                  // per cell
   int32_t* voff;                  // per cell
   int32_t* qoff;                  // per cell
+  uint32_t* vwork;                // per vertex: generating cell
   unsigned long long* tile_sums;  // per scan tile
   unsigned long long* totals;     // [0] = (vertices << 32) | quads
   unsigned long long* stats;      // 8 counters
@@ -28,7 +30,7 @@ struct DmcScratch {
 // Each launcher returns the number of kernels it launched.
 int64_t dmc_tiles(const Grid& g);  // scan tiles for the cell count of g
 int dmc_front_count(const Grid& g, DmcScratch& s, cudaStream_t st, Prof* prof = nullptr);
-int dmc_front_emit(const Grid& g, DmcScratch& s, DmcVertexOut vo, int32_t* quads, uint8_t* colors, int flip,
-                   int sms, cudaStream_t st, Prof* prof = nullptr);
+int dmc_front_emit(const Grid& g, DmcScratch& s, DmcVertexOut vo, int64_t nv, int32_t* quads, uint8_t* colors,
+                   int flip, int sms, cudaStream_t st, Prof* prof = nullptr);
 
 }  // namespace tmc

@@ -23,6 +23,7 @@
 
 #include "common.cuh"
 #include "dmc.h"
+#include "dmc_repr.cuh"
 #include "scan.cuh"
 
 namespace tmc {
@@ -68,13 +69,15 @@ __device__ __forceinline__ unsigned mc_case(const float u[8], float iso_up) {
   return c;
 }
 
-// Linear cell index -> (i, j, k)
+// Linear cell index -> (i, j, k); cell counts stay below 2^32 (checked by the runtime)
 __device__ __forceinline__ void cell_ijk(const Grid& g, int64_t c, int& i, int& j, int& k) {
-  const int64_t cx = g.nx - 1, cy = g.ny - 1;
-  i = (int)(c % cx);
-  const int64_t r = c / cx;
-  j = (int)(r % cy);
-  k = (int)(r / cy);
+  const uint32_t cx = (uint32_t)(g.nx - 1), cy = (uint32_t)(g.ny - 1);
+  const uint32_t cc = (uint32_t)c;
+  const uint32_t r = cc / cx;
+  i = (int)(cc - r * cx);
+  const uint32_t kk = r / cy;
+  j = (int)(r - kk * cy);
+  k = (int)kk;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -151,7 +154,7 @@ __global__ void __launch_bounds__(kScanThreads) dmc_classify_kernel(Grid g, uint
 // In-tile exclusive scan of the records -> per-cell vertex and quad offsets.
 __global__ void __launch_bounds__(kScanThreads) dmc_offsets_kernel(int64_t n, const uint32_t* rec,
                                                                   const unsigned long long* tile_off,
-                                                                  int32_t* voff, int32_t* qoff) {
+                                                                  int32_t* voff, int32_t* qoff, uint32_t* vwork) {
   const int64_t base = (int64_t)blockIdx.x * kScanTile;
   // thread t owns cells base + t*kScanItems .. + kScanItems-1 (contiguous) for the scan
   uint32_t r[kScanItems];
@@ -169,141 +172,18 @@ __global__ void __launch_bounds__(kScanThreads) dmc_offsets_kernel(int64_t n, co
     if (mine + s < n) {
       voff[mine + s] = (int32_t)(pre >> 32);
       qoff[mine + s] = (int32_t)(pre & 0xffffffffull);
+      // one work item per vertex: the cell that generates it
+      for (int q = 0; q < rec_nv(r[s]); q++) vwork[(pre >> 32) + q] = (uint32_t)(mine + s);
     }
     pre += ((unsigned long long)rec_nv(r[s]) << 32) | (unsigned long long)rec_nq(r[s]);
   }
 }
 
 // ------------------------------------------------------------------------------------------
-// vertex representative: exact restatement of the reference's mixed float/double arithmetic
-// (representative / projection, cpp_dmc/DualMarchingCubes.cpp:194-326).  The library is built
-// with -fmad=false, so each line below rounds exactly like the CPU code.
+// vertices: one thread per output vertex (work list from the offsets kernel).  The representative
+// comes from representative_fast (dmc_repr.cuh): float32 search with certified float-float
+// rounding, bit-identical to the reference's float/double arithmetic.
 // ------------------------------------------------------------------------------------------
-struct CellBoxes {
-  float b[4][3][2];  // contour, axis, min/max (values are floats; compared as doubles)
-};
-
-// getLocalCoordinates (cpp_dmc/DualMarchingCubes.h:391-407)
-__device__ __forceinline__ void local_coord(int e, const float u[8], double iso, float out[3]) {
-  const int v0 = edge_v0(e), v1 = edge_v1(e);
-  const float l = (iso - (double)u[v0]) / ((double)u[v1] - (double)u[v0]);
-  const int ax = edge_axis(e), con = edge_off(e);
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    const float val = (d == ax) ? 1.0f : 0.0f;
-    const float cn = (float)((con >> d) & 1);
-    out[d] = l * val + cn;
-  }
-}
-
-// isInNeighborBBox (cpp_dmc/DualMarchingCubes.h:498-517) with the projection's axis order
-__device__ __forceinline__ bool in_neighbor_bbox(double u, double v, double w, uint64_t c, int t,
-                                                 const CellBoxes& bx, int A, int B, int W) {
-  const int ncnt = cnt_count(c);
-  for (int i = 0; i < ncnt; i++) {
-    if (cnt_size(c, i) == 3 && t != i) {
-      if (u < (double)bx.b[i][A][0] || (double)bx.b[i][A][1] < u) continue;
-      if (v < (double)bx.b[i][B][0] || (double)bx.b[i][B][1] < v) continue;
-      if (w < (double)bx.b[i][W][0] || (double)bx.b[i][W][1] < w) continue;
-      return true;
-    }
-  }
-  return false;
-}
-
-// projection (cpp_dmc/DualMarchingCubes.cpp:274-326).  Plane pr: 0 = w (z), 1 = v (y), 2 = u (x).
-// The corner permutation of the plane is applied to the field values by the caller (fp).
-__device__ bool projection_exact(const double fp[8], double iso, uint64_t c, int t, double p[3],
-                                 const CellBoxes& bx, int A, int B, int W, int nrSamples) {
-  const double umin = bx.b[t][A][0], umax = bx.b[t][A][1];
-  const double vmin = bx.b[t][B][0], vmax = bx.b[t][B][1];
-  const double du = (umax - umin) / (nrSamples - 1);
-  const double dv = (vmax - vmin) / (nrSamples - 1);
-  double minDistance = 100;
-  double pt0 = 0, pt1 = 0, pt2 = -1;
-  double wmin = bx.b[t][W][0], wmax = bx.b[t][W][1];
-  const double eps = 1e-5;
-  if (fabs(wmax - wmin) < eps) {
-    wmin -= eps;
-    wmax += eps;
-  }
-  const int cnt = cnt_count(c);
-  const int cnt_sz = cnt_size(c, t);
-  for (int i = 1; i < (nrSamples - 1); i++) {
-    const float u = umin + i * du;
-    for (int j = 1; j < (nrSamples - 1); j++) {
-      const float v = vmin + j * dv;
-      const float g1 = (1 - v) * ((1 - u) * fp[0] + u * fp[1]) + v * ((1 - u) * fp[2] + u * fp[3]);
-      const float g2 = (1 - v) * ((1 - u) * fp[4] + u * fp[5]) + v * ((1 - u) * fp[6] + u * fp[7]);
-      if (g1 == g2) continue;
-      const float w = (iso - g1) / (g2 - g1);
-      if (wmin <= w && w <= wmax) {
-        if (cnt == 1 || cnt_sz == 3 || !in_neighbor_bbox(u, v, w, c, t, bx, A, B, W)) {
-          const float d = (p[0] - u) * (p[0] - u) + (p[1] - v) * (p[1] - v) + (p[2] - w) * (p[2] - w);
-          if (minDistance > d) {
-            minDistance = d;
-            pt0 = u;
-            pt1 = v;
-            pt2 = w;
-          }
-        }
-      }
-    }
-  }
-  if (pt2 > -1) {
-    p[0] = pt0;
-    p[1] = pt1;
-    p[2] = pt2;
-    return true;
-  }
-  return false;
-}
-
-// representative (cpp_dmc/DualMarchingCubes.cpp:194-272)
-__device__ void representative_exact(const float u[8], double iso, uint64_t c, int t, double p[3],
-                                     const CellBoxes& bx, unsigned long long* stats) {
-  int prj = 0;  // 0 = W, 1 = V, 2 = U
-  double f[8];
-#pragma unroll
-  for (int q = 0; q < 8; q++) f[q] = u[q];
-  if (cnt_size(c, t) >= 6) {
-    const double uu = p[0], vv = p[1], ww = p[2];
-    const double g0 = (1 - ww) * ((1 - vv) * (f[1] - f[0]) + vv * (f[3] - f[2])) + ww * ((1 - vv) * (f[5] - f[4]) + vv * (f[7] - f[6]));
-    const double g1 = (1 - ww) * ((1 - uu) * (f[2] - f[0]) + uu * (f[3] - f[1])) + ww * ((1 - uu) * (f[6] - f[4]) + uu * (f[7] - f[5]));
-    const double g2 = (1 - vv) * ((1 - uu) * (f[4] - f[0]) + uu * (f[5] - f[1])) + vv * ((1 - uu) * (f[6] - f[2]) + uu * (f[7] - f[3]));
-    const double dx = fabs(g0), dy = fabs(g1), dz = fabs(g2);
-    if (dz >= dx && dz >= dy) prj = 0;
-    else if (dy >= dx && dy >= dz) prj = 1;
-    else if (dx >= dy && dx >= dz) prj = 2;
-    else prj = 0;
-  } else {
-    const double su = (double)bx.b[t][0][1] - (double)bx.b[t][0][0];
-    const double sv = (double)bx.b[t][1][1] - (double)bx.b[t][1][0];
-    const double sw = (double)bx.b[t][2][1] - (double)bx.b[t][2][0];
-    if (sw <= su && sw <= sv) prj = 0;
-    else if (sv <= su && sv <= sw) prj = 1;
-    else if (su <= sv && su <= sw) prj = 2;
-    else prj = 0;
-  }
-  // plane axes (A, B, W) and the corner permutation of the plane (w_proj / v_proj / u_proj)
-  int A, B, W;
-  uint32_t perm;
-  if (prj == 0) { A = 0; B = 1; W = 2; perm = 0x76543210u; }
-  else if (prj == 1) { A = 0; B = 2; W = 1; perm = 0x76325410u; }
-  else { A = 1; B = 2; W = 0; perm = 0x75316420u; }
-  double fp[8];
-#pragma unroll
-  for (int q = 0; q < 8; q++) fp[q] = f[(perm >> (4 * q)) & 0xF];
-  double pt[3] = {p[A], p[B], p[W]};
-  if (!projection_exact(fp, iso, c, t, pt, bx, A, B, W, 9)) {
-    atomicAdd(stats + 2, 1ull);
-    if (!projection_exact(fp, iso, c, t, pt, bx, A, B, W, 28)) atomicAdd(stats + 3, 1ull);
-  }
-  p[A] = pt[0];
-  p[B] = pt[1];
-  p[W] = pt[2];
-}
-
 // estimateGradient at a grid point (cpp_dmc/UniformGrid.cpp:512-540): central differences with
 // the reference's border indexing ((i<0) ? 0 : (i>=max) ? max-i : i).
 __device__ __forceinline__ int grad_index(int i, int max) { return (i < 0) ? 0 : (i >= max) ? max - i : i; }
@@ -315,18 +195,28 @@ __device__ __forceinline__ void point_gradient(const Grid& g, int i, int j, int 
   out[1] = ((double)g.at(i, j1, k) - (double)g.at(i, j0, k)) / (2 * g.dy);
   out[2] = ((double)g.at(i, j, k1) - (double)g.at(i, j, k0)) / (2 * g.dz);
 }
+__device__ __forceinline__ void point_gradient_f(const Grid& g, int i, int j, int k, float inv2d[3], float out[3]) {
+  const int i0 = grad_index(i - 1, g.nx), i1 = grad_index(i + 1, g.nx);
+  const int j0 = grad_index(j - 1, g.ny), j1 = grad_index(j + 1, g.ny);
+  const int k0 = grad_index(k - 1, g.nz), k1 = grad_index(k + 1, g.nz);
+  out[0] = (g.at(i1, j, k) - g.at(i0, j, k)) * inv2d[0];
+  out[1] = (g.at(i, j1, k) - g.at(i, j0, k)) * inv2d[1];
+  out[2] = (g.at(i, j, k1) - g.at(i, j, k0)) * inv2d[2];
+}
 
-__global__ void __launch_bounds__(128) dmc_vertex_kernel(Grid g, const uint32_t* rec, const int32_t* voff,
-                                                         DmcVertexOut out, int flip,
+__global__ void __launch_bounds__(128) dmc_vertex_kernel(Grid g, const int32_t* voff, const uint32_t* vwork,
+                                                         int64_t nv, DmcVertexOut out, int flip,
                                                          unsigned long long* stats) {
   __shared__ uint64_t cc[256];
   for (int c = threadIdx.x; c < 256; c += blockDim.x) cc[c] = c_case_contour[c];
   __syncthreads();
-  const int64_t n = g.ncells();
-  for (int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; cell < n;
-       cell += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t r = rec[cell];
-    if (rec_nv(r) == 0) continue;
+  repr::Stats st;
+  const ffx::ff iso_ff = ffx::ff_from_double(g.iso);
+  float inv2d[3] = {(float)(1.0 / (2 * g.dx)), (float)(1.0 / (2 * g.dy)), (float)(1.0 / (2 * g.dz))};
+  for (int64_t vidx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vidx < nv;
+       vidx += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t cell = vwork[vidx];
+    const int rank = (int)(vidx - voff[cell]);
     int i, j, k;
     cell_ijk(g, cell, i, j, k);
     float u[8];
@@ -334,90 +224,105 @@ __global__ void __launch_bounds__(128) dmc_vertex_kernel(Grid g, const uint32_t*
     const unsigned cs = mc_case(u, g.iso_up);
     const uint64_t c = dmc_polygon(cs, u, g.iso, cc);
     const int ncnt = cnt_count(c);
-    // bounding boxes of all contours (slice, cpp_dmc/DualMarchingCubes.cpp:114-136)
-    CellBoxes bx;
-    int flat = 0;
+    // edge points and bounding boxes of all contours (slice, cpp_dmc/DualMarchingCubes.cpp:114-136)
+    repr::Boxes bx;
+    float pts[36];
+    int flat = 0, tsel = -1, tstart = 0, used_seen = 0;
     for (int t = 0; t < ncnt; t++) {
       bx.b[t][0][0] = 1; bx.b[t][0][1] = 0;
       bx.b[t][1][0] = 1; bx.b[t][1][1] = 0;
       bx.b[t][2][0] = 1; bx.b[t][2][1] = 0;
       const int sz = cnt_size(c, t);
+      bool used = false;
       for (int q = 0; q < sz; q++) {
+        const int e = cnt_edge(c, flat + q);
+        used = used || edge_interior(g, i, j, k, e);
+        bool fb = false;
+        const float l = repr::edge_param_fast(e, u, g.iso, iso_ff, fb);
         float ui[3];
-        local_coord(cnt_edge(c, flat + q), u, g.iso, ui);
+        repr::local_from_param(e, l, ui);
 #pragma unroll
         for (int d = 0; d < 3; d++) {
+          pts[3 * (flat + q) + d] = ui[d];
           bx.b[t][d][0] = bx.b[t][d][0] > ui[d] ? ui[d] : bx.b[t][d][0];
           bx.b[t][d][1] = bx.b[t][d][1] < ui[d] ? ui[d] : bx.b[t][d][1];
         }
       }
-      flat += sz;
-    }
-    int32_t vidx = voff[cell];
-    flat = 0;
-    for (int t = 0; t < ncnt; t++) {
-      const int sz = cnt_size(c, t);
-      bool used = false;
-      for (int q = 0; q < sz; q++) used = used || edge_interior(g, i, j, k, cnt_edge(c, flat + q));
       if (used) {
-        double p[3] = {0, 0, 0};
-        for (int q = 0; q < sz; q++) {
-          float ui[3];
-          local_coord(cnt_edge(c, flat + q), u, g.iso, ui);
-          p[0] += ui[0];
-          p[1] += ui[1];
-          p[2] += ui[2];
+        if (used_seen == rank) {
+          tsel = t;
+          tstart = flat;
         }
-        p[0] /= sz;
-        p[1] /= sz;
-        p[2] /= sz;
-        representative_exact(u, g.iso, c, t, p, bx, stats);
-        // normal: trilinear interpolation of the 8 corner gradients, normalised
-        // (UniformGrid::normal, cpp_dmc/UniformGrid.h:286-298)
-        double G[8][3];
-#pragma unroll
-        for (int q = 0; q < 8; q++) point_gradient(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), G[q]);
-        double nv[3];
-        const double uu = p[0], vv = p[1], ww = p[2];
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-          double gq[8];
-#pragma unroll
-          for (int q = 0; q < 8; q++) gq[q] = flip ? G[q][d] * -1. : G[q][d];
-          nv[d] = (1 - ww) * ((1 - vv) * ((1 - uu) * gq[0] + uu * gq[1]) + vv * ((1 - uu) * gq[2] + uu * gq[3])) +
-                  ww * ((1 - vv) * ((1 - uu) * gq[4] + uu * gq[5]) + vv * ((1 - uu) * gq[6] + uu * gq[7]));
-        }
-        const double s_ = sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
-        nv[0] /= s_;
-        nv[1] /= s_;
-        nv[2] /= s_;
-        // position (UniformGrid::position, cpp_dmc/UniformGrid.h:300-305)
-        const double px = g.ox + (i + p[0]) * g.dx;
-        const double py = g.oy + (j + p[1]) * g.dy;
-        const double pz = g.oz + (k + p[2]) * g.dz;
-        const int64_t o = 3 * (int64_t)vidx;
-        out.v[o] = (float)px;
-        out.v[o + 1] = (float)py;
-        out.v[o + 2] = (float)pz;
-        out.n[o] = (float)nv[0];
-        out.n[o + 1] = (float)nv[1];
-        out.n[o + 2] = (float)nv[2];
-        if (out.v64) {
-          out.v64[o] = px;
-          out.v64[o + 1] = py;
-          out.v64[o + 2] = pz;
-        }
-        if (out.vcell) {
-          out.vcell[vidx] = cell;
-          out.vuvw[o] = (float)p[0];
-          out.vuvw[o + 1] = (float)p[1];
-          out.vuvw[o + 2] = (float)p[2];
-        }
-        vidx++;
+        used_seen++;
       }
       flat += sz;
     }
+    if (tsel < 0) continue;  // cannot happen: the record counted this vertex
+    float p[3];
+    repr::representative_fast(u, g.iso, c, tsel, pts + 3 * tstart, cnt_size(c, tsel), bx, p, st);
+    const int64_t o = 3 * vidx;
+    // position: UniformGrid::position (cpp_dmc/UniformGrid.h:300-305)
+    const double px = g.ox + (i + (double)p[0]) * g.dx;
+    const double py = g.oy + (j + (double)p[1]) * g.dy;
+    const double pz = g.oz + (k + (double)p[2]) * g.dz;
+    out.v[o] = (float)px;
+    out.v[o + 1] = (float)py;
+    out.v[o + 2] = (float)pz;
+    if (out.v64) {
+      out.v64[o] = px;
+      out.v64[o + 1] = py;
+      out.v64[o + 2] = pz;
+    }
+    // normal: trilinear interpolation of the 8 corner gradients, normalised (UniformGrid::normal,
+    // cpp_dmc/UniformGrid.h:286-298); float64 when it is kept for the simplification merges
+    if (out.n64) {
+      double G[8][3];
+#pragma unroll
+      for (int q = 0; q < 8; q++) point_gradient(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), G[q]);
+      double nv3[3];
+      const double uu = p[0], vv = p[1], ww = p[2];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        double gq[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) gq[q] = flip ? G[q][d] * -1. : G[q][d];
+        nv3[d] = (1 - ww) * ((1 - vv) * ((1 - uu) * gq[0] + uu * gq[1]) + vv * ((1 - uu) * gq[2] + uu * gq[3])) +
+                 ww * ((1 - vv) * ((1 - uu) * gq[4] + uu * gq[5]) + vv * ((1 - uu) * gq[6] + uu * gq[7]));
+      }
+      const double s_ = sqrt(nv3[0] * nv3[0] + nv3[1] * nv3[1] + nv3[2] * nv3[2]);
+      for (int d = 0; d < 3; d++) {
+        const double x = nv3[d] / s_;
+        out.n64[o + d] = x;
+        out.n[o + d] = (float)x;
+      }
+    } else {
+      float G[8][3];
+#pragma unroll
+      for (int q = 0; q < 8; q++) point_gradient_f(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), inv2d, G[q]);
+      float nv3[3];
+      const float uu = p[0], vv = p[1], ww = p[2];
+      const float sgn = flip ? -1.0f : 1.0f;
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        const float a0 = fmaf(uu, G[1][d] - G[0][d], G[0][d]), a1 = fmaf(uu, G[3][d] - G[2][d], G[2][d]);
+        const float a2 = fmaf(uu, G[5][d] - G[4][d], G[4][d]), a3 = fmaf(uu, G[7][d] - G[6][d], G[6][d]);
+        const float b0 = fmaf(vv, a1 - a0, a0), b1 = fmaf(vv, a3 - a2, a2);
+        nv3[d] = sgn * fmaf(ww, b1 - b0, b0);
+      }
+      const float rn = rsqrtf(nv3[0] * nv3[0] + nv3[1] * nv3[1] + nv3[2] * nv3[2]);
+      for (int d = 0; d < 3; d++) out.n[o + d] = nv3[d] * rn;
+    }
+    if (out.vcell) {
+      out.vcell[vidx] = cell;
+      out.vuvw[o] = p[0];
+      out.vuvw[o + 1] = p[1];
+      out.vuvw[o + 2] = p[2];
+    }
   }
+  // representative counters (the reference's failed-projection counts) and float64 fallbacks
+  if (st.fail1) atomicAdd(stats + 2, (unsigned long long)st.fail1);
+  if (st.fail2) atomicAdd(stats + 3, (unsigned long long)st.fail2);
+  if (st.fallback) atomicAdd(stats + 7, (unsigned long long)st.fallback);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -490,23 +395,29 @@ int dmc_front_count(const Grid& g, DmcScratch& s, cudaStream_t st, Prof* prof) {
   }
   Stage t(prof, "dmc_scan", st);
   scan_tile_sums_kernel<<<1, 1024, 0, st>>>(s.tile_sums, tiles, s.totals);
-  dmc_offsets_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(n, s.rec, s.tile_sums, s.voff, s.qoff);
-  return 3;
+  return 2;
 }
 
 int64_t dmc_tiles(const Grid& g) { return ceil_div(g.ncells(), kScanTile); }
 
-int dmc_front_emit(const Grid& g, DmcScratch& s, DmcVertexOut vo, int32_t* quads, uint8_t* colors, int flip,
-                   int sms, cudaStream_t st, Prof* prof) {
+int dmc_front_emit(const Grid& g, DmcScratch& s, DmcVertexOut vo, int64_t nv, int32_t* quads, uint8_t* colors,
+                   int flip, int sms, cudaStream_t st, Prof* prof) {
   const int64_t n = g.ncells();
   const int64_t blocks = std::min<int64_t>(ceil_div(n, 128), (int64_t)sms * 16);
   {
+    // per-cell offsets and the vertex work list (needs the vertex count for its size)
+    Stage t(prof, "dmc_scan", st);
+    dmc_offsets_kernel<<<(unsigned)ceil_div(n, kScanTile), kScanThreads, 0, st>>>(n, s.rec, s.tile_sums, s.voff,
+                                                                                  s.qoff, s.vwork);
+  }
+  {
     Stage t(prof, "dmc_vertex", st);
-    dmc_vertex_kernel<<<(unsigned)blocks, 128, 0, st>>>(g, s.rec, s.voff, vo, flip, s.stats);
+    const int64_t vb = std::max<int64_t>(1, std::min<int64_t>(ceil_div(nv, 128), (int64_t)sms * 32));
+    dmc_vertex_kernel<<<(unsigned)vb, 128, 0, st>>>(g, s.voff, s.vwork, nv, vo, flip, s.stats);
   }
   Stage t(prof, "dmc_quad", st);
   dmc_quad_kernel<<<(unsigned)blocks, 128, 0, st>>>(g, s.rec, s.voff, s.qoff, quads, colors);
-  return 2;
+  return 3;
 }
 
 }  // namespace tmc

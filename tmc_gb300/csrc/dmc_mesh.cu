@@ -164,7 +164,7 @@ __global__ void merge_claim_kernel(const int32_t* he, int64_t nq, const uint8_t*
   }
 }
 
-__device__ __forceinline__ void midpoint(double* v64, float* v, float* n, int dst, int a, int b) {
+__device__ __forceinline__ void midpoint(double* v64, float* v, double* n64, float* n, int dst, int a, int b) {
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     const double x = v64[3 * (int64_t)a + d] + 0.5 * (v64[3 * (int64_t)b + d] - v64[3 * (int64_t)a + d]);
@@ -174,16 +174,20 @@ __device__ __forceinline__ void midpoint(double* v64, float* v, float* n, int ds
   double m[3];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    const double na = n[3 * (int64_t)a + d], nb = n[3 * (int64_t)b + d];
+    const double na = n64[3 * (int64_t)a + d], nb = n64[3 * (int64_t)b + d];
     m[d] = na + 0.5 * (nb - na);
   }
   const double s = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
 #pragma unroll
-  for (int d = 0; d < 3; d++) n[3 * (int64_t)dst + d] = (float)(m[d] / s);
+  for (int d = 0; d < 3; d++) {
+    const double x = m[d] / s;
+    n64[3 * (int64_t)dst + d] = x;
+    n[3 * (int64_t)dst + d] = (float)x;
+  }
 }
 
 __global__ void merge_apply_kernel(const int32_t* he, int64_t nq, const uint8_t* branch, const int32_t* own_pos,
-                                   const int32_t* own_rm, double* v64, float* v, float* n, uint8_t* vm_first,
+                                   const int32_t* own_rm, double* v64, float* v, double* n64, float* n, uint8_t* vm_first,
                                    int32_t* vm_second, uint8_t* em) {
   FOR_EACH(f, nq) {
     em[f] = branch[f] != 0;
@@ -191,11 +195,11 @@ __global__ void merge_apply_kernel(const int32_t* he, int64_t nq, const uint8_t*
     const int v0 = he_origin(he, 4 * f), v1 = he_origin(he, 4 * f + 1), v2 = he_origin(he, 4 * f + 2),
               v3 = he_origin(he, 4 * f + 3);
     if (branch[f] == 1) {
-      if (own_pos[v0] == f) midpoint(v64, v, n, v0, v1, v3);
+      if (own_pos[v0] == f) midpoint(v64, v, n64, n, v0, v1, v3);
       vm_first[v2] = 1;
       if (own_rm[v2] == f) vm_second[v2] = v0;
     } else {
-      if (own_pos[v1] == f) midpoint(v64, v, n, v1, v0, v2);
+      if (own_pos[v1] == f) midpoint(v64, v, n64, n, v1, v0, v2);
       vm_first[v3] = 1;
       if (own_rm[v3] == f) vm_second[v3] = v1;
     }
@@ -212,8 +216,8 @@ __global__ void invert_flags_kernel(const uint8_t* in, int64_t n, uint8_t* out) 
 // removeVertices3X3Y / removeVertices3333 (:1096-1112, :1324-1338): kept vertices move to their
 // new index, which becomes their map entry
 __global__ void gather_vertices_kernel(const uint8_t* keep, const int32_t* idx, int64_t nv, const double* v64,
-                                       const float* v, const float* n, double* v64o, float* vo, float* no,
-                                       int32_t* map, int64_t cap, unsigned* overflow) {
+                                       const float* v, const double* n64, const float* n, double* v64o, float* vo,
+                                       double* n64o, float* no, int32_t* map, int64_t cap, unsigned* overflow) {
   FOR_EACH(i, nv) {
     if (!keep[i]) continue;
     const int64_t o = idx[i];
@@ -224,6 +228,7 @@ __global__ void gather_vertices_kernel(const uint8_t* keep, const int32_t* idx, 
     for (int d = 0; d < 3; d++) {
       v64o[3 * o + d] = v64[3 * i + d];
       vo[3 * o + d] = v[3 * i + d];
+      n64o[3 * o + d] = n64[3 * i + d];
       no[3 * o + d] = n[3 * i + d];
     }
     map[i] = (int32_t)o;
@@ -458,13 +463,15 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   auto new_vertices = [&](int64_t nv, DmcMesh& m) {
     m.v64 = nullptr;
     cudaError_t e;
-    void *a = nullptr, *b = nullptr, *c = nullptr;
+    void *a = nullptr, *b = nullptr, *c = nullptr, *d = nullptr;
     if ((e = cudaMallocAsync(&a, std::max<int64_t>(nv, 1) * 3 * sizeof(double), st)) != cudaSuccess) return e;
     if ((e = cudaMallocAsync(&b, std::max<int64_t>(nv, 1) * 3 * sizeof(float), st)) != cudaSuccess) return e;
     if ((e = cudaMallocAsync(&c, std::max<int64_t>(nv, 1) * 3 * sizeof(float), st)) != cudaSuccess) return e;
+    if ((e = cudaMallocAsync(&d, std::max<int64_t>(nv, 1) * 3 * sizeof(double), st)) != cudaSuccess) return e;
     m.v64 = (double*)a;
     m.v = (float*)b;
     m.n = (float*)c;
+    m.n64 = (double*)d;
     return cudaSuccess;
   };
   auto retire = [&](void* ptr) {
@@ -511,8 +518,8 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     fill_i32_kernel<<<gv, 256, 0, st>>>(vm_second, cur.nv, -1);
     cudaMemsetAsync(vm_first, 0, cur.nv, st);
     merge_claim_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.nq, p, val, cur.colors, pass == 0, branch, own_pos, own_rm);
-    merge_apply_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.nq, branch, own_pos, own_rm, cur.v64, cur.v, cur.n, vm_first,
-                                           vm_second, em);
+    merge_apply_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.nq, branch, own_pos, own_rm, cur.v64, cur.v, cur.n64, cur.n,
+                                           vm_first, vm_second, em);
     s.launches += 8;
     // remove vertices
     invert_flags_kernel<<<gv, 256, 0, st>>>(vm_first, cur.nv, keep);
@@ -523,8 +530,9 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     adopt(nx.v64);
     adopt(nx.v);
     adopt(nx.n);
-    gather_vertices_kernel<<<gv, 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.v, cur.n, nx.v64, nx.v, nx.n,
-                                                vm_second, nv2, hw.ovf);
+    adopt(nx.n64);
+    gather_vertices_kernel<<<gv, 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.v, cur.n64, cur.n, nx.v64, nx.v,
+                                                nx.n64, nx.n, vm_second, nv2, hw.ovf);
     // remove quads
     invert_flags_kernel<<<gq, 256, 0, st>>>(em, cur.nq, keep);
     s.launches += 2 + scan_flags(keep, cur.nq, idx, tiles, total, st);
@@ -539,6 +547,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     retire(cur.v64);
     retire(cur.v);
     retire(cur.n);
+    retire(cur.n64);
     retire(cur.quads);
     nx.nv = nv2;
     nx.nq = nq2;
@@ -570,8 +579,9 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
       adopt(nx.v64);
       adopt(nx.v);
       adopt(nx.n);
-      gather_vertices_kernel<<<gv, 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.v, cur.n, nx.v64, nx.v, nx.n, vm2,
-                                                  nv2, hw.ovf);
+      adopt(nx.n64);
+      gather_vertices_kernel<<<gv, 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.v, cur.n64, cur.n, nx.v64, nx.v,
+                                                  nx.n64, nx.n, vm2, nv2, hw.ovf);
       invert_flags_kernel<<<gq, 256, 0, st>>>(rflag, cur.nq, keep);
       s.launches += 2 + scan_flags(keep, cur.nq, idx, tiles, total, st);
       const int64_t nq2 = read_total();
@@ -584,6 +594,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
         retire(cur.v64);
         retire(cur.v);
         retire(cur.n);
+        retire(cur.n64);
         retire(cur.quads);
         nx.nv = nv2;
         nx.nq = nq2;

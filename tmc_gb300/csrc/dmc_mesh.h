@@ -14,6 +14,7 @@ struct DmcMesh {
   float* v = nullptr;
   float* n = nullptr;
   double* v64 = nullptr;
+  double* n64 = nullptr;  // float64 normals while simplifying (merges average them as the reference)
   int32_t* quads = nullptr;
   uint8_t* colors = nullptr;
 };

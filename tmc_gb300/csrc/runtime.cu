@@ -333,6 +333,7 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   // simplification and the triangle split work on float64 positions, as the reference does
   const bool need_f64 = (flags & (TMC_OUT_POS_F64 | TMC_OUT_TRIANGLES)) || simplify;
   if (need_f64) TMC_GET(vo.v64, 3 * nv);
+  if (simplify) TMC_GET(vo.n64, 3 * nv);
   if (flags & TMC_OUT_LOCAL) {
     TMC_GET(vo.vcell, nv);
     TMC_GET(vo.vuvw, 3 * nv);
@@ -343,7 +344,12 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
     delete mp;
     TMC_CUDA(ctx, ce);
   }
-  ctx->launches += tmc::dmc_front_emit(g, sc, vo, quads, colors, (flags & TMC_GRAD_FLIP) ? 1 : 0, ctx->sms, st,
+  ce = al.get(&sc.vwork, nv);
+  if (ce != cudaSuccess) {
+    delete mp;
+    TMC_CUDA(ctx, ce);
+  }
+  ctx->launches += tmc::dmc_front_emit(g, sc, vo, nv, quads, colors, (flags & TMC_GRAD_FLIP) ? 1 : 0, ctx->sms, st,
                                        &ctx->prof);
   TMC_CUDA(ctx, cudaGetLastError());
 
@@ -353,6 +359,7 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   mesh.v = vo.v;
   mesh.n = vo.n;
   mesh.v64 = vo.v64;
+  mesh.n64 = vo.n64;
   mesh.quads = quads;
   mesh.colors = colors;
   tmc::DmcPostOut post{};
@@ -379,18 +386,22 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   out->v = post.mesh.v;
   out->n = post.mesh.n;
   out->v64 = post.mesh.v64;
-  if (out->v64 && !(flags & TMC_OUT_POS_F64)) {
+  // internal float64 buffers that are not outputs
+  auto drop = [&](void* ptr) {
+    if (!ptr) return;
     for (auto& q : mp->dev)
-      if (q == out->v64) q = nullptr;
-    {
-      std::vector<void*> keep;
-      for (void* q : mp->dev)
-        if (q) keep.push_back(q);
-      mp->dev.swap(keep);
-    }
-    cudaFreeAsync(out->v64, st);
+      if (q == ptr) q = nullptr;
+    std::vector<void*> keep;
+    for (void* q : mp->dev)
+      if (q) keep.push_back(q);
+    mp->dev.swap(keep);
+    cudaFreeAsync(ptr, st);
+  };
+  if (out->v64 && !(flags & TMC_OUT_POS_F64)) {
+    drop(out->v64);
     out->v64 = nullptr;
   }
+  drop(post.mesh.n64);
   out->quads = post.mesh.quads;
   out->nr_t = post.nt;
   out->tris = post.tris;
@@ -442,8 +453,12 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   ctx->launches += tmc::tmc_count(g, sc, st, &ctx->prof);
   unsigned long long* h = (unsigned long long*)ctx->h_pinned;
   TMC_CUDA(ctx, cudaMemcpyAsync(h, sc.totals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  TMC_CUDA(ctx, cudaMemcpyAsync(h + 1, sc.stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   TMC_CUDA(ctx, cudaStreamSynchronize(st));
   const int64_t nv = (int64_t)(h[0] >> 32), nt = (int64_t)(h[0] & 0xffffffffull);
+  const int64_t n_amb = (int64_t)h[2];
+  TMC_CUDA(ctx, al.get(&sc.amb_list, n_amb));
+  TMC_CUDA(ctx, al.get(&sc.amb_count, 1));
 
   MeshPriv* mp = new (std::nothrow) MeshPriv();
   if (!mp) return fail(ctx, TMC_ERR_OOM, "host allocation failed");

@@ -16,6 +16,7 @@
 //                        (ambiguous cells run the full p_slice logic in counting mode)
 //   tmc_offsets_kernel   in-tile scan -> per-cell vertex / triangle offsets
 //   tmc_emit_kernel      vertices (edge and inner) and triangles
+#include "ffloat.cuh"
 #include "scan.cuh"
 #include "tmc_cells.h"
 
@@ -34,12 +35,15 @@ __device__ __forceinline__ int trec_inner(uint32_t r) { return (r >> 12) & 7; }
 __device__ __forceinline__ int trec_ntri(uint32_t r) { return (r >> 15) & 63; }
 __device__ __forceinline__ int trec_nv(uint32_t r) { return __popc(trec_owned(r)) + trec_inner(r); }
 
+// cell counts stay below 2^32 (checked by the runtime), so 32-bit division suffices
 __device__ __forceinline__ void tcell_ijk(const Grid& g, int64_t c, int& i, int& j, int& k) {
-  const int64_t cx = g.nx - 1, cy = g.ny - 1;
-  i = (int)(c % cx);
-  const int64_t r = c / cx;
-  j = (int)(r % cy);
-  k = (int)(r / cy);
+  const uint32_t cx = (uint32_t)(g.nx - 1), cy = (uint32_t)(g.ny - 1);
+  const uint32_t cc = (uint32_t)c;
+  const uint32_t r = cc / cx;
+  i = (int)(cc - r * cx);
+  const uint32_t kk = r / cy;
+  j = (int)(r - kk * cy);
+  k = (int)kk;
 }
 
 __device__ __forceinline__ void tload_corners(const Grid& g, int i, int j, int k, float u[8]) {
@@ -554,13 +558,76 @@ __device__ __forceinline__ void edge_vertex_f64(const Grid& g, int i, int j, int
   }
 }
 
-__global__ void __launch_bounds__(128) tmc_emit_kernel(Grid g, const uint32_t* rec, const int32_t* voff,
-                                                       const int32_t* toff, TmcVertexOut out, int32_t* tris) {
-  const int64_t n = g.ncells();
-  for (int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; cell < n;
-       cell += (int64_t)gridDim.x * blockDim.x) {
+// edge vertex in float32 (positions within an ulp: the grid coordinate i + l is formed exactly as a
+// float pair); the float64 variant above is used when float64 positions are requested
+__device__ __forceinline__ void tmc_gradient_f(const Grid& g, int i, int j, int k, const float inv[3],
+                                               const float inv2[3], float out[3]) {
+  if (i == 0) out[0] = (g.at(i + 1, j, k) - g.at(i, j, k)) * inv[0];
+  else if (i == g.nx - 1) out[0] = (g.at(i, j, k) - g.at(i - 1, j, k)) * inv[0];
+  else out[0] = (g.at(i + 1, j, k) - g.at(i - 1, j, k)) * inv2[0];
+  if (j == 0) out[1] = (g.at(i, j + 1, k) - g.at(i, j, k)) * inv[1];
+  else if (j == g.ny - 1) out[1] = (g.at(i, j, k) - g.at(i, j - 1, k)) * inv[1];
+  else out[1] = (g.at(i, j + 1, k) - g.at(i, j - 1, k)) * inv2[1];
+  if (k == 0) out[2] = (g.at(i, j, k + 1) - g.at(i, j, k)) * inv[2];
+  else if (k == g.nz - 1) out[2] = (g.at(i, j, k) - g.at(i, j, k - 1)) * inv[2];
+  else out[2] = (g.at(i, j, k + 1) - g.at(i, j, k - 1)) * inv2[2];
+}
+
+__device__ __forceinline__ void edge_vertex_f32(const Grid& g, int i, int j, int k, int e, const float u[8],
+                                                const TmcVertexOut& out, int32_t idx, const float inv[3],
+                                                const float inv2[3]) {
+  const int v0 = edge_v0(e), v1 = edge_v1(e), ax = edge_axis(e);
+  const float F0 = u[v0], F1 = u[v1];
+  const float l = ((float)g.iso - F0) / (F1 - F0);
+  const int i0 = i + (v0 & 1), j0 = j + ((v0 >> 1) & 1), k0 = k + ((v0 >> 2) & 1);
+  const int i1 = i + (v1 & 1), j1 = j + ((v1 >> 1) & 1), k1 = k + ((v1 >> 2) & 1);
+  const int gi[3] = {i0, j0, k0};
+  const double o[3] = {g.ox, g.oy, g.oz}, dd[3] = {g.dx, g.dy, g.dz};
+  const int64_t base = 3 * (int64_t)idx;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    // origin + (index + l) * spacing, with index + l exact as a float pair
+    const ffx::ff t = (d == ax) ? ffx::two_sum((float)gi[d], l) : ffx::ff_from((float)gi[d]);
+    const ffx::ff x = ffx::ff_add(ffx::ff_from_double(o[d]), ffx::ff_mul(t, ffx::ff_from_double(dd[d])));
+    out.v[base + d] = x.hi + x.lo;
+  }
+  float n0[3], n1[3];
+  tmc_gradient_f(g, i0, j0, k0, inv, inv2, n0);
+  tmc_gradient_f(g, i1, j1, k1, inv, inv2, n1);
+  float in[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) in[d] = fmaf(l, n1[d] - n0[d], n0[d]);
+  const float rn = rsqrtf(in[0] * in[0] + in[1] * in[1] + in[2] * in[2]);
+#pragma unroll
+  for (int d = 0; d < 3; d++) out.n[base + d] = in[d] * rn;
+}
+
+__device__ __forceinline__ void tmc_vertex_ids(const Grid& g, int i, int j, int k, uint32_t em, uint32_t own,
+                                               int32_t vbase, const uint32_t* rec, const int32_t* voff,
+                                               int32_t vid[12]) {
+  int rank = 0;
+  for (int e = 0; e < 12; e++) {
+    vid[e] = -1;
+    if (!(em & (1u << e))) continue;
+    if (own & (1u << e)) {
+      vid[e] = vbase + rank++;
+    } else {
+      int oi, oj, ok, oe = 0;
+      edge_owner(i, j, k, e, oi, oj, ok, oe);
+      const int64_t oc = g.cell_index(oi, oj, ok);
+      vid[e] = voff[oc] + __popc(trec_owned(rec[oc]) & ((1u << oe) - 1u));
+    }
+  }
+}
+
+// Ambiguous cells (listed by the emit kernel): p_slice triangles and inner vertices, float64.
+__global__ void __launch_bounds__(128) tmc_ambiguous_kernel(Grid g, const uint32_t* rec, const int32_t* voff,
+                                                            const int32_t* toff, TmcVertexOut out, int32_t* tris,
+                                                            const uint32_t* list, const unsigned* count) {
+  const unsigned na = *count;
+  for (unsigned a = blockIdx.x * blockDim.x + threadIdx.x; a < na; a += gridDim.x * blockDim.x) {
+    const int64_t cell = list[a];
     const uint32_t r = rec[cell];
-    if (r == 0) continue;
     int i, j, k;
     tcell_ijk(g, cell, i, j, k);
     float u[8];
@@ -570,41 +637,105 @@ __global__ void __launch_bounds__(128) tmc_emit_kernel(Grid g, const uint32_t* r
     for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
     const uint32_t em = case_edge_mask(cs);
     const uint32_t own = trec_owned(r);
-    const int32_t vbase = voff[cell];
-    // owned edge vertices, in edge order
     int32_t vid[12];
-    int rank = 0;
-    for (int e = 0; e < 12; e++) {
-      vid[e] = -1;
-      if (!(em & (1u << e))) continue;
-      if (own & (1u << e)) {
-        vid[e] = vbase + rank;
-        edge_vertex_f64(g, i, j, k, e, u, out, vid[e]);
-        rank++;
-      } else {
-        int oi, oj, ok, oe = 0;
-        edge_owner(i, j, k, e, oi, oj, ok, oe);
-        const int64_t oc = g.cell_index(oi, oj, ok);
-        const uint32_t orec = rec[oc];
-        vid[e] = voff[oc] + __popc(trec_owned(orec) & ((1u << oe) - 1u));
-      }
-    }
+    tmc_vertex_ids(g, i, j, k, em, own, voff[cell], rec, voff, vid);
     TriSink ts{tris + 3 * (int64_t)toff[cell], 0};
-    if (!((r >> 21) & 1)) {
-      // unambiguous: table triangles with reversed winding (t_mc, mc/MarchingCubes.cpp:276-294)
-      const uint64_t tw = c_tmc_tris[cs];
-      const int nt = (int)(tw & 0xF);
-      for (int t = 0; t < nt; t++) {
-        const int e0 = (int)((tw >> (4 + 12 * t)) & 0xF), e1 = (int)((tw >> (8 + 12 * t)) & 0xF),
-                  e2 = (int)((tw >> (12 + 12 * t)) & 0xF);
-        ts.put(vid[e2], vid[e1], vid[e0]);
-      }
-    } else if (!((r >> 22) & 1)) {
-      AmbCell a;
-      load_amb_cell(g, i, j, k, u, em, a, true);
-      InnerOut io{out.v, out.n, out.v64};
-      p_slice_dev(cs, a.F, g.iso, a.ec, vid, vbase + rank, ts, a.P, a.N, &io);
+    AmbCell amb;
+    load_amb_cell(g, i, j, k, u, em, amb, true);
+    InnerOut io{out.v, out.n, out.v64};
+    p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, voff[cell] + __popc(own), ts, amb.P, amb.N, &io);
+  }
+}
+
+__global__ void __launch_bounds__(256) tmc_emit_kernel(Grid g, const uint32_t* rec, const int32_t* voff,
+                                                       const int32_t* toff, TmcVertexOut out, int32_t* tris,
+                                                       uint32_t* amb_list, unsigned* amb_count) {
+  // One block per scan tile: the tile's active cells are compacted into shared memory with warp
+  // ballots, then processed one per thread.
+  __shared__ uint32_t active[kScanTile];
+  __shared__ int wcount[kScanThreads / 32];
+  __shared__ int total;
+  const int64_t n = g.ncells();
+  const float inv[3] = {(float)(1.0 / g.dx), (float)(1.0 / g.dy), (float)(1.0 / g.dz)};
+  const float inv2[3] = {(float)(1.0 / (2 * g.dx)), (float)(1.0 / (2 * g.dy)), (float)(1.0 / (2 * g.dz))};
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int64_t tile = blockIdx.x; tile * kScanTile < n; tile += gridDim.x) {
+    const int64_t base = tile * kScanTile;
+    // compaction: thread t looks at cells base + s*256 + t
+    int mine = 0;
+    bool act[kScanItems];
+#pragma unroll
+    for (int s = 0; s < kScanItems; s++) {
+      const int64_t c = base + (int64_t)s * kScanThreads + threadIdx.x;
+      act[s] = (c < n) && rec[c] != 0;
+      mine += act[s];
     }
+    int pre = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, pre, o);
+      if (lane >= o) pre += y;
+    }
+    if (lane == 31) wcount[wid] = pre;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int s = 0;
+      for (int w = 0; w < kScanThreads / 32; w++) {
+        const int x = wcount[w];
+        wcount[w] = s;
+        s += x;
+      }
+      total = s;
+    }
+    __syncthreads();
+    int pos = wcount[wid] + pre - mine;
+#pragma unroll
+    for (int s = 0; s < kScanItems; s++)
+      if (act[s]) active[pos++] = (uint32_t)(s * kScanThreads + threadIdx.x);
+    __syncthreads();
+    const int na = total;
+    for (int a = threadIdx.x; a < na; a += blockDim.x) {
+      const int64_t cell = base + active[a];
+      const uint32_t r = rec[cell];
+      int i, j, k;
+      tcell_ijk(g, cell, i, j, k);
+      float u[8];
+      tload_corners(g, i, j, k, u);
+      unsigned cs = 0;
+#pragma unroll
+      for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
+      const uint32_t em = case_edge_mask(cs);
+      const uint32_t own = trec_owned(r);
+      const int32_t vbase = voff[cell];
+      // owned edge vertices, in edge order
+      int rank = 0;
+      for (int e = 0; e < 12; e++) {
+        if ((em & own) & (1u << e)) {
+          if (out.v64) edge_vertex_f64(g, i, j, k, e, u, out, vbase + rank);
+          else edge_vertex_f32(g, i, j, k, e, u, out, vbase + rank, inv, inv2);
+          rank++;
+        }
+      }
+      if ((r >> 21) & 1) {
+        // ambiguous: triangles and inner vertices in a separate float64 pass
+        if (!((r >> 22) & 1)) amb_list[atomicAdd(amb_count, 1u)] = (uint32_t)cell;
+        continue;
+      }
+      int32_t vid[12];
+      tmc_vertex_ids(g, i, j, k, em, own, vbase, rec, voff, vid);
+      TriSink ts{tris + 3 * (int64_t)toff[cell], 0};
+      {
+        // unambiguous: table triangles with reversed winding (t_mc, mc/MarchingCubes.cpp:276-294)
+        const uint64_t tw = c_tmc_tris[cs];
+        const int nt = (int)(tw & 0xF);
+        for (int t = 0; t < nt; t++) {
+          const int e0 = (int)((tw >> (4 + 12 * t)) & 0xF), e1 = (int)((tw >> (8 + 12 * t)) & 0xF),
+                    e2 = (int)((tw >> (12 + 12 * t)) & 0xF);
+          ts.put(vid[e2], vid[e1], vid[e0]);
+        }
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -629,10 +760,15 @@ int tmc_count(const Grid& g, TmcScratch& s, cudaStream_t st, Prof* prof) {
 int tmc_emit(const Grid& g, TmcScratch& s, TmcVertexOut vo, int32_t* tris, int sms, cudaStream_t st,
              Prof* prof) {
   Stage t(prof, "tmc_emit", st);
-  const int64_t n = g.ncells();
-  const int64_t blocks = std::min<int64_t>(ceil_div(n, 128), (int64_t)sms * 16);
-  tmc_emit_kernel<<<(unsigned)blocks, 128, 0, st>>>(g, s.rec, s.voff, s.toff, vo, tris);
-  return 1;
+  const int64_t tiles = tmc_tiles(g);
+  const int64_t blocks = std::min<int64_t>(tiles, (int64_t)sms * 8);
+  cudaMemsetAsync(s.amb_count, 0, sizeof(unsigned), st);
+  tmc_emit_kernel<<<(unsigned)blocks, kScanThreads, 0, st>>>(g, s.rec, s.voff, s.toff, vo, tris, s.amb_list,
+                                                            s.amb_count);
+  Stage t2(prof, "tmc_ambiguous", st);
+  tmc_ambiguous_kernel<<<(unsigned)std::max<int64_t>(1, (int64_t)sms * 8), 128, 0, st>>>(g, s.rec, s.voff, s.toff, vo,
+                                                                                         tris, s.amb_list, s.amb_count);
+  return 2;
 }
 
 }  // namespace tmc

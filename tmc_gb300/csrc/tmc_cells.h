@@ -21,6 +21,8 @@ struct TmcScratch {
   unsigned long long* tile_sums;
   unsigned long long* totals;
   unsigned long long* stats;
+  uint32_t* amb_list;   // ambiguous cells with triangles, filled by the emit kernel
+  unsigned* amb_count;
 };
 
 int64_t tmc_tiles(const Grid& g);
