@@ -187,13 +187,16 @@ __global__ void __launch_bounds__(kScanThreads) dmc_offsets_kernel(int64_t n, co
 // estimateGradient at a grid point (cpp_dmc/UniformGrid.cpp:512-540): central differences with
 // the reference's border indexing ((i<0) ? 0 : (i>=max) ? max-i : i).
 __device__ __forceinline__ int grad_index(int i, int max) { return (i < 0) ? 0 : (i >= max) ? max - i : i; }
-__device__ __forceinline__ void point_gradient(const Grid& g, int i, int j, int k, double out[3]) {
+// float64 gradient with reciprocal spacing (normals are compared within a tolerance; the
+// reciprocal saves 24 float64 divisions per vertex)
+__device__ __forceinline__ void point_gradient(const Grid& g, int i, int j, int k, const double inv2d[3],
+                                               double out[3]) {
   const int i0 = grad_index(i - 1, g.nx), i1 = grad_index(i + 1, g.nx);
   const int j0 = grad_index(j - 1, g.ny), j1 = grad_index(j + 1, g.ny);
   const int k0 = grad_index(k - 1, g.nz), k1 = grad_index(k + 1, g.nz);
-  out[0] = ((double)g.at(i1, j, k) - (double)g.at(i0, j, k)) / (2 * g.dx);
-  out[1] = ((double)g.at(i, j1, k) - (double)g.at(i, j0, k)) / (2 * g.dy);
-  out[2] = ((double)g.at(i, j, k1) - (double)g.at(i, j, k0)) / (2 * g.dz);
+  out[0] = ((double)g.at(i1, j, k) - (double)g.at(i0, j, k)) * inv2d[0];
+  out[1] = ((double)g.at(i, j1, k) - (double)g.at(i, j0, k)) * inv2d[1];
+  out[2] = ((double)g.at(i, j, k1) - (double)g.at(i, j, k0)) * inv2d[2];
 }
 __device__ __forceinline__ void point_gradient_f(const Grid& g, int i, int j, int k, float inv2d[3], float out[3]) {
   const int i0 = grad_index(i - 1, g.nx), i1 = grad_index(i + 1, g.nx);
@@ -276,9 +279,11 @@ __global__ void __launch_bounds__(128) dmc_vertex_kernel(Grid g, const int32_t* 
     // normal: trilinear interpolation of the 8 corner gradients, normalised (UniformGrid::normal,
     // cpp_dmc/UniformGrid.h:286-298); float64 when it is kept for the simplification merges
     if (out.n64) {
+      const double inv2dd[3] = {1.0 / (2 * g.dx), 1.0 / (2 * g.dy), 1.0 / (2 * g.dz)};
       double G[8][3];
 #pragma unroll
-      for (int q = 0; q < 8; q++) point_gradient(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), G[q]);
+      for (int q = 0; q < 8; q++)
+        point_gradient(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), inv2dd, G[q]);
       double nv3[3];
       const double uu = p[0], vv = p[1], ww = p[2];
 #pragma unroll

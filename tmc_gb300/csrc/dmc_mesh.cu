@@ -319,14 +319,8 @@ __global__ void fill_i32_kernel(int32_t* p, int64_t n, int32_t v) {
 // cases (the host library's acosf is not, so splits decided by a 1-ulp tie may differ)
 __device__ __forceinline__ float acos_f(float x) { return (float)acos((double)x); }
 
-__device__ __forceinline__ double min_angle(const double* p0, const double* p1, const double* p2) {
-  auto dist = [](const double* a, const double* b) {
-    const double d = (a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]);
-    return sqrt(d);
-  };
-  const float a = dist(p0, p1);
-  const float b = dist(p1, p2);
-  const float c = dist(p2, p0);
+// minAngle exactly as the reference (three acos, float min)
+__device__ __forceinline__ float min_angle_full(float a, float b, float c) {
   const float A = acos_f((b * b + c * c - a * a) / (2 * b * c));
   const float B = acos_f((a * a + c * c - b * b) / (2 * a * c));
   const float C = acos_f((b * b + a * a - c * c) / (2 * b * a));
@@ -334,19 +328,59 @@ __device__ __forceinline__ double min_angle(const double* p0, const double* p1, 
   return (C < mAB) ? C : mAB;
 }
 
+// The smallest angle is the acos of the largest cosine (acos is monotone); false when a cosine is
+// not a number in [-1, 1], where the reference's min of NaNs is replayed instead.
+__device__ __forceinline__ bool max_cosine(float a, float b, float c, float& m) {
+  const float cA = (b * b + c * c - a * a) / (2 * b * c);
+  const float cB = (a * a + c * c - b * b) / (2 * a * c);
+  const float cC = (b * b + a * a - c * c) / (2 * b * a);
+  if (!(cA >= -1.f && cA <= 1.f && cB >= -1.f && cB <= 1.f && cC >= -1.f && cC <= 1.f)) return false;
+  m = fmaxf(cA, fmaxf(cB, cC));
+  return true;
+}
+
+__device__ __forceinline__ float side(const double* p, const double* q) {
+  const double d = (p[0] - q[0]) * (p[0] - q[0]) + (p[1] - q[1]) * (p[1] - q[1]) + (p[2] - q[2]) * (p[2] - q[2]);
+  return (float)sqrt(d);
+}
+
+// collectTriangles (:1387-1460).  Six distinct side lengths (float of a float64 distance, as the
+// reference), four largest cosines in float32; acos only where two candidate angles are within a
+// few ulps of each other.
 __global__ void triangles_kernel(const int32_t* q, int64_t nq, const double* v64, int32_t* t) {
   FOR_EACH(i, nq) {
     const int v0 = q[4 * i], v1 = q[4 * i + 1], v2 = q[4 * i + 2], v3 = q[4 * i + 3];
     const double *P0 = v64 + 3 * (int64_t)v0, *P1 = v64 + 3 * (int64_t)v1, *P2 = v64 + 3 * (int64_t)v2,
                  *P3 = v64 + 3 * (int64_t)v3;
-    double a1 = min_angle(P0, P1, P2);
-    double a2 = min_angle(P0, P2, P3);
-    const double b1 = a2 < a1 ? a2 : a1, b2 = a1 < a2 ? a2 : a1;
-    a1 = min_angle(P1, P3, P0);
-    a2 = min_angle(P1, P2, P3);
-    const double c1 = a2 < a1 ? a2 : a1, c2 = a1 < a2 ? a2 : a1;
+    const float d01 = side(P0, P1), d12 = side(P1, P2), d20 = side(P2, P0), d23 = side(P2, P3), d30 = side(P3, P0),
+                d13 = side(P1, P3);
+    // triangles (v0,v1,v2), (v0,v2,v3) | (v1,v3,v0), (v1,v2,v3); sides a = |p0p1|, b = |p1p2|, c = |p2p0|
+    float m1, m2, m3, m4;
+    bool ok = max_cosine(d01, d12, d20, m1) && max_cosine(d20, d23, d30, m2) && max_cosine(d13, d30, d01, m3) &&
+              max_cosine(d12, d23, d13, m4);
+    bool first;  // true: split along v1-v3
+    if (ok) {
+      // b1 = min angle of the first split, b2 = max; c1, c2 for the second
+      const float xb1 = fmaxf(m1, m2), xb2 = fminf(m1, m2), xc1 = fmaxf(m3, m4), xc2 = fminf(m3, m4);
+      float b1 = acosf(xb1), c1 = acosf(xc1);
+      const float tol = 4.0f * 1.2e-7f * fmaxf(fabsf(b1), fabsf(c1)) + 1e-30f;
+      if (fabsf(b1 - c1) > tol) {
+        first = b1 < c1;
+      } else {
+        b1 = acos_f(xb1);
+        c1 = acos_f(xc1);
+        if (b1 != c1) first = b1 < c1;
+        else first = acos_f(xb2) <= acos_f(xc2);
+      }
+    } else {
+      const double a1 = min_angle_full(d01, d12, d20), a2 = min_angle_full(d20, d23, d30);
+      const double b1 = a2 < a1 ? a2 : a1, b2 = a1 < a2 ? a2 : a1;
+      const double a3 = min_angle_full(d13, d30, d01), a4 = min_angle_full(d12, d23, d13);
+      const double c1 = a4 < a3 ? a4 : a3, c2 = a3 < a4 ? a4 : a3;
+      first = (b1 < c1 || (b1 == c1 && b2 <= c2));
+    }
     int32_t* o = t + 6 * i;
-    if (b1 < c1 || (b1 == c1 && b2 <= c2)) {
+    if (first) {
       o[0] = v1; o[1] = v3; o[2] = v0; o[3] = v1; o[4] = v2; o[5] = v3;
     } else {
       o[0] = v0; o[1] = v1; o[2] = v2; o[3] = v0; o[4] = v2; o[5] = v3;

@@ -37,13 +37,6 @@ __device__ __forceinline__ uint64_t mix(uint64_t x) {
   return x;
 }
 
-__global__ void he_init_kernel(HeTable t) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < t.size; i += (int64_t)gridDim.x * blockDim.x) {
-    t.keys[i] = kEmpty;
-    t.count[i] = 0;
-  }
-}
-
 __global__ void he_vertex_init_kernel(int32_t* hv, unsigned long long* hv_key, int64_t nv) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (int64_t)gridDim.x * blockDim.x) {
     hv[i] = -1;
@@ -82,30 +75,38 @@ __global__ void he_build_kernel(const int32_t* faces, int P, int64_t nf, int32_t
   }
 }
 
-// one thread per bucket: sort ids, apply the pairing rules
-__global__ void he_twin_kernel(HeTable t, int32_t* he, int32_t* hv, unsigned long long* hv_key,
-                               unsigned long long* non_manifold) {
+// One thread per halfedge.  Edges with two halfedges (the manifold majority) pair without any
+// coordination; an edge with 3 or 4 halfedges is resolved by its lowest halfedge's thread.
+__device__ __forceinline__ int sorted_ids(const HeTable& t, int64_t b, int id[4]) {
+  const int c = min(t.count[b], 4);
+  for (int q = 0; q < 4; q++) id[q] = q < c ? t.ids[4 * b + q] : 0x7fffffff;
+  for (int x = 1; x < c; x++)
+    for (int y = x; y > 0 && id[y - 1] > id[y]; y--) {
+      const int tmp = id[y];
+      id[y] = id[y - 1];
+      id[y - 1] = tmp;
+    }
+  return c;
+}
+
+__global__ void he_twin_kernel(HeTable t, const int32_t* slot_of, int64_t nh, int32_t* he,
+                               unsigned long long* hv_key, unsigned long long* non_manifold) {
   unsigned long long nm = 0;
-  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < t.size; b += (int64_t)gridDim.x * blockDim.x) {
-    if (t.keys[b] == kEmpty) continue;
-    const int c = min(t.count[b], 4);
-    int id[4];
-    for (int q = 0; q < 4; q++) id[q] = q < c ? t.ids[4 * b + q] : 0x7fffffff;
-    // sort the (at most four) halfedge ids: insertion order of the reference
-    for (int x = 1; x < c; x++)
-      for (int y = x; y > 0 && id[y - 1] > id[y]; y--) {
-        const int tmp = id[y];
-        id[y] = id[y - 1];
-        id[y - 1] = tmp;
-      }
+  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = slot_of[h];
+    const int cnt = t.count[b];
+    if (cnt > 4) continue;  // more than four faces at an edge: left unpaired
 #define HE(x) (he + 5 * (int64_t)(x))
-    if (t.count[b] > 4) continue;  // more than four faces at an edge: left unpaired
-    if (c == 1) {
-      HE(id[0])[3] = -1;
-    } else if (c == 2) {
-      HE(id[0])[3] = id[1];
-      HE(id[1])[3] = id[0];
-    } else if (c == 3) {
+    if (cnt == 2) {
+      const int a = t.ids[4 * b], c = t.ids[4 * b + 1];
+      HE(h)[3] = (a == (int)h) ? c : a;
+      continue;
+    }
+    if (cnt == 1) continue;
+    int id[4];
+    const int c = sorted_ids(t, b, id);
+    if (id[0] != (int)h) continue;  // the lowest halfedge resolves the edge
+    if (c == 3) {
       const int e0 = id[0], e1 = id[1], e2 = id[2];
       const int v0 = HE(e0)[0], v1 = HE(e1)[0], v2 = HE(e2)[0];
       HE(e0)[4] = 2;
@@ -138,17 +139,14 @@ __global__ void he_twin_kernel(HeTable t, int32_t* he, int32_t* hv, unsigned lon
   if ((threadIdx.x & 31) == 0 && nm) atomicAdd(non_manifold, nm);
 }
 
-// three-halfedge buckets whose key won the vertex override write the handle
-__global__ void he_override_kernel(HeTable t, const int32_t* he, int32_t* hv, const unsigned long long* hv_key) {
-  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < t.size; b += (int64_t)gridDim.x * blockDim.x) {
-    if (t.keys[b] == kEmpty || t.count[b] != 3) continue;
-    for (int q = 0; q < 3; q++) {
-      const int e = t.ids[4 * b + q];
-      if (he[5 * (int64_t)e + 3] == -1) {
-        const int v = he[5 * (int64_t)e];
-        if (hv_key[v] == t.keys[b] + 1ull) hv[v] = e;
-      }
-    }
+// three-halfedge edges whose key won the vertex override write the handle
+__global__ void he_override_kernel(HeTable t, const int32_t* slot_of, int64_t nh, const int32_t* he, int32_t* hv,
+                                   const unsigned long long* hv_key) {
+  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = slot_of[h];
+    if (t.count[b] != 3 || he[5 * h + 3] != -1) continue;
+    const int v = he[5 * h];
+    if (hv_key[v] == t.keys[b] + 1ull) hv[v] = (int32_t)h;
   }
 }
 
@@ -161,9 +159,10 @@ __global__ void he_pack4_kernel(const int32_t* he5, int64_t nh, int32_t* he4) {
 
 }  // namespace
 
+// Unique edges are about half the halfedges, so a table of >= nh buckets runs at load ~0.5.
 int64_t he_table_size(int64_t nh) {
   int64_t s = 1024;
-  while (s < 2 * nh) s <<= 1;
+  while (s < nh) s <<= 1;
   return s;
 }
 
@@ -172,12 +171,13 @@ int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& 
                     cudaStream_t st) {
   const int64_t nh = nf * P;
   auto grid = [&](int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)sms * 8)); };
-  he_init_kernel<<<grid(t.size), 256, 0, st>>>(t);
+  cudaMemsetAsync(t.keys, 0xFF, (size_t)t.size * sizeof(unsigned long long), st);
+  cudaMemsetAsync(t.count, 0, (size_t)t.size * sizeof(int32_t), st);
   he_vertex_init_kernel<<<grid(nv), 256, 0, st>>>(o.hv, hv_key, nv);
   he_build_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, o.he, o.hv, o.hf, t, slot_of, overflow);
-  he_twin_kernel<<<grid(t.size), 256, 0, st>>>(t, o.he, o.hv, hv_key, non_manifold);
-  he_override_kernel<<<grid(t.size), 256, 0, st>>>(t, o.he, o.hv, hv_key);
-  return 5;
+  he_twin_kernel<<<grid(nh), 256, 0, st>>>(t, slot_of, nh, o.he, hv_key, non_manifold);
+  he_override_kernel<<<grid(nh), 256, 0, st>>>(t, slot_of, nh, o.he, o.hv, hv_key);
+  return 4;
 }
 
 int pack_halfedges4(const int32_t* he5, int64_t nh, int32_t* he4, int sms, cudaStream_t st) {

@@ -1,6 +1,7 @@
 // Host runtime behind the C ABI (include/tmc_gb300.h): contexts, stream-ordered pooled device
 // memory, argument checking, and the extraction drivers that sequence the kernels.
 #include <atomic>
+#include <map>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -29,6 +30,27 @@ struct tmc_ctx {
   unsigned long long* d_stats = nullptr;  // 8 counters, reused per call
   void* h_pinned = nullptr;               // small pinned staging area (totals, stats)
   tmc::Prof prof;                         // stage timings (off unless enabled)
+  // pinned host blocks for TMC_OUT_HOST results, reused across calls (size -> block)
+  std::multimap<size_t, void*> pinned_free;
+  std::map<void*, size_t> pinned_size;
+  void* pinned_get(size_t bytes) {
+    bytes = (bytes + 4095) & ~(size_t)4095;
+    auto it = pinned_free.lower_bound(bytes);
+    if (it != pinned_free.end() && it->first <= 2 * bytes) {
+      void* p = it->second;
+      pinned_free.erase(it);
+      return p;
+    }
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+    pinned_size[p] = bytes;
+    return p;
+  }
+  void pinned_put(void* p) {
+    auto it = pinned_size.find(p);
+    if (it == pinned_size.end()) return;
+    pinned_free.emplace(it->second, p);
+  }
 };
 
 namespace {
@@ -143,7 +165,7 @@ void mesh_reset(tmc_mesh* m) { std::memset(m, 0, sizeof(*m)); }
 template <typename T>
 tmc_status to_host(tmc_ctx* ctx, T** p, size_t count, MeshPriv* mp) {
   if (!*p) return TMC_OK;
-  T* h = (T*)std::malloc(count ? count * sizeof(T) : 16);
+  T* h = (T*)ctx->pinned_get(count ? count * sizeof(T) : 16);
   if (!h) return fail(ctx, TMC_ERR_OOM, "host allocation of %zu bytes failed", count * sizeof(T));
   if (count) TMC_CUDA(ctx, cudaMemcpyAsync(h, *p, count * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
   mp->host.push_back(h);
@@ -221,6 +243,7 @@ tmc_status tmc_ctx_destroy(tmc_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->d_stats) cudaFree(ctx->d_stats);
+  for (auto& kv : ctx->pinned_size) cudaFreeHost(kv.first);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -270,7 +293,8 @@ tmc_status tmc_mesh_free(tmc_ctx* ctx, tmc_mesh* mesh) {
   if (mp) {
     cudaSetDevice(ctx->device);
     for (void* p : mp->dev) cudaFreeAsync(p, ctx->stream);
-    for (void* p : mp->host) std::free(p);
+    cudaStreamSynchronize(ctx->stream);  // the next call may reuse these pinned blocks
+    for (void* p : mp->host) ctx->pinned_put(p);
     delete mp;
   }
   mesh_reset(mesh);

@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(kScanThreads) tmc_classify_kernel(Grid g, uint
                                                                    unsigned long long* stats) {
   const int64_t n = g.ncells();
   const int64_t base = (int64_t)blockIdx.x * kScanTile;
-  unsigned long long local = 0, act = 0, amb = 0, sing = 0;
+  unsigned long long local = 0, act = 0, amb = 0;
   for (int s = 0; s < kScanItems; s++) {
     const int64_t c = base + (int64_t)s * kScanThreads + threadIdx.x;
     if (c >= n) break;
@@ -476,15 +476,9 @@ __global__ void __launch_bounds__(kScanThreads) tmc_classify_kernel(Grid g, uint
       if (!case_ambiguous(cs)) {
         r |= (uint32_t)(c_tmc_tris[cs] & 0xF) << 15;
       } else {
-        AmbCell a;
-        load_amb_cell(g, i, j, k, u, em, a, false);
-        int32_t vid[12];
-        for (int e = 0; e < 12; e++) vid[e] = 0;
-        TriSink ts{nullptr, 0};
-        const AmbResult ar = p_slice_dev(cs, a.F, g.iso, a.ec, vid, 0, ts, a.P, a.N, nullptr);
-        r |= (uint32_t)ar.inner << 12 | (uint32_t)ts.n << 15 | (1u << 21) | (ar.error ? (1u << 22) : 0u);
+        // counted by tmc_amb_count_kernel (dense, float64), which adds to this tile's sums
+        r |= 1u << 21;
         amb++;
-        sing += ar.error;
       }
       act++;
     }
@@ -497,13 +491,93 @@ __global__ void __launch_bounds__(kScanThreads) tmc_classify_kernel(Grid g, uint
   for (int o = 16; o; o >>= 1) {
     act += __shfl_down_sync(0xffffffffu, act, o);
     amb += __shfl_down_sync(0xffffffffu, amb, o);
-    sing += __shfl_down_sync(0xffffffffu, sing, o);
   }
-  if ((threadIdx.x & 31) == 0 && (act | amb | sing)) {
+  if ((threadIdx.x & 31) == 0 && (act | amb)) {
     atomicAdd(stats + 0, act);
     atomicAdd(stats + 1, amb);
-    atomicAdd(stats + 5, sing);
   }
+}
+
+// Block-wide compaction of the cells of one tile that satisfy `pred` into list[0..return).
+template <typename Pred>
+__device__ __forceinline__ int compact_tile(const uint32_t* rec, int64_t base, int64_t n, Pred pred, uint32_t* list,
+                                            int* wcount, int* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  bool act[kScanItems];
+  int mine = 0;
+#pragma unroll
+  for (int s = 0; s < kScanItems; s++) {
+    const int64_t c = base + (int64_t)s * kScanThreads + threadIdx.x;
+    act[s] = (c < n) && pred(rec[c]);
+    mine += act[s];
+  }
+  int pre = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, pre, o);
+    if (lane >= o) pre += y;
+  }
+  if (lane == 31) wcount[wid] = pre;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int w = 0; w < kScanThreads / 32; w++) {
+      const int x = wcount[w];
+      wcount[w] = s;
+      s += x;
+    }
+    *total = s;
+  }
+  __syncthreads();
+  int pos = wcount[wid] + pre - mine;
+#pragma unroll
+  for (int s = 0; s < kScanItems; s++)
+    if (act[s]) list[pos++] = (uint32_t)(s * kScanThreads + threadIdx.x);
+  __syncthreads();
+  return *total;
+}
+
+// Ambiguous cells of each tile, densely: p_slice in counting mode (float64), then the counts go into
+// the cell record and the tile's sum.
+__global__ void __launch_bounds__(kScanThreads) tmc_amb_count_kernel(Grid g, uint32_t* rec,
+                                                                    unsigned long long* tile_sums,
+                                                                    unsigned long long* stats) {
+  __shared__ uint32_t list[kScanTile];
+  __shared__ int wcount[kScanThreads / 32];
+  __shared__ int total;
+  __shared__ unsigned long long add;
+  const int64_t n = g.ncells();
+  unsigned long long sing = 0;
+  for (int64_t tile = blockIdx.x; tile * kScanTile < n; tile += gridDim.x) {
+    const int64_t base = tile * kScanTile;
+    if (threadIdx.x == 0) add = 0;
+    const int na = compact_tile(rec, base, n, [](uint32_t r) { return ((r >> 21) & 1) != 0; }, list, wcount, &total);
+    unsigned long long local = 0;
+    for (int a = threadIdx.x; a < na; a += blockDim.x) {
+      const int64_t cell = base + list[a];
+      int i, j, k;
+      tcell_ijk(g, cell, i, j, k);
+      float u[8];
+      tload_corners(g, i, j, k, u);
+      unsigned cs = 0;
+#pragma unroll
+      for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
+      AmbCell amb;
+      load_amb_cell(g, i, j, k, u, case_edge_mask(cs), amb, false);
+      int32_t vid[12];
+      for (int e = 0; e < 12; e++) vid[e] = 0;
+      TriSink ts{nullptr, 0};
+      const AmbResult ar = p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, 0, ts, amb.P, amb.N, nullptr);
+      rec[cell] |= (uint32_t)ar.inner << 12 | (uint32_t)ts.n << 15 | (ar.error ? (1u << 22) : 0u);
+      local += ((unsigned long long)ar.inner << 32) | (unsigned long long)ts.n;
+      sing += ar.error;
+    }
+    if (local) atomicAdd(&add, local);
+    __syncthreads();
+    if (threadIdx.x == 0 && add) tile_sums[tile] += add;
+    __syncthreads();
+  }
+  if (sing) atomicAdd(stats + 5, sing);
 }
 
 __global__ void __launch_bounds__(kScanThreads) tmc_offsets_kernel(int64_t n, const uint32_t* rec,
@@ -751,10 +825,15 @@ int tmc_count(const Grid& g, TmcScratch& s, cudaStream_t st, Prof* prof) {
     Stage t(prof, "tmc_classify", st);
     tmc_classify_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(g, s.rec, s.tile_sums, s.stats);
   }
+  {
+    Stage ta(prof, "tmc_amb_count", st);
+    tmc_amb_count_kernel<<<(unsigned)std::min<int64_t>(tiles, 65535), kScanThreads, 0, st>>>(g, s.rec, s.tile_sums,
+                                                                                              s.stats);
+  }
   Stage t(prof, "tmc_scan", st);
   scan_tile_sums_kernel<<<1, 1024, 0, st>>>(s.tile_sums, tiles, s.totals);
   tmc_offsets_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(n, s.rec, s.tile_sums, s.voff, s.toff);
-  return 3;
+  return 4;
 }
 
 int tmc_emit(const Grid& g, TmcScratch& s, TmcVertexOut vo, int32_t* tris, int sms, cudaStream_t st,
