@@ -11,6 +11,7 @@
 
 using namespace tmc;
 
+static long g_decider_mismatch = 0;
 static uint64_t polygon(unsigned cs, const float u[8], double iso) {
   if (!case_ambiguous(cs)) return table_contour(TMC_CASE_CONTOUR[cs]);
   uint64_t to = ~0ull;
@@ -18,7 +19,12 @@ static uint64_t polygon(unsigned cs, const float u[8], double iso) {
     const uint32_t fv = face_v_pack(f);
     const int fc = face_case(cs, fv);
     int sep = 0;
-    if (fc == 6 || fc == 9) sep = decider(u[nib(fv, 0)], u[nib(fv, 1)], u[nib(fv, 2)], u[nib(fv, 3)]) >= iso;
+    if (fc == 6 || fc == 9) {
+      const float a = u[nib(fv, 0)], b = u[nib(fv, 1)], c = u[nib(fv, 2)], d = u[nib(fv, 3)];
+      sep = decider(a, b, c, d) >= iso;
+      // the float-float decision used on the GPU must agree
+      if (decider_ge(a, b, c, d, iso, ffx::ff_from_double(iso)) != (bool)sep) g_decider_mismatch++;
+    }
     face_segments(fc, sep, face_e_pack(f), to);
   }
   return connect_contours(to, case_edge_mask(cs));
@@ -69,11 +75,12 @@ int main(int argc, char** argv) {
         }
         for (int t = 0; t < n; t++) {
           const int sz = cnt_size(c, t);
-          double pe[3];
-          repr::mean_point_exact(pts[t], sz, pe);
+          const repr::Point64 pm = repr::mean_point_exact(pts[t], sz);
+          double pe[3] = {pm.p[0], pm.p[1], pm.p[2]};
           repr::representative_exact(u, iso, c, t, pe, bx, se);
           float pf[3];
-          repr::representative_fast(u, iso, c, t, pts[t], sz, bx, pf, sf);
+          float lb[49];
+          repr::representative_fast(u, iso, c, t, pts[t], sz, bx, pf, sf, lb, 1);
           contours++;
           if ((float)pe[0] != pf[0] || (float)pe[1] != pf[1] || (float)pe[2] != pf[2]) {
             if (mism < 5)
@@ -83,6 +90,7 @@ int main(int argc, char** argv) {
           }
         }
       }
+  mism += g_decider_mismatch;
   printf("%ld %ld %d %d %d %d %d\n", contours, mism, sf.fallback, sf.fail1, sf.fail2, se.fail1, se.fail2);
   return 0;
 }

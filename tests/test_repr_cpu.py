@@ -32,6 +32,7 @@ def _cases():
     V.seed_saddles(sad, rng, frac=0.5)
     return {
         "noise40": V.small_noise_volume(40, seed=5, coarse=7),
+        "noise28": V.small_noise_volume(28, seed=21, coarse=5),
         "blobs48": V.blobs_volume(48, seed=0),
         "saddle25": V.Volume(sad, spacing=(2 / 24,) * 3, iso=0.0),
         "batch2": V.batch_volumes(3, seed=2)[2],

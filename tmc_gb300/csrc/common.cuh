@@ -9,6 +9,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "ffloat.cuh"
 #include "mc_tables.h"
 
 namespace tmc {
@@ -157,20 +158,40 @@ __host__ __device__ __forceinline__ uint64_t table_contour(uint64_t w) {
   return (w >> 4) | ((uint64_t)sz << 48);
 }
 
+// decider(f0..f3) >= iso, decided in float-float when the margin is clear, else in float64.
+// The reference evaluates (f0*f3 - f1*f2) / (f0 + f3 - f1 - f2) in double: the products are exact,
+// the difference and the sum round once or twice; both are reproduced within ~2^-46.
+// Out of line: ambiguous faces are rare and six inlined copies would bloat every caller.
+inline __host__ __device__ __noinline__ bool decider_ge(float f0, float f1, float f2, float f3, double iso,
+                                                 ffx::ff iso_ff) {
+  using namespace ffx;
+  const ff a = two_prod(f0, f3), b = two_prod(f1, f2);
+  const ff num = ff_sub(a, b);
+  const ff den = ff_sub(ff_sub(ff_add(ff_from(f0), ff_from(f3)), ff_from(f1)), ff_from(f2));
+  if (den.hi != 0.0f) {
+    const ff q = ff_div(num, den);
+    const ff d = ff_sub(q, iso_ff);
+    const float mag = fabsf(a.hi) + fabsf(b.hi);
+    const float err = mag * 0x1p-44f / fabsf(den.hi) + fabsf(q.hi) * 0x1p-44f + fabsf(iso_ff.hi) * 0x1p-46f +
+                      (fabsf(f0) + fabsf(f1) + fabsf(f2) + fabsf(f3)) * 0x1p-44f * fabsf(q.hi) / fabsf(den.hi);
+    if (d.hi > err) return true;
+    if (d.hi < -err) return false;
+  }
+  return decider(f0, f1, f2, f3) >= iso;
+}
+
 // DMC MC polygon (mc_polygon, cpp_dmc/DualMarchingCubes.cpp:328-487): table contour for the
-// unambiguous cases, face rules with the float64 decider (>= iso) for the ambiguous ones.
+// unambiguous cases, face rules with the decider (>= iso) for the ambiguous ones.
 __device__ __forceinline__ uint64_t dmc_polygon(unsigned cs, const float u[8], double iso, const uint64_t* case_contour) {
   if (!case_ambiguous(cs)) return table_contour(case_contour[cs]);
+  const ffx::ff iso_ff = ffx::ff_from_double(iso);
   uint64_t to = ~0ull;
 #pragma unroll
   for (int f = 0; f < 6; f++) {
     const uint32_t fv = face_v_pack(f);
     const int fc = face_case(cs, fv);
     int sep = 0;
-    if (fc == 6 || fc == 9) {
-      const double val = decider(u[nib(fv, 0)], u[nib(fv, 1)], u[nib(fv, 2)], u[nib(fv, 3)]);
-      sep = val >= iso;
-    }
+    if (fc == 6 || fc == 9) sep = decider_ge(u[nib(fv, 0)], u[nib(fv, 1)], u[nib(fv, 2)], u[nib(fv, 3)], iso, iso_ff);
     face_segments(fc, sep, face_e_pack(f), to);
   }
   return connect_contours(to, case_edge_mask(cs));

@@ -207,10 +207,12 @@ __device__ __forceinline__ void point_gradient_f(const Grid& g, int i, int j, in
   out[2] = (g.at(i, j, k1) - g.at(i, j, k0)) * inv2d[2];
 }
 
-__global__ void __launch_bounds__(128) dmc_vertex_kernel(Grid g, const int32_t* voff, const uint32_t* vwork,
+constexpr int kVertexThreads = 128;
+__global__ void __launch_bounds__(kVertexThreads) dmc_vertex_kernel(Grid g, const int32_t* voff, const uint32_t* vwork,
                                                          int64_t nv, DmcVertexOut out, int flip,
                                                          unsigned long long* stats) {
   __shared__ uint64_t cc[256];
+  __shared__ float sample_lb[49 * kVertexThreads];  // per-thread sample bounds, column per thread
   for (int c = threadIdx.x; c < 256; c += blockDim.x) cc[c] = c_case_contour[c];
   __syncthreads();
   repr::Stats st;
@@ -262,7 +264,8 @@ __global__ void __launch_bounds__(128) dmc_vertex_kernel(Grid g, const int32_t* 
     }
     if (tsel < 0) continue;  // cannot happen: the record counted this vertex
     float p[3];
-    repr::representative_fast(u, g.iso, c, tsel, pts + 3 * tstart, cnt_size(c, tsel), bx, p, st);
+    repr::representative_fast(u, g.iso, c, tsel, pts + 3 * tstart, cnt_size(c, tsel), bx, p, st,
+                              sample_lb + threadIdx.x, kVertexThreads);
     const int64_t o = 3 * vidx;
     // position: UniformGrid::position (cpp_dmc/UniformGrid.h:300-305)
     const double px = g.ox + (i + (double)p[0]) * g.dx;
@@ -418,7 +421,7 @@ int dmc_front_emit(const Grid& g, DmcScratch& s, DmcVertexOut vo, int64_t nv, in
   {
     Stage t(prof, "dmc_vertex", st);
     const int64_t vb = std::max<int64_t>(1, std::min<int64_t>(ceil_div(nv, 128), (int64_t)sms * 32));
-    dmc_vertex_kernel<<<(unsigned)vb, 128, 0, st>>>(g, s.voff, s.vwork, nv, vo, flip, s.stats);
+    dmc_vertex_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(g, s.voff, s.vwork, nv, vo, flip, s.stats);
   }
   Stage t(prof, "dmc_quad", st);
   dmc_quad_kernel<<<(unsigned)blocks, 128, 0, st>>>(g, s.rec, s.voff, s.qoff, quads, colors);

@@ -413,13 +413,11 @@ struct Pool {
   }
 };
 
-struct HeWork {
+struct HeBufs {
   int32_t* he5 = nullptr;
   int32_t* hv = nullptr;
   int32_t* hf = nullptr;
-  HeTable t{};
-  int32_t* slot = nullptr;
-  unsigned long long* hv_key = nullptr;
+  HeWork w{};
   unsigned long long* nm = nullptr;
   unsigned* ovf = nullptr;
 };
@@ -440,17 +438,19 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
 
   // working mesh (double buffered)
   DmcMesh cur = in;
-  HeWork hw;
+  HeBufs hw;
   hw.he5 = pool.get<int32_t>(5 * 4 * NQ);
   hw.hv = pool.get<int32_t>(NV);
   hw.hf = pool.get<int32_t>(NQ);
-  hw.t.size = he_table_size(4 * NQ);
-  hw.t.keys = pool.get<unsigned long long>(hw.t.size);
-  hw.t.count = pool.get<int32_t>(hw.t.size);
-  hw.t.ids = pool.get<int32_t>(4 * hw.t.size);
-  hw.slot = pool.get<int32_t>(4 * NQ);
-  hw.hv_key = pool.get<unsigned long long>(NV);
+  hw.w.deg = pool.get<int32_t>(NV);
+  hw.w.off = pool.get<int32_t>(NV);
+  hw.w.cursor = pool.get<int32_t>(NV);
+  hw.w.list = pool.get<int2>(4 * NQ);
+  hw.w.hv_key = pool.get<unsigned long long>(NV);
+  hw.w.tiles = pool.get<unsigned long long>(scan_tiles(NV) + 2);
+  hw.w.total = pool.get<unsigned long long>(2);
   hw.nm = pool.get<unsigned long long>(2);
+  hw.w.non_manifold = hw.nm;
   hw.ovf = pool.get<unsigned>(2);
   unsigned long long* tiles = pool.get<unsigned long long>(scan_tiles(4 * NQ) + 2);
   if (hw.ovf) cudaMemsetAsync(hw.ovf, 0, 2 * sizeof(unsigned), st);
@@ -464,7 +464,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     Stage tm(prof, "dmc_halfedges", st);
     cudaMemsetAsync(hw.nm, 0, 2 * sizeof(unsigned long long), st);
     HeOut ho{hw.he5, hw.hv, hw.hf};
-    s.launches += build_halfedges(m.quads, 4, m.nq, m.nv, ho, hw.t, hw.slot, hw.hv_key, hw.nm, hw.ovf, sms, st);
+    s.launches += build_halfedges(m.quads, 4, m.nq, m.nv, ho, hw.w, sms, st);
   };
   auto read_total = [&]() -> int64_t {
     cudaMemcpyAsync(h_cnt, total, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);

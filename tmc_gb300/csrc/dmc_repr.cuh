@@ -45,7 +45,7 @@ struct Stats {
 // ---------------------------------------------------------------------------------------------
 // edge parameter: getLocalCoordinates (cpp_dmc/DualMarchingCubes.h:391-407), l rounded to float
 // ---------------------------------------------------------------------------------------------
-TMC_HD float edge_param_exact(int e, const float u[8], double iso) {
+TMC_HD_COLD float edge_param_exact(int e, const float u[8], double iso) {
   const int v0 = nibr(EDGE_V0, e), v1 = nibr(EDGE_V1, e);
   return (float)((iso - (double)u[v0]) / ((double)u[v1] - (double)u[v0]));
 }
@@ -92,7 +92,7 @@ TMC_HD bool in_neighbor_bbox(double u, double v, double w, uint64_t c, int t, co
 }
 
 TMC_HD bool projection_exact(const double fp[8], double iso, uint64_t c, int t, double p[3], const Boxes& bx, int A,
-                             int B, int W, int nrSamples) {
+                        int B, int W, int nrSamples) {
   const double umin = bx.b[t][A][0], umax = bx.b[t][A][1];
   const double vmin = bx.b[t][B][0], vmax = bx.b[t][B][1];
   const double du = (umax - umin) / (nrSamples - 1);
@@ -170,16 +170,21 @@ TMC_HD int plane_from_extent(const Boxes& bx, int t) {
 }
 
 // the contour's mean point exactly as the reference accumulates it (float64)
-TMC_HD void mean_point_exact(const float* pts, int n, double p[3]) {
-  p[0] = p[1] = p[2] = 0;
+struct Point64 {
+  double p[3];
+};
+TMC_HD_COLD Point64 mean_point_exact(const float* pts, int n) {
+  Point64 r;
+  r.p[0] = r.p[1] = r.p[2] = 0;
   for (int q = 0; q < n; q++) {
-    p[0] += pts[3 * q];
-    p[1] += pts[3 * q + 1];
-    p[2] += pts[3 * q + 2];
+    r.p[0] += pts[3 * q];
+    r.p[1] += pts[3 * q + 1];
+    r.p[2] += pts[3 * q + 2];
   }
-  p[0] /= n;
-  p[1] /= n;
-  p[2] /= n;
+  r.p[0] /= n;
+  r.p[1] /= n;
+  r.p[2] /= n;
+  return r;
 }
 
 // representative with the projection from `prj`; p in: mean point, out: representative
@@ -299,25 +304,33 @@ TMC_HD SampleApprox sample_approx(const ProjCtx& P, float u, float v) {
   return r;
 }
 
+// One exactly evaluated sample.  Results are returned by value: the out-of-line evaluators write
+// nothing through pointers into the caller's frame.
+struct SampleOut {
+  float w, d;
+  int status;  // 0 invalid, 1 valid, 2 rounding not certified (evaluate in float64)
+};
+
 // float64 evaluation of one sample, as the reference's loop body (projection, :298-316)
-TMC_HD void sample_f64(const ProjCtx& P, const double pd[3], float u, float v, bool& valid, float& w_out,
-                       float& d_out) {
+TMC_HD_COLD SampleOut sample_f64(const ProjCtx& P, double pd0, double pd1, double pd2, float u, float v) {
+  SampleOut r{0.0f, 0.0f, 0};
   double fp[8];
   for (int q = 0; q < 8; q++) fp[q] = P.fp[q];
   const float g1 = (1 - v) * ((1 - u) * fp[0] + u * fp[1]) + v * ((1 - u) * fp[2] + u * fp[3]);
   const float g2 = (1 - v) * ((1 - u) * fp[4] + u * fp[5]) + v * ((1 - u) * fp[6] + u * fp[7]);
-  valid = false;
-  if (g1 == g2) return;
+  if (g1 == g2) return r;
   const float w = (P.iso_d - g1) / (g2 - g1);
-  if (!(w >= P.wlo && w <= P.whi)) return;
-  if (P.cnt != 1 && P.cnt_sz != 3 && in_neighbor_bbox(u, v, w, P.c, P.t, *P.bx, P.A, P.B, P.W)) return;
-  valid = true;
-  w_out = w;
-  d_out = (pd[0] - u) * (pd[0] - u) + (pd[1] - v) * (pd[1] - v) + (pd[2] - w) * (pd[2] - w);
+  if (!(w >= P.wlo && w <= P.whi)) return r;
+  if (P.cnt != 1 && P.cnt_sz != 3 && in_neighbor_bbox(u, v, w, P.c, P.t, *P.bx, P.A, P.B, P.W)) return r;
+  r.status = 1;
+  r.w = w;
+  r.d = (pd0 - u) * (pd0 - u) + (pd1 - v) * (pd1 - v) + (pd2 - w) * (pd2 - w);
+  return r;
 }
 
-// exact evaluation of one sample; returns false when a rounding cannot be certified
-TMC_HD bool sample_exact(const ProjCtx& P, float u, float v, bool& valid, float& w_out, float& d_out) {
+// exact evaluation of one sample (status 2 when a rounding cannot be certified)
+TMC_HD_COLD SampleOut sample_exact(const ProjCtx& P, float u, float v) {
+  SampleOut r{0.0f, 0.0f, 2};
   const float omu = 1 - u, omv = 1 - v;
   const float* f = P.fp;
   const ff A1 = ffx::ff_add(ffx::two_prod(omu, f[0]), ffx::two_prod(u, f[1]));
@@ -329,19 +342,19 @@ TMC_HD bool sample_exact(const ProjCtx& P, float u, float v, bool& valid, float&
   const float S1 = fabsf(omv) * (fabsf(omu * f[0]) + fabsf(u * f[1])) + fabsf(v) * (fabsf(omu * f[2]) + fabsf(u * f[3]));
   const float S2 = fabsf(omv) * (fabsf(omu * f[4]) + fabsf(u * f[5])) + fabsf(v) * (fabsf(omu * f[6]) + fabsf(u * f[7]));
   float g1, g2;
-  if (!ffx::ff_round(G1, S1 * 0x1p-45f, g1)) return false;
-  if (!ffx::ff_round(G2, S2 * 0x1p-45f, g2)) return false;
+  if (!ffx::ff_round(G1, S1 * 0x1p-45f, g1)) return r;
+  if (!ffx::ff_round(G2, S2 * 0x1p-45f, g2)) return r;
   if (g1 == g2) {
-    valid = false;
-    return true;
+    r.status = 0;
+    return r;
   }
   const float den = g2 - g1;  // the reference subtracts the two floats
   const ff num = ffx::ff_sub(P.iso_ff, ffx::ff_from(g1));
   const ff W = ffx::ff_div(num, ffx::ff_from(den));
   const float errW = fabsf(W.hi) * 0x1p-42f + (fabsf(P.iso_ff.hi) * 0x1p-46f + fabsf(num.hi) * 0x1p-50f) / fabsf(den);
   float w;
-  if (!ffx::ff_round(W, errW, w)) return false;
-  valid = (w >= P.wlo && w <= P.whi);
+  if (!ffx::ff_round(W, errW, w)) return r;
+  bool valid = (w >= P.wlo && w <= P.whi);
   if (valid && P.cnt != 1 && P.cnt_sz != 3) {
     const Boxes& bx = *P.bx;
     for (int i = 0; i < P.cnt; i++) {
@@ -354,17 +367,21 @@ TMC_HD bool sample_exact(const ProjCtx& P, float u, float v, bool& valid, float&
       }
     }
   }
-  if (!valid) return true;
+  if (!valid) {
+    r.status = 0;
+    return r;
+  }
   const ff d0 = ffx::ff_sub(P.pff[0], ffx::ff_from(u));
   const ff d1 = ffx::ff_sub(P.pff[1], ffx::ff_from(v));
   const ff d2 = ffx::ff_sub(P.pff[2], ffx::ff_from(w));
   const ff D = ffx::ff_add(ffx::ff_add(ffx::ff_mul(d0, d0), ffx::ff_mul(d1, d1)), ffx::ff_mul(d2, d2));
   const float errD = fabsf(D.hi) * 0x1p-40f + (fabsf(d0.hi) + fabsf(d1.hi) + fabsf(d2.hi)) * 0x1p-41f;
   float d;
-  if (!ffx::ff_round(D, errD, d)) return false;
-  w_out = w;
-  d_out = d;
-  return true;
+  if (!ffx::ff_round(D, errD, d)) return r;
+  r.w = w;
+  r.d = d;
+  r.status = 1;
+  return r;
 }
 
 // u_i = fl32(umin + i*(umax-umin)/8) as the reference computes it in float64, for i = 1..7.
@@ -372,7 +389,7 @@ TMC_HD bool sample_exact(const ProjCtx& P, float u, float v, bool& valid, float&
 // float64 computation is exact (at most 24+20+3 significant bits), so the reference rounds the
 // exact value once; the float-float sum is exact too and its high part is that rounding.
 // Otherwise the value is certified, and computed in float64 when that fails.
-TMC_HD float sample_coord_f64(float lo, float hi, int i) {
+TMC_HD_COLD float sample_coord_f64(float lo, float hi, int i) {
   const double du = ((double)hi - (double)lo) / 8;
   return (float)((double)lo + i * du);
 }
@@ -380,6 +397,7 @@ TMC_HD void sample_coords(float lo, float hi, float out[7], int& f64_count) {
   const ff D = ffx::two_sum(hi, -lo);  // exact difference
   const int ehi = (int)((ffx::fbits(hi) >> 23) & 0xFF), elo = (int)((ffx::fbits(lo) >> 23) & 0xFF);
   const bool exact = (lo == 0.0f) || (hi == lo) || (ehi - elo <= 20 && elo > 0);
+#pragma unroll 1
   for (int i = 1; i <= 7; i++) {
     const ff a = ffx::two_prod((float)i, D.hi);
     const ff b = ffx::two_prod((float)i, D.lo);
@@ -399,8 +417,10 @@ TMC_HD void sample_coords(float lo, float hi, float out[7], int& f64_count) {
   }
 }
 
-// 0 = found (pt set), 1 = no valid sample, 2 = cannot certify (use the float64 projection)
-TMC_HD int projection_fast(ProjCtx& P, float pt[3]) {
+// 0 = found (pt set), 1 = no valid sample.  buf: 49 slots (lower bound of each sample's distance,
+// +inf for a certainly invalid sample), slot q at buf[q * stride] (shared memory on the GPU, one
+// column per thread), so that every sample is approximated once.
+TMC_HD int projection_fast(ProjCtx& P, float pt[3], float* buf, int stride) {
   const Boxes& bx = *P.bx;
   const float umin = bx.b[P.t][P.A][0], umax = bx.b[P.t][P.A][1];
   const float vmin = bx.b[P.t][P.B][0], vmax = bx.b[P.t][P.B][1];
@@ -414,62 +434,68 @@ TMC_HD int projection_fast(ProjCtx& P, float pt[3]) {
   }
   P.wlo = ffx::f_ceil(wmin);
   P.whi = ffx::f_floor(wmax);
-  // pass 1: the smallest certain upper bound of a valid sample's distance
+  // pass 1: every sample once; the smallest certain upper bound of a valid sample's distance
+  // (loops kept rolled: 49 inlined copies of the sample code overflow the instruction cache)
   float m = INFINITY;
+#pragma unroll 1
   for (int i = 0; i < 7; i++)
+#pragma unroll 1
     for (int j = 0; j < 7; j++) {
       const SampleApprox s = sample_approx(P, P.us[i], P.vs[j]);
       if (s.status == 1) m = fminf(m, s.D + s.ED);
+      buf[(7 * i + j) * stride] = (s.status == 0) ? INFINITY : s.D - s.ED;
     }
   // pass 2: exact evaluation of every sample that can still win, in the reference's loop order
   float best = 100.0f;
   bool found = false;
+#pragma unroll 1
   for (int i = 0; i < 7; i++)
+#pragma unroll 1
     for (int j = 0; j < 7; j++) {
-      const SampleApprox s = sample_approx(P, P.us[i], P.vs[j]);
-      if (s.status == 0) continue;
-      if (!(s.D - s.ED <= m)) continue;
-      bool valid = false;
-      float w = 0, d = 0;
-      if (!sample_exact(P, P.us[i], P.vs[j], valid, w, d)) {
+      if (!(buf[(7 * i + j) * stride] <= m)) continue;
+      SampleOut s = sample_exact(P, P.us[i], P.vs[j]);
+      if (s.status == 2) {
         if (!P.have_pd) {
-          double pm[3];
-          mean_point_exact(P.pts, P.npts, pm);
-          P.pd[0] = pm[P.A];
-          P.pd[1] = pm[P.B];
-          P.pd[2] = pm[P.W];
+          const Point64 pm = mean_point_exact(P.pts, P.npts);
+          P.pd[0] = pm.p[P.A];
+          P.pd[1] = pm.p[P.B];
+          P.pd[2] = pm.p[P.W];
           P.have_pd = true;
         }
-        sample_f64(P, P.pd, P.us[i], P.vs[j], valid, w, d);
+        s = sample_f64(P, P.pd[0], P.pd[1], P.pd[2], P.us[i], P.vs[j]);
         P.f64_samples++;
       }
-      if (!valid) continue;
-      if (best > d) {
-        best = d;
+      if (s.status != 1) continue;
+      if (best > s.d) {
+        best = s.d;
         pt[0] = P.us[i];
         pt[1] = P.vs[j];
-        pt[2] = w;
+        pt[2] = s.w;
         found = true;
       }
     }
   return found ? 0 : 1;
 }
 
+struct TailOut {
+  float p[3];
+  int fail2;
+};
+TMC_HD_COLD TailOut representative_tail(const float* u, double iso, uint64_t c, int t, const float* pts, int n,
+                                        const Boxes& bx, int prj);
+
 // Representative of contour t.  pts: the contour's edge points (3 floats each, in contour order),
 // n of them.  On return p holds the local coordinates (floats) of the representative.
 TMC_HD void representative_fast(const float u[8], double iso, uint64_t c, int t, const float* pts, int n,
-                                const Boxes& bx, float p_out[3], Stats& st) {
+                                const Boxes& bx, float p_out[3], Stats& st, float* buf, int stride) {
   const int cnt_sz = csize(c, t);
   int prj;
-  double pd[3];
-  bool have_pd = false;
   if (cnt_sz >= 6) {
     // gradient plane: decided in float64 (large contours are a small minority)
-    mean_point_exact(pts, n, pd);
-    have_pd = true;
+    const Point64 pd = mean_point_exact(pts, n);
     double f[8];
     for (int q = 0; q < 8; q++) f[q] = u[q];
-    prj = plane_from_gradient(f, pd);
+    prj = plane_from_gradient(f, pd.p);
   } else {
     prj = plane_from_extent(bx, t);  // three float64 differences
   }
@@ -501,7 +527,7 @@ TMC_HD void representative_fast(const float u[8], double iso, uint64_t c, int t,
   P.c = c;
   P.bx = &bx;
   float pt[3];
-  const int r = projection_fast(P, pt);
+  const int r = projection_fast(P, pt, buf, stride);
   st.fallback += P.f64_samples;
   if (r == 0) {
     p_out[P.A] = pt[0];
@@ -509,29 +535,36 @@ TMC_HD void representative_fast(const float u[8], double iso, uint64_t c, int t,
     p_out[P.W] = pt[2];
     return;
   }
-  // no sample or not certified: the float64 path from the mean point
-  if (!have_pd) mean_point_exact(pts, n, pd);
-  if (r == 1) {
-    // the 7x7 projection is known to be empty: the reference then tries 26x26
-    double f[8];
-    for (int q = 0; q < 8; q++) f[q] = u[q];
-    int A, B, W;
-    uint32_t pm2;
-    plane(prj, A, B, W, pm2);
-    double fp[8];
-    for (int q = 0; q < 8; q++) fp[q] = f[(pm2 >> (4 * q)) & 0xF];
-    double ptd[3] = {pd[A], pd[B], pd[W]};
-    st.fail1++;
-    if (!projection_exact(fp, iso, c, t, ptd, bx, A, B, W, 28)) st.fail2++;
-    pd[A] = ptd[0];
-    pd[B] = ptd[1];
-    pd[W] = ptd[2];
-  } else {
-    representative_exact_plane(u, iso, c, t, pd, bx, prj, st);
-  }
-  p_out[0] = (float)pd[0];
-  p_out[1] = (float)pd[1];
-  p_out[2] = (float)pd[2];
+  // no valid 7x7 sample (r == 1)
+  st.fail1++;
+  const TailOut tail = representative_tail(u, iso, c, t, pts, n, bx, prj);
+  st.fail2 += tail.fail2;
+  p_out[0] = tail.p[0];
+  p_out[1] = tail.p[1];
+  p_out[2] = tail.p[2];
+}
+
+// The 7x7 projection is empty: the reference then tries 26x26 samples from the mean point, in
+// float64, and keeps the mean point when that finds nothing either.
+TMC_HD_COLD TailOut representative_tail(const float* u, double iso, uint64_t c, int t, const float* pts, int n,
+                                        const Boxes& bx, int prj) {
+  const Point64 pm = mean_point_exact(pts, n);
+  int A, B, W;
+  uint32_t perm;
+  plane(prj, A, B, W, perm);
+  double fp[8];
+  for (int q = 0; q < 8; q++) fp[q] = (double)u[(perm >> (4 * q)) & 0xF];
+  double pd[3] = {pm.p[0], pm.p[1], pm.p[2]};
+  double ptd[3] = {pd[A], pd[B], pd[W]};
+  TailOut r;
+  r.fail2 = projection_exact(fp, iso, c, t, ptd, bx, A, B, W, 28) ? 0 : 1;
+  pd[A] = ptd[0];
+  pd[B] = ptd[1];
+  pd[W] = ptd[2];
+  r.p[0] = (float)pd[0];
+  r.p[1] = (float)pd[1];
+  r.p[2] = (float)pd[2];
+  return r;
 }
 
 }  // namespace repr

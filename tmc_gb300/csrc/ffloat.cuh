@@ -17,8 +17,11 @@
 
 #ifdef __CUDACC__
 #define TMC_HD __host__ __device__ __forceinline__
+// rare paths stay out of line so that the hot loop fits the instruction cache
+#define TMC_HD_COLD inline __host__ __device__ __noinline__
 #else
 #define TMC_HD inline
+#define TMC_HD_COLD inline
 #endif
 
 namespace tmc {

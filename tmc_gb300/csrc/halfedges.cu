@@ -10,49 +10,36 @@
 //                  the third is a boundary halfedge and becomes its origin's handle
 //   4           -> flag 1 (non-manifold): paired by origin
 // The vertex handle he_v[v] is the last halfedge (in index order) with origin v, overridden by the
-// three-halfedge rule in edge-key order.
+// three-halfedge rule in edge-key order (key = min vertex << 32 | max vertex).
 //
-// GPU scheme: an open-addressing table keyed by the 64-bit unordered vertex pair collects the
-// halfedges of every edge (atomic slot append), each bucket then sorts its <= 4 ids, which restores
-// the reference's insertion order whatever order the atomics ran in.
+// GPU scheme: no hash table.  Halfedges are bucketed by origin vertex (counting sort: degree
+// count, exclusive scan, scatter of (halfedge, target) pairs), so the halfedges of edge {a, b} are
+// the entries of a's list with target b and of b's list with target a.  Vertex lists are short
+// (valence ~4) and spatially coherent, so the pairing pass reads mostly from L2.  Sorting the few
+// ids of an edge restores the reference's insertion order.
 #include "halfedges.h"
+#include "scan.cuh"
 
 namespace tmc {
 
 namespace {
 
-constexpr unsigned long long kEmpty = ~0ull;
-
-__device__ __forceinline__ unsigned long long edge_key(int a, int b) {
-  const unsigned lo = (unsigned)min(a, b), hi = (unsigned)max(a, b);
-  return ((unsigned long long)lo << 32) | hi;
-}
-
-__device__ __forceinline__ uint64_t mix(uint64_t x) {
-  x ^= x >> 33;
-  x *= 0xff51afd7ed558ccdull;
-  x ^= x >> 33;
-  x *= 0xc4ceb9fe1a85ec53ull;
-  x ^= x >> 33;
-  return x;
-}
-
-__global__ void he_vertex_init_kernel(int32_t* hv, unsigned long long* hv_key, int64_t nv) {
+__global__ void he_vertex_init_kernel(int32_t* hv, unsigned long long* hv_key, int32_t* deg, int64_t nv) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (int64_t)gridDim.x * blockDim.x) {
     hv[i] = -1;
-    if (hv_key) hv_key[i] = 0;
+    hv_key[i] = 0;
+    deg[i] = 0;
   }
 }
 
-// one thread per halfedge: fill the record, vertex handle (max index), insert into the table
+// records, face handles, vertex handles (highest index) and out-degrees
 __global__ void he_build_kernel(const int32_t* faces, int P, int64_t nf, int32_t* he, int32_t* hv, int32_t* hf,
-                                HeTable t, int32_t* slot_of, unsigned* overflow) {
+                                int32_t* deg) {
   const int64_t nh = nf * P;
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
     const int64_t f = h / P;
     const int r = (int)(h - f * P);
     const int v0 = faces[h];
-    const int v1 = faces[f * P + (r + 1) % P];
     int32_t* e = he + 5 * h;
     e[0] = v0;
     e[1] = (int32_t)f;
@@ -61,25 +48,35 @@ __global__ void he_build_kernel(const int32_t* faces, int P, int64_t nf, int32_t
     e[4] = 0;
     if (r == 0) hf[f] = (int32_t)(f * P);
     atomicMax(hv + v0, (int32_t)h);
-    const unsigned long long key = edge_key(v0, v1);
-    uint64_t b = mix(key) & (uint64_t)(t.size - 1);
-    for (int64_t probe = 0; probe < t.size; probe++) {
-      const unsigned long long old = atomicCAS(t.keys + b, kEmpty, key);
-      if (old == kEmpty || old == key) break;
-      b = (b + 1) & (uint64_t)(t.size - 1);
-    }
-    const int s = atomicAdd(t.count + b, 1);
-    if (s < 4) t.ids[4 * b + s] = (int32_t)h;
-    else atomicAdd(overflow, 1u);
-    slot_of[h] = (int32_t)b;
+    atomicAdd(deg + v0, 1);
   }
 }
 
-// One thread per halfedge.  Edges with two halfedges (the manifold majority) pair without any
-// coordination; an edge with 3 or 4 halfedges is resolved by its lowest halfedge's thread.
-__device__ __forceinline__ int sorted_ids(const HeTable& t, int64_t b, int id[4]) {
-  const int c = min(t.count[b], 4);
-  for (int q = 0; q < 4; q++) id[q] = q < c ? t.ids[4 * b + q] : 0x7fffffff;
+__global__ void he_scatter_kernel(const int32_t* faces, int P, int64_t nf, const int32_t* off, int32_t* cursor,
+                                  int2* list) {
+  const int64_t nh = nf * P;
+  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = h / P;
+    const int r = (int)(h - f * P);
+    const int v0 = faces[h], v1 = faces[f * P + (r + 1) % P];
+    list[off[v0] + atomicAdd(cursor + v0, 1)] = make_int2((int)h, v1);
+  }
+}
+
+// ids of all halfedges of the undirected edge {a, b} (sorted); returns their number (capped at 8)
+__device__ __forceinline__ int edge_halfedges(const int2* list, const int32_t* off, const int32_t* deg, int a, int b,
+                                              int id[8]) {
+  int c = 0;
+  for (int q = off[a], e = off[a] + deg[a]; q < e; q++) {
+    const int2 x = list[q];
+    if (x.y == b && c < 8) id[c++] = x.x;
+  }
+  if (a != b) {
+    for (int q = off[b], e = off[b] + deg[b]; q < e; q++) {
+      const int2 x = list[q];
+      if (x.y == a && c < 8) id[c++] = x.x;
+    }
+  }
   for (int x = 1; x < c; x++)
     for (int y = x; y > 0 && id[y - 1] > id[y]; y--) {
       const int tmp = id[y];
@@ -89,41 +86,44 @@ __device__ __forceinline__ int sorted_ids(const HeTable& t, int64_t b, int id[4]
   return c;
 }
 
-__global__ void he_twin_kernel(HeTable t, const int32_t* slot_of, int64_t nh, int32_t* he,
-                               unsigned long long* hv_key, unsigned long long* non_manifold) {
+// one thread per halfedge: two-halfedge edges pair without coordination; 3 or 4 are resolved by
+// the edge's lowest halfedge
+__global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const int2* list, const int32_t* off,
+                               const int32_t* deg, int32_t* he, unsigned long long* hv_key,
+                               unsigned long long* non_manifold) {
+  const int64_t nh = nf * P;
   unsigned long long nm = 0;
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = slot_of[h];
-    const int cnt = t.count[b];
-    if (cnt > 4) continue;  // more than four faces at an edge: left unpaired
+    const int64_t f = h / P;
+    const int r = (int)(h - f * P);
+    const int v0 = faces[h], v1 = faces[f * P + (r + 1) % P];
+    int id[8];
+    const int c = edge_halfedges(list, off, deg, v0, v1, id);
 #define HE(x) (he + 5 * (int64_t)(x))
-    if (cnt == 2) {
-      const int a = t.ids[4 * b], c = t.ids[4 * b + 1];
-      HE(h)[3] = (a == (int)h) ? c : a;
+    if (c == 2) {
+      HE(h)[3] = (id[0] == (int)h) ? id[1] : id[0];
       continue;
     }
-    if (cnt == 1) continue;
-    int id[4];
-    const int c = sorted_ids(t, b, id);
-    if (id[0] != (int)h) continue;  // the lowest halfedge resolves the edge
+    if (c < 3 || c > 4 || id[0] != (int)h) continue;  // boundary, or resolved by the lowest halfedge
     if (c == 3) {
       const int e0 = id[0], e1 = id[1], e2 = id[2];
-      const int v0 = HE(e0)[0], v1 = HE(e1)[0], v2 = HE(e2)[0];
+      const int a0 = HE(e0)[0], a1 = HE(e1)[0], a2 = HE(e2)[0];
       HE(e0)[4] = 2;
       HE(e1)[4] = 2;
       HE(e2)[4] = 2;
       int lone_v;
-      if (v0 != v1) {
-        HE(e0)[3] = e1; HE(e1)[3] = e0; HE(e2)[3] = -1; lone_v = v2;
-      } else if (v0 != v2) {
-        HE(e0)[3] = e2; HE(e2)[3] = e0; HE(e1)[3] = -1; lone_v = v1;
+      if (a0 != a1) {
+        HE(e0)[3] = e1; HE(e1)[3] = e0; HE(e2)[3] = -1; lone_v = a2;
+      } else if (a0 != a2) {
+        HE(e0)[3] = e2; HE(e2)[3] = e0; HE(e1)[3] = -1; lone_v = a1;
       } else {
-        HE(e1)[3] = e2; HE(e2)[3] = e1; HE(e0)[3] = -1; lone_v = v0;
+        HE(e1)[3] = e2; HE(e2)[3] = e1; HE(e0)[3] = -1; lone_v = a0;
       }
       // the last override in key order wins: remember the largest key (+1 so that 0 = none)
-      atomicMax(hv_key + lone_v, t.keys[b] + 1ull);
+      const unsigned long long key = ((unsigned long long)(unsigned)min(v0, v1) << 32) | (unsigned)max(v0, v1);
+      atomicMax(hv_key + lone_v, key + 1ull);
       nm++;
-    } else if (c == 4) {
+    } else {
       const int e0 = id[0], e1 = id[1], e2 = id[2], e3 = id[3];
       if (HE(e0)[0] != HE(e1)[0]) {
         HE(e0)[3] = e1; HE(e1)[3] = e0; HE(e2)[3] = e3; HE(e3)[3] = e2;
@@ -139,14 +139,17 @@ __global__ void he_twin_kernel(HeTable t, const int32_t* slot_of, int64_t nh, in
   if ((threadIdx.x & 31) == 0 && nm) atomicAdd(non_manifold, nm);
 }
 
-// three-halfedge edges whose key won the vertex override write the handle
-__global__ void he_override_kernel(HeTable t, const int32_t* slot_of, int64_t nh, const int32_t* he, int32_t* hv,
+// the lone halfedge of a three-halfedge edge whose key won its origin's override sets the handle
+__global__ void he_override_kernel(const int32_t* faces, int P, int64_t nf, const int32_t* he, int32_t* hv,
                                    const unsigned long long* hv_key) {
+  const int64_t nh = nf * P;
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = slot_of[h];
-    if (t.count[b] != 3 || he[5 * h + 3] != -1) continue;
-    const int v = he[5 * h];
-    if (hv_key[v] == t.keys[b] + 1ull) hv[v] = (int32_t)h;
+    if (he[5 * h + 4] != 2 || he[5 * h + 3] != -1) continue;
+    const int64_t f = h / P;
+    const int r = (int)(h - f * P);
+    const int v0 = faces[h], v1 = faces[f * P + (r + 1) % P];
+    const unsigned long long key = ((unsigned long long)(unsigned)min(v0, v1) << 32) | (unsigned)max(v0, v1);
+    if (hv_key[v0] == key + 1ull) hv[v0] = (int32_t)h;
   }
 }
 
@@ -159,25 +162,21 @@ __global__ void he_pack4_kernel(const int32_t* he5, int64_t nh, int32_t* he4) {
 
 }  // namespace
 
-// Unique edges are about half the halfedges, so a table of >= nh buckets runs at load ~0.5.
-int64_t he_table_size(int64_t nh) {
-  int64_t s = 1024;
-  while (s < nh) s <<= 1;
-  return s;
-}
-
-int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& o, HeTable t, int32_t* slot_of,
-                    unsigned long long* hv_key, unsigned long long* non_manifold, unsigned* overflow, int sms,
+int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& o, HeWork& w, int sms,
                     cudaStream_t st) {
   const int64_t nh = nf * P;
-  auto grid = [&](int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)sms * 8)); };
-  cudaMemsetAsync(t.keys, 0xFF, (size_t)t.size * sizeof(unsigned long long), st);
-  cudaMemsetAsync(t.count, 0, (size_t)t.size * sizeof(int32_t), st);
-  he_vertex_init_kernel<<<grid(nv), 256, 0, st>>>(o.hv, hv_key, nv);
-  he_build_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, o.he, o.hv, o.hf, t, slot_of, overflow);
-  he_twin_kernel<<<grid(nh), 256, 0, st>>>(t, slot_of, nh, o.he, hv_key, non_manifold);
-  he_override_kernel<<<grid(nh), 256, 0, st>>>(t, slot_of, nh, o.he, o.hv, hv_key);
-  return 4;
+  auto grid = [&](int64_t n) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)sms * 8));
+  };
+  int k = 0;
+  he_vertex_init_kernel<<<grid(nv), 256, 0, st>>>(o.hv, w.hv_key, w.deg, nv);
+  he_build_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, o.he, o.hv, o.hf, w.deg);
+  k += 2 + scan_i32(w.deg, nv, w.off, w.tiles, w.total, st);
+  cudaMemsetAsync(w.cursor, 0, (size_t)std::max<int64_t>(nv, 1) * sizeof(int32_t), st);
+  he_scatter_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.off, w.cursor, w.list);
+  he_twin_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.list, w.off, w.deg, o.he, w.hv_key, w.non_manifold);
+  he_override_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, o.he, o.hv, w.hv_key);
+  return k + 3;
 }
 
 int pack_halfedges4(const int32_t* he5, int64_t nh, int32_t* he4, int sms, cudaStream_t st) {

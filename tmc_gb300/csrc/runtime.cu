@@ -16,6 +16,7 @@
 #include "dmc.h"
 #include "dmc_mesh.h"
 #include "halfedges.h"
+#include "scan.cuh"
 #include "profiler.h"
 #include "tmc_cells.h"
 
@@ -514,30 +515,27 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   int64_t non_manifold = 0;
   if (flags & TMC_OUT_HALFEDGES) {
     const int64_t nh = 3 * nt;
-    tmc::HeTable t{};
-    t.size = tmc::he_table_size(nh);
-    int32_t *he5 = nullptr, *slot = nullptr, *he4 = nullptr, *hv = nullptr, *hf = nullptr;
-    unsigned long long *hv_key = nullptr, *nm = nullptr;
-    unsigned* ovf = nullptr;
-    TMC_CUDA(ctx, al.get(&t.keys, t.size));
-    TMC_CUDA(ctx, al.get(&t.count, t.size));
-    TMC_CUDA(ctx, al.get(&t.ids, 4 * t.size));
+    int32_t *he5 = nullptr, *he4 = nullptr, *hv = nullptr, *hf = nullptr;
+    tmc::HeWork w{};
+    TMC_CUDA(ctx, al.get(&w.deg, nv));
+    TMC_CUDA(ctx, al.get(&w.off, nv));
+    TMC_CUDA(ctx, al.get(&w.cursor, nv));
+    TMC_CUDA(ctx, al.get(&w.list, nh));
+    TMC_CUDA(ctx, al.get(&w.hv_key, nv));
+    TMC_CUDA(ctx, al.get(&w.tiles, tmc::scan_tiles(nv) + 2));
+    TMC_CUDA(ctx, al.get(&w.total, 2));
+    TMC_CUDA(ctx, al.get(&w.non_manifold, 2));
     TMC_CUDA(ctx, al.get(&he5, 5 * nh));
-    TMC_CUDA(ctx, al.get(&slot, nh));
-    TMC_CUDA(ctx, al.get(&hv_key, nv));
-    TMC_CUDA(ctx, al.get(&nm, 2));
-    TMC_CUDA(ctx, al.get(&ovf, 2));
-    TMC_CUDA(ctx, cudaMemsetAsync(nm, 0, 2 * sizeof(unsigned long long), st));
-    TMC_CUDA(ctx, cudaMemsetAsync(ovf, 0, 2 * sizeof(unsigned), st));
+    TMC_CUDA(ctx, cudaMemsetAsync(w.non_manifold, 0, 2 * sizeof(unsigned long long), st));
     TMC_OWN(he4, 4 * nh);
     TMC_OWN(hv, nv);
     TMC_OWN(hf, nt);
     tmc::HeOut ho{he5, hv, hf};
     tmc::Stage stage(&ctx->prof, "tmc_halfedges", st);
-    ctx->launches += tmc::build_halfedges(tris, 3, nt, nv, ho, t, slot, hv_key, nm, ovf, ctx->sms, st);
+    ctx->launches += tmc::build_halfedges(tris, 3, nt, nv, ho, w, ctx->sms, st);
     ctx->launches += tmc::pack_halfedges4(he5, nh, he4, ctx->sms, st);
     TMC_CUDA(ctx, cudaGetLastError());
-    TMC_CUDA(ctx, cudaMemcpyAsync(h + 8, nm, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    TMC_CUDA(ctx, cudaMemcpyAsync(h + 8, w.non_manifold, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     TMC_CUDA(ctx, cudaStreamSynchronize(st));
     non_manifold = (int64_t)h[8];
     out->nr_he = nh;

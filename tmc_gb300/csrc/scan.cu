@@ -83,3 +83,54 @@ int scan_flags(const uint8_t* flags, int64_t n, int32_t* out, unsigned long long
 }
 
 }  // namespace tmc
+
+namespace tmc {
+
+// Exclusive scan of non-negative int32 values: out[i] = sum of in[0..i).
+__global__ void __launch_bounds__(kScanThreads) i32_tile_sum_kernel(const int32_t* in, int64_t n,
+                                                                   unsigned long long* tile_sums) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  unsigned long long s = 0;
+  for (int q = 0; q < kScanItems; q++) {
+    const int64_t i = base + (int64_t)q * kScanThreads + threadIdx.x;
+    if (i < n) s += (unsigned long long)in[i];
+  }
+  unsigned long long tot;
+  block_exclusive_scan<unsigned long long>(s, &tot);
+  if (threadIdx.x == 0) tile_sums[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kScanThreads) i32_offsets_kernel(const int32_t* in, int64_t n,
+                                                                  const unsigned long long* tile_off, int32_t* out) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  const int64_t mine = base + (int64_t)threadIdx.x * kScanItems;
+  int32_t v[kScanItems];
+  unsigned long long s = 0;
+#pragma unroll
+  for (int q = 0; q < kScanItems; q++) {
+    v[q] = (mine + q < n) ? in[mine + q] : 0;
+    s += (unsigned long long)v[q];
+  }
+  unsigned long long tot;
+  unsigned long long pre = block_exclusive_scan<unsigned long long>(s, &tot) + tile_off[blockIdx.x];
+#pragma unroll
+  for (int q = 0; q < kScanItems; q++) {
+    if (mine + q < n) out[mine + q] = (int32_t)pre;
+    pre += (unsigned long long)v[q];
+  }
+}
+
+int scan_i32(const int32_t* in, int64_t n, int32_t* out, unsigned long long* tile_sums, unsigned long long* total,
+             cudaStream_t st) {
+  const int64_t tiles = scan_tiles(n);
+  if (tiles == 0) {
+    cudaMemsetAsync(total, 0, sizeof(unsigned long long), st);
+    return 0;
+  }
+  i32_tile_sum_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(in, n, tile_sums);
+  scan_tile_sums_kernel<<<1, 1024, 0, st>>>(tile_sums, tiles, total);
+  i32_offsets_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(in, n, tile_sums, out);
+  return 3;
+}
+
+}  // namespace tmc

@@ -56,5 +56,8 @@ __global__ void scan_tile_sums_kernel(unsigned long long* sums, int64_t ntiles, 
 int64_t scan_tiles(int64_t n);
 int scan_flags(const uint8_t* flags, int64_t n, int32_t* out, unsigned long long* tile_sums,
                unsigned long long* total, cudaStream_t st);
+// Device-wide exclusive scan of non-negative int32 values (same tile scheme).
+int scan_i32(const int32_t* in, int64_t n, int32_t* out, unsigned long long* tile_sums, unsigned long long* total,
+             cudaStream_t st);
 
 }  // namespace tmc
