@@ -10,6 +10,7 @@
  *   tmc_tmc_halfedge       p_mc::MarchingCubes::mc_halfedge         cuda_tmc/MarchingCubes.h:71
  *   tmc_batch_extract      (no single reference call: many dualMC / mc_sharedvertex calls in one launch)
  *   tmc_server_*           (no reference counterpart: request loop around the calls above)
+ *   tmc_dmc_count_static   (no reference counterpart: DMC mesh sizes without allocating)
  *
  * Threading: a context is thread-compatible, not thread-safe; use one context per host thread.
  * All work of a context runs on its own CUDA stream.
@@ -113,6 +114,17 @@ tmc_status tmc_tmc_sharedvertex(tmc_ctx* ctx, const tmc_volume* vol, double iso,
 /* Topologically correct Marching Cubes with the triangle halfedge structure. */
 tmc_status tmc_tmc_halfedge(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t flags, tmc_mesh* out);
 tmc_status tmc_mesh_free(tmc_ctx* ctx, tmc_mesh* mesh);
+
+/* Sizes of a DMC extraction without allocating (no counterpart in the reference).
+ * counts[0] vertices, [1] quads: tmc_dmc_extract's nr_v and nr_q without simplification flags;
+ * counts[2] active cells, [3] ambiguous cells: its stats[0] and stats[1].
+ * For callers that must not allocate device memory at call time, e.g. a server sizing a mesh
+ * before admitting the request against a fixed memory budget.  The field must be device memory.
+ * Scratch is one static 512 KiB device array per device: grids above 134,217,728 cells (513^3
+ * points) fail with TMC_ERR_CAPACITY; calls overlapping in time on one device race on the array
+ * and must be serialised; the first call on a device does a one-time set-up
+ * (cudaGetSymbolAddress) and should precede any stream capture on that device. */
+tmc_status tmc_dmc_count_static(tmc_ctx* ctx, const tmc_volume* vol, double iso, int64_t counts[4]);
 
 /* batched extraction ------------------------------------------------------------------------ */
 enum { TMC_ALGO_DMC = 0, TMC_ALGO_TMC = 1 };

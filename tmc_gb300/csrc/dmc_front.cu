@@ -23,6 +23,7 @@
 
 #include "common.cuh"
 #include "dmc.h"
+#include "dmc_cell.cuh"
 #include "dmc_repr.cuh"
 #include "scan.cuh"
 
@@ -30,91 +31,9 @@ namespace tmc {
 
 __constant__ uint64_t c_case_contour[256] = TMC_CASE_CONTOUR_INIT;
 
-// per-cell record
-//   bits 0-2   nV: used contours (vertices this cell emits)
-//   bits 3-4   nQ: crossed interior edges among the cell's edges 0, 3, 8 (quads it owns)
-//   bits 5-28  for each edge e, 2 bits: rank of the used contour holding e
-//   bit  29    ambiguous case
-__device__ __forceinline__ int rec_nv(uint32_t r) { return r & 7; }
-__device__ __forceinline__ int rec_nq(uint32_t r) { return (r >> 3) & 3; }
-__device__ __forceinline__ int rec_rank(uint32_t r, int e) { return (r >> (5 + 2 * e)) & 3; }
-
-__device__ __forceinline__ bool edge_interior(const Grid& g, int i, int j, int k, int e) {
-  const int off = edge_off(e), ax = edge_axis(e);
-  const int gi = i + (off & 1), gj = j + ((off >> 1) & 1), gk = k + ((off >> 2) & 1);
-  bool ok = true;
-  if (ax != 0) ok = ok && gi >= 1 && gi <= g.nx - 2;
-  if (ax != 1) ok = ok && gj >= 1 && gj <= g.ny - 2;
-  if (ax != 2) ok = ok && gk >= 1 && gk <= g.nz - 2;
-  return ok;
-}
-
-__device__ __forceinline__ void load_corners(const Grid& g, int i, int j, int k, float u[8]) {
-  const float* p = g.f + ((int64_t)k * g.ny + j) * g.nx + i;
-  const int64_t sy = g.nx, sz = (int64_t)g.nx * g.ny;
-  u[0] = __ldg(p);
-  u[1] = __ldg(p + 1);
-  u[2] = __ldg(p + sy);
-  u[3] = __ldg(p + sy + 1);
-  u[4] = __ldg(p + sz);
-  u[5] = __ldg(p + sz + 1);
-  u[6] = __ldg(p + sz + sy);
-  u[7] = __ldg(p + sz + sy + 1);
-}
-
-__device__ __forceinline__ unsigned mc_case(const float u[8], float iso_up) {
-  unsigned c = 0;
-#pragma unroll
-  for (int v = 0; v < 8; v++) c |= (unsigned)(u[v] >= iso_up) << v;
-  return c;
-}
-
-// Linear cell index -> (i, j, k); cell counts stay below 2^32 (checked by the runtime)
-__device__ __forceinline__ void cell_ijk(const Grid& g, int64_t c, int& i, int& j, int& k) {
-  const uint32_t cx = (uint32_t)(g.nx - 1), cy = (uint32_t)(g.ny - 1);
-  const uint32_t cc = (uint32_t)c;
-  const uint32_t r = cc / cx;
-  i = (int)(cc - r * cx);
-  const uint32_t kk = r / cy;
-  j = (int)(r - kk * cy);
-  k = (int)kk;
-}
-
 // ------------------------------------------------------------------------------------------
-// classification
+// classification (per-cell helpers in dmc_cell.cuh)
 // ------------------------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t classify_cell(const Grid& g, int i, int j, int k, const uint64_t* cc,
-                                                  unsigned long long* stats) {
-  float u[8];
-  load_corners(g, i, j, k, u);
-  const unsigned cs = mc_case(u, g.iso_up);
-  if (cs == 0 || cs == 255) return 0;
-  const bool amb = case_ambiguous(cs);
-  const uint64_t c = dmc_polygon(cs, u, g.iso, cc);
-  const int ncnt = cnt_count(c);
-  uint32_t rec = amb ? (1u << 29) : 0u;
-  int nv = 0, flat = 0;
-  for (int t = 0; t < ncnt; t++) {
-    const int sz = cnt_size(c, t);
-    bool used = false;
-    for (int q = 0; q < sz; q++) used = used || edge_interior(g, i, j, k, cnt_edge(c, flat + q));
-    if (used) {
-      for (int q = 0; q < sz; q++) rec |= (uint32_t)nv << (5 + 2 * cnt_edge(c, flat + q));
-      nv++;
-    }
-    flat += sz;
-  }
-  // owned quads: crossed interior edges 0 (x), 3 (y), 8 (z) at the cell's lower corner
-  const uint32_t em = case_edge_mask(cs);
-  int nq = 0;
-  nq += ((em >> 0) & 1) && edge_interior(g, i, j, k, 0);
-  nq += ((em >> 3) & 1) && edge_interior(g, i, j, k, 3);
-  nq += ((em >> 8) & 1) && edge_interior(g, i, j, k, 8);
-  rec |= (uint32_t)nv | ((uint32_t)nq << 3);
-  (void)stats;
-  return rec;
-}
-
 // One block handles kScanTile consecutive cells (linear order), writes their records and the
 // tile's packed (vertices << 32 | quads) sum.
 __global__ void __launch_bounds__(kScanThreads) dmc_classify_kernel(Grid g, uint32_t* rec,

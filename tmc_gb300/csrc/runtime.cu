@@ -566,3 +566,11 @@ tmc_status tmc_batch_extract(tmc_ctx* ctx, int32_t, const tmc_request*, tmc_mesh
   return fail(ctx, TMC_ERR_INTERNAL, "batched extraction is not built yet");
 }
 }
+
+// Context access for entry points defined in other translation units (ctx_access.h).
+namespace tmc {
+int ctx_device(const tmc_ctx* ctx) { return ctx->device; }
+cudaStream_t ctx_stream(const tmc_ctx* ctx) { return ctx->stream; }
+tmc_status ctx_fail(tmc_ctx* ctx, tmc_status s, const char* msg) { return fail(ctx, s, "%s", msg); }
+void ctx_count_launches(tmc_ctx* ctx, int64_t n) { ctx->launches += n; }
+}  // namespace tmc

@@ -14,6 +14,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libtmc_gb300.so")
 
 TMC_OK = 0
+TMC_ERR_INVALID_ARG = 1
+TMC_ERR_OOM = 2
+TMC_ERR_CAPACITY = 3
 STATUS = {0: "TMC_OK", 1: "TMC_ERR_INVALID_ARG", 2: "TMC_ERR_OOM", 3: "TMC_ERR_CAPACITY", 4: "TMC_ERR_CUDA",
           5: "TMC_ERR_TIMEOUT", 6: "TMC_ERR_NUMERIC", 7: "TMC_ERR_INTERNAL"}
 
@@ -34,7 +37,7 @@ ALGO_TMC = 1
 # every symbol include/tmc_gb300.h declares
 EXPORTS = ["tmc_ctx_create", "tmc_ctx_destroy", "tmc_last_error", "tmc_ctx_stream", "tmc_ctx_synchronize",
            "tmc_ctx_launch_count", "tmc_ctx_set_profiling", "tmc_ctx_profile_read", "tmc_dmc_extract", "tmc_tmc_sharedvertex", "tmc_tmc_halfedge",
-           "tmc_mesh_free", "tmc_batch_extract"]
+           "tmc_mesh_free", "tmc_batch_extract", "tmc_dmc_count_static"]
 
 
 class TmcError(RuntimeError):
@@ -94,6 +97,9 @@ def load(path: str = LIB_PATH):
     lib.tmc_ctx_profile_read.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_char_p,
                                          ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]
     lib.tmc_ctx_profile_read.restype = ctypes.c_int32
+    lib.tmc_dmc_count_static.argtypes = [ctypes.c_void_p, ctypes.POINTER(Volume), ctypes.c_double,
+                                         ctypes.POINTER(ctypes.c_int64)]
+    lib.tmc_dmc_count_static.restype = ctypes.c_int
     if hasattr(lib, "tmc_batch_extract"):
         lib.tmc_batch_extract.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(Request), ctypes.POINTER(Mesh)]
     _lib = lib
@@ -192,6 +198,13 @@ class Context:
 
     def tmc_raw(self, volume: Volume, iso: float, flags: int, halfedge: bool = False) -> Mesh:
         return self._run("tmc_tmc_halfedge" if halfedge else "tmc_tmc_sharedvertex", volume, iso, flags)
+
+    def dmc_count_static(self, volume: Volume, iso: float) -> tuple:
+        """tmc_dmc_count_static: (vertices, quads, active cells, ambiguous cells) of a DMC extraction
+        of a device-resident field, computed in a static scratch array without allocating."""
+        counts = (ctypes.c_int64 * 4)()
+        self._check(self.lib.tmc_dmc_count_static(self.h, ctypes.byref(volume), float(iso), counts))
+        return tuple(counts)
 
     # -- numpy results --------------------------------------------------------------------
     def fetch(self, m: Mesh) -> dict:
