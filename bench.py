@@ -7,10 +7,12 @@ P3333 simplification).  Synthetic data (no datasets exist for this path).  The f
 larger than L2, so no L2 flush is needed between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+    python bench.py --grid 320 --steps 1 --warmup 1 --no-cpu-baseline   # small case for profiling
 
 Prints one JSON line.  `value` is device-resident throughput (field already in HBM); `e2e` is the
 same metric through the C ABI with host buffers (field copied in, mesh copied out every step).
-Cells per step = 2 * 511^3 (each extraction visits every cell once).
+Cells per step = 511^3: each step extracts the one volume with both algorithms, and its cells are
+counted once (the CPU baseline and the reference arm count the same way).
 """
 from __future__ import annotations
 
@@ -39,6 +41,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--grid", type=int, default=N, help="points per axis of the noise field (profiling cases)")
     return p.parse_args()
 
 
@@ -132,7 +135,8 @@ def run_ours(args, rank, world, local):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    vol = volumes.noise_volume(N, seed=SEED + rank)
+    n = args.grid
+    vol = volumes.noise_volume(n, seed=SEED + rank)
     cells = vol.cells
     voxels = vol.data.size
     ctx = native.Context(local)
@@ -162,11 +166,13 @@ def run_ours(args, rank, world, local):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
+    sizes = {}
     for _ in range(args.warmup):
         mt, md = step(vdev)
+        sizes = {"tmc_v": mt.nr_v, "tmc_t": mt.nr_t, "dmc_v": md.nr_v, "dmc_q": md.nr_q, "dmc_t": md.nr_t,
+                 "dmc_he": md.nr_he}
         ctx.free(mt)
         ctx.free(md)
-    sizes = {"tmc_v": mt.nr_v, "tmc_t": mt.nr_t, "dmc_v": md.nr_v, "dmc_q": md.nr_q}
     # ---- device-resident timed region ----
     barrier()
     l0 = ctx.launches()
@@ -182,7 +188,7 @@ def run_ours(args, rank, world, local):
     launches = ctx.launches() - l0
     ms = max_over_ranks(e0.elapsed_time(e1))
     ms_step = ms / args.steps
-    value = world * 2 * cells * args.steps / (ms * 1e-3) / 1e9
+    value = world * cells * args.steps / (ms * 1e-3) / 1e9
     # ---- end to end through the C ABI with host buffers ----
     for _ in range(1):
         mt, md = step(vhost, native.OUT_HOST)
@@ -199,7 +205,7 @@ def run_ours(args, rank, world, local):
         ctx.free(md)
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e = world * 2 * cells * args.steps / e2e_s / 1e9
+    e2e = world * cells * args.steps / e2e_s / 1e9
     # ---- per-stage profile (separate pass, not timed above) ----
     ctx.set_profiling(True)
     m = ctx.dmc_raw(vdev, vol.iso, native.OUT_LOCAL)  # front end alone, for its mesh sizes
@@ -236,10 +242,10 @@ def run_ours(args, rank, world, local):
         "metric": METRIC, "value": round(value, 4), "unit": "Gcells/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "512^3 noise field (33^3 U[-1,1] upsampled + 0.02 N(0,1)), isovalue 0: TMC shared-vertex"
+        "config": {"workload": f"{n}^3 noise field (33^3 U[-1,1] upsampled + 0.02 N(0,1)), isovalue 0: TMC shared-vertex"
                                " + DMC halfedge/triangles with P3X3Y+P3333 simplification per step",
-                   "grid": [N, N, N], "cells_per_step": 2 * cells, "seed": SEED,
-                   "l2": "inputs larger than L2 (512 MiB field)", "parallelism": f"replicas x{world}"},
+                   "grid": [n, n, n], "cells_per_step": cells, "seed": SEED,
+                   "l2": f"inputs larger than L2 ({4 * voxels / 2**20:.0f} MiB field)", "parallelism": f"replicas x{world}"},
         "mesh": sizes,
         "e2e": {"value": round(e2e, 4), "unit": "Gcells/s", "h2d_bytes_per_step": 2 * 4 * voxels,
                 "d2h_bytes_per_step": int(d2h)},
@@ -279,7 +285,7 @@ def cpu_baseline_port(vol, planes=24):
     o.tmc(s)
     o.dmc(s, 1)
     dt = time.perf_counter() - t0
-    cells = 2 * s.cells
+    cells = s.cells
     return {"value": round(cells / dt / 1e9, 6), "unit": "Gcells/s", "cores": 1, "kind": "port",
             "sample": f"z-slab of {planes} planes ({s.dims[0]}x{s.dims[1]}x{s.dims[2]}) of the same field, "
                       f"TMC + DMC(simplify), {dt:.2f} s"}
@@ -303,7 +309,7 @@ def _ref_worker(a):
     t0 = time.perf_counter()
     lib.tmc(vol)
     lib.dmc(vol, 1)
-    return time.perf_counter() - t0, 2 * vol.cells
+    return time.perf_counter() - t0, vol.cells
 
 
 def run_reference(args, rank, world):

@@ -86,7 +86,8 @@ typedef struct tmc_mesh {
   int64_t* vcell;    /* nr_v generating cell (TMC_OUT_LOCAL) */
   float* vuvw;       /* 3*nr_v local coordinates in the generating cell (TMC_OUT_LOCAL) */
   int64_t stats[8];  /* [0] active cells [1] ambiguous cells [2,3] representative fallbacks
-                        (7x7 then 26x26 failed) [4] non-manifold edges [5] singular faces [6] cells */
+                        (7x7 then 26x26 failed) [4] non-manifold edges [5] singular faces [6] cells
+                        [7] values the DMC vertex kernel recomputed in float64 (samples, normals) */
   void* priv;
 } tmc_mesh;
 

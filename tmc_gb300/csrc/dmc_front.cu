@@ -106,16 +106,50 @@ __global__ void __launch_bounds__(kScanThreads) dmc_offsets_kernel(int64_t n, co
 // estimateGradient at a grid point (cpp_dmc/UniformGrid.cpp:512-540): central differences with
 // the reference's border indexing ((i<0) ? 0 : (i>=max) ? max-i : i).
 __device__ __forceinline__ int grad_index(int i, int max) { return (i < 0) ? 0 : (i >= max) ? max - i : i; }
-// float64 gradient with reciprocal spacing (normals are compared within a tolerance; the
-// reciprocal saves 24 float64 divisions per vertex)
-__device__ __forceinline__ void point_gradient(const Grid& g, int i, int j, int k, const double inv2d[3],
-                                               double out[3]) {
+// Central differences at a grid point, exact as float pairs (the reference's float64 difference
+// of two floats); the 1/(2*spacing) factor is applied after the interpolation.
+__device__ __forceinline__ void point_diff_ff(const Grid& g, int i, int j, int k, ffx::ff out[3]) {
   const int i0 = grad_index(i - 1, g.nx), i1 = grad_index(i + 1, g.nx);
   const int j0 = grad_index(j - 1, g.ny), j1 = grad_index(j + 1, g.ny);
   const int k0 = grad_index(k - 1, g.nz), k1 = grad_index(k + 1, g.nz);
-  out[0] = ((double)g.at(i1, j, k) - (double)g.at(i0, j, k)) * inv2d[0];
-  out[1] = ((double)g.at(i, j1, k) - (double)g.at(i, j0, k)) * inv2d[1];
-  out[2] = ((double)g.at(i, j, k1) - (double)g.at(i, j, k0)) * inv2d[2];
+  out[0] = ffx::two_sum(g.at(i1, j, k), -g.at(i0, j, k));
+  out[1] = ffx::two_sum(g.at(i, j1, k), -g.at(i, j0, k));
+  out[2] = ffx::two_sum(g.at(i, j, k1), -g.at(i, j, k0));
+}
+// a + t*(b - a) in float-float
+__device__ __forceinline__ ffx::ff ff_lerp(ffx::ff a, ffx::ff b, float t) {
+  return ffx::ff_add(a, ffx::ff_mul_f(ffx::ff_sub(b, a), t));
+}
+
+struct Normal64 {
+  double n[3];
+};
+// The reference's float64 normal (UniformGrid::normal on estimateGradient values), for the rare
+// vertices whose gradients cancel so much that the float-float result would lose its margin.
+__device__ __noinline__ Normal64 normal_f64(const Grid g, int i, int j, int k, float pu, float pv, float pw, int flip) {
+  const double inv2d[3] = {1.0 / (2 * g.dx), 1.0 / (2 * g.dy), 1.0 / (2 * g.dz)};
+  double G[8][3];
+  for (int q = 0; q < 8; q++) {
+    const int a = i + (q & 1), b = j + ((q >> 1) & 1), c = k + ((q >> 2) & 1);
+    const int i0 = grad_index(a - 1, g.nx), i1 = grad_index(a + 1, g.nx);
+    const int j0 = grad_index(b - 1, g.ny), j1 = grad_index(b + 1, g.ny);
+    const int k0 = grad_index(c - 1, g.nz), k1 = grad_index(c + 1, g.nz);
+    G[q][0] = ((double)g.at(i1, b, c) - (double)g.at(i0, b, c)) * inv2d[0];
+    G[q][1] = ((double)g.at(a, j1, c) - (double)g.at(a, j0, c)) * inv2d[1];
+    G[q][2] = ((double)g.at(a, b, k1) - (double)g.at(a, b, k0)) * inv2d[2];
+  }
+  const double uu = pu, vv = pv, ww = pw;
+  double nv3[3];
+  for (int d = 0; d < 3; d++) {
+    double gq[8];
+    for (int q = 0; q < 8; q++) gq[q] = flip ? G[q][d] * -1. : G[q][d];
+    nv3[d] = (1 - ww) * ((1 - vv) * ((1 - uu) * gq[0] + uu * gq[1]) + vv * ((1 - uu) * gq[2] + uu * gq[3])) +
+             ww * ((1 - vv) * ((1 - uu) * gq[4] + uu * gq[5]) + vv * ((1 - uu) * gq[6] + uu * gq[7]));
+  }
+  const double s = sqrt(nv3[0] * nv3[0] + nv3[1] * nv3[1] + nv3[2] * nv3[2]);
+  Normal64 r;
+  for (int d = 0; d < 3; d++) r.n[d] = nv3[d] / s;
+  return r;
 }
 __device__ __forceinline__ void point_gradient_f(const Grid& g, int i, int j, int k, float inv2d[3], float out[3]) {
   const int i0 = grad_index(i - 1, g.nx), i1 = grad_index(i + 1, g.nx);
@@ -137,6 +171,8 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_kernel(Grid g, cons
   repr::Stats st;
   const ffx::ff iso_ff = ffx::ff_from_double(g.iso);
   float inv2d[3] = {(float)(1.0 / (2 * g.dx)), (float)(1.0 / (2 * g.dy)), (float)(1.0 / (2 * g.dz))};
+  const ffx::ff inv2d_ff[3] = {ffx::ff_from_double(1.0 / (2 * g.dx)), ffx::ff_from_double(1.0 / (2 * g.dy)),
+                               ffx::ff_from_double(1.0 / (2 * g.dz))};
   for (int64_t vidx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vidx < nv;
        vidx += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t cell = vwork[vidx];
@@ -199,28 +235,46 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_kernel(Grid g, cons
       out.v64[o + 2] = pz;
     }
     // normal: trilinear interpolation of the 8 corner gradients, normalised (UniformGrid::normal,
-    // cpp_dmc/UniformGrid.h:286-298); float64 when it is kept for the simplification merges
+    // cpp_dmc/UniformGrid.h:286-298).  When it is kept for the simplification merges it is computed
+    // in float-float (relative error ~2^-40, far below the float32 output's 2^-24) on the FP32 pipes.
     if (out.n64) {
-      const double inv2dd[3] = {1.0 / (2 * g.dx), 1.0 / (2 * g.dy), 1.0 / (2 * g.dz)};
-      double G[8][3];
+      ffx::ff G[8][3];
 #pragma unroll
-      for (int q = 0; q < 8; q++)
-        point_gradient(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), inv2dd, G[q]);
-      double nv3[3];
-      const double uu = p[0], vv = p[1], ww = p[2];
+      for (int q = 0; q < 8; q++) point_diff_ff(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), G[q]);
+      ffx::ff nv3[3];
+      float scale = 0;  // largest |difference| * 1/(2 spacing): the size of the interpolation's inputs
 #pragma unroll
       for (int d = 0; d < 3; d++) {
-        double gq[8];
+        float md = 0;
 #pragma unroll
-        for (int q = 0; q < 8; q++) gq[q] = flip ? G[q][d] * -1. : G[q][d];
-        nv3[d] = (1 - ww) * ((1 - vv) * ((1 - uu) * gq[0] + uu * gq[1]) + vv * ((1 - uu) * gq[2] + uu * gq[3])) +
-                 ww * ((1 - vv) * ((1 - uu) * gq[4] + uu * gq[5]) + vv * ((1 - uu) * gq[6] + uu * gq[7]));
+        for (int q = 0; q < 8; q++) md = fmaxf(md, fabsf(G[q][d].hi));
+        scale = fmaxf(scale, md * inv2d[d]);
+        const ffx::ff a0 = ff_lerp(G[0][d], G[1][d], p[0]), a1 = ff_lerp(G[2][d], G[3][d], p[0]);
+        const ffx::ff a2 = ff_lerp(G[4][d], G[5][d], p[0]), a3 = ff_lerp(G[6][d], G[7][d], p[0]);
+        const ffx::ff b0 = ff_lerp(a0, a1, p[1]), b1 = ff_lerp(a2, a3, p[1]);
+        const ffx::ff t = ffx::ff_mul(ff_lerp(b0, b1, p[2]), inv2d_ff[d]);
+        nv3[d] = flip ? ffx::ff_neg(t) : t;
       }
-      const double s_ = sqrt(nv3[0] * nv3[0] + nv3[1] * nv3[1] + nv3[2] * nv3[2]);
-      for (int d = 0; d < 3; d++) {
-        const double x = nv3[d] / s_;
-        out.n64[o + d] = x;
-        out.n[o + d] = (float)x;
+      const ffx::ff dot =
+          ffx::ff_add(ffx::ff_add(ffx::ff_mul(nv3[0], nv3[0]), ffx::ff_mul(nv3[1], nv3[1])), ffx::ff_mul(nv3[2], nv3[2]));
+      // 1/sqrt(dot): float estimate and one Newton step in float-float
+      const float r0 = rsqrtf(dot.hi);
+      const ffx::ff h = ffx::ff_mul_f(ffx::ff_mul_f(dot, r0), r0);
+      const ffx::ff r = ffx::ff_mul_f(ffx::ff_sub(ffx::ff_from(1.5f), ffx::ff_mul_f(h, 0.5f)), r0);
+      if (scale <= 0x1p10f * sqrtf(dot.hi)) {
+        for (int d = 0; d < 3; d++) {
+          const ffx::ff x = ffx::ff_mul(nv3[d], r);
+          out.n64[o + d] = (double)x.hi + (double)x.lo;
+          out.n[o + d] = x.hi;
+        }
+      } else {
+        // the gradients cancel to below 2^-10 of their size: float64, as the reference
+        const Normal64 nf = normal_f64(g, i, j, k, p[0], p[1], p[2], flip);
+        for (int d = 0; d < 3; d++) {
+          out.n64[o + d] = nf.n[d];
+          out.n[o + d] = (float)nf.n[d];
+        }
+        st.normal_f64++;
       }
     } else {
       float G[8][3];
@@ -249,7 +303,7 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_kernel(Grid g, cons
   // representative counters (the reference's failed-projection counts) and float64 fallbacks
   if (st.fail1) atomicAdd(stats + 2, (unsigned long long)st.fail1);
   if (st.fail2) atomicAdd(stats + 3, (unsigned long long)st.fail2);
-  if (st.fallback) atomicAdd(stats + 7, (unsigned long long)st.fallback);
+  if (st.fallback + st.normal_f64) atomicAdd(stats + 7, (unsigned long long)(st.fallback + st.normal_f64));
 }
 
 // ------------------------------------------------------------------------------------------

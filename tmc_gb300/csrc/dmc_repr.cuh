@@ -40,6 +40,7 @@ struct Boxes {
 struct Stats {
   int fail1 = 0, fail2 = 0;  // 7x7 projection found nothing / 26x26 neither (the reference's counters)
   int fallback = 0;          // sample values that needed float64
+  int normal_f64 = 0;        // normals computed in float64 (strong cancellation)
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -223,33 +224,35 @@ TMC_HD void representative_exact(const float u[8], double iso, uint64_t c, int t
 // ---------------------------------------------------------------------------------------------
 // fast path
 // ---------------------------------------------------------------------------------------------
+// Corner values passed by value to out-of-line helpers (the caller's copy stays in registers).
+struct Corners {
+  float f[8];
+};
+
 struct SampleApprox {
   float D, ED;
   int status;  // 0 invalid, 1 valid, 2 uncertain
 };
 
+// Projection state: scalar fields and constant-indexed arrays only, so that it lives in registers.
 struct ProjCtx {
-  float fp[8];          // permuted corner values
-  float umin, vmin;     // sample grid origin
-  float us[7], vs[7];   // exact sample coordinates
-  float wlo, whi;       // w >= wlo && w <= whi  <=>  wmin <= w <= wmax (double bounds)
-  float pf[3];          // mean point (approximate, |error| <= 2^-23)
-  ff pff[3];            // mean point (float-float, within 2^-43 of the reference's double)
+  float fp[8];             // permuted corner values
+  float wlo, whi;          // w >= wlo && w <= whi  <=>  wmin <= w <= wmax (double bounds)
+  float pf[3];             // mean point (approximate, |error| <= 2^-23)
+  ff pff[3];               // mean point (float-float, within 2^-43 of the reference's double)
   float iso_f;
-  float iso_err;        // |iso - iso_f|
+  float iso_err;           // |iso - iso_f|
   ff iso_ff;
   double iso_d;
-  double pd[3];         // mean point in float64, permuted (valid when have_pd)
-  bool have_pd;
-  const float* pts;     // contour edge points (for the float64 mean)
-  int npts;
-  int f64_samples;      // samples evaluated in float64
-  int cnt, cnt_sz, t, A, B, W;
+  float sabs_lo, sabs_hi;  // max |f| over the w = 0 and the w = 1 face (bounds of the bilinear sums)
+  bool excl;               // the neighbour-contour exclusion applies (more than one contour, size != 3)
+  int cnt, t, A, B, W;
   uint64_t c;
   const Boxes* bx;
 };
 
-// float32 evaluation of one sample with error bounds
+// float32 evaluation of one sample with error bounds.  With u, v in [0, 1] the bilinear weights
+// are in [0, 1] and sum to 1, so every partial sum is bounded by the face's max |f|.
 TMC_HD SampleApprox sample_approx(const ProjCtx& P, float u, float v) {
   SampleApprox r;
   const float omu = 1 - u, omv = 1 - v;
@@ -257,10 +260,8 @@ TMC_HD SampleApprox sample_approx(const ProjCtx& P, float u, float v) {
   const float A1 = ffx::fma_rn(u, f[1], omu * f[0]), B1 = ffx::fma_rn(u, f[3], omu * f[2]);
   const float A2 = ffx::fma_rn(u, f[5], omu * f[4]), B2 = ffx::fma_rn(u, f[7], omu * f[6]);
   const float g1 = ffx::fma_rn(v, B1, omv * A1), g2 = ffx::fma_rn(v, B2, omv * A2);
-  const float S1 = fabsf(omv) * (fabsf(omu * f[0]) + fabsf(u * f[1])) + fabsf(v) * (fabsf(omu * f[2]) + fabsf(u * f[3]));
-  const float S2 = fabsf(omv) * (fabsf(omu * f[4]) + fabsf(u * f[5])) + fabsf(v) * (fabsf(omu * f[6]) + fabsf(u * f[7]));
-  const float Eg1 = S1 * 0x1p-20f + fabsf(g1) * 0x1p-23f;
-  const float Eg2 = S2 * 0x1p-20f + fabsf(g2) * 0x1p-23f;
+  const float Eg1 = P.sabs_lo * 0x1p-20f + fabsf(g1) * 0x1p-23f;
+  const float Eg2 = P.sabs_hi * 0x1p-20f + fabsf(g2) * 0x1p-23f;
   const float den = g2 - g1;
   const float Eden = (Eg1 + Eg2 + fabsf(den) * 0x1p-23f) * 1.0001f;
   if (!(fabsf(den) > 2 * Eden)) {  // w unknown (includes g1 == g2)
@@ -278,7 +279,7 @@ TMC_HD SampleApprox sample_approx(const ProjCtx& P, float u, float v) {
   const bool sure_in = (w - Ew >= P.wlo) && (w + Ew <= P.whi);
   const bool sure_out = (w + Ew < P.wlo) || (w - Ew > P.whi);
   int status = sure_out ? 0 : (sure_in ? 1 : 2);
-  if (status != 0 && P.cnt != 1 && P.cnt_sz != 3) {
+  if (status != 0 && P.excl) {
     for (int i = 0; i < P.cnt; i++) {
       if (csize(P.c, i) == 3 && P.t != i) {
         const Boxes& bx = *P.bx;
@@ -304,15 +305,15 @@ TMC_HD SampleApprox sample_approx(const ProjCtx& P, float u, float v) {
   return r;
 }
 
-// One exactly evaluated sample.  Results are returned by value: the out-of-line evaluators write
-// nothing through pointers into the caller's frame.
+// One exactly evaluated sample, returned by value.
 struct SampleOut {
   float w, d;
   int status;  // 0 invalid, 1 valid, 2 rounding not certified (evaluate in float64)
 };
 
-// float64 evaluation of one sample, as the reference's loop body (projection, :298-316)
-TMC_HD_COLD SampleOut sample_f64(const ProjCtx& P, double pd0, double pd1, double pd2, float u, float v) {
+// float64 evaluation of one sample, as the reference's loop body (projection, :298-316).  Rare:
+// out of line, with the context copied (the caller's stays in registers).
+TMC_HD_COLD SampleOut sample_f64(const ProjCtx P, double pd0, double pd1, double pd2, float u, float v) {
   SampleOut r{0.0f, 0.0f, 0};
   double fp[8];
   for (int q = 0; q < 8; q++) fp[q] = P.fp[q];
@@ -321,7 +322,7 @@ TMC_HD_COLD SampleOut sample_f64(const ProjCtx& P, double pd0, double pd1, doubl
   if (g1 == g2) return r;
   const float w = (P.iso_d - g1) / (g2 - g1);
   if (!(w >= P.wlo && w <= P.whi)) return r;
-  if (P.cnt != 1 && P.cnt_sz != 3 && in_neighbor_bbox(u, v, w, P.c, P.t, *P.bx, P.A, P.B, P.W)) return r;
+  if (P.excl && in_neighbor_bbox(u, v, w, P.c, P.t, *P.bx, P.A, P.B, P.W)) return r;
   r.status = 1;
   r.w = w;
   r.d = (pd0 - u) * (pd0 - u) + (pd1 - v) * (pd1 - v) + (pd2 - w) * (pd2 - w);
@@ -329,7 +330,7 @@ TMC_HD_COLD SampleOut sample_f64(const ProjCtx& P, double pd0, double pd1, doubl
 }
 
 // exact evaluation of one sample (status 2 when a rounding cannot be certified)
-TMC_HD_COLD SampleOut sample_exact(const ProjCtx& P, float u, float v) {
+TMC_HD SampleOut sample_exact(const ProjCtx& P, float u, float v) {
   SampleOut r{0.0f, 0.0f, 2};
   const float omu = 1 - u, omv = 1 - v;
   const float* f = P.fp;
@@ -339,11 +340,9 @@ TMC_HD_COLD SampleOut sample_exact(const ProjCtx& P, float u, float v) {
   const ff B2 = ffx::ff_add(ffx::two_prod(omu, f[6]), ffx::two_prod(u, f[7]));
   const ff G1 = ffx::ff_add(ffx::ff_mul_f(A1, omv), ffx::ff_mul_f(B1, v));
   const ff G2 = ffx::ff_add(ffx::ff_mul_f(A2, omv), ffx::ff_mul_f(B2, v));
-  const float S1 = fabsf(omv) * (fabsf(omu * f[0]) + fabsf(u * f[1])) + fabsf(v) * (fabsf(omu * f[2]) + fabsf(u * f[3]));
-  const float S2 = fabsf(omv) * (fabsf(omu * f[4]) + fabsf(u * f[5])) + fabsf(v) * (fabsf(omu * f[6]) + fabsf(u * f[7]));
   float g1, g2;
-  if (!ffx::ff_round(G1, S1 * 0x1p-45f, g1)) return r;
-  if (!ffx::ff_round(G2, S2 * 0x1p-45f, g2)) return r;
+  if (!ffx::ff_round(G1, P.sabs_lo * 0x1p-44f, g1)) return r;
+  if (!ffx::ff_round(G2, P.sabs_hi * 0x1p-44f, g2)) return r;
   if (g1 == g2) {
     r.status = 0;
     return r;
@@ -355,7 +354,7 @@ TMC_HD_COLD SampleOut sample_exact(const ProjCtx& P, float u, float v) {
   float w;
   if (!ffx::ff_round(W, errW, w)) return r;
   bool valid = (w >= P.wlo && w <= P.whi);
-  if (valid && P.cnt != 1 && P.cnt_sz != 3) {
+  if (valid && P.excl) {
     const Boxes& bx = *P.bx;
     for (int i = 0; i < P.cnt; i++) {
       if (csize(P.c, i) == 3 && P.t != i) {
@@ -417,59 +416,114 @@ TMC_HD void sample_coords(float lo, float hi, float out[7], int& f64_count) {
   }
 }
 
-// 0 = found (pt set), 1 = no valid sample.  buf: 49 slots (lower bound of each sample's distance,
-// +inf for a certainly invalid sample), slot q at buf[q * stride] (shared memory on the GPU, one
-// column per thread), so that every sample is approximated once.
-TMC_HD int projection_fast(ProjCtx& P, float pt[3], float* buf, int stride) {
-  const Boxes& bx = *P.bx;
-  const float umin = bx.b[P.t][P.A][0], umax = bx.b[P.t][P.A][1];
-  const float vmin = bx.b[P.t][P.B][0], vmax = bx.b[P.t][P.B][1];
-  sample_coords(umin, umax, P.us, P.f64_samples);
-  sample_coords(vmin, vmax, P.vs, P.f64_samples);
-  // w window in float64, as the reference widens it (wmin -= 1e-5 when the box is flat)
-  double wmin = bx.b[P.t][P.W][0], wmax = bx.b[P.t][P.W][1];
+// index of the coordinate nearest to x (the first on ties)
+TMC_HD int nearest_sample(const float s[7], float x) {
+  int k = 0;
+  float best = fabsf(s[0] - x);
+#pragma unroll 1
+  for (int q = 1; q < 7; q++) {
+    const float d = fabsf(s[q] - x);
+    if (d < best) {
+      best = d;
+      k = q;
+    }
+  }
+  return k;
+}
+
+// Evaluates sample (i, j) in float32: records the lower bound of its distance (+inf when it is
+// surely invalid) and lowers m, the smallest certain upper bound of a valid sample's distance.
+TMC_HD void approx_into(const ProjCtx& P, const float* us, const float* vs, int i, int j, float* buf, int stride,
+                        float& m) {
+  const SampleApprox s = sample_approx(P, us[i], vs[j]);
+  if (s.status == 1) m = fminf(m, s.D + s.ED);
+  buf[(7 * i + j) * stride] = (s.status == 0) ? INFINITY : s.D - s.ED;
+}
+
+// w window from the box's w extent, as the reference widens it (wmin -= 1e-5, wmax += 1e-5 when
+// the extent is below 1e-5), as the float range [wlo, whi] of values inside the float64 window.
+TMC_HD_COLD void w_window_flat(float lo, float hi, float& wlo, float& whi) {
+  double wmin = lo, wmax = hi;
   if (fabs(wmax - wmin) < 1e-5) {
     wmin -= 1e-5;
     wmax += 1e-5;
   }
-  P.wlo = ffx::f_ceil(wmin);
-  P.whi = ffx::f_floor(wmax);
-  // pass 1: every sample once; the smallest certain upper bound of a valid sample's distance
-  // (loops kept rolled: 49 inlined copies of the sample code overflow the instruction cache)
+  wlo = ffx::f_ceil(wmin);
+  whi = ffx::f_floor(wmax);
+}
+TMC_HD void w_window(float lo, float hi, float& wlo, float& whi) {
+  const float ext = hi - lo;  // within one ulp of the exact extent
+  if (ext > 1.001e-5f) {      // surely not flat: the window is the box itself
+    wlo = lo;
+    whi = hi;
+    return;
+  }
+  w_window_flat(lo, hi, wlo, whi);
+}
+
+// 0 = found (pt set), 1 = no valid sample.  buf: 49 slots (lower bound of each sample's distance,
+// +inf when it cannot win), slot q at buf[q * stride] (shared memory on the GPU, one column per
+// thread).  The 3x3 samples around the mean point are approximated first; every other sample is
+// skipped when even its distance within the sample plane exceeds the best certain bound (its w
+// cannot make it smaller).  The surviving candidates are then evaluated exactly in the reference's
+// loop order, so that ties resolve as the reference's strict `minDistance > d`.
+TMC_HD int projection_fast(const ProjCtx& P, const float* us, const float* vs, float pt[3], float* buf, int stride,
+                           int& f64_samples, const float* pts, int npts) {
   float m = INFINITY;
+  uint64_t done = 0;
+  const int i0 = nearest_sample(us, P.pf[0]), j0 = nearest_sample(vs, P.pf[1]);
+  const int ia = i0 > 0 ? i0 - 1 : 0, ib = i0 < 6 ? i0 + 1 : 6;
+  const int ja = j0 > 0 ? j0 - 1 : 0, jb = j0 < 6 ? j0 + 1 : 6;
 #pragma unroll 1
-  for (int i = 0; i < 7; i++)
+  for (int i = ia; i <= ib; i++)
+#pragma unroll 1
+    for (int j = ja; j <= jb; j++) {
+      approx_into(P, us, vs, i, j, buf, stride, m);
+      done |= 1ull << (7 * i + j);
+    }
+  const float Ep = 0x1p-22f;
+#pragma unroll 1
+  for (int i = 0; i < 7; i++) {
+    const float e0 = fmaxf(fabsf(P.pf[0] - us[i]) - Ep, 0.0f);
 #pragma unroll 1
     for (int j = 0; j < 7; j++) {
-      const SampleApprox s = sample_approx(P, P.us[i], P.vs[j]);
-      if (s.status == 1) m = fminf(m, s.D + s.ED);
-      buf[(7 * i + j) * stride] = (s.status == 0) ? INFINITY : s.D - s.ED;
+      if ((done >> (7 * i + j)) & 1) continue;
+      const float e1 = fmaxf(fabsf(P.pf[1] - vs[j]) - Ep, 0.0f);
+      // lower bound of the reference's float distance, whatever w is
+      if ((e0 * e0 + e1 * e1) * (1.0f - 0x1p-20f) > m) {
+        buf[(7 * i + j) * stride] = INFINITY;
+        continue;
+      }
+      approx_into(P, us, vs, i, j, buf, stride, m);
     }
-  // pass 2: exact evaluation of every sample that can still win, in the reference's loop order
+  }
+  // exact evaluation of every sample that can still win, in the reference's loop order
   float best = 100.0f;
   bool found = false;
+  bool have_pd = false;
+  double pd[3] = {0, 0, 0};
 #pragma unroll 1
   for (int i = 0; i < 7; i++)
 #pragma unroll 1
     for (int j = 0; j < 7; j++) {
       if (!(buf[(7 * i + j) * stride] <= m)) continue;
-      SampleOut s = sample_exact(P, P.us[i], P.vs[j]);
+      SampleOut s = sample_exact(P, us[i], vs[j]);
       if (s.status == 2) {
-        if (!P.have_pd) {
-          const Point64 pm = mean_point_exact(P.pts, P.npts);
-          P.pd[0] = pm.p[P.A];
-          P.pd[1] = pm.p[P.B];
-          P.pd[2] = pm.p[P.W];
-          P.have_pd = true;
+        if (!have_pd) {
+          const Point64 pm = mean_point_exact(pts, npts);
+          pd[0] = pm.p[P.A];
+          pd[1] = pm.p[P.B];
+          pd[2] = pm.p[P.W];
+          have_pd = true;
         }
-        s = sample_f64(P, P.pd[0], P.pd[1], P.pd[2], P.us[i], P.vs[j]);
-        P.f64_samples++;
+        s = sample_f64(P, pd[0], pd[1], pd[2], us[i], vs[j]);
+        f64_samples++;
       }
       if (s.status != 1) continue;
       if (best > s.d) {
         best = s.d;
-        pt[0] = P.us[i];
-        pt[1] = P.vs[j];
+        pt[0] = us[i];
+        pt[1] = vs[j];
         pt[2] = s.w;
         found = true;
       }
@@ -477,11 +531,66 @@ TMC_HD int projection_fast(ProjCtx& P, float pt[3], float* buf, int stride) {
   return found ? 0 : 1;
 }
 
+// exact comparison a <= b of two normalised float pairs
+TMC_HD bool ff_le(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
+
+// the exact difference (s, e) of two floats is a float64 value (the reference's subtraction does
+// not round) when its bits span at most 53 places
+TMC_HD bool exact_in_f64(ff x) {
+  if (x.lo == 0.0f) return true;
+  const int es = (int)((ffx::fbits(x.hi) >> 23) & 0xFF), ee = (int)((ffx::fbits(x.lo) >> 23) & 0xFF);
+  return ee > 0 && es - ee <= 29;
+}
+
+// projection plane from the box extents (minProjection).  The extents are float differences, held
+// exactly as float pairs; when the reference's float64 subtractions are exact too the comparison
+// is exact, otherwise (-1) it is redone in float64.
+TMC_HD int plane_from_extent_ff(const Boxes& bx, int t) {
+  const ff su = ffx::two_sum(bx.b[t][0][1], -bx.b[t][0][0]);
+  const ff sv = ffx::two_sum(bx.b[t][1][1], -bx.b[t][1][0]);
+  const ff sw = ffx::two_sum(bx.b[t][2][1], -bx.b[t][2][0]);
+  if (!exact_in_f64(su) || !exact_in_f64(sv) || !exact_in_f64(sw)) return -1;
+  if (ff_le(sw, su) && ff_le(sw, sv)) return 0;
+  if (ff_le(sv, su) && ff_le(sv, sw)) return 1;
+  if (ff_le(su, sv) && ff_le(su, sw)) return 2;
+  return 0;
+}
+
+// projection plane from the trilinear gradient at the mean point (contours of 6 or more edges),
+// decided in float32 when no comparison is within its error bound, else in float64 (-1)
+TMC_HD int plane_from_gradient_f(const float f[8], float uu, float vv, float ww) {
+  const float a0 = f[1] - f[0], a1 = f[3] - f[2], a2 = f[5] - f[4], a3 = f[7] - f[6];
+  const float b0 = f[2] - f[0], b1 = f[3] - f[1], b2 = f[6] - f[4], b3 = f[7] - f[5];
+  const float c0 = f[4] - f[0], c1 = f[5] - f[1], c2 = f[6] - f[2], c3 = f[7] - f[3];
+  const float g0 = (1 - ww) * ((1 - vv) * a0 + vv * a1) + ww * ((1 - vv) * a2 + vv * a3);
+  const float g1 = (1 - ww) * ((1 - uu) * b0 + uu * b1) + ww * ((1 - uu) * b2 + uu * b3);
+  const float g2 = (1 - vv) * ((1 - uu) * c0 + uu * c1) + vv * ((1 - uu) * c2 + uu * c3);
+  float m = 0;
+  for (int q = 0; q < 8; q++) m = fmaxf(m, fabsf(f[q]));
+  // each |g| is within 2^-18 * max|f| of the reference's (weights in [0, 1], a dozen roundings and
+  // the mean point within 2^-22)
+  const float e = m * 0x1p-18f;
+  const float dx = fabsf(g0), dy = fabsf(g1), dz = fabsf(g2);
+  auto sure = [&](float a, float b) { return fabsf(a - b) > 2 * e; };  // a >= b decided
+  if (!sure(dz, dx) || !sure(dz, dy) || !sure(dy, dx)) return -1;
+  if (dz >= dx && dz >= dy) return 0;
+  if (dy >= dx && dy >= dz) return 1;
+  if (dx >= dy && dx >= dz) return 2;
+  return 0;
+}
+TMC_HD_COLD int plane_from_extent_f64(const Boxes& bx, int t) { return plane_from_extent(bx, t); }
+TMC_HD_COLD int plane_from_gradient_exact(const float* pts, int n, Corners u) {
+  const Point64 pd = mean_point_exact(pts, n);
+  double f[8];
+  for (int q = 0; q < 8; q++) f[q] = u.f[q];
+  return plane_from_gradient(f, pd.p);
+}
+
 struct TailOut {
   float p[3];
   int fail2;
 };
-TMC_HD_COLD TailOut representative_tail(const float* u, double iso, uint64_t c, int t, const float* pts, int n,
+TMC_HD_COLD TailOut representative_tail(Corners u, double iso, uint64_t c, int t, const float* pts, int n,
                                         const Boxes& bx, int prj);
 
 // Representative of contour t.  pts: the contour's edge points (3 floats each, in contour order),
@@ -489,55 +598,69 @@ TMC_HD_COLD TailOut representative_tail(const float* u, double iso, uint64_t c, 
 TMC_HD void representative_fast(const float u[8], double iso, uint64_t c, int t, const float* pts, int n,
                                 const Boxes& bx, float p_out[3], Stats& st, float* buf, int stride) {
   const int cnt_sz = csize(c, t);
+  // mean point, float-float
+  ff s[3] = {ffx::ff_from(0.0f), ffx::ff_from(0.0f), ffx::ff_from(0.0f)};
+#pragma unroll 1
+  for (int q = 0; q < n; q++) {
+    s[0] = ffx::ff_add(s[0], ffx::ff_from(pts[3 * q]));
+    s[1] = ffx::ff_add(s[1], ffx::ff_from(pts[3 * q + 1]));
+    s[2] = ffx::ff_add(s[2], ffx::ff_from(pts[3 * q + 2]));
+  }
+  const ff nn = ffx::ff_from((float)n);
+  const ff pm[3] = {ffx::ff_div(s[0], nn), ffx::ff_div(s[1], nn), ffx::ff_div(s[2], nn)};
   int prj;
   if (cnt_sz >= 6) {
-    // gradient plane: decided in float64 (large contours are a small minority)
-    const Point64 pd = mean_point_exact(pts, n);
-    double f[8];
-    for (int q = 0; q < 8; q++) f[q] = u[q];
-    prj = plane_from_gradient(f, pd.p);
+    prj = plane_from_gradient_f(u, pm[0].hi, pm[1].hi, pm[2].hi);
+    if (prj < 0) {
+      Corners uc;
+      for (int q = 0; q < 8; q++) uc.f[q] = u[q];
+      prj = plane_from_gradient_exact(pts, n, uc);
+    }
   } else {
-    prj = plane_from_extent(bx, t);  // three float64 differences
+    prj = plane_from_extent_ff(bx, t);
+    if (prj < 0) prj = plane_from_extent_f64(bx, t);
   }
   ProjCtx P;
   uint32_t perm;
   plane(prj, P.A, P.B, P.W, perm);
+#pragma unroll
   for (int q = 0; q < 8; q++) P.fp[q] = u[(perm >> (4 * q)) & 0xF];
-  // mean point, float-float
-  ff s[3] = {ffx::ff_from(0.0f), ffx::ff_from(0.0f), ffx::ff_from(0.0f)};
-  for (int q = 0; q < n; q++)
-    for (int d = 0; d < 3; d++) s[d] = ffx::ff_add(s[d], ffx::ff_from(pts[3 * q + d]));
-  ff pm[3];
-  for (int d = 0; d < 3; d++) pm[d] = ffx::ff_div(s[d], ffx::ff_from((float)n));
-  P.pff[0] = pm[P.A];
-  P.pff[1] = pm[P.B];
-  P.pff[2] = pm[P.W];
+  P.sabs_lo = fmaxf(fmaxf(fabsf(P.fp[0]), fabsf(P.fp[1])), fmaxf(fabsf(P.fp[2]), fabsf(P.fp[3])));
+  P.sabs_hi = fmaxf(fmaxf(fabsf(P.fp[4]), fabsf(P.fp[5])), fmaxf(fabsf(P.fp[6]), fabsf(P.fp[7])));
+  P.pff[0] = P.A == 0 ? pm[0] : pm[1];
+  P.pff[1] = P.B == 1 ? pm[1] : pm[2];
+  P.pff[2] = P.W == 2 ? pm[2] : (P.W == 1 ? pm[1] : pm[0]);
   for (int d = 0; d < 3; d++) P.pf[d] = P.pff[d].hi;
   P.iso_ff = ffx::ff_from_double(iso);
   P.iso_d = iso;
-  P.have_pd = false;
-  P.pts = pts;
-  P.npts = n;
-  P.f64_samples = 0;
   P.iso_f = (float)iso;
   P.iso_err = fabsf((float)(iso - (double)P.iso_f)) + fabsf(P.iso_f) * 0x1p-30f;
   P.cnt = ccount(c);
-  P.cnt_sz = cnt_sz;
+  P.excl = P.cnt != 1 && cnt_sz != 3;
   P.t = t;
   P.c = c;
   P.bx = &bx;
+  const float umin = bx.b[t][P.A][0], umax = bx.b[t][P.A][1];
+  const float vmin = bx.b[t][P.B][0], vmax = bx.b[t][P.B][1];
+  float us[7], vs[7];
+  int f64_samples = 0;
+  sample_coords(umin, umax, us, f64_samples);
+  sample_coords(vmin, vmax, vs, f64_samples);
+  w_window(bx.b[t][P.W][0], bx.b[t][P.W][1], P.wlo, P.whi);
   float pt[3];
-  const int r = projection_fast(P, pt, buf, stride);
-  st.fallback += P.f64_samples;
+  const int r = projection_fast(P, us, vs, pt, buf, stride, f64_samples, pts, n);
+  st.fallback += f64_samples;
   if (r == 0) {
     p_out[P.A] = pt[0];
     p_out[P.B] = pt[1];
     p_out[P.W] = pt[2];
     return;
   }
-  // no valid 7x7 sample (r == 1)
+  // no valid 7x7 sample
   st.fail1++;
-  const TailOut tail = representative_tail(u, iso, c, t, pts, n, bx, prj);
+  Corners uc;
+  for (int q = 0; q < 8; q++) uc.f[q] = u[q];
+  const TailOut tail = representative_tail(uc, iso, c, t, pts, n, bx, prj);
   st.fail2 += tail.fail2;
   p_out[0] = tail.p[0];
   p_out[1] = tail.p[1];
@@ -546,14 +669,14 @@ TMC_HD void representative_fast(const float u[8], double iso, uint64_t c, int t,
 
 // The 7x7 projection is empty: the reference then tries 26x26 samples from the mean point, in
 // float64, and keeps the mean point when that finds nothing either.
-TMC_HD_COLD TailOut representative_tail(const float* u, double iso, uint64_t c, int t, const float* pts, int n,
+TMC_HD_COLD TailOut representative_tail(Corners u, double iso, uint64_t c, int t, const float* pts, int n,
                                         const Boxes& bx, int prj) {
   const Point64 pm = mean_point_exact(pts, n);
   int A, B, W;
   uint32_t perm;
   plane(prj, A, B, W, perm);
   double fp[8];
-  for (int q = 0; q < 8; q++) fp[q] = (double)u[(perm >> (4 * q)) & 0xF];
+  for (int q = 0; q < 8; q++) fp[q] = (double)u.f[(perm >> (4 * q)) & 0xF];
   double pd[3] = {pm.p[0], pm.p[1], pm.p[2]};
   double ptd[3] = {pd[A], pd[B], pd[W]};
   TailOut r;
