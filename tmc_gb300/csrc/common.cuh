@@ -24,7 +24,9 @@ struct Grid {
   double dx, dy, dz;  // spacing
   double iso;
   float iso_up;       // smallest float >= iso:  (double)f >= iso  <=>  f >= iso_up
-  int pad;
+  int flags;          // kGridFlip | kGridNormal64 | kGridPos64
+  int64_t vbase;      // index of cell 0 in the launch's cell space (0 for a single volume)
+  double inv2[3];     // 1 / (2 * spacing), for the central-difference gradients
   __host__ __device__ int cx() const { return nx - 1; }
   __host__ __device__ int cy() const { return ny - 1; }
   __host__ __device__ int cz() const { return nz - 1; }
@@ -35,7 +37,39 @@ struct Grid {
   __host__ __device__ __forceinline__ int64_t cell_index(int i, int j, int k) const {
     return ((int64_t)k * (ny - 1) + j) * (nx - 1) + i;
   }
+  // index of cell (i, j, k) in the launch's cell space (per-cell scratch arrays)
+  __host__ __device__ __forceinline__ int64_t vcell(int i, int j, int k) const { return vbase + cell_index(i, j, k); }
 };
+
+// Grid::flags: per-volume output choices (a batch mixes requests with different flags)
+constexpr int kGridFlip = 1;      // DMC normals from the negated gradient
+constexpr int kGridNormal64 = 2;  // DMC: float64 normals (kept while the mesh is simplified)
+constexpr int kGridPos64 = 4;     // TMC: float64 edge-vertex positions and normals
+
+// The cells one launch works on: a single volume, or a batch of volumes laid out one after another
+// in a linear cell space.  In a batch every volume starts on a scan-tile boundary (kScanTile cells),
+// so a tile never straddles two volumes; the rest of a volume's last tile is padding whose records
+// stay empty.  Per-cell scratch (records, offsets) is indexed in this space.
+struct CellSpace {
+  Grid one;                 // single-volume launches
+  const Grid* grids;        // batch: grid of each volume (vbase set), else nullptr
+  const int32_t* tile_vol;  // batch: volume of each tile
+  int64_t n;                // cells in the space, padding included
+  __device__ __forceinline__ Grid grid_of_tile(int64_t tile) const {
+    if (!grids) return one;
+    return grids[__ldg(tile_vol + tile)];
+  }
+};
+
+inline CellSpace single_space(const Grid& g) {
+  CellSpace cs;
+  cs.one = g;
+  cs.one.vbase = 0;
+  cs.grids = nullptr;
+  cs.tile_vol = nullptr;
+  cs.n = g.ncells();
+  return cs;
+}
 
 // ------------------------------------------------------------------------------------------
 // packed topology lookups (4 bits per entry)

@@ -28,9 +28,12 @@ struct DmcScratch {
 };
 
 // Each launcher returns the number of kernels it launched.
-int64_t dmc_tiles(const Grid& g);  // scan tiles for the cell count of g
-int dmc_front_count(const Grid& g, DmcScratch& s, cudaStream_t st, Prof* prof = nullptr);
-int dmc_front_emit(const Grid& g, DmcScratch& s, DmcVertexOut vo, int64_t nv, int32_t* quads, uint8_t* colors,
-                   int flip, int sms, cudaStream_t st, Prof* prof = nullptr);
+// Per-cell scratch is indexed in the cell space (space.n cells, padding included).
+int64_t dmc_tiles(const CellSpace& space);  // scan tiles of the space
+int dmc_front_count(const CellSpace& space, DmcScratch& s, cudaStream_t st, Prof* prof = nullptr);
+// Quads hold vertex indices within their own volume; vertices and quads of the volumes follow one
+// another in the output arrays.
+int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64_t nv, int32_t* quads,
+                   uint8_t* colors, int flip, int sms, cudaStream_t st, Prof* prof = nullptr);
 
 }  // namespace tmc

@@ -36,22 +36,27 @@ __constant__ uint64_t c_case_contour[256] = TMC_CASE_CONTOUR_INIT;
 // ------------------------------------------------------------------------------------------
 // One block handles kScanTile consecutive cells (linear order), writes their records and the
 // tile's packed (vertices << 32 | quads) sum.
-__global__ void __launch_bounds__(kScanThreads) dmc_classify_kernel(Grid g, uint32_t* rec,
+__global__ void __launch_bounds__(kScanThreads) dmc_classify_kernel(CellSpace space, uint32_t* rec,
                                                                    unsigned long long* tile_sums,
                                                                    unsigned long long* stats) {
   __shared__ uint64_t cc[256];
   for (int c = threadIdx.x; c < 256; c += blockDim.x) cc[c] = c_case_contour[c];
   __syncthreads();
+  const Grid g = space.grid_of_tile(blockIdx.x);
   const int64_t n = g.ncells();
-  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  const int64_t vbase = (int64_t)blockIdx.x * kScanTile;  // first cell of the tile in the space
   unsigned long long local = 0, act = 0, amb = 0;
   for (int s = 0; s < kScanItems; s++) {
-    const int64_t c = base + (int64_t)s * kScanThreads + threadIdx.x;
-    if (c >= n) break;
-    int i, j, k;
-    cell_ijk(g, c, i, j, k);
-    const uint32_t r = classify_cell(g, i, j, k, cc, stats);
-    rec[c] = r;
+    const int64_t vc = vbase + (int64_t)s * kScanThreads + threadIdx.x;
+    if (vc >= space.n) break;
+    const int64_t c = vc - g.vbase;  // cell of the volume (beyond its last cell: padding)
+    uint32_t r = 0;
+    if (c < n) {
+      int i, j, k;
+      cell_ijk(g, c, i, j, k);
+      r = classify_cell(g, i, j, k, cc, stats);
+    }
+    rec[vc] = r;
     local += ((unsigned long long)rec_nv(r) << 32) | (unsigned long long)rec_nq(r);
     act += r != 0;
     amb += (r >> 29) & 1;
@@ -161,22 +166,36 @@ __device__ __forceinline__ void point_gradient_f(const Grid& g, int i, int j, in
 }
 
 constexpr int kVertexThreads = 128;
-__global__ void __launch_bounds__(kVertexThreads) dmc_vertex_kernel(Grid g, const int32_t* voff, const uint32_t* vwork,
-                                                         int64_t nv, DmcVertexOut out, int flip,
-                                                         unsigned long long* stats) {
+__global__ void __launch_bounds__(kVertexThreads) dmc_vertex_kernel(CellSpace space, const int32_t* voff,
+                                                                     const uint32_t* vwork, int64_t nv,
+                                                                     DmcVertexOut out, int flip_all,
+                                                                     unsigned long long* stats) {
   __shared__ uint64_t cc[256];
   __shared__ float sample_lb[49 * kVertexThreads];  // per-thread sample bounds, column per thread
   for (int c = threadIdx.x; c < 256; c += blockDim.x) cc[c] = c_case_contour[c];
   __syncthreads();
   repr::Stats st;
-  const ffx::ff iso_ff = ffx::ff_from_double(g.iso);
-  float inv2d[3] = {(float)(1.0 / (2 * g.dx)), (float)(1.0 / (2 * g.dy)), (float)(1.0 / (2 * g.dz))};
-  const ffx::ff inv2d_ff[3] = {ffx::ff_from_double(1.0 / (2 * g.dx)), ffx::ff_from_double(1.0 / (2 * g.dy)),
-                               ffx::ff_from_double(1.0 / (2 * g.dz))};
+  int gvol = -1;  // volume whose grid is loaded
+  Grid g{};
+  ffx::ff iso_ff{0, 0};
+  float inv2d[3] = {0, 0, 0};
+  ffx::ff inv2d_ff[3] = {{0, 0}, {0, 0}, {0, 0}};
   for (int64_t vidx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vidx < nv;
        vidx += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t cell = vwork[vidx];
-    const int rank = (int)(vidx - voff[cell]);
+    const uint32_t vcell = vwork[vidx];
+    const int rank = (int)(vidx - voff[vcell]);
+    const int vol = space.grids ? __ldg(space.tile_vol + vcell / kScanTile) : 0;
+    if (vol != gvol) {
+      g = space.grids ? space.grids[vol] : space.one;
+      gvol = vol;
+      iso_ff = ffx::ff_from_double(g.iso);
+      for (int d = 0; d < 3; d++) {
+        inv2d[d] = (float)g.inv2[d];
+        inv2d_ff[d] = ffx::ff_from_double(g.inv2[d]);
+      }
+    }
+    const int64_t cell = vcell - g.vbase;
+    const int flip = flip_all | (g.flags & kGridFlip);
     int i, j, k;
     cell_ijk(g, cell, i, j, k);
     float u[8];
@@ -237,7 +256,7 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_kernel(Grid g, cons
     // normal: trilinear interpolation of the 8 corner gradients, normalised (UniformGrid::normal,
     // cpp_dmc/UniformGrid.h:286-298).  When it is kept for the simplification merges it is computed
     // in float-float (relative error ~2^-40, far below the float32 output's 2^-24) on the FP32 pipes.
-    if (out.n64) {
+    if (out.n64 && (g.flags & kGridNormal64)) {
       ffx::ff G[8][3];
 #pragma unroll
       for (int q = 0; q < 8; q++) point_diff_ff(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), G[q]);
@@ -311,18 +330,23 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_kernel(Grid g, cons
 // four cells around it.  Slot by the side of the edge's first end vertex (get_vertex_pos,
 // cpp_dmc/DualMarchingCubes.h:221-224); colour 3*parity(i,j,k) + axis (:177-180).
 // ------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) dmc_quad_kernel(Grid g, const uint32_t* rec, const int32_t* voff,
-                                                       const int32_t* qoff, int32_t* quads, uint8_t* colors) {
-  const int64_t n = g.ncells();
+// Quad corners are vertex indices within the quad's own volume: the space-wide offsets minus the
+// volume's first vertex (the scanned tile offset of its first tile; 0 for a single volume).
+__global__ void __launch_bounds__(128) dmc_quad_kernel(CellSpace space, const uint32_t* rec, const int32_t* voff,
+                                                       const int32_t* qoff, const unsigned long long* tile_off,
+                                                       int32_t* quads, uint8_t* colors) {
   // cell offsets (di, dj, dk) and local edge of the four cells around the owned edges 0, 3, 8
   // x edge: (0,-1,-1) e6, (0,0,-1) e4, (0,-1,0) e2, (0,0,0) e0
   // y edge: (-1,0,-1) e5, (0,0,-1) e7, (-1,0,0) e1, (0,0,0) e3
   // z edge: (-1,-1,0) e10, (0,-1,0) e11, (-1,0,0) e9, (0,0,0) e8
   const int AX_E[3] = {0, 3, 8};
-  for (int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; cell < n;
-       cell += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t r = rec[cell];
-    if (rec_nq(r) == 0) continue;
+  for (int64_t vc = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vc < space.n;
+       vc += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t r = rec[vc];
+    if (rec_nq(r) == 0) continue;  // padding records are empty
+    const Grid g = space.grid_of_tile(vc / kScanTile);
+    const int32_t vfirst = (int32_t)(tile_off[g.vbase / kScanTile] >> 32);
+    const int64_t cell = vc - g.vbase;
     int i, j, k;
     cell_ijk(g, cell, i, j, k);
     const float f0 = g.at(i, j, k);
@@ -330,7 +354,7 @@ __global__ void __launch_bounds__(128) dmc_quad_kernel(Grid g, const uint32_t* r
     const float fx = g.at(i + 1, j, k), fy = g.at(i, j + 1, k), fz = g.at(i, j, k + 1);
     const bool s0 = f0 >= g.iso_up;
     const bool crossed[3] = {s0 != (fx >= g.iso_up), s0 != (fy >= g.iso_up), s0 != (fz >= g.iso_up)};
-    int32_t q = qoff[cell];
+    int32_t q = qoff[vc];
     const int par = (i & 1) | ((j & 1) << 1) | ((k & 1) << 2);
     for (int a = 0; a < 3; a++) {
       if (!crossed[a] || !edge_interior(g, i, j, k, AX_E[a])) continue;
@@ -353,9 +377,9 @@ __global__ void __launch_bounds__(128) dmc_quad_kernel(Grid g, const uint32_t* r
       }
       int32_t qv[4];
       for (int s = 0; s < 4; s++) {
-        const int64_t nc = g.cell_index(i + di[s], j + dj[s], k + dk[s]);
+        const int64_t nc = g.vcell(i + di[s], j + dj[s], k + dk[s]);
         const uint32_t rn = rec[nc];
-        qv[quad_slot(le[s], neg)] = voff[nc] + rec_rank(rn, le[s]);
+        qv[quad_slot(le[s], neg)] = voff[nc] - vfirst + rec_rank(rn, le[s]);
       }
       reinterpret_cast<int4*>(quads)[q] = make_int4(qv[0], qv[1], qv[2], qv[3]);
       if (colors) colors[q] = (uint8_t)(3 * par + a);
@@ -367,24 +391,23 @@ __global__ void __launch_bounds__(128) dmc_quad_kernel(Grid g, const uint32_t* r
 // ------------------------------------------------------------------------------------------
 // host-side launches
 // ------------------------------------------------------------------------------------------
-int dmc_front_count(const Grid& g, DmcScratch& s, cudaStream_t st, Prof* prof) {
-  const int64_t n = g.ncells();
-  const int64_t tiles = ceil_div(n, kScanTile);
+int dmc_front_count(const CellSpace& space, DmcScratch& s, cudaStream_t st, Prof* prof) {
+  const int64_t tiles = ceil_div(space.n, kScanTile);
   {
     Stage t(prof, "dmc_classify", st);
-    dmc_classify_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(g, s.rec, s.tile_sums, s.stats);
+    dmc_classify_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(space, s.rec, s.tile_sums, s.stats);
   }
   Stage t(prof, "dmc_scan", st);
   scan_tile_sums_kernel<<<1, 1024, 0, st>>>(s.tile_sums, tiles, s.totals);
   return 2;
 }
 
-int64_t dmc_tiles(const Grid& g) { return ceil_div(g.ncells(), kScanTile); }
+int64_t dmc_tiles(const CellSpace& space) { return ceil_div(space.n, kScanTile); }
 
-int dmc_front_emit(const Grid& g, DmcScratch& s, DmcVertexOut vo, int64_t nv, int32_t* quads, uint8_t* colors,
-                   int flip, int sms, cudaStream_t st, Prof* prof) {
-  const int64_t n = g.ncells();
-  const int64_t blocks = std::min<int64_t>(ceil_div(n, 128), (int64_t)sms * 16);
+int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64_t nv, int32_t* quads,
+                   uint8_t* colors, int flip, int sms, cudaStream_t st, Prof* prof) {
+  const int64_t n = space.n;
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 128), (int64_t)sms * 16));
   {
     // per-cell offsets and the vertex work list (needs the vertex count for its size)
     Stage t(prof, "dmc_scan", st);
@@ -394,10 +417,10 @@ int dmc_front_emit(const Grid& g, DmcScratch& s, DmcVertexOut vo, int64_t nv, in
   {
     Stage t(prof, "dmc_vertex", st);
     const int64_t vb = std::max<int64_t>(1, std::min<int64_t>(ceil_div(nv, 128), (int64_t)sms * 32));
-    dmc_vertex_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(g, s.voff, s.vwork, nv, vo, flip, s.stats);
+    dmc_vertex_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(space, s.voff, s.vwork, nv, vo, flip, s.stats);
   }
   Stage t(prof, "dmc_quad", st);
-  dmc_quad_kernel<<<(unsigned)blocks, 128, 0, st>>>(g, s.rec, s.voff, s.qoff, quads, colors);
+  dmc_quad_kernel<<<(unsigned)blocks, 128, 0, st>>>(space, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
   return 3;
 }
 

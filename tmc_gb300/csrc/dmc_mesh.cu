@@ -425,7 +425,7 @@ struct HeBufs {
 }  // namespace
 
 DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaStream_t st, DmcPostOut* out,
-                              Prof* prof) {
+                              Prof* prof, bool borrowed) {
   DmcPostStatus s;
   out->mesh = in;
   const bool c3x3y = flags & TMC_DMC_P3X3Y_COLOR, i3x3y = flags & TMC_DMC_P3X3Y_ISOLATED,
@@ -517,7 +517,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
         mine = true;
       }
     if (!mine) out->freed.push_back(ptr);
-    cudaFreeAsync(ptr, st);
+    if (mine || !borrowed) cudaFreeAsync(ptr, st);
   };
   auto adopt = [&](void* ptr) { out->owned.push_back(ptr); };
 

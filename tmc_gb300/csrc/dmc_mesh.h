@@ -36,7 +36,9 @@ struct DmcPostStatus {
   int launches = 0;
 };
 
+// borrowed: the input arrays belong to the caller (e.g. slices of a batch's shared arrays) and are
+// never freed here; they are still listed in out->freed once the result no longer uses them.
 DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaStream_t st, DmcPostOut* out,
-                              Prof* prof = nullptr);
+                              Prof* prof = nullptr, bool borrowed = false);
 
 }  // namespace tmc

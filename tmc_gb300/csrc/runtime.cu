@@ -2,6 +2,7 @@
 // memory, argument checking, and the extraction drivers that sequence the kernels.
 #include <atomic>
 #include <map>
+#include <memory>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -56,9 +57,20 @@ struct tmc_ctx {
 
 namespace {
 
+// Device arrays shared by the meshes of one batch (each mesh points at its slice); released when
+// the last of those meshes is freed.
+struct SharedBlock {
+  std::vector<void*> dev;
+  cudaStream_t stream = nullptr;
+  ~SharedBlock() {
+    for (void* p : dev) cudaFreeAsync(p, stream);
+  }
+};
+
 struct MeshPriv {
   std::vector<void*> dev;
   std::vector<void*> host;
+  std::shared_ptr<SharedBlock> shared;
 };
 
 tmc_status fail(tmc_ctx* ctx, tmc_status s, const char* fmt, ...) {
@@ -157,6 +169,9 @@ tmc::Grid make_grid(const tmc_volume* vol, const float* dev, double iso) {
   g.dz = vol->spacing[2];
   g.iso = iso;
   g.iso_up = iso_up(iso);
+  g.inv2[0] = 1.0 / (2 * g.dx);
+  g.inv2[1] = 1.0 / (2 * g.dy);
+  g.inv2[2] = 1.0 / (2 * g.dz);
   return g;
 }
 
@@ -191,6 +206,7 @@ tmc_status finish_mesh(tmc_ctx* ctx, uint32_t flags, tmc_mesh* out, MeshPriv* mp
     TMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     for (void* p : mp->dev) cudaFreeAsync(p, ctx->stream);
     mp->dev.clear();
+    mp->shared.reset();
     out->on_device = 0;
   } else {
     out->on_device = 1;
@@ -294,6 +310,7 @@ tmc_status tmc_mesh_free(tmc_ctx* ctx, tmc_mesh* mesh) {
   if (mp) {
     cudaSetDevice(ctx->device);
     for (void* p : mp->dev) cudaFreeAsync(p, ctx->stream);
+    mp->shared.reset();
     cudaStreamSynchronize(ctx->stream);  // the next call may reuse these pinned blocks
     for (void* p : mp->host) ctx->pinned_put(p);
     delete mp;
@@ -317,18 +334,20 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   Allocs al(ctx);
   const float* field = nullptr;
   if ((s = field_on_device(ctx, vol, al, &field))) return s;
-  const tmc::Grid g = make_grid(vol, field, iso);
+  tmc::Grid g = make_grid(vol, field, iso);
+  g.flags = ((flags & TMC_GRAD_FLIP) ? tmc::kGridFlip : 0) | (simplify ? tmc::kGridNormal64 : 0);
+  const tmc::CellSpace space = tmc::single_space(g);
   const int64_t ncell = g.ncells();
 
   tmc::DmcScratch sc{};
   TMC_CUDA(ctx, al.get(&sc.rec, ncell));
   TMC_CUDA(ctx, al.get(&sc.voff, ncell));
   TMC_CUDA(ctx, al.get(&sc.qoff, ncell));
-  TMC_CUDA(ctx, al.get(&sc.tile_sums, tmc::dmc_tiles(g)));
+  TMC_CUDA(ctx, al.get(&sc.tile_sums, tmc::dmc_tiles(space)));
   TMC_CUDA(ctx, al.get(&sc.totals, 2));
   sc.stats = ctx->d_stats;
   TMC_CUDA(ctx, cudaMemsetAsync(sc.stats, 0, 8 * sizeof(unsigned long long), st));
-  ctx->launches += tmc::dmc_front_count(g, sc, st, &ctx->prof);
+  ctx->launches += tmc::dmc_front_count(space, sc, st, &ctx->prof);
   unsigned long long* h = (unsigned long long*)ctx->h_pinned;
   TMC_CUDA(ctx, cudaMemcpyAsync(h, sc.totals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   TMC_CUDA(ctx, cudaStreamSynchronize(st));
@@ -374,7 +393,7 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
     delete mp;
     TMC_CUDA(ctx, ce);
   }
-  ctx->launches += tmc::dmc_front_emit(g, sc, vo, nv, quads, colors, (flags & TMC_GRAD_FLIP) ? 1 : 0, ctx->sms, st,
+  ctx->launches += tmc::dmc_front_emit(space, sc, vo, nv, quads, colors, (flags & TMC_GRAD_FLIP) ? 1 : 0, ctx->sms, st,
                                        &ctx->prof);
   TMC_CUDA(ctx, cudaGetLastError());
 
@@ -465,17 +484,19 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   Allocs al(ctx);
   const float* field = nullptr;
   if ((s = field_on_device(ctx, vol, al, &field))) return s;
-  const tmc::Grid g = make_grid(vol, field, iso);
+  tmc::Grid g = make_grid(vol, field, iso);
+  g.flags = (flags & TMC_OUT_POS_F64) ? tmc::kGridPos64 : 0;
   const int64_t ncell = g.ncells();
   tmc::TmcScratch sc{};
   TMC_CUDA(ctx, al.get(&sc.rec, ncell));
   TMC_CUDA(ctx, al.get(&sc.voff, ncell));
   TMC_CUDA(ctx, al.get(&sc.toff, ncell));
-  TMC_CUDA(ctx, al.get(&sc.tile_sums, tmc::tmc_tiles(g)));
+  const tmc::CellSpace space = tmc::single_space(g);
+  TMC_CUDA(ctx, al.get(&sc.tile_sums, tmc::tmc_tiles(space)));
   TMC_CUDA(ctx, al.get(&sc.totals, 2));
   sc.stats = ctx->d_stats;
   TMC_CUDA(ctx, cudaMemsetAsync(sc.stats, 0, 8 * sizeof(unsigned long long), st));
-  ctx->launches += tmc::tmc_count(g, sc, st, &ctx->prof);
+  ctx->launches += tmc::tmc_count(space, sc, st, &ctx->prof);
   unsigned long long* h = (unsigned long long*)ctx->h_pinned;
   TMC_CUDA(ctx, cudaMemcpyAsync(h, sc.totals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   TMC_CUDA(ctx, cudaMemcpyAsync(h + 1, sc.stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
@@ -504,7 +525,7 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   TMC_OWN(vo.n, 3 * nv);
   if (flags & TMC_OUT_POS_F64) TMC_OWN(vo.v64, 3 * nv);
   TMC_OWN(tris, 3 * nt);
-  ctx->launches += tmc::tmc_emit(g, sc, vo, tris, ctx->sms, st, &ctx->prof);
+  ctx->launches += tmc::tmc_emit(space, sc, vo, tris, ctx->sms, st, &ctx->prof);
   TMC_CUDA(ctx, cudaGetLastError());
   out->nr_v = nv;
   out->nr_t = nt;
@@ -553,6 +574,266 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   return finish_mesh(ctx, flags, out, mp);
 }
 
+// One batch of requests of one algorithm: all volumes share one cell space, so every stage is one
+// launch for the whole batch; one host synchronisation reads the per-volume output sizes.
+// Requests with simplification, triangles or halfedges finish with the per-mesh post-processing on
+// their slice of the batch's arrays.
+tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_request* reqs, tmc_mesh* outs, bool dmc) {
+  const int nb = (int)idx.size();
+  tmc_status s = TMC_OK;
+  bool any_f64 = false, any_n64 = false, any_local = false, any_amb = false;
+  for (int q = 0; q < nb; q++) {
+    const tmc_request& r = reqs[idx[q]];
+    if ((s = check_volume(ctx, &r.vol))) return fail(ctx, s, "request %d: %s", idx[q], ctx->err.c_str());
+    if (!std::isfinite(r.iso)) return fail(ctx, TMC_ERR_INVALID_ARG, "request %d: isovalue must be finite", idx[q]);
+    uint32_t f = r.flags;
+    if (f & TMC_DMC_SIMPLIFY) f |= TMC_DMC_P3X3Y_COLOR | TMC_DMC_P3X3Y_ISOLATED | TMC_DMC_P3333;
+    const bool simp = f & (TMC_DMC_P3X3Y_COLOR | TMC_DMC_P3X3Y_ISOLATED | TMC_DMC_P3333);
+    if (dmc) {
+      if ((f & TMC_OUT_LOCAL) && simp)
+        return fail(ctx, TMC_ERR_INVALID_ARG, "request %d: local coordinates exist only without simplification",
+                    idx[q]);
+      any_f64 |= (f & (TMC_OUT_POS_F64 | TMC_OUT_TRIANGLES)) || simp;
+      any_n64 |= simp;
+      any_local |= (f & TMC_OUT_LOCAL) != 0;
+    } else {
+      if (f & (TMC_DMC_SIMPLIFY | TMC_DMC_P3X3Y_COLOR | TMC_DMC_P3X3Y_ISOLATED | TMC_DMC_P3333 | TMC_OUT_LOCAL))
+        return fail(ctx, TMC_ERR_INVALID_ARG, "request %d: DMC-only flag given to a TMC extraction", idx[q]);
+      any_f64 |= (f & TMC_OUT_POS_F64) != 0;
+    }
+  }
+  TMC_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  Allocs al(ctx);
+  // ---- the cell space: volumes one after another, each from a tile boundary ----
+  std::vector<tmc::Grid> grids(nb);
+  std::vector<int64_t> tile0(nb + 1, 0);
+  for (int q = 0; q < nb; q++) {
+    const tmc_request& r = reqs[idx[q]];
+    const float* field = nullptr;
+    if ((s = field_on_device(ctx, &r.vol, al, &field))) return s;
+    grids[q] = make_grid(&r.vol, field, r.iso);
+    {
+      const bool simp = r.flags & (TMC_DMC_SIMPLIFY | TMC_DMC_P3X3Y_COLOR | TMC_DMC_P3X3Y_ISOLATED | TMC_DMC_P3333);
+      grids[q].flags = dmc ? (((r.flags & TMC_GRAD_FLIP) ? tmc::kGridFlip : 0) | (simp ? tmc::kGridNormal64 : 0))
+                           : ((r.flags & TMC_OUT_POS_F64) ? tmc::kGridPos64 : 0);
+    }
+    grids[q].vbase = tile0[q] * tmc::kScanTile;
+    tile0[q + 1] = tile0[q] + tmc::ceil_div(grids[q].ncells(), tmc::kScanTile);
+  }
+  const int64_t tiles = tile0[nb];
+  const int64_t ncell = tiles * tmc::kScanTile;
+  if (ncell > ((int64_t)1 << 32) - tmc::kScanTile)
+    return fail(ctx, TMC_ERR_CAPACITY, "batch of %lld cells: a batch holds at most 2^32 cells", (long long)ncell);
+  std::vector<int32_t> tile_vol((size_t)tiles);
+  for (int q = 0; q < nb; q++)
+    for (int64_t t = tile0[q]; t < tile0[q + 1]; t++) tile_vol[(size_t)t] = q;
+  tmc::Grid* d_grids = nullptr;
+  int32_t* d_tile_vol = nullptr;
+  TMC_CUDA(ctx, al.get(&d_grids, nb));
+  TMC_CUDA(ctx, al.get(&d_tile_vol, tiles));
+  TMC_CUDA(ctx, cudaMemcpyAsync(d_grids, grids.data(), nb * sizeof(tmc::Grid), cudaMemcpyHostToDevice, st));
+  TMC_CUDA(ctx, cudaMemcpyAsync(d_tile_vol, tile_vol.data(), tiles * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  tmc::CellSpace space{};
+  space.one = grids[0];
+  space.grids = d_grids;
+  space.tile_vol = d_tile_vol;
+  space.n = ncell;
+
+  // ---- count ----
+  uint32_t* rec = nullptr;
+  int32_t *voff = nullptr, *qoff = nullptr;
+  unsigned long long *tile_sums = nullptr, *totals = nullptr;
+  TMC_CUDA(ctx, al.get(&rec, ncell));
+  TMC_CUDA(ctx, al.get(&voff, ncell));
+  TMC_CUDA(ctx, al.get(&qoff, ncell));
+  TMC_CUDA(ctx, al.get(&tile_sums, tiles));
+  TMC_CUDA(ctx, al.get(&totals, 2));
+  TMC_CUDA(ctx, cudaMemsetAsync(ctx->d_stats, 0, 8 * sizeof(unsigned long long), st));
+  tmc::DmcScratch dsc{};
+  tmc::TmcScratch tsc{};
+  if (dmc) {
+    dsc = tmc::DmcScratch{rec, voff, qoff, nullptr, tile_sums, totals, ctx->d_stats};
+    ctx->launches += tmc::dmc_front_count(space, dsc, st, &ctx->prof);
+  } else {
+    tsc = tmc::TmcScratch{rec, voff, qoff, tile_sums, totals, ctx->d_stats, nullptr, nullptr};
+    ctx->launches += tmc::tmc_count(space, tsc, st, &ctx->prof);
+  }
+  std::vector<unsigned long long> toff((size_t)tiles + 1);
+  unsigned long long* h = (unsigned long long*)ctx->h_pinned;
+  TMC_CUDA(ctx, cudaMemcpyAsync(toff.data(), tile_sums, tiles * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  TMC_CUDA(ctx, cudaMemcpyAsync(h, totals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  TMC_CUDA(ctx, cudaMemcpyAsync(h + 1, ctx->d_stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  TMC_CUDA(ctx, cudaStreamSynchronize(st));
+  toff[(size_t)tiles] = h[0];
+  const int64_t NV = (int64_t)(h[0] >> 32), NF = (int64_t)(h[0] & 0xffffffffull);
+  const int64_t n_amb = (int64_t)h[2];
+  if (NV >= ((int64_t)1 << 31) || NF >= ((int64_t)1 << 31))
+    return fail(ctx, TMC_ERR_CAPACITY, "batch output above 2^31 vertices or faces; split the batch");
+  std::vector<int64_t> vb(nb + 1), fb(nb + 1);
+  for (int q = 0; q <= nb; q++) {
+    const unsigned long long w = toff[(size_t)tile0[q]];
+    vb[q] = (int64_t)(w >> 32);
+    fb[q] = (int64_t)(w & 0xffffffffull);
+  }
+
+  // ---- outputs shared by the batch's meshes ----
+  auto block = std::make_shared<SharedBlock>();
+  block->stream = st;
+  cudaError_t ce = cudaSuccess;
+  auto get_shared = [&](auto** p, int64_t count) -> cudaError_t {
+    ce = al.get(p, count);
+    if (ce == cudaSuccess) {
+      al.release(*p);
+      block->dev.push_back(*p);
+    }
+    return ce;
+  };
+  float *v = nullptr, *nn = nullptr, *vuvw = nullptr;
+  double *v64 = nullptr, *n64 = nullptr;
+  int64_t* vcell = nullptr;
+  int32_t* faces = nullptr;
+  uint8_t* colors = nullptr;
+  TMC_CUDA(ctx, get_shared(&v, 3 * NV));
+  TMC_CUDA(ctx, get_shared(&nn, 3 * NV));
+  if (any_f64) TMC_CUDA(ctx, get_shared(&v64, 3 * NV));
+  if (dmc) {
+    if (any_n64) TMC_CUDA(ctx, get_shared(&n64, 3 * NV));
+    if (any_local) {
+      TMC_CUDA(ctx, get_shared(&vcell, NV));
+      TMC_CUDA(ctx, get_shared(&vuvw, 3 * NV));
+    }
+    TMC_CUDA(ctx, get_shared(&faces, 4 * NF));
+    TMC_CUDA(ctx, get_shared(&colors, NF));
+    TMC_CUDA(ctx, al.get(&dsc.vwork, NV));
+    tmc::DmcVertexOut vo{v, nn, v64, n64, vcell, vuvw};
+    ctx->launches += tmc::dmc_front_emit(space, dsc, vo, NV, faces, colors, 0, ctx->sms, st, &ctx->prof);
+  } else {
+    TMC_CUDA(ctx, get_shared(&faces, 3 * NF));
+    TMC_CUDA(ctx, al.get(&tsc.amb_list, n_amb));
+    TMC_CUDA(ctx, al.get(&tsc.amb_count, 1));
+    tmc::TmcVertexOut vo{v, nn, v64};
+    ctx->launches += tmc::tmc_emit(space, tsc, vo, faces, ctx->sms, st, &ctx->prof);
+  }
+  TMC_CUDA(ctx, cudaGetLastError());
+
+  // ---- one mesh per request ----
+  for (int q = 0; q < nb; q++) {
+    const tmc_request& r = reqs[idx[q]];
+    tmc_mesh* out = &outs[idx[q]];
+    uint32_t f = r.flags;
+    if (f & TMC_DMC_SIMPLIFY) f |= TMC_DMC_P3X3Y_COLOR | TMC_DMC_P3X3Y_ISOLATED | TMC_DMC_P3333;
+    const bool simp = dmc && (f & (TMC_DMC_P3X3Y_COLOR | TMC_DMC_P3X3Y_ISOLATED | TMC_DMC_P3333));
+    const int64_t nv = vb[q + 1] - vb[q], nf = fb[q + 1] - fb[q];
+    MeshPriv* mp = new (std::nothrow) MeshPriv();
+    if (!mp) return fail(ctx, TMC_ERR_OOM, "host allocation failed");
+    mp->shared = block;
+    out->priv = mp;
+    out->stats[6] = grids[q].ncells();
+    float* sv = v + 3 * vb[q];
+    float* sn = nn + 3 * vb[q];
+    double* sv64 = v64 ? v64 + 3 * vb[q] : nullptr;
+    if (dmc) {
+      tmc::DmcMesh mesh{};
+      mesh.nv = nv;
+      mesh.nq = nf;
+      mesh.v = sv;
+      mesh.n = sn;
+      mesh.v64 = sv64;
+      mesh.n64 = n64 ? n64 + 3 * vb[q] : nullptr;
+      mesh.quads = faces + 4 * fb[q];
+      mesh.colors = colors + fb[q];
+      tmc::DmcPostOut post{};
+      if (simp || (f & (TMC_OUT_TRIANGLES | TMC_OUT_HALFEDGES))) {
+        tmc::DmcPostStatus ps = tmc::dmc_postprocess(mesh, f, ctx->sms, st, &post, &ctx->prof, true);
+        for (void* p : post.owned) mp->dev.push_back(p);
+        if (ps.err != cudaSuccess) TMC_CUDA(ctx, ps.err);
+        ctx->launches += ps.launches;
+      } else {
+        post.mesh = mesh;
+      }
+      out->nr_v = post.mesh.nv;
+      out->nr_q = post.mesh.nq;
+      out->v = post.mesh.v;
+      out->n = post.mesh.n;
+      out->v64 = (f & TMC_OUT_POS_F64) ? post.mesh.v64 : nullptr;
+      out->quads = post.mesh.quads;
+      out->nr_t = post.nt;
+      out->tris = post.tris;
+      out->nr_he = post.nhe;
+      out->he = post.he;
+      out->he_v = post.he_v;
+      out->he_f = post.he_f;
+      if (f & TMC_OUT_LOCAL) {
+        out->vcell = vcell + vb[q];
+        out->vuvw = vuvw + 3 * vb[q];
+      }
+      out->stats[4] = post.non_manifold;
+      // float64 arrays the post-processing made that are not outputs
+      auto drop = [&](void* ptr) {
+        if (!ptr) return;
+        for (auto& d : mp->dev)
+          if (d == ptr) {
+            d = nullptr;
+            cudaFreeAsync(ptr, st);
+          }
+      };
+      if (!(f & TMC_OUT_POS_F64)) drop(post.mesh.v64);
+      drop(post.mesh.n64);
+      std::vector<void*> keep;
+      for (void* d : mp->dev)
+        if (d) keep.push_back(d);
+      mp->dev.swap(keep);
+    } else {
+      out->nr_v = nv;
+      out->nr_t = nf;
+      out->v = sv;
+      out->n = sn;
+      out->v64 = (f & TMC_OUT_POS_F64) ? sv64 : nullptr;
+      out->tris = faces + 3 * fb[q];
+      if (f & TMC_OUT_HALFEDGES) {
+        const int64_t nh = 3 * nf;
+        int32_t *he5 = nullptr, *he4 = nullptr, *hv = nullptr, *hf = nullptr;
+        tmc::HeWork w{};
+        TMC_CUDA(ctx, al.get(&w.deg, nv));
+        TMC_CUDA(ctx, al.get(&w.off, nv));
+        TMC_CUDA(ctx, al.get(&w.cursor, nv));
+        TMC_CUDA(ctx, al.get(&w.list, nh));
+        TMC_CUDA(ctx, al.get(&w.hv_key, nv));
+        TMC_CUDA(ctx, al.get(&w.tiles, tmc::scan_tiles(nv) + 2));
+        TMC_CUDA(ctx, al.get(&w.total, 2));
+        TMC_CUDA(ctx, al.get(&w.non_manifold, 2));
+        TMC_CUDA(ctx, al.get(&he5, 5 * nh));
+        TMC_CUDA(ctx, cudaMemsetAsync(w.non_manifold, 0, 2 * sizeof(unsigned long long), st));
+        TMC_CUDA(ctx, al.get(&he4, 4 * nh));
+        al.release(he4);
+        mp->dev.push_back(he4);
+        TMC_CUDA(ctx, al.get(&hv, nv));
+        al.release(hv);
+        mp->dev.push_back(hv);
+        TMC_CUDA(ctx, al.get(&hf, nf));
+        al.release(hf);
+        mp->dev.push_back(hf);
+        tmc::HeOut ho{he5, hv, hf};
+        tmc::Stage stage(&ctx->prof, "tmc_halfedges", st);
+        ctx->launches += tmc::build_halfedges(out->tris, 3, nf, nv, ho, w, ctx->sms, st);
+        ctx->launches += tmc::pack_halfedges4(he5, nh, he4, ctx->sms, st);
+        TMC_CUDA(ctx, cudaGetLastError());
+        TMC_CUDA(ctx, cudaMemcpyAsync(h + 8, w.non_manifold, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        TMC_CUDA(ctx, cudaStreamSynchronize(st));
+        out->stats[4] = (int64_t)h[8];
+        out->nr_he = nh;
+        out->he = he4;
+        out->he_v = hv;
+        out->he_f = hf;
+      }
+    }
+    if ((s = finish_mesh(ctx, f, out, mp))) return s;
+  }
+  ctx->prof.collect();
+  return TMC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -562,8 +843,25 @@ tmc_status tmc_tmc_sharedvertex(tmc_ctx* ctx, const tmc_volume* vol, double iso,
 tmc_status tmc_tmc_halfedge(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t flags, tmc_mesh* out) {
   return tmc_extract(ctx, vol, iso, flags, out, true);
 }
-tmc_status tmc_batch_extract(tmc_ctx* ctx, int32_t, const tmc_request*, tmc_mesh*) {
-  return fail(ctx, TMC_ERR_INTERNAL, "batched extraction is not built yet");
+tmc_status tmc_batch_extract(tmc_ctx* ctx, int32_t n, const tmc_request* reqs, tmc_mesh* outs) {
+  if (!ctx) return TMC_ERR_INVALID_ARG;
+  if (n < 0 || (n > 0 && (!reqs || !outs))) return fail(ctx, TMC_ERR_INVALID_ARG, "bad request array");
+  for (int32_t b = 0; b < n; b++) mesh_reset(&outs[b]);
+  std::vector<int> dmc, tmcs;
+  for (int32_t b = 0; b < n; b++) {
+    if (reqs[b].algo == TMC_ALGO_DMC) dmc.push_back(b);
+    else if (reqs[b].algo == TMC_ALGO_TMC) tmcs.push_back(b);
+    else return fail(ctx, TMC_ERR_INVALID_ARG, "request %d: unknown algorithm %u", b, reqs[b].algo);
+  }
+  tmc_status s = TMC_OK;
+  if (!dmc.empty()) s = batch_run(ctx, dmc, reqs, outs, true);
+  if (!s && !tmcs.empty()) s = batch_run(ctx, tmcs, reqs, outs, false);
+  if (s) {
+    const std::string msg = ctx->err;
+    for (int32_t b = 0; b < n; b++) tmc_mesh_free(ctx, &outs[b]);
+    ctx->err = msg;
+  }
+  return s;
 }
 }
 

@@ -453,15 +453,21 @@ __device__ void load_amb_cell(const Grid& g, int i, int j, int k, const float u[
 // ------------------------------------------------------------------------------------------
 // kernels
 // ------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kScanThreads) tmc_classify_kernel(Grid g, uint32_t* rec,
+__global__ void __launch_bounds__(kScanThreads) tmc_classify_kernel(CellSpace space, uint32_t* rec,
                                                                    unsigned long long* tile_sums,
                                                                    unsigned long long* stats) {
+  const Grid g = space.grid_of_tile(blockIdx.x);
   const int64_t n = g.ncells();
-  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  const int64_t vbase = (int64_t)blockIdx.x * kScanTile;
   unsigned long long local = 0, act = 0, amb = 0;
   for (int s = 0; s < kScanItems; s++) {
-    const int64_t c = base + (int64_t)s * kScanThreads + threadIdx.x;
-    if (c >= n) break;
+    const int64_t vc = vbase + (int64_t)s * kScanThreads + threadIdx.x;
+    if (vc >= space.n) break;
+    const int64_t c = vc - g.vbase;
+    if (c >= n) {  // padding after the volume's last cell
+      rec[vc] = 0;
+      continue;
+    }
     int i, j, k;
     tcell_ijk(g, c, i, j, k);
     float u[8];
@@ -482,7 +488,7 @@ __global__ void __launch_bounds__(kScanThreads) tmc_classify_kernel(Grid g, uint
       }
       act++;
     }
-    rec[c] = r;
+    rec[vc] = r;
     local += ((unsigned long long)trec_nv(r) << 32) | (unsigned long long)trec_ntri(r);
   }
   unsigned long long tot;
@@ -539,22 +545,24 @@ __device__ __forceinline__ int compact_tile(const uint32_t* rec, int64_t base, i
 
 // Ambiguous cells of each tile, densely: p_slice in counting mode (float64), then the counts go into
 // the cell record and the tile's sum.
-__global__ void __launch_bounds__(kScanThreads) tmc_amb_count_kernel(Grid g, uint32_t* rec,
+__global__ void __launch_bounds__(kScanThreads) tmc_amb_count_kernel(CellSpace space, uint32_t* rec,
                                                                     unsigned long long* tile_sums,
                                                                     unsigned long long* stats) {
   __shared__ uint32_t list[kScanTile];
   __shared__ int wcount[kScanThreads / 32];
   __shared__ int total;
   __shared__ unsigned long long add;
-  const int64_t n = g.ncells();
+  const int64_t n = space.n;
   unsigned long long sing = 0;
   for (int64_t tile = blockIdx.x; tile * kScanTile < n; tile += gridDim.x) {
     const int64_t base = tile * kScanTile;
+    const Grid g = space.grid_of_tile(tile);
     if (threadIdx.x == 0) add = 0;
     const int na = compact_tile(rec, base, n, [](uint32_t r) { return ((r >> 21) & 1) != 0; }, list, wcount, &total);
     unsigned long long local = 0;
     for (int a = threadIdx.x; a < na; a += blockDim.x) {
-      const int64_t cell = base + list[a];
+      const int64_t vcell = base + list[a];
+      const int64_t cell = vcell - g.vbase;
       int i, j, k;
       tcell_ijk(g, cell, i, j, k);
       float u[8];
@@ -568,7 +576,7 @@ __global__ void __launch_bounds__(kScanThreads) tmc_amb_count_kernel(Grid g, uin
       for (int e = 0; e < 12; e++) vid[e] = 0;
       TriSink ts{nullptr, 0};
       const AmbResult ar = p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, 0, ts, amb.P, amb.N, nullptr);
-      rec[cell] |= (uint32_t)ar.inner << 12 | (uint32_t)ts.n << 15 | (ar.error ? (1u << 22) : 0u);
+      rec[vcell] |= (uint32_t)ar.inner << 12 | (uint32_t)ts.n << 15 | (ar.error ? (1u << 22) : 0u);
       local += ((unsigned long long)ar.inner << 32) | (unsigned long long)ts.n;
       sing += ar.error;
     }
@@ -676,32 +684,39 @@ __device__ __forceinline__ void edge_vertex_f32(const Grid& g, int i, int j, int
   for (int d = 0; d < 3; d++) out.n[base + d] = in[d] * rn;
 }
 
+// Vertex index of each crossed edge of a cell, within the cell's volume (vfirst: the volume's first
+// vertex in the space-wide numbering; vbase: the cell's first vertex, space-wide).
 __device__ __forceinline__ void tmc_vertex_ids(const Grid& g, int i, int j, int k, uint32_t em, uint32_t own,
-                                               int32_t vbase, const uint32_t* rec, const int32_t* voff,
-                                               int32_t vid[12]) {
+                                               int32_t vbase, int32_t vfirst, const uint32_t* rec,
+                                               const int32_t* voff, int32_t vid[12]) {
   int rank = 0;
   for (int e = 0; e < 12; e++) {
     vid[e] = -1;
     if (!(em & (1u << e))) continue;
     if (own & (1u << e)) {
-      vid[e] = vbase + rank++;
+      vid[e] = vbase - vfirst + rank++;
     } else {
       int oi, oj, ok, oe = 0;
       edge_owner(i, j, k, e, oi, oj, ok, oe);
-      const int64_t oc = g.cell_index(oi, oj, ok);
-      vid[e] = voff[oc] + __popc(trec_owned(rec[oc]) & ((1u << oe) - 1u));
+      const int64_t oc = g.vcell(oi, oj, ok);
+      vid[e] = voff[oc] - vfirst + __popc(trec_owned(rec[oc]) & ((1u << oe) - 1u));
     }
   }
 }
 
 // Ambiguous cells (listed by the emit kernel): p_slice triangles and inner vertices, float64.
-__global__ void __launch_bounds__(128) tmc_ambiguous_kernel(Grid g, const uint32_t* rec, const int32_t* voff,
-                                                            const int32_t* toff, TmcVertexOut out, int32_t* tris,
-                                                            const uint32_t* list, const unsigned* count) {
+__global__ void __launch_bounds__(128) tmc_ambiguous_kernel(CellSpace space, const uint32_t* rec,
+                                                            const int32_t* voff, const int32_t* toff,
+                                                            const unsigned long long* tile_off, TmcVertexOut out,
+                                                            int32_t* tris, const uint32_t* list,
+                                                            const unsigned* count) {
   const unsigned na = *count;
   for (unsigned a = blockIdx.x * blockDim.x + threadIdx.x; a < na; a += gridDim.x * blockDim.x) {
-    const int64_t cell = list[a];
-    const uint32_t r = rec[cell];
+    const int64_t vcell = list[a];
+    const uint32_t r = rec[vcell];
+    const Grid g = space.grid_of_tile(vcell / kScanTile);
+    const int32_t vfirst = (int32_t)(tile_off[g.vbase / kScanTile] >> 32);
+    const int64_t cell = vcell - g.vbase;
     int i, j, k;
     tcell_ijk(g, cell, i, j, k);
     float u[8];
@@ -712,29 +727,33 @@ __global__ void __launch_bounds__(128) tmc_ambiguous_kernel(Grid g, const uint32
     const uint32_t em = case_edge_mask(cs);
     const uint32_t own = trec_owned(r);
     int32_t vid[12];
-    tmc_vertex_ids(g, i, j, k, em, own, voff[cell], rec, voff, vid);
-    TriSink ts{tris + 3 * (int64_t)toff[cell], 0};
+    tmc_vertex_ids(g, i, j, k, em, own, voff[vcell], vfirst, rec, voff, vid);
+    TriSink ts{tris + 3 * (int64_t)toff[vcell], 0};
     AmbCell amb;
     load_amb_cell(g, i, j, k, u, em, amb, true);
-    InnerOut io{out.v, out.n, out.v64};
-    p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, voff[cell] + __popc(own), ts, amb.P, amb.N, &io);
+    // inner vertices are numbered within the volume: shift the outputs to its first vertex
+    InnerOut io{out.v + 3 * (int64_t)vfirst, out.n + 3 * (int64_t)vfirst, out.v64 ? out.v64 + 3 * (int64_t)vfirst : nullptr};
+    p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, voff[vcell] - vfirst + __popc(own), ts, amb.P, amb.N, &io);
   }
 }
 
-__global__ void __launch_bounds__(256) tmc_emit_kernel(Grid g, const uint32_t* rec, const int32_t* voff,
-                                                       const int32_t* toff, TmcVertexOut out, int32_t* tris,
-                                                       uint32_t* amb_list, unsigned* amb_count) {
+__global__ void __launch_bounds__(256) tmc_emit_kernel(CellSpace space, const uint32_t* rec, const int32_t* voff,
+                                                       const int32_t* toff, const unsigned long long* tile_off,
+                                                       TmcVertexOut out, int32_t* tris, uint32_t* amb_list,
+                                                       unsigned* amb_count) {
   // One block per scan tile: the tile's active cells are compacted into shared memory with warp
   // ballots, then processed one per thread.
   __shared__ uint32_t active[kScanTile];
   __shared__ int wcount[kScanThreads / 32];
   __shared__ int total;
-  const int64_t n = g.ncells();
-  const float inv[3] = {(float)(1.0 / g.dx), (float)(1.0 / g.dy), (float)(1.0 / g.dz)};
-  const float inv2[3] = {(float)(1.0 / (2 * g.dx)), (float)(1.0 / (2 * g.dy)), (float)(1.0 / (2 * g.dz))};
+  const int64_t n = space.n;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int64_t tile = blockIdx.x; tile * kScanTile < n; tile += gridDim.x) {
     const int64_t base = tile * kScanTile;
+    const Grid g = space.grid_of_tile(tile);
+    const int32_t vfirst = (int32_t)(tile_off[g.vbase / kScanTile] >> 32);
+    const float inv[3] = {(float)(2 * g.inv2[0]), (float)(2 * g.inv2[1]), (float)(2 * g.inv2[2])};
+    const float inv2[3] = {(float)g.inv2[0], (float)g.inv2[1], (float)g.inv2[2]};
     // compaction: thread t looks at cells base + s*256 + t
     int mine = 0;
     bool act[kScanItems];
@@ -769,8 +788,9 @@ __global__ void __launch_bounds__(256) tmc_emit_kernel(Grid g, const uint32_t* r
     __syncthreads();
     const int na = total;
     for (int a = threadIdx.x; a < na; a += blockDim.x) {
-      const int64_t cell = base + active[a];
-      const uint32_t r = rec[cell];
+      const int64_t vcell = base + active[a];
+      const int64_t cell = vcell - g.vbase;
+      const uint32_t r = rec[vcell];
       int i, j, k;
       tcell_ijk(g, cell, i, j, k);
       float u[8];
@@ -780,24 +800,24 @@ __global__ void __launch_bounds__(256) tmc_emit_kernel(Grid g, const uint32_t* r
       for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
       const uint32_t em = case_edge_mask(cs);
       const uint32_t own = trec_owned(r);
-      const int32_t vbase = voff[cell];
+      const int32_t vbase = voff[vcell];
       // owned edge vertices, in edge order
       int rank = 0;
       for (int e = 0; e < 12; e++) {
         if ((em & own) & (1u << e)) {
-          if (out.v64) edge_vertex_f64(g, i, j, k, e, u, out, vbase + rank);
+          if (out.v64 && (g.flags & kGridPos64)) edge_vertex_f64(g, i, j, k, e, u, out, vbase + rank);
           else edge_vertex_f32(g, i, j, k, e, u, out, vbase + rank, inv, inv2);
           rank++;
         }
       }
       if ((r >> 21) & 1) {
         // ambiguous: triangles and inner vertices in a separate float64 pass
-        if (!((r >> 22) & 1)) amb_list[atomicAdd(amb_count, 1u)] = (uint32_t)cell;
+        if (!((r >> 22) & 1)) amb_list[atomicAdd(amb_count, 1u)] = (uint32_t)vcell;
         continue;
       }
       int32_t vid[12];
-      tmc_vertex_ids(g, i, j, k, em, own, vbase, rec, voff, vid);
-      TriSink ts{tris + 3 * (int64_t)toff[cell], 0};
+      tmc_vertex_ids(g, i, j, k, em, own, vbase, vfirst, rec, voff, vid);
+      TriSink ts{tris + 3 * (int64_t)toff[vcell], 0};
       {
         // unambiguous: table triangles with reversed winding (t_mc, mc/MarchingCubes.cpp:276-294)
         const uint64_t tw = c_tmc_tris[cs];
@@ -816,19 +836,19 @@ __global__ void __launch_bounds__(256) tmc_emit_kernel(Grid g, const uint32_t* r
 // ------------------------------------------------------------------------------------------
 // host-side launches
 // ------------------------------------------------------------------------------------------
-int64_t tmc_tiles(const Grid& g) { return ceil_div(g.ncells(), kScanTile); }
+int64_t tmc_tiles(const CellSpace& space) { return ceil_div(space.n, kScanTile); }
 
-int tmc_count(const Grid& g, TmcScratch& s, cudaStream_t st, Prof* prof) {
-  const int64_t n = g.ncells();
-  const int64_t tiles = tmc_tiles(g);
+int tmc_count(const CellSpace& space, TmcScratch& s, cudaStream_t st, Prof* prof) {
+  const int64_t n = space.n;
+  const int64_t tiles = tmc_tiles(space);
   {
     Stage t(prof, "tmc_classify", st);
-    tmc_classify_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(g, s.rec, s.tile_sums, s.stats);
+    tmc_classify_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(space, s.rec, s.tile_sums, s.stats);
   }
   {
     Stage ta(prof, "tmc_amb_count", st);
-    tmc_amb_count_kernel<<<(unsigned)std::min<int64_t>(tiles, 65535), kScanThreads, 0, st>>>(g, s.rec, s.tile_sums,
-                                                                                              s.stats);
+    tmc_amb_count_kernel<<<(unsigned)std::min<int64_t>(tiles, 65535), kScanThreads, 0, st>>>(space, s.rec,
+                                                                                              s.tile_sums, s.stats);
   }
   Stage t(prof, "tmc_scan", st);
   scan_tile_sums_kernel<<<1, 1024, 0, st>>>(s.tile_sums, tiles, s.totals);
@@ -836,17 +856,17 @@ int tmc_count(const Grid& g, TmcScratch& s, cudaStream_t st, Prof* prof) {
   return 4;
 }
 
-int tmc_emit(const Grid& g, TmcScratch& s, TmcVertexOut vo, int32_t* tris, int sms, cudaStream_t st,
+int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tris, int sms, cudaStream_t st,
              Prof* prof) {
   Stage t(prof, "tmc_emit", st);
-  const int64_t tiles = tmc_tiles(g);
-  const int64_t blocks = std::min<int64_t>(tiles, (int64_t)sms * 8);
+  const int64_t tiles = tmc_tiles(space);
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sms * 8));
   cudaMemsetAsync(s.amb_count, 0, sizeof(unsigned), st);
-  tmc_emit_kernel<<<(unsigned)blocks, kScanThreads, 0, st>>>(g, s.rec, s.voff, s.toff, vo, tris, s.amb_list,
-                                                            s.amb_count);
+  tmc_emit_kernel<<<(unsigned)blocks, kScanThreads, 0, st>>>(space, s.rec, s.voff, s.toff, s.tile_sums, vo, tris,
+                                                            s.amb_list, s.amb_count);
   Stage t2(prof, "tmc_ambiguous", st);
-  tmc_ambiguous_kernel<<<(unsigned)std::max<int64_t>(1, (int64_t)sms * 8), 128, 0, st>>>(g, s.rec, s.voff, s.toff, vo,
-                                                                                         tris, s.amb_list, s.amb_count);
+  tmc_ambiguous_kernel<<<(unsigned)std::max<int64_t>(1, (int64_t)sms * 8), 128, 0, st>>>(
+      space, s.rec, s.voff, s.toff, s.tile_sums, vo, tris, s.amb_list, s.amb_count);
   return 2;
 }
 

@@ -25,9 +25,11 @@ struct TmcScratch {
   unsigned* amb_count;
 };
 
-int64_t tmc_tiles(const Grid& g);
-int tmc_count(const Grid& g, TmcScratch& s, cudaStream_t st, Prof* prof = nullptr);
-int tmc_emit(const Grid& g, TmcScratch& s, TmcVertexOut vo, int32_t* tris, int sms, cudaStream_t st,
+// Per-cell scratch is indexed in the cell space; triangles hold vertex indices within their own
+// volume, and the volumes' vertices and triangles follow one another in the outputs.
+int64_t tmc_tiles(const CellSpace& space);
+int tmc_count(const CellSpace& space, TmcScratch& s, cudaStream_t st, Prof* prof = nullptr);
+int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tris, int sms, cudaStream_t st,
              Prof* prof = nullptr);
 
 }  // namespace tmc

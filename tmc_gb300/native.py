@@ -206,6 +206,25 @@ class Context:
         self._check(self.lib.tmc_dmc_count_static(self.h, ctypes.byref(volume), float(iso), counts))
         return tuple(counts)
 
+    def batch_raw(self, volumes: list, isos: list, algos: list, flags: list) -> list:
+        """tmc_batch_extract over prepared tmc_volume structs; returns the meshes (caller frees)."""
+        n = len(volumes)
+        reqs = (Request * n)()
+        for q in range(n):
+            reqs[q].vol = volumes[q]
+            reqs[q].iso = float(isos[q])
+            reqs[q].algo = int(algos[q])
+            reqs[q].flags = int(flags[q])
+        outs = (Mesh * n)()
+        self._check(self.lib.tmc_batch_extract(self.h, n, reqs, outs))
+        return [outs[q] for q in range(n)]
+
+    def batch(self, vols: list, algos: list, flags: list) -> list:
+        """Batched extraction of host volumes (tmc_gb300.volumes.Volume); numpy results."""
+        tv = [make_volume(v) for v in vols]
+        ms = self.batch_raw(tv, [v.iso for v in vols], algos, [f | OUT_HOST for f in flags])
+        return [self.fetch(m) for m in ms]
+
     # -- numpy results --------------------------------------------------------------------
     def fetch(self, m: Mesh) -> dict:
         """Copy a host-resident mesh (OUT_HOST) into numpy arrays and free it."""
