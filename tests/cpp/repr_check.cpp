@@ -39,7 +39,7 @@ int main(int argc, char** argv) {
   if (!in || fread(f.data(), 4, f.size(), in) != f.size()) return 3;
   fclose(in);
   const float iso_up = [&] { float x = (float)iso; if ((double)x < iso) x = nextafterf(x, INFINITY); return x; }();
-  long contours = 0, mism = 0;
+  long contours = 0, mism = 0, two_pass = 0;
   repr::Stats se, sf;
   for (int k = 0; k < nz - 1; k++)
     for (int j = 0; j < ny - 1; j++)
@@ -81,6 +81,22 @@ int main(int argc, char** argv) {
           float pf[3];
           float lb[49];
           repr::representative_fast(u, iso, c, t, pts[t], sz, bx, pf, sf, lb, 1);
+          // the two-pass form must agree wherever it applies
+          {
+            repr::ProjRecord R;
+            int f64c = 0;
+            if (repr::projection_record(u, iso, c, t, pts[t], sz, bx, R, f64c)) {
+              float pr[3];
+              const int rr = repr::projection_from_record(R, pr, lb, 1);
+              if (rr == 0) {
+                two_pass++;
+                if (pr[0] != pf[0] || pr[1] != pf[1] || pr[2] != pf[2]) {
+                  if (mism < 5) fprintf(stderr, "two-pass differs cell %d %d %d t %d\n", i, j, k, t);
+                  mism++;
+                }
+              }
+            }
+          }
           contours++;
           if ((float)pe[0] != pf[0] || (float)pe[1] != pf[1] || (float)pe[2] != pf[2]) {
             if (mism < 5)
@@ -91,6 +107,6 @@ int main(int argc, char** argv) {
         }
       }
   mism += g_decider_mismatch;
-  printf("%ld %ld %d %d %d %d %d\n", contours, mism, sf.fallback, sf.fail1, sf.fail2, se.fail1, se.fail2);
+  printf("%ld %ld %d %d %d %d %d %ld\n", contours, mism, sf.fallback, sf.fail1, sf.fail2, se.fail1, se.fail2, two_pass);
   return 0;
 }

@@ -48,7 +48,7 @@ def test_fast_representative_matches_exact(checker, tmp_path, name):
     nx, ny, nz = vol.dims
     r = subprocess.run([str(checker), str(f), str(nx), str(ny), str(nz), repr(vol.iso)], capture_output=True,
                        text=True, check=True)
-    contours, mism, f64, fail1f, fail2f, fail1e, fail2e = (int(x) for x in r.stdout.split())
+    contours, mism, f64, fail1f, fail2f, fail1e, fail2e, two_pass = (int(x) for x in r.stdout.split())
     assert contours > 0
     assert mism == 0, r.stderr
     assert (fail1f, fail2f) == (fail1e, fail2e)

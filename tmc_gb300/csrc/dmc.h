@@ -17,6 +17,10 @@ struct DmcVertexOut {
   float* vuvw;
 };
 
+namespace repr {
+struct ProjRecord;
+}
+
 struct DmcScratch {
   uint32_t* rec;                  // per cell
   int32_t* voff;                  // per cell
@@ -25,7 +29,13 @@ struct DmcScratch {
   unsigned long long* tile_sums;  // per scan tile
   unsigned long long* totals;     // [0] = (vertices << 32) | quads
   unsigned long long* stats;      // 8 counters
+  // two-pass vertices (per vertex): projection records, projected points, the one-pass list
+  repr::ProjRecord* proj;
+  float4* vp;
+  uint32_t* fb_list;
+  unsigned* fb_count;
 };
+constexpr size_t kProjRecordBytes = 144;  // sizeof(repr::ProjRecord)
 
 // Each launcher returns the number of kernels it launched.
 // Per-cell scratch is indexed in the cell space (space.n cells, padding included).

@@ -29,6 +29,8 @@
 
 namespace tmc {
 
+static_assert(sizeof(repr::ProjRecord) == kProjRecordBytes, "record size");
+
 __constant__ uint64_t c_case_contour[256] = TMC_CASE_CONTOUR_INIT;
 
 // ------------------------------------------------------------------------------------------
@@ -166,8 +168,176 @@ __device__ __forceinline__ void point_gradient_f(const Grid& g, int i, int j, in
 }
 
 constexpr int kVertexThreads = 128;
+
+// The current volume's grid and the constants derived from it, cached per thread (a batch mixes
+// volumes; consecutive vertices mostly share one).
+struct GridCache {
+  int vol = -1;
+  Grid g{};
+  ffx::ff iso_ff{0, 0};
+  float inv2d[3] = {0, 0, 0};
+  ffx::ff inv2d_ff[3] = {{0, 0}, {0, 0}, {0, 0}};
+  __device__ __forceinline__ void load(const CellSpace& space, uint32_t vcell) {
+    const int v = space.grids ? __ldg(space.tile_vol + vcell / kScanTile) : 0;
+    if (v == vol) return;
+    vol = v;
+    g = space.grids ? space.grids[v] : space.one;
+    iso_ff = ffx::ff_from_double(g.iso);
+    for (int d = 0; d < 3; d++) {
+      inv2d[d] = (float)g.inv2[d];
+      inv2d_ff[d] = ffx::ff_from_double(g.inv2[d]);
+    }
+  }
+};
+
+// The contour behind vertex `rank` of a cell: corners, MC polygon, and the edge points and bounding
+// boxes of all its contours (slice, cpp_dmc/DualMarchingCubes.cpp:114-136).
+struct VertexContour {
+  float u[8];
+  uint64_t c;
+  repr::Boxes bx;
+  float pts[36];
+  int tsel, tstart;
+};
+__device__ __forceinline__ bool vertex_contour(const Grid& g, int i, int j, int k, int rank, const uint64_t* cc,
+                                               ffx::ff iso_ff, VertexContour& V) {
+  load_corners(g, i, j, k, V.u);
+  const unsigned cs = mc_case(V.u, g.iso_up);
+  V.c = dmc_polygon(cs, V.u, g.iso, cc);
+  const int ncnt = cnt_count(V.c);
+  int flat = 0, used_seen = 0;
+  V.tsel = -1;
+  V.tstart = 0;
+  for (int t = 0; t < ncnt; t++) {
+    V.bx.b[t][0][0] = 1; V.bx.b[t][0][1] = 0;
+    V.bx.b[t][1][0] = 1; V.bx.b[t][1][1] = 0;
+    V.bx.b[t][2][0] = 1; V.bx.b[t][2][1] = 0;
+    const int sz = cnt_size(V.c, t);
+    bool used = false;
+    for (int q = 0; q < sz; q++) {
+      const int e = cnt_edge(V.c, flat + q);
+      used = used || edge_interior(g, i, j, k, e);
+      bool fb = false;
+      const float l = repr::edge_param_fast(e, V.u, g.iso, iso_ff, fb);
+      float ui[3];
+      repr::local_from_param(e, l, ui);
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        V.pts[3 * (flat + q) + d] = ui[d];
+        V.bx.b[t][d][0] = V.bx.b[t][d][0] > ui[d] ? ui[d] : V.bx.b[t][d][0];
+        V.bx.b[t][d][1] = V.bx.b[t][d][1] < ui[d] ? ui[d] : V.bx.b[t][d][1];
+      }
+    }
+    if (used) {
+      if (used_seen == rank) {
+        V.tsel = t;
+        V.tstart = flat;
+      }
+      used_seen++;
+    }
+    flat += sz;
+  }
+  return V.tsel >= 0;
+}
+
+// Position, normal and local coordinates of vertex vidx at local coordinates p of cell (i, j, k).
+__device__ __forceinline__ void vertex_outputs(const GridCache& G, int i, int j, int k, int64_t cell,
+                                               const float p[3], int64_t vidx, const DmcVertexOut& out, int flip,
+                                               repr::Stats& st) {
+  const Grid& g = G.g;
+  const int64_t o = 3 * vidx;
+  // position: UniformGrid::position (cpp_dmc/UniformGrid.h:300-305)
+  const double px = g.ox + (i + (double)p[0]) * g.dx;
+  const double py = g.oy + (j + (double)p[1]) * g.dy;
+  const double pz = g.oz + (k + (double)p[2]) * g.dz;
+  out.v[o] = (float)px;
+  out.v[o + 1] = (float)py;
+  out.v[o + 2] = (float)pz;
+  if (out.v64) {
+    out.v64[o] = px;
+    out.v64[o + 1] = py;
+    out.v64[o + 2] = pz;
+  }
+  // normal: trilinear interpolation of the 8 corner gradients, normalised (UniformGrid::normal,
+  // cpp_dmc/UniformGrid.h:286-298).  When it is kept for the simplification merges it is computed
+  // in float-float (relative error ~2^-40, far below the float32 output's 2^-24) on the FP32 pipes.
+  if (out.n64 && (g.flags & kGridNormal64)) {
+    ffx::ff Gq[8][3];
+#pragma unroll
+    for (int q = 0; q < 8; q++) point_diff_ff(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), Gq[q]);
+    ffx::ff nv3[3];
+    float scale = 0;  // largest |difference| * 1/(2 spacing): the size of the interpolation's inputs
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      float md = 0;
+#pragma unroll
+      for (int q = 0; q < 8; q++) md = fmaxf(md, fabsf(Gq[q][d].hi));
+      scale = fmaxf(scale, md * G.inv2d[d]);
+      const ffx::ff a0 = ff_lerp(Gq[0][d], Gq[1][d], p[0]), a1 = ff_lerp(Gq[2][d], Gq[3][d], p[0]);
+      const ffx::ff a2 = ff_lerp(Gq[4][d], Gq[5][d], p[0]), a3 = ff_lerp(Gq[6][d], Gq[7][d], p[0]);
+      const ffx::ff b0 = ff_lerp(a0, a1, p[1]), b1 = ff_lerp(a2, a3, p[1]);
+      const ffx::ff t = ffx::ff_mul(ff_lerp(b0, b1, p[2]), G.inv2d_ff[d]);
+      nv3[d] = flip ? ffx::ff_neg(t) : t;
+    }
+    const ffx::ff dot =
+        ffx::ff_add(ffx::ff_add(ffx::ff_mul(nv3[0], nv3[0]), ffx::ff_mul(nv3[1], nv3[1])), ffx::ff_mul(nv3[2], nv3[2]));
+    // 1/sqrt(dot): float estimate and one Newton step in float-float
+    const float r0 = rsqrtf(dot.hi);
+    const ffx::ff h = ffx::ff_mul_f(ffx::ff_mul_f(dot, r0), r0);
+    const ffx::ff r = ffx::ff_mul_f(ffx::ff_sub(ffx::ff_from(1.5f), ffx::ff_mul_f(h, 0.5f)), r0);
+    if (scale <= 0x1p10f * sqrtf(dot.hi)) {
+      for (int d = 0; d < 3; d++) {
+        const ffx::ff x = ffx::ff_mul(nv3[d], r);
+        out.n64[o + d] = (double)x.hi + (double)x.lo;
+        out.n[o + d] = x.hi;
+      }
+    } else {
+      // the gradients cancel to below 2^-10 of their size: float64, as the reference
+      const Normal64 nf = normal_f64(g, i, j, k, p[0], p[1], p[2], flip);
+      for (int d = 0; d < 3; d++) {
+        out.n64[o + d] = nf.n[d];
+        out.n[o + d] = (float)nf.n[d];
+      }
+      st.normal_f64++;
+    }
+  } else {
+    float Gq[8][3];
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+      point_gradient_f(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), (float*)G.inv2d, Gq[q]);
+    float nv3[3];
+    const float uu = p[0], vv = p[1], ww = p[2];
+    const float sgn = flip ? -1.0f : 1.0f;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const float a0 = fmaf(uu, Gq[1][d] - Gq[0][d], Gq[0][d]), a1 = fmaf(uu, Gq[3][d] - Gq[2][d], Gq[2][d]);
+      const float a2 = fmaf(uu, Gq[5][d] - Gq[4][d], Gq[4][d]), a3 = fmaf(uu, Gq[7][d] - Gq[6][d], Gq[6][d]);
+      const float b0 = fmaf(vv, a1 - a0, a0), b1 = fmaf(vv, a3 - a2, a2);
+      nv3[d] = sgn * fmaf(ww, b1 - b0, b0);
+    }
+    const float rn = rsqrtf(nv3[0] * nv3[0] + nv3[1] * nv3[1] + nv3[2] * nv3[2]);
+    for (int d = 0; d < 3; d++) out.n[o + d] = nv3[d] * rn;
+  }
+  if (out.vcell) {
+    out.vcell[vidx] = cell;
+    out.vuvw[o] = p[0];
+    out.vuvw[o + 1] = p[1];
+    out.vuvw[o + 2] = p[2];
+  }
+}
+
+__device__ __forceinline__ void flush_stats(const repr::Stats& st, unsigned long long* stats) {
+  // representative counters (the reference's failed-projection counts) and float64 fallbacks
+  if (st.fail1) atomicAdd(stats + 2, (unsigned long long)st.fail1);
+  if (st.fail2) atomicAdd(stats + 3, (unsigned long long)st.fail2);
+  if (st.fallback + st.normal_f64) atomicAdd(stats + 7, (unsigned long long)(st.fallback + st.normal_f64));
+}
+
+// One-pass vertex kernel: every vertex of the list (all nv when list is null), with every fallback
+// of the reference's arithmetic (neighbour-contour exclusion, float64 samples, the 26x26 tail).
 __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_kernel(CellSpace space, const int32_t* voff,
                                                                      const uint32_t* vwork, int64_t nv,
+                                                                     const uint32_t* list, const unsigned* count,
                                                                      DmcVertexOut out, int flip_all,
                                                                      unsigned long long* stats) {
   __shared__ uint64_t cc[256];
@@ -175,154 +345,106 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_kernel(CellSpace sp
   for (int c = threadIdx.x; c < 256; c += blockDim.x) cc[c] = c_case_contour[c];
   __syncthreads();
   repr::Stats st;
-  int gvol = -1;  // volume whose grid is loaded
-  Grid g{};
-  ffx::ff iso_ff{0, 0};
-  float inv2d[3] = {0, 0, 0};
-  ffx::ff inv2d_ff[3] = {{0, 0}, {0, 0}, {0, 0}};
-  for (int64_t vidx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vidx < nv;
-       vidx += (int64_t)gridDim.x * blockDim.x) {
+  GridCache G;
+  const int64_t n = list ? (int64_t)*count : nv;
+  for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t vidx = list ? (int64_t)list[a] : a;
     const uint32_t vcell = vwork[vidx];
     const int rank = (int)(vidx - voff[vcell]);
-    const int vol = space.grids ? __ldg(space.tile_vol + vcell / kScanTile) : 0;
-    if (vol != gvol) {
-      g = space.grids ? space.grids[vol] : space.one;
-      gvol = vol;
-      iso_ff = ffx::ff_from_double(g.iso);
-      for (int d = 0; d < 3; d++) {
-        inv2d[d] = (float)g.inv2[d];
-        inv2d_ff[d] = ffx::ff_from_double(g.inv2[d]);
-      }
-    }
+    G.load(space, vcell);
+    const Grid& g = G.g;
     const int64_t cell = vcell - g.vbase;
     const int flip = flip_all | (g.flags & kGridFlip);
     int i, j, k;
     cell_ijk(g, cell, i, j, k);
-    float u[8];
-    load_corners(g, i, j, k, u);
-    const unsigned cs = mc_case(u, g.iso_up);
-    const uint64_t c = dmc_polygon(cs, u, g.iso, cc);
-    const int ncnt = cnt_count(c);
-    // edge points and bounding boxes of all contours (slice, cpp_dmc/DualMarchingCubes.cpp:114-136)
-    repr::Boxes bx;
-    float pts[36];
-    int flat = 0, tsel = -1, tstart = 0, used_seen = 0;
-    for (int t = 0; t < ncnt; t++) {
-      bx.b[t][0][0] = 1; bx.b[t][0][1] = 0;
-      bx.b[t][1][0] = 1; bx.b[t][1][1] = 0;
-      bx.b[t][2][0] = 1; bx.b[t][2][1] = 0;
-      const int sz = cnt_size(c, t);
-      bool used = false;
-      for (int q = 0; q < sz; q++) {
-        const int e = cnt_edge(c, flat + q);
-        used = used || edge_interior(g, i, j, k, e);
-        bool fb = false;
-        const float l = repr::edge_param_fast(e, u, g.iso, iso_ff, fb);
-        float ui[3];
-        repr::local_from_param(e, l, ui);
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-          pts[3 * (flat + q) + d] = ui[d];
-          bx.b[t][d][0] = bx.b[t][d][0] > ui[d] ? ui[d] : bx.b[t][d][0];
-          bx.b[t][d][1] = bx.b[t][d][1] < ui[d] ? ui[d] : bx.b[t][d][1];
-        }
-      }
-      if (used) {
-        if (used_seen == rank) {
-          tsel = t;
-          tstart = flat;
-        }
-        used_seen++;
-      }
-      flat += sz;
-    }
-    if (tsel < 0) continue;  // cannot happen: the record counted this vertex
+    VertexContour V;
+    if (!vertex_contour(g, i, j, k, rank, cc, G.iso_ff, V)) continue;  // cannot happen: counted
     float p[3];
-    repr::representative_fast(u, g.iso, c, tsel, pts + 3 * tstart, cnt_size(c, tsel), bx, p, st,
+    repr::representative_fast(V.u, g.iso, V.c, V.tsel, V.pts + 3 * V.tstart, cnt_size(V.c, V.tsel), V.bx, p, st,
                               sample_lb + threadIdx.x, kVertexThreads);
-    const int64_t o = 3 * vidx;
-    // position: UniformGrid::position (cpp_dmc/UniformGrid.h:300-305)
-    const double px = g.ox + (i + (double)p[0]) * g.dx;
-    const double py = g.oy + (j + (double)p[1]) * g.dy;
-    const double pz = g.oz + (k + (double)p[2]) * g.dz;
-    out.v[o] = (float)px;
-    out.v[o + 1] = (float)py;
-    out.v[o + 2] = (float)pz;
-    if (out.v64) {
-      out.v64[o] = px;
-      out.v64[o + 1] = py;
-      out.v64[o + 2] = pz;
-    }
-    // normal: trilinear interpolation of the 8 corner gradients, normalised (UniformGrid::normal,
-    // cpp_dmc/UniformGrid.h:286-298).  When it is kept for the simplification merges it is computed
-    // in float-float (relative error ~2^-40, far below the float32 output's 2^-24) on the FP32 pipes.
-    if (out.n64 && (g.flags & kGridNormal64)) {
-      ffx::ff G[8][3];
-#pragma unroll
-      for (int q = 0; q < 8; q++) point_diff_ff(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), G[q]);
-      ffx::ff nv3[3];
-      float scale = 0;  // largest |difference| * 1/(2 spacing): the size of the interpolation's inputs
-#pragma unroll
-      for (int d = 0; d < 3; d++) {
-        float md = 0;
-#pragma unroll
-        for (int q = 0; q < 8; q++) md = fmaxf(md, fabsf(G[q][d].hi));
-        scale = fmaxf(scale, md * inv2d[d]);
-        const ffx::ff a0 = ff_lerp(G[0][d], G[1][d], p[0]), a1 = ff_lerp(G[2][d], G[3][d], p[0]);
-        const ffx::ff a2 = ff_lerp(G[4][d], G[5][d], p[0]), a3 = ff_lerp(G[6][d], G[7][d], p[0]);
-        const ffx::ff b0 = ff_lerp(a0, a1, p[1]), b1 = ff_lerp(a2, a3, p[1]);
-        const ffx::ff t = ffx::ff_mul(ff_lerp(b0, b1, p[2]), inv2d_ff[d]);
-        nv3[d] = flip ? ffx::ff_neg(t) : t;
-      }
-      const ffx::ff dot =
-          ffx::ff_add(ffx::ff_add(ffx::ff_mul(nv3[0], nv3[0]), ffx::ff_mul(nv3[1], nv3[1])), ffx::ff_mul(nv3[2], nv3[2]));
-      // 1/sqrt(dot): float estimate and one Newton step in float-float
-      const float r0 = rsqrtf(dot.hi);
-      const ffx::ff h = ffx::ff_mul_f(ffx::ff_mul_f(dot, r0), r0);
-      const ffx::ff r = ffx::ff_mul_f(ffx::ff_sub(ffx::ff_from(1.5f), ffx::ff_mul_f(h, 0.5f)), r0);
-      if (scale <= 0x1p10f * sqrtf(dot.hi)) {
-        for (int d = 0; d < 3; d++) {
-          const ffx::ff x = ffx::ff_mul(nv3[d], r);
-          out.n64[o + d] = (double)x.hi + (double)x.lo;
-          out.n[o + d] = x.hi;
-        }
-      } else {
-        // the gradients cancel to below 2^-10 of their size: float64, as the reference
-        const Normal64 nf = normal_f64(g, i, j, k, p[0], p[1], p[2], flip);
-        for (int d = 0; d < 3; d++) {
-          out.n64[o + d] = nf.n[d];
-          out.n[o + d] = (float)nf.n[d];
-        }
-        st.normal_f64++;
-      }
-    } else {
-      float G[8][3];
-#pragma unroll
-      for (int q = 0; q < 8; q++) point_gradient_f(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), inv2d, G[q]);
-      float nv3[3];
-      const float uu = p[0], vv = p[1], ww = p[2];
-      const float sgn = flip ? -1.0f : 1.0f;
-#pragma unroll
-      for (int d = 0; d < 3; d++) {
-        const float a0 = fmaf(uu, G[1][d] - G[0][d], G[0][d]), a1 = fmaf(uu, G[3][d] - G[2][d], G[2][d]);
-        const float a2 = fmaf(uu, G[5][d] - G[4][d], G[4][d]), a3 = fmaf(uu, G[7][d] - G[6][d], G[6][d]);
-        const float b0 = fmaf(vv, a1 - a0, a0), b1 = fmaf(vv, a3 - a2, a2);
-        nv3[d] = sgn * fmaf(ww, b1 - b0, b0);
-      }
-      const float rn = rsqrtf(nv3[0] * nv3[0] + nv3[1] * nv3[1] + nv3[2] * nv3[2]);
-      for (int d = 0; d < 3; d++) out.n[o + d] = nv3[d] * rn;
-    }
-    if (out.vcell) {
-      out.vcell[vidx] = cell;
-      out.vuvw[o] = p[0];
-      out.vuvw[o + 1] = p[1];
-      out.vuvw[o + 2] = p[2];
-    }
+    vertex_outputs(G, i, j, k, cell, p, vidx, out, flip, st);
   }
-  // representative counters (the reference's failed-projection counts) and float64 fallbacks
-  if (st.fail1) atomicAdd(stats + 2, (unsigned long long)st.fail1);
-  if (st.fail2) atomicAdd(stats + 3, (unsigned long long)st.fail2);
-  if (st.fallback + st.normal_f64) atomicAdd(stats + 7, (unsigned long long)(st.fallback + st.normal_f64));
+  flush_stats(st, stats);
+}
+
+// Two-pass vertices, pass 1: contour, plane, sample coordinates, mean point -> one record per
+// vertex.  Contours with neighbour-contour exclusion go to the one-pass kernel's list.
+__global__ void __launch_bounds__(kVertexThreads) dmc_vertex_setup_kernel(CellSpace space, const int32_t* voff,
+                                                                           const uint32_t* vwork, int64_t nv,
+                                                                           repr::ProjRecord* recs, uint32_t* list,
+                                                                           unsigned* count,
+                                                                           unsigned long long* stats) {
+  __shared__ uint64_t cc[256];
+  for (int c = threadIdx.x; c < 256; c += blockDim.x) cc[c] = c_case_contour[c];
+  __syncthreads();
+  GridCache G;
+  int f64 = 0;
+  for (int64_t vidx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vidx < nv;
+       vidx += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t vcell = vwork[vidx];
+    const int rank = (int)(vidx - voff[vcell]);
+    G.load(space, vcell);
+    const Grid& g = G.g;
+    int i, j, k;
+    cell_ijk(g, vcell - g.vbase, i, j, k);
+    VertexContour V;
+    repr::ProjRecord R;
+    bool ok = vertex_contour(g, i, j, k, rank, cc, G.iso_ff, V);
+    if (ok) {
+      int f64c = 0;
+      ok = repr::projection_record(V.u, g.iso, V.c, V.tsel, V.pts + 3 * V.tstart, cnt_size(V.c, V.tsel), V.bx, R,
+                                   f64c);
+      if (ok) f64 += f64c;  // contours redone by the one-pass kernel are counted there
+    }
+    if (!ok) {
+      R.prj = -1;
+      list[atomicAdd(count, 1u)] = (uint32_t)vidx;
+    }
+    recs[vidx] = R;
+  }
+  if (f64) atomicAdd(stats + 7, (unsigned long long)f64);
+}
+
+// Two-pass vertices, pass 2: the projection from the record.  p (local coordinates) goes to vp;
+// vertices that need float64 go to the one-pass kernel's list (vp.w = 1 marks them).
+__global__ void __launch_bounds__(kVertexThreads) dmc_project_kernel(const repr::ProjRecord* recs, int64_t nv,
+                                                                     float4* vp, uint32_t* list, unsigned* count) {
+  __shared__ float sample_lb[49 * kVertexThreads];
+  for (int64_t vidx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vidx < nv;
+       vidx += (int64_t)gridDim.x * blockDim.x) {
+    const repr::ProjRecord& R = recs[vidx];
+    if (R.prj < 0) {  // already listed by the set-up pass
+      vp[vidx] = make_float4(0, 0, 0, 1);
+      continue;
+    }
+    float p[3] = {0, 0, 0};
+    const int r = repr::projection_from_record(R, p, sample_lb + threadIdx.x, kVertexThreads);
+    if (r != 0) list[atomicAdd(count, 1u)] = (uint32_t)vidx;
+    vp[vidx] = make_float4(p[0], p[1], p[2], r != 0 ? 1.0f : 0.0f);
+  }
+}
+
+// Two-pass vertices, pass 3: positions, normals and local coordinates of the projected vertices.
+__global__ void __launch_bounds__(kVertexThreads) dmc_vertex_finish_kernel(CellSpace space, const uint32_t* vwork,
+                                                                            int64_t nv, const float4* vp,
+                                                                            DmcVertexOut out, int flip_all,
+                                                                            unsigned long long* stats) {
+  repr::Stats st;
+  GridCache G;
+  for (int64_t vidx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vidx < nv;
+       vidx += (int64_t)gridDim.x * blockDim.x) {
+    const float4 q = vp[vidx];
+    if (q.w != 0.0f) continue;  // done by the one-pass kernel
+    const uint32_t vcell = vwork[vidx];
+    G.load(space, vcell);
+    const Grid& g = G.g;
+    const int64_t cell = vcell - g.vbase;
+    int i, j, k;
+    cell_ijk(g, cell, i, j, k);
+    const float p[3] = {q.x, q.y, q.z};
+    vertex_outputs(G, i, j, k, cell, p, vidx, out, flip_all | (g.flags & kGridFlip), st);
+  }
+  flush_stats(st, stats);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -414,14 +536,31 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
     dmc_offsets_kernel<<<(unsigned)ceil_div(n, kScanTile), kScanThreads, 0, st>>>(n, s.rec, s.tile_sums, s.voff,
                                                                                   s.qoff, s.vwork);
   }
+  const int64_t vb = std::max<int64_t>(1, std::min<int64_t>(ceil_div(nv, kVertexThreads), (int64_t)sms * 32));
   {
+    Stage t(prof, "dmc_vertex_setup", st);
+    cudaMemsetAsync(s.fb_count, 0, sizeof(unsigned), st);
+    dmc_vertex_setup_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(space, s.voff, s.vwork, nv, s.proj, s.fb_list,
+                                                                     s.fb_count, s.stats);
+  }
+  {
+    Stage t(prof, "dmc_project", st);
+    dmc_project_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(s.proj, nv, s.vp, s.fb_list, s.fb_count);
+  }
+  {
+    Stage t(prof, "dmc_vertex_finish", st);
+    dmc_vertex_finish_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(space, s.vwork, nv, s.vp, vo, flip, s.stats);
+  }
+  {
+    // the listed vertices, one pass with every float64 fallback
     Stage t(prof, "dmc_vertex", st);
-    const int64_t vb = std::max<int64_t>(1, std::min<int64_t>(ceil_div(nv, 128), (int64_t)sms * 32));
-    dmc_vertex_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(space, s.voff, s.vwork, nv, vo, flip, s.stats);
+    const unsigned fb = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nv, kVertexThreads), (int64_t)sms * 8));
+    dmc_vertex_kernel<<<fb, kVertexThreads, 0, st>>>(space, s.voff, s.vwork, nv, s.fb_list, s.fb_count, vo, flip,
+                                                      s.stats);
   }
   Stage t(prof, "dmc_quad", st);
   dmc_quad_kernel<<<(unsigned)blocks, 128, 0, st>>>(space, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
-  return 3;
+  return 6;
 }
 
 }  // namespace tmc

@@ -467,6 +467,9 @@ TMC_HD void w_window(float lo, float hi, float& wlo, float& whi) {
 // skipped when even its distance within the sample plane exceeds the best certain bound (its w
 // cannot make it smaller).  The surviving candidates are then evaluated exactly in the reference's
 // loop order, so that ties resolve as the reference's strict `minDistance > d`.
+// F64: evaluate uncertified samples in float64 (needs the contour points); otherwise return 2 at the
+// first such sample.
+template <bool F64 = true>
 TMC_HD int projection_fast(const ProjCtx& P, const float* us, const float* vs, float pt[3], float* buf, int stride,
                            int& f64_samples, const float* pts, int npts) {
   float m = INFINITY;
@@ -509,6 +512,7 @@ TMC_HD int projection_fast(const ProjCtx& P, const float* us, const float* vs, f
       if (!(buf[(7 * i + j) * stride] <= m)) continue;
       SampleOut s = sample_exact(P, us[i], vs[j]);
       if (s.status == 2) {
+        if (!F64) return 2;
         if (!have_pd) {
           const Point64 pm = mean_point_exact(pts, npts);
           pd[0] = pm.p[P.A];
@@ -593,10 +597,10 @@ struct TailOut {
 TMC_HD_COLD TailOut representative_tail(Corners u, double iso, uint64_t c, int t, const float* pts, int n,
                                         const Boxes& bx, int prj);
 
-// Representative of contour t.  pts: the contour's edge points (3 floats each, in contour order),
-// n of them.  On return p holds the local coordinates (floats) of the representative.
-TMC_HD void representative_fast(const float u[8], double iso, uint64_t c, int t, const float* pts, int n,
-                                const Boxes& bx, float p_out[3], Stats& st, float* buf, int stride) {
+// Projection set-up of contour t: plane, permuted corners, mean point, sample coordinates and the
+// w window.  Returns the plane; f64_coords counts sample coordinates computed in float64.
+TMC_HD int projection_setup(const float u[8], double iso, uint64_t c, int t, const float* pts, int n,
+                            const Boxes& bx, ProjCtx& P, float us[7], float vs[7], int& f64_coords) {
   const int cnt_sz = csize(c, t);
   // mean point, float-float
   ff s[3] = {ffx::ff_from(0.0f), ffx::ff_from(0.0f), ffx::ff_from(0.0f)};
@@ -620,7 +624,6 @@ TMC_HD void representative_fast(const float u[8], double iso, uint64_t c, int t,
     prj = plane_from_extent_ff(bx, t);
     if (prj < 0) prj = plane_from_extent_f64(bx, t);
   }
-  ProjCtx P;
   uint32_t perm;
   plane(prj, P.A, P.B, P.W, perm);
 #pragma unroll
@@ -642,13 +645,22 @@ TMC_HD void representative_fast(const float u[8], double iso, uint64_t c, int t,
   P.bx = &bx;
   const float umin = bx.b[t][P.A][0], umax = bx.b[t][P.A][1];
   const float vmin = bx.b[t][P.B][0], vmax = bx.b[t][P.B][1];
+  sample_coords(umin, umax, us, f64_coords);
+  sample_coords(vmin, vmax, vs, f64_coords);
+  w_window(bx.b[t][P.W][0], bx.b[t][P.W][1], P.wlo, P.whi);
+  return prj;
+}
+
+// Representative of contour t.  pts: the contour's edge points (3 floats each, in contour order),
+// n of them.  On return p holds the local coordinates (floats) of the representative.
+TMC_HD void representative_fast(const float u[8], double iso, uint64_t c, int t, const float* pts, int n,
+                                const Boxes& bx, float p_out[3], Stats& st, float* buf, int stride) {
+  ProjCtx P;
   float us[7], vs[7];
   int f64_samples = 0;
-  sample_coords(umin, umax, us, f64_samples);
-  sample_coords(vmin, vmax, vs, f64_samples);
-  w_window(bx.b[t][P.W][0], bx.b[t][P.W][1], P.wlo, P.whi);
+  const int prj = projection_setup(u, iso, c, t, pts, n, bx, P, us, vs, f64_samples);
   float pt[3];
-  const int r = projection_fast(P, us, vs, pt, buf, stride, f64_samples, pts, n);
+  const int r = projection_fast<true>(P, us, vs, pt, buf, stride, f64_samples, pts, n);
   st.fallback += f64_samples;
   if (r == 0) {
     p_out[P.A] = pt[0];
@@ -665,6 +677,78 @@ TMC_HD void representative_fast(const float u[8], double iso, uint64_t c, int t,
   p_out[0] = tail.p[0];
   p_out[1] = tail.p[1];
   p_out[2] = tail.p[2];
+}
+
+// ---------------------------------------------------------------------------------------------
+// two-pass form: a set-up pass writes one ProjRecord per vertex, a projection pass reads it.  Each
+// pass is a small kernel (registers, instruction cache); contours that need anything beyond the
+// float32 / float-float path (the neighbour-contour exclusion, a float64 sample, the 26x26 tail) are
+// left to the one-pass kernel.
+// ---------------------------------------------------------------------------------------------
+struct alignas(16) ProjRecord {
+  float fp[8];        // corner values permuted to the projection frame
+  float us[7], vs[7];  // sample coordinates
+  float wlo, whi;      // w window
+  float pff[6];        // mean point in the projection frame, float pairs (hi, lo)
+  float iso_hi, iso_lo;
+  int32_t prj;         // projection plane (0..2)
+  int32_t pad;
+};
+
+// Set-up pass of one contour.  Returns false when the contour needs the one-pass kernel.
+TMC_HD bool projection_record(const float u[8], double iso, uint64_t c, int t, const float* pts, int n,
+                              const Boxes& bx, ProjRecord& R, int& f64_coords) {
+  ProjCtx P;
+  const int prj = projection_setup(u, iso, c, t, pts, n, bx, P, R.us, R.vs, f64_coords);
+  if (P.excl) return false;
+  for (int q = 0; q < 8; q++) R.fp[q] = P.fp[q];
+  R.wlo = P.wlo;
+  R.whi = P.whi;
+  for (int d = 0; d < 3; d++) {
+    R.pff[2 * d] = P.pff[d].hi;
+    R.pff[2 * d + 1] = P.pff[d].lo;
+  }
+  R.iso_hi = P.iso_ff.hi;
+  R.iso_lo = P.iso_ff.lo;
+  R.prj = prj;
+  R.pad = 0;
+  return true;
+}
+
+// Projection pass: 0 = found (p set, local coordinates), 1 = no valid sample, 2 = a sample needs
+// float64.  The last two go to the one-pass kernel.
+TMC_HD int projection_from_record(const ProjRecord& R, float p_out[3], float* buf, int stride) {
+  ProjCtx P;
+  uint32_t perm;
+  plane(R.prj, P.A, P.B, P.W, perm);
+#pragma unroll
+  for (int q = 0; q < 8; q++) P.fp[q] = R.fp[q];
+  P.sabs_lo = fmaxf(fmaxf(fabsf(P.fp[0]), fabsf(P.fp[1])), fmaxf(fabsf(P.fp[2]), fabsf(P.fp[3])));
+  P.sabs_hi = fmaxf(fmaxf(fabsf(P.fp[4]), fabsf(P.fp[5])), fmaxf(fabsf(P.fp[6]), fabsf(P.fp[7])));
+  for (int d = 0; d < 3; d++) {
+    P.pff[d] = ff{R.pff[2 * d], R.pff[2 * d + 1]};
+    P.pf[d] = R.pff[2 * d];
+  }
+  P.iso_ff = ff{R.iso_hi, R.iso_lo};
+  P.iso_d = (double)R.iso_hi + (double)R.iso_lo;
+  P.iso_f = R.iso_hi;
+  P.iso_err = fabsf(R.iso_lo) + fabsf(R.iso_hi) * 0x1p-30f;
+  P.cnt = 1;
+  P.excl = false;
+  P.t = 0;
+  P.c = 0;
+  P.bx = nullptr;
+  P.wlo = R.wlo;
+  P.whi = R.whi;
+  float pt[3];
+  int f64 = 0;
+  const int r = projection_fast<false>(P, R.us, R.vs, pt, buf, stride, f64, nullptr, 0);
+  if (r == 0) {
+    p_out[P.A] = pt[0];
+    p_out[P.B] = pt[1];
+    p_out[P.W] = pt[2];
+  }
+  return r;
 }
 
 // The 7x7 projection is empty: the reference then tries 26x26 samples from the mean point, in

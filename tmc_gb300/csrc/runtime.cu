@@ -177,6 +177,17 @@ tmc::Grid make_grid(const tmc_volume* vol, const float* dev, double iso) {
 
 void mesh_reset(tmc_mesh* m) { std::memset(m, 0, sizeof(*m)); }
 
+// per-vertex scratch of the two-pass vertex kernels
+cudaError_t dmc_vertex_scratch(Allocs& al, tmc::DmcScratch& sc, int64_t nv) {
+  uint8_t* rec = nullptr;
+  cudaError_t e = al.get(&rec, nv * (int64_t)tmc::kProjRecordBytes);
+  sc.proj = reinterpret_cast<tmc::repr::ProjRecord*>(rec);
+  if (e == cudaSuccess) e = al.get(&sc.vp, nv);
+  if (e == cudaSuccess) e = al.get(&sc.fb_list, nv);
+  if (e == cudaSuccess) e = al.get(&sc.fb_count, 1);
+  return e;
+}
+
 // Move device arrays of a finished mesh to host memory when TMC_OUT_HOST is set.
 template <typename T>
 tmc_status to_host(tmc_ctx* ctx, T** p, size_t count, MeshPriv* mp) {
@@ -389,6 +400,7 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
     TMC_CUDA(ctx, ce);
   }
   ce = al.get(&sc.vwork, nv);
+  if (ce == cudaSuccess) ce = dmc_vertex_scratch(al, sc, nv);
   if (ce != cudaSuccess) {
     delete mp;
     TMC_CUDA(ctx, ce);
@@ -706,6 +718,7 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
     TMC_CUDA(ctx, get_shared(&faces, 4 * NF));
     TMC_CUDA(ctx, get_shared(&colors, NF));
     TMC_CUDA(ctx, al.get(&dsc.vwork, NV));
+    TMC_CUDA(ctx, dmc_vertex_scratch(al, dsc, NV));
     tmc::DmcVertexOut vo{v, nn, v64, n64, vcell, vuvw};
     ctx->launches += tmc::dmc_front_emit(space, dsc, vo, NV, faces, colors, 0, ctx->sms, st, &ctx->prof);
   } else {
