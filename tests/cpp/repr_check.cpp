@@ -87,7 +87,8 @@ int main(int argc, char** argv) {
             int f64c = 0;
             if (repr::projection_record(u, iso, c, t, pts[t], sz, bx, R, f64c)) {
               float pr[3];
-              const int rr = repr::projection_from_record(R, pr, lb, 1);
+              int f64r = 0;
+              const int rr = repr::projection_from_record(R, pr, lb, 1, f64r);
               if (rr == 0) {
                 two_pass++;
                 if (pr[0] != pf[0] || pr[1] != pf[1] || pr[2] != pf[2]) {

@@ -55,3 +55,6 @@ def test_fast_representative_matches_exact(checker, tmp_path, name):
     # float64 stays the exception on generic fields; the seeded saddles put many samples exactly on
     # rounding ties and zeros, which are resolved in float64
     assert f64 < (6 if name.startswith("saddle") else 1) * contours
+    # the two-pass kernels (float32 / float-float only) handle almost every contour of a generic field
+    if not name.startswith("saddle"):
+        assert two_pass >= 0.98 * contours

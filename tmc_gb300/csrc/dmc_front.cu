@@ -408,8 +408,10 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_setup_kernel(CellSp
 // Two-pass vertices, pass 2: the projection from the record.  p (local coordinates) goes to vp;
 // vertices that need float64 go to the one-pass kernel's list (vp.w = 1 marks them).
 __global__ void __launch_bounds__(kVertexThreads) dmc_project_kernel(const repr::ProjRecord* recs, int64_t nv,
-                                                                     float4* vp, uint32_t* list, unsigned* count) {
+                                                                     float4* vp, uint32_t* list, unsigned* count,
+                                                                     unsigned long long* stats) {
   __shared__ float sample_lb[49 * kVertexThreads];
+  int f64 = 0;
   for (int64_t vidx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vidx < nv;
        vidx += (int64_t)gridDim.x * blockDim.x) {
     const repr::ProjRecord& R = recs[vidx];
@@ -418,10 +420,13 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_project_kernel(const repr:
       continue;
     }
     float p[3] = {0, 0, 0};
-    const int r = repr::projection_from_record(R, p, sample_lb + threadIdx.x, kVertexThreads);
-    if (r != 0) list[atomicAdd(count, 1u)] = (uint32_t)vidx;
+    int f = 0;
+    const int r = repr::projection_from_record(R, p, sample_lb + threadIdx.x, kVertexThreads, f);
+    if (r != 0) list[atomicAdd(count, 1u)] = (uint32_t)vidx;  // redone (and counted) by the one-pass kernel
+    else f64 += f;
     vp[vidx] = make_float4(p[0], p[1], p[2], r != 0 ? 1.0f : 0.0f);
   }
+  if (f64) atomicAdd(stats + 7, (unsigned long long)f64);
 }
 
 // Two-pass vertices, pass 3: positions, normals and local coordinates of the projected vertices.
@@ -545,7 +550,7 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
   }
   {
     Stage t(prof, "dmc_project", st);
-    dmc_project_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(s.proj, nv, s.vp, s.fb_list, s.fb_count);
+    dmc_project_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(s.proj, nv, s.vp, s.fb_list, s.fb_count, s.stats);
   }
   {
     Stage t(prof, "dmc_vertex_finish", st);

@@ -57,11 +57,26 @@ __device__ __forceinline__ bool non_manifold(const int32_t* he, int64_t f) {
 // class of an inherited colour: 0..18 for colours 5..23, 19 for colour 4, -1 otherwise
 __device__ __forceinline__ int color_class(int c) { return c > 4 ? c - 5 : (c == 4 ? 19 : -1); }
 
-__global__ void color_count_kernel(const uint8_t* col, int64_t nq, int32_t* cnt) {
-  FOR_EACH(f, nq) {
-    const int k = color_class(col[f]);
-    if (k >= 0) atomicAdd(cnt + k, 1);
+// Class histograms and lists are aggregated per block (shared-memory ranks, one global atomic per
+// class and block): 20 global counters hit by every face serialise the whole pass otherwise.  The
+// order of faces within a class list does not matter (faces of one class never touch).
+constexpr int kColorThreads = 256, kColorItems = 8, kColorTile = kColorThreads * kColorItems;
+
+__global__ void __launch_bounds__(kColorThreads) color_count_kernel(const uint8_t* col, int64_t nq, int32_t* cnt) {
+  __shared__ int h[20];
+  if (threadIdx.x < 20) h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kColorTile;
+#pragma unroll
+  for (int s = 0; s < kColorItems; s++) {
+    const int64_t f = base + s * kColorThreads + threadIdx.x;
+    if (f < nq) {
+      const int k = color_class(col[f]);
+      if (k >= 0) atomicAdd(&h[k], 1);
+    }
   }
+  __syncthreads();
+  if (threadIdx.x < 20 && h[threadIdx.x]) atomicAdd(cnt + threadIdx.x, h[threadIdx.x]);
 }
 
 __global__ void color_offsets_kernel(const int32_t* cnt, int32_t* off, int32_t* cursor) {
@@ -76,11 +91,25 @@ __global__ void color_offsets_kernel(const int32_t* cnt, int32_t* off, int32_t* 
   }
 }
 
-__global__ void color_scatter_kernel(const uint8_t* col, int64_t nq, int32_t* cursor, int32_t* list) {
-  FOR_EACH(f, nq) {
-    const int k = color_class(col[f]);
-    if (k >= 0) list[atomicAdd(cursor + k, 1)] = (int32_t)f;
+__global__ void __launch_bounds__(kColorThreads) color_scatter_kernel(const uint8_t* col, int64_t nq, int32_t* cursor,
+                                                                     int32_t* list) {
+  __shared__ int h[20], at[20];
+  if (threadIdx.x < 20) h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kColorTile;
+  int ks[kColorItems], rs[kColorItems];
+#pragma unroll
+  for (int s = 0; s < kColorItems; s++) {
+    const int64_t f = base + s * kColorThreads + threadIdx.x;
+    ks[s] = (f < nq) ? color_class(col[f]) : -1;
+    rs[s] = (ks[s] >= 0) ? atomicAdd(&h[ks[s]], 1) : 0;
   }
+  __syncthreads();
+  if (threadIdx.x < 20 && h[threadIdx.x]) at[threadIdx.x] = atomicAdd(cursor + threadIdx.x, h[threadIdx.x]);
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < kColorItems; s++)
+    if (ks[s] >= 0) list[at[ks[s]] + rs[s]] = (int32_t)(base + s * kColorThreads + threadIdx.x);
 }
 
 __global__ void color_reduce_kernel(const int32_t* he, uint8_t* col, const int32_t* list, const int32_t* off, int k,
@@ -425,7 +454,7 @@ struct HeBufs {
 }  // namespace
 
 DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaStream_t st, DmcPostOut* out,
-                              Prof* prof, bool borrowed) {
+                              unsigned long long* h_cnt, Prof* prof, bool borrowed) {
   DmcPostStatus s;
   out->mesh = in;
   const bool c3x3y = flags & TMC_DMC_P3X3Y_COLOR, i3x3y = flags & TMC_DMC_P3X3Y_ISOLATED,
@@ -433,8 +462,6 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   if (!(c3x3y || i3x3y || p3333 || want_t || want_he)) return s;
   Pool pool{st};
   const int64_t NV = std::max<int64_t>(in.nv, 1), NQ = std::max<int64_t>(in.nq, 1);
-  unsigned long long* h_cnt = nullptr;
-  if ((s.err = cudaMallocHost(&h_cnt, 4 * sizeof(unsigned long long))) != cudaSuccess) return s;
 
   // working mesh (double buffered)
   DmcMesh cur = in;
@@ -457,7 +484,6 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   unsigned long long* total = pool.get<unsigned long long>(2);
   if (pool.err) {
     s.err = pool.err;
-    cudaFreeHost(h_cnt);
     return s;
   }
   auto halfedges = [&](const DmcMesh& m) {
@@ -489,8 +515,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     idx = pool.get<int32_t>(std::max(NV, NQ));
     if (pool.err) {
       s.err = pool.err;
-      cudaFreeHost(h_cnt);
-      return s;
+        return s;
     }
   }
   // new output buffers replace the input ones after each compaction
@@ -535,9 +560,10 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
       int32_t* list = pool.get<int32_t>(NQ);
       if (pool.err) break;
       cudaMemsetAsync(cnt, 0, 24 * sizeof(int32_t), st);
-      color_count_kernel<<<gq, 256, 0, st>>>(cur.colors, cur.nq, cnt);
+      const unsigned gc = (unsigned)std::max<int64_t>(1, ceil_div(cur.nq, kColorTile));
+      color_count_kernel<<<gc, kColorThreads, 0, st>>>(cur.colors, cur.nq, cnt);
       color_offsets_kernel<<<1, 32, 0, st>>>(cnt, off, cursor);
-      color_scatter_kernel<<<gq, 256, 0, st>>>(cur.colors, cur.nq, cursor, list);
+      color_scatter_kernel<<<gc, kColorThreads, 0, st>>>(cur.colors, cur.nq, cursor, list);
       s.launches += 3;
       for (int k = 0; k < 19; k++) color_reduce_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.colors, list, off, k, 4);
       color_reduce_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.colors, list, off, 19, 3);
@@ -677,8 +703,6 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     out->owned.swap(keepv);
   }
   if (s.err == cudaSuccess) s.err = cudaGetLastError();
-  cudaStreamSynchronize(st);
-  cudaFreeHost(h_cnt);
   out->mesh = cur;
   return s;
 }

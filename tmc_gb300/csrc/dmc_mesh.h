@@ -38,7 +38,8 @@ struct DmcPostStatus {
 
 // borrowed: the input arrays belong to the caller (e.g. slices of a batch's shared arrays) and are
 // never freed here; they are still listed in out->freed once the result no longer uses them.
+// h_staging: pinned host memory for 4 words (counts read back between the passes).
 DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaStream_t st, DmcPostOut* out,
-                              Prof* prof = nullptr, bool borrowed = false);
+                              unsigned long long* h_staging, Prof* prof = nullptr, bool borrowed = false);
 
 }  // namespace tmc

@@ -308,8 +308,22 @@ TMC_HD SampleApprox sample_approx(const ProjCtx& P, float u, float v) {
 // One exactly evaluated sample, returned by value.
 struct SampleOut {
   float w, d;
-  int status;  // 0 invalid, 1 valid, 2 rounding not certified (evaluate in float64)
+  int status;  // 0 invalid, 1 valid, 2 distance rounding not certified (evaluate in float64)
+  int f64;     // values recomputed in float64
 };
+
+// The reference's bilinear value of one face at (u, v), float64 rounded to float (its (1 - u) is a
+// float subtraction, cpp_dmc/DualMarchingCubes.cpp:302-303).  Used where the float-float value lies
+// on (or within its error of) a float rounding midpoint, e.g. exact ties at dyadic samples.
+TMC_HD_COLD float bilinear_f64(float f0, float f1, float f2, float f3, float u, float v) {
+  const float omu = 1 - u, omv = 1 - v;
+  return (float)((double)omv * ((double)omu * f0 + (double)u * f1) + (double)v * ((double)omu * f2 + (double)u * f3));
+}
+// the reference's w = (iso - g1) / (g2 - g1): float64 over the float difference (:305)
+TMC_HD_COLD float w_f64(double iso, float g1, float g2) {
+  const float den = g2 - g1;
+  return (float)((iso - (double)g1) / (double)den);
+}
 
 // float64 evaluation of one sample, as the reference's loop body (projection, :298-316).  Rare:
 // out of line, with the context copied (the caller's stays in registers).
@@ -331,7 +345,7 @@ TMC_HD_COLD SampleOut sample_f64(const ProjCtx P, double pd0, double pd1, double
 
 // exact evaluation of one sample (status 2 when a rounding cannot be certified)
 TMC_HD SampleOut sample_exact(const ProjCtx& P, float u, float v) {
-  SampleOut r{0.0f, 0.0f, 2};
+  SampleOut r{0.0f, 0.0f, 2, 0};
   const float omu = 1 - u, omv = 1 - v;
   const float* f = P.fp;
   const ff A1 = ffx::ff_add(ffx::two_prod(omu, f[0]), ffx::two_prod(u, f[1]));
@@ -340,9 +354,19 @@ TMC_HD SampleOut sample_exact(const ProjCtx& P, float u, float v) {
   const ff B2 = ffx::ff_add(ffx::two_prod(omu, f[6]), ffx::two_prod(u, f[7]));
   const ff G1 = ffx::ff_add(ffx::ff_mul_f(A1, omv), ffx::ff_mul_f(B1, v));
   const ff G2 = ffx::ff_add(ffx::ff_mul_f(A2, omv), ffx::ff_mul_f(B2, v));
+  // |G - the reference's float64 value| <= ~2^-45 * (|1-v| |A| + |v| |B|): the float-float
+  // operations' relative errors on these magnitudes plus the reference's own float64 roundings
+  const float S1 = fabsf(omv) * fabsf(A1.hi) + fabsf(v) * fabsf(B1.hi);
+  const float S2 = fabsf(omv) * fabsf(A2.hi) + fabsf(v) * fabsf(B2.hi);
   float g1, g2;
-  if (!ffx::ff_round(G1, P.sabs_lo * 0x1p-44f, g1)) return r;
-  if (!ffx::ff_round(G2, P.sabs_hi * 0x1p-44f, g2)) return r;
+  if (!ffx::ff_round(G1, S1 * 0x1p-44f, g1)) {
+    g1 = bilinear_f64(f[0], f[1], f[2], f[3], u, v);
+    r.f64++;
+  }
+  if (!ffx::ff_round(G2, S2 * 0x1p-44f, g2)) {
+    g2 = bilinear_f64(f[4], f[5], f[6], f[7], u, v);
+    r.f64++;
+  }
   if (g1 == g2) {
     r.status = 0;
     return r;
@@ -352,7 +376,10 @@ TMC_HD SampleOut sample_exact(const ProjCtx& P, float u, float v) {
   const ff W = ffx::ff_div(num, ffx::ff_from(den));
   const float errW = fabsf(W.hi) * 0x1p-42f + (fabsf(P.iso_ff.hi) * 0x1p-46f + fabsf(num.hi) * 0x1p-50f) / fabsf(den);
   float w;
-  if (!ffx::ff_round(W, errW, w)) return r;
+  if (!ffx::ff_round(W, errW, w)) {
+    w = w_f64(P.iso_d, g1, g2);
+    r.f64++;
+  }
   bool valid = (w >= P.wlo && w <= P.whi);
   if (valid && P.excl) {
     const Boxes& bx = *P.bx;
@@ -511,6 +538,7 @@ TMC_HD int projection_fast(const ProjCtx& P, const float* us, const float* vs, f
     for (int j = 0; j < 7; j++) {
       if (!(buf[(7 * i + j) * stride] <= m)) continue;
       SampleOut s = sample_exact(P, us[i], vs[j]);
+      f64_samples += s.f64;
       if (s.status == 2) {
         if (!F64) return 2;
         if (!have_pd) {
@@ -690,7 +718,7 @@ struct alignas(16) ProjRecord {
   float us[7], vs[7];  // sample coordinates
   float wlo, whi;      // w window
   float pff[6];        // mean point in the projection frame, float pairs (hi, lo)
-  float iso_hi, iso_lo;
+  double iso;
   int32_t prj;         // projection plane (0..2)
   int32_t pad;
 };
@@ -708,16 +736,15 @@ TMC_HD bool projection_record(const float u[8], double iso, uint64_t c, int t, c
     R.pff[2 * d] = P.pff[d].hi;
     R.pff[2 * d + 1] = P.pff[d].lo;
   }
-  R.iso_hi = P.iso_ff.hi;
-  R.iso_lo = P.iso_ff.lo;
+  R.iso = iso;
   R.prj = prj;
   R.pad = 0;
   return true;
 }
 
-// Projection pass: 0 = found (p set, local coordinates), 1 = no valid sample, 2 = a sample needs
-// float64.  The last two go to the one-pass kernel.
-TMC_HD int projection_from_record(const ProjRecord& R, float p_out[3], float* buf, int stride) {
+// Projection pass: 0 = found (p set, local coordinates), 1 = no valid sample, 2 = a sample distance
+// needs float64.  The last two go to the one-pass kernel.  f64 counts values recomputed in float64.
+TMC_HD int projection_from_record(const ProjRecord& R, float p_out[3], float* buf, int stride, int& f64) {
   ProjCtx P;
   uint32_t perm;
   plane(R.prj, P.A, P.B, P.W, perm);
@@ -729,10 +756,10 @@ TMC_HD int projection_from_record(const ProjRecord& R, float p_out[3], float* bu
     P.pff[d] = ff{R.pff[2 * d], R.pff[2 * d + 1]};
     P.pf[d] = R.pff[2 * d];
   }
-  P.iso_ff = ff{R.iso_hi, R.iso_lo};
-  P.iso_d = (double)R.iso_hi + (double)R.iso_lo;
-  P.iso_f = R.iso_hi;
-  P.iso_err = fabsf(R.iso_lo) + fabsf(R.iso_hi) * 0x1p-30f;
+  P.iso_ff = ffx::ff_from_double(R.iso);
+  P.iso_d = R.iso;
+  P.iso_f = P.iso_ff.hi;
+  P.iso_err = fabsf(P.iso_ff.lo) + fabsf(P.iso_ff.hi) * 0x1p-30f;
   P.cnt = 1;
   P.excl = false;
   P.t = 0;
@@ -741,7 +768,6 @@ TMC_HD int projection_from_record(const ProjRecord& R, float p_out[3], float* bu
   P.wlo = R.wlo;
   P.whi = R.whi;
   float pt[3];
-  int f64 = 0;
   const int r = projection_fast<false>(P, R.us, R.vs, pt, buf, stride, f64, nullptr, 0);
   if (r == 0) {
     p_out[P.A] = pt[0];

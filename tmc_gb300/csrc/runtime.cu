@@ -419,7 +419,8 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   mesh.quads = quads;
   mesh.colors = colors;
   tmc::DmcPostOut post{};
-  tmc::DmcPostStatus ps = tmc::dmc_postprocess(mesh, flags, ctx->sms, st, &post, &ctx->prof);
+  tmc::DmcPostStatus ps =
+      tmc::dmc_postprocess(mesh, flags, ctx->sms, st, &post, (unsigned long long*)ctx->h_pinned + 64, &ctx->prof);
   if (ps.err != cudaSuccess) {
     delete mp;
     TMC_CUDA(ctx, ps.err);
@@ -758,7 +759,8 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
       mesh.colors = colors + fb[q];
       tmc::DmcPostOut post{};
       if (simp || (f & (TMC_OUT_TRIANGLES | TMC_OUT_HALFEDGES))) {
-        tmc::DmcPostStatus ps = tmc::dmc_postprocess(mesh, f, ctx->sms, st, &post, &ctx->prof, true);
+        tmc::DmcPostStatus ps = tmc::dmc_postprocess(mesh, f, ctx->sms, st, &post,
+                                                     (unsigned long long*)ctx->h_pinned + 64, &ctx->prof, true);
         for (void* p : post.owned) mp->dev.push_back(p);
         if (ps.err != cudaSuccess) TMC_CUDA(ctx, ps.err);
         ctx->launches += ps.launches;
