@@ -110,18 +110,38 @@ class ClockSampler:
 # ------------------------------------------------------------------------------------------------
 # our arm
 # ------------------------------------------------------------------------------------------------
-def algorithmic_bytes(stage: str, sizes: dict, cells: int, voxels: int) -> float:
-    """Algorithmic bytes of one launch of a stage: field read once (4 B/voxel) for the classifying
-    kernels, emitted mesh bytes for the emitting kernels (24 B/vertex, 16 B/quad, 12 B/triangle);
-    scratch, hash tables and re-reads excluded."""
-    if stage in ("tmc_classify", "dmc_classify"):
+# Kernel groups of the roofline: the profiler stages of one piece of work, and the DRAM traffic per
+# algorithmic byte that ncu measured for them on the 320^3 case of this workload (profiles/
+# dmc_vertex_noise320.md: 2,908 MB for 5.49 M vertices; tmc_emit_noise320.md: 847.4 MB for 267.7 MB of
+# mesh; dmc_classify_noise320.md: 224.0 MB for a 131.1 MB field), scaled to the full launch by the units
+# it processes (traffic grows with the vertex / cell count).
+ROOFLINE_GROUPS = {
+    "dmc_vertex": (("dmc_vertex_setup", "dmc_project", "dmc_vertex_finish", "dmc_vertex"), 2908.0 / 131.6),
+    "dmc_halfedges": (("dmc_halfedges",), None),
+    "tmc_emit": (("tmc_emit",), 847.4 / 267.7),
+    "dmc_classify": (("dmc_classify",), 224.0 / 131.1),
+    "tmc_classify": (("tmc_classify",), None),
+    "dmc_quad": (("dmc_quad",), None),
+    "dmc_triangles": (("dmc_triangles",), None),
+}
+
+
+def algorithmic_bytes(group: str, sizes: dict, cells: int, voxels: int) -> float:
+    """Algorithmic bytes of one launch of a kernel group: the field read once (4 B/voxel) for the
+    classifying kernels, the mesh bytes a group emits for the others (24 B/vertex, 16 B/quad,
+    12 B/triangle, 16 B/halfedge + 4 B/vertex + 4 B/face); scratch and re-reads excluded."""
+    if group in ("tmc_classify", "dmc_classify"):
         return 4.0 * voxels
-    if stage == "tmc_emit":
+    if group == "tmc_emit":
         return 24.0 * sizes["tmc_v"] + 12.0 * sizes["tmc_t"]
-    if stage == "dmc_vertex":
+    if group == "dmc_vertex":
         return 24.0 * sizes["dmc_front_v"]
-    if stage == "dmc_quad":
+    if group == "dmc_quad":
         return 16.0 * sizes["dmc_front_q"]
+    if group == "dmc_halfedges":
+        return 16.0 * sizes["dmc_he"] + 4.0 * sizes["dmc_v"] + 4.0 * sizes["dmc_q"]
+    if group == "dmc_triangles":
+        return 12.0 * sizes["dmc_t"]
     return 0.0
 
 
@@ -223,8 +243,18 @@ def run_ours(args, rank, world, local):
     prof = ctx.profile()
     ctx.set_profiling(False)
     total_ms = sum(v[0] for v in prof.values())
-    dom = max(prof.items(), key=lambda kv: kv[1][0])
-    dom_name, (dom_ms, dom_cnt) = dom
+    # kernel groups (the vertex passes count as one), the dominant one by time
+    groups = {}
+    grouped = set()
+    for gname, (members, _) in ROOFLINE_GROUPS.items():
+        present = [m for m in members if m in prof]
+        if present:
+            groups[gname] = (sum(prof[m][0] for m in present), max(prof[m][1] for m in present))
+            grouped.update(present)
+    for k, v in prof.items():
+        if k not in grouped:
+            groups[k] = v
+    dom_name, (dom_ms, dom_cnt) = max(groups.items(), key=lambda kv: kv[1][0])
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -234,6 +264,8 @@ def run_ours(args, rank, world, local):
     avg_ms = dom_ms / max(dom_cnt, 1)
     algo = algorithmic_bytes(dom_name, sizes, cells, voxels)
     achieved = algo / (avg_ms * 1e-3) / 1e9 if algo else 0.0
+    ratio = ROOFLINE_GROUPS.get(dom_name, ((), None))[1]
+    traffic = round(ratio * algo) if (ratio and algo) else None
     stages = {k: {"ms_per_step": round(v[0] / 2, 4), "share": round(v[0] / total_ms, 4)} for k, v in prof.items()}
     # memory-bound classifier, reported beside the dominant kernel
     cls = {}
@@ -255,8 +287,11 @@ def run_ours(args, rank, world, local):
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum on the 320^3 case, "
+                                       "scaled by vertices" if traffic else None,
                      "algorithmic_bytes_per_launch": algo, "avg_launch_ms": round(avg_ms, 4),
+                     "kernels": list(ROOFLINE_GROUPS.get(dom_name, ((dom_name,), None))[0]),
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s"},
         "classify_roofline": cls,
         "stages": stages,
