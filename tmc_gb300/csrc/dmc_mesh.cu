@@ -215,23 +215,57 @@ __device__ __forceinline__ void midpoint(double* v64, float* v, double* n64, flo
   }
 }
 
+// Marks the removed vertices and lists the midpoint merges (destination, two sources); the
+// float64 midpoints run densely in midpoint_kernel (a few merging faces per warp would otherwise
+// pay the float64 pipe for the whole warp).  Each destination has one owner, and the sources are
+// never destinations (valence >= 5 vs valence 3), so the merges are independent.
 __global__ void merge_apply_kernel(const int32_t* he, int64_t nq, const uint8_t* branch, const int32_t* own_pos,
-                                   const int32_t* own_rm, double* v64, float* v, double* n64, float* n, uint8_t* vm_first,
-                                   int32_t* vm_second, uint8_t* em) {
+                                   const int32_t* own_rm, uint8_t* vm_first, int32_t* vm_second, uint8_t* em,
+                                   int4* jobs, unsigned* njobs) {
+  const int lane = threadIdx.x & 31;
   FOR_EACH(f, nq) {
-    em[f] = branch[f] != 0;
-    if (!branch[f]) continue;
-    const int v0 = he_origin(he, 4 * f), v1 = he_origin(he, 4 * f + 1), v2 = he_origin(he, 4 * f + 2),
-              v3 = he_origin(he, 4 * f + 3);
-    if (branch[f] == 1) {
-      if (own_pos[v0] == f) midpoint(v64, v, n64, n, v0, v1, v3);
-      vm_first[v2] = 1;
-      if (own_rm[v2] == f) vm_second[v2] = v0;
-    } else {
-      if (own_pos[v1] == f) midpoint(v64, v, n64, n, v1, v0, v2);
-      vm_first[v3] = 1;
-      if (own_rm[v3] == f) vm_second[v3] = v1;
+    const uint8_t br = branch[f];
+    em[f] = br != 0;
+    bool job = false;
+    int4 jv = make_int4(0, 0, 0, 0);
+    if (br) {
+      const int v0 = he_origin(he, 4 * f), v1 = he_origin(he, 4 * f + 1), v2 = he_origin(he, 4 * f + 2),
+                v3 = he_origin(he, 4 * f + 3);
+      if (br == 1) {
+        if (own_pos[v0] == f) {
+          job = true;
+          jv = make_int4(v0, v1, v3, 0);
+        }
+        vm_first[v2] = 1;
+        if (own_rm[v2] == f) vm_second[v2] = v0;
+      } else {
+        if (own_pos[v1] == f) {
+          job = true;
+          jv = make_int4(v1, v0, v2, 0);
+        }
+        vm_first[v3] = 1;
+        if (own_rm[v3] == f) vm_second[v3] = v1;
+      }
     }
+    // warp-aggregated append
+    const unsigned act = __activemask();
+    const unsigned bal = __ballot_sync(act, job);
+    if (bal) {
+      const int leader = __ffs(bal) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(njobs, (unsigned)__popc(bal));
+      base = __shfl_sync(act, base, leader);
+      if (job) jobs[base + __popc(bal & ((1u << lane) - 1u))] = jv;
+    }
+  }
+}
+
+__global__ void midpoint_kernel(const int4* jobs, const unsigned* njobs, double* v64, float* v, double* n64,
+                                float* n) {
+  const int64_t nj = *njobs;
+  FOR_EACH(a, nj) {
+    const int4 j = jobs[a];
+    midpoint(v64, v, n64, n, j.x, j.y, j.z);
   }
 }
 
@@ -502,6 +536,8 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   int32_t* val = nullptr;
   uint8_t *p = nullptr, *branch = nullptr, *vm_first = nullptr, *em = nullptr, *keep = nullptr;
   int32_t *own_pos = nullptr, *own_rm = nullptr, *vm_second = nullptr, *idx = nullptr;
+  int4* jobs = nullptr;
+  unsigned* njobs = nullptr;
   if (simplify) {
     val = pool.get<int32_t>(NV);
     p = pool.get<uint8_t>(NQ);
@@ -512,6 +548,8 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     own_pos = pool.get<int32_t>(NV);
     own_rm = pool.get<int32_t>(NV);
     vm_second = pool.get<int32_t>(NV);
+    jobs = pool.get<int4>(NQ);
+    njobs = pool.get<unsigned>(2);
     idx = pool.get<int32_t>(std::max(NV, NQ));
     if (pool.err) {
       s.err = pool.err;
@@ -578,9 +616,11 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     fill_i32_kernel<<<gv, 256, 0, st>>>(vm_second, cur.nv, -1);
     cudaMemsetAsync(vm_first, 0, cur.nv, st);
     merge_claim_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.nq, p, val, cur.colors, pass == 0, branch, own_pos, own_rm);
-    merge_apply_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.nq, branch, own_pos, own_rm, cur.v64, cur.v, cur.n64, cur.n,
-                                           vm_first, vm_second, em);
-    s.launches += 8;
+    cudaMemsetAsync(njobs, 0, sizeof(unsigned), st);
+    merge_apply_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.nq, branch, own_pos, own_rm, vm_first, vm_second, em, jobs,
+                                           njobs);
+    midpoint_kernel<<<gq, 256, 0, st>>>(jobs, njobs, cur.v64, cur.v, cur.n64, cur.n);
+    s.launches += 9;
     // remove vertices
     invert_flags_kernel<<<gv, 256, 0, st>>>(vm_first, cur.nv, keep);
     s.launches += 1 + scan_flags(keep, cur.nv, idx, tiles, total, st);

@@ -507,6 +507,7 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   const tmc::CellSpace space = tmc::single_space(g);
   TMC_CUDA(ctx, al.get(&sc.tile_sums, tmc::tmc_tiles(space)));
   TMC_CUDA(ctx, al.get(&sc.totals, 2));
+  TMC_CUDA(ctx, al.get(&sc.amb_n, 1));
   sc.stats = ctx->d_stats;
   TMC_CUDA(ctx, cudaMemsetAsync(sc.stats, 0, 8 * sizeof(unsigned long long), st));
   ctx->launches += tmc::tmc_count(space, sc, st, &ctx->prof);
@@ -669,7 +670,8 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
     dsc = tmc::DmcScratch{rec, voff, qoff, nullptr, tile_sums, totals, ctx->d_stats};
     ctx->launches += tmc::dmc_front_count(space, dsc, st, &ctx->prof);
   } else {
-    tsc = tmc::TmcScratch{rec, voff, qoff, tile_sums, totals, ctx->d_stats, nullptr, nullptr};
+    tsc = tmc::TmcScratch{rec, voff, qoff, tile_sums, totals, ctx->d_stats, nullptr, nullptr, nullptr};
+    TMC_CUDA(ctx, al.get(&tsc.amb_n, 1));
     ctx->launches += tmc::tmc_count(space, tsc, st, &ctx->prof);
   }
   std::vector<unsigned long long> toff((size_t)tiles + 1);

@@ -453,9 +453,11 @@ __device__ void load_amb_cell(const Grid& g, int i, int j, int k, const float u[
 // ------------------------------------------------------------------------------------------
 // kernels
 // ------------------------------------------------------------------------------------------
+// Ambiguous cells are listed (amb_list, warp-aggregated appends) for the float64 counting pass.
 __global__ void __launch_bounds__(kScanThreads) tmc_classify_kernel(CellSpace space, uint32_t* rec,
                                                                    unsigned long long* tile_sums,
-                                                                   unsigned long long* stats) {
+                                                                   unsigned long long* stats, uint32_t* amb_list,
+                                                                   unsigned* amb_n) {
   const Grid g = space.grid_of_tile(blockIdx.x);
   const int64_t n = g.ncells();
   const int64_t vbase = (int64_t)blockIdx.x * kScanTile;
@@ -463,33 +465,42 @@ __global__ void __launch_bounds__(kScanThreads) tmc_classify_kernel(CellSpace sp
   for (int s = 0; s < kScanItems; s++) {
     const int64_t vc = vbase + (int64_t)s * kScanThreads + threadIdx.x;
     if (vc >= space.n) break;
-    const int64_t c = vc - g.vbase;
-    if (c >= n) {  // padding after the volume's last cell
-      rec[vc] = 0;
-      continue;
-    }
-    int i, j, k;
-    tcell_ijk(g, c, i, j, k);
-    float u[8];
-    tload_corners(g, i, j, k, u);
-    unsigned cs = 0;
-#pragma unroll
-    for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
+    const int64_t c = vc - g.vbase;  // cell of the volume (beyond its last cell: padding)
     uint32_t r = 0;
-    if (cs != 0 && cs != 255) {
-      const uint32_t em = case_edge_mask(cs);
-      r = em & owned_edges(i, j, k);
-      if (!case_ambiguous(cs)) {
-        r |= (uint32_t)(c_tmc_tris[cs] & 0xF) << 15;
-      } else {
-        // counted by tmc_amb_count_kernel (dense, float64), which adds to this tile's sums
-        r |= 1u << 21;
-        amb++;
+    bool listed = false;
+    if (c < n) {
+      int i, j, k;
+      tcell_ijk(g, c, i, j, k);
+      float u[8];
+      tload_corners(g, i, j, k, u);
+      unsigned cs = 0;
+#pragma unroll
+      for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
+      if (cs != 0 && cs != 255) {
+        const uint32_t em = case_edge_mask(cs);
+        r = em & owned_edges(i, j, k);
+        if (!case_ambiguous(cs)) {
+          r |= (uint32_t)(c_tmc_tris[cs] & 0xF) << 15;
+        } else {
+          // counted by tmc_amb_count_kernel (float64), which adds to this tile's sums
+          r |= 1u << 21;
+          amb++;
+          listed = true;
+        }
+        act++;
       }
-      act++;
     }
     rec[vc] = r;
     local += ((unsigned long long)trec_nv(r) << 32) | (unsigned long long)trec_ntri(r);
+    const unsigned am = __activemask();
+    const unsigned bal = __ballot_sync(am, listed);
+    if (bal) {
+      const int lane = threadIdx.x & 31, leader = __ffs(bal) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(amb_n, (unsigned)__popc(bal));
+      base = __shfl_sync(am, base, leader);
+      if (listed) amb_list[base + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)vc;
+    }
   }
   unsigned long long tot;
   block_exclusive_scan<unsigned long long>(local, &tot);
@@ -543,47 +554,36 @@ __device__ __forceinline__ int compact_tile(const uint32_t* rec, int64_t base, i
   return *total;
 }
 
-// Ambiguous cells of each tile, densely: p_slice in counting mode (float64), then the counts go into
-// the cell record and the tile's sum.
-__global__ void __launch_bounds__(kScanThreads) tmc_amb_count_kernel(CellSpace space, uint32_t* rec,
-                                                                    unsigned long long* tile_sums,
-                                                                    unsigned long long* stats) {
-  __shared__ uint32_t list[kScanTile];
-  __shared__ int wcount[kScanThreads / 32];
-  __shared__ int total;
-  __shared__ unsigned long long add;
-  const int64_t n = space.n;
+// Ambiguous cells from the classification's list: p_slice in counting mode (float64); the counts go
+// into the cell record and, atomically, into the cell's tile sum (one thread per listed cell, no
+// tile barrier to wait on).
+__global__ void __launch_bounds__(128) tmc_amb_count_kernel(CellSpace space, uint32_t* rec,
+                                                            unsigned long long* tile_sums,
+                                                            unsigned long long* stats, const uint32_t* list,
+                                                            const unsigned* count) {
+  const unsigned na = *count;
   unsigned long long sing = 0;
-  for (int64_t tile = blockIdx.x; tile * kScanTile < n; tile += gridDim.x) {
-    const int64_t base = tile * kScanTile;
-    const Grid g = space.grid_of_tile(tile);
-    if (threadIdx.x == 0) add = 0;
-    const int na = compact_tile(rec, base, n, [](uint32_t r) { return ((r >> 21) & 1) != 0; }, list, wcount, &total);
-    unsigned long long local = 0;
-    for (int a = threadIdx.x; a < na; a += blockDim.x) {
-      const int64_t vcell = base + list[a];
-      const int64_t cell = vcell - g.vbase;
-      int i, j, k;
-      tcell_ijk(g, cell, i, j, k);
-      float u[8];
-      tload_corners(g, i, j, k, u);
-      unsigned cs = 0;
+  for (unsigned a = blockIdx.x * blockDim.x + threadIdx.x; a < na; a += gridDim.x * blockDim.x) {
+    const int64_t vcell = list[a];
+    const Grid g = space.grid_of_tile(vcell / kScanTile);
+    const int64_t cell = vcell - g.vbase;
+    int i, j, k;
+    tcell_ijk(g, cell, i, j, k);
+    float u[8];
+    tload_corners(g, i, j, k, u);
+    unsigned cs = 0;
 #pragma unroll
-      for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
-      AmbCell amb;
-      load_amb_cell(g, i, j, k, u, case_edge_mask(cs), amb, false);
-      int32_t vid[12];
-      for (int e = 0; e < 12; e++) vid[e] = 0;
-      TriSink ts{nullptr, 0};
-      const AmbResult ar = p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, 0, ts, amb.P, amb.N, nullptr);
-      rec[vcell] |= (uint32_t)ar.inner << 12 | (uint32_t)ts.n << 15 | (ar.error ? (1u << 22) : 0u);
-      local += ((unsigned long long)ar.inner << 32) | (unsigned long long)ts.n;
-      sing += ar.error;
-    }
-    if (local) atomicAdd(&add, local);
-    __syncthreads();
-    if (threadIdx.x == 0 && add) tile_sums[tile] += add;
-    __syncthreads();
+    for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
+    AmbCell amb;
+    load_amb_cell(g, i, j, k, u, case_edge_mask(cs), amb, false);
+    int32_t vid[12];
+    for (int e = 0; e < 12; e++) vid[e] = 0;
+    TriSink ts{nullptr, 0};
+    const AmbResult ar = p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, 0, ts, amb.P, amb.N, nullptr);
+    rec[vcell] |= (uint32_t)ar.inner << 12 | (uint32_t)ts.n << 15 | (ar.error ? (1u << 22) : 0u);
+    const unsigned long long add = ((unsigned long long)ar.inner << 32) | (unsigned long long)ts.n;
+    if (add) atomicAdd(tile_sums + vcell / kScanTile, add);
+    sing += ar.error;
   }
   if (sing) atomicAdd(stats + 5, sing);
 }
@@ -841,14 +841,18 @@ int64_t tmc_tiles(const CellSpace& space) { return ceil_div(space.n, kScanTile);
 int tmc_count(const CellSpace& space, TmcScratch& s, cudaStream_t st, Prof* prof) {
   const int64_t n = space.n;
   const int64_t tiles = tmc_tiles(space);
+  // the ambiguous-cell list lives in toff until the offsets kernel overwrites it
+  uint32_t* amb_cells = reinterpret_cast<uint32_t*>(s.toff);
   {
     Stage t(prof, "tmc_classify", st);
-    tmc_classify_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(space, s.rec, s.tile_sums, s.stats);
+    cudaMemsetAsync(s.amb_n, 0, sizeof(unsigned), st);
+    tmc_classify_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(space, s.rec, s.tile_sums, s.stats, amb_cells,
+                                                                  s.amb_n);
   }
   {
     Stage ta(prof, "tmc_amb_count", st);
-    tmc_amb_count_kernel<<<(unsigned)std::min<int64_t>(tiles, 65535), kScanThreads, 0, st>>>(space, s.rec,
-                                                                                              s.tile_sums, s.stats);
+    tmc_amb_count_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 128 * 64), 152 * 16)), 128, 0,
+                           st>>>(space, s.rec, s.tile_sums, s.stats, amb_cells, s.amb_n);
   }
   Stage t(prof, "tmc_scan", st);
   scan_tile_sums_kernel<<<1, 1024, 0, st>>>(s.tile_sums, tiles, s.totals);

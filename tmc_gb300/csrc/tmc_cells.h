@@ -23,6 +23,7 @@ struct TmcScratch {
   unsigned long long* stats;
   uint32_t* amb_list;   // ambiguous cells with triangles, filled by the emit kernel
   unsigned* amb_count;
+  unsigned* amb_n;      // ambiguous cells listed by the classification (count)
 };
 
 // Per-cell scratch is indexed in the cell space; triangles hold vertex indices within their own
