@@ -80,7 +80,13 @@ int main(int argc, char** argv) {
           repr::representative_exact(u, iso, c, t, pe, bx, se);
           float pf[3];
           float lb[49];
-          repr::representative_fast(u, iso, c, t, pts[t], sz, bx, pf, sf, lb, 1);
+          double p64[3];
+          repr::representative_fast(u, iso, c, t, pts[t], sz, bx, pf, sf, lb, 1, p64);
+          // the float64 position the reference uses (its mean point, unrounded, when nothing is found)
+          if (pe[0] != p64[0] || pe[1] != p64[1] || pe[2] != p64[2]) {
+            if (mism < 5) fprintf(stderr, "float64 representative differs cell %d %d %d t %d\n", i, j, k, t);
+            mism++;
+          }
           // the two-pass form must agree wherever it applies
           {
             repr::ProjRecord R;

@@ -139,3 +139,18 @@ def test_dmc_full_pipeline_matches_oracle(ctx, oracle, name, simplify):
     gt, wt = got["t"].reshape(-1, 6), want["t"].reshape(-1, 6)
     diff = np.nonzero(np.any(gt != wt, axis=1))[0]
     assert diff.size <= max(1, gt.shape[0] // 100000), f"{diff.size} quads split differently"
+
+
+def test_dmc_saddle_crops_float64_mean_point(ctx):
+    """Crops of the 1024^3 precision-stress field around contours with no valid projection sample
+    even at 26x26: float64 positions bit-equal to the reference's (its unrounded mean point)."""
+    from tmc_gb300 import native
+    import os
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "saddle_crops.npz"))
+    sp = tuple(z["spacing"].tolist())
+    for q in range(11):
+        vol = V.Volume(z[f"f{q}"], origin=tuple(z[f"o{q}"].tolist()), spacing=sp, iso=0.0)
+        got = ctx.dmc(vol, native.OUT_POS_F64)
+        np.testing.assert_array_equal(got["q"], z[f"q{q}"])
+        np.testing.assert_array_equal(got["v64"], z[f"v{q}"])
+        assert got["stats"][3] >= 1  # the reference's 26x26 failure counter

@@ -114,3 +114,19 @@ def test_oracle_empty_volume(oracle):
     out = oracle.dmc(vol, 1, 0)
     assert out["v"].size == 0 and out["q"].size == 0
     assert oracle.tmc(vol)["t"].size == 0
+
+
+def _saddle_crops():
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "saddle_crops.npz"))
+    sp = tuple(z["spacing"].tolist())
+    return [(V.Volume(z[f"f{q}"], origin=tuple(z[f"o{q}"].tolist()), spacing=sp, iso=0.0), z[f"v{q}"], z[f"q{q}"])
+            for q in range(11)]
+
+
+def test_oracle_saddle_crops(oracle):
+    """Cells of the precision-stress field whose projection fails completely: the reference keeps
+    its float64 mean point; the oracle must return the same doubles."""
+    for vol, v, q in _saddle_crops():
+        got = oracle.dmc(vol, 0)
+        np.testing.assert_array_equal(got["q"], q)
+        np.testing.assert_array_equal(got["v"], v)

@@ -58,3 +58,23 @@ def test_fast_representative_matches_exact(checker, tmp_path, name):
     # the two-pass kernels (float32 / float-float only) handle almost every contour of a generic field
     if not name.startswith("saddle"):
         assert two_pass >= 0.98 * contours
+
+
+def _saddle_crops():
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "saddle_crops.npz"))
+    return [z[f"f{q}"] for q in range(11)]
+
+
+def test_fast_representative_keeps_float64_mean_point(checker, tmp_path):
+    """Crops of the 1024^3 precision-stress field around the contours that find no projection
+    sample even at 26x26: the vertex sits at the reference's float64 mean point, unrounded."""
+    fail2 = 0
+    for crop in _saddle_crops():
+        f = tmp_path / "c.raw"
+        crop.astype(np.float32).tofile(f)
+        r = subprocess.run([str(checker), str(f), "4", "4", "4", "0.0"], capture_output=True, text=True, check=True)
+        contours, mism, f64, fail1f, fail2f, fail1e, fail2e, two_pass = (int(x) for x in r.stdout.split())
+        assert mism == 0, r.stderr
+        assert (fail1f, fail2f) == (fail1e, fail2e)
+        fail2 += fail2f
+    assert fail2 == 11

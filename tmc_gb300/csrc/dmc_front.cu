@@ -133,7 +133,8 @@ struct Normal64 {
 };
 // The reference's float64 normal (UniformGrid::normal on estimateGradient values), for the rare
 // vertices whose gradients cancel so much that the float-float result would lose its margin.
-__device__ __noinline__ Normal64 normal_f64(const Grid g, int i, int j, int k, float pu, float pv, float pw, int flip) {
+__device__ __noinline__ Normal64 normal_f64(const Grid g, int i, int j, int k, double pu, double pv, double pw,
+                                            int flip) {
   const double inv2d[3] = {1.0 / (2 * g.dx), 1.0 / (2 * g.dy), 1.0 / (2 * g.dz)};
   double G[8][3];
   for (int q = 0; q < 8; q++) {
@@ -241,15 +242,18 @@ __device__ __forceinline__ bool vertex_contour(const Grid& g, int i, int j, int 
 }
 
 // Position, normal and local coordinates of vertex vidx at local coordinates p of cell (i, j, k).
+// p64: the float64 local coordinates when they are not the floats p (the reference's unrounded mean
+// point, for contours without any valid projection sample), else null.
 __device__ __forceinline__ void vertex_outputs(const GridCache& G, int i, int j, int k, int64_t cell,
-                                               const float p[3], int64_t vidx, const DmcVertexOut& out, int flip,
-                                               repr::Stats& st) {
+                                               const float p[3], const double* p64, int64_t vidx,
+                                               const DmcVertexOut& out, int flip, repr::Stats& st) {
   const Grid& g = G.g;
   const int64_t o = 3 * vidx;
   // position: UniformGrid::position (cpp_dmc/UniformGrid.h:300-305)
-  const double px = g.ox + (i + (double)p[0]) * g.dx;
-  const double py = g.oy + (j + (double)p[1]) * g.dy;
-  const double pz = g.oz + (k + (double)p[2]) * g.dz;
+  const double lx = p64 ? p64[0] : (double)p[0], ly = p64 ? p64[1] : (double)p[1], lz = p64 ? p64[2] : (double)p[2];
+  const double px = g.ox + (i + lx) * g.dx;
+  const double py = g.oy + (j + ly) * g.dy;
+  const double pz = g.oz + (k + lz) * g.dz;
   out.v[o] = (float)px;
   out.v[o + 1] = (float)py;
   out.v[o + 2] = (float)pz;
@@ -261,7 +265,15 @@ __device__ __forceinline__ void vertex_outputs(const GridCache& G, int i, int j,
   // normal: trilinear interpolation of the 8 corner gradients, normalised (UniformGrid::normal,
   // cpp_dmc/UniformGrid.h:286-298).  When it is kept for the simplification merges it is computed
   // in float-float (relative error ~2^-40, far below the float32 output's 2^-24) on the FP32 pipes.
-  if (out.n64 && (g.flags & kGridNormal64)) {
+  if (p64) {
+    // float64 local coordinates: the reference's float64 normal at them
+    const Normal64 nf = normal_f64(g, i, j, k, lx, ly, lz, flip);
+    for (int d = 0; d < 3; d++) {
+      if (out.n64 && (g.flags & kGridNormal64)) out.n64[o + d] = nf.n[d];
+      out.n[o + d] = (float)nf.n[d];
+    }
+    st.normal_f64++;
+  } else if (out.n64 && (g.flags & kGridNormal64)) {
     ffx::ff Gq[8][3];
 #pragma unroll
     for (int q = 0; q < 8; q++) point_diff_ff(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), Gq[q]);
@@ -360,9 +372,11 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_kernel(CellSpace sp
     VertexContour V;
     if (!vertex_contour(g, i, j, k, rank, cc, G.iso_ff, V)) continue;  // cannot happen: counted
     float p[3];
+    double p64[3];
     repr::representative_fast(V.u, g.iso, V.c, V.tsel, V.pts + 3 * V.tstart, cnt_size(V.c, V.tsel), V.bx, p, st,
-                              sample_lb + threadIdx.x, kVertexThreads);
-    vertex_outputs(G, i, j, k, cell, p, vidx, out, flip, st);
+                              sample_lb + threadIdx.x, kVertexThreads, p64);
+    const bool exact = (double)p[0] == p64[0] && (double)p[1] == p64[1] && (double)p[2] == p64[2];
+    vertex_outputs(G, i, j, k, cell, p, exact ? nullptr : p64, vidx, out, flip, st);
   }
   flush_stats(st, stats);
 }
@@ -447,7 +461,7 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_finish_kernel(CellS
     int i, j, k;
     cell_ijk(g, cell, i, j, k);
     const float p[3] = {q.x, q.y, q.z};
-    vertex_outputs(G, i, j, k, cell, p, vidx, out, flip_all | (g.flags & kGridFlip), st);
+    vertex_outputs(G, i, j, k, cell, p, nullptr, vidx, out, flip_all | (g.flags & kGridFlip), st);
   }
   flush_stats(st, stats);
 }

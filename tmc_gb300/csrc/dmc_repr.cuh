@@ -620,6 +620,7 @@ TMC_HD_COLD int plane_from_gradient_exact(const float* pts, int n, Corners u) {
 
 struct TailOut {
   float p[3];
+  double p64[3];  // the representative in float64: the mean point itself when nothing is found
   int fail2;
 };
 TMC_HD_COLD TailOut representative_tail(Corners u, double iso, uint64_t c, int t, const float* pts, int n,
@@ -680,9 +681,12 @@ TMC_HD int projection_setup(const float u[8], double iso, uint64_t c, int t, con
 }
 
 // Representative of contour t.  pts: the contour's edge points (3 floats each, in contour order),
-// n of them.  On return p holds the local coordinates (floats) of the representative.
+// n of them.  On return p_out holds the local coordinates (floats) of the representative and p64
+// the float64 value the reference places the vertex at: the same floats, except when no sample is
+// valid even at 26x26 (the reference then keeps its float64 mean point, unrounded).
 TMC_HD void representative_fast(const float u[8], double iso, uint64_t c, int t, const float* pts, int n,
-                                const Boxes& bx, float p_out[3], Stats& st, float* buf, int stride) {
+                                const Boxes& bx, float p_out[3], Stats& st, float* buf, int stride,
+                                double p64[3]) {
   ProjCtx P;
   float us[7], vs[7];
   int f64_samples = 0;
@@ -694,6 +698,7 @@ TMC_HD void representative_fast(const float u[8], double iso, uint64_t c, int t,
     p_out[P.A] = pt[0];
     p_out[P.B] = pt[1];
     p_out[P.W] = pt[2];
+    for (int d = 0; d < 3; d++) p64[d] = p_out[d];
     return;
   }
   // no valid 7x7 sample
@@ -702,9 +707,10 @@ TMC_HD void representative_fast(const float u[8], double iso, uint64_t c, int t,
   for (int q = 0; q < 8; q++) uc.f[q] = u[q];
   const TailOut tail = representative_tail(uc, iso, c, t, pts, n, bx, prj);
   st.fail2 += tail.fail2;
-  p_out[0] = tail.p[0];
-  p_out[1] = tail.p[1];
-  p_out[2] = tail.p[2];
+  for (int d = 0; d < 3; d++) {
+    p_out[d] = tail.p[d];
+    p64[d] = tail.p64[d];
+  }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -794,9 +800,10 @@ TMC_HD_COLD TailOut representative_tail(Corners u, double iso, uint64_t c, int t
   pd[A] = ptd[0];
   pd[B] = ptd[1];
   pd[W] = ptd[2];
-  r.p[0] = (float)pd[0];
-  r.p[1] = (float)pd[1];
-  r.p[2] = (float)pd[2];
+  for (int d = 0; d < 3; d++) {
+    r.p64[d] = pd[d];
+    r.p[d] = (float)pd[d];
+  }
   return r;
 }
 
