@@ -10,6 +10,7 @@ larger than L2, so no L2 flush is needed between steps.
     python bench.py --grid 320 --steps 1 --warmup 1 --no-cpu-baseline   # small case for profiling
     python bench.py --workload batch          # 256 uneven volumes: one batched call vs 256 plain calls
     python bench.py --workload precision      # 1024^3 seeded saddles: topology vs the oracle, position error
+    python bench.py --workload serve          # Poisson request stream: server vs one call per request
 
 Prints one JSON line.  `value` is device-resident throughput (field already in HBM); `e2e` is the
 same metric through the C ABI with host buffers (field copied in, mesh copied out every step).
@@ -44,10 +45,13 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--grid", type=int, default=N, help="points per axis of the noise field (profiling cases)")
-    p.add_argument("--workload", default="single", choices=["single", "batch", "precision"],
+    p.add_argument("--workload", default="single", choices=["single", "batch", "precision", "serve"],
                    help="single: the 512^3 volume (TMC + DMC); batch: 256 uneven volumes, DMC; "
                         "precision: 1024^3 periodic field with seeded near-singular saddles")
     p.add_argument("--volumes", type=int, default=256, help="volumes of the batch workload")
+    p.add_argument("--requests", type=int, default=256, help="requests per arrival rate of the serve workload")
+    p.add_argument("--rates", default="0.5,0.8,1.0,1.5",
+                   help="arrival rates of the serve workload, as multiples of the plain loop's capacity")
     return p.parse_args()
 
 
@@ -613,6 +617,145 @@ def run_precision(args, rank, world, local):
     return out if rank == 0 else None
 
 
+# ------------------------------------------------------------------------------------------------
+# serving: Poisson request stream, continuous batching vs one call per request
+# ------------------------------------------------------------------------------------------------
+def _drive(submit, poll, collect, arrivals):
+    """Submit request q at arrivals[q] (seconds from start); a monitor polls every ticket and records
+    its completion time.  Returns (latencies in s, makespan in s)."""
+    n = len(arrivals)
+    tickets = [None] * n
+    t_sub = [0.0] * n
+    t_done = [None] * n
+    start = time.perf_counter()
+
+    def submitter():
+        for q in range(n):
+            dt = arrivals[q] - (time.perf_counter() - start)
+            if dt > 0:
+                time.sleep(dt)
+            t_sub[q] = time.perf_counter()
+            tickets[q] = submit(q)
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    left = n
+    while left:
+        for q in range(n):
+            if t_done[q] is None and tickets[q] is not None and poll(tickets[q]):
+                t_done[q] = time.perf_counter()
+                left -= 1
+        time.sleep(0.0002)
+    th.join()
+    for q in range(n):
+        collect(tickets[q])
+    lat = [t_done[q] - t_sub[q] for q in range(n)]
+    return lat, max(t_done) - start
+
+
+def run_serve(args, rank, world, local):
+    import queue
+
+    import numpy as np
+    import torch
+
+    from tmc_gb300 import native, volumes
+    try:
+        native.load()
+    except RuntimeError:
+        from tmc_gb300 import build
+        build.build()
+    torch.cuda.set_device(local)
+    rng = np.random.Generator(np.random.PCG64(4 + 1000 * rank))
+    n = args.requests
+    vols = [volumes.serve_request(rng) for _ in range(n)]
+    flags = [(0 if q % 2 == 0 else native.OUT_HALFEDGES) | native.OUT_HOST for q in range(n)]
+    cells = sum(v.cells for v in vols)
+    pins = [torch.from_numpy(np.ascontiguousarray(v.data)).pin_memory() for v in vols]
+    tv = [native.make_volume(v, p.data_ptr(), on_device=False) for v, p in zip(vols, pins)]
+    ctx = native.Context(local)
+
+    # the plain loop: one thread, one tmc_dmc_extract call per request, in arrival order
+    class Plain:
+        def __init__(self):
+            self.q = queue.Queue()
+            self.done = {}
+            self.th = threading.Thread(target=self.loop, daemon=True)
+            self.th.start()
+
+        def loop(self):
+            while True:
+                k = self.q.get()
+                if k is None:
+                    return
+                m = ctx.dmc_raw(tv[k], vols[k].iso, flags[k])
+                ctx.free(m)
+                self.done[k] = True
+
+        def submit(self, k):
+            self.q.put(k)
+            return k
+
+        def poll(self, k):
+            return k in self.done
+
+        def close(self):
+            self.q.put(None)
+            self.th.join()
+
+    # capacity of the plain loop (closed loop, all requests queued at once)
+    pl = Plain()
+    lat0, span0 = _drive(pl.submit, pl.poll, lambda k: None, [0.0] * n)
+    pl.close()
+    capacity = n / span0
+    srv = native.Server(local)
+
+    def srv_submit(k):
+        return srv.submit(tv[k], vols[k].iso, native.ALGO_DMC, flags[k])
+
+    def srv_collect(t):
+        srv.release(srv.wait_raw(t))
+
+    # warm-up: every request once (the plain loop's capacity run warmed its context the same way)
+    _drive(srv_submit, srv.poll, srv_collect, [0.0] * n)
+    results = []
+    with ClockSampler(local) as clk:
+        for mult in [float(x) for x in args.rates.split(",")]:
+            lam = mult * capacity
+            gaps = rng.exponential(1.0 / lam, size=n)
+            arrivals = list(np.cumsum(gaps) - gaps[0])
+            lat_s, span_s = _drive(srv_submit, srv.poll, srv_collect, arrivals)
+            pl = Plain()
+            lat_p, span_p = _drive(pl.submit, pl.poll, lambda k: None, arrivals)
+            pl.close()
+            pct = lambda a, p: float(np.percentile(np.asarray(a) * 1e3, p))
+            results.append({
+                "rate_req_s": round(lam, 2), "rate_over_plain_capacity": mult,
+                "server": {"p50_ms": round(pct(lat_s, 50), 2), "p99_ms": round(pct(lat_s, 99), 2),
+                           "gcells_s": round(cells / span_s / 1e9, 4)},
+                "plain": {"p50_ms": round(pct(lat_p, 50), 2), "p99_ms": round(pct(lat_p, 99), 2),
+                          "gcells_s": round(cells / span_p / 1e9, 4)}})
+    st = srv.stats()
+    srv.close()
+    ctx.close()
+    best = max(results, key=lambda r: r["server"]["gcells_s"])
+    out = {
+        "metric": METRIC, "value": best["server"]["gcells_s"], "unit": "Gcells/s", "n_gpus": world,
+        "steps": len(results), "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{n} requests per rate, per-axis size lognormal (median 128, sigma 0.5) clipped to "
+                               "[48, 512], blob / periodic fields, iso U[-0.3, 0.3], DMC shared-vertex or halfedge "
+                               "(50/50), host fields in, host meshes out; Poisson arrivals; 120 GB admission budget",
+                   "cells_per_rate": cells, "seed": 4, "plain_capacity_req_s": round(capacity, 2)},
+        "rates": results,
+        "server_stats": {"batches": st[2], "requests": st[3], "largest_batch": st[5], "peak_admitted_bytes": st[4]},
+        "e2e": {"value": best["server"]["gcells_s"], "unit": "Gcells/s",
+                "h2d_bytes_per_step": int(sum(4 * v.data.size for v in vols)), "d2h_bytes_per_step": None},
+        "clocks": clk.summary(),
+    }
+    return out if rank == 0 else None
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -622,6 +765,8 @@ def main():
         out = run_batch(args, rank, world, local)
     elif args.workload == "precision":
         out = run_precision(args, rank, world, local)
+    elif args.workload == "serve":
+        out = run_serve(args, rank, world, local)
     else:
         out = run_ours(args, rank, world, local)
     if out is not None and rank == 0:

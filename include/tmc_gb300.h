@@ -138,6 +138,32 @@ typedef struct tmc_request {
 /* Extract n independent requests in one batched pipeline (device-resident fields). */
 tmc_status tmc_batch_extract(tmc_ctx* ctx, int32_t n, const tmc_request* reqs, tmc_mesh* outs);
 
+/* request server (no reference counterpart) ------------------------------------------------------
+ * Continuous batching: clients submit requests from any thread; worker threads (one stream each)
+ * take the oldest pending requests whenever they are free, as many as the HBM budget and the batch
+ * limit admit, and run them as one batched extraction, so several batches are in flight at once.
+ * A request's field must stay valid until its ticket completes.  Each mesh equals the mesh of the
+ * same request extracted alone. */
+typedef struct tmc_server tmc_server;
+typedef struct tmc_server_opts {
+  size_t hbm_budget;  /* device bytes admitted requests may use at once, by estimate (0 = 120 GiB) */
+  int32_t workers;    /* batches in flight, one CUDA stream each (0 = 2) */
+  int32_t max_batch;  /* requests per batch (0 = 64) */
+} tmc_server_opts;
+tmc_status tmc_server_create(int device, const tmc_server_opts* opts, tmc_server** out);
+tmc_status tmc_server_destroy(tmc_server* server);
+tmc_status tmc_server_submit(tmc_server* server, const tmc_request* req, int64_t* ticket);
+/* *done = 1 once the ticket's mesh (or error) is ready */
+tmc_status tmc_server_poll(tmc_server* server, int64_t ticket, int32_t* done);
+/* Blocks until the ticket completes (timeout_s < 0: no limit; TMC_ERR_TIMEOUT when it runs out) and
+ * hands over its mesh (mesh.reserved records the worker that owns it). */
+tmc_status tmc_server_wait(tmc_server* server, int64_t ticket, double timeout_s, tmc_mesh* out);
+tmc_status tmc_server_release(tmc_server* server, tmc_mesh* mesh);
+const char* tmc_server_last_error(const tmc_server* server);
+/* [0] submitted [1] completed [2] batches [3] requests in batches [4] peak admitted bytes
+ * [5] largest batch [6] pending now [7] admitted bytes now */
+tmc_status tmc_server_stats(tmc_server* server, int64_t out[8]);
+
 #ifdef __cplusplus
 }
 #endif

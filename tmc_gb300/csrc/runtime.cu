@@ -36,7 +36,10 @@ struct tmc_ctx {
   std::multimap<size_t, void*> pinned_free;
   std::map<void*, size_t> pinned_size;
   void* pinned_get(size_t bytes) {
-    bytes = (bytes + 4095) & ~(size_t)4095;
+    // power-of-two size classes (from 4 KiB): varied request sizes still reuse blocks
+    size_t cls = 4096;
+    while (cls < bytes) cls <<= 1;
+    bytes = cls;
     auto it = pinned_free.lower_bound(bytes);
     if (it != pinned_free.end() && it->first <= 2 * bytes) {
       void* p = it->second;

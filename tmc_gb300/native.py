@@ -37,7 +37,9 @@ ALGO_TMC = 1
 # every symbol include/tmc_gb300.h declares
 EXPORTS = ["tmc_ctx_create", "tmc_ctx_destroy", "tmc_last_error", "tmc_ctx_stream", "tmc_ctx_synchronize",
            "tmc_ctx_launch_count", "tmc_ctx_set_profiling", "tmc_ctx_profile_read", "tmc_dmc_extract", "tmc_tmc_sharedvertex", "tmc_tmc_halfedge",
-           "tmc_mesh_free", "tmc_batch_extract", "tmc_dmc_count_static"]
+           "tmc_mesh_free", "tmc_batch_extract", "tmc_dmc_count_static", "tmc_server_create", "tmc_server_destroy",
+           "tmc_server_submit", "tmc_server_poll", "tmc_server_wait", "tmc_server_release", "tmc_server_last_error",
+           "tmc_server_stats"]
 
 
 class TmcError(RuntimeError):
@@ -67,6 +69,10 @@ class Mesh(ctypes.Structure):
 
 class Request(ctypes.Structure):
     _fields_ = [("vol", Volume), ("iso", ctypes.c_double), ("algo", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
+
+
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("hbm_budget", ctypes.c_size_t), ("workers", ctypes.c_int32), ("max_batch", ctypes.c_int32)]
 
 
 _lib = None
@@ -100,6 +106,15 @@ def load(path: str = LIB_PATH):
     lib.tmc_dmc_count_static.argtypes = [ctypes.c_void_p, ctypes.POINTER(Volume), ctypes.c_double,
                                          ctypes.POINTER(ctypes.c_int64)]
     lib.tmc_dmc_count_static.restype = ctypes.c_int
+    lib.tmc_server_create.argtypes = [ctypes.c_int, ctypes.POINTER(ServerOpts), ctypes.POINTER(ctypes.c_void_p)]
+    lib.tmc_server_destroy.argtypes = [ctypes.c_void_p]
+    lib.tmc_server_submit.argtypes = [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_int64)]
+    lib.tmc_server_poll.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32)]
+    lib.tmc_server_wait.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.POINTER(Mesh)]
+    lib.tmc_server_release.argtypes = [ctypes.c_void_p, ctypes.POINTER(Mesh)]
+    lib.tmc_server_last_error.argtypes = [ctypes.c_void_p]
+    lib.tmc_server_last_error.restype = ctypes.c_char_p
+    lib.tmc_server_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]
     if hasattr(lib, "tmc_batch_extract"):
         lib.tmc_batch_extract.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(Request), ctypes.POINTER(Mesh)]
     _lib = lib
@@ -248,3 +263,74 @@ class Context:
     def tmc(self, vol, flags: int = 0, halfedge: bool = False, iso: float | None = None) -> dict:
         m = self.tmc_raw(make_volume(vol), vol.iso if iso is None else iso, flags | OUT_HOST, halfedge)
         return self.fetch(m)
+
+
+class Server:
+    """tmc_server_*: continuous batching of requests on one GPU (thread-safe submit / wait)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0, workers: int = 0, max_batch: int = 0):
+        self.lib = load()
+        self.h = ctypes.c_void_p()
+        opts = ServerOpts(hbm_budget, workers, max_batch)
+        st = self.lib.tmc_server_create(device, ctypes.byref(opts), ctypes.byref(self.h))
+        if st != TMC_OK:
+            raise TmcError(st, "tmc_server_create failed")
+
+    def close(self):
+        if self.h:
+            self.lib.tmc_server_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != TMC_OK:
+            raise TmcError(st, self.lib.tmc_server_last_error(self.h).decode())
+
+    def submit(self, volume: Volume, iso: float, algo: int, flags: int) -> int:
+        r = Request()
+        r.vol = volume
+        r.iso = float(iso)
+        r.algo = int(algo)
+        r.flags = int(flags)
+        t = ctypes.c_int64()
+        self._check(self.lib.tmc_server_submit(self.h, ctypes.byref(r), ctypes.byref(t)))
+        return t.value
+
+    def poll(self, ticket: int) -> bool:
+        d = ctypes.c_int32()
+        self._check(self.lib.tmc_server_poll(self.h, ticket, ctypes.byref(d)))
+        return bool(d.value)
+
+    def wait_raw(self, ticket: int, timeout: float = -1.0) -> Mesh:
+        m = Mesh()
+        self._check(self.lib.tmc_server_wait(self.h, ticket, float(timeout), ctypes.byref(m)))
+        return m
+
+    def release(self, m: Mesh):
+        self._check(self.lib.tmc_server_release(self.h, ctypes.byref(m)))
+
+    def wait(self, ticket: int, timeout: float = -1.0) -> dict:
+        """The ticket's mesh as numpy arrays (the request must have TMC_OUT_HOST); releases it."""
+        m = self.wait_raw(ticket, timeout)
+        assert not m.on_device, "wait() needs a request with OUT_HOST"
+        nv, nq, nt, nh = m.nr_v, m.nr_q, m.nr_t, m.nr_he
+        out = dict(v=_host_array(m.v, 3 * nv, np.float32), n=_host_array(m.n, 3 * nv, np.float32),
+                   v64=_host_array(m.v64, 3 * nv, np.float64), q=_host_array(m.quads, 4 * nq, np.int32),
+                   t=_host_array(m.tris, 3 * nt, np.int32), he=_host_array(m.he, 4 * nh, np.int32),
+                   hv=_host_array(m.he_v, nv if m.he_v else 0, np.int32),
+                   hf=_host_array(m.he_f, (nq if nq else nt) if m.he_f else 0, np.int32),
+                   vcell=_host_array(m.vcell, nv if m.vcell else 0, np.int64),
+                   vuvw=_host_array(m.vuvw, 3 * nv if m.vuvw else 0, np.float32),
+                   stats=np.array(list(m.stats)))
+        self.release(m)
+        return out
+
+    def stats(self) -> list:
+        a = (ctypes.c_int64 * 8)()
+        self._check(self.lib.tmc_server_stats(self.h, a))
+        return list(a)
