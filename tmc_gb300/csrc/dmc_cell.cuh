@@ -57,14 +57,12 @@ __device__ __forceinline__ void cell_ijk(const Grid& g, int64_t c, int& i, int& 
 }
 
 // Record of one cell (0 for an inactive cell); cc: the 256 packed case contours.
-__device__ __forceinline__ uint32_t classify_cell(const Grid& g, int i, int j, int k, const uint64_t* cc,
-                                                  unsigned long long* stats) {
-  float u[8];
-  load_corners(g, i, j, k, u);
-  const unsigned cs = mc_case(u, g.iso_up);
-  if (cs == 0 || cs == 255) return 0;
+// Record of an active cell (case cs, neither 0 nor 255); u, the corners, are read only for the
+// ambiguous cases (the decider).
+__device__ __forceinline__ uint32_t classify_active(const Grid& g, int i, int j, int k, unsigned cs, const float* u,
+                                                    const uint64_t* cc) {
   const bool amb = case_ambiguous(cs);
-  const uint64_t c = dmc_polygon(cs, u, g.iso, cc);
+  const uint64_t c = amb ? dmc_polygon(cs, u, g.iso, cc) : table_contour(cc[cs]);
   const int ncnt = cnt_count(c);
   uint32_t rec = amb ? (1u << 29) : 0u;
   int nv = 0, flat = 0;
@@ -85,8 +83,17 @@ __device__ __forceinline__ uint32_t classify_cell(const Grid& g, int i, int j, i
   nq += ((em >> 3) & 1) && edge_interior(g, i, j, k, 3);
   nq += ((em >> 8) & 1) && edge_interior(g, i, j, k, 8);
   rec |= (uint32_t)nv | ((uint32_t)nq << 3);
-  (void)stats;
   return rec;
+}
+
+__device__ __forceinline__ uint32_t classify_cell(const Grid& g, int i, int j, int k, const uint64_t* cc,
+                                                  unsigned long long* stats) {
+  float u[8];
+  load_corners(g, i, j, k, u);
+  const unsigned cs = mc_case(u, g.iso_up);
+  (void)stats;
+  if (cs == 0 || cs == 255) return 0;
+  return classify_active(g, i, j, k, cs, u, cc);
 }
 
 }  // namespace tmc

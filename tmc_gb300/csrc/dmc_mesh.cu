@@ -133,10 +133,11 @@ __global__ void color_reduce_kernel(const int32_t* he, uint8_t* col, const int32
 // ---------------------------------------------------------------------------------------------
 // valence and patterns
 // ---------------------------------------------------------------------------------------------
-// vertexValence (:847-871)
-__global__ void valence_kernel(const int32_t* he, int64_t nh, int32_t* val) {
+// vertexValence (:847-871): outgoing halfedges, +1 at the origin of a boundary halfedge's next.
+// The outgoing count is the out-degree the halfedge build just counted; only boundary halfedges
+// (rare) add with atomics.
+__global__ void valence_boundary_kernel(const int32_t* he, int64_t nh, int32_t* val) {
   FOR_EACH(h, nh) {
-    atomicAdd(val + he_origin(he, h), 1);
     if (he_twin(he, h) == -1) atomicAdd(val + he_origin(he, he[5 * h + 2]), 1);
   }
 }
@@ -505,7 +506,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   hw.hf = pool.get<int32_t>(NQ);
   hw.w.deg = pool.get<int32_t>(NV);
   hw.w.off = pool.get<int32_t>(NV);
-  hw.w.cursor = pool.get<int32_t>(NV);
+  hw.w.rank = pool.get<int32_t>(4 * NQ);
   hw.w.list = pool.get<int2>(4 * NQ);
   hw.w.hv_key = pool.get<unsigned long long>(NV);
   hw.w.tiles = pool.get<unsigned long long>(scan_tiles(NV) + 2);
@@ -608,8 +609,8 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
       s.launches += 20;
     }
     Stage tm(prof, "dmc_p3x3y", st);
-    cudaMemsetAsync(val, 0, cur.nv * sizeof(int32_t), st);
-    valence_kernel<<<grid_for(4 * cur.nq, sms), 256, 0, st>>>(hw.he5, 4 * cur.nq, val);
+    cudaMemcpyAsync(val, hw.w.deg, cur.nv * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+    valence_boundary_kernel<<<grid_for(4 * cur.nq, sms), 256, 0, st>>>(hw.he5, 4 * cur.nq, val);
     mark3x3y_kernel<<<gq, 256, 0, st>>>(cur.quads, cur.nq, val, p);
     fill_i32_kernel<<<gv, 256, 0, st>>>(own_pos, cur.nv, -1);
     fill_i32_kernel<<<gv, 256, 0, st>>>(own_rm, cur.nv, -1);
@@ -663,8 +664,8 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     uint8_t* vm0 = vm_first;
     int32_t* vm1 = own_pos;
     int32_t* vm2 = vm_second;
-    cudaMemsetAsync(val, 0, cur.nv * sizeof(int32_t), st);
-    valence_kernel<<<grid_for(4 * cur.nq, sms), 256, 0, st>>>(hw.he5, 4 * cur.nq, val);
+    cudaMemcpyAsync(val, hw.w.deg, cur.nv * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+    valence_boundary_kernel<<<grid_for(4 * cur.nq, sms), 256, 0, st>>>(hw.he5, 4 * cur.nq, val);
     cudaMemsetAsync(p3, 0, cur.nq, st);
     cudaMemsetAsync(rflag, 0, cur.nq, st);
     cudaMemsetAsync(vm0, 0, cur.nv, st);

@@ -24,17 +24,17 @@ namespace tmc {
 
 namespace {
 
-__global__ void he_vertex_init_kernel(int32_t* hv, unsigned long long* hv_key, int32_t* deg, int64_t nv) {
+__global__ void he_vertex_init_kernel(unsigned long long* hv_key, int32_t* deg, int64_t nv) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (int64_t)gridDim.x * blockDim.x) {
-    hv[i] = -1;
     hv_key[i] = 0;
     deg[i] = 0;
   }
 }
 
-// records, face handles, vertex handles (highest index) and out-degrees
-__global__ void he_build_kernel(const int32_t* faces, int P, int64_t nf, int32_t* he, int32_t* hv, int32_t* hf,
-                                int32_t* deg) {
+// records, face handles and out-degrees; the degree counter's old value is the halfedge's slot in
+// its origin's list (one atomic per halfedge)
+__global__ void he_build_kernel(const int32_t* faces, int P, int64_t nf, int32_t* he, int32_t* hf, int32_t* deg,
+                                int32_t* rank) {
   const int64_t nh = nf * P;
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
     const int64_t f = h / P;
@@ -47,19 +47,28 @@ __global__ void he_build_kernel(const int32_t* faces, int P, int64_t nf, int32_t
     e[3] = -1;
     e[4] = 0;
     if (r == 0) hf[f] = (int32_t)(f * P);
-    atomicMax(hv + v0, (int32_t)h);
-    atomicAdd(deg + v0, 1);
+    rank[h] = atomicAdd(deg + v0, 1);
   }
 }
 
-__global__ void he_scatter_kernel(const int32_t* faces, int P, int64_t nf, const int32_t* off, int32_t* cursor,
+__global__ void he_scatter_kernel(const int32_t* faces, int P, int64_t nf, const int32_t* off, const int32_t* rank,
                                   int2* list) {
   const int64_t nh = nf * P;
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
     const int64_t f = h / P;
     const int r = (int)(h - f * P);
     const int v0 = faces[h], v1 = faces[f * P + (r + 1) % P];
-    list[off[v0] + atomicAdd(cursor + v0, 1)] = make_int2((int)h, v1);
+    list[off[v0] + rank[h]] = make_int2((int)h, v1);
+  }
+}
+
+// vertex handle: the highest halfedge with origin v (the reference's last insertion), -1 if none
+__global__ void he_vertex_handle_kernel(const int2* list, const int32_t* off, const int32_t* deg, int64_t nv,
+                                        int32_t* hv) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+    int m = -1;
+    for (int q = off[v], e = off[v] + deg[v]; q < e; q++) m = max(m, list[q].x);
+    hv[v] = m;
   }
 }
 
@@ -169,14 +178,14 @@ int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& 
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)sms * 8));
   };
   int k = 0;
-  he_vertex_init_kernel<<<grid(nv), 256, 0, st>>>(o.hv, w.hv_key, w.deg, nv);
-  he_build_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, o.he, o.hv, o.hf, w.deg);
+  he_vertex_init_kernel<<<grid(nv), 256, 0, st>>>(w.hv_key, w.deg, nv);
+  he_build_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, o.he, o.hf, w.deg, w.rank);
   k += 2 + scan_i32(w.deg, nv, w.off, w.tiles, w.total, st);
-  cudaMemsetAsync(w.cursor, 0, (size_t)std::max<int64_t>(nv, 1) * sizeof(int32_t), st);
-  he_scatter_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.off, w.cursor, w.list);
+  he_scatter_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.off, w.rank, w.list);
   he_twin_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.list, w.off, w.deg, o.he, w.hv_key, w.non_manifold);
+  he_vertex_handle_kernel<<<grid(nv), 256, 0, st>>>(w.list, w.off, w.deg, nv, o.hv);
   he_override_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, o.he, o.hv, w.hv_key);
-  return k + 3;
+  return k + 4;
 }
 
 int pack_halfedges4(const int32_t* he5, int64_t nh, int32_t* he4, int sms, cudaStream_t st) {

@@ -18,7 +18,7 @@ struct HeOut {
 struct HeWork {
   int32_t* deg;                     // nv
   int32_t* off;                     // nv
-  int32_t* cursor;                  // nv
+  int32_t* rank;                    // nh: slot of each halfedge in its origin's list
   int2* list;                       // nh: (halfedge, target vertex) grouped by origin
   unsigned long long* hv_key;       // nv
   unsigned long long* tiles;        // scan_tiles(nv)

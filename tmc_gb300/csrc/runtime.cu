@@ -557,7 +557,7 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
     tmc::HeWork w{};
     TMC_CUDA(ctx, al.get(&w.deg, nv));
     TMC_CUDA(ctx, al.get(&w.off, nv));
-    TMC_CUDA(ctx, al.get(&w.cursor, nv));
+    TMC_CUDA(ctx, al.get(&w.rank, nh));
     TMC_CUDA(ctx, al.get(&w.list, nh));
     TMC_CUDA(ctx, al.get(&w.hv_key, nv));
     TMC_CUDA(ctx, al.get(&w.tiles, tmc::scan_tiles(nv) + 2));
@@ -817,7 +817,7 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
         tmc::HeWork w{};
         TMC_CUDA(ctx, al.get(&w.deg, nv));
         TMC_CUDA(ctx, al.get(&w.off, nv));
-        TMC_CUDA(ctx, al.get(&w.cursor, nv));
+        TMC_CUDA(ctx, al.get(&w.rank, nh));
         TMC_CUDA(ctx, al.get(&w.list, nh));
         TMC_CUDA(ctx, al.get(&w.hv_key, nv));
         TMC_CUDA(ctx, al.get(&w.tiles, tmc::scan_tiles(nv) + 2));
