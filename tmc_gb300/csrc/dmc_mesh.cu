@@ -408,11 +408,95 @@ __device__ __forceinline__ float side(const double* p, const double* q) {
   return (float)sqrt(d);
 }
 
-// collectTriangles (:1387-1460).  Six distinct side lengths (float of a float64 distance, as the
-// reference), four largest cosines in float32; acos only where two candidate angles are within a
-// few ulps of each other.
-__global__ void triangles_kernel(const int32_t* q, int64_t nq, const double* v64, int32_t* t) {
+__device__ __forceinline__ void write_split(int32_t* t, int64_t i, int v0, int v1, int v2, int v3, bool first) {
+  int32_t* o = t + 6 * i;
+  if (first) {
+    o[0] = v1; o[1] = v3; o[2] = v0; o[3] = v1; o[4] = v2; o[5] = v3;
+  } else {
+    o[0] = v0; o[1] = v1; o[2] = v2; o[3] = v0; o[4] = v2; o[5] = v3;
+  }
+}
+
+// Largest cosine of a triangle from float sides with their error bounds, and the bound of the
+// result; false when the cosines are not surely inside [-1, 1].
+__device__ __forceinline__ bool max_cosine_bounded(float a, float b, float c, float ea, float eb, float ec, float& m,
+                                                   float& em) {
+  const float cA = (b * b + c * c - a * a) / (2 * b * c);
+  const float cB = (a * a + c * c - b * b) / (2 * a * c);
+  const float cC = (b * b + a * a - c * c) / (2 * b * a);
+  // first-order propagation of the side errors (doubled), plus the rounding of both evaluations
+  const float rel = ea / a + eb / b + ec / c;
+  const float eA = 2.0f * (2.0f * (a * ea + b * eb + c * ec) / (2 * b * c) + fabsf(cA) * rel) + 0x1p-20f;
+  const float eB = 2.0f * (2.0f * (a * ea + b * eb + c * ec) / (2 * a * c) + fabsf(cB) * rel) + 0x1p-20f;
+  const float eC = 2.0f * (2.0f * (a * ea + b * eb + c * ec) / (2 * b * a) + fabsf(cC) * rel) + 0x1p-20f;
+  if (!(cA - eA >= -1.f && cA + eA <= 1.f && cB - eB >= -1.f && cB + eB <= 1.f && cC - eC >= -1.f &&
+        cC + eC <= 1.f))
+    return false;
+  m = fmaxf(cA, fmaxf(cB, cC));
+  em = fmaxf(eA, fmaxf(eB, eC));
+  return true;
+}
+
+// |p - q| from float positions and a bound of its distance to the reference's float (rounded from
+// the float64 length of the float64 difference); each float position is within 2^-24 |x| of its
+// float64 value.
+__device__ __forceinline__ float side_f(const float* p, const float* q, float& err) {
+  const float dx = p[0] - q[0], dy = p[1] - q[1], dz = p[2] - q[2];
+  const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+  const float mag = fabsf(p[0]) + fabsf(q[0]) + fabsf(p[1]) + fabsf(q[1]) + fabsf(p[2]) + fabsf(q[2]);
+  err = mag * 0x1p-23f + d * 0x1p-20f;
+  return d;
+}
+
+// collectTriangles (:1387-1460), first pass: decides the split from the float positions wherever
+// the two candidates' smallest angles are apart by more than the error bounds; the other quads are
+// listed for the exact pass.
+__global__ void triangles_fast_kernel(const int32_t* q, int64_t nq, const float* v, int32_t* t, uint32_t* list,
+                                      unsigned* count) {
+  const int lane = threadIdx.x & 31;
   FOR_EACH(i, nq) {
+    const int v0 = q[4 * i], v1 = q[4 * i + 1], v2 = q[4 * i + 2], v3 = q[4 * i + 3];
+    const float *P0 = v + 3 * (int64_t)v0, *P1 = v + 3 * (int64_t)v1, *P2 = v + 3 * (int64_t)v2,
+                *P3 = v + 3 * (int64_t)v3;
+    float e01, e12, e20, e23, e30, e13;
+    const float d01 = side_f(P0, P1, e01), d12 = side_f(P1, P2, e12), d20 = side_f(P2, P0, e20),
+                d23 = side_f(P2, P3, e23), d30 = side_f(P3, P0, e30), d13 = side_f(P1, P3, e13);
+    float m1, m2, m3, m4, x1, x2, x3, x4;
+    bool sure = d01 > 0 && d12 > 0 && d20 > 0 && d23 > 0 && d30 > 0 && d13 > 0 &&
+                max_cosine_bounded(d01, d12, d20, e01, e12, e20, m1, x1) &&
+                max_cosine_bounded(d20, d23, d30, e20, e23, e30, m2, x2) &&
+                max_cosine_bounded(d13, d30, d01, e13, e30, e01, m3, x3) &&
+                max_cosine_bounded(d12, d23, d13, e12, e23, e13, m4, x4);
+    bool first = false;
+    if (sure) {
+      // smallest angle of a split = acos of its largest cosine (acos decreasing): the first split
+      // (along v1-v3) wins when its largest cosine is smaller
+      const float xb = fmaxf(m1, m2), eb = fmaxf(x1, x2), xc = fmaxf(m3, m4), ec = fmaxf(x3, x4);
+      if (xb + eb < xc - ec) first = false;       // b1 > c1
+      else if (xb - eb > xc + ec) first = true;  // b1 < c1
+      else sure = false;
+    }
+    if (sure) write_split(t, i, v0, v1, v2, v3, first);
+    const unsigned am = __activemask();
+    const unsigned bal = __ballot_sync(am, !sure);
+    if (bal) {
+      const int leader = __ffs(bal) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(count, (unsigned)__popc(bal));
+      base = __shfl_sync(am, base, leader);
+      if (!sure) list[base + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)i;
+    }
+  }
+}
+
+// collectTriangles (:1387-1460), exact pass over the listed quads.  Six distinct side lengths
+// (float of a float64 distance, as the reference), four largest cosines in float32; acos only where
+// two candidate angles are within a few ulps of each other.
+__global__ void triangles_kernel(const int32_t* q, const uint32_t* list, const unsigned* count, const double* v64,
+                                 int32_t* t) {
+  const int64_t nl = *count;
+  FOR_EACH(a, nl) {
+    const int64_t i = list[a];
     const int v0 = q[4 * i], v1 = q[4 * i + 1], v2 = q[4 * i + 2], v3 = q[4 * i + 3];
     const double *P0 = v64 + 3 * (int64_t)v0, *P1 = v64 + 3 * (int64_t)v1, *P2 = v64 + 3 * (int64_t)v2,
                  *P3 = v64 + 3 * (int64_t)v3;
@@ -443,12 +527,7 @@ __global__ void triangles_kernel(const int32_t* q, int64_t nq, const double* v64
       const double c1 = a4 < a3 ? a4 : a3, c2 = a3 < a4 ? a4 : a3;
       first = (b1 < c1 || (b1 == c1 && b2 <= c2));
     }
-    int32_t* o = t + 6 * i;
-    if (first) {
-      o[0] = v1; o[1] = v3; o[2] = v0; o[3] = v1; o[4] = v2; o[5] = v3;
-    } else {
-      o[0] = v0; o[1] = v1; o[2] = v2; o[3] = v0; o[4] = v2; o[5] = v3;
-    }
+    write_split(t, i, v0, v1, v2, v3, first);
   }
 }
 
@@ -731,8 +810,15 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     if ((s.err = cudaMallocAsync(&tr, std::max<int64_t>(2 * cur.nq, 1) * 3 * sizeof(int32_t), st)) == cudaSuccess) {
       adopt(tr);
       Stage tm(prof, "dmc_triangles", st);
-      triangles_kernel<<<grid_for(cur.nq, sms), 256, 0, st>>>(cur.quads, cur.nq, cur.v64, (int32_t*)tr);
-      s.launches += 1;
+      uint32_t* tlist = pool.get<uint32_t>(std::max<int64_t>(cur.nq, 1));
+      unsigned* tcount = pool.get<unsigned>(2);
+      if ((s.err = pool.err) == cudaSuccess) {
+        cudaMemsetAsync(tcount, 0, sizeof(unsigned), st);
+        triangles_fast_kernel<<<grid_for(cur.nq, sms), 256, 0, st>>>(cur.quads, cur.nq, cur.v, (int32_t*)tr, tlist,
+                                                                      tcount);
+        triangles_kernel<<<grid_for(cur.nq, sms), 256, 0, st>>>(cur.quads, tlist, tcount, cur.v64, (int32_t*)tr);
+        s.launches += 2;
+      }
       out->nt = 2 * cur.nq;
       out->tris = (int32_t*)tr;
     }
