@@ -11,6 +11,7 @@ larger than L2, so no L2 flush is needed between steps.
     python bench.py --workload batch          # 256 uneven volumes: one batched call vs 256 plain calls
     python bench.py --workload precision      # 1024^3 seeded saddles: topology vs the oracle, position error
     python bench.py --workload serve          # Poisson request stream: server vs one call per request
+    python bench.py --workload plain64        # the 64^3 Gaussian-blob plain DMC call (latency-bound)
 
 Prints one JSON line.  `value` is device-resident throughput (field already in HBM); `e2e` is the
 same metric through the C ABI with host buffers (field copied in, mesh copied out every step).
@@ -45,7 +46,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--grid", type=int, default=N, help="points per axis of the noise field (profiling cases)")
-    p.add_argument("--workload", default="single", choices=["single", "batch", "precision", "serve"],
+    p.add_argument("--workload", default="single", choices=["single", "batch", "precision", "serve", "plain64"],
                    help="single: the 512^3 volume (TMC + DMC); batch: 256 uneven volumes, DMC; "
                         "precision: 1024^3 periodic field with seeded near-singular saddles")
     p.add_argument("--volumes", type=int, default=256, help="volumes of the batch workload")
@@ -756,6 +757,72 @@ def run_serve(args, rank, world, local):
     return out if rank == 0 else None
 
 
+# ------------------------------------------------------------------------------------------------
+# the 64^3 Gaussian-blob plain DMC call (no simplification), the reference's CPU-runnable case
+# ------------------------------------------------------------------------------------------------
+def run_plain64(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    from tmc_gb300 import native, volumes
+    try:
+        native.load()
+    except RuntimeError:
+        from tmc_gb300 import build
+        build.build()
+    torch.cuda.set_device(local)
+    vol = volumes.blobs_volume(64, seed=0)
+    cells = vol.cells
+    ctx = native.Context(local)
+    dev = torch.from_numpy(vol.data).cuda()
+    vdev = native.make_volume(vol, dev.data_ptr(), on_device=True)
+    pin = torch.from_numpy(vol.data).pin_memory()
+    vhost = native.make_volume(vol, pin.data_ptr(), on_device=False)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    reps = 200  # calls per step: one call is tens of microseconds
+    for _ in range(args.warmup * reps):
+        ctx.free(ctx.dmc_raw(vdev, vol.iso, 0))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps * reps):
+            m = ctx.dmc_raw(vdev, vol.iso, 0)
+            nv, nq = m.nr_v, m.nr_q
+            ctx.free(m)
+        e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1) / (args.steps * reps)
+    t0 = time.perf_counter()
+    for _ in range(args.steps * reps):
+        ctx.free(ctx.dmc_raw(vhost, vol.iso, native.OUT_HOST))
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / (args.steps * reps)
+    out = {
+        "metric": METRIC, "value": round(cells / (ms * 1e-3) / 1e9, 4), "unit": "Gcells/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms * reps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "64^3 field of 8 Gaussian blobs on [-1,1]^3 (seed 0), isovalue 0.5: plain DMC "
+                               f"(shared-vertex quads, no simplification), {reps} calls per step",
+                   "cells_per_call": cells, "ms_per_call": round(ms, 4), "l2": "field resident (1 MiB): latency-bound"},
+        "mesh": {"v": nv, "q": nq},
+        "e2e": {"value": round(cells / (e2e_ms * 1e-3) / 1e9, 4), "unit": "Gcells/s", "ms_per_call": round(e2e_ms, 4),
+                "h2d_bytes_per_step": 4 * vol.data.size * reps, "d2h_bytes_per_step": (24 * nv + 16 * nq) * reps},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from cpu_libs import OracleLib
+        o = OracleLib()
+        t0 = time.perf_counter()
+        for _ in range(5):
+            o.dmc(vol, 0)
+        dt = (time.perf_counter() - t0) / 5
+        out["cpu_baseline"] = {"value": round(cells / dt / 1e9, 6), "unit": "Gcells/s", "cores": 1, "kind": "port",
+                               "sample": f"the whole 64^3 field, plain DMC, {dt * 1e3:.1f} ms per call"}
+    ctx.close()
+    return out if rank == 0 else None
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -767,6 +834,8 @@ def main():
         out = run_precision(args, rank, world, local)
     elif args.workload == "serve":
         out = run_serve(args, rank, world, local)
+    elif args.workload == "plain64":
+        out = run_plain64(args, rank, world, local)
     else:
         out = run_ours(args, rank, world, local)
     if out is not None and rank == 0:

@@ -31,13 +31,21 @@ inline unsigned grid_for(int64_t n, int sms) {
 
 #define FOR_EACH(i, n) for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
 
-__device__ __forceinline__ int he_twin(const int32_t* he, int64_t h) { return he[5 * h + 3]; }
-__device__ __forceinline__ int he_face(const int32_t* he, int64_t h) { return he[5 * h + 1]; }
-__device__ __forceinline__ int he_origin(const int32_t* he, int64_t h) { return he[5 * h]; }
-__device__ __forceinline__ int he_flag(const int32_t* he, int64_t h) { return he[5 * h + 4]; }
+// Halfedges of a quad mesh: halfedge r of face f is 4f + r; its origin is quad corner r and its
+// next 4f + (r+1)%4 (implicit); twins and flags come from the halfedge build.
+struct HeView {
+  const int32_t* q;
+  const int32_t* twin;
+  const uint8_t* flag;
+};
+__device__ __forceinline__ int he_twin(const HeView& he, int64_t h) { return he.twin[h]; }
+__device__ __forceinline__ int he_face(const HeView&, int64_t h) { return (int)(h >> 2); }
+__device__ __forceinline__ int he_origin(const HeView& he, int64_t h) { return he.q[h]; }
+__device__ __forceinline__ int he_flag(const HeView& he, int64_t h) { return he.flag[h]; }
+__device__ __forceinline__ int64_t he_next(int64_t h) { return (h & ~(int64_t)3) | ((h + 1) & 3); }
 
 // collectNeighbors (cpp_dmc/DualMarchingCubes.cpp:673-702); halfedge r of face f is 4f + r
-__device__ __forceinline__ void neighbors(const int32_t* he, int64_t f, int n[4]) {
+__device__ __forceinline__ void neighbors(const HeView& he, int64_t f, int n[4]) {
 #pragma unroll
   for (int r = 0; r < 4; r++) {
     const int t = he_twin(he, 4 * f + r);
@@ -46,7 +54,7 @@ __device__ __forceinline__ void neighbors(const int32_t* he, int64_t f, int n[4]
 }
 
 // isNonManifold (:874-885)
-__device__ __forceinline__ bool non_manifold(const int32_t* he, int64_t f) {
+__device__ __forceinline__ bool non_manifold(const HeView& he, int64_t f) {
   return he_flag(he, 4 * f) == 1 || he_flag(he, 4 * f + 1) == 1 || he_flag(he, 4 * f + 2) == 1 ||
          he_flag(he, 4 * f + 3) == 1;
 }
@@ -112,7 +120,7 @@ __global__ void __launch_bounds__(kColorThreads) color_scatter_kernel(const uint
     if (ks[s] >= 0) list[at[ks[s]] + rs[s]] = (int32_t)(base + s * kColorThreads + threadIdx.x);
 }
 
-__global__ void color_reduce_kernel(const int32_t* he, uint8_t* col, const int32_t* list, const int32_t* off, int k,
+__global__ void color_reduce_kernel(HeView he, uint8_t* col, const int32_t* list, const int32_t* off, int k,
                                     int lim) {
   const int64_t b = off[k], e = off[k + 1];
   FOR_EACH(idx, e - b) {
@@ -136,9 +144,9 @@ __global__ void color_reduce_kernel(const int32_t* he, uint8_t* col, const int32
 // vertexValence (:847-871): outgoing halfedges, +1 at the origin of a boundary halfedge's next.
 // The outgoing count is the out-degree the halfedge build just counted; only boundary halfedges
 // (rare) add with atomics.
-__global__ void valence_boundary_kernel(const int32_t* he, int64_t nh, int32_t* val) {
+__global__ void valence_boundary_kernel(HeView he, int64_t nh, int32_t* val) {
   FOR_EACH(h, nh) {
-    if (he_twin(he, h) == -1) atomicAdd(val + he_origin(he, he[5 * h + 2]), 1);
+    if (he_twin(he, h) == -1) atomicAdd(val + he_origin(he, he_next(h)), 1);
   }
 }
 
@@ -151,7 +159,7 @@ __global__ void mark3x3y_kernel(const int32_t* q, int64_t nq, const int32_t* val
 }
 
 // mergeVertices3X3Y, both variants (:916-1094): decide removal, claim written vertices
-__global__ void merge_claim_kernel(const int32_t* he, int64_t nq, const uint8_t* p, const int32_t* val,
+__global__ void merge_claim_kernel(HeView he, int64_t nq, const uint8_t* p, const int32_t* val,
                                    const uint8_t* col, int color_pass, uint8_t* branch, int32_t* own_pos,
                                    int32_t* own_rm) {
   FOR_EACH(f, nq) {
@@ -220,7 +228,7 @@ __device__ __forceinline__ void midpoint(double* v64, float* v, double* n64, flo
 // float64 midpoints run densely in midpoint_kernel (a few merging faces per warp would otherwise
 // pay the float64 pipe for the whole warp).  Each destination has one owner, and the sources are
 // never destinations (valence >= 5 vs valence 3), so the merges are independent.
-__global__ void merge_apply_kernel(const int32_t* he, int64_t nq, const uint8_t* branch, const int32_t* own_pos,
+__global__ void merge_apply_kernel(HeView he, int64_t nq, const uint8_t* branch, const int32_t* own_pos,
                                    const int32_t* own_rm, uint8_t* vm_first, int32_t* vm_second, uint8_t* em,
                                    int4* jobs, unsigned* njobs) {
   const int lane = threadIdx.x & 31;
@@ -318,7 +326,7 @@ __global__ void gather_quads_3x3y_kernel(const uint8_t* em, const int32_t* idx, 
 }
 
 // mark3333 (:1189-1322)
-__global__ void mark3333_kernel(const int32_t* he, int64_t nq, const int32_t* val, uint8_t* p3, uint8_t* rflag,
+__global__ void mark3333_kernel(HeView he, int64_t nq, const int32_t* val, uint8_t* p3, uint8_t* rflag,
                                 uint8_t* vm0, int32_t* vm1) {
   FOR_EACH(f, nq) {
     if (non_manifold(he, f)) continue;
@@ -333,7 +341,7 @@ __global__ void mark3333_kernel(const int32_t* he, int64_t nq, const int32_t* va
         break;
       }
       fo[r] = he_face(he, twin);
-      const int nx = he[5 * (int64_t)he[5 * (int64_t)twin + 2] + 2];
+      const int64_t nx = he_next(he_next(twin));
       vo[r] = he_origin(he, nx);
     }
     if (boundary) continue;
@@ -557,9 +565,9 @@ struct Pool {
 };
 
 struct HeBufs {
-  int32_t* he5 = nullptr;
+  int32_t* twin = nullptr;
+  uint8_t* flag = nullptr;
   int32_t* hv = nullptr;
-  int32_t* hf = nullptr;
   HeWork w{};
   unsigned long long* nm = nullptr;
   unsigned* ovf = nullptr;
@@ -580,9 +588,9 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   // working mesh (double buffered)
   DmcMesh cur = in;
   HeBufs hw;
-  hw.he5 = pool.get<int32_t>(5 * 4 * NQ);
+  hw.twin = pool.get<int32_t>(4 * NQ);
+  hw.flag = pool.get<uint8_t>(4 * NQ);
   hw.hv = pool.get<int32_t>(NV);
-  hw.hf = pool.get<int32_t>(NQ);
   hw.w.deg = pool.get<int32_t>(NV);
   hw.w.off = pool.get<int32_t>(NV);
   hw.w.rank = pool.get<int32_t>(4 * NQ);
@@ -603,7 +611,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   auto halfedges = [&](const DmcMesh& m) {
     Stage tm(prof, "dmc_halfedges", st);
     cudaMemsetAsync(hw.nm, 0, 2 * sizeof(unsigned long long), st);
-    HeOut ho{hw.he5, hw.hv, hw.hf};
+    HeOut ho{hw.twin, hw.flag, hw.hv};
     s.launches += build_halfedges(m.quads, 4, m.nq, m.nv, ho, hw.w, sms, st);
   };
   auto read_total = [&]() -> int64_t {
@@ -683,21 +691,21 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
       color_offsets_kernel<<<1, 32, 0, st>>>(cnt, off, cursor);
       color_scatter_kernel<<<gc, kColorThreads, 0, st>>>(cur.colors, cur.nq, cursor, list);
       s.launches += 3;
-      for (int k = 0; k < 19; k++) color_reduce_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.colors, list, off, k, 4);
-      color_reduce_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.colors, list, off, 19, 3);
+      for (int k = 0; k < 19; k++) color_reduce_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.colors, list, off, k, 4);
+      color_reduce_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.colors, list, off, 19, 3);
       s.launches += 20;
     }
     Stage tm(prof, "dmc_p3x3y", st);
     cudaMemcpyAsync(val, hw.w.deg, cur.nv * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
-    valence_boundary_kernel<<<grid_for(4 * cur.nq, sms), 256, 0, st>>>(hw.he5, 4 * cur.nq, val);
+    valence_boundary_kernel<<<grid_for(4 * cur.nq, sms), 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, 4 * cur.nq, val);
     mark3x3y_kernel<<<gq, 256, 0, st>>>(cur.quads, cur.nq, val, p);
     fill_i32_kernel<<<gv, 256, 0, st>>>(own_pos, cur.nv, -1);
     fill_i32_kernel<<<gv, 256, 0, st>>>(own_rm, cur.nv, -1);
     fill_i32_kernel<<<gv, 256, 0, st>>>(vm_second, cur.nv, -1);
     cudaMemsetAsync(vm_first, 0, cur.nv, st);
-    merge_claim_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.nq, p, val, cur.colors, pass == 0, branch, own_pos, own_rm);
+    merge_claim_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.nq, p, val, cur.colors, pass == 0, branch, own_pos, own_rm);
     cudaMemsetAsync(njobs, 0, sizeof(unsigned), st);
-    merge_apply_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.nq, branch, own_pos, own_rm, vm_first, vm_second, em, jobs,
+    merge_apply_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.nq, branch, own_pos, own_rm, vm_first, vm_second, em, jobs,
                                            njobs);
     midpoint_kernel<<<gq, 256, 0, st>>>(jobs, njobs, cur.v64, cur.v, cur.n64, cur.n);
     s.launches += 9;
@@ -744,13 +752,13 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     int32_t* vm1 = own_pos;
     int32_t* vm2 = vm_second;
     cudaMemcpyAsync(val, hw.w.deg, cur.nv * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
-    valence_boundary_kernel<<<grid_for(4 * cur.nq, sms), 256, 0, st>>>(hw.he5, 4 * cur.nq, val);
+    valence_boundary_kernel<<<grid_for(4 * cur.nq, sms), 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, 4 * cur.nq, val);
     cudaMemsetAsync(p3, 0, cur.nq, st);
     cudaMemsetAsync(rflag, 0, cur.nq, st);
     cudaMemsetAsync(vm0, 0, cur.nv, st);
     fill_i32_kernel<<<gv, 256, 0, st>>>(vm1, cur.nv, -1);
     fill_i32_kernel<<<gv, 256, 0, st>>>(vm2, cur.nv, -1);
-    mark3333_kernel<<<gq, 256, 0, st>>>(hw.he5, cur.nq, val, p3, rflag, vm0, vm1);
+    mark3333_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.nq, val, p3, rflag, vm0, vm1);
     invert_flags_kernel<<<gv, 256, 0, st>>>(vm0, cur.nv, keep);
     s.launches += 5 + scan_flags(keep, cur.nv, idx, tiles, total, st);
     const int64_t nv2 = read_total();
@@ -793,9 +801,8 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
       adopt(he4);
       adopt(hv);
       adopt(hf);
-      s.launches += pack_halfedges4(hw.he5, 4 * cur.nq, (int32_t*)he4, sms, st);
+      s.launches += pack_halfedges4(cur.quads, 4, hw.twin, 4 * cur.nq, (int32_t*)he4, (int32_t*)hf, sms, st);
       cudaMemcpyAsync(hv, hw.hv, cur.nv * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
-      cudaMemcpyAsync(hf, hw.hf, cur.nq * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
       cudaMemcpyAsync(h_cnt + 1, hw.nm, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
       cudaStreamSynchronize(st);
       out->non_manifold = (int64_t)h_cnt[1];

@@ -1,7 +1,7 @@
 // Halfedge structure of a polygon mesh (quads or triangles), deterministic, as the reference's
 // DualMarchingCubes::halfedges builds it (cpp_dmc/DualMarchingCubes.cpp:488-671):
 //   halfedge r of face f = index P*f + r (P = 4 or 3): origin = face vertex r, face f,
-//   next = P*f + (r+1)%P, twin via the unordered vertex pair of the edge.
+//   next = P*f + (r+1)%P (all three implicit), twin via the unordered vertex pair of the edge.
 // The reference inserts halfedges into a std::map in index order, so within one edge the
 // halfedges are ranked by index; an edge with
 //   1 halfedge  -> boundary (twin -1)
@@ -31,23 +31,14 @@ __global__ void he_vertex_init_kernel(unsigned long long* hv_key, int32_t* deg, 
   }
 }
 
-// records, face handles and out-degrees; the degree counter's old value is the halfedge's slot in
-// its origin's list (one atomic per halfedge)
-__global__ void he_build_kernel(const int32_t* faces, int P, int64_t nf, int32_t* he, int32_t* hf, int32_t* deg,
+// twins reset, out-degrees; the degree counter's old value is the halfedge's slot in its origin's
+// list (one atomic per halfedge)
+__global__ void he_build_kernel(const int32_t* faces, int64_t nh, int32_t* twin, uint8_t* flag, int32_t* deg,
                                 int32_t* rank) {
-  const int64_t nh = nf * P;
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t f = h / P;
-    const int r = (int)(h - f * P);
-    const int v0 = faces[h];
-    int32_t* e = he + 5 * h;
-    e[0] = v0;
-    e[1] = (int32_t)f;
-    e[2] = (int32_t)(f * P + (r + 1) % P);
-    e[3] = -1;
-    e[4] = 0;
-    if (r == 0) hf[f] = (int32_t)(f * P);
-    rank[h] = atomicAdd(deg + v0, 1);
+    twin[h] = -1;
+    flag[h] = 0;
+    rank[h] = atomicAdd(deg + faces[h], 1);
   }
 }
 
@@ -98,7 +89,7 @@ __device__ __forceinline__ int edge_halfedges(const int2* list, const int32_t* o
 // one thread per halfedge: two-halfedge edges pair without coordination; 3 or 4 are resolved by
 // the edge's lowest halfedge
 __global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const int2* list, const int32_t* off,
-                               const int32_t* deg, int32_t* he, unsigned long long* hv_key,
+                               const int32_t* deg, int32_t* twin, uint8_t* flag, unsigned long long* hv_key,
                                unsigned long long* non_manifold) {
   const int64_t nh = nf * P;
   unsigned long long nm = 0;
@@ -108,25 +99,24 @@ __global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const in
     const int v0 = faces[h], v1 = faces[f * P + (r + 1) % P];
     int id[8];
     const int c = edge_halfedges(list, off, deg, v0, v1, id);
-#define HE(x) (he + 5 * (int64_t)(x))
     if (c == 2) {
-      HE(h)[3] = (id[0] == (int)h) ? id[1] : id[0];
+      twin[h] = (id[0] == (int)h) ? id[1] : id[0];
       continue;
     }
     if (c < 3 || c > 4 || id[0] != (int)h) continue;  // boundary, or resolved by the lowest halfedge
     if (c == 3) {
       const int e0 = id[0], e1 = id[1], e2 = id[2];
-      const int a0 = HE(e0)[0], a1 = HE(e1)[0], a2 = HE(e2)[0];
-      HE(e0)[4] = 2;
-      HE(e1)[4] = 2;
-      HE(e2)[4] = 2;
+      const int a0 = faces[e0], a1 = faces[e1], a2 = faces[e2];
+      flag[e0] = 2;
+      flag[e1] = 2;
+      flag[e2] = 2;
       int lone_v;
       if (a0 != a1) {
-        HE(e0)[3] = e1; HE(e1)[3] = e0; HE(e2)[3] = -1; lone_v = a2;
+        twin[e0] = e1; twin[e1] = e0; twin[e2] = -1; lone_v = a2;
       } else if (a0 != a2) {
-        HE(e0)[3] = e2; HE(e2)[3] = e0; HE(e1)[3] = -1; lone_v = a1;
+        twin[e0] = e2; twin[e2] = e0; twin[e1] = -1; lone_v = a1;
       } else {
-        HE(e1)[3] = e2; HE(e2)[3] = e1; HE(e0)[3] = -1; lone_v = a0;
+        twin[e1] = e2; twin[e2] = e1; twin[e0] = -1; lone_v = a0;
       }
       // the last override in key order wins: remember the largest key (+1 so that 0 = none)
       const unsigned long long key = ((unsigned long long)(unsigned)min(v0, v1) << 32) | (unsigned)max(v0, v1);
@@ -134,26 +124,25 @@ __global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const in
       nm++;
     } else {
       const int e0 = id[0], e1 = id[1], e2 = id[2], e3 = id[3];
-      if (HE(e0)[0] != HE(e1)[0]) {
-        HE(e0)[3] = e1; HE(e1)[3] = e0; HE(e2)[3] = e3; HE(e3)[3] = e2;
+      if (faces[e0] != faces[e1]) {
+        twin[e0] = e1; twin[e1] = e0; twin[e2] = e3; twin[e3] = e2;
       } else {
-        HE(e0)[3] = e2; HE(e2)[3] = e0; HE(e1)[3] = e3; HE(e3)[3] = e1;
+        twin[e0] = e2; twin[e2] = e0; twin[e1] = e3; twin[e3] = e1;
       }
-      HE(e0)[4] = 1; HE(e1)[4] = 1; HE(e2)[4] = 1; HE(e3)[4] = 1;
+      flag[e0] = 1; flag[e1] = 1; flag[e2] = 1; flag[e3] = 1;
       nm++;
     }
-#undef HE
   }
   for (int o = 16; o; o >>= 1) nm += __shfl_down_sync(0xffffffffu, nm, o);
   if ((threadIdx.x & 31) == 0 && nm) atomicAdd(non_manifold, nm);
 }
 
 // the lone halfedge of a three-halfedge edge whose key won its origin's override sets the handle
-__global__ void he_override_kernel(const int32_t* faces, int P, int64_t nf, const int32_t* he, int32_t* hv,
-                                   const unsigned long long* hv_key) {
+__global__ void he_override_kernel(const int32_t* faces, int P, int64_t nf, const int32_t* twin, const uint8_t* flag,
+                                   int32_t* hv, const unsigned long long* hv_key) {
   const int64_t nh = nf * P;
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
-    if (he[5 * h + 4] != 2 || he[5 * h + 3] != -1) continue;
+    if (flag[h] != 2 || twin[h] != -1) continue;
     const int64_t f = h / P;
     const int r = (int)(h - f * P);
     const int v0 = faces[h], v1 = faces[f * P + (r + 1) % P];
@@ -162,10 +151,13 @@ __global__ void he_override_kernel(const int32_t* faces, int P, int64_t nf, cons
   }
 }
 
-__global__ void he_pack4_kernel(const int32_t* he5, int64_t nh, int32_t* he4) {
+__global__ void he_pack4_kernel(const int32_t* faces, int P, const int32_t* twin, int64_t nh, int32_t* he4,
+                                int32_t* hf) {
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t* e = he5 + 5 * h;
-    reinterpret_cast<int4*>(he4)[h] = make_int4(e[0], e[1], e[2], e[3]);
+    const int64_t f = h / P;
+    const int r = (int)(h - f * P);
+    reinterpret_cast<int4*>(he4)[h] = make_int4(faces[h], (int)f, (int)(f * P + (r + 1) % P), twin[h]);
+    if (r == 0 && hf) hf[f] = (int32_t)h;
   }
 }
 
@@ -179,18 +171,20 @@ int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& 
   };
   int k = 0;
   he_vertex_init_kernel<<<grid(nv), 256, 0, st>>>(w.hv_key, w.deg, nv);
-  he_build_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, o.he, o.hf, w.deg, w.rank);
+  he_build_kernel<<<grid(nh), 256, 0, st>>>(faces, nh, o.twin, o.flag, w.deg, w.rank);
   k += 2 + scan_i32(w.deg, nv, w.off, w.tiles, w.total, st);
   he_scatter_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.off, w.rank, w.list);
-  he_twin_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.list, w.off, w.deg, o.he, w.hv_key, w.non_manifold);
+  he_twin_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.list, w.off, w.deg, o.twin, o.flag, w.hv_key,
+                                           w.non_manifold);
   he_vertex_handle_kernel<<<grid(nv), 256, 0, st>>>(w.list, w.off, w.deg, nv, o.hv);
-  he_override_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, o.he, o.hv, w.hv_key);
+  he_override_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, o.twin, o.flag, o.hv, w.hv_key);
   return k + 4;
 }
 
-int pack_halfedges4(const int32_t* he5, int64_t nh, int32_t* he4, int sms, cudaStream_t st) {
+int pack_halfedges4(const int32_t* faces, int P, const int32_t* twin, int64_t nh, int32_t* he4, int32_t* hf, int sms,
+                    cudaStream_t st) {
   const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nh, 256), (int64_t)sms * 8));
-  he_pack4_kernel<<<g, 256, 0, st>>>(he5, nh, he4);
+  he_pack4_kernel<<<g, 256, 0, st>>>(faces, P, twin, nh, he4, hf);
   return 1;
 }
 

@@ -8,10 +8,12 @@
 
 namespace tmc {
 
+// Halfedge h of face f = h / P starts at the face's corner h % P: its origin is faces[h], its next
+// is P*f + (h+1)%P.  Only the twin and the flag are stored.
 struct HeOut {
-  int32_t* he;  // 5 per halfedge: origin, face, next, twin, flag (0 manifold, 1 non-manifold, 2 boundary multiple)
-  int32_t* hv;  // per vertex
-  int32_t* hf;  // per face
+  int32_t* twin;  // per halfedge: twin halfedge, -1 on the boundary
+  uint8_t* flag;  // per halfedge: 0 manifold, 1 non-manifold (4 halfedges), 2 boundary multiple (3)
+  int32_t* hv;    // per vertex: one outgoing halfedge
 };
 
 // scratch for build_halfedges, sized for nv vertices and nh halfedges
@@ -29,7 +31,9 @@ struct HeWork {
 // Returns the number of kernels launched.
 int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& o, HeWork& w, int sms,
                     cudaStream_t st);
-// {origin, face, next, twin} int4 records for the public output
-int pack_halfedges4(const int32_t* he5, int64_t nh, int32_t* he4, int sms, cudaStream_t st);
+// {origin, face, next, twin} int4 records and the face handles (first halfedge of each face) of the
+// public output
+int pack_halfedges4(const int32_t* faces, int P, const int32_t* twin, int64_t nh, int32_t* he4, int32_t* hf, int sms,
+                    cudaStream_t st);
 
 }  // namespace tmc

@@ -553,7 +553,8 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   int64_t non_manifold = 0;
   if (flags & TMC_OUT_HALFEDGES) {
     const int64_t nh = 3 * nt;
-    int32_t *he5 = nullptr, *he4 = nullptr, *hv = nullptr, *hf = nullptr;
+    int32_t *twin = nullptr, *he4 = nullptr, *hv = nullptr, *hf = nullptr;
+    uint8_t* flag = nullptr;
     tmc::HeWork w{};
     TMC_CUDA(ctx, al.get(&w.deg, nv));
     TMC_CUDA(ctx, al.get(&w.off, nv));
@@ -563,15 +564,16 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
     TMC_CUDA(ctx, al.get(&w.tiles, tmc::scan_tiles(nv) + 2));
     TMC_CUDA(ctx, al.get(&w.total, 2));
     TMC_CUDA(ctx, al.get(&w.non_manifold, 2));
-    TMC_CUDA(ctx, al.get(&he5, 5 * nh));
+    TMC_CUDA(ctx, al.get(&twin, nh));
+    TMC_CUDA(ctx, al.get(&flag, nh));
     TMC_CUDA(ctx, cudaMemsetAsync(w.non_manifold, 0, 2 * sizeof(unsigned long long), st));
     TMC_OWN(he4, 4 * nh);
     TMC_OWN(hv, nv);
     TMC_OWN(hf, nt);
-    tmc::HeOut ho{he5, hv, hf};
+    tmc::HeOut ho{twin, flag, hv};
     tmc::Stage stage(&ctx->prof, "tmc_halfedges", st);
     ctx->launches += tmc::build_halfedges(tris, 3, nt, nv, ho, w, ctx->sms, st);
-    ctx->launches += tmc::pack_halfedges4(he5, nh, he4, ctx->sms, st);
+    ctx->launches += tmc::pack_halfedges4(tris, 3, twin, nh, he4, hf, ctx->sms, st);
     TMC_CUDA(ctx, cudaGetLastError());
     TMC_CUDA(ctx, cudaMemcpyAsync(h + 8, w.non_manifold, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     TMC_CUDA(ctx, cudaStreamSynchronize(st));
@@ -813,7 +815,8 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
       out->tris = faces + 3 * fb[q];
       if (f & TMC_OUT_HALFEDGES) {
         const int64_t nh = 3 * nf;
-        int32_t *he5 = nullptr, *he4 = nullptr, *hv = nullptr, *hf = nullptr;
+        int32_t *twin = nullptr, *he4 = nullptr, *hv = nullptr, *hf = nullptr;
+        uint8_t* flag = nullptr;
         tmc::HeWork w{};
         TMC_CUDA(ctx, al.get(&w.deg, nv));
         TMC_CUDA(ctx, al.get(&w.off, nv));
@@ -823,7 +826,8 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
         TMC_CUDA(ctx, al.get(&w.tiles, tmc::scan_tiles(nv) + 2));
         TMC_CUDA(ctx, al.get(&w.total, 2));
         TMC_CUDA(ctx, al.get(&w.non_manifold, 2));
-        TMC_CUDA(ctx, al.get(&he5, 5 * nh));
+        TMC_CUDA(ctx, al.get(&twin, nh));
+        TMC_CUDA(ctx, al.get(&flag, nh));
         TMC_CUDA(ctx, cudaMemsetAsync(w.non_manifold, 0, 2 * sizeof(unsigned long long), st));
         TMC_CUDA(ctx, al.get(&he4, 4 * nh));
         al.release(he4);
@@ -834,10 +838,10 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
         TMC_CUDA(ctx, al.get(&hf, nf));
         al.release(hf);
         mp->dev.push_back(hf);
-        tmc::HeOut ho{he5, hv, hf};
+        tmc::HeOut ho{twin, flag, hv};
         tmc::Stage stage(&ctx->prof, "tmc_halfedges", st);
         ctx->launches += tmc::build_halfedges(out->tris, 3, nf, nv, ho, w, ctx->sms, st);
-        ctx->launches += tmc::pack_halfedges4(he5, nh, he4, ctx->sms, st);
+        ctx->launches += tmc::pack_halfedges4(out->tris, 3, twin, nh, he4, hf, ctx->sms, st);
         TMC_CUDA(ctx, cudaGetLastError());
         TMC_CUDA(ctx, cudaMemcpyAsync(h + 8, w.non_manifold, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         TMC_CUDA(ctx, cudaStreamSynchronize(st));
