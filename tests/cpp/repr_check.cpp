@@ -40,7 +40,7 @@ int main(int argc, char** argv) {
   fclose(in);
   const float iso_up = [&] { float x = (float)iso; if ((double)x < iso) x = nextafterf(x, INFINITY); return x; }();
   long contours = 0, mism = 0, two_pass = 0;
-  repr::Stats se, sf;
+  repr::Stats se, sf, sl;
   for (int k = 0; k < nz - 1; k++)
     for (int j = 0; j < ny - 1; j++)
       for (int i = 0; i < nx - 1; i++) {
@@ -87,6 +87,17 @@ int main(int argc, char** argv) {
             if (mism < 5) fprintf(stderr, "float64 representative differs cell %d %d %d t %d\n", i, j, k, t);
             mism++;
           }
+          // the lane-split form (warp per vertex on the GPU) must agree everywhere
+          {
+            float pl[3];
+            double pl64[3];
+            repr::representative_lanes_host(u, iso, c, t, pts[t], sz, bx, pl, pl64, sl);
+            if (pl[0] != pf[0] || pl[1] != pf[1] || pl[2] != pf[2] || pl64[0] != p64[0] || pl64[1] != p64[1] ||
+                pl64[2] != p64[2]) {
+              if (mism < 5) fprintf(stderr, "lane-split differs cell %d %d %d t %d\n", i, j, k, t);
+              mism++;
+            }
+          }
           // the two-pass form must agree wherever it applies
           {
             repr::ProjRecord R;
@@ -95,6 +106,16 @@ int main(int argc, char** argv) {
               float pr[3];
               int f64r = 0;
               const int rr = repr::projection_from_record(R, pr, lb, 1, f64r);
+              // the lane-group form of the same pass (small meshes) must agree where it finds a point
+              for (int nl : {4, 8, 32}) {
+                float pg[3];
+                const int rg = repr::projection_from_record_lanes_host(R, nl, pg);
+                if (rg == 0 && (pg[0] != pf[0] || pg[1] != pf[1] || pg[2] != pf[2] || rr == 1)) {
+                  if (mism < 5) fprintf(stderr, "lane-group projection differs cell %d %d %d t %d\n", i, j, k, t);
+                  mism++;
+                }
+                if (rg == 1 && rr == 0) mism++;  // a certain empty projection cannot have a winner
+              }
               if (rr == 0) {
                 two_pass++;
                 if (pr[0] != pf[0] || pr[1] != pf[1] || pr[2] != pf[2]) {
@@ -114,6 +135,10 @@ int main(int argc, char** argv) {
         }
       }
   mism += g_decider_mismatch;
+  if (sl.fail1 != se.fail1 || sl.fail2 != se.fail2) {
+    fprintf(stderr, "lane-split failure counters %d %d\n", sl.fail1, sl.fail2);
+    mism++;
+  }
   printf("%ld %ld %d %d %d %d %d %ld\n", contours, mism, sf.fallback, sf.fail1, sf.fail2, se.fail1, se.fail2, two_pass);
   return 0;
 }

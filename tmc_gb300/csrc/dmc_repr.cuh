@@ -680,24 +680,34 @@ TMC_HD int projection_setup(const float u[8], double iso, uint64_t c, int t, con
   return prj;
 }
 
-// Representative of contour t.  pts: the contour's edge points (3 floats each, in contour order),
-// n of them.  On return p_out holds the local coordinates (floats) of the representative and p64
-// the float64 value the reference places the vertex at: the same floats, except when no sample is
-// valid even at 26x26 (the reference then keeps its float64 mean point, unrounded).
-TMC_HD void representative_fast(const float u[8], double iso, uint64_t c, int t, const float* pts, int n,
-                                const Boxes& bx, float p_out[3], Stats& st, float* buf, int stride,
-                                double p64[3]) {
+// 7x7 projection of contour t.  pts: the contour's edge points (3 floats each, in contour order),
+// n of them.  Returns true with p_out (local coordinates) set when a valid sample exists; false
+// when the reference goes on to its 26x26 retry (representative_tail, or the lane-split retry).
+TMC_HD bool representative_7x7(const float u[8], double iso, uint64_t c, int t, const float* pts, int n,
+                               const Boxes& bx, float p_out[3], Stats& st, float* buf, int stride, int& prj) {
   ProjCtx P;
   float us[7], vs[7];
   int f64_samples = 0;
-  const int prj = projection_setup(u, iso, c, t, pts, n, bx, P, us, vs, f64_samples);
+  prj = projection_setup(u, iso, c, t, pts, n, bx, P, us, vs, f64_samples);
   float pt[3];
   const int r = projection_fast<true>(P, us, vs, pt, buf, stride, f64_samples, pts, n);
   st.fallback += f64_samples;
-  if (r == 0) {
-    p_out[P.A] = pt[0];
-    p_out[P.B] = pt[1];
-    p_out[P.W] = pt[2];
+  if (r != 0) return false;
+  p_out[P.A] = pt[0];
+  p_out[P.B] = pt[1];
+  p_out[P.W] = pt[2];
+  return true;
+}
+
+// Representative of contour t.  On return p_out holds the local coordinates (floats) of the
+// representative and p64 the float64 value the reference places the vertex at: the same floats,
+// except when no sample is valid even at 26x26 (the reference then keeps its float64 mean point,
+// unrounded).
+TMC_HD void representative_fast(const float u[8], double iso, uint64_t c, int t, const float* pts, int n,
+                                const Boxes& bx, float p_out[3], Stats& st, float* buf, int stride,
+                                double p64[3]) {
+  int prj = 0;
+  if (representative_7x7(u, iso, c, t, pts, n, bx, p_out, st, buf, stride, prj)) {
     for (int d = 0; d < 3; d++) p64[d] = p_out[d];
     return;
   }
@@ -750,8 +760,8 @@ TMC_HD bool projection_record(const float u[8], double iso, uint64_t c, int t, c
 
 // Projection pass: 0 = found (p set, local coordinates), 1 = no valid sample, 2 = a sample distance
 // needs float64.  The last two go to the one-pass kernel.  f64 counts values recomputed in float64.
-TMC_HD int projection_from_record(const ProjRecord& R, float p_out[3], float* buf, int stride, int& f64) {
-  ProjCtx P;
+// projection state of a record (contours with a record have no neighbour-contour exclusion)
+TMC_HD void ctx_from_record(const ProjRecord& R, ProjCtx& P) {
   uint32_t perm;
   plane(R.prj, P.A, P.B, P.W, perm);
 #pragma unroll
@@ -773,6 +783,11 @@ TMC_HD int projection_from_record(const ProjRecord& R, float p_out[3], float* bu
   P.bx = nullptr;
   P.wlo = R.wlo;
   P.whi = R.whi;
+}
+
+TMC_HD int projection_from_record(const ProjRecord& R, float p_out[3], float* buf, int stride, int& f64) {
+  ProjCtx P;
+  ctx_from_record(R, P);
   float pt[3];
   const int r = projection_fast<false>(P, R.us, R.vs, pt, buf, stride, f64, nullptr, 0);
   if (r == 0) {
@@ -781,6 +796,149 @@ TMC_HD int projection_from_record(const ProjRecord& R, float p_out[3], float* bu
     p_out[P.W] = pt[2];
   }
   return r;
+}
+
+// ---------------------------------------------------------------------------------------------
+// lane-split forms: the samples of one contour are spread over a group of lanes, lane l of nl
+// evaluating samples l, l + nl, ... exactly (no pruning), and the lanes' winners are combined by
+// (distance, loop index) -- the reference's strict `minDistance > d` over its loop order keeps the
+// first of equal distances.  A 26x26 retry then costs ~22 samples per lane of a warp instead of 676
+// on one thread, and a small mesh's 7x7 projections a few samples per lane.
+// ---------------------------------------------------------------------------------------------
+struct LaneBest {
+  float d, w;
+  int q;  // sample index i * ns + j in the reference's loop order; kNoSample when none is valid
+};
+constexpr int kNoSample = 0x7fffffff;
+TMC_HD LaneBest lane_none() { return LaneBest{INFINITY, 0.0f, kNoSample}; }
+TMC_HD bool lane_better(const LaneBest& a, const LaneBest& b) { return a.d < b.d || (a.d == b.d && a.q < b.q); }
+
+// u_i = fl32(umin + i*(umax-umin)/27), i = 1..26: the 26x26 retry's coordinates, in float64 as the
+// reference computes them (projection with nrSamples = 28, cpp_dmc/DualMarchingCubes.cpp:284-299)
+TMC_HD float tail_coord(float lo, float hi, int i) {
+  const double du = ((double)hi - (double)lo) / 27;
+  return (float)((double)lo + i * du);
+}
+
+// The lane's share of the ns x ns samples at (us[i], vs[j]).  Samples whose float-float distance
+// cannot be certified are evaluated in float64 from the mean point of pts.  f64 counts values
+// computed in float64.
+TMC_HD LaneBest grid_lane(const ProjCtx& P, const float* us, const float* vs, int ns, int lane, int nl,
+                          const float* pts, int npts, int& f64) {
+  LaneBest b = lane_none();
+  bool have_pd = false;
+  double pd[3] = {0, 0, 0};
+#pragma unroll 1
+  for (int q = lane; q < ns * ns; q += nl) {
+    const int i = q / ns, j = q - i * ns;
+    SampleOut s = sample_exact(P, us[i], vs[j]);
+    f64 += s.f64;
+    if (s.status == 2) {
+      if (!have_pd) {
+        const Point64 pm = mean_point_exact(pts, npts);
+        pd[0] = pm.p[P.A];
+        pd[1] = pm.p[P.B];
+        pd[2] = pm.p[P.W];
+        have_pd = true;
+      }
+      s = sample_f64(P, pd[0], pd[1], pd[2], us[i], vs[j]);
+      f64++;
+    }
+    // the reference's minDistance starts at 100 (float64): a sample must be closer to count
+    if (s.status != 1 || !(s.d < 100.0f)) continue;
+    if (s.d < b.d) {  // the lane's samples come in loop order: the first of equal distances stays
+      b.d = s.d;
+      b.w = s.w;
+      b.q = q;
+    }
+  }
+  return b;
+}
+
+// The lane's share of a record's 7x7 samples, all evaluated exactly without float64 distances:
+// `uncertain` is set when a distance cannot be certified, and the vertex then goes to the one-pass
+// kernels like the single-thread pass's.
+TMC_HD LaneBest record_lane(const ProjCtx& P, const ProjRecord& R, int lane, int nl, int& f64, bool& uncertain) {
+  LaneBest b = lane_none();
+#pragma unroll 1
+  for (int q = lane; q < 49; q += nl) {
+    const int i = q / 7, j = q - i * 7;
+    const SampleOut s = sample_exact(P, R.us[i], R.vs[j]);
+    f64 += s.f64;
+    if (s.status == 2) uncertain = true;
+    if (s.status != 1 || !(s.d < 100.0f)) continue;
+    if (s.d < b.d) {
+      b.d = s.d;
+      b.w = s.w;
+      b.q = q;
+    }
+  }
+  return b;
+}
+
+// Local coordinates of the winning sample b of an ns x ns grid.
+TMC_HD void lane_point(const ProjCtx& P, const float* us, const float* vs, int ns, const LaneBest& b, float p[3]) {
+  const int i = b.q / ns, j = b.q - i * ns;
+  p[P.A] = us[i];
+  p[P.B] = vs[j];
+  p[P.W] = b.w;
+}
+
+// Host forms (the lanes run one after another and are combined as the device combines them).
+// The lane-split representative, 7x7 and retry alike; returns what representative_fast returns.
+inline void representative_lanes_host(const float u[8], double iso, uint64_t c, int t, const float* pts, int n,
+                                      const Boxes& bx, float p_out[3], double p64[3], Stats& st) {
+  ProjCtx P;
+  float us[26], vs[26];
+  int f64 = 0;
+  projection_setup(u, iso, c, t, pts, n, bx, P, us, vs, f64);
+  LaneBest b = lane_none();
+  for (int lane = 0; lane < 32; lane++) {
+    const LaneBest x = grid_lane(P, us, vs, 7, lane, 32, pts, n, f64);
+    if (lane_better(x, b)) b = x;
+  }
+  int ns = 7;
+  if (b.q == kNoSample) {
+    st.fail1++;
+    for (int a = 0; a < 26; a++) {
+      us[a] = tail_coord(bx.b[t][P.A][0], bx.b[t][P.A][1], a + 1);
+      vs[a] = tail_coord(bx.b[t][P.B][0], bx.b[t][P.B][1], a + 1);
+    }
+    ns = 26;
+    for (int lane = 0; lane < 32; lane++) {
+      const LaneBest x = grid_lane(P, us, vs, 26, lane, 32, pts, n, f64);
+      if (lane_better(x, b)) b = x;
+    }
+  }
+  st.fallback += f64;
+  if (b.q != kNoSample) {
+    lane_point(P, us, vs, ns, b, p_out);
+    for (int d = 0; d < 3; d++) p64[d] = p_out[d];
+    return;
+  }
+  st.fail2++;
+  const Point64 pm = mean_point_exact(pts, n);
+  for (int d = 0; d < 3; d++) {
+    p64[d] = pm.p[d];
+    p_out[d] = (float)pm.p[d];
+  }
+}
+// The lane-group projection pass (nl lanes per record); returns 0 (p_out set), 1 (no valid sample)
+// or 2 (a distance needs float64), as projection_from_record.
+inline int projection_from_record_lanes_host(const ProjRecord& R, int nl, float p_out[3]) {
+  ProjCtx P;
+  ctx_from_record(R, P);
+  LaneBest b = lane_none();
+  bool unc = false;
+  int f64 = 0;
+  for (int lane = 0; lane < nl; lane++) {
+    const LaneBest x = record_lane(P, R, lane, nl, f64, unc);
+    if (lane_better(x, b)) b = x;
+  }
+  if (unc) return 2;
+  if (b.q == kNoSample) return 1;
+  lane_point(P, R.us, R.vs, 7, b, p_out);
+  return 0;
 }
 
 // The 7x7 projection is empty: the reference then tries 26x26 samples from the mean point, in
