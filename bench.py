@@ -797,6 +797,14 @@ def run_plain64(args, rank, world, local):
     for _ in range(args.steps * reps):
         ctx.free(ctx.dmc_raw(vhost, vol.iso, native.OUT_HOST))
     e2e_ms = (time.perf_counter() - t0) * 1e3 / (args.steps * reps)
+    # per-stage device time of one call (separate pass, not timed above)
+    ctx.set_profiling(True)
+    for _ in range(20):
+        m = ctx.dmc_raw(vdev, vol.iso, 0)
+        fails = (m.stats[2], m.stats[3])
+        ctx.free(m)
+    prof = ctx.profile()
+    ctx.set_profiling(False)
     out = {
         "metric": METRIC, "value": round(cells / (ms * 1e-3) / 1e9, 4), "unit": "Gcells/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms * reps, 3), "higher_is_better": True,
@@ -804,7 +812,8 @@ def run_plain64(args, rank, world, local):
         "config": {"workload": "64^3 field of 8 Gaussian blobs on [-1,1]^3 (seed 0), isovalue 0.5: plain DMC "
                                f"(shared-vertex quads, no simplification), {reps} calls per step",
                    "cells_per_call": cells, "ms_per_call": round(ms, 4), "l2": "field resident (1 MiB): latency-bound"},
-        "mesh": {"v": nv, "q": nq},
+        "mesh": {"v": nv, "q": nq, "projection_fail_7x7": fails[0], "projection_fail_26x26": fails[1]},
+        "stages_us_per_call": {k: round(v[0] / 20 * 1e3, 2) for k, v in prof.items()},
         "e2e": {"value": round(cells / (e2e_ms * 1e-3) / 1e9, 4), "unit": "Gcells/s", "ms_per_call": round(e2e_ms, 4),
                 "h2d_bytes_per_step": 4 * vol.data.size * reps, "d2h_bytes_per_step": (24 * nv + 16 * nq) * reps},
         "clocks": clk.summary(),

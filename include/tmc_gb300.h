@@ -11,6 +11,7 @@
  *   tmc_batch_extract      (no single reference call: many dualMC / mc_sharedvertex calls in one launch)
  *   tmc_server_*           (no reference counterpart: request loop around the calls above)
  *   tmc_dmc_count_static   (no reference counterpart: DMC mesh sizes without allocating)
+ *   tmc_ctx_*_tuning, tmc_ctx_autotune  (no reference counterpart: launch shapes and their tuner)
  *
  * Threading: a context is thread-compatible, not thread-safe; use one context per host thread.
  * All work of a context runs on its own CUDA stream.
@@ -106,6 +107,20 @@ tmc_status tmc_ctx_set_profiling(tmc_ctx* ctx, int on);
  * Returns the number of stages, or -1. */
 int32_t tmc_ctx_profile_read(tmc_ctx* ctx, int32_t max, char* names, double* ms, int64_t* counts);
 
+/* Launch shapes (no reference counterpart: the reference's kernels use fixed launch sizes).  Every
+ * setting gives identical meshes; the settings trade the latency of small calls against the
+ * throughput of large ones.  Defaults follow the device's SM count; tmc_ctx_autotune measures. */
+enum {
+  TMC_TUNE_GROUP_LANES = 1,          /* lanes the DMC projection pass may fill with a group of lanes
+                                        per vertex (small meshes); 0 = one thread per vertex */
+  TMC_TUNE_WARP_LIST_MAX = 2,        /* DMC float64-fallback lists up to this length run one warp
+                                        per vertex (0 = one thread per vertex, retries by warp) */
+  TMC_TUNE_VERTEX_BLOCKS_PER_SM = 3, /* grid cap of the per-vertex DMC passes, 1..64 */
+  TMC_TUNE_EMIT_BLOCKS_PER_SM = 4    /* grid cap of the TMC emission kernel, 1..64 */
+};
+tmc_status tmc_ctx_set_tuning(tmc_ctx* ctx, int32_t key, int64_t value);
+tmc_status tmc_ctx_get_tuning(const tmc_ctx* ctx, int32_t key, int64_t* value);
+
 /* extraction -------------------------------------------------------------------------------- */
 /* Dual Marching Cubes: quad mesh (+ triangles, + halfedges).  Vertices in generating-cell order,
  * quads in dual-edge key order, as the reference CPU path emits them. */
@@ -137,6 +152,10 @@ typedef struct tmc_request {
 } tmc_request;
 /* Extract n independent requests in one batched pipeline (device-resident fields). */
 tmc_status tmc_batch_extract(tmc_ctx* ctx, int32_t n, const tmc_request* reqs, tmc_mesh* outs);
+/* Autotuner (no reference counterpart): times `rounds` batched extractions of the given requests
+ * for each candidate launch shape (coordinate descent over the TMC_TUNE_* keys) and keeps the
+ * fastest in the context; *best_ms (optional) receives the time of one batch with the result. */
+tmc_status tmc_ctx_autotune(tmc_ctx* ctx, int32_t n, const tmc_request* reqs, int32_t rounds, double* best_ms);
 
 /* request server (no reference counterpart) ------------------------------------------------------
  * Continuous batching: clients submit requests from any thread; worker threads (one stream each)

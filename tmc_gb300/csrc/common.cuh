@@ -244,4 +244,22 @@ struct DevFlags {
 
 __host__ __device__ __forceinline__ int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// Launch shapes of a context.  Every setting gives identical meshes; they trade the latency of a
+// small call against the throughput of a large one.  Defaults follow the SM count; tmc_ctx_autotune
+// measures candidates on the caller's own volumes.
+struct Tuning {
+  int sms = 1;
+  int64_t group_lanes = 0;        // lanes the projection pass may fill with lane groups (0: one thread per vertex)
+  int64_t warp_list_max = 0;      // float64 fallback lists up to this length run one warp per vertex
+  int vertex_blocks_per_sm = 32;  // grid cap of the per-vertex passes
+  int emit_blocks_per_sm = 8;     // grid cap of the TMC emission kernel
+  static Tuning defaults(int sms) {
+    Tuning t;
+    t.sms = sms;
+    t.group_lanes = (int64_t)sms * 24 * 32;
+    t.warp_list_max = (int64_t)sms * 32;
+    return t;
+  }
+};
+
 }  // namespace tmc

@@ -33,7 +33,8 @@ struct DmcScratch {
   repr::ProjRecord* proj;
   float4* vp;
   uint32_t* fb_list;
-  unsigned* fb_count;
+  unsigned* fb_count;             // [0] fb_list entries, [1] tail_list entries
+  uint32_t* tail_list;            // vertices without a valid 7x7 sample (26x26 retry)
 };
 constexpr size_t kProjRecordBytes = 144;  // sizeof(repr::ProjRecord)
 
@@ -44,6 +45,6 @@ int dmc_front_count(const CellSpace& space, DmcScratch& s, cudaStream_t st, Prof
 // Quads hold vertex indices within their own volume; vertices and quads of the volumes follow one
 // another in the output arrays.
 int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64_t nv, int32_t* quads,
-                   uint8_t* colors, int flip, int sms, cudaStream_t st, Prof* prof = nullptr);
+                   uint8_t* colors, int flip, const Tuning& tu, cudaStream_t st, Prof* prof = nullptr);
 
 }  // namespace tmc

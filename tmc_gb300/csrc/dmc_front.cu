@@ -15,8 +15,12 @@
 //   dmc_classify_kernel  case, contours, per-cell record (counts + edge->vertex rank map) and
 //                        per-tile sums for the scan
 //   dmc_offsets_kernel   in-tile scan -> per-cell vertex / quad offsets
-//   dmc_vertex_kernel    vertex representatives (cpp_dmc representative/projection), normals,
-//                        positions
+//   dmc_vertex_setup_kernel, dmc_project_kernel (dmc_project_group_kernel for small meshes),
+//   dmc_vertex_finish_kernel
+//                        vertex representatives (cpp_dmc representative/projection) in float32
+//                        and float-float, normals, positions
+//   dmc_vertex_kernel    the vertices those leave, with every float64 fallback
+//   dmc_vertex_warp_kernel  the reference's 26x26 retry (and short lists whole), one warp per vertex
 //   dmc_quad_kernel      each cell emits the quads of its crossed interior edges 0, 3, 8 by
 //                        looking up the four cells around the edge
 #include <cstdio>
@@ -398,39 +402,150 @@ __device__ __forceinline__ void flush_stats(const repr::Stats& st, unsigned long
   if (st.fallback + st.normal_f64) atomicAdd(stats + 7, (unsigned long long)(st.fallback + st.normal_f64));
 }
 
-// One-pass vertex kernel: every vertex of the list (all nv when list is null), with every fallback
-// of the reference's arithmetic (neighbour-contour exclusion, float64 samples, the 26x26 tail).
+// One-pass vertex kernel over the vertices the two-pass kernels list (neighbour-contour exclusion,
+// a distance that needs float64): the 7x7 projection with every float64 fallback.  Contours
+// without a valid 7x7 sample go on to the tail list (the reference's 26x26 retry, one warp each).
+// A list of at most `warp_max` entries is left whole to the warp kernel: one thread's serial
+// projection (~0.1 ms) would set the latency of a small call.
 __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_kernel(CellSpace space, const int32_t* voff,
-                                                                     const uint32_t* vwork, int64_t nv,
-                                                                     const uint32_t* list, const unsigned* count,
+                                                                     const uint32_t* vwork, const uint32_t* list,
+                                                                     const unsigned* count, uint32_t* tail_list,
+                                                                     unsigned* tail_count, unsigned warp_max,
                                                                      DmcVertexOut out, int flip_all,
                                                                      unsigned long long* stats) {
   __shared__ uint64_t cc[256];
   __shared__ float sample_lb[49 * kVertexThreads];  // per-thread sample bounds, column per thread
+  const unsigned n = *count;
+  if (n <= warp_max) return;
   for (int c = threadIdx.x; c < 256; c += blockDim.x) cc[c] = c_case_contour[c];
   __syncthreads();
   repr::Stats st;
   GridCache G;
-  const int64_t n = list ? (int64_t)*count : nv;
   for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t vidx = list ? (int64_t)list[a] : a;
+    const int64_t vidx = (int64_t)list[a];
     const uint32_t vcell = vwork[vidx];
     const int rank = (int)(vidx - voff[vcell]);
     G.load(space, vcell);
     const Grid& g = G.g;
     const int64_t cell = vcell - g.vbase;
-    const int flip = flip_all | (g.flags & kGridFlip);
     int i, j, k;
     cell_ijk(g, cell, i, j, k);
     VertexContour V;
     if (!vertex_contour(g, i, j, k, rank, cc, G.iso_ff, V)) continue;  // cannot happen: counted
     float p[3];
-    double p64[3];
-    repr::representative_fast(V.u, g.iso, V.c, V.tsel, V.pts + 3 * V.tstart, cnt_size(V.c, V.tsel), V.bx, p, st,
-                              sample_lb + threadIdx.x, kVertexThreads, p64);
-    const bool exact = (double)p[0] == p64[0] && (double)p[1] == p64[1] && (double)p[2] == p64[2];
-    vertex_outputs(G, i, j, k, cell, p, exact ? nullptr : p64, vidx, out, flip, st);
+    int prj;
+    if (!repr::representative_7x7(V.u, g.iso, V.c, V.tsel, V.pts + 3 * V.tstart, cnt_size(V.c, V.tsel), V.bx, p,
+                                  st, sample_lb + threadIdx.x, kVertexThreads, prj)) {
+      st.fail1++;
+      tail_list[atomicAdd(tail_count, 1u)] = (uint32_t)vidx;
+      continue;
+    }
+    vertex_outputs(G, i, j, k, cell, p, nullptr, vidx, out, flip_all | (g.flags & kGridFlip), st);
   }
+  flush_stats(st, stats);
+}
+
+// warp-wide winner of the lanes' samples: smallest distance, then smallest loop index
+__device__ __forceinline__ repr::LaneBest warp_best(repr::LaneBest b) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    repr::LaneBest x;
+    x.d = __shfl_xor_sync(0xffffffffu, b.d, o);
+    x.w = __shfl_xor_sync(0xffffffffu, b.w, o);
+    x.q = __shfl_xor_sync(0xffffffffu, b.q, o);
+    if (repr::lane_better(x, b)) b = x;
+  }
+  return b;
+}
+
+// One warp per vertex: every lane rebuilds the contour and its projection frame (same cell, no
+// divergence), the lanes split the samples, and lane 0 writes the outputs.  A listed vertex takes
+// ~2 samples per lane for its 7x7 projection and ~22 for the reference's 26x26 retry, instead of up
+// to 725 on one thread.  Work: the whole one-pass list when it has at most `warp_max` entries
+// (the one-pass kernel then does nothing), otherwise the one-pass kernel's tail list.
+__global__ void __launch_bounds__(kVertexThreads) dmc_vertex_warp_kernel(CellSpace space, const int32_t* voff,
+                                                                          const uint32_t* vwork, const uint32_t* list,
+                                                                          const unsigned* count,
+                                                                          const uint32_t* tail_list,
+                                                                          const unsigned* tail_count,
+                                                                          unsigned warp_max, DmcVertexOut out,
+                                                                          int flip_all, unsigned long long* stats) {
+  constexpr int kWarps = kVertexThreads / 32;
+  __shared__ uint64_t cc[256];
+  __shared__ float coords[kWarps][2][26];  // each warp's sample coordinates
+  const bool whole = *count <= warp_max;   // 7x7 projections too, not only retries
+  const uint32_t* L = whole ? list : tail_list;
+  const int64_t n = whole ? (int64_t)*count : (int64_t)*tail_count;
+  if (n == 0) return;
+  for (int c = threadIdx.x; c < 256; c += blockDim.x) cc[c] = c_case_contour[c];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  float* su = coords[wib][0];
+  float* sv = coords[wib][1];
+  repr::Stats st;
+  GridCache G;
+  int f64 = 0;
+  for (int64_t a = (int64_t)blockIdx.x * kWarps + wib; a < n; a += (int64_t)gridDim.x * kWarps) {
+    const int64_t vidx = (int64_t)L[a];
+    const uint32_t vcell = vwork[vidx];
+    const int rank = (int)(vidx - voff[vcell]);
+    G.load(space, vcell);
+    const Grid& g = G.g;
+    const int64_t cell = vcell - g.vbase;
+    int i, j, k;
+    cell_ijk(g, cell, i, j, k);
+    VertexContour V;
+    if (!vertex_contour(g, i, j, k, rank, cc, G.iso_ff, V)) continue;  // cannot happen (warp-uniform)
+    const float* pts = V.pts + 3 * V.tstart;
+    const int npts = cnt_size(V.c, V.tsel);
+    repr::ProjCtx P;
+    float us[7], vs[7];
+    int f64c = 0;  // float64 sample coordinates: the same on every lane (counted once)
+    repr::projection_setup(V.u, g.iso, V.c, V.tsel, pts, npts, V.bx, P, us, vs, f64c);
+    if (whole && lane == 0) f64 += f64c;  // a retry's set-up was counted by the one-pass kernel
+    repr::LaneBest b = repr::lane_none();
+    int ns = 7;
+    if (whole) {
+      __syncwarp();  // the previous vertex's coordinates are no longer read
+      if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < 7; q++) {
+          su[q] = us[q];
+          sv[q] = vs[q];
+        }
+      }
+      __syncwarp();
+      b = warp_best(repr::grid_lane(P, su, sv, 7, lane, 32, pts, npts, f64));
+      if (b.q == repr::kNoSample && lane == 0) st.fail1++;
+    }
+    if (b.q == repr::kNoSample) {
+      // the reference's retry with 26x26 samples from the same mean point
+      __syncwarp();
+      if (lane < 26) {
+        su[lane] = repr::tail_coord(V.bx.b[V.tsel][P.A][0], V.bx.b[V.tsel][P.A][1], lane + 1);
+        sv[lane] = repr::tail_coord(V.bx.b[V.tsel][P.B][0], V.bx.b[V.tsel][P.B][1], lane + 1);
+      }
+      __syncwarp();
+      b = warp_best(repr::grid_lane(P, su, sv, 26, lane, 32, pts, npts, f64));
+      ns = 26;
+    }
+    if (lane == 0) {
+      float p[3];
+      if (b.q != repr::kNoSample) {
+        repr::lane_point(P, su, sv, ns, b, p);
+        vertex_outputs(G, i, j, k, cell, p, nullptr, vidx, out, flip_all | (g.flags & kGridFlip), st);
+      } else {
+        // nothing valid at 26x26 either: the reference keeps its float64 mean point, unrounded
+        st.fail2++;
+        const repr::Point64 pm = repr::mean_point_exact(pts, npts);
+        for (int d = 0; d < 3; d++) p[d] = (float)pm.p[d];
+        const bool exact = (double)p[0] == pm.p[0] && (double)p[1] == pm.p[1] && (double)p[2] == pm.p[2];
+        vertex_outputs(G, i, j, k, cell, p, exact ? nullptr : pm.p, vidx, out, flip_all | (g.flags & kGridFlip),
+                       st);
+      }
+    }
+  }
+  st.fallback += f64;
   flush_stats(st, stats);
 }
 
@@ -496,8 +611,57 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_project_kernel(const repr:
   if (f64) atomicAdd(stats + 7, (unsigned long long)f64);
 }
 
+// Two-pass vertices, pass 2 for small meshes: G lanes per record (G a power of two, 2..32) split
+// its 49 samples, so that a call's latency is that of ~49/G exact samples instead of one thread's
+// serial projection.  Same outputs and lists as dmc_project_kernel.
+__global__ void __launch_bounds__(kVertexThreads) dmc_project_group_kernel(const repr::ProjRecord* recs, int64_t nv,
+                                                                           int G, float4* vp, uint32_t* list,
+                                                                           unsigned* count,
+                                                                           unsigned long long* stats) {
+  const int lane = threadIdx.x & 31;
+  const int gl = lane & (G - 1);
+  const int64_t per_warp = 32 / G;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int f64 = 0;
+  // base is the same on every lane of a warp, so all lanes reach the shuffles
+  for (int64_t base = warp * per_warp; base < nv; base += nwarps * per_warp) {
+    const int64_t vidx = base + lane / G;
+    const bool valid = vidx < nv;
+    const repr::ProjRecord& R = recs[valid ? vidx : base];
+    const bool listed = R.prj < 0;  // already listed by the set-up pass (same for the whole group)
+    repr::LaneBest b = repr::lane_none();
+    bool unc = false;
+    repr::ProjCtx P;
+    if (valid && !listed) {
+      repr::ctx_from_record(R, P);
+      b = repr::record_lane(P, R, gl, G, f64, unc);
+    }
+    for (int o = G >> 1; o > 0; o >>= 1) {
+      repr::LaneBest x;
+      x.d = __shfl_xor_sync(0xffffffffu, b.d, o);
+      x.w = __shfl_xor_sync(0xffffffffu, b.w, o);
+      x.q = __shfl_xor_sync(0xffffffffu, b.q, o);
+      unc = __shfl_xor_sync(0xffffffffu, (int)unc, o) != 0 || unc;
+      if (repr::lane_better(x, b)) b = x;
+    }
+    if (!valid || gl != 0) continue;
+    if (listed) {
+      vp[vidx] = make_float4(0, 0, 0, 1);
+    } else if (unc || b.q == repr::kNoSample) {
+      list[atomicAdd(count, 1u)] = (uint32_t)vidx;  // redone (and counted) by the one-pass kernels
+      vp[vidx] = make_float4(0, 0, 0, 1);
+    } else {
+      float p[3];
+      repr::lane_point(P, R.us, R.vs, 7, b, p);
+      vp[vidx] = make_float4(p[0], p[1], p[2], 0.0f);
+    }
+  }
+  if (f64) atomicAdd(stats + 7, (unsigned long long)f64);
+}
+
 // Two-pass vertices, pass 3: positions, normals and local coordinates of the projected vertices.
-__global__ void __launch_bounds__(kVertexThreads) dmc_vertex_finish_kernel(CellSpace space, const uint32_t* vwork,
+__global__ void __launch_bounds__(kVertexThreads, 4) dmc_vertex_finish_kernel(CellSpace space, const uint32_t* vwork,
                                                                             int64_t nv, const float4* vp,
                                                                             DmcVertexOut out, int flip_all,
                                                                             unsigned long long* stats) {
@@ -599,7 +763,8 @@ int dmc_front_count(const CellSpace& space, DmcScratch& s, cudaStream_t st, Prof
 int64_t dmc_tiles(const CellSpace& space) { return ceil_div(space.n, kScanTile); }
 
 int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64_t nv, int32_t* quads,
-                   uint8_t* colors, int flip, int sms, cudaStream_t st, Prof* prof) {
+                   uint8_t* colors, int flip, const Tuning& tu, cudaStream_t st, Prof* prof) {
+  const int sms = tu.sms;
   const int64_t n = space.n;
   const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 128), (int64_t)sms * 16));
   {
@@ -608,31 +773,42 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
     dmc_offsets_kernel<<<(unsigned)ceil_div(n, kScanTile), kScanThreads, 0, st>>>(n, s.rec, s.tile_sums, s.voff,
                                                                                   s.qoff, s.vwork);
   }
-  const int64_t vb = std::max<int64_t>(1, std::min<int64_t>(ceil_div(nv, kVertexThreads), (int64_t)sms * 32));
+  const int64_t vb = std::max<int64_t>(1, std::min<int64_t>(ceil_div(nv, kVertexThreads), (int64_t)sms * tu.vertex_blocks_per_sm));
   {
     Stage t(prof, "dmc_vertex_setup", st);
-    cudaMemsetAsync(s.fb_count, 0, sizeof(unsigned), st);
+    cudaMemsetAsync(s.fb_count, 0, 2 * sizeof(unsigned), st);
     dmc_vertex_setup_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(space, s.voff, s.vwork, nv, s.proj, s.fb_list,
                                                                      s.fb_count, s.stats);
   }
   {
     Stage t(prof, "dmc_project", st);
-    dmc_project_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(s.proj, nv, s.vp, s.fb_list, s.fb_count, s.stats);
+    // lanes per record: as many as the tuning's lane budget allows (small meshes), else one thread
+    int G = 1;
+    while (G < 32 && nv * G * 2 <= tu.group_lanes) G *= 2;
+    if (G >= 4)
+      dmc_project_group_kernel<<<(unsigned)std::max<int64_t>(1, ceil_div(nv * G, kVertexThreads)), kVertexThreads, 0,
+                                 st>>>(s.proj, nv, G, s.vp, s.fb_list, s.fb_count, s.stats);
+    else
+      dmc_project_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(s.proj, nv, s.vp, s.fb_list, s.fb_count, s.stats);
   }
   {
     Stage t(prof, "dmc_vertex_finish", st);
     dmc_vertex_finish_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(space, s.vwork, nv, s.vp, vo, flip, s.stats);
   }
   {
-    // the listed vertices, one pass with every float64 fallback
+    // the listed vertices: one thread each with every float64 fallback, the 26x26 retries one warp
+    // each; a short list (small calls) entirely one warp per vertex
     Stage t(prof, "dmc_vertex", st);
+    const unsigned warp_max = (unsigned)std::min<int64_t>(tu.warp_list_max, 0x7fffffff);
     const unsigned fb = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nv, kVertexThreads), (int64_t)sms * 8));
-    dmc_vertex_kernel<<<fb, kVertexThreads, 0, st>>>(space, s.voff, s.vwork, nv, s.fb_list, s.fb_count, vo, flip,
-                                                      s.stats);
+    dmc_vertex_kernel<<<fb, kVertexThreads, 0, st>>>(space, s.voff, s.vwork, s.fb_list, s.fb_count, s.tail_list,
+                                                      s.fb_count + 1, warp_max, vo, flip, s.stats);
+    dmc_vertex_warp_kernel<<<(unsigned)std::max(1, sms * 3), kVertexThreads, 0, st>>>(
+        space, s.voff, s.vwork, s.fb_list, s.fb_count, s.tail_list, s.fb_count + 1, warp_max, vo, flip, s.stats);
   }
   Stage t(prof, "dmc_quad", st);
   dmc_quad_kernel<<<(unsigned)blocks, 128, 0, st>>>(space, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
-  return 6;
+  return 7;
 }
 
 }  // namespace tmc

@@ -24,6 +24,7 @@
 struct tmc_ctx {
   int device = 0;
   int sms = 0;
+  tmc::Tuning tune;                       // launch shapes (defaults from the SM count)
   cudaStream_t stream = nullptr;
   cudaMemPool_t pool = nullptr;
   tmc_ctx_opts opts{};
@@ -187,7 +188,8 @@ cudaError_t dmc_vertex_scratch(Allocs& al, tmc::DmcScratch& sc, int64_t nv) {
   sc.proj = reinterpret_cast<tmc::repr::ProjRecord*>(rec);
   if (e == cudaSuccess) e = al.get(&sc.vp, nv);
   if (e == cudaSuccess) e = al.get(&sc.fb_list, nv);
-  if (e == cudaSuccess) e = al.get(&sc.fb_count, 1);
+  if (e == cudaSuccess) e = al.get(&sc.fb_count, 2);
+  if (e == cudaSuccess) e = al.get(&sc.tail_list, nv);
   return e;
 }
 
@@ -251,6 +253,7 @@ tmc_status tmc_ctx_create(int device, const tmc_ctx_opts* opts, tmc_ctx** out) {
     return TMC_ERR_CUDA;
   }
   cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+  ctx->tune = tmc::Tuning::defaults(ctx->sms);
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete ctx;
     return TMC_ERR_CUDA;
@@ -298,6 +301,42 @@ tmc_status tmc_ctx_set_profiling(tmc_ctx* ctx, int on) {
   ctx->prof.on = on != 0;
   ctx->prof.acc.clear();
   return TMC_OK;
+}
+
+tmc_status tmc_ctx_set_tuning(tmc_ctx* ctx, int32_t key, int64_t value) {
+  if (!ctx) return TMC_ERR_INVALID_ARG;
+  switch (key) {
+    case TMC_TUNE_GROUP_LANES:
+      if (value < 0) break;
+      ctx->tune.group_lanes = value;
+      return TMC_OK;
+    case TMC_TUNE_WARP_LIST_MAX:
+      if (value < 0 || value > 0x7fffffff) break;
+      ctx->tune.warp_list_max = value;
+      return TMC_OK;
+    case TMC_TUNE_VERTEX_BLOCKS_PER_SM:
+      if (value < 1 || value > 64) break;
+      ctx->tune.vertex_blocks_per_sm = (int)value;
+      return TMC_OK;
+    case TMC_TUNE_EMIT_BLOCKS_PER_SM:
+      if (value < 1 || value > 64) break;
+      ctx->tune.emit_blocks_per_sm = (int)value;
+      return TMC_OK;
+    default:
+      return fail(ctx, TMC_ERR_INVALID_ARG, "unknown tuning key %d", key);
+  }
+  return fail(ctx, TMC_ERR_INVALID_ARG, "tuning key %d: value %lld out of range", key, (long long)value);
+}
+
+tmc_status tmc_ctx_get_tuning(const tmc_ctx* ctx, int32_t key, int64_t* value) {
+  if (!ctx || !value) return TMC_ERR_INVALID_ARG;
+  switch (key) {
+    case TMC_TUNE_GROUP_LANES: *value = ctx->tune.group_lanes; return TMC_OK;
+    case TMC_TUNE_WARP_LIST_MAX: *value = ctx->tune.warp_list_max; return TMC_OK;
+    case TMC_TUNE_VERTEX_BLOCKS_PER_SM: *value = ctx->tune.vertex_blocks_per_sm; return TMC_OK;
+    case TMC_TUNE_EMIT_BLOCKS_PER_SM: *value = ctx->tune.emit_blocks_per_sm; return TMC_OK;
+    default: return TMC_ERR_INVALID_ARG;
+  }
 }
 
 int32_t tmc_ctx_profile_read(tmc_ctx* ctx, int32_t max, char* names, double* ms, int64_t* counts) {
@@ -408,7 +447,7 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
     delete mp;
     TMC_CUDA(ctx, ce);
   }
-  ctx->launches += tmc::dmc_front_emit(space, sc, vo, nv, quads, colors, (flags & TMC_GRAD_FLIP) ? 1 : 0, ctx->sms, st,
+  ctx->launches += tmc::dmc_front_emit(space, sc, vo, nv, quads, colors, (flags & TMC_GRAD_FLIP) ? 1 : 0, ctx->tune, st,
                                        &ctx->prof);
   TMC_CUDA(ctx, cudaGetLastError());
 
@@ -542,7 +581,7 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   TMC_OWN(vo.n, 3 * nv);
   if (flags & TMC_OUT_POS_F64) TMC_OWN(vo.v64, 3 * nv);
   TMC_OWN(tris, 3 * nt);
-  ctx->launches += tmc::tmc_emit(space, sc, vo, tris, ctx->sms, st, &ctx->prof);
+  ctx->launches += tmc::tmc_emit(space, sc, vo, tris, ctx->tune, st, &ctx->prof);
   TMC_CUDA(ctx, cudaGetLastError());
   out->nr_v = nv;
   out->nr_t = nt;
@@ -728,13 +767,13 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
     TMC_CUDA(ctx, al.get(&dsc.vwork, NV));
     TMC_CUDA(ctx, dmc_vertex_scratch(al, dsc, NV));
     tmc::DmcVertexOut vo{v, nn, v64, n64, vcell, vuvw};
-    ctx->launches += tmc::dmc_front_emit(space, dsc, vo, NV, faces, colors, 0, ctx->sms, st, &ctx->prof);
+    ctx->launches += tmc::dmc_front_emit(space, dsc, vo, NV, faces, colors, 0, ctx->tune, st, &ctx->prof);
   } else {
     TMC_CUDA(ctx, get_shared(&faces, 3 * NF));
     TMC_CUDA(ctx, al.get(&tsc.amb_list, n_amb));
     TMC_CUDA(ctx, al.get(&tsc.amb_count, 1));
     tmc::TmcVertexOut vo{v, nn, v64};
-    ctx->launches += tmc::tmc_emit(space, tsc, vo, faces, ctx->sms, st, &ctx->prof);
+    ctx->launches += tmc::tmc_emit(space, tsc, vo, faces, ctx->tune, st, &ctx->prof);
   }
   TMC_CUDA(ctx, cudaGetLastError());
 
@@ -887,6 +926,74 @@ tmc_status tmc_batch_extract(tmc_ctx* ctx, int32_t n, const tmc_request* reqs, t
   }
   return s;
 }
+}
+
+// Autotuner: coordinate descent over the launch-shape settings, each candidate timed with CUDA
+// events over `rounds` batched extractions of the caller's requests (after one untimed call).  A
+// candidate replaces the current value only when it is at least 2 % faster.  The meshes do not
+// depend on the settings, so the search only changes speed.
+extern "C" tmc_status tmc_ctx_autotune(tmc_ctx* ctx, int32_t n, const tmc_request* reqs, int32_t rounds,
+                                       double* best_ms) {
+  if (!ctx) return TMC_ERR_INVALID_ARG;
+  if (n <= 0 || !reqs || rounds < 1) return fail(ctx, TMC_ERR_INVALID_ARG, "autotune needs requests and rounds >= 1");
+  std::vector<tmc_mesh> outs((size_t)n);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  TMC_CUDA(ctx, cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return fail(ctx, TMC_ERR_CUDA, "cudaEventCreate failed");
+  }
+  auto run = [&](bool timed, double& ms) -> tmc_status {
+    const int reps = timed ? rounds : 1;
+    cudaEventRecord(e0, ctx->stream);
+    for (int r = 0; r < reps; r++) {
+      tmc_status st = tmc_batch_extract(ctx, n, reqs, outs.data());
+      if (st) return st;
+      for (auto& m : outs) tmc_mesh_free(ctx, &m);
+    }
+    cudaEventRecord(e1, ctx->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) return fail(ctx, TMC_ERR_CUDA, "autotune timing failed");
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    ms = t / reps;
+    return TMC_OK;
+  };
+  const int64_t sm = ctx->sms;
+  struct Axis {
+    int32_t key;
+    std::vector<int64_t> values;
+  };
+  const Axis axes[] = {
+      {TMC_TUNE_GROUP_LANES, {0, sm * 12 * 32, sm * 24 * 32, sm * 48 * 32}},
+      {TMC_TUNE_WARP_LIST_MAX, {0, sm * 8, sm * 32, sm * 128}},
+      {TMC_TUNE_VERTEX_BLOCKS_PER_SM, {8, 16, 32}},
+      {TMC_TUNE_EMIT_BLOCKS_PER_SM, {4, 8, 16}},
+  };
+  double best = 0, ms = 0;
+  tmc_status st = run(false, ms);  // warm-up: pools, pinned blocks
+  if (!st) st = run(true, best);
+  for (const Axis& ax : axes) {
+    if (st) break;
+    int64_t keep = 0;
+    tmc_ctx_get_tuning(ctx, ax.key, &keep);
+    const int64_t start = keep;
+    for (int64_t v : ax.values) {
+      if (v == start) continue;
+      tmc_ctx_set_tuning(ctx, ax.key, v);
+      st = run(true, ms);
+      if (st) break;
+      if (ms < 0.98 * best) {
+        best = ms;
+        keep = v;
+      }
+    }
+    tmc_ctx_set_tuning(ctx, ax.key, keep);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  if (best_ms) *best_ms = best;
+  return TMC_OK;
 }
 
 // Context access for entry points defined in other translation units (ctx_access.h).

@@ -737,7 +737,7 @@ __global__ void __launch_bounds__(128) tmc_ambiguous_kernel(CellSpace space, con
   }
 }
 
-__global__ void __launch_bounds__(256) tmc_emit_kernel(CellSpace space, const uint32_t* rec, const int32_t* voff,
+__global__ void __launch_bounds__(256, 4) tmc_emit_kernel(CellSpace space, const uint32_t* rec, const int32_t* voff,
                                                        const int32_t* toff, const unsigned long long* tile_off,
                                                        TmcVertexOut out, int32_t* tris, uint32_t* amb_list,
                                                        unsigned* amb_count) {
@@ -860,11 +860,12 @@ int tmc_count(const CellSpace& space, TmcScratch& s, cudaStream_t st, Prof* prof
   return 4;
 }
 
-int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tris, int sms, cudaStream_t st,
+int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tris, const Tuning& tu, cudaStream_t st,
              Prof* prof) {
+  const int sms = tu.sms;
   Stage t(prof, "tmc_emit", st);
   const int64_t tiles = tmc_tiles(space);
-  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sms * 8));
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sms * tu.emit_blocks_per_sm));
   cudaMemsetAsync(s.amb_count, 0, sizeof(unsigned), st);
   tmc_emit_kernel<<<(unsigned)blocks, kScanThreads, 0, st>>>(space, s.rec, s.voff, s.toff, s.tile_sums, vo, tris,
                                                             s.amb_list, s.amb_count);

@@ -30,7 +30,7 @@ struct TmcScratch {
 // volume, and the volumes' vertices and triangles follow one another in the outputs.
 int64_t tmc_tiles(const CellSpace& space);
 int tmc_count(const CellSpace& space, TmcScratch& s, cudaStream_t st, Prof* prof = nullptr);
-int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tris, int sms, cudaStream_t st,
+int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tris, const Tuning& tu, cudaStream_t st,
              Prof* prof = nullptr);
 
 }  // namespace tmc

@@ -39,7 +39,12 @@ EXPORTS = ["tmc_ctx_create", "tmc_ctx_destroy", "tmc_last_error", "tmc_ctx_strea
            "tmc_ctx_launch_count", "tmc_ctx_set_profiling", "tmc_ctx_profile_read", "tmc_dmc_extract", "tmc_tmc_sharedvertex", "tmc_tmc_halfedge",
            "tmc_mesh_free", "tmc_batch_extract", "tmc_dmc_count_static", "tmc_server_create", "tmc_server_destroy",
            "tmc_server_submit", "tmc_server_poll", "tmc_server_wait", "tmc_server_release", "tmc_server_last_error",
-           "tmc_server_stats"]
+           "tmc_server_stats", "tmc_ctx_set_tuning", "tmc_ctx_get_tuning", "tmc_ctx_autotune"]
+
+TUNE_GROUP_LANES = 1
+TUNE_WARP_LIST_MAX = 2
+TUNE_VERTEX_BLOCKS_PER_SM = 3
+TUNE_EMIT_BLOCKS_PER_SM = 4
 
 
 class TmcError(RuntimeError):
@@ -115,6 +120,10 @@ def load(path: str = LIB_PATH):
     lib.tmc_server_last_error.argtypes = [ctypes.c_void_p]
     lib.tmc_server_last_error.restype = ctypes.c_char_p
     lib.tmc_server_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]
+    lib.tmc_ctx_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64]
+    lib.tmc_ctx_get_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
+    lib.tmc_ctx_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(Request), ctypes.c_int32,
+                                     ctypes.POINTER(ctypes.c_double)]
     if hasattr(lib, "tmc_batch_extract"):
         lib.tmc_batch_extract.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(Request), ctypes.POINTER(Mesh)]
     _lib = lib
@@ -233,6 +242,27 @@ class Context:
         outs = (Mesh * n)()
         self._check(self.lib.tmc_batch_extract(self.h, n, reqs, outs))
         return [outs[q] for q in range(n)]
+
+    def set_tuning(self, key: int, value: int):
+        self._check(self.lib.tmc_ctx_set_tuning(self.h, key, int(value)))
+
+    def get_tuning(self, key: int) -> int:
+        v = ctypes.c_int64()
+        self._check(self.lib.tmc_ctx_get_tuning(self.h, key, ctypes.byref(v)))
+        return v.value
+
+    def autotune(self, volumes: list, isos: list, algos: list, flags: list, rounds: int = 3) -> float:
+        """tmc_ctx_autotune over prepared tmc_volume structs; returns the best batch time (ms)."""
+        n = len(volumes)
+        reqs = (Request * n)()
+        for q in range(n):
+            reqs[q].vol = volumes[q]
+            reqs[q].iso = float(isos[q])
+            reqs[q].algo = int(algos[q])
+            reqs[q].flags = int(flags[q])
+        best = ctypes.c_double()
+        self._check(self.lib.tmc_ctx_autotune(self.h, n, reqs, rounds, ctypes.byref(best)))
+        return best.value
 
     def batch(self, vols: list, algos: list, flags: list) -> list:
         """Batched extraction of host volumes (tmc_gb300.volumes.Volume); numpy results."""
