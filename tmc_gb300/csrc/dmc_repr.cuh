@@ -488,6 +488,15 @@ TMC_HD void w_window(float lo, float hi, float& wlo, float& whi) {
   w_window_flat(lo, hi, wlo, whi);
 }
 
+// index of the lowest set bit of a non-zero mask
+TMC_HD int lowest_bit(uint64_t x) {
+#ifdef __CUDA_ARCH__
+  return __ffsll((long long)x) - 1;
+#else
+  return __builtin_ctzll(x);
+#endif
+}
+
 // 0 = found (pt set), 1 = no valid sample.  buf: 49 slots (lower bound of each sample's distance,
 // +inf when it cannot win), slot q at buf[q * stride] (shared memory on the GPU, one column per
 // thread).  The 3x3 samples around the mean point are approximated first; every other sample is
@@ -527,39 +536,45 @@ TMC_HD int projection_fast(const ProjCtx& P, const float* us, const float* vs, f
       approx_into(P, us, vs, i, j, buf, stride, m);
     }
   }
-  // exact evaluation of every sample that can still win, in the reference's loop order
+  // exact evaluation of every sample that can still win, in the reference's loop order.  The
+  // candidates come from a bit mask, lowest first: the lanes of a warp then evaluate their k-th
+  // candidates together instead of one loop slot at a time (a slot is rarely everyone's candidate).
+  uint64_t cand = 0;
+#pragma unroll 1
+  for (int q = 0; q < 49; q++)
+    if (buf[q * stride] <= m) cand |= 1ull << q;
   float best = 100.0f;
   bool found = false;
   bool have_pd = false;
   double pd[3] = {0, 0, 0};
 #pragma unroll 1
-  for (int i = 0; i < 7; i++)
-#pragma unroll 1
-    for (int j = 0; j < 7; j++) {
-      if (!(buf[(7 * i + j) * stride] <= m)) continue;
-      SampleOut s = sample_exact(P, us[i], vs[j]);
-      f64_samples += s.f64;
-      if (s.status == 2) {
-        if (!F64) return 2;
-        if (!have_pd) {
-          const Point64 pm = mean_point_exact(pts, npts);
-          pd[0] = pm.p[P.A];
-          pd[1] = pm.p[P.B];
-          pd[2] = pm.p[P.W];
-          have_pd = true;
-        }
-        s = sample_f64(P, pd[0], pd[1], pd[2], us[i], vs[j]);
-        f64_samples++;
+  while (cand) {
+    const int q = lowest_bit(cand);
+    cand &= cand - 1;
+    const int i = q / 7, j = q - 7 * i;
+    SampleOut s = sample_exact(P, us[i], vs[j]);
+    f64_samples += s.f64;
+    if (s.status == 2) {
+      if (!F64) return 2;
+      if (!have_pd) {
+        const Point64 pm = mean_point_exact(pts, npts);
+        pd[0] = pm.p[P.A];
+        pd[1] = pm.p[P.B];
+        pd[2] = pm.p[P.W];
+        have_pd = true;
       }
-      if (s.status != 1) continue;
-      if (best > s.d) {
-        best = s.d;
-        pt[0] = us[i];
-        pt[1] = vs[j];
-        pt[2] = s.w;
-        found = true;
-      }
+      s = sample_f64(P, pd[0], pd[1], pd[2], us[i], vs[j]);
+      f64_samples++;
     }
+    if (s.status != 1) continue;
+    if (best > s.d) {
+      best = s.d;
+      pt[0] = us[i];
+      pt[1] = vs[j];
+      pt[2] = s.w;
+      found = true;
+    }
+  }
   return found ? 0 : 1;
 }
 
