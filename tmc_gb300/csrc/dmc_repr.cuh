@@ -520,21 +520,41 @@ TMC_HD int projection_fast(const ProjCtx& P, const float* us, const float* vs, f
       approx_into(P, us, vs, i, j, buf, stride, m);
       done |= 1ull << (7 * i + j);
     }
+  // every other sample: skipped when even its distance within the sample plane (a lower bound of
+  // the reference's float distance, whatever w is) exceeds m.  The samples that survive the bound
+  // of the 3x3 seeds form a mask, taken lowest first so that the lanes of a warp evaluate their
+  // k-th survivors together; m keeps falling meanwhile, so each is checked again before its turn.
   const float Ep = 0x1p-22f;
+  float e1s[7];
+#pragma unroll
+  for (int j = 0; j < 7; j++) {
+    const float e1 = fmaxf(fabsf(P.pf[1] - vs[j]) - Ep, 0.0f);
+    e1s[j] = e1 * e1;
+  }
+  uint64_t need = 0;
 #pragma unroll 1
   for (int i = 0; i < 7; i++) {
     const float e0 = fmaxf(fabsf(P.pf[0] - us[i]) - Ep, 0.0f);
-#pragma unroll 1
+#pragma unroll
     for (int j = 0; j < 7; j++) {
-      if ((done >> (7 * i + j)) & 1) continue;
-      const float e1 = fmaxf(fabsf(P.pf[1] - vs[j]) - Ep, 0.0f);
-      // lower bound of the reference's float distance, whatever w is
-      if ((e0 * e0 + e1 * e1) * (1.0f - 0x1p-20f) > m) {
-        buf[(7 * i + j) * stride] = INFINITY;
-        continue;
-      }
-      approx_into(P, us, vs, i, j, buf, stride, m);
+      const int q = 7 * i + j;
+      if ((done >> q) & 1) continue;
+      if ((e0 * e0 + e1s[j]) * (1.0f - 0x1p-20f) > m) buf[q * stride] = INFINITY;
+      else need |= 1ull << q;
     }
+  }
+#pragma unroll 1
+  while (need) {
+    const int q = lowest_bit(need);
+    need &= need - 1;
+    const int i = q / 7, j = q - 7 * i;
+    const float e0 = fmaxf(fabsf(P.pf[0] - us[i]) - Ep, 0.0f);
+    const float e1 = fmaxf(fabsf(P.pf[1] - vs[j]) - Ep, 0.0f);
+    if ((e0 * e0 + e1 * e1) * (1.0f - 0x1p-20f) > m) {
+      buf[q * stride] = INFINITY;
+      continue;
+    }
+    approx_into(P, us, vs, i, j, buf, stride, m);
   }
   // exact evaluation of every sample that can still win, in the reference's loop order.  The
   // candidates come from a bit mask, lowest first: the lanes of a warp then evaluate their k-th
