@@ -612,11 +612,19 @@ __global__ void __launch_bounds__(kScanThreads) tmc_offsets_kernel(int64_t n, co
   }
 }
 
+// corner value v of a cell's eight (selects, so that a run-time index keeps u in registers)
+__device__ __forceinline__ float pick8(const float u[8], int v) {
+  float r = u[0];
+#pragma unroll
+  for (int q = 1; q < 8; q++) r = (v == q) ? u[q] : r;
+  return r;
+}
+
 // edge vertex: interpolation as t_mc (mc/MarchingCubes.cpp:241-254), float64
 __device__ __forceinline__ void edge_vertex_f64(const Grid& g, int i, int j, int k, int e, const float u[8],
                                                 const TmcVertexOut& out, int32_t idx) {
   const int v0 = edge_v0(e), v1 = edge_v1(e);
-  const double F0 = u[v0], F1 = u[v1];
+  const double F0 = pick8(u, v0), F1 = pick8(u, v1);
   const double l = (g.iso - F0) / (F1 - F0);
   const int i0 = i + (v0 & 1), j0 = j + ((v0 >> 1) & 1), k0 = k + ((v0 >> 2) & 1);
   const int i1 = i + (v1 & 1), j1 = j + ((v1 >> 1) & 1), k1 = k + ((v1 >> 2) & 1);
@@ -659,7 +667,7 @@ __device__ __forceinline__ void edge_vertex_f32(const Grid& g, int i, int j, int
                                                 const TmcVertexOut& out, int32_t idx, const float inv[3],
                                                 const float inv2[3]) {
   const int v0 = edge_v0(e), v1 = edge_v1(e), ax = edge_axis(e);
-  const float F0 = u[v0], F1 = u[v1];
+  const float F0 = pick8(u, v0), F1 = pick8(u, v1);
   const float l = ((float)g.iso - F0) / (F1 - F0);
   const int i0 = i + (v0 & 1), j0 = j + ((v0 >> 1) & 1), k0 = k + ((v0 >> 2) & 1);
   const int i1 = i + (v1 & 1), j1 = j + ((v1 >> 1) & 1), k1 = k + ((v1 >> 2) & 1);
@@ -689,12 +697,13 @@ __device__ __forceinline__ void edge_vertex_f32(const Grid& g, int i, int j, int
 __device__ __forceinline__ void tmc_vertex_ids(const Grid& g, int i, int j, int k, uint32_t em, uint32_t own,
                                                int32_t vbase, int32_t vfirst, const uint32_t* rec,
                                                const int32_t* voff, int32_t vid[12]) {
-  int rank = 0;
-  for (int e = 0; e < 12; e++) {
-    vid[e] = -1;
-    if (!(em & (1u << e))) continue;
+#pragma unroll
+  for (int e = 0; e < 12; e++) vid[e] = -1;
+  // crossed edges as a mask, lowest first: the lanes of a warp resolve their k-th edges together
+  for (uint32_t m = em; m; m &= m - 1) {
+    const int e = __ffs(m) - 1;
     if (own & (1u << e)) {
-      vid[e] = vbase - vfirst + rank++;
+      vid[e] = vbase - vfirst + __popc(own & em & ((1u << e) - 1u));
     } else {
       int oi, oj, ok, oe = 0;
       edge_owner(i, j, k, e, oi, oj, ok, oe);
@@ -801,14 +810,13 @@ __global__ void __launch_bounds__(256, 4) tmc_emit_kernel(CellSpace space, const
       const uint32_t em = case_edge_mask(cs);
       const uint32_t own = trec_owned(r);
       const int32_t vbase = voff[vcell];
-      // owned edge vertices, in edge order
+      // owned edge vertices, in edge order; the crossed owned edges as a mask, lowest first, so
+      // that the lanes of a warp emit their k-th vertices together
       int rank = 0;
-      for (int e = 0; e < 12; e++) {
-        if ((em & own) & (1u << e)) {
-          if (out.v64 && (g.flags & kGridPos64)) edge_vertex_f64(g, i, j, k, e, u, out, vbase + rank);
-          else edge_vertex_f32(g, i, j, k, e, u, out, vbase + rank, inv, inv2);
-          rank++;
-        }
+      for (uint32_t mo = em & own; mo; mo &= mo - 1, rank++) {
+        const int e = __ffs(mo) - 1;
+        if (out.v64 && (g.flags & kGridPos64)) edge_vertex_f64(g, i, j, k, e, u, out, vbase + rank);
+        else edge_vertex_f32(g, i, j, k, e, u, out, vbase + rank, inv, inv2);
       }
       if ((r >> 21) & 1) {
         // ambiguous: triangles and inner vertices in a separate float64 pass
