@@ -27,6 +27,7 @@ struct Grid {
   int flags;          // kGridFlip | kGridNormal64 | kGridPos64
   int64_t vbase;      // index of cell 0 in the launch's cell space (0 for a single volume)
   double inv2[3];     // 1 / (2 * spacing), for the central-difference gradients
+  float inv2f[3];     // the same rounded to float
   __host__ __device__ int cx() const { return nx - 1; }
   __host__ __device__ int cy() const { return ny - 1; }
   __host__ __device__ int cz() const { return nz - 1; }

@@ -551,7 +551,7 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_warp_kernel(CellSpa
 
 // Two-pass vertices, pass 1: contour, plane, sample coordinates, mean point -> one record per
 // vertex.  Contours with neighbour-contour exclusion go to the one-pass kernel's list.
-__global__ void __launch_bounds__(kVertexThreads) dmc_vertex_setup_kernel(CellSpace space, const int32_t* voff,
+__global__ void __launch_bounds__(kVertexThreads, 5) dmc_vertex_setup_kernel(CellSpace space, const int32_t* voff,
                                                                            const uint32_t* vwork, int64_t nv,
                                                                            repr::ProjRecord* recs, uint32_t* list,
                                                                            unsigned* count,

@@ -746,98 +746,97 @@ __global__ void __launch_bounds__(128) tmc_ambiguous_kernel(CellSpace space, con
   }
 }
 
-__global__ void __launch_bounds__(256, 4) tmc_emit_kernel(CellSpace space, const uint32_t* rec, const int32_t* voff,
-                                                       const int32_t* toff, const unsigned long long* tile_off,
-                                                       TmcVertexOut out, int32_t* tris, uint32_t* amb_list,
-                                                       unsigned* amb_count) {
-  // One block per scan tile: the tile's active cells are compacted into shared memory with warp
-  // ballots, then processed one per thread.
-  __shared__ uint32_t active[kScanTile];
-  __shared__ int wcount[kScanThreads / 32];
-  __shared__ int total;
-  const int64_t n = space.n;
+// One active cell: its owned edge vertices and (unambiguous case) its table triangles; ambiguous
+// cells go to the list of the float64 pass.
+__device__ __forceinline__ void emit_cell(const Grid& g, int32_t vfirst, int64_t vcell, const uint32_t* rec,
+                                          const int32_t* voff, const int32_t* toff, const TmcVertexOut& out,
+                                          int32_t* tris, uint32_t* amb_list, unsigned* amb_count) {
+  const int64_t cell = vcell - g.vbase;
+  const uint32_t r = rec[vcell];
+  int i, j, k;
+  tcell_ijk(g, cell, i, j, k);
+  float u[8];
+  tload_corners(g, i, j, k, u);
+  unsigned cs = 0;
+#pragma unroll
+  for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
+  const uint32_t em = case_edge_mask(cs);
+  const uint32_t own = trec_owned(r);
+  const int32_t vbase = voff[vcell];
+  // owned edge vertices, in edge order (the crossed owned edges as a mask, lowest first)
+  int rank = 0;
+  for (uint32_t mo = em & own; mo; mo &= mo - 1, rank++) {
+    const int e = __ffs(mo) - 1;
+    if (out.v64 && (g.flags & kGridPos64)) edge_vertex_f64(g, i, j, k, e, u, out, vbase + rank);
+    else {
+      const float inv2[3] = {g.inv2f[0], g.inv2f[1], g.inv2f[2]};
+      const float inv[3] = {2 * inv2[0], 2 * inv2[1], 2 * inv2[2]};  // = fl(1/spacing): doubling is exact
+      edge_vertex_f32(g, i, j, k, e, u, out, vbase + rank, inv, inv2);
+    }
+  }
+  if ((r >> 21) & 1) {
+    // ambiguous: triangles and inner vertices in a separate float64 pass
+    if (!((r >> 22) & 1)) amb_list[atomicAdd(amb_count, 1u)] = (uint32_t)vcell;
+    return;
+  }
+  int32_t vid[12];
+  tmc_vertex_ids(g, i, j, k, em, own, vbase, vfirst, rec, voff, vid);
+  TriSink ts{tris + 3 * (int64_t)toff[vcell], 0};
+  // unambiguous: table triangles with reversed winding (t_mc, mc/MarchingCubes.cpp:276-294)
+  const uint64_t tw = c_tmc_tris[cs];
+  const int nt = (int)(tw & 0xF);
+  for (int t = 0; t < nt; t++) {
+    const int e0 = (int)((tw >> (4 + 12 * t)) & 0xF), e1 = (int)((tw >> (8 + 12 * t)) & 0xF),
+              e2 = (int)((tw >> (12 + 12 * t)) & 0xF);
+    ts.put(vid[e2], vid[e1], vid[e0]);
+  }
+}
+
+// Each warp walks chunks of 32 consecutive cells, appends the active ones to its own queue in
+// shared memory (ballot + popcount), and processes the queue 32 cells at a time, one per lane: all
+// lanes busy, and no block barrier (warps never wait for one another).
+constexpr int kEmitThreads = 256;
+template <bool kBatch>
+__global__ void __launch_bounds__(kEmitThreads, 4) tmc_emit_kernel(CellSpace space, const uint32_t* rec,
+                                                                   const int32_t* voff, const int32_t* toff,
+                                                                   const unsigned long long* tile_off,
+                                                                   TmcVertexOut out, int32_t* tris,
+                                                                   uint32_t* amb_list, unsigned* amb_count) {
+  constexpr int kWarps = kEmitThreads / 32;
+  __shared__ uint32_t queue[kWarps][64];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int64_t tile = blockIdx.x; tile * kScanTile < n; tile += gridDim.x) {
-    const int64_t base = tile * kScanTile;
-    const Grid g = space.grid_of_tile(tile);
-    const int32_t vfirst = (int32_t)(tile_off[g.vbase / kScanTile] >> 32);
-    const float inv[3] = {(float)(2 * g.inv2[0]), (float)(2 * g.inv2[1]), (float)(2 * g.inv2[2])};
-    const float inv2[3] = {(float)g.inv2[0], (float)g.inv2[1], (float)g.inv2[2]};
-    // compaction: thread t looks at cells base + s*256 + t
-    int mine = 0;
-    bool act[kScanItems];
-#pragma unroll
-    for (int s = 0; s < kScanItems; s++) {
-      const int64_t c = base + (int64_t)s * kScanThreads + threadIdx.x;
-      act[s] = (c < n) && rec[c] != 0;
-      mine += act[s];
+  uint32_t* Q = queue[wid];
+  const int64_t n = space.n;
+  const int64_t chunks = ceil_div(n, 32);
+  int qn = 0;  // queued cells (the same on every lane)
+  for (int64_t chunk = (int64_t)blockIdx.x * kWarps + wid;; chunk += (int64_t)gridDim.x * kWarps) {
+    const bool more = chunk < chunks;
+    if (more) {
+      const int64_t c = chunk * 32 + lane;
+      const bool act = c < n && rec[c] != 0;
+      const unsigned bal = __ballot_sync(0xffffffffu, act);
+      if (act) Q[qn + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)c;
+      qn += __popc(bal);
+      __syncwarp();
     }
-    int pre = mine;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, pre, o);
-      if (lane >= o) pre += y;
+    while (qn >= 32 || (!more && qn > 0)) {
+      const int take = qn < 32 ? qn : 32;
+      if (lane < take) {
+        const int64_t vcell = Q[lane];
+        // the cell's volume: read in place (a batch's grid table, or the launch parameter)
+        const Grid& g = kBatch ? space.grids[__ldg(space.tile_vol + vcell / kScanTile)] : space.one;
+        const int32_t vfirst = kBatch ? (int32_t)(tile_off[g.vbase / kScanTile] >> 32) : 0;
+        emit_cell(g, vfirst, vcell, rec, voff, toff, out, tris, amb_list, amb_count);
+      }
+      __syncwarp();
+      const int rest = qn - take;  // at most 31: move them to the front
+      const uint32_t x = lane < rest ? Q[take + lane] : 0u;
+      __syncwarp();
+      if (lane < rest) Q[lane] = x;
+      __syncwarp();
+      qn = rest;
     }
-    if (lane == 31) wcount[wid] = pre;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int s = 0;
-      for (int w = 0; w < kScanThreads / 32; w++) {
-        const int x = wcount[w];
-        wcount[w] = s;
-        s += x;
-      }
-      total = s;
-    }
-    __syncthreads();
-    int pos = wcount[wid] + pre - mine;
-#pragma unroll
-    for (int s = 0; s < kScanItems; s++)
-      if (act[s]) active[pos++] = (uint32_t)(s * kScanThreads + threadIdx.x);
-    __syncthreads();
-    const int na = total;
-    for (int a = threadIdx.x; a < na; a += blockDim.x) {
-      const int64_t vcell = base + active[a];
-      const int64_t cell = vcell - g.vbase;
-      const uint32_t r = rec[vcell];
-      int i, j, k;
-      tcell_ijk(g, cell, i, j, k);
-      float u[8];
-      tload_corners(g, i, j, k, u);
-      unsigned cs = 0;
-#pragma unroll
-      for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
-      const uint32_t em = case_edge_mask(cs);
-      const uint32_t own = trec_owned(r);
-      const int32_t vbase = voff[vcell];
-      // owned edge vertices, in edge order; the crossed owned edges as a mask, lowest first, so
-      // that the lanes of a warp emit their k-th vertices together
-      int rank = 0;
-      for (uint32_t mo = em & own; mo; mo &= mo - 1, rank++) {
-        const int e = __ffs(mo) - 1;
-        if (out.v64 && (g.flags & kGridPos64)) edge_vertex_f64(g, i, j, k, e, u, out, vbase + rank);
-        else edge_vertex_f32(g, i, j, k, e, u, out, vbase + rank, inv, inv2);
-      }
-      if ((r >> 21) & 1) {
-        // ambiguous: triangles and inner vertices in a separate float64 pass
-        if (!((r >> 22) & 1)) amb_list[atomicAdd(amb_count, 1u)] = (uint32_t)vcell;
-        continue;
-      }
-      int32_t vid[12];
-      tmc_vertex_ids(g, i, j, k, em, own, vbase, vfirst, rec, voff, vid);
-      TriSink ts{tris + 3 * (int64_t)toff[vcell], 0};
-      {
-        // unambiguous: table triangles with reversed winding (t_mc, mc/MarchingCubes.cpp:276-294)
-        const uint64_t tw = c_tmc_tris[cs];
-        const int nt = (int)(tw & 0xF);
-        for (int t = 0; t < nt; t++) {
-          const int e0 = (int)((tw >> (4 + 12 * t)) & 0xF), e1 = (int)((tw >> (8 + 12 * t)) & 0xF),
-                    e2 = (int)((tw >> (12 + 12 * t)) & 0xF);
-          ts.put(vid[e2], vid[e1], vid[e0]);
-        }
-      }
-    }
-    __syncthreads();
+    if (!more) break;
   }
 }
 
@@ -873,9 +872,14 @@ int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tr
   const int sms = tu.sms;
   Stage t(prof, "tmc_emit", st);
   const int64_t tiles = tmc_tiles(space);
-  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sms * tu.emit_blocks_per_sm));
+  const int64_t blocks = std::max<int64_t>(
+      1, std::min<int64_t>(ceil_div(space.n, 32 * (kEmitThreads / 32)), (int64_t)sms * tu.emit_blocks_per_sm));
   cudaMemsetAsync(s.amb_count, 0, sizeof(unsigned), st);
-  tmc_emit_kernel<<<(unsigned)blocks, kScanThreads, 0, st>>>(space, s.rec, s.voff, s.toff, s.tile_sums, vo, tris,
+  if (space.grids)
+    tmc_emit_kernel<true><<<(unsigned)blocks, kEmitThreads, 0, st>>>(space, s.rec, s.voff, s.toff, s.tile_sums, vo, tris,
+                                                            s.amb_list, s.amb_count);
+  else
+    tmc_emit_kernel<false><<<(unsigned)blocks, kEmitThreads, 0, st>>>(space, s.rec, s.voff, s.toff, s.tile_sums, vo, tris,
                                                             s.amb_list, s.amb_count);
   Stage t2(prof, "tmc_ambiguous", st);
   tmc_ambiguous_kernel<<<(unsigned)std::max<int64_t>(1, (int64_t)sms * 8), 128, 0, st>>>(
