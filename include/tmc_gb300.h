@@ -12,6 +12,10 @@
  *   tmc_server_*           (no reference counterpart: request loop around the calls above)
  *   tmc_dmc_count_static   (no reference counterpart: DMC mesh sizes without allocating)
  *   tmc_ctx_*_tuning, tmc_ctx_autotune  (no reference counterpart: launch shapes and their tuner)
+ *   tmc_field_load         dmc::UniformGrid::init(file)              cpp_dmc/UniformGrid.cpp:3-45
+ *                          readFromFile<T> / readDataFromFile<T>     cpp_dmc/Volumes.h:47, dmc/UniformGrid.h:431
+ *                          p_mc::MarchingCubes::readDataFromFile    cuda_tmc/MarchingCubes.cu:3363
+ *   tmc_mesh_write_obj/off the OBJ / OFF writers                     cpp_dmc/main.cpp:33-87, mc/MarchingCubes.cpp:98-141
  *
  * Threading: a context is thread-compatible, not thread-safe; use one context per host thread.
  * All work of a context runs on its own CUDA stream.
@@ -141,6 +145,37 @@ tmc_status tmc_mesh_free(tmc_ctx* ctx, tmc_mesh* mesh);
  * and must be serialised; the first call on a device does a one-time set-up
  * (cudaGetSymbolAddress) and should precede any stream capture on that device. */
 tmc_status tmc_dmc_count_static(tmc_ctx* ctx, const tmc_volume* vol, double iso, int64_t counts[4]);
+
+/* volume files and mesh files --------------------------------------------------------------- */
+/* The reference's volume file layouts (origin 0; the data x fastest):
+ *   TMC_FILE_DMC      int32 nx,ny,nz; float64 dx,dy,dz; float32 data   cpp_dmc/UniformGrid.cpp:3-45
+ *   TMC_FILE_INT_F32  int32 nx,ny,nz; float32 dx,dy,dz; float32 data   cpp_dmc/Volumes.h:47-105,
+ *                                                                      dmc/UniformGrid.h:431-468
+ *   TMC_FILE_INT_U16  int32 nx,ny,nz; float32 dx,dy,dz; uint16 data    (their ushort instances)
+ *   TMC_FILE_U16      uint16 nx,ny,nz; float32 dx,dy,dz; uint16 data   mc/MarchingCubes.cpp:22-66,
+ *                                                                      cuda_tmc/MarchingCubes.cu:3363-3407 */
+enum { TMC_FILE_DMC = 0, TMC_FILE_INT_F32 = 1, TMC_FILE_INT_U16 = 2, TMC_FILE_U16 = 3 };
+/* A field loaded into device memory; `vol` describes it (on_device = 1) until tmc_field_free. */
+typedef struct tmc_field {
+  tmc_volume vol;
+  void* priv;
+} tmc_field;
+/* Header of a volume file: dimensions, spacing (float64) and the offset of the first data byte.
+ * Checks that the file holds all the data it announces.  Needs no context and no GPU. */
+tmc_status tmc_volume_file_info(const char* path, int32_t format, int32_t dims[3], double spacing[3],
+                                int64_t* data_offset);
+/* Reads a volume file into device memory as float32 (uint16 data is copied as it is and widened on
+ * the GPU).  Replaces the reference's readers, which exit the process on a bad file. */
+tmc_status tmc_field_load(tmc_ctx* ctx, const char* path, int32_t format, tmc_field* out);
+tmc_status tmc_field_free(tmc_ctx* ctx, tmc_field* field);
+/* OBJ output in the reference's layouts: TMC_OBJ_DMC_TRIS / TMC_OBJ_DMC_QUADS as cpp_dmc/main.cpp:33-87
+ * (the triangle or the quad file), TMC_OBJ_TMC as mc/MarchingCubes.cpp:98-118 (including its use of
+ * the second vertex's index as the third normal index).  OFF output as mc/MarchingCubes.cpp:123-141
+ * (a mesh with quads and no triangles writes 4-vertex faces).  Positions are written from the
+ * float64 array when the mesh has one.  ctx may be NULL for a mesh in host memory. */
+enum { TMC_OBJ_DMC_TRIS = 0, TMC_OBJ_DMC_QUADS = 1, TMC_OBJ_TMC = 2 };
+tmc_status tmc_mesh_write_obj(tmc_ctx* ctx, const tmc_mesh* mesh, const char* path, int32_t style);
+tmc_status tmc_mesh_write_off(tmc_ctx* ctx, const tmc_mesh* mesh, const char* path);
 
 /* batched extraction ------------------------------------------------------------------------ */
 enum { TMC_ALGO_DMC = 0, TMC_ALGO_TMC = 1 };

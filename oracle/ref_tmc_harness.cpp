@@ -82,4 +82,12 @@ void ref_tmc_copy(void* h, double* v, double* n, int* tris) {
 
 void ref_tmc_free(void* h) { delete (TmcResult*)h; }
 
+// The reference's own file path: MarchingCubes::operator() reads a ushort volume file
+// (mc/MarchingCubes.cpp:12-78) and writes its OBJ and OFF files (:98-141).
+void ref_tmc_files(double iso, const char* volume, const char* obj, const char* off) {
+  QuietStdout q;
+  tmc::MarchingCubes mc;
+  mc(iso, std::string(volume), false, true, std::string(obj), true, std::string(off));
+}
+
 }  // extern "C"

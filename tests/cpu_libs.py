@@ -103,6 +103,10 @@ class OracleLib(_Lib):
         self.lib.oracle_tmc_free(h)
         return out
 
+    def tmc_files(self, iso, volume, obj, off):
+        """The reference's MarchingCubes::operator(): ushort volume file in, OBJ and OFF files out."""
+        self.lib.ref_tmc_files(ctypes.c_double(iso), volume.encode(), obj.encode(), off.encode())
+
     def color_valence(self, nv, quads, colors):
         q = np.ascontiguousarray(quads, dtype=np.int32)
         col = np.ascontiguousarray(colors, dtype=np.int32).copy()
@@ -144,6 +148,10 @@ class RefLib(_Lib):
         h, out = self._tmc_fetch(self.lib.ref_tmc_run(*a))
         self.lib.ref_tmc_free(h)
         return out
+
+    def tmc_files(self, iso, volume, obj, off):
+        """The reference's MarchingCubes::operator(): ushort volume file in, OBJ and OFF files out."""
+        self.lib.ref_tmc_files(ctypes.c_double(iso), volume.encode(), obj.encode(), off.encode())
 
     def color_valence(self, nv, quads, colors):
         q = np.ascontiguousarray(quads, dtype=np.int32)

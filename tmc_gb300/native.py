@@ -39,7 +39,16 @@ EXPORTS = ["tmc_ctx_create", "tmc_ctx_destroy", "tmc_last_error", "tmc_ctx_strea
            "tmc_ctx_launch_count", "tmc_ctx_set_profiling", "tmc_ctx_profile_read", "tmc_dmc_extract", "tmc_tmc_sharedvertex", "tmc_tmc_halfedge",
            "tmc_mesh_free", "tmc_batch_extract", "tmc_dmc_count_static", "tmc_server_create", "tmc_server_destroy",
            "tmc_server_submit", "tmc_server_poll", "tmc_server_wait", "tmc_server_release", "tmc_server_last_error",
-           "tmc_server_stats", "tmc_ctx_set_tuning", "tmc_ctx_get_tuning", "tmc_ctx_autotune"]
+           "tmc_server_stats", "tmc_ctx_set_tuning", "tmc_ctx_get_tuning", "tmc_ctx_autotune",
+           "tmc_volume_file_info", "tmc_field_load", "tmc_field_free", "tmc_mesh_write_obj", "tmc_mesh_write_off"]
+
+FILE_DMC = 0
+FILE_INT_F32 = 1
+FILE_INT_U16 = 2
+FILE_U16 = 3
+OBJ_DMC_TRIS = 0
+OBJ_DMC_QUADS = 1
+OBJ_TMC = 2
 
 TUNE_GROUP_LANES = 1
 TUNE_WARP_LIST_MAX = 2
@@ -70,6 +79,10 @@ class Mesh(ctypes.Structure):
                 ("quads", ctypes.c_void_p), ("tris", ctypes.c_void_p), ("he", ctypes.c_void_p),
                 ("he_v", ctypes.c_void_p), ("he_f", ctypes.c_void_p), ("vcell", ctypes.c_void_p),
                 ("vuvw", ctypes.c_void_p), ("stats", ctypes.c_int64 * 8), ("priv", ctypes.c_void_p)]
+
+
+class Field(ctypes.Structure):
+    _fields_ = [("vol", Volume), ("priv", ctypes.c_void_p)]
 
 
 class Request(ctypes.Structure):
@@ -120,6 +133,12 @@ def load(path: str = LIB_PATH):
     lib.tmc_server_last_error.argtypes = [ctypes.c_void_p]
     lib.tmc_server_last_error.restype = ctypes.c_char_p
     lib.tmc_server_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]
+    lib.tmc_volume_file_info.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]
+    lib.tmc_field_load.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(Field)]
+    lib.tmc_field_free.argtypes = [ctypes.c_void_p, ctypes.POINTER(Field)]
+    lib.tmc_mesh_write_obj.argtypes = [ctypes.c_void_p, ctypes.POINTER(Mesh), ctypes.c_char_p, ctypes.c_int32]
+    lib.tmc_mesh_write_off.argtypes = [ctypes.c_void_p, ctypes.POINTER(Mesh), ctypes.c_char_p]
     lib.tmc_ctx_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64]
     lib.tmc_ctx_get_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
     lib.tmc_ctx_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(Request), ctypes.c_int32,
@@ -146,6 +165,52 @@ def make_volume(vol, data_ptr: int | None = None, on_device: bool = False) -> Vo
         v.data = data_ptr
         v.on_device = 1 if on_device else 0
     return v
+
+
+def volume_file_info(path: str, fmt: int):
+    """tmc_volume_file_info: (dims, spacing, data offset) of a volume file; needs no GPU."""
+    lib = load()
+    dims = (ctypes.c_int32 * 3)()
+    sp = (ctypes.c_double * 3)()
+    off = ctypes.c_int64()
+    st = lib.tmc_volume_file_info(path.encode(), int(fmt), dims, sp, ctypes.byref(off))
+    if st != TMC_OK:
+        raise TmcError(st, f"{path}: not a valid volume file of format {fmt}")
+    return tuple(dims), tuple(sp), off.value
+
+
+def host_mesh(v, n, quads=None, tris=None, v64=None) -> Mesh:
+    """A tmc_mesh over numpy arrays in host memory (for the writers); keeps the arrays alive."""
+    m = Mesh()
+    keep = []
+
+    def ptr(a, dtype):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=dtype)
+        keep.append(a)
+        return a.ctypes.data
+
+    m.nr_v = len(v) // 3
+    m.nr_q = 0 if quads is None else len(quads) // 4
+    m.nr_t = 0 if tris is None else len(tris) // 3
+    m.on_device = 0
+    m.v, m.n, m.v64 = ptr(v, np.float32), ptr(n, np.float32), ptr(v64, np.float64)
+    m.quads, m.tris = ptr(quads, np.int32), ptr(tris, np.int32)
+    m._keep = keep
+    return m
+
+
+def write_obj(mesh: Mesh, path: str, style: int, ctx=None):
+    st = load().tmc_mesh_write_obj(ctx.h if ctx else None, ctypes.byref(mesh), path.encode(), int(style))
+    if st != TMC_OK:
+        raise TmcError(st, ctx.lib.tmc_last_error(ctx.h).decode() if ctx else f"writing {path} failed")
+
+
+def write_off(mesh: Mesh, path: str, ctx=None):
+    st = load().tmc_mesh_write_off(ctx.h if ctx else None, ctypes.byref(mesh), path.encode())
+    if st != TMC_OK:
+        raise TmcError(st, ctx.lib.tmc_last_error(ctx.h).decode() if ctx else f"writing {path} failed")
 
 
 def _host_array(ptr, count, dtype):
@@ -242,6 +307,15 @@ class Context:
         outs = (Mesh * n)()
         self._check(self.lib.tmc_batch_extract(self.h, n, reqs, outs))
         return [outs[q] for q in range(n)]
+
+    def field_load(self, path: str, fmt: int) -> Field:
+        """tmc_field_load: a volume file read into device memory (float32)."""
+        f = Field()
+        self._check(self.lib.tmc_field_load(self.h, path.encode(), int(fmt), ctypes.byref(f)))
+        return f
+
+    def field_free(self, f: Field):
+        self._check(self.lib.tmc_field_free(self.h, ctypes.byref(f)))
 
     def set_tuning(self, key: int, value: int):
         self._check(self.lib.tmc_ctx_set_tuning(self.h, key, int(value)))
