@@ -870,17 +870,18 @@ int tmc_count(const CellSpace& space, TmcScratch& s, cudaStream_t st, Prof* prof
 int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tris, const Tuning& tu, cudaStream_t st,
              Prof* prof) {
   const int sms = tu.sms;
-  Stage t(prof, "tmc_emit", st);
-  const int64_t tiles = tmc_tiles(space);
-  const int64_t blocks = std::max<int64_t>(
-      1, std::min<int64_t>(ceil_div(space.n, 32 * (kEmitThreads / 32)), (int64_t)sms * tu.emit_blocks_per_sm));
-  cudaMemsetAsync(s.amb_count, 0, sizeof(unsigned), st);
-  if (space.grids)
-    tmc_emit_kernel<true><<<(unsigned)blocks, kEmitThreads, 0, st>>>(space, s.rec, s.voff, s.toff, s.tile_sums, vo, tris,
-                                                            s.amb_list, s.amb_count);
-  else
-    tmc_emit_kernel<false><<<(unsigned)blocks, kEmitThreads, 0, st>>>(space, s.rec, s.voff, s.toff, s.tile_sums, vo, tris,
-                                                            s.amb_list, s.amb_count);
+  {
+    Stage t(prof, "tmc_emit", st);
+    const int64_t blocks = std::max<int64_t>(
+        1, std::min<int64_t>(ceil_div(space.n, 32 * (kEmitThreads / 32)), (int64_t)sms * tu.emit_blocks_per_sm));
+    cudaMemsetAsync(s.amb_count, 0, sizeof(unsigned), st);
+    if (space.grids)
+      tmc_emit_kernel<true><<<(unsigned)blocks, kEmitThreads, 0, st>>>(space, s.rec, s.voff, s.toff, s.tile_sums, vo,
+                                                                       tris, s.amb_list, s.amb_count);
+    else
+      tmc_emit_kernel<false><<<(unsigned)blocks, kEmitThreads, 0, st>>>(space, s.rec, s.voff, s.toff, s.tile_sums, vo,
+                                                                        tris, s.amb_list, s.amb_count);
+  }
   Stage t2(prof, "tmc_ambiguous", st);
   tmc_ambiguous_kernel<<<(unsigned)std::max<int64_t>(1, (int64_t)sms * 8), 128, 0, st>>>(
       space, s.rec, s.voff, s.toff, s.tile_sums, vo, tris, s.amb_list, s.amb_count);
