@@ -16,6 +16,8 @@
  *                          readFromFile<T> / readDataFromFile<T>     cpp_dmc/Volumes.h:47, dmc/UniformGrid.h:431
  *                          p_mc::MarchingCubes::readDataFromFile    cuda_tmc/MarchingCubes.cu:3363
  *   tmc_mesh_write_obj/off the OBJ / OFF writers                     cpp_dmc/main.cpp:33-87, mc/MarchingCubes.cpp:98-141
+ *   tmc_mesh_quality       p_mc::EstimateElementQuality::q           dmc/EstimateElementQuality.cu:39-56
+ *   tmc_mesh_valence       p_mc::VertexValence::vertexValence        dmc/VertexValence.cu:79-170
  *
  * Threading: a context is thread-compatible, not thread-safe; use one context per host thread.
  * All work of a context runs on its own CUDA stream.
@@ -176,6 +178,19 @@ tmc_status tmc_field_free(tmc_ctx* ctx, tmc_field* field);
 enum { TMC_OBJ_DMC_TRIS = 0, TMC_OBJ_DMC_QUADS = 1, TMC_OBJ_TMC = 2 };
 tmc_status tmc_mesh_write_obj(tmc_ctx* ctx, const tmc_mesh* mesh, const char* path, int32_t style);
 tmc_status tmc_mesh_write_off(tmc_ctx* ctx, const tmc_mesh* mesh, const char* path);
+
+/* mesh validation metrics (the reference's validation kernels, not part of its extraction path) -- */
+enum { TMC_FACES_QUADS = 0, TMC_FACES_TRIS = 1 };
+/* Element quality as p_mc::EstimateElementQuality (dmc/EstimateElementQuality.cu:1-56,
+ * dmc/ElementQuality.h:69-93): per quad the smallest 2|e1 x e2| / (|e1|^2 + |e2|^2) over its corners,
+ * per triangle the mean ratio 2 sqrt(3)|e1 x e2| / (l0 + l1 + l2) (0 with a zero-length edge), float32.
+ * quality (host, one per face) and summary (host: min, max, mean) may each be NULL.  The mesh may be
+ * in host or device memory. */
+tmc_status tmc_mesh_quality(tmc_ctx* ctx, const tmc_mesh* mesh, int32_t faces, float* quality, double summary[3]);
+/* Valence distribution as p_mc::VertexValence::vertexValence (dmc/VertexValence.cu:79-170):
+ * hist[k] = number of vertices with k distinct incident edges (k = 99 also counts higher valences);
+ * *len = the last non-empty bin + 1, as the reference trims its vector. */
+tmc_status tmc_mesh_valence(tmc_ctx* ctx, const tmc_mesh* mesh, int32_t faces, uint32_t hist[100], int32_t* len);
 
 /* batched extraction ------------------------------------------------------------------------ */
 enum { TMC_ALGO_DMC = 0, TMC_ALGO_TMC = 1 };

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libtmc_gb300.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["runtime.cu", "dmc_front.cu", "dmc_mesh.cu", "tmc_cells.cu", "halfedges.cu", "scan.cu", "count_static.cu", "server.cu", "volume_io.cu"]
+SOURCES = ["runtime.cu", "dmc_front.cu", "dmc_mesh.cu", "tmc_cells.cu", "halfedges.cu", "scan.cu", "count_static.cu", "server.cu", "volume_io.cu", "mesh_stats.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-diag-suppress", "177"]

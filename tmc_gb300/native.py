@@ -40,7 +40,11 @@ EXPORTS = ["tmc_ctx_create", "tmc_ctx_destroy", "tmc_last_error", "tmc_ctx_strea
            "tmc_mesh_free", "tmc_batch_extract", "tmc_dmc_count_static", "tmc_server_create", "tmc_server_destroy",
            "tmc_server_submit", "tmc_server_poll", "tmc_server_wait", "tmc_server_release", "tmc_server_last_error",
            "tmc_server_stats", "tmc_ctx_set_tuning", "tmc_ctx_get_tuning", "tmc_ctx_autotune",
-           "tmc_volume_file_info", "tmc_field_load", "tmc_field_free", "tmc_mesh_write_obj", "tmc_mesh_write_off"]
+           "tmc_volume_file_info", "tmc_field_load", "tmc_field_free", "tmc_mesh_write_obj", "tmc_mesh_write_off",
+           "tmc_mesh_quality", "tmc_mesh_valence"]
+
+FACES_QUADS = 0
+FACES_TRIS = 1
 
 FILE_DMC = 0
 FILE_INT_F32 = 1
@@ -139,6 +143,10 @@ def load(path: str = LIB_PATH):
     lib.tmc_field_free.argtypes = [ctypes.c_void_p, ctypes.POINTER(Field)]
     lib.tmc_mesh_write_obj.argtypes = [ctypes.c_void_p, ctypes.POINTER(Mesh), ctypes.c_char_p, ctypes.c_int32]
     lib.tmc_mesh_write_off.argtypes = [ctypes.c_void_p, ctypes.POINTER(Mesh), ctypes.c_char_p]
+    lib.tmc_mesh_quality.argtypes = [ctypes.c_void_p, ctypes.POINTER(Mesh), ctypes.c_int32,
+                                     ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_double)]
+    lib.tmc_mesh_valence.argtypes = [ctypes.c_void_p, ctypes.POINTER(Mesh), ctypes.c_int32,
+                                     ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int32)]
     lib.tmc_ctx_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64]
     lib.tmc_ctx_get_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
     lib.tmc_ctx_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(Request), ctypes.c_int32,
@@ -307,6 +315,22 @@ class Context:
         outs = (Mesh * n)()
         self._check(self.lib.tmc_batch_extract(self.h, n, reqs, outs))
         return [outs[q] for q in range(n)]
+
+    def quality(self, m: Mesh, faces: int):
+        """tmc_mesh_quality: (per-face quality, (min, max, mean))."""
+        nf = m.nr_q if faces == FACES_QUADS else m.nr_t
+        q = np.zeros(max(nf, 1), np.float32)
+        summ = (ctypes.c_double * 3)()
+        self._check(self.lib.tmc_mesh_quality(self.h, ctypes.byref(m), int(faces),
+                                              q.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), summ))
+        return q[:nf], tuple(summ)
+
+    def valence(self, m: Mesh, faces: int) -> np.ndarray:
+        """tmc_mesh_valence: the valence distribution, trimmed after its last non-empty bin."""
+        h = (ctypes.c_uint32 * 100)()
+        n = ctypes.c_int32()
+        self._check(self.lib.tmc_mesh_valence(self.h, ctypes.byref(m), int(faces), h, ctypes.byref(n)))
+        return np.array(list(h)[:n.value], np.int64)
 
     def field_load(self, path: str, fmt: int) -> Field:
         """tmc_field_load: a volume file read into device memory (float32)."""
