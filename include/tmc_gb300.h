@@ -18,6 +18,7 @@
  *   tmc_mesh_write_obj/off the OBJ / OFF writers                     cpp_dmc/main.cpp:33-87, mc/MarchingCubes.cpp:98-141
  *   tmc_mesh_quality       p_mc::EstimateElementQuality::q           dmc/EstimateElementQuality.cu:39-56
  *   tmc_mesh_valence       p_mc::VertexValence::vertexValence        dmc/VertexValence.cu:79-170
+ *   tmc_mesh_check         tmc::MarchingCubes::connectivity (counts) mc/MarchingCubes.cpp:1769-2226
  *
  * Threading: a context is thread-compatible, not thread-safe; use one context per host thread.
  * All work of a context runs on its own CUDA stream.
@@ -191,6 +192,13 @@ tmc_status tmc_mesh_quality(tmc_ctx* ctx, const tmc_mesh* mesh, int32_t faces, f
  * hist[k] = number of vertices with k distinct incident edges (k = 99 also counts higher valences);
  * *len = the last non-empty bin + 1, as the reference trims its vector. */
 tmc_status tmc_mesh_valence(tmc_ctx* ctx, const tmc_mesh* mesh, int32_t faces, uint32_t hist[100], int32_t* len);
+/* Mesh check, the counts of tmc::MarchingCubes::connectivity (mc/MarchingCubes.cpp:1769-2226), which
+ * repairs orientation in a sequential walk; here a parallel validator that changes nothing:
+ * report[0] connected components (faces joined across shared edges), [1] orientation defects (edges
+ * whose two faces run them in the same direction; 0 on a consistently oriented mesh, where the
+ * reference flips nothing), [2] boundary edges, [3] halfedges on non-manifold edges,
+ * [4] degenerate faces (a repeated vertex), [5] boundary vertices. */
+tmc_status tmc_mesh_check(tmc_ctx* ctx, const tmc_mesh* mesh, int32_t faces, int64_t report[6]);
 
 /* batched extraction ------------------------------------------------------------------------ */
 enum { TMC_ALGO_DMC = 0, TMC_ALGO_TMC = 1 };

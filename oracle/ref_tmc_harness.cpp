@@ -7,6 +7,8 @@
 // UGrid::gradient() (one-sided differences at the border, :1451), then t_mc(i0) (:151).
 // The input here is an in-memory float32 field instead of a ushort file.
 #include <algorithm>
+#include <cstdlib>
+#include <string>
 #include <array>
 #include <bitset>
 #include <cstdint>
@@ -81,6 +83,48 @@ void ref_tmc_copy(void* h, double* v, double* n, int* tris) {
 }
 
 void ref_tmc_free(void* h) { delete (TmcResult*)h; }
+
+// The reference's connectivity() (mc/MarchingCubes.cpp:1769-2226) on the t_mc mesh of a field: it
+// reports the components it found and the orientations it changed on stdout; out2 gets both.
+void ref_tmc_connectivity(int nx, int ny, int nz, const double* origin, const double* spacing, const float* field,
+                          double iso, int64_t* out2) {
+  out2[0] = out2[1] = -1;
+  std::string text;
+  // the set-up of ref_tmc_run, keeping the MarchingCubes object for connectivity()
+  QuietStdout q;
+  tmc::MarchingCubes mc;
+  std::array<tmc::MarchingCubes::Point, 8> bb;
+  const double xs[2] = {origin[0], origin[0] + spacing[0] * (nx - 1.)};
+  const double ys[2] = {origin[1], origin[1] + spacing[1] * (ny - 1.)};
+  const double zs[2] = {origin[2], origin[2] + spacing[2] * (nz - 1.)};
+  for (int c = 0; c < 8; c++) bb[c] = tmc::MarchingCubes::Point{{xs[c & 1], ys[(c >> 1) & 1], zs[(c >> 2) & 1]}};
+  mc.m_nx = nx;
+  mc.m_ny = ny;
+  mc.m_nz = nz;
+  mc.m_dx = spacing[0];
+  mc.m_dy = spacing[1];
+  mc.m_dz = spacing[2];
+  mc.m_ugrid.init(nx, ny, nz, bb);
+  mc.m_ugrid.set_dx(spacing[0]);
+  mc.m_ugrid.set_dy(spacing[1]);
+  mc.m_ugrid.set_dz(spacing[2]);
+  const size_t n = (size_t)nx * ny * nz;
+  for (size_t s = 0; s < n; s++) mc.m_ugrid.scalar((int)s, (double)field[s]);
+  mc.m_ugrid.gradient();
+  mc.t_mc(iso);
+  mc.connectivity();
+  text = q.sink.str();
+  const auto grab = [&](const std::string& before, const std::string& after) -> int64_t {
+    const size_t b = text.find(before);
+    if (b == std::string::npos) return -1;
+    const size_t s0 = b + before.size();
+    const size_t e = text.find(after, s0);
+    if (e == std::string::npos) return -1;
+    return std::atoll(text.substr(s0, e - s0).c_str());
+  };
+  out2[0] = grab(" connectivity found ", " components");
+  out2[1] = grab(" connectivity has changed ", " triangle orientations");
+}
 
 // The reference's own file path: MarchingCubes::operator() reads a ushort volume file
 // (mc/MarchingCubes.cpp:12-78) and writes its OBJ and OFF files (:98-141).

@@ -103,6 +103,13 @@ class OracleLib(_Lib):
         self.lib.oracle_tmc_free(h)
         return out
 
+    def tmc_connectivity(self, vol):
+        """The reference's connectivity() on its t_mc mesh: (components, orientation changes)."""
+        d, a = _vol_args(vol)
+        out = (ctypes.c_int64 * 2)()
+        self.lib.ref_tmc_connectivity(*a, out)
+        return int(out[0]), int(out[1])
+
     def tmc_files(self, iso, volume, obj, off):
         """The reference's MarchingCubes::operator(): ushort volume file in, OBJ and OFF files out."""
         self.lib.ref_tmc_files(ctypes.c_double(iso), volume.encode(), obj.encode(), off.encode())
@@ -148,6 +155,13 @@ class RefLib(_Lib):
         h, out = self._tmc_fetch(self.lib.ref_tmc_run(*a))
         self.lib.ref_tmc_free(h)
         return out
+
+    def tmc_connectivity(self, vol):
+        """The reference's connectivity() on its t_mc mesh: (components, orientation changes)."""
+        d, a = _vol_args(vol)
+        out = (ctypes.c_int64 * 2)()
+        self.lib.ref_tmc_connectivity(*a, out)
+        return int(out[0]), int(out[1])
 
     def tmc_files(self, iso, volume, obj, off):
         """The reference's MarchingCubes::operator(): ushort volume file in, OBJ and OFF files out."""

@@ -104,3 +104,44 @@ def test_metrics_of_device_mesh_equal_host_mesh(ctx):
     finally:
         ctx.free(md)
         ctx.free(mh)
+
+
+def _check_cases():
+    import math
+    rng = np.random.Generator(np.random.PCG64(31))
+    sad = V.periodic(21, 21, 21, 6 * math.pi)
+    V.seed_saddles(sad, rng, frac=0.5)
+    return {"noise40": CASES["noise40"], "blobs48": CASES["blobs48"],
+            "saddle21": V.Volume(sad, spacing=(0.1, 0.1, 0.1), iso=0.0)}
+
+
+@pytest.mark.parametrize("name", ["blobs48", "noise40", "saddle21"])
+def test_mesh_check_against_numpy(ctx, name):
+    """tmc_mesh_check equals the numpy check (pinned to the reference's connectivity() in
+    test_mesh_check_cpu.py) on TMC triangle meshes and DMC quad and triangle meshes.  On edges with
+    three or more faces the twins follow the halfedge rules, so components are compared only where
+    every edge has at most two faces."""
+    from mesh_check_np import mesh_check_np
+    vol = _check_cases()[name]
+    tv = native.make_volume(vol)
+    for algo in ("tmc", "dmc"):
+        if algo == "tmc":
+            m = ctx.tmc_raw(tv, vol.iso, native.OUT_HOST)
+            kinds = [(native.FACES_TRIS, 3)]
+        else:
+            m = ctx.dmc_raw(tv, vol.iso, native.OUT_HOST | native.OUT_TRIANGLES)
+            kinds = [(native.FACES_QUADS, 4), (native.FACES_TRIS, 3)]
+        try:
+            for faces, P in kinds:
+                f = native._host_array(m.quads if P == 4 else m.tris, P * (m.nr_q if P == 4 else m.nr_t), np.int32)
+                got = ctx.check(m, faces)
+                want = mesh_check_np(m.nr_v, f, P)
+                keys = list(want)
+                if want["nonmanifold_halfedges"]:
+                    keys = [k for k in keys if k not in ("components", "boundary_edges", "boundary_vertices")]
+                for k in keys:
+                    assert got[k] == want[k], (name, algo, P, k, got, want)
+                if name != "saddle21":
+                    assert got["orientation_defects"] == 0
+        finally:
+            ctx.free(m)

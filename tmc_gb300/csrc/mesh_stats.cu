@@ -20,6 +20,7 @@
 #include "../../include/tmc_gb300.h"
 #include "common.cuh"
 #include "ctx_access.h"
+#include "halfedges.h"
 #include "scan.cuh"
 
 namespace tmc {
@@ -283,3 +284,165 @@ tmc_status tmc_mesh_valence(tmc_ctx* ctx, const tmc_mesh* mesh, int32_t faces, u
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------------------
+// Mesh check: the counts tmc::MarchingCubes::connectivity (mc/MarchingCubes.cpp:1769-2226) reports,
+// computed in parallel.  The reference walks the triangles depth-first from each unvisited one,
+// counts the components it starts and flips every triangle whose orientation disagrees with its
+// visited neighbour; here the components come from a union-find over the halfedge twins and the
+// orientation is checked edge by edge (a twin pair that runs its edge in the same direction is a
+// defect).  On a consistently oriented mesh both report no correction; the component counts agree
+// whenever each edge has at most two faces (the reference links a face only to the first other
+// face it finds on an edge).
+// ------------------------------------------------------------------------------------------------
+namespace tmc {
+namespace {
+
+constexpr int kFindSteps = 1 << 20;  // bound on one find / link loop (never reached: see below)
+
+// root of x with path halving; gives up (returns -1) after kFindSteps steps
+__device__ __forceinline__ int32_t uf_find(int32_t* parent, int32_t x) {
+  for (int s = 0; s < kFindSteps; s++) {
+    const int32_t p = parent[x];
+    if (p == x) return x;
+    const int32_t gp = parent[p];
+    if (gp != p) atomicCAS(parent + x, p, gp);  // halve the path; losing the race is harmless
+    x = gp;
+  }
+  return -1;
+}
+
+// Union by linking the larger root under the smaller one (a root's parent only ever decreases, so
+// every loop makes progress); each step is bounded all the same.
+__device__ __forceinline__ bool uf_union(int32_t* parent, int32_t a, int32_t b) {
+  for (int s = 0; s < kFindSteps; s++) {
+    a = uf_find(parent, a);
+    b = uf_find(parent, b);
+    if (a < 0 || b < 0) return false;
+    if (a == b) return true;
+    if (a < b) {
+      const int32_t t = a;
+      a = b;
+      b = t;
+    }
+    if (atomicCAS(parent + a, a, b) == a) return true;
+  }
+  return false;
+}
+
+// counts[0] orientation defects, [1] boundary edges, [2] non-manifold halfedges, [3] degenerate
+// faces, [4] gave-up unions
+__global__ void check_edges_kernel(const int32_t* faces, int P, int64_t nf, const int32_t* twin, const uint8_t* flag,
+                                   int32_t* parent, uint8_t* vbound, unsigned long long* counts) {
+  const int64_t nh = nf * P;
+  unsigned long long c[5] = {0, 0, 0, 0, 0};
+  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = h / P;
+    const int r = (int)(h - f * P);
+    const int a = faces[h], b = faces[f * P + (r + 1) % P];
+    if (r == 0) {
+      bool deg = false;
+      for (int x = 0; x < P; x++)
+        for (int y = x + 1; y < P; y++) deg = deg || faces[f * P + x] == faces[f * P + y];
+      c[3] += deg;
+    }
+    if (flag[h]) c[2]++;
+    const int32_t t = twin[h];
+    if (t < 0) {
+      c[1]++;
+      vbound[a] = 1;
+      vbound[b] = 1;
+      continue;
+    }
+    if (t < h) continue;  // each pair once
+    if (faces[t] == a) c[0]++;  // the twin starts where h starts: both faces run the edge one way
+    if (!uf_union(parent, (int32_t)f, (int32_t)(t / P))) c[4]++;
+  }
+  for (int q = 0; q < 5; q++) {
+    unsigned long long x = c[q];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0 && x) atomicAdd(counts + q, x);
+  }
+}
+
+__global__ void iota_kernel(int32_t* p, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = (int32_t)i;
+}
+// counts[5] components (roots), counts[6] boundary vertices
+__global__ void count_roots_kernel(const int32_t* parent, int64_t nf, const uint8_t* vbound, int64_t nv,
+                                   unsigned long long* counts) {
+  unsigned long long roots = 0, bv = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nf || i < nv; i += (int64_t)gridDim.x * blockDim.x) {
+    if (i < nf) roots += parent[i] == (int32_t)i;
+    if (i < nv) bv += vbound[i];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    roots += __shfl_down_sync(0xffffffffu, roots, o);
+    bv += __shfl_down_sync(0xffffffffu, bv, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (roots) atomicAdd(counts + 5, roots);
+    if (bv) atomicAdd(counts + 6, bv);
+  }
+}
+
+}  // namespace
+}  // namespace tmc
+
+extern "C" tmc_status tmc_mesh_check(tmc_ctx* ctx, const tmc_mesh* mesh, int32_t faces, int64_t report[6]) {
+  if (!ctx || !mesh || !report) return TMC_ERR_INVALID_ARG;
+  if (faces != TMC_FACES_QUADS && faces != TMC_FACES_TRIS) return ctx_fail(ctx, TMC_ERR_INVALID_ARG, "unknown face kind");
+  const int P = faces == TMC_FACES_QUADS ? 4 : 3;
+  const int64_t nf = P == 4 ? mesh->nr_q : mesh->nr_t;
+  const int64_t nv = mesh->nr_v;
+  if (4 * nf >= (int64_t)0x7fffffff) return ctx_fail(ctx, TMC_ERR_CAPACITY, "too many faces for 32-bit halfedge ids");
+  cudaError_t e = cudaSetDevice(ctx_device(ctx));
+  if (e != cudaSuccess) return ctx_fail(ctx, TMC_ERR_CUDA, cudaGetErrorString(e));
+  DevMesh d;
+  tmc_status s = dev_mesh(ctx, mesh, P, d);
+  if (s) return s;
+  for (int q = 0; q < 6; q++) report[q] = 0;
+  if (nf == 0 || nv == 0) return TMC_OK;
+  cudaStream_t st = ctx_stream(ctx);
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx_device(ctx));
+  const int64_t nh = nf * P;
+  std::vector<void*> bufs;
+  auto get = [&](size_t bytes) -> void* {
+    void* p = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc(&p, std::max<size_t>(bytes, 16));
+    if (e == cudaSuccess) bufs.push_back(p);
+    return p;
+  };
+  HeOut ho{(int32_t*)get(nh * 4), (uint8_t*)get(nh), (int32_t*)get(nv * 4)};
+  HeWork w{(int32_t*)get(nv * 4), (int32_t*)get(nv * 4), (int32_t*)get(nh * 4), (int2*)get(nh * 8),
+           (unsigned long long*)get(nv * 8), (unsigned long long*)get((scan_tiles(nv) + 2) * 8),
+           (unsigned long long*)get(16), (unsigned long long*)get(16)};
+  int32_t* parent = (int32_t*)get(nf * 4);
+  uint8_t* vbound = (uint8_t*)get(nv);
+  unsigned long long* counts = (unsigned long long*)get(8 * 8);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.non_manifold, 0, 16, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(vbound, 0, nv, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, 64, st);
+  unsigned long long h_counts[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (e == cudaSuccess) {
+    int k = build_halfedges(d.faces, P, nf, nv, ho, w, sms, st);
+    iota_kernel<<<grid_of(nf, sms), 256, 0, st>>>(parent, nf);
+    check_edges_kernel<<<grid_of(nh, sms), 256, 0, st>>>(d.faces, P, nf, ho.twin, ho.flag, parent, vbound, counts);
+    count_roots_kernel<<<grid_of(std::max(nf, nv), sms), 256, 0, st>>>(parent, nf, vbound, nv, counts);
+    ctx_count_launches(ctx, k + 3);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h_counts, counts, sizeof h_counts, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  for (void* p : bufs) cudaFree(p);
+  if (e != cudaSuccess) return ctx_fail(ctx, TMC_ERR_CUDA, cudaGetErrorString(e));
+  if (h_counts[4]) return ctx_fail(ctx, TMC_ERR_TIMEOUT, "a union-find step gave up after its bound");
+  report[0] = (int64_t)h_counts[5];  // components
+  report[1] = (int64_t)h_counts[0];  // orientation defects
+  report[2] = (int64_t)h_counts[1];  // boundary edges
+  report[3] = (int64_t)h_counts[2];  // non-manifold halfedges
+  report[4] = (int64_t)h_counts[3];  // degenerate faces
+  report[5] = (int64_t)h_counts[6];  // boundary vertices
+  return TMC_OK;
+}

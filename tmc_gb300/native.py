@@ -41,7 +41,7 @@ EXPORTS = ["tmc_ctx_create", "tmc_ctx_destroy", "tmc_last_error", "tmc_ctx_strea
            "tmc_server_submit", "tmc_server_poll", "tmc_server_wait", "tmc_server_release", "tmc_server_last_error",
            "tmc_server_stats", "tmc_ctx_set_tuning", "tmc_ctx_get_tuning", "tmc_ctx_autotune",
            "tmc_volume_file_info", "tmc_field_load", "tmc_field_free", "tmc_mesh_write_obj", "tmc_mesh_write_off",
-           "tmc_mesh_quality", "tmc_mesh_valence"]
+           "tmc_mesh_quality", "tmc_mesh_valence", "tmc_mesh_check"]
 
 FACES_QUADS = 0
 FACES_TRIS = 1
@@ -147,6 +147,7 @@ def load(path: str = LIB_PATH):
                                      ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_double)]
     lib.tmc_mesh_valence.argtypes = [ctypes.c_void_p, ctypes.POINTER(Mesh), ctypes.c_int32,
                                      ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int32)]
+    lib.tmc_mesh_check.argtypes = [ctypes.c_void_p, ctypes.POINTER(Mesh), ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
     lib.tmc_ctx_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64]
     lib.tmc_ctx_get_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
     lib.tmc_ctx_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(Request), ctypes.c_int32,
@@ -331,6 +332,13 @@ class Context:
         n = ctypes.c_int32()
         self._check(self.lib.tmc_mesh_valence(self.h, ctypes.byref(m), int(faces), h, ctypes.byref(n)))
         return np.array(list(h)[:n.value], np.int64)
+
+    def check(self, m: Mesh, faces: int) -> dict:
+        """tmc_mesh_check: components, orientation defects, boundary / non-manifold / degenerate counts."""
+        r = (ctypes.c_int64 * 6)()
+        self._check(self.lib.tmc_mesh_check(self.h, ctypes.byref(m), int(faces), r))
+        return dict(zip(("components", "orientation_defects", "boundary_edges", "nonmanifold_halfedges",
+                         "degenerate_faces", "boundary_vertices"), list(r)))
 
     def field_load(self, path: str, fmt: int) -> Field:
         """tmc_field_load: a volume file read into device memory (float32)."""
