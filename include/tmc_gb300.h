@@ -15,6 +15,7 @@
  *   tmc_field_load         dmc::UniformGrid::init(file)              cpp_dmc/UniformGrid.cpp:3-45
  *                          readFromFile<T> / readDataFromFile<T>     cpp_dmc/Volumes.h:47, dmc/UniformGrid.h:431
  *                          p_mc::MarchingCubes::readDataFromFile    cuda_tmc/MarchingCubes.cu:3363
+ *   tmc_field_generate     p_mc::UniformGrid::generateVolume         dmc/UniformGrid.cu:177-217
  *   tmc_mesh_write_obj/off the OBJ / OFF writers                     cpp_dmc/main.cpp:33-87, mc/MarchingCubes.cpp:98-141
  *   tmc_mesh_quality       p_mc::EstimateElementQuality::q           dmc/EstimateElementQuality.cu:39-56
  *   tmc_mesh_valence       p_mc::VertexValence::vertexValence        dmc/VertexValence.cu:79-170
@@ -171,6 +172,15 @@ tmc_status tmc_volume_file_info(const char* path, int32_t format, int32_t dims[3
  * the GPU).  Replaces the reference's readers, which exit the process on a bad file. */
 tmc_status tmc_field_load(tmc_ctx* ctx, const char* path, int32_t format, tmc_field* out);
 tmc_status tmc_field_free(tmc_ctx* ctx, tmc_field* field);
+/* The reference's predefined implicit surfaces (p_mc::UniformGrid::generateVolume,
+ * dmc/UniformGrid.cu:21-217) sampled on the GPU on [-1, 1]^3 (spacing 2 / (n - 1) in float32, as the
+ * reference), into device memory; free with tmc_field_free.  Isovalue 0 for every surface. */
+enum {
+  TMC_SURF_SPHERE = 0, TMC_SURF_TORUS = 1, TMC_SURF_TWO_HOLED_TORUS = 2, TMC_SURF_FOUR_HOLED_TORUS = 3,
+  TMC_SURF_GENUS_TWO = 4, TMC_SURF_IWP = 5, TMC_SURF_PW_HYBRID = 6, TMC_SURF_NEOVIUS = 7, TMC_SURF_GOURSAT = 8,
+  TMC_SURF_STEINER_ROMAN = 9
+};
+tmc_status tmc_field_generate(tmc_ctx* ctx, int32_t surface, int32_t nx, int32_t ny, int32_t nz, tmc_field* out);
 /* OBJ output in the reference's layouts: TMC_OBJ_DMC_TRIS / TMC_OBJ_DMC_QUADS as cpp_dmc/main.cpp:33-87
  * (the triangle or the quad file), TMC_OBJ_TMC as mc/MarchingCubes.cpp:98-118 (including its use of
  * the second vertex's index as the third normal index).  OFF output as mc/MarchingCubes.cpp:123-141

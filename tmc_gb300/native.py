@@ -41,7 +41,10 @@ EXPORTS = ["tmc_ctx_create", "tmc_ctx_destroy", "tmc_last_error", "tmc_ctx_strea
            "tmc_server_submit", "tmc_server_poll", "tmc_server_wait", "tmc_server_release", "tmc_server_last_error",
            "tmc_server_stats", "tmc_ctx_set_tuning", "tmc_ctx_get_tuning", "tmc_ctx_autotune",
            "tmc_volume_file_info", "tmc_field_load", "tmc_field_free", "tmc_mesh_write_obj", "tmc_mesh_write_off",
-           "tmc_mesh_quality", "tmc_mesh_valence", "tmc_mesh_check"]
+           "tmc_mesh_quality", "tmc_mesh_valence", "tmc_mesh_check", "tmc_field_generate"]
+
+SURFACES = ("sphere", "torus", "two_holed_torus", "four_holed_torus", "genus_two", "iwp", "pw_hybrid", "neovius",
+            "goursat", "steiner_roman")
 
 FACES_QUADS = 0
 FACES_TRIS = 1
@@ -147,6 +150,8 @@ def load(path: str = LIB_PATH):
                                      ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_double)]
     lib.tmc_mesh_valence.argtypes = [ctypes.c_void_p, ctypes.POINTER(Mesh), ctypes.c_int32,
                                      ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int32)]
+    lib.tmc_field_generate.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                       ctypes.POINTER(Field)]
     lib.tmc_mesh_check.argtypes = [ctypes.c_void_p, ctypes.POINTER(Mesh), ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
     lib.tmc_ctx_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64]
     lib.tmc_ctx_get_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
@@ -344,6 +349,12 @@ class Context:
         """tmc_field_load: a volume file read into device memory (float32)."""
         f = Field()
         self._check(self.lib.tmc_field_load(self.h, path.encode(), int(fmt), ctypes.byref(f)))
+        return f
+
+    def field_generate(self, surface: int, nx: int, ny: int, nz: int) -> Field:
+        """tmc_field_generate: one of the reference's implicit surfaces sampled on [-1, 1]^3."""
+        f = Field()
+        self._check(self.lib.tmc_field_generate(self.h, int(surface), nx, ny, nz, ctypes.byref(f)))
         return f
 
     def field_free(self, f: Field):
