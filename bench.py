@@ -21,6 +21,7 @@ counted once (the CPU baseline and the reference arm count the same way).
 from __future__ import annotations
 
 import argparse
+import concurrent.futures
 import json
 import math
 import os
@@ -177,8 +178,18 @@ def run_ours(args, rank, world, local):
     vhost = native.make_volume(vol, host.data_ptr(), on_device=False)
     stream = torch.cuda.ExternalStream(ctx.stream)
     dmc_flags = native.DMC_SIMPLIFY | native.OUT_HALFEDGES | native.OUT_TRIANGLES
+    # The step's two extractions are independent: the TMC one runs on its own context (stream) from a
+    # helper thread while this thread runs the DMC one, so their kernels share the GPU.
+    ctx_t = native.Context(local)
+    stream_t = torch.cuda.ExternalStream(ctx_t.stream)
+    helper = concurrent.futures.ThreadPoolExecutor(1)
 
     def step(v, extra=0):
+        ft = helper.submit(ctx_t.tmc_raw, v, vol.iso, extra)
+        md = ctx.dmc_raw(v, vol.iso, dmc_flags | extra)
+        return ft.result(), md
+
+    def step_sequential(v, extra=0):  # both on one context, for the per-stage profile
         mt = ctx.tmc_raw(v, vol.iso, extra)
         md = ctx.dmc_raw(v, vol.iso, dmc_flags | extra)
         return mt, md
@@ -202,28 +213,32 @@ def run_ours(args, rank, world, local):
         mt, md = step(vdev)
         sizes = {"tmc_v": mt.nr_v, "tmc_t": mt.nr_t, "dmc_v": md.nr_v, "dmc_q": md.nr_q, "dmc_t": md.nr_t,
                  "dmc_he": md.nr_he}
-        ctx.free(mt)
+        ctx_t.free(mt)
         ctx.free(md)
     # ---- device-resident timed region ----
     barrier()
-    l0 = ctx.launches()
+    l0 = ctx.launches() + ctx_t.launches()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    et = torch.cuda.Event()
     with ClockSampler(local) as clk:
         e0.record(stream)
+        stream_t.wait_event(e0)  # the TMC stream starts inside the timed region
         for _ in range(args.steps):
             mt, md = step(vdev)
-            ctx.free(mt)
+            ctx_t.free(mt)
             ctx.free(md)
+        et.record(stream_t)
+        stream.wait_event(et)  # e1 follows the work of both streams
         e1.record(stream)
         barrier()
-    launches = ctx.launches() - l0
+    launches = ctx.launches() + ctx_t.launches() - l0
     ms = max_over_ranks(e0.elapsed_time(e1))
     ms_step = ms / args.steps
     value = world * cells * args.steps / (ms * 1e-3) / 1e9
     # ---- end to end through the C ABI with host buffers ----
     for _ in range(1):
         mt, md = step(vhost, native.OUT_HOST)
-        ctx.free(mt)
+        ctx_t.free(mt)
         ctx.free(md)
     barrier()
     d2h = 0
@@ -232,7 +247,7 @@ def run_ours(args, rank, world, local):
         mt, md = step(vhost, native.OUT_HOST)
         d2h = (24 * mt.nr_v + 12 * mt.nr_t) + (24 * md.nr_v + 16 * md.nr_q + 12 * md.nr_t + 16 * md.nr_he +
                                                  4 * md.nr_v + 4 * md.nr_q)
-        ctx.free(mt)
+        ctx_t.free(mt)
         ctx.free(md)
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
@@ -244,7 +259,7 @@ def run_ours(args, rank, world, local):
     ctx.free(m)
     ctx.set_profiling(True)
     for _ in range(2):
-        mt, md = step(vdev)
+        mt, md = step_sequential(vdev)
         ctx.free(mt)
         ctx.free(md)
     prof = ctx.profile()
@@ -288,7 +303,9 @@ def run_ours(args, rank, world, local):
         "config": {"workload": f"{n}^3 noise field (33^3 U[-1,1] upsampled + 0.02 N(0,1)), isovalue 0: TMC shared-vertex"
                                " + DMC halfedge/triangles with P3X3Y+P3333 simplification per step",
                    "grid": [n, n, n], "cells_per_step": cells, "seed": SEED,
-                   "l2": f"inputs larger than L2 ({4 * voxels / 2**20:.0f} MiB field)", "parallelism": f"replicas x{world}"},
+                   "l2": f"inputs larger than L2 ({4 * voxels / 2**20:.0f} MiB field)", "parallelism": f"replicas x{world}",
+                   "streams": "the TMC and the DMC extraction of a step run concurrently, one context (stream) each; "
+                              "the stage profile and the roofline come from a separate sequential pass"},
         "mesh": sizes,
         "e2e": {"value": round(e2e, 4), "unit": "Gcells/s", "h2d_bytes_per_step": 2 * 4 * voxels,
                 "d2h_bytes_per_step": int(d2h)},
@@ -306,6 +323,8 @@ def run_ours(args, rank, world, local):
     }
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_port(vol)
+    helper.shutdown()
+    ctx_t.close()
     ctx.close()
     if world > 1:
         import torch.distributed as dist
