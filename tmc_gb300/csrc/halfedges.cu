@@ -31,15 +31,11 @@ __global__ void he_vertex_init_kernel(unsigned long long* hv_key, int32_t* deg, 
   }
 }
 
-// twins reset, out-degrees; the degree counter's old value is the halfedge's slot in its origin's
-// list (one atomic per halfedge)
-__global__ void he_build_kernel(const int32_t* faces, int64_t nh, int32_t* twin, uint8_t* flag, int32_t* deg,
-                                int32_t* rank) {
-  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
-    twin[h] = -1;
-    flag[h] = 0;
+// out-degrees; the degree counter's old value is the halfedge's slot in its origin's list (one
+// atomic per halfedge).  Twins and flags are written by he_twin_kernel, every entry once.
+__global__ void he_build_kernel(const int32_t* faces, int64_t nh, int32_t* deg, int32_t* rank) {
+  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x)
     rank[h] = atomicAdd(deg + faces[h], 1);
-  }
 }
 
 __global__ void he_scatter_kernel(const int32_t* faces, int P, int64_t nf, const int32_t* off, const int32_t* rank,
@@ -87,7 +83,8 @@ __device__ __forceinline__ int edge_halfedges(const int2* list, const int32_t* o
 }
 
 // one thread per halfedge: two-halfedge edges pair without coordination; 3 or 4 are resolved by
-// the edge's lowest halfedge
+// the edge's lowest halfedge, which writes the twins and flags of all of them; every other
+// halfedge writes its own (each entry is written exactly once)
 __global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const int2* list, const int32_t* off,
                                const int32_t* deg, int32_t* twin, uint8_t* flag, unsigned long long* hv_key,
                                unsigned long long* non_manifold) {
@@ -101,9 +98,15 @@ __global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const in
     const int c = edge_halfedges(list, off, deg, v0, v1, id);
     if (c == 2) {
       twin[h] = (id[0] == (int)h) ? id[1] : id[0];
+      flag[h] = 0;
       continue;
     }
-    if (c < 3 || c > 4 || id[0] != (int)h) continue;  // boundary, or resolved by the lowest halfedge
+    if (c < 3 || c > 4) {  // boundary, or more halfedges than the rules pair: no twin
+      twin[h] = -1;
+      flag[h] = 0;
+      continue;
+    }
+    if (id[0] != (int)h) continue;  // resolved by the edge's lowest halfedge
     if (c == 3) {
       const int e0 = id[0], e1 = id[1], e2 = id[2];
       const int a0 = faces[e0], a1 = faces[e1], a2 = faces[e2];
@@ -171,7 +174,7 @@ int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& 
   };
   int k = 0;
   he_vertex_init_kernel<<<grid(nv), 256, 0, st>>>(w.hv_key, w.deg, nv);
-  he_build_kernel<<<grid(nh), 256, 0, st>>>(faces, nh, o.twin, o.flag, w.deg, w.rank);
+  he_build_kernel<<<grid(nh), 256, 0, st>>>(faces, nh, w.deg, w.rank);
   k += 2 + scan_i32(w.deg, nv, w.off, w.tiles, w.total, st);
   he_scatter_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.off, w.rank, w.list);
   he_twin_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.list, w.off, w.deg, o.twin, o.flag, w.hv_key,
