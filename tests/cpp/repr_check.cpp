@@ -4,6 +4,7 @@
 //   repr_check field.raw nx ny nz iso  -> prints "contours mismatches fallbacks fail1 fail2"
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "../../tmc_gb300/csrc/common.cuh"
@@ -102,7 +103,24 @@ int main(int argc, char** argv) {
           {
             repr::ProjRecord R;
             int f64c = 0;
-            if (repr::projection_record(u, iso, c, t, pts[t], sz, bx, R, f64c)) {
+            std::memset(&R, 0, sizeof R);  // the record's tail padding is compared too
+            const bool rec_ok = repr::projection_record(u, iso, c, t, pts[t], sz, bx, R, f64c);
+            {
+              // the set-up kernel's form: sums and box accumulated without the point array
+              int tstart = 0;
+              for (int t2 = 0; t2 < t; t2++) tstart += cnt_size(c, t2);
+              repr::ContourAcc A;
+              repr::contour_acc(u, iso, ffx::ff_from_double(iso), c, tstart, sz, A);
+              repr::ProjRecord R2;
+              std::memset(&R2, 0, sizeof R2);
+              int f64a = 0;
+              const bool acc_ok = repr::projection_record_acc(u, iso, c, t, tstart, sz, A, R2, f64a);
+              if (acc_ok != rec_ok || (rec_ok && (std::memcmp(&R, &R2, sizeof R) != 0 || f64a != f64c))) {
+                if (mism < 5) fprintf(stderr, "accumulated set-up differs cell %d %d %d t %d\n", i, j, k, t);
+                mism++;
+              }
+            }
+            if (rec_ok) {
               float pr[3];
               int f64r = 0;
               const int rr = repr::projection_from_record(R, pr, lb, 1, f64r);

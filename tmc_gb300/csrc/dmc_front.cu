@@ -550,12 +550,14 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_warp_kernel(CellSpa
 }
 
 // Two-pass vertices, pass 1: contour, plane, sample coordinates, mean point -> one record per
-// vertex.  Contours with neighbour-contour exclusion go to the one-pass kernel's list.
+// vertex.  Only the vertex's own contour is evaluated: its edge points are summed and boxed as they
+// are computed (no point array, nothing in local memory).  Contours with neighbour-contour
+// exclusion go to the one-pass kernel's list.
 __global__ void __launch_bounds__(kVertexThreads, 5) dmc_vertex_setup_kernel(CellSpace space, const int32_t* voff,
-                                                                           const uint32_t* vwork, int64_t nv,
-                                                                           repr::ProjRecord* recs, uint32_t* list,
-                                                                           unsigned* count,
-                                                                           unsigned long long* stats) {
+                                                                              const uint32_t* vwork, int64_t nv,
+                                                                              repr::ProjRecord* recs, uint32_t* list,
+                                                                              unsigned* count,
+                                                                              unsigned long long* stats) {
   __shared__ uint64_t cc[256];
   for (int c = threadIdx.x; c < 256; c += blockDim.x) cc[c] = c_case_contour[c];
   __syncthreads();
@@ -569,20 +571,39 @@ __global__ void __launch_bounds__(kVertexThreads, 5) dmc_vertex_setup_kernel(Cel
     const Grid& g = G.g;
     int i, j, k;
     cell_ijk(g, vcell - g.vbase, i, j, k);
-    VertexContour V;
-    repr::ProjRecord R;
-    bool ok = vertex_contour(g, i, j, k, rank, cc, G.iso_ff, V);
+    float u[8];
+    load_corners(g, i, j, k, u);
+    const uint64_t c = dmc_polygon(mc_case(u, g.iso_up), u, g.iso, cc);
+    // the rank-th used contour (one with an interior edge), as vertex_contour selects it
+    const int ncnt = cnt_count(c);
+    int flat = 0, seen = 0, tsel = -1, tstart = 0;
+    for (int t = 0; t < ncnt && tsel < 0; t++) {
+      const int sz = cnt_size(c, t);
+      bool used = false;
+      for (int q = 0; q < sz; q++) used = used || edge_interior(g, i, j, k, cnt_edge(c, flat + q));
+      if (used) {
+        if (seen == rank) {
+          tsel = t;
+          tstart = flat;
+        }
+        seen++;
+      }
+      flat += sz;
+    }
+    repr::ProjRecord& R = recs[vidx];  // written in place: no copy in local memory
+    bool ok = tsel >= 0;              // cannot fail: counted
     if (ok) {
+      const int n = cnt_size(c, tsel);
+      repr::ContourAcc A;
+      repr::contour_acc(u, g.iso, G.iso_ff, c, tstart, n, A);
       int f64c = 0;
-      ok = repr::projection_record(V.u, g.iso, V.c, V.tsel, V.pts + 3 * V.tstart, cnt_size(V.c, V.tsel), V.bx, R,
-                                   f64c);
+      ok = repr::projection_record_acc(u, g.iso, c, tsel, tstart, n, A, R, f64c);
       if (ok) f64 += f64c;  // contours redone by the one-pass kernel are counted there
     }
     if (!ok) {
       R.prj = -1;
       list[atomicAdd(count, 1u)] = (uint32_t)vidx;
     }
-    recs[vidx] = R;
   }
   if (f64) atomicAdd(stats + 7, (unsigned long long)f64);
 }

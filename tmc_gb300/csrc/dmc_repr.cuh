@@ -46,14 +46,27 @@ struct Stats {
 // ---------------------------------------------------------------------------------------------
 // edge parameter: getLocalCoordinates (cpp_dmc/DualMarchingCubes.h:391-407), l rounded to float
 // ---------------------------------------------------------------------------------------------
-TMC_HD_COLD float edge_param_exact(int e, const float u[8], double iso) {
+// the reference's float64 parameter; the two corner values are passed by value (a pointer would
+// force the caller's corners into local memory)
+TMC_HD_COLD float edge_param_f64(double iso, float f0, float f1) {
+  return (float)((iso - (double)f0) / ((double)f1 - (double)f0));
+}
+TMC_HD float edge_param_exact(int e, const float u[8], double iso) {
   const int v0 = nibr(EDGE_V0, e), v1 = nibr(EDGE_V1, e);
-  return (float)((iso - (double)u[v0]) / ((double)u[v1] - (double)u[v0]));
+  return edge_param_f64(iso, u[v0], u[v1]);
+}
+
+// corner value v of the eight (selects: a run-time index keeps u in registers)
+TMC_HD float corner_at(const float u[8], int v) {
+  float r = u[0];
+#pragma unroll
+  for (int q = 1; q < 8; q++) r = (v == q) ? u[q] : r;
+  return r;
 }
 
 TMC_HD float edge_param_fast(int e, const float u[8], double iso, ff iso_ff, bool& fallback) {
   const int v0 = nibr(EDGE_V0, e), v1 = nibr(EDGE_V1, e);
-  const float f0 = u[v0], f1 = u[v1];
+  const float f0 = corner_at(u, v0), f1 = corner_at(u, v1);
   const ff num = ffx::ff_sub(iso_ff, ffx::ff_from(f0));
   const ff den = ffx::two_sum(f1, -f0);  // exact
   const ff q = ffx::ff_div(num, den);
@@ -63,7 +76,7 @@ TMC_HD float edge_param_fast(int e, const float u[8], double iso, ff iso_ff, boo
   float l;
   if (ffx::ff_round(q, err, l)) return l;
   fallback = true;
-  return edge_param_exact(e, u, iso);
+  return edge_param_f64(iso, f0, f1);
 }
 
 // local coordinates of the crossing on edge e: l * val + con in float, as the reference
@@ -423,7 +436,7 @@ TMC_HD void sample_coords(float lo, float hi, float out[7], int& f64_count) {
   const ff D = ffx::two_sum(hi, -lo);  // exact difference
   const int ehi = (int)((ffx::fbits(hi) >> 23) & 0xFF), elo = (int)((ffx::fbits(lo) >> 23) & 0xFF);
   const bool exact = (lo == 0.0f) || (hi == lo) || (ehi - elo <= 20 && elo > 0);
-#pragma unroll 1
+#pragma unroll
   for (int i = 1; i <= 7; i++) {
     const ff a = ffx::two_prod((float)i, D.hi);
     const ff b = ffx::two_prod((float)i, D.lo);
@@ -469,14 +482,16 @@ TMC_HD void approx_into(const ProjCtx& P, const float* us, const float* vs, int 
 
 // w window from the box's w extent, as the reference widens it (wmin -= 1e-5, wmax += 1e-5 when
 // the extent is below 1e-5), as the float range [wlo, whi] of values inside the float64 window.
-TMC_HD_COLD void w_window_flat(float lo, float hi, float& wlo, float& whi) {
+struct Window {
+  float lo, hi;
+};
+TMC_HD_COLD Window w_window_flat(float lo, float hi) {
   double wmin = lo, wmax = hi;
   if (fabs(wmax - wmin) < 1e-5) {
     wmin -= 1e-5;
     wmax += 1e-5;
   }
-  wlo = ffx::f_ceil(wmin);
-  whi = ffx::f_floor(wmax);
+  return Window{ffx::f_ceil(wmin), ffx::f_floor(wmax)};
 }
 TMC_HD void w_window(float lo, float hi, float& wlo, float& whi) {
   const float ext = hi - lo;  // within one ulp of the exact extent
@@ -485,7 +500,9 @@ TMC_HD void w_window(float lo, float hi, float& wlo, float& whi) {
     whi = hi;
     return;
   }
-  w_window_flat(lo, hi, wlo, whi);
+  const Window w = w_window_flat(lo, hi);
+  wlo = w.lo;
+  whi = w.hi;
 }
 
 // index of the lowest set bit of a non-zero mask
@@ -612,10 +629,10 @@ TMC_HD bool exact_in_f64(ff x) {
 // projection plane from the box extents (minProjection).  The extents are float differences, held
 // exactly as float pairs; when the reference's float64 subtractions are exact too the comparison
 // is exact, otherwise (-1) it is redone in float64.
-TMC_HD int plane_from_extent_ff(const Boxes& bx, int t) {
-  const ff su = ffx::two_sum(bx.b[t][0][1], -bx.b[t][0][0]);
-  const ff sv = ffx::two_sum(bx.b[t][1][1], -bx.b[t][1][0]);
-  const ff sw = ffx::two_sum(bx.b[t][2][1], -bx.b[t][2][0]);
+TMC_HD int plane_from_extent_box_ff(const float b[3][2]) {
+  const ff su = ffx::two_sum(b[0][1], -b[0][0]);
+  const ff sv = ffx::two_sum(b[1][1], -b[1][0]);
+  const ff sw = ffx::two_sum(b[2][1], -b[2][0]);
   if (!exact_in_f64(su) || !exact_in_f64(sv) || !exact_in_f64(sw)) return -1;
   if (ff_le(sw, su) && ff_le(sw, sv)) return 0;
   if (ff_le(sv, su) && ff_le(sv, sw)) return 1;
@@ -645,6 +662,19 @@ TMC_HD int plane_from_gradient_f(const float f[8], float uu, float vv, float ww)
   if (dx >= dy && dx >= dz) return 2;
   return 0;
 }
+TMC_HD int plane_from_extent_ff(const Boxes& bx, int t) { return plane_from_extent_box_ff(bx.b[t]); }
+struct Box3 {
+  float b[3][2];
+};
+TMC_HD_COLD int plane_from_extent_box_f64(Box3 x) {
+  const double su = (double)x.b[0][1] - (double)x.b[0][0];
+  const double sv = (double)x.b[1][1] - (double)x.b[1][0];
+  const double sw = (double)x.b[2][1] - (double)x.b[2][0];
+  if (sw <= su && sw <= sv) return 0;
+  if (sv <= su && sv <= sw) return 1;
+  if (su <= sv && su <= sw) return 2;
+  return 0;
+}
 TMC_HD_COLD int plane_from_extent_f64(const Boxes& bx, int t) { return plane_from_extent(bx, t); }
 TMC_HD_COLD int plane_from_gradient_exact(const float* pts, int n, Corners u) {
   const Point64 pd = mean_point_exact(pts, n);
@@ -661,19 +691,32 @@ struct TailOut {
 TMC_HD_COLD TailOut representative_tail(Corners u, double iso, uint64_t c, int t, const float* pts, int n,
                                         const Boxes& bx, int prj);
 
-// Projection set-up of contour t: plane, permuted corners, mean point, sample coordinates and the
-// w window.  Returns the plane; f64_coords counts sample coordinates computed in float64.
-TMC_HD int projection_setup(const float u[8], double iso, uint64_t c, int t, const float* pts, int n,
-                            const Boxes& bx, ProjCtx& P, float us[7], float vs[7], int& f64_coords) {
-  const int cnt_sz = csize(c, t);
-  // mean point, float-float
-  ff s[3] = {ffx::ff_from(0.0f), ffx::ff_from(0.0f), ffx::ff_from(0.0f)};
-#pragma unroll 1
+// edge points of contour t (flat edge positions tstart .. tstart + n) recomputed from the corners
+TMC_HD void contour_points(const float u[8], double iso, uint64_t c, int tstart, int n, float pts[36]) {
+  const ff iso_ff = ffx::ff_from_double(iso);
   for (int q = 0; q < n; q++) {
-    s[0] = ffx::ff_add(s[0], ffx::ff_from(pts[3 * q]));
-    s[1] = ffx::ff_add(s[1], ffx::ff_from(pts[3 * q + 1]));
-    s[2] = ffx::ff_add(s[2], ffx::ff_from(pts[3 * q + 2]));
+    const int e = cedge(c, tstart + q);
+    bool fb = false;
+    const float l = edge_param_fast(e, u, iso, iso_ff, fb);
+    local_from_param(e, l, pts + 3 * q);
   }
+}
+// float64 plane decision from the gradient at the reference's float64 mean point, with the points
+// recomputed (rare: only when the float32 decision is within its error bound)
+TMC_HD_COLD int plane_from_gradient_recomputed(Corners u, double iso, uint64_t c, int tstart, int n) {
+  float pts[36];
+  contour_points(u.f, iso, c, tstart, n, pts);
+  return plane_from_gradient_exact(pts, n, u);
+}
+
+// Projection set-up of contour t from its coordinate sums s (float-float, in contour order) and its
+// box: plane, permuted corners, mean point, sample coordinates and the w window.  Returns the
+// plane; f64_coords counts sample coordinates computed in float64.  pts (the edge points) is only
+// read by a rare float64 plane decision; without it (null) the points are recomputed from tstart.
+TMC_HD int projection_setup_core(const float u[8], double iso, uint64_t c, int t, const ff s[3], int n,
+                                 const float box[3][2], const float* pts, int tstart, ProjCtx& P, float us[7],
+                                 float vs[7], int& f64_coords) {
+  const int cnt_sz = csize(c, t);
   const ff nn = ffx::ff_from((float)n);
   const ff pm[3] = {ffx::ff_div(s[0], nn), ffx::ff_div(s[1], nn), ffx::ff_div(s[2], nn)};
   int prj;
@@ -682,16 +725,24 @@ TMC_HD int projection_setup(const float u[8], double iso, uint64_t c, int t, con
     if (prj < 0) {
       Corners uc;
       for (int q = 0; q < 8; q++) uc.f[q] = u[q];
-      prj = plane_from_gradient_exact(pts, n, uc);
+      prj = pts ? plane_from_gradient_exact(pts, n, uc) : plane_from_gradient_recomputed(uc, iso, c, tstart, n);
     }
   } else {
-    prj = plane_from_extent_ff(bx, t);
-    if (prj < 0) prj = plane_from_extent_f64(bx, t);
+    prj = plane_from_extent_box_ff(box);
+    if (prj < 0) {
+      Box3 x;
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        x.b[d][0] = box[d][0];
+        x.b[d][1] = box[d][1];
+      }
+      prj = plane_from_extent_box_f64(x);
+    }
   }
   uint32_t perm;
   plane(prj, P.A, P.B, P.W, perm);
 #pragma unroll
-  for (int q = 0; q < 8; q++) P.fp[q] = u[(perm >> (4 * q)) & 0xF];
+  for (int q = 0; q < 8; q++) P.fp[q] = corner_at(u, (perm >> (4 * q)) & 0xF);
   P.sabs_lo = fmaxf(fmaxf(fabsf(P.fp[0]), fabsf(P.fp[1])), fmaxf(fabsf(P.fp[2]), fabsf(P.fp[3])));
   P.sabs_hi = fmaxf(fmaxf(fabsf(P.fp[4]), fabsf(P.fp[5])), fmaxf(fabsf(P.fp[6]), fabsf(P.fp[7])));
   P.pff[0] = P.A == 0 ? pm[0] : pm[1];
@@ -706,13 +757,60 @@ TMC_HD int projection_setup(const float u[8], double iso, uint64_t c, int t, con
   P.excl = P.cnt != 1 && cnt_sz != 3;
   P.t = t;
   P.c = c;
-  P.bx = &bx;
-  const float umin = bx.b[t][P.A][0], umax = bx.b[t][P.A][1];
-  const float vmin = bx.b[t][P.B][0], vmax = bx.b[t][P.B][1];
+  P.bx = nullptr;
+  const float umin = P.A == 0 ? box[0][0] : box[1][0], umax = P.A == 0 ? box[0][1] : box[1][1];
+  const float vmin = P.B == 1 ? box[1][0] : box[2][0], vmax = P.B == 1 ? box[1][1] : box[2][1];
+  const float wlo = P.W == 2 ? box[2][0] : (P.W == 1 ? box[1][0] : box[0][0]);
+  const float whi = P.W == 2 ? box[2][1] : (P.W == 1 ? box[1][1] : box[0][1]);
   sample_coords(umin, umax, us, f64_coords);
   sample_coords(vmin, vmax, vs, f64_coords);
-  w_window(bx.b[t][P.W][0], bx.b[t][P.W][1], P.wlo, P.whi);
+  w_window(wlo, whi, P.wlo, P.whi);
   return prj;
+}
+
+// The same from the contour's edge points and the boxes of all the cell's contours (the boxes of
+// the others serve the neighbour-contour exclusion of the sample evaluation).
+TMC_HD int projection_setup(const float u[8], double iso, uint64_t c, int t, const float* pts, int n,
+                            const Boxes& bx, ProjCtx& P, float us[7], float vs[7], int& f64_coords) {
+  ff s[3] = {ffx::ff_from(0.0f), ffx::ff_from(0.0f), ffx::ff_from(0.0f)};
+#pragma unroll 1
+  for (int q = 0; q < n; q++) {
+    s[0] = ffx::ff_add(s[0], ffx::ff_from(pts[3 * q]));
+    s[1] = ffx::ff_add(s[1], ffx::ff_from(pts[3 * q + 1]));
+    s[2] = ffx::ff_add(s[2], ffx::ff_from(pts[3 * q + 2]));
+  }
+  const int prj = projection_setup_core(u, iso, c, t, s, n, bx.b[t], pts, 0, P, us, vs, f64_coords);
+  P.bx = &bx;
+  return prj;
+}
+
+// Contour t's coordinate sums and box accumulated while its edge points are computed (edge order,
+// as projection_setup sums them), without keeping the points.
+struct ContourAcc {
+  ff s[3];
+  float box[3][2];
+};
+TMC_HD void contour_acc(const float u[8], double iso, ff iso_ff, uint64_t c, int tstart, int n, ContourAcc& A) {
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    A.s[d] = ffx::ff_from(0.0f);
+    A.box[d][0] = 1;
+    A.box[d][1] = 0;
+  }
+#pragma unroll 1
+  for (int q = 0; q < n; q++) {
+    const int e = cedge(c, tstart + q);
+    bool fb = false;
+    const float l = edge_param_fast(e, u, iso, iso_ff, fb);
+    float ui[3];
+    local_from_param(e, l, ui);
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      A.s[d] = ffx::ff_add(A.s[d], ffx::ff_from(ui[d]));
+      A.box[d][0] = A.box[d][0] > ui[d] ? ui[d] : A.box[d][0];
+      A.box[d][1] = A.box[d][1] < ui[d] ? ui[d] : A.box[d][1];
+    }
+  }
 }
 
 // 7x7 projection of contour t.  pts: the contour's edge points (3 floats each, in contour order),
@@ -780,6 +878,26 @@ TMC_HD bool projection_record(const float u[8], double iso, uint64_t c, int t, c
   ProjCtx P;
   const int prj = projection_setup(u, iso, c, t, pts, n, bx, P, R.us, R.vs, f64_coords);
   if (P.excl) return false;
+  for (int q = 0; q < 8; q++) R.fp[q] = P.fp[q];
+  R.wlo = P.wlo;
+  R.whi = P.whi;
+  for (int d = 0; d < 3; d++) {
+    R.pff[2 * d] = P.pff[d].hi;
+    R.pff[2 * d + 1] = P.pff[d].lo;
+  }
+  R.iso = iso;
+  R.prj = prj;
+  R.pad = 0;
+  return true;
+}
+
+// Set-up pass of contour t (edges tstart .. tstart + n of the cell's contour word c) from its
+// accumulated sums and box; returns false when the contour needs the one-pass kernel.
+TMC_HD bool projection_record_acc(const float u[8], double iso, uint64_t c, int t, int tstart, int n,
+                                  const ContourAcc& A, ProjRecord& R, int& f64_coords) {
+  if (ccount(c) != 1 && csize(c, t) != 3) return false;  // neighbour-contour exclusion applies
+  ProjCtx P;
+  const int prj = projection_setup_core(u, iso, c, t, A.s, n, A.box, nullptr, tstart, P, R.us, R.vs, f64_coords);
   for (int q = 0; q < 8; q++) R.fp[q] = P.fp[q];
   R.wlo = P.wlo;
   R.whi = P.whi;
