@@ -739,7 +739,8 @@ __global__ void __launch_bounds__(128) tmc_ambiguous_kernel(CellSpace space, con
     tmc_vertex_ids(g, i, j, k, em, own, voff[vcell], vfirst, rec, voff, vid);
     TriSink ts{tris + 3 * (int64_t)toff[vcell], 0};
     AmbCell amb;
-    load_amb_cell(g, i, j, k, u, em, amb, true);
+    // corner positions and gradients serve only inner vertices, which the counting pass recorded
+    load_amb_cell(g, i, j, k, u, em, amb, trec_inner(r) > 0);
     // inner vertices are numbered within the volume: shift the outputs to its first vertex
     InnerOut io{out.v + 3 * (int64_t)vfirst, out.n + 3 * (int64_t)vfirst, out.v64 ? out.v64 + 3 * (int64_t)vfirst : nullptr};
     p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, voff[vcell] - vfirst + __popc(own), ts, amb.P, amb.N, &io);
