@@ -608,11 +608,16 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     s.err = pool.err;
     return s;
   }
+  // The mesh changes only where a pass merges or removes something; a pass that changes nothing
+  // keeps `cur` as it is, and the halfedges (and out-degrees) built for it stay valid.
+  int mesh_version = 0, he_version = -1;
   auto halfedges = [&](const DmcMesh& m) {
+    if (he_version == mesh_version) return;
     Stage tm(prof, "dmc_halfedges", st);
     cudaMemsetAsync(hw.nm, 0, 2 * sizeof(unsigned long long), st);
     HeOut ho{hw.twin, hw.flag, hw.hv};
     s.launches += build_halfedges(m.quads, 4, m.nq, m.nv, ho, hw.w, sms, st);
+    he_version = mesh_version;
   };
   auto read_total = [&]() -> int64_t {
     cudaMemcpyAsync(h_cnt, total, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
@@ -712,7 +717,17 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     // remove vertices
     invert_flags_kernel<<<gv, 256, 0, st>>>(vm_first, cur.nv, keep);
     s.launches += 1 + scan_flags(keep, cur.nv, idx, tiles, total, st);
-    const int64_t nv2 = read_total();
+    int64_t nv2 = read_total();
+    if (nv2 == cur.nv) {
+      // no vertex merged: if no quad was removed either the pass changed nothing (only the merged
+      // pair's midpoints are written), and the mesh stays as it is
+      invert_flags_kernel<<<gq, 256, 0, st>>>(em, cur.nq, keep);
+      s.launches += 1 + scan_flags(keep, cur.nq, idx, tiles, total, st);
+      if (read_total() == cur.nq) continue;
+      invert_flags_kernel<<<gv, 256, 0, st>>>(vm_first, cur.nv, keep);
+      s.launches += 1 + scan_flags(keep, cur.nv, idx, tiles, total, st);
+      nv2 = read_total();
+    }
     DmcMesh nx = cur;
     if ((s.err = new_vertices(nv2, nx)) != cudaSuccess) break;
     adopt(nx.v64);
@@ -741,6 +756,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     nx.nq = nq2;
     nx.quads = (int32_t*)qn;
     cur = nx;
+    mesh_version++;
   }
   // ---- P3333 (simplify3333, :1362-1385) ----
   if (s.err == cudaSuccess && p3333 && cur.nq > 0) {
@@ -761,9 +777,21 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     mark3333_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.nq, val, p3, rflag, vm0, vm1);
     invert_flags_kernel<<<gv, 256, 0, st>>>(vm0, cur.nv, keep);
     s.launches += 5 + scan_flags(keep, cur.nv, idx, tiles, total, st);
-    const int64_t nv2 = read_total();
+    int64_t nv2 = read_total();
+    bool unchanged = false;
+    if (nv2 == cur.nv) {
+      // no vertex removed: with no quad removed either, the mesh stays as it is
+      invert_flags_kernel<<<gq, 256, 0, st>>>(rflag, cur.nq, keep);
+      s.launches += 1 + scan_flags(keep, cur.nq, idx, tiles, total, st);
+      unchanged = read_total() == cur.nq;
+      if (!unchanged) {
+        invert_flags_kernel<<<gv, 256, 0, st>>>(vm0, cur.nv, keep);
+        s.launches += 1 + scan_flags(keep, cur.nv, idx, tiles, total, st);
+        nv2 = read_total();
+      }
+    }
     DmcMesh nx = cur;
-    if ((s.err = new_vertices(nv2, nx)) == cudaSuccess) {
+    if (!unchanged && (s.err = new_vertices(nv2, nx)) == cudaSuccess) {
       adopt(nx.v64);
       adopt(nx.v);
       adopt(nx.n);
@@ -788,6 +816,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
         nx.nq = nq2;
         nx.quads = (int32_t*)qn;
         cur = nx;
+        mesh_version++;
       }
     }
   }
