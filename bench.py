@@ -120,11 +120,11 @@ class ClockSampler:
 # ------------------------------------------------------------------------------------------------
 # Kernel groups of the roofline: the profiler stages of one piece of work, and the DRAM traffic per
 # algorithmic byte that ncu measured for them on the 320^3 case of this workload (profiles/
-# dmc_vertex_noise320.md: 3,264 MB for 5.49 M vertices; tmc_emit_noise320.md: 1,207 MB for 267.7 MB of
+# dmc_vertex_noise320.md: 2,822 MB for 5.49 M vertices; tmc_emit_noise320.md: 1,207 MB for 267.7 MB of
 # mesh; dmc_classify_noise320.md: 224.0 MB for a 131.1 MB field), scaled to the full launch by the units
 # it processes (traffic grows with the vertex / cell count).
 ROOFLINE_GROUPS = {
-    "dmc_vertex": (("dmc_vertex_setup", "dmc_project", "dmc_vertex_finish", "dmc_vertex"), 3264.3 / 131.6),
+    "dmc_vertex": (("dmc_vertex_setup", "dmc_project", "dmc_vertex_finish", "dmc_vertex"), 2822.1 / 131.6),
     "dmc_halfedges": (("dmc_halfedges",), None),
     "tmc_emit": (("tmc_emit",), 1207.3 / 267.7),
     "dmc_classify": (("dmc_classify",), 224.0 / 131.1),
