@@ -286,24 +286,25 @@ __global__ void invert_flags_kernel(const uint8_t* in, int64_t n, uint8_t* out) 
 }
 
 // removeVertices3X3Y / removeVertices3333 (:1096-1112, :1324-1338): kept vertices move to their
-// new index, which becomes their map entry
+// new index, which becomes their map entry.  One thread per vertex component (x, y or z of all four
+// arrays): every load and store is unit-stride across the warp.
 __global__ void gather_vertices_kernel(const uint8_t* keep, const int32_t* idx, int64_t nv, const double* v64,
                                        const float* v, const double* n64, const float* n, double* v64o, float* vo,
                                        double* n64o, float* no, int32_t* map, int64_t cap, unsigned* overflow) {
-  FOR_EACH(i, nv) {
+  FOR_EACH(e, 3 * nv) {
+    const int64_t i = e / 3;
     if (!keep[i]) continue;
     const int64_t o = idx[i];
+    const int d = (int)(e - 3 * i);
     if (o < 0 || o >= cap) {
-      atomicAdd(overflow, 1u);
+      if (d == 0) atomicAdd(overflow, 1u);
       continue;
     }
-    for (int d = 0; d < 3; d++) {
-      v64o[3 * o + d] = v64[3 * i + d];
-      vo[3 * o + d] = v[3 * i + d];
-      n64o[3 * o + d] = n64[3 * i + d];
-      no[3 * o + d] = n[3 * i + d];
-    }
-    map[i] = (int32_t)o;
+    v64o[3 * o + d] = v64[e];
+    vo[3 * o + d] = v[e];
+    n64o[3 * o + d] = n64[e];
+    no[3 * o + d] = n[e];
+    if (d == 0) map[i] = (int32_t)o;
   }
 }
 
@@ -734,7 +735,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     adopt(nx.v);
     adopt(nx.n);
     adopt(nx.n64);
-    gather_vertices_kernel<<<gv, 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.v, cur.n64, cur.n, nx.v64, nx.v,
+    gather_vertices_kernel<<<grid_for(3 * cur.nv, sms), 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.v, cur.n64, cur.n, nx.v64, nx.v,
                                                 nx.n64, nx.n, vm_second, nv2, hw.ovf);
     // remove quads
     invert_flags_kernel<<<gq, 256, 0, st>>>(em, cur.nq, keep);
@@ -796,7 +797,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
       adopt(nx.v);
       adopt(nx.n);
       adopt(nx.n64);
-      gather_vertices_kernel<<<gv, 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.v, cur.n64, cur.n, nx.v64, nx.v,
+      gather_vertices_kernel<<<grid_for(3 * cur.nv, sms), 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.v, cur.n64, cur.n, nx.v64, nx.v,
                                                   nx.n64, nx.n, vm2, nv2, hw.ovf);
       invert_flags_kernel<<<gq, 256, 0, st>>>(rflag, cur.nq, keep);
       s.launches += 2 + scan_flags(keep, cur.nq, idx, tiles, total, st);
