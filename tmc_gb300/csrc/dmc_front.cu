@@ -134,31 +134,30 @@ __global__ void __launch_bounds__(kScanThreads) dmc_classify_kernel(CellSpace sp
   if (threadIdx.x == 0) tile_sums[blockIdx.x] = tile_sum;
 }
 
-// In-tile exclusive scan of the records -> per-cell vertex and quad offsets.
+// In-tile exclusive scan of the records -> per-cell vertex and quad offsets (striped: coalesced
+// record loads and offset stores), and one work item per vertex: the cell that generates it.
 __global__ void __launch_bounds__(kScanThreads) dmc_offsets_kernel(int64_t n, const uint32_t* rec,
                                                                   const unsigned long long* tile_off,
                                                                   int32_t* voff, int32_t* qoff, uint32_t* vwork) {
-  const int64_t base = (int64_t)blockIdx.x * kScanTile;
-  // thread t owns cells base + t*kScanItems .. + kScanItems-1 (contiguous) for the scan
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t seg = (int64_t)blockIdx.x * kScanTile + (int64_t)w * 32 * kScanItems;
   uint32_t r[kScanItems];
-  unsigned long long local = 0;
-  const int64_t mine = base + (int64_t)threadIdx.x * kScanItems;
+  unsigned long long v[kScanItems];
 #pragma unroll
   for (int s = 0; s < kScanItems; s++) {
-    r[s] = (mine + s < n) ? rec[mine + s] : 0u;
-    local += ((unsigned long long)rec_nv(r[s]) << 32) | (unsigned long long)rec_nq(r[s]);
+    const int64_t c = seg + 32 * s + lane;
+    r[s] = c < n ? rec[c] : 0u;
+    v[s] = ((unsigned long long)rec_nv(r[s]) << 32) | (unsigned long long)rec_nq(r[s]);
   }
-  unsigned long long tot;
-  unsigned long long pre = block_exclusive_scan<unsigned long long>(local, &tot) + tile_off[blockIdx.x];
+  tile_striped_exclusive_scan(v, tile_off[blockIdx.x]);
 #pragma unroll
   for (int s = 0; s < kScanItems; s++) {
-    if (mine + s < n) {
-      voff[mine + s] = (int32_t)(pre >> 32);
-      qoff[mine + s] = (int32_t)(pre & 0xffffffffull);
-      // one work item per vertex: the cell that generates it
-      for (int q = 0; q < rec_nv(r[s]); q++) vwork[(pre >> 32) + q] = (uint32_t)(mine + s);
+    const int64_t c = seg + 32 * s + lane;
+    if (c < n) {
+      voff[c] = (int32_t)(v[s] >> 32);
+      qoff[c] = (int32_t)(v[s] & 0xffffffffull);
+      for (int q = 0; q < rec_nv(r[s]); q++) vwork[(v[s] >> 32) + q] = (uint32_t)c;
     }
-    pre += ((unsigned long long)rec_nv(r[s]) << 32) | (unsigned long long)rec_nq(r[s]);
   }
 }
 

@@ -41,6 +41,36 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T* total) {
   return warp_prefix + x - v;
 }
 
+// Striped in-tile exclusive scan: warp w of the block owns the tile's cells 256w .. 256w + 255, in
+// kScanItems rounds of 32 consecutive cells (lane l takes cell 256w + 32s + l in round s), so that
+// the loads of the values and the stores of the offsets are coalesced.  v[s] is the lane's value in
+// round s; on return v[s] holds its exclusive prefix within the tile (plus `base`).
+__device__ __forceinline__ void tile_striped_exclusive_scan(unsigned long long v[kScanItems],
+                                                            unsigned long long base) {
+  __shared__ unsigned long long wsum[kScanThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long run = 0;
+#pragma unroll
+  for (int s = 0; s < kScanItems; s++) {
+    unsigned long long x = v[s];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    const unsigned long long tot = __shfl_sync(0xffffffffu, x, 31);
+    v[s] = run + x - v[s];
+    run += tot;
+  }
+  if (lane == 0) wsum[w] = run;
+  __syncthreads();
+  unsigned long long pre = base;
+  for (int q = 0; q < w; q++) pre += wsum[q];
+#pragma unroll
+  for (int s = 0; s < kScanItems; s++) v[s] += pre;
+  __syncthreads();  // wsum is reused by the block's next tile
+}
+
 // Two counters packed in one 64-bit word (high: a, low: b) scan together: both stay far below
 // 2^32 per tile, so carries never cross.
 struct Pair {

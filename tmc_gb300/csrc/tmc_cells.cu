@@ -591,24 +591,24 @@ __global__ void __launch_bounds__(128) tmc_amb_count_kernel(CellSpace space, uin
 __global__ void __launch_bounds__(kScanThreads) tmc_offsets_kernel(int64_t n, const uint32_t* rec,
                                                                   const unsigned long long* tile_off,
                                                                   int32_t* voff, int32_t* toff) {
-  const int64_t base = (int64_t)blockIdx.x * kScanTile;
-  uint32_t r[kScanItems];
-  unsigned long long local = 0;
-  const int64_t mine = base + (int64_t)threadIdx.x * kScanItems;
+  // striped in-tile scan: coalesced record loads and offset stores
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t seg = (int64_t)blockIdx.x * kScanTile + (int64_t)w * 32 * kScanItems;
+  unsigned long long v[kScanItems];
 #pragma unroll
   for (int s = 0; s < kScanItems; s++) {
-    r[s] = (mine + s < n) ? rec[mine + s] : 0u;
-    local += ((unsigned long long)trec_nv(r[s]) << 32) | (unsigned long long)trec_ntri(r[s]);
+    const int64_t c = seg + 32 * s + lane;
+    const uint32_t r = c < n ? rec[c] : 0u;
+    v[s] = ((unsigned long long)trec_nv(r) << 32) | (unsigned long long)trec_ntri(r);
   }
-  unsigned long long tot;
-  unsigned long long pre = block_exclusive_scan<unsigned long long>(local, &tot) + tile_off[blockIdx.x];
+  tile_striped_exclusive_scan(v, tile_off[blockIdx.x]);
 #pragma unroll
   for (int s = 0; s < kScanItems; s++) {
-    if (mine + s < n) {
-      voff[mine + s] = (int32_t)(pre >> 32);
-      toff[mine + s] = (int32_t)(pre & 0xffffffffull);
+    const int64_t c = seg + 32 * s + lane;
+    if (c < n) {
+      voff[c] = (int32_t)(v[s] >> 32);
+      toff[c] = (int32_t)(v[s] & 0xffffffffull);
     }
-    pre += ((unsigned long long)trec_nv(r[s]) << 32) | (unsigned long long)trec_ntri(r[s]);
   }
 }
 
