@@ -2,33 +2,53 @@
 
 namespace tmc {
 
-// One block of 1024 threads scans all tile sums: each thread owns a contiguous chunk.
+// One block of 1024 threads scans all tile sums in place.  Warp w owns a contiguous segment of
+// 32 * rounds sums and walks it in rounds of 32 consecutive sums (coalesced), carrying its running
+// sum; the warps' totals are scanned in shared memory, then each warp writes its exclusive prefixes.
 __global__ void scan_tile_sums_kernel(unsigned long long* sums, int64_t ntiles, unsigned long long* totals) {
-  constexpr int T = 1024;
-  __shared__ unsigned long long part[T];
-  const int tid = threadIdx.x;
-  const int64_t per = (ntiles + T - 1) / T;
-  const int64_t b = tid * per, e = b + per < ntiles ? b + per : ntiles;
-  unsigned long long s = 0;
-  for (int64_t i = b; i < e; i++) s += sums[i];
-  part[tid] = s;
+  constexpr int T = 1024, W = T / 32;
+  __shared__ unsigned long long wsum[W];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t rounds = (ntiles + T - 1) / T;
+  const int64_t seg = (int64_t)w * 32 * rounds;
+  unsigned long long run = 0;
+  for (int64_t r = 0; r < rounds; r++) {
+    const int64_t i = seg + 32 * r + lane;
+    unsigned long long x = i < ntiles ? sums[i] : 0ull;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    run += __shfl_sync(0xffffffffu, x, 31);
+  }
+  if (lane == 0) wsum[w] = run;
   __syncthreads();
-  // Hillis-Steele over 1024 partial sums
-  for (int o = 1; o < T; o <<= 1) {
-    unsigned long long y = (tid >= o) ? part[tid - o] : 0ull;
-    __syncthreads();
-    part[tid] += y;
-    __syncthreads();
+  if (w == 0) {
+    unsigned long long x = wsum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    wsum[lane] = x;  // inclusive
   }
-  unsigned long long run = tid ? part[tid - 1] : 0ull;
-  for (int64_t i = b; i < e; i++) {
-    const unsigned long long v = sums[i];
-    sums[i] = run;
-    run += v;
+  __syncthreads();
+  unsigned long long pre = w ? wsum[w - 1] : 0ull;
+  for (int64_t r = 0; r < rounds; r++) {
+    const int64_t i = seg + 32 * r + lane;
+    const unsigned long long v = i < ntiles ? sums[i] : 0ull;
+    unsigned long long x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (i < ntiles) sums[i] = pre + x - v;
+    pre += __shfl_sync(0xffffffffu, x, 31);
   }
-  if (tid == T - 1) totals[0] = part[T - 1];
+  if (threadIdx.x == T - 1) totals[0] = wsum[W - 1];
 }
-
 }  // namespace tmc
 
 namespace tmc {
@@ -49,24 +69,21 @@ __global__ void __launch_bounds__(kScanThreads) flag_tile_sum_kernel(const uint8
 
 __global__ void __launch_bounds__(kScanThreads) flag_offsets_kernel(const uint8_t* flags, int64_t n,
                                                                    const unsigned long long* tile_off, int32_t* out) {
-  const int64_t base = (int64_t)blockIdx.x * kScanTile;
-  const int64_t mine = base + (int64_t)threadIdx.x * kScanItems;
-  uint8_t f[kScanItems];
-  unsigned long long s = 0;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t seg = (int64_t)blockIdx.x * kScanTile + (int64_t)w * 32 * kScanItems;
+  unsigned long long v[kScanItems];
 #pragma unroll
   for (int q = 0; q < kScanItems; q++) {
-    f[q] = (mine + q < n) ? (flags[mine + q] != 0) : 0;
-    s += f[q];
+    const int64_t i = seg + 32 * q + lane;
+    v[q] = (i < n && flags[i] != 0) ? 1ull : 0ull;
   }
-  unsigned long long tot;
-  unsigned long long pre = block_exclusive_scan<unsigned long long>(s, &tot) + tile_off[blockIdx.x];
+  tile_striped_exclusive_scan(v, tile_off[blockIdx.x]);
 #pragma unroll
   for (int q = 0; q < kScanItems; q++) {
-    if (mine + q < n) out[mine + q] = (int32_t)pre;
-    pre += f[q];
+    const int64_t i = seg + 32 * q + lane;
+    if (i < n) out[i] = (int32_t)v[q];
   }
 }
-
 int64_t scan_tiles(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
 
 int scan_flags(const uint8_t* flags, int64_t n, int32_t* out, unsigned long long* tile_sums,
@@ -102,21 +119,19 @@ __global__ void __launch_bounds__(kScanThreads) i32_tile_sum_kernel(const int32_
 
 __global__ void __launch_bounds__(kScanThreads) i32_offsets_kernel(const int32_t* in, int64_t n,
                                                                   const unsigned long long* tile_off, int32_t* out) {
-  const int64_t base = (int64_t)blockIdx.x * kScanTile;
-  const int64_t mine = base + (int64_t)threadIdx.x * kScanItems;
-  int32_t v[kScanItems];
-  unsigned long long s = 0;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t seg = (int64_t)blockIdx.x * kScanTile + (int64_t)w * 32 * kScanItems;
+  unsigned long long v[kScanItems];
 #pragma unroll
   for (int q = 0; q < kScanItems; q++) {
-    v[q] = (mine + q < n) ? in[mine + q] : 0;
-    s += (unsigned long long)v[q];
+    const int64_t i = seg + 32 * q + lane;
+    v[q] = i < n ? (unsigned long long)in[i] : 0ull;
   }
-  unsigned long long tot;
-  unsigned long long pre = block_exclusive_scan<unsigned long long>(s, &tot) + tile_off[blockIdx.x];
+  tile_striped_exclusive_scan(v, tile_off[blockIdx.x]);
 #pragma unroll
   for (int q = 0; q < kScanItems; q++) {
-    if (mine + q < n) out[mine + q] = (int32_t)pre;
-    pre += (unsigned long long)v[q];
+    const int64_t i = seg + 32 * q + lane;
+    if (i < n) out[i] = (int32_t)v[q];
   }
 }
 
