@@ -710,59 +710,101 @@ __global__ void __launch_bounds__(kVertexThreads, 4) dmc_vertex_finish_kernel(Ce
 // ------------------------------------------------------------------------------------------
 // Quad corners are vertex indices within the quad's own volume: the space-wide offsets minus the
 // volume's first vertex (the scanned tile offset of its first tile; 0 for a single volume).
-__global__ void __launch_bounds__(128) dmc_quad_kernel(CellSpace space, const uint32_t* rec, const int32_t* voff,
-                                                       const int32_t* qoff, const unsigned long long* tile_off,
-                                                       int32_t* quads, uint8_t* colors) {
+// The quads a cell owns (one per crossed interior edge 0, 3, 8), from the records of the four
+// cells around each edge.
+__device__ __forceinline__ void cell_quads(const Grid& g, int32_t vfirst, int64_t vc, const uint32_t* rec,
+                                           const int32_t* voff, const int32_t* qoff, int32_t* quads,
+                                           uint8_t* colors) {
   // cell offsets (di, dj, dk) and local edge of the four cells around the owned edges 0, 3, 8
   // x edge: (0,-1,-1) e6, (0,0,-1) e4, (0,-1,0) e2, (0,0,0) e0
   // y edge: (-1,0,-1) e5, (0,0,-1) e7, (-1,0,0) e1, (0,0,0) e3
   // z edge: (-1,-1,0) e10, (0,-1,0) e11, (-1,0,0) e9, (0,0,0) e8
-  const int AX_E[3] = {0, 3, 8};
-  for (int64_t vc = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vc < space.n;
-       vc += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t r = rec[vc];
-    if (rec_nq(r) == 0) continue;  // padding records are empty
-    const Grid g = space.grid_of_tile(vc / kScanTile);
-    const int32_t vfirst = (int32_t)(tile_off[g.vbase / kScanTile] >> 32);
-    const int64_t cell = vc - g.vbase;
-    int i, j, k;
-    cell_ijk(g, cell, i, j, k);
-    const float f0 = g.at(i, j, k);
-    const int neg = !(f0 >= g.iso_up);  // first end vertex below the isovalue
-    const float fx = g.at(i + 1, j, k), fy = g.at(i, j + 1, k), fz = g.at(i, j, k + 1);
-    const bool s0 = f0 >= g.iso_up;
-    const bool crossed[3] = {s0 != (fx >= g.iso_up), s0 != (fy >= g.iso_up), s0 != (fz >= g.iso_up)};
-    int32_t q = qoff[vc];
-    const int par = (i & 1) | ((j & 1) << 1) | ((k & 1) << 2);
-    for (int a = 0; a < 3; a++) {
-      if (!crossed[a] || !edge_interior(g, i, j, k, AX_E[a])) continue;
-      int di[4], dj[4], dk[4], le[4];
-      if (a == 0) {
-        di[0] = 0; dj[0] = -1; dk[0] = -1; le[0] = 6;
-        di[1] = 0; dj[1] = 0; dk[1] = -1; le[1] = 4;
-        di[2] = 0; dj[2] = -1; dk[2] = 0; le[2] = 2;
-        di[3] = 0; dj[3] = 0; dk[3] = 0; le[3] = 0;
-      } else if (a == 1) {
-        di[0] = -1; dj[0] = 0; dk[0] = -1; le[0] = 5;
-        di[1] = 0; dj[1] = 0; dk[1] = -1; le[1] = 7;
-        di[2] = -1; dj[2] = 0; dk[2] = 0; le[2] = 1;
-        di[3] = 0; dj[3] = 0; dk[3] = 0; le[3] = 3;
-      } else {
-        di[0] = -1; dj[0] = -1; dk[0] = 0; le[0] = 10;
-        di[1] = 0; dj[1] = -1; dk[1] = 0; le[1] = 11;
-        di[2] = -1; dj[2] = 0; dk[2] = 0; le[2] = 9;
-        di[3] = 0; dj[3] = 0; dk[3] = 0; le[3] = 8;
-      }
-      int32_t qv[4];
-      for (int s = 0; s < 4; s++) {
-        const int64_t nc = g.vcell(i + di[s], j + dj[s], k + dk[s]);
-        const uint32_t rn = rec[nc];
-        qv[quad_slot(le[s], neg)] = voff[nc] - vfirst + rec_rank(rn, le[s]);
-      }
-      reinterpret_cast<int4*>(quads)[q] = make_int4(qv[0], qv[1], qv[2], qv[3]);
-      if (colors) colors[q] = (uint8_t)(3 * par + a);
-      q++;
+  const int64_t cell = vc - g.vbase;
+  int i, j, k;
+  cell_ijk(g, cell, i, j, k);
+  const float f0 = g.at(i, j, k);
+  const int neg = !(f0 >= g.iso_up);  // first end vertex below the isovalue
+  const float fx = g.at(i + 1, j, k), fy = g.at(i, j + 1, k), fz = g.at(i, j, k + 1);
+  const bool s0 = f0 >= g.iso_up;
+  const bool crossed[3] = {s0 != (fx >= g.iso_up), s0 != (fy >= g.iso_up), s0 != (fz >= g.iso_up)};
+  int32_t q = qoff[vc];
+  const int par = (i & 1) | ((j & 1) << 1) | ((k & 1) << 2);
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    if (!crossed[a] || !edge_interior(g, i, j, k, a == 0 ? 0 : (a == 1 ? 3 : 8))) continue;
+    int di[4], dj[4], dk[4], le[4];
+    if (a == 0) {
+      di[0] = 0; dj[0] = -1; dk[0] = -1; le[0] = 6;
+      di[1] = 0; dj[1] = 0; dk[1] = -1; le[1] = 4;
+      di[2] = 0; dj[2] = -1; dk[2] = 0; le[2] = 2;
+      di[3] = 0; dj[3] = 0; dk[3] = 0; le[3] = 0;
+    } else if (a == 1) {
+      di[0] = -1; dj[0] = 0; dk[0] = -1; le[0] = 5;
+      di[1] = 0; dj[1] = 0; dk[1] = -1; le[1] = 7;
+      di[2] = -1; dj[2] = 0; dk[2] = 0; le[2] = 1;
+      di[3] = 0; dj[3] = 0; dk[3] = 0; le[3] = 3;
+    } else {
+      di[0] = -1; dj[0] = -1; dk[0] = 0; le[0] = 10;
+      di[1] = 0; dj[1] = -1; dk[1] = 0; le[1] = 11;
+      di[2] = -1; dj[2] = 0; dk[2] = 0; le[2] = 9;
+      di[3] = 0; dj[3] = 0; dk[3] = 0; le[3] = 8;
     }
+    int32_t qv[4];
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+      const int64_t nc = g.vcell(i + di[s], j + dj[s], k + dk[s]);
+      const uint32_t rn = rec[nc];
+      qv[quad_slot(le[s], neg)] = voff[nc] - vfirst + rec_rank(rn, le[s]);
+    }
+    reinterpret_cast<int4*>(quads)[q] = make_int4(qv[0], qv[1], qv[2], qv[3]);
+    if (colors) colors[q] = (uint8_t)(3 * par + a);
+    q++;
+  }
+}
+
+// Each warp walks chunks of 32 consecutive cells, queues those that own quads (ballot) in shared
+// memory and processes the queue 32 cells at a time, one per lane: ~12 % of the cells own quads,
+// so a plain cell loop would leave most lanes idle.  No block barrier.
+constexpr int kQuadThreads = 256;
+template <bool kBatch>
+__global__ void __launch_bounds__(kQuadThreads) dmc_quad_kernel(CellSpace space, const uint32_t* rec,
+                                                                const int32_t* voff, const int32_t* qoff,
+                                                                const unsigned long long* tile_off, int32_t* quads,
+                                                                uint8_t* colors) {
+  constexpr int kWarps = kQuadThreads / 32;
+  __shared__ uint32_t queue[kWarps][64];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t* Q = queue[wid];
+  const int64_t n = space.n;
+  const int64_t chunks = ceil_div(n, 32);
+  int qn = 0;  // queued cells (the same on every lane)
+  for (int64_t chunk = (int64_t)blockIdx.x * kWarps + wid;; chunk += (int64_t)gridDim.x * kWarps) {
+    const bool more = chunk < chunks;
+    if (more) {
+      const int64_t c = chunk * 32 + lane;
+      const bool own = c < n && rec_nq(rec[c]) != 0;  // padding records are empty
+      const unsigned bal = __ballot_sync(0xffffffffu, own);
+      if (own) Q[qn + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)c;
+      qn += __popc(bal);
+      __syncwarp();
+    }
+    while (qn >= 32 || (!more && qn > 0)) {
+      const int take = qn < 32 ? qn : 32;
+      if (lane < take) {
+        const int64_t vc = Q[lane];
+        const Grid& g = kBatch ? space.grids[__ldg(space.tile_vol + vc / kScanTile)] : space.one;
+        const int32_t vfirst = kBatch ? (int32_t)(tile_off[g.vbase / kScanTile] >> 32) : 0;
+        cell_quads(g, vfirst, vc, rec, voff, qoff, quads, colors);
+      }
+      __syncwarp();
+      const int rest = qn - take;  // at most 31: move them to the front
+      const uint32_t x = lane < rest ? Q[take + lane] : 0u;
+      __syncwarp();
+      if (lane < rest) Q[lane] = x;
+      __syncwarp();
+      qn = rest;
+    }
+    if (!more) break;
   }
 }
 
@@ -786,7 +828,6 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
                    uint8_t* colors, int flip, const Tuning& tu, cudaStream_t st, Prof* prof) {
   const int sms = tu.sms;
   const int64_t n = space.n;
-  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 128), (int64_t)sms * 16));
   {
     // per-cell offsets and the vertex work list (needs the vertex count for its size)
     Stage t(prof, "dmc_scan", st);
@@ -827,7 +868,12 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
         space, s.voff, s.vwork, s.fb_list, s.fb_count, s.tail_list, s.fb_count + 1, warp_max, vo, flip, s.stats);
   }
   Stage t(prof, "dmc_quad", st);
-  dmc_quad_kernel<<<(unsigned)blocks, 128, 0, st>>>(space, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
+  const unsigned qb = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 32 * (kQuadThreads / 32)),
+                                                                       (int64_t)sms * 8));
+  if (space.grids)
+    dmc_quad_kernel<true><<<qb, kQuadThreads, 0, st>>>(space, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
+  else
+    dmc_quad_kernel<false><<<qb, kQuadThreads, 0, st>>>(space, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
   return 7;
 }
 
