@@ -45,7 +45,7 @@ __constant__ uint64_t c_case_contour[256] = TMC_CASE_CONTOUR_INIT;
 // eight corner loads coalesced across the block) and compacts the active cells (12 % on the 512^3
 // workload) into shared memory with warp scans; pass 2 builds their contours densely, so that the
 // polygon and edge work does not keep mostly-inactive warps busy.
-__global__ void __launch_bounds__(kScanThreads) dmc_classify_kernel(CellSpace space, uint32_t* rec,
+__global__ void __launch_bounds__(kScanThreads, 4) dmc_classify_kernel(CellSpace space, uint32_t* rec,
                                                                    unsigned long long* tile_sums,
                                                                    unsigned long long* stats) {
   __shared__ uint64_t cc[256];
