@@ -24,18 +24,26 @@ namespace tmc {
 
 namespace {
 
-__global__ void he_vertex_init_kernel(unsigned long long* hv_key, int32_t* deg, int64_t nv) {
+__global__ void he_vertex_init_kernel(unsigned long long* hv_key, int32_t* deg, int32_t* hv, int64_t nv,
+                                      unsigned long long* lone_count) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (int64_t)gridDim.x * blockDim.x) {
     hv_key[i] = 0;
     deg[i] = 0;
+    hv[i] = -1;
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *lone_count = 0;
 }
 
 // out-degrees; the degree counter's old value is the halfedge's slot in its origin's list (one
-// atomic per halfedge).  Twins and flags are written by he_twin_kernel, every entry once.
-__global__ void he_build_kernel(const int32_t* faces, int64_t nh, int32_t* deg, int32_t* rank) {
-  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x)
-    rank[h] = atomicAdd(deg + faces[h], 1);
+// atomic per halfedge).  The vertex handle is the highest halfedge with that origin (the
+// reference's last insertion): a fire-and-forget atomic maximum.  Twins and flags are written by
+// he_twin_kernel, every entry once.
+__global__ void he_build_kernel(const int32_t* faces, int64_t nh, int32_t* deg, int32_t* rank, int32_t* hv) {
+  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
+    const int v = faces[h];
+    rank[h] = atomicAdd(deg + v, 1);
+    atomicMax(hv + v, (int32_t)h);
+  }
 }
 
 __global__ void he_scatter_kernel(const int32_t* faces, int P, int64_t nf, const int32_t* off, const int32_t* rank,
@@ -46,16 +54,6 @@ __global__ void he_scatter_kernel(const int32_t* faces, int P, int64_t nf, const
     const int r = (int)(h - f * P);
     const int v0 = faces[h], v1 = faces[f * P + (r + 1) % P];
     list[off[v0] + rank[h]] = make_int2((int)h, v1);
-  }
-}
-
-// vertex handle: the highest halfedge with origin v (the reference's last insertion), -1 if none
-__global__ void he_vertex_handle_kernel(const int2* list, const int32_t* off, const int32_t* deg, int64_t nv,
-                                        int32_t* hv) {
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
-    int m = -1;
-    for (int q = off[v], e = off[v] + deg[v]; q < e; q++) m = max(m, list[q].x);
-    hv[v] = m;
   }
 }
 
@@ -87,7 +85,7 @@ __device__ __forceinline__ int edge_halfedges(const int2* list, const int32_t* o
 // halfedge writes its own (each entry is written exactly once)
 __global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const int2* list, const int32_t* off,
                                const int32_t* deg, int32_t* twin, uint8_t* flag, unsigned long long* hv_key,
-                               unsigned long long* non_manifold) {
+                               unsigned long long* non_manifold, int32_t* lone, unsigned long long* lone_count) {
   const int64_t nh = nf * P;
   unsigned long long nm = 0;
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
@@ -113,14 +111,15 @@ __global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const in
       flag[e0] = 2;
       flag[e1] = 2;
       flag[e2] = 2;
-      int lone_v;
+      int lone_v, lone_h;
       if (a0 != a1) {
-        twin[e0] = e1; twin[e1] = e0; twin[e2] = -1; lone_v = a2;
+        twin[e0] = e1; twin[e1] = e0; twin[e2] = -1; lone_v = a2; lone_h = e2;
       } else if (a0 != a2) {
-        twin[e0] = e2; twin[e2] = e0; twin[e1] = -1; lone_v = a1;
+        twin[e0] = e2; twin[e2] = e0; twin[e1] = -1; lone_v = a1; lone_h = e1;
       } else {
-        twin[e1] = e2; twin[e2] = e1; twin[e0] = -1; lone_v = a0;
+        twin[e1] = e2; twin[e2] = e1; twin[e0] = -1; lone_v = a0; lone_h = e0;
       }
+      lone[atomicAdd(lone_count, 1ull)] = lone_h;  // for the handle override
       // the last override in key order wins: remember the largest key (+1 so that 0 = none)
       const unsigned long long key = ((unsigned long long)(unsigned)min(v0, v1) << 32) | (unsigned)max(v0, v1);
       atomicMax(hv_key + lone_v, key + 1ull);
@@ -141,11 +140,12 @@ __global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const in
 }
 
 // the lone halfedge of a three-halfedge edge whose key won its origin's override sets the handle
-__global__ void he_override_kernel(const int32_t* faces, int P, int64_t nf, const int32_t* twin, const uint8_t* flag,
+// (the lone halfedges are listed by he_twin_kernel)
+__global__ void he_override_kernel(const int32_t* faces, int P, const int32_t* lone, const unsigned long long* lone_count,
                                    int32_t* hv, const unsigned long long* hv_key) {
-  const int64_t nh = nf * P;
-  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
-    if (flag[h] != 2 || twin[h] != -1) continue;
+  const int64_t n = (int64_t)*lone_count;
+  for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t h = lone[a];
     const int64_t f = h / P;
     const int r = (int)(h - f * P);
     const int v0 = faces[h], v1 = faces[f * P + (r + 1) % P];
@@ -173,15 +173,16 @@ int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& 
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)sms * 8));
   };
   int k = 0;
-  he_vertex_init_kernel<<<grid(nv), 256, 0, st>>>(w.hv_key, w.deg, nv);
-  he_build_kernel<<<grid(nh), 256, 0, st>>>(faces, nh, w.deg, w.rank);
+  // the lone-halfedge list reuses the slot array, which is dead once the lists are scattered
+  unsigned long long* lone_count = w.total + 1;
+  he_vertex_init_kernel<<<grid(nv), 256, 0, st>>>(w.hv_key, w.deg, o.hv, nv, lone_count);
+  he_build_kernel<<<grid(nh), 256, 0, st>>>(faces, nh, w.deg, w.rank, o.hv);
   k += 2 + scan_i32(w.deg, nv, w.off, w.tiles, w.total, st);
   he_scatter_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.off, w.rank, w.list);
   he_twin_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.list, w.off, w.deg, o.twin, o.flag, w.hv_key,
-                                           w.non_manifold);
-  he_vertex_handle_kernel<<<grid(nv), 256, 0, st>>>(w.list, w.off, w.deg, nv, o.hv);
-  he_override_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, o.twin, o.flag, o.hv, w.hv_key);
-  return k + 4;
+                                           w.non_manifold, w.rank, lone_count);
+  he_override_kernel<<<(unsigned)std::max(1, sms), 256, 0, st>>>(faces, P, w.rank, lone_count, o.hv, w.hv_key);
+  return k + 3;
 }
 
 int pack_halfedges4(const int32_t* faces, int P, const int32_t* twin, int64_t nh, int32_t* he4, int32_t* hf, int sms,

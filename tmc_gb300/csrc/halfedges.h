@@ -24,7 +24,7 @@ struct HeWork {
   int2* list;                       // nh: (halfedge, target vertex) grouped by origin
   unsigned long long* hv_key;       // nv
   unsigned long long* tiles;        // scan_tiles(nv)
-  unsigned long long* total;        // 1
+  unsigned long long* total;        // 2: [0] the degree scan total, [1] listed lone halfedges
   unsigned long long* non_manifold; // 1 (accumulated; zero it before a build)
 };
 
