@@ -436,7 +436,9 @@ TMC_HD void sample_coords(float lo, float hi, float out[7], int& f64_count) {
   const ff D = ffx::two_sum(hi, -lo);  // exact difference
   const int ehi = (int)((ffx::fbits(hi) >> 23) & 0xFF), elo = (int)((ffx::fbits(lo) >> 23) & 0xFF);
   const bool exact = (lo == 0.0f) || (hi == lo) || (ehi - elo <= 20 && elo > 0);
-#pragma unroll
+  // not unrolled: the set-up pass writes `out` straight into its record in global memory, and
+  // one copy of the body keeps the pass's code small (it is bound by instruction fetch)
+#pragma unroll 1
   for (int i = 1; i <= 7; i++) {
     const ff a = ffx::two_prod((float)i, D.hi);
     const ff b = ffx::two_prod((float)i, D.lo);
