@@ -300,6 +300,8 @@ __device__ __forceinline__ bool vertex_contour(const Grid& g, int i, int j, int 
 // Position, normal and local coordinates of vertex vidx at local coordinates p of cell (i, j, k).
 // p64: the float64 local coordinates when they are not the floats p (the reference's unrounded mean
 // point, for contours without any valid projection sample), else null.
+// kFF: the float-float normal path (float64 normals kept for the simplification) is compiled in
+template <bool kFF = true>
 __device__ __forceinline__ void vertex_outputs(const GridCache& G, int i, int j, int k, int64_t cell,
                                                const float p[3], const double* p64, int64_t vidx,
                                                const DmcVertexOut& out, int flip, repr::Stats& st) {
@@ -329,7 +331,7 @@ __device__ __forceinline__ void vertex_outputs(const GridCache& G, int i, int j,
       out.n[o + d] = (float)nf.n[d];
     }
     st.normal_f64++;
-  } else if (out.n64 && (g.flags & kGridNormal64)) {
+  } else if (kFF && out.n64 && (g.flags & kGridNormal64)) {
     ffx::ff Gq[8][3];
 #pragma unroll
     for (int q = 0; q < 8; q++) point_diff_ff(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), Gq[q]);
@@ -681,6 +683,7 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_project_group_kernel(const
 }
 
 // Two-pass vertices, pass 3: positions, normals and local coordinates of the projected vertices.
+template <bool kFF>
 __global__ void __launch_bounds__(kVertexThreads, 4) dmc_vertex_finish_kernel(CellSpace space, const uint32_t* vwork,
                                                                             int64_t nv, const float4* vp,
                                                                             DmcVertexOut out, int flip_all,
@@ -698,7 +701,7 @@ __global__ void __launch_bounds__(kVertexThreads, 4) dmc_vertex_finish_kernel(Ce
     int i, j, k;
     cell_ijk(g, cell, i, j, k);
     const float p[3] = {q.x, q.y, q.z};
-    vertex_outputs(G, i, j, k, cell, p, nullptr, vidx, out, flip_all | (g.flags & kGridFlip), st);
+    vertex_outputs<kFF>(G, i, j, k, cell, p, nullptr, vidx, out, flip_all | (g.flags & kGridFlip), st);
   }
   flush_stats(st, stats);
 }
@@ -854,7 +857,11 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
   }
   {
     Stage t(prof, "dmc_vertex_finish", st);
-    dmc_vertex_finish_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(space, s.vwork, nv, s.vp, vo, flip, s.stats);
+    // the float-float normals only when some volume keeps float64 normals (simplification)
+    if (vo.n64)
+      dmc_vertex_finish_kernel<true><<<(unsigned)vb, kVertexThreads, 0, st>>>(space, s.vwork, nv, s.vp, vo, flip, s.stats);
+    else
+      dmc_vertex_finish_kernel<false><<<(unsigned)vb, kVertexThreads, 0, st>>>(space, s.vwork, nv, s.vp, vo, flip, s.stats);
   }
   {
     // the listed vertices: one thread each with every float64 fallback, the 26x26 retries one warp

@@ -749,6 +749,7 @@ __global__ void __launch_bounds__(128) tmc_ambiguous_kernel(CellSpace space, con
 
 // One active cell: its owned edge vertices and (unambiguous case) its table triangles; ambiguous
 // cells go to the list of the float64 pass.
+template <bool kPos64>
 __device__ __forceinline__ void emit_cell(const Grid& g, int32_t vfirst, int64_t vcell, const uint32_t* rec,
                                           const int32_t* voff, const int32_t* toff, const TmcVertexOut& out,
                                           int32_t* tris, uint32_t* amb_list, unsigned* amb_count) {
@@ -768,7 +769,7 @@ __device__ __forceinline__ void emit_cell(const Grid& g, int32_t vfirst, int64_t
   int rank = 0;
   for (uint32_t mo = em & own; mo; mo &= mo - 1, rank++) {
     const int e = __ffs(mo) - 1;
-    if (out.v64 && (g.flags & kGridPos64)) edge_vertex_f64(g, i, j, k, e, u, out, vbase + rank);
+    if (kPos64 && out.v64 && (g.flags & kGridPos64)) edge_vertex_f64(g, i, j, k, e, u, out, vbase + rank);
     else {
       const float inv2[3] = {g.inv2f[0], g.inv2f[1], g.inv2f[2]};
       const float inv[3] = {2 * inv2[0], 2 * inv2[1], 2 * inv2[2]};  // = fl(1/spacing): doubling is exact
@@ -797,7 +798,9 @@ __device__ __forceinline__ void emit_cell(const Grid& g, int32_t vfirst, int64_t
 // shared memory (ballot + popcount), and processes the queue 32 cells at a time, one per lane: all
 // lanes busy, and no block barrier (warps never wait for one another).
 constexpr int kEmitThreads = 256;
-template <bool kBatch>
+// kPos64: some volume of the launch wants float64 positions (the float64 edge-vertex path is
+// compiled only into that instantiation, which keeps the common one's code small)
+template <bool kBatch, bool kPos64>
 __global__ void __launch_bounds__(kEmitThreads, 4) tmc_emit_kernel(CellSpace space, const uint32_t* rec,
                                                                    const int32_t* voff, const int32_t* toff,
                                                                    const unsigned long long* tile_off,
@@ -827,7 +830,7 @@ __global__ void __launch_bounds__(kEmitThreads, 4) tmc_emit_kernel(CellSpace spa
         // the cell's volume: read in place (a batch's grid table, or the launch parameter)
         const Grid& g = kBatch ? space.grids[__ldg(space.tile_vol + vcell / kScanTile)] : space.one;
         const int32_t vfirst = kBatch ? (int32_t)(tile_off[g.vbase / kScanTile] >> 32) : 0;
-        emit_cell(g, vfirst, vcell, rec, voff, toff, out, tris, amb_list, amb_count);
+        emit_cell<kPos64>(g, vfirst, vcell, rec, voff, toff, out, tris, amb_list, amb_count);
       }
       __syncwarp();
       const int rest = qn - take;  // at most 31: move them to the front
@@ -876,12 +879,18 @@ int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tr
     const int64_t blocks = std::max<int64_t>(
         1, std::min<int64_t>(ceil_div(space.n, 32 * (kEmitThreads / 32)), (int64_t)sms * tu.emit_blocks_per_sm));
     cudaMemsetAsync(s.amb_count, 0, sizeof(unsigned), st);
-    if (space.grids)
-      tmc_emit_kernel<true><<<(unsigned)blocks, kEmitThreads, 0, st>>>(space, s.rec, s.voff, s.toff, s.tile_sums, vo,
-                                                                       tris, s.amb_list, s.amb_count);
-    else
-      tmc_emit_kernel<false><<<(unsigned)blocks, kEmitThreads, 0, st>>>(space, s.rec, s.voff, s.toff, s.tile_sums, vo,
-                                                                        tris, s.amb_list, s.amb_count);
+#define TMC_EMIT(B, P)                                                                                       \
+  tmc_emit_kernel<B, P><<<(unsigned)blocks, kEmitThreads, 0, st>>>(space, s.rec, s.voff, s.toff, s.tile_sums, vo, \
+                                                                  tris, s.amb_list, s.amb_count)
+    const bool pos64 = vo.v64 != nullptr;
+    if (space.grids) {
+      if (pos64) TMC_EMIT(true, true);
+      else TMC_EMIT(true, false);
+    } else {
+      if (pos64) TMC_EMIT(false, true);
+      else TMC_EMIT(false, false);
+    }
+#undef TMC_EMIT
   }
   Stage t2(prof, "tmc_ambiguous", st);
   tmc_ambiguous_kernel<<<(unsigned)std::max<int64_t>(1, (int64_t)sms * 8), 128, 0, st>>>(
