@@ -593,7 +593,6 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   hw.flag = pool.get<uint8_t>(4 * NQ);
   hw.hv = pool.get<int32_t>(NV);
   hw.w.deg = pool.get<int32_t>(NV);
-  hw.w.cnt = pool.get<int32_t>(NV);
   hw.w.off = pool.get<int32_t>(NV);
   hw.w.rank = pool.get<int32_t>(4 * NQ);
   hw.w.list = pool.get<int2>(4 * NQ);

@@ -12,11 +12,11 @@
 // The vertex handle he_v[v] is the last halfedge (in index order) with origin v, overridden by the
 // three-halfedge rule in edge-key order (key = min vertex << 32 | max vertex).
 //
-// GPU scheme: no hash table.  Halfedges are bucketed under the smaller end vertex of their edge
-// (counting sort: bucket count, exclusive scan, scatter of (halfedge, larger end) pairs), so all
-// halfedges of edge {a, b} are the entries of bucket min(a, b) with partner max(a, b): one short,
-// spatially coherent list per edge, read mostly from L2.  Sorting the few ids of an edge restores
-// the reference's insertion order.
+// GPU scheme: no hash table.  Halfedges are bucketed by origin vertex (counting sort: degree
+// count, exclusive scan, scatter of (halfedge, target) pairs), so the halfedges of edge {a, b} are
+// the entries of a's list with target b and of b's list with target a.  Vertex lists are short
+// (valence ~4) and spatially coherent, so the pairing pass reads mostly from L2.  Sorting the few
+// ids of an edge restores the reference's insertion order.
 #include "halfedges.h"
 #include "scan.cuh"
 
@@ -24,31 +24,25 @@ namespace tmc {
 
 namespace {
 
-__global__ void he_vertex_init_kernel(unsigned long long* hv_key, int32_t* deg, int32_t* cnt, int32_t* hv, int64_t nv,
+__global__ void he_vertex_init_kernel(unsigned long long* hv_key, int32_t* deg, int32_t* hv, int64_t nv,
                                       unsigned long long* lone_count) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (int64_t)gridDim.x * blockDim.x) {
     hv_key[i] = 0;
     deg[i] = 0;
-    cnt[i] = 0;
     hv[i] = -1;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) *lone_count = 0;
 }
 
-// Bucket counts: the bucket counter's old value is the halfedge's slot in bucket min(origin,
-// target) (one returning atomic per halfedge).  Out-degrees and the vertex handle (the highest
-// halfedge with that origin: the reference's last insertion) are fire-and-forget atomics.  Twins
-// and flags are written by he_twin_kernel, every entry once.
-__global__ void he_build_kernel(const int32_t* faces, int P, int64_t nf, int32_t* deg, int32_t* cnt, int32_t* rank,
-                                int32_t* hv) {
-  const int64_t nh = nf * P;
+// out-degrees; the degree counter's old value is the halfedge's slot in its origin's list (one
+// atomic per halfedge).  The vertex handle is the highest halfedge with that origin (the
+// reference's last insertion): a fire-and-forget atomic maximum.  Twins and flags are written by
+// he_twin_kernel, every entry once.
+__global__ void he_build_kernel(const int32_t* faces, int64_t nh, int32_t* deg, int32_t* rank, int32_t* hv) {
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t f = h / P;
-    const int r = (int)(h - f * P);
-    const int a = faces[h], b = faces[f * P + (r + 1) % P];
-    rank[h] = atomicAdd(cnt + min(a, b), 1);
-    atomicAdd(deg + a, 1);
-    atomicMax(hv + a, (int32_t)h);
+    const int v = faces[h];
+    rank[h] = atomicAdd(deg + v, 1);
+    atomicMax(hv + v, (int32_t)h);
   }
 }
 
@@ -58,19 +52,24 @@ __global__ void he_scatter_kernel(const int32_t* faces, int P, int64_t nf, const
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
     const int64_t f = h / P;
     const int r = (int)(h - f * P);
-    const int a = faces[h], b = faces[f * P + (r + 1) % P];
-    list[off[min(a, b)] + rank[h]] = make_int2((int)h, max(a, b));
+    const int v0 = faces[h], v1 = faces[f * P + (r + 1) % P];
+    list[off[v0] + rank[h]] = make_int2((int)h, v1);
   }
 }
 
 // ids of all halfedges of the undirected edge {a, b} (sorted); returns their number (capped at 8)
-__device__ __forceinline__ int edge_halfedges(const int2* list, const int32_t* off, const int32_t* cnt, int a, int b,
+__device__ __forceinline__ int edge_halfedges(const int2* list, const int32_t* off, const int32_t* deg, int a, int b,
                                               int id[8]) {
-  const int lo = min(a, b), hi = max(a, b);
   int c = 0;
-  for (int q = off[lo], e = off[lo] + cnt[lo]; q < e; q++) {
+  for (int q = off[a], e = off[a] + deg[a]; q < e; q++) {
     const int2 x = list[q];
-    if (x.y == hi && c < 8) id[c++] = x.x;
+    if (x.y == b && c < 8) id[c++] = x.x;
+  }
+  if (a != b) {
+    for (int q = off[b], e = off[b] + deg[b]; q < e; q++) {
+      const int2 x = list[q];
+      if (x.y == a && c < 8) id[c++] = x.x;
+    }
   }
   for (int x = 1; x < c; x++)
     for (int y = x; y > 0 && id[y - 1] > id[y]; y--) {
@@ -85,7 +84,7 @@ __device__ __forceinline__ int edge_halfedges(const int2* list, const int32_t* o
 // the edge's lowest halfedge, which writes the twins and flags of all of them; every other
 // halfedge writes its own (each entry is written exactly once)
 __global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const int2* list, const int32_t* off,
-                               const int32_t* cnt, int32_t* twin, uint8_t* flag, unsigned long long* hv_key,
+                               const int32_t* deg, int32_t* twin, uint8_t* flag, unsigned long long* hv_key,
                                unsigned long long* non_manifold, int32_t* lone, unsigned long long* lone_count) {
   const int64_t nh = nf * P;
   unsigned long long nm = 0;
@@ -94,7 +93,7 @@ __global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const in
     const int r = (int)(h - f * P);
     const int v0 = faces[h], v1 = faces[f * P + (r + 1) % P];
     int id[8];
-    const int c = edge_halfedges(list, off, cnt, v0, v1, id);
+    const int c = edge_halfedges(list, off, deg, v0, v1, id);
     if (c == 2) {
       twin[h] = (id[0] == (int)h) ? id[1] : id[0];
       flag[h] = 0;
@@ -176,11 +175,11 @@ int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& 
   int k = 0;
   // the lone-halfedge list reuses the slot array, which is dead once the lists are scattered
   unsigned long long* lone_count = w.total + 1;
-  he_vertex_init_kernel<<<grid(nv), 256, 0, st>>>(w.hv_key, w.deg, w.cnt, o.hv, nv, lone_count);
-  he_build_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.deg, w.cnt, w.rank, o.hv);
-  k += 2 + scan_i32(w.cnt, nv, w.off, w.tiles, w.total, st);
+  he_vertex_init_kernel<<<grid(nv), 256, 0, st>>>(w.hv_key, w.deg, o.hv, nv, lone_count);
+  he_build_kernel<<<grid(nh), 256, 0, st>>>(faces, nh, w.deg, w.rank, o.hv);
+  k += 2 + scan_i32(w.deg, nv, w.off, w.tiles, w.total, st);
   he_scatter_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.off, w.rank, w.list);
-  he_twin_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.list, w.off, w.cnt, o.twin, o.flag, w.hv_key,
+  he_twin_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.list, w.off, w.deg, o.twin, o.flag, w.hv_key,
                                            w.non_manifold, w.rank, lone_count);
   he_override_kernel<<<(unsigned)std::max(1, sms), 256, 0, st>>>(faces, P, w.rank, lone_count, o.hv, w.hv_key);
   return k + 3;

@@ -18,15 +18,14 @@ struct HeOut {
 
 // scratch for build_halfedges, sized for nv vertices and nh halfedges
 struct HeWork {
-  int32_t* deg;                     // nv: out-degrees (the simplification's valences)
-  int32_t* off;                     // nv: first slot of each bucket
-  int32_t* rank;                    // nh: slot of each halfedge in its bucket
-  int2* list;                       // nh: (halfedge, larger end vertex) grouped by the smaller end
+  int32_t* deg;                     // nv
+  int32_t* off;                     // nv
+  int32_t* rank;                    // nh: slot of each halfedge in its origin's list
+  int2* list;                       // nh: (halfedge, target vertex) grouped by origin
   unsigned long long* hv_key;       // nv
   unsigned long long* tiles;        // scan_tiles(nv)
   unsigned long long* total;        // 2: [0] the degree scan total, [1] listed lone halfedges
   unsigned long long* non_manifold; // 1 (accumulated; zero it before a build)
-  int32_t* cnt;                     // nv: halfedges bucketed under v (edges whose smaller end is v)
 };
 
 // Returns the number of kernels launched.

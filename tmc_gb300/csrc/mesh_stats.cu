@@ -417,7 +417,7 @@ extern "C" tmc_status tmc_mesh_check(tmc_ctx* ctx, const tmc_mesh* mesh, int32_t
   HeOut ho{(int32_t*)get(nh * 4), (uint8_t*)get(nh), (int32_t*)get(nv * 4)};
   HeWork w{(int32_t*)get(nv * 4), (int32_t*)get(nv * 4), (int32_t*)get(nh * 4), (int2*)get(nh * 8),
            (unsigned long long*)get(nv * 8), (unsigned long long*)get((scan_tiles(nv) + 2) * 8),
-           (unsigned long long*)get(16), (unsigned long long*)get(16), (int32_t*)get(nv * 4)};
+           (unsigned long long*)get(16), (unsigned long long*)get(16)};
   int32_t* parent = (int32_t*)get(nf * 4);
   uint8_t* vbound = (uint8_t*)get(nv);
   unsigned long long* counts = (unsigned long long*)get(8 * 8);

@@ -597,7 +597,6 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
     uint8_t* flag = nullptr;
     tmc::HeWork w{};
     TMC_CUDA(ctx, al.get(&w.deg, nv));
-    TMC_CUDA(ctx, al.get(&w.cnt, nv));
     TMC_CUDA(ctx, al.get(&w.off, nv));
     TMC_CUDA(ctx, al.get(&w.rank, nh));
     TMC_CUDA(ctx, al.get(&w.list, nh));
@@ -860,7 +859,6 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
         uint8_t* flag = nullptr;
         tmc::HeWork w{};
         TMC_CUDA(ctx, al.get(&w.deg, nv));
-        TMC_CUDA(ctx, al.get(&w.cnt, nv));
         TMC_CUDA(ctx, al.get(&w.off, nv));
         TMC_CUDA(ctx, al.get(&w.rank, nh));
         TMC_CUDA(ctx, al.get(&w.list, nh));
