@@ -255,7 +255,6 @@ __device__ AmbResult p_slice_dev(unsigned ic, const double F[8], double iso, con
       }
     }
     if (geo) {
-#pragma unroll 1
       for (int s = 0; s < 6; s++) {
         double hp[3], hn[3];
         cell_trilinear3(P, hvt[s][0], hvt[s][1], hvt[s][2], hp);
@@ -280,7 +279,6 @@ __device__ AmbResult p_slice_dev(unsigned ic, const double F[8], double iso, con
           double dist = 1000.;
           const int ci = cnt_edge(c, flat + r);
           const double ue = e_vert(ecoord, ci, 0), ve = e_vert(ecoord, ci, 1), we = e_vert(ecoord, ci, 2);
-#pragma unroll 1
           for (int s = 0; s < 6; s++) {
             const double uval = ue - hvt[s][0], vval = ve - hvt[s][1], wval = we - hvt[s][2];
             const double val = uval * uval + vval * vval + wval * wval;
@@ -348,7 +346,6 @@ __device__ AmbResult p_slice_dev(unsigned ic, const double F[8], double iso, con
     for (int t = 0; t < cnt; t++) {
       const int sz = cnt_size(c, t);
       int e[6];
-#pragma unroll 1
       for (int q = 0; q < 6; q++) e[q] = (q < sz) ? vid[cnt_edge(c, flat + q)] : -1;
       switch (sz) {
         case 3: tri.put(e[0], e[1], e[2]); break;
@@ -435,8 +432,6 @@ __device__ void load_amb_cell(const Grid& g, int i, int j, int k, const float u[
                               bool geometry) {
 #pragma unroll
   for (int q = 0; q < 8; q++) a.F[q] = u[q];
-  // rolled loops: the float64 bodies are large and the cell record lives in local memory anyway
-#pragma unroll 1
   for (int e = 0; e < 12; e++) {
     a.ec[e] = 0;
     if (emask & (1u << e)) {
@@ -445,7 +440,6 @@ __device__ void load_amb_cell(const Grid& g, int i, int j, int k, const float u[
     }
   }
   if (geometry) {
-#pragma unroll 1
     for (int q = 0; q < 8; q++) {
       const int ii = i + (q & 1), jj = j + ((q >> 1) & 1), kk = k + ((q >> 2) & 1);
       a.P[q][0] = g.ox + ii * g.dx;
