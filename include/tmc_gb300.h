@@ -236,6 +236,10 @@ typedef struct tmc_server_opts {
   size_t hbm_budget;  /* device bytes admitted requests may use at once, by estimate (0 = 120 GiB) */
   int32_t workers;    /* batches in flight, one CUDA stream each (0 = 2) */
   int32_t max_batch;  /* requests per batch (0 = 64) */
+  int32_t reserved;
+  int64_t max_batch_cells; /* cells per batch (0 = 2^25); a larger request runs alone.  The requests of
+                              a batch complete together: the cap bounds how long a small request
+                              waits for the large ones batched with it */
 } tmc_server_opts;
 tmc_status tmc_server_create(int device, const tmc_server_opts* opts, tmc_server** out);
 tmc_status tmc_server_destroy(tmc_server* server);

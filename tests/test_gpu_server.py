@@ -94,6 +94,20 @@ def test_server_admission_by_budget(ctx):
         _same(got[q], _alone(ctx, vol, algo, flags), f"request {q}")
 
 
+def test_server_batch_cell_cap(ctx):
+    """A cell cap below every request's size puts each request in a batch of its own; results unchanged."""
+    reqs = _requests()[:5]
+    srv = native.Server(0, workers=2, max_batch_cells=1)
+    try:
+        got = _serve(srv, reqs, threads=2)
+        st = srv.stats()
+    finally:
+        srv.close()
+    assert st[5] == 1  # largest batch
+    for q, (vol, algo, flags) in enumerate(reqs):
+        _same(got[q], _alone(ctx, vol, algo, flags), f"request {q}")
+
+
 def test_server_poll_wait_and_errors():
     vol = V.small_noise_volume(24, seed=5)
     tv = native.make_volume(vol)

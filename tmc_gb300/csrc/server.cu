@@ -33,6 +33,7 @@ namespace {
 struct Ticket {
   tmc_request req{};
   int64_t est = 0;       // admitted bytes
+  int64_t cells = 0;     // the request's cells (batch size cap)
   bool done = false;
   tmc_status status = TMC_OK;
   std::string err;
@@ -85,6 +86,7 @@ struct tmc_server {
   int device = 0;
   int64_t budget = 0;
   int max_batch = 64;
+  int64_t max_batch_cells = (int64_t)1 << 25;
   std::mutex m;
   std::condition_variable cv_work, cv_done;
   std::deque<int64_t> pending;
@@ -108,12 +110,16 @@ struct tmc_server {
         std::unique_lock<std::mutex> lk(m);
         cv_work.wait(lk, [&] { return stop || !pending.empty(); });
         if (stop && pending.empty()) return;
-        // admit the oldest requests while the budget and the batch limit allow
+        // admit the oldest requests while the budget and the batch limits allow: a batch's requests
+        // complete together, so the cell cap keeps small requests from waiting for a large one
+        int64_t batch_cells = 0;
         while (!pending.empty() && (int)batch.size() < max_batch) {
           Ticket& t = tickets[pending.front()];
+          if (!batch.empty() && batch_cells + t.cells > max_batch_cells) break;
           if (!batch.empty() && in_flight + t.est > budget) break;
           if (batch.empty() && in_flight > 0 && in_flight + t.est > budget) break;  // wait for memory
           in_flight += t.est;
+          batch_cells += t.cells;
           batch.push_back(pending.front());
           pending.pop_front();
         }
@@ -187,6 +193,7 @@ tmc_status tmc_server_create(int device, const tmc_server_opts* opts, tmc_server
   const int nworkers = (opts && opts->workers > 0) ? opts->workers : 2;
   s->budget = (opts && opts->hbm_budget) ? (int64_t)opts->hbm_budget : (int64_t)120 << 30;
   s->max_batch = (opts && opts->max_batch > 0) ? opts->max_batch : 64;
+  s->max_batch_cells = (opts && opts->max_batch_cells > 0) ? opts->max_batch_cells : (int64_t)1 << 25;
   for (int w = 0; w < nworkers; w++) {
     Worker* W = new (std::nothrow) Worker();
     if (!W) {
@@ -242,6 +249,7 @@ tmc_status tmc_server_submit(tmc_server* s, const tmc_request* req, int64_t* tic
     Ticket& t = s->tickets[id];
     t.req = *req;
     t.est = estimate_bytes(*req);
+    t.cells = (int64_t)(req->vol.nx - 1) * (req->vol.ny - 1) * (req->vol.nz - 1);
     s->pending.push_back(id);
     s->n_submitted++;
     *ticket = id;

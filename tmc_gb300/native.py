@@ -97,7 +97,8 @@ class Request(ctypes.Structure):
 
 
 class ServerOpts(ctypes.Structure):
-    _fields_ = [("hbm_budget", ctypes.c_size_t), ("workers", ctypes.c_int32), ("max_batch", ctypes.c_int32)]
+    _fields_ = [("hbm_budget", ctypes.c_size_t), ("workers", ctypes.c_int32), ("max_batch", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("max_batch_cells", ctypes.c_int64)]
 
 
 _lib = None
@@ -415,10 +416,11 @@ class Context:
 class Server:
     """tmc_server_*: continuous batching of requests on one GPU (thread-safe submit / wait)."""
 
-    def __init__(self, device: int = 0, hbm_budget: int = 0, workers: int = 0, max_batch: int = 0):
+    def __init__(self, device: int = 0, hbm_budget: int = 0, workers: int = 0, max_batch: int = 0,
+                 max_batch_cells: int = 0):
         self.lib = load()
         self.h = ctypes.c_void_p()
-        opts = ServerOpts(hbm_budget, workers, max_batch)
+        opts = ServerOpts(hbm_budget, workers, max_batch, 0, max_batch_cells)
         st = self.lib.tmc_server_create(device, ctypes.byref(opts), ctypes.byref(self.h))
         if st != TMC_OK:
             raise TmcError(st, "tmc_server_create failed")
