@@ -50,7 +50,9 @@ typedef struct tmc_ctx tmc_ctx;
 typedef struct tmc_ctx_opts {
   size_t reserve_bytes; /* device memory the context keeps pooled between calls (0 = default) */
   int32_t check_numeric; /* 1: scan the field for NaN/Inf and fail with TMC_ERR_NUMERIC */
-  int32_t reserved;
+  /* stream priority of the context's work: 0 = default; a negative value lets its kernels take
+   * SMs ahead of other streams' work (clamped to cudaDeviceGetStreamPriorityRange) */
+  int32_t priority;
 } tmc_ctx_opts;
 
 /* A uniform grid: point (i,j,k) sits at origin + (i,j,k)*spacing; data[(k*ny + j)*nx + i]. */

@@ -263,4 +263,12 @@ struct Tuning {
   }
 };
 
+// Classification may start before the whole field is on the device (a host field copied in z
+// slabs): the scan tiles below tile_end may run once `ready` has completed.  Gates come in order,
+// the last one covers every tile.
+struct TileGate {
+  int64_t tile_end;
+  cudaEvent_t ready;
+};
+
 }  // namespace tmc

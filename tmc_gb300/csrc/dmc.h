@@ -41,7 +41,10 @@ constexpr size_t kProjRecordBytes = 144;  // sizeof(repr::ProjRecord)
 // Each launcher returns the number of kernels it launched.
 // Per-cell scratch is indexed in the cell space (space.n cells, padding included).
 int64_t dmc_tiles(const CellSpace& space);  // scan tiles of the space
-int dmc_front_count(const CellSpace& space, DmcScratch& s, cudaStream_t st, Prof* prof = nullptr);
+// gates: classify the tiles of each gate once its event has completed (a host field arriving in
+// slabs); none: the whole field is on the device
+int dmc_front_count(const CellSpace& space, DmcScratch& s, cudaStream_t st, Prof* prof = nullptr,
+                    const TileGate* gates = nullptr, int ngates = 0);
 // Quads hold vertex indices within their own volume; vertices and quads of the volumes follow one
 // another in the output arrays.
 int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64_t nv, int32_t* quads,

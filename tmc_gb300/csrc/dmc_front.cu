@@ -45,9 +45,10 @@ __constant__ uint64_t c_case_contour[256] = TMC_CASE_CONTOUR_INIT;
 // eight corner loads coalesced across the block) and compacts the active cells (12 % on the 512^3
 // workload) into shared memory with warp scans; pass 2 builds their contours densely, so that the
 // polygon and edge work does not keep mostly-inactive warps busy.
-__global__ void __launch_bounds__(kScanThreads, 4) dmc_classify_kernel(CellSpace space, uint32_t* rec,
+__global__ void __launch_bounds__(kScanThreads, 4) dmc_classify_kernel(CellSpace space, int64_t tile0, uint32_t* rec,
                                                                    unsigned long long* tile_sums,
                                                                    unsigned long long* stats) {
+  const int64_t tile = tile0 + blockIdx.x;
   __shared__ uint64_t cc[256];
   __shared__ uint16_t act_list[kScanTile];
   __shared__ uint8_t case_of[kScanTile];
@@ -56,9 +57,9 @@ __global__ void __launch_bounds__(kScanThreads, 4) dmc_classify_kernel(CellSpace
   __shared__ unsigned long long tile_sum;
   for (int c = threadIdx.x; c < 256; c += blockDim.x) cc[c] = c_case_contour[c];
   if (threadIdx.x == 0) tile_sum = 0;
-  const Grid g = space.grid_of_tile(blockIdx.x);
+  const Grid g = space.grid_of_tile(tile);
   const int64_t n = g.ncells();
-  const int64_t vbase = (int64_t)blockIdx.x * kScanTile;  // first cell of the tile in the space
+  const int64_t vbase = tile * kScanTile;  // first cell of the tile in the space
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   // pass 1: cases; inactive records are final here
   bool act[kScanItems];
@@ -131,7 +132,7 @@ __global__ void __launch_bounds__(kScanThreads, 4) dmc_classify_kernel(CellSpace
   if (lane == 0 && amb) atomicAdd(stats + 1, amb);
   if (lane == 0 && nact) atomicAdd(stats + 0, nact);
   __syncthreads();
-  if (threadIdx.x == 0) tile_sums[blockIdx.x] = tile_sum;
+  if (threadIdx.x == 0) tile_sums[tile] = tile_sum;
 }
 
 // In-tile exclusive scan of the records -> per-cell vertex and quad offsets (striped: coalesced
@@ -814,15 +815,29 @@ __global__ void __launch_bounds__(kQuadThreads) dmc_quad_kernel(CellSpace space,
 // ------------------------------------------------------------------------------------------
 // host-side launches
 // ------------------------------------------------------------------------------------------
-int dmc_front_count(const CellSpace& space, DmcScratch& s, cudaStream_t st, Prof* prof) {
+int dmc_front_count(const CellSpace& space, DmcScratch& s, cudaStream_t st, Prof* prof, const TileGate* gates,
+                    int ngates) {
   const int64_t tiles = ceil_div(space.n, kScanTile);
+  int k = 0;
   {
     Stage t(prof, "dmc_classify", st);
-    dmc_classify_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(space, s.rec, s.tile_sums, s.stats);
+    auto classify = [&](int64_t t0, int64_t t1) {
+      if (t1 <= t0) return;
+      dmc_classify_kernel<<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(space, t0, s.rec, s.tile_sums, s.stats);
+      k++;
+    };
+    if (ngates == 0) classify(0, tiles);
+    int64_t t0 = 0;
+    for (int q = 0; q < ngates; q++) {
+      cudaStreamWaitEvent(st, gates[q].ready, 0);
+      const int64_t t1 = (q == ngates - 1) ? tiles : std::min(gates[q].tile_end, tiles);
+      classify(t0, t1);
+      t0 = std::max(t0, t1);
+    }
   }
   Stage t(prof, "dmc_scan", st);
   scan_tile_sums_kernel<<<1, 1024, 0, st>>>(s.tile_sums, tiles, s.totals);
-  return 2;
+  return k + 1;
 }
 
 int64_t dmc_tiles(const CellSpace& space) { return ceil_div(space.n, kScanTile); }

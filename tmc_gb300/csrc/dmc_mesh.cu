@@ -577,7 +577,7 @@ struct HeBufs {
 }  // namespace
 
 DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaStream_t st, DmcPostOut* out,
-                              unsigned long long* h_cnt, Prof* prof, bool borrowed) {
+                              unsigned long long* h_cnt, Prof* prof, bool borrowed, const ReadyFn* ready) {
   DmcPostStatus s;
   out->mesh = in;
   const bool c3x3y = flags & TMC_DMC_P3X3Y_COLOR, i3x3y = flags & TMC_DMC_P3X3Y_ISOLATED,
@@ -822,6 +822,12 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     }
   }
   // ---- final halfedges and triangles ----
+  if (s.err == cudaSuccess && ready) {
+    (*ready)(cur.v, (size_t)cur.nv * 3 * sizeof(float));
+    (*ready)(cur.n, (size_t)cur.nv * 3 * sizeof(float));
+    if (flags & TMC_OUT_POS_F64) (*ready)(cur.v64, (size_t)cur.nv * 3 * sizeof(double));
+    (*ready)(cur.quads, (size_t)cur.nq * 4 * sizeof(int32_t));
+  }
   if (s.err == cudaSuccess && want_he) {
     halfedges(cur);
     void *he4 = nullptr, *hv = nullptr, *hf = nullptr;
@@ -833,6 +839,11 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
       adopt(hf);
       s.launches += pack_halfedges4(cur.quads, 4, hw.twin, 4 * cur.nq, (int32_t*)he4, (int32_t*)hf, sms, st);
       cudaMemcpyAsync(hv, hw.hv, cur.nv * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+      if (ready) {
+        (*ready)(he4, (size_t)cur.nq * 16 * sizeof(int32_t));
+        (*ready)(hv, (size_t)cur.nv * sizeof(int32_t));
+        (*ready)(hf, (size_t)cur.nq * sizeof(int32_t));
+      }
       cudaMemcpyAsync(h_cnt + 1, hw.nm, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
       cudaStreamSynchronize(st);
       out->non_manifold = (int64_t)h_cnt[1];
@@ -855,6 +866,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
                                                                       tcount);
         triangles_kernel<<<grid_for(cur.nq, sms), 256, 0, st>>>(cur.quads, tlist, tcount, cur.v64, (int32_t*)tr);
         s.launches += 2;
+        if (ready) (*ready)(tr, (size_t)cur.nq * 6 * sizeof(int32_t));
       }
       out->nt = 2 * cur.nq;
       out->tris = (int32_t*)tr;

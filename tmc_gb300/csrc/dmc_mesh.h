@@ -2,6 +2,7 @@
 // simplification, quad -> triangle split).
 #pragma once
 #include <cstdint>
+#include <functional>
 #include <vector>
 #include <cuda_runtime.h>
 
@@ -36,10 +37,17 @@ struct DmcPostStatus {
   int launches = 0;
 };
 
+// Receives result arrays (device pointer, bytes) as soon as no later kernel of the post-processing
+// writes them, in the stream order of `st`: the final vertices (float32 positions and normals, and
+// float64 positions with TMC_OUT_POS_F64) and quads before the final halfedges are built, then the
+// halfedge arrays, then the triangles.  The caller may start copying them out.
+using ReadyFn = std::function<void(const void* dev, size_t bytes)>;
+
 // borrowed: the input arrays belong to the caller (e.g. slices of a batch's shared arrays) and are
 // never freed here; they are still listed in out->freed once the result no longer uses them.
 // h_staging: pinned host memory for 4 words (counts read back between the passes).
 DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaStream_t st, DmcPostOut* out,
-                              unsigned long long* h_staging, Prof* prof = nullptr, bool borrowed = false);
+                              unsigned long long* h_staging, Prof* prof = nullptr, bool borrowed = false,
+                              const ReadyFn* ready = nullptr);
 
 }  // namespace tmc

@@ -26,6 +26,12 @@ struct tmc_ctx {
   int sms = 0;
   tmc::Tuning tune;                       // launch shapes (defaults from the SM count)
   cudaStream_t stream = nullptr;
+  // device-to-host copies of result arrays that are final before the call ends, so that they
+  // overlap the call's remaining kernels (created on first use, same priority as `stream`)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_event = nullptr;
+  std::vector<cudaEvent_t> slab_events;   // arrival of the slabs of a host field (field_slabs)
+  int priority = 0;
   cudaMemPool_t pool = nullptr;
   tmc_ctx_opts opts{};
   std::string err;
@@ -145,16 +151,90 @@ tmc_status check_volume(tmc_ctx* ctx, const tmc_volume* vol) {
   return TMC_OK;
 }
 
+// The context's copy stream and its event (created on first use).
+cudaError_t ensure_copy_stream(tmc_ctx* ctx) {
+  cudaError_t e = cudaSuccess;
+  if (!ctx->copy_stream &&
+      (e = cudaStreamCreateWithPriority(&ctx->copy_stream, cudaStreamNonBlocking, ctx->priority)) != cudaSuccess)
+    return e;
+  if (!ctx->copy_event) e = cudaEventCreateWithFlags(&ctx->copy_event, cudaEventDisableTiming);
+  return e;
+}
+
+// TMC_ERR_NUMERIC: any NaN or Inf in the field sets *flag
+__global__ void nonfinite_kernel(const float* f, int64_t n, unsigned* flag) {
+  bool bad = false;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    bad |= !isfinite(f[i]);
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) *flag = 1u;
+}
+
+// With the context's check_numeric option: fail with TMC_ERR_NUMERIC when the field holds NaN or Inf.
+tmc_status check_field_numeric(tmc_ctx* ctx, const float* field, const tmc_volume* vol, Allocs& al) {
+  if (!ctx->opts.check_numeric) return TMC_OK;
+  const int64_t n = (int64_t)vol->nx * vol->ny * vol->nz;
+  unsigned* flag = nullptr;
+  TMC_CUDA(ctx, al.get(&flag, 1));
+  TMC_CUDA(ctx, cudaMemsetAsync(flag, 0, sizeof(unsigned), ctx->stream));
+  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(tmc::ceil_div(n, 256), (int64_t)ctx->sms * 8));
+  nonfinite_kernel<<<blocks, 256, 0, ctx->stream>>>(field, n, flag);
+  ctx->launches += 1;
+  unsigned* h = (unsigned*)ctx->h_pinned + 256;
+  TMC_CUDA(ctx, cudaMemcpyAsync(h, flag, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+  TMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (*h) return fail(ctx, TMC_ERR_NUMERIC, "the field holds NaN or Inf");
+  return TMC_OK;
+}
+
 // Bring the field to the device (copy from host memory when needed).
 tmc_status field_on_device(tmc_ctx* ctx, const tmc_volume* vol, Allocs& al, const float** out) {
   const size_t n = (size_t)vol->nx * vol->ny * vol->nz;
   if (vol->on_device) {
     *out = vol->data;
-    return TMC_OK;
+    return check_field_numeric(ctx, *out, vol, al);
   }
   float* d = nullptr;
   TMC_CUDA(ctx, al.get(&d, n));
   TMC_CUDA(ctx, cudaMemcpyAsync(d, vol->data, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  *out = d;
+  return check_field_numeric(ctx, *out, vol, al);
+}
+
+// A host field for one extraction, copied in z slabs on the copy stream: classification of the
+// planes that have arrived runs beside the copy of the rest.  gates[q] holds the scan tiles whose
+// cells lie in the planes of slabs 0..q (a cell needs its planes z and z + 1) and the event that
+// slab q has arrived.  A device field, a small one, or a context that checks the field for NaN/Inf
+// (which needs the whole field first) takes field_on_device and no gates.
+constexpr size_t kSlabBytes = (size_t)32 << 20;
+constexpr int kMaxSlabs = 16;
+tmc_status field_slabs(tmc_ctx* ctx, const tmc_volume* vol, Allocs& al, const float** out,
+                       std::vector<tmc::TileGate>& gates) {
+  gates.clear();
+  const size_t plane = (size_t)vol->nx * vol->ny, n = plane * vol->nz;
+  const int slabs = (int)std::min<size_t>({(size_t)kMaxSlabs, n * sizeof(float) / kSlabBytes, (size_t)vol->nz / 2});
+  if (vol->on_device || ctx->opts.check_numeric || slabs < 2) return field_on_device(ctx, vol, al, out);
+  float* d = nullptr;
+  TMC_CUDA(ctx, al.get(&d, n));
+  TMC_CUDA(ctx, ensure_copy_stream(ctx));
+  while ((int)ctx->slab_events.size() < slabs) {
+    cudaEvent_t e;
+    TMC_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ctx->slab_events.push_back(e);
+  }
+  // the copies follow the allocation, which is ordered on the context stream
+  TMC_CUDA(ctx, cudaEventRecord(ctx->copy_event, ctx->stream));
+  TMC_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_event, 0));
+  const int64_t cells_per_plane = (int64_t)(vol->nx - 1) * (vol->ny - 1);
+  int z0 = 0;
+  for (int q = 0; q < slabs; q++) {
+    const int z1 = (q == slabs - 1) ? vol->nz : (int)((int64_t)vol->nz * (q + 1) / slabs);
+    TMC_CUDA(ctx, cudaMemcpyAsync(d + z0 * plane, vol->data + z0 * plane, (size_t)(z1 - z0) * plane * sizeof(float),
+                                  cudaMemcpyHostToDevice, ctx->copy_stream));
+    TMC_CUDA(ctx, cudaEventRecord(ctx->slab_events[q], ctx->copy_stream));
+    // cells in planes z < z1 - 1 have all eight corners on the device; whole tiles only
+    gates.push_back({(int64_t)(z1 - 1) * cells_per_plane / tmc::kScanTile, ctx->slab_events[q]});
+    z0 = z1;
+  }
   *out = d;
   return TMC_OK;
 }
@@ -194,10 +274,55 @@ cudaError_t dmc_vertex_scratch(Allocs& al, tmc::DmcScratch& sc, int64_t nv) {
   return e;
 }
 
+// Early device-to-host copies for TMC_OUT_HOST: an array handed to issue() is final (no later
+// kernel of the call writes it), so its copy starts on the context's copy stream, after the work
+// queued so far on the context stream, and runs beside the call's remaining kernels.
+// finish_mesh then takes the host block from here instead of copying the array again.
+struct EarlyCopies {
+  tmc_ctx* ctx = nullptr;
+  MeshPriv* mp = nullptr;
+  std::vector<std::pair<const void*, void*>> done;  // device array -> pinned host block
+  cudaError_t err = cudaSuccess;
+
+  void issue(const void* dev, size_t bytes) {
+    if (!dev || !bytes || err != cudaSuccess || host_of(dev)) return;
+    if ((err = ensure_copy_stream(ctx)) != cudaSuccess) return;
+    void* h = ctx->pinned_get(bytes);
+    if (!h) {
+      err = cudaErrorMemoryAllocation;
+      return;
+    }
+    mp->host.push_back(h);
+    if ((err = cudaEventRecord(ctx->copy_event, ctx->stream)) != cudaSuccess ||
+        (err = cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_event, 0)) != cudaSuccess ||
+        (err = cudaMemcpyAsync(h, dev, bytes, cudaMemcpyDeviceToHost, ctx->copy_stream)) != cudaSuccess)
+      return;
+    done.emplace_back(dev, h);
+  }
+  void* host_of(const void* dev) const {
+    for (const auto& d : done)
+      if (d.first == dev) return d.second;
+    return nullptr;
+  }
+  // the context stream waits for the copies issued so far
+  cudaError_t join() {
+    if (done.empty()) return err;
+    if (err == cudaSuccess) err = cudaEventRecord(ctx->copy_event, ctx->copy_stream);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(ctx->stream, ctx->copy_event, 0);
+    return err;
+  }
+};
+
 // Move device arrays of a finished mesh to host memory when TMC_OUT_HOST is set.
 template <typename T>
-tmc_status to_host(tmc_ctx* ctx, T** p, size_t count, MeshPriv* mp) {
+tmc_status to_host(tmc_ctx* ctx, T** p, size_t count, MeshPriv* mp, const EarlyCopies* early) {
   if (!*p) return TMC_OK;
+  if (early) {
+    if (void* e = early->host_of(*p)) {
+      *p = (T*)e;
+      return TMC_OK;
+    }
+  }
   T* h = (T*)ctx->pinned_get(count ? count * sizeof(T) : 16);
   if (!h) return fail(ctx, TMC_ERR_OOM, "host allocation of %zu bytes failed", count * sizeof(T));
   if (count) TMC_CUDA(ctx, cudaMemcpyAsync(h, *p, count * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
@@ -206,20 +331,21 @@ tmc_status to_host(tmc_ctx* ctx, T** p, size_t count, MeshPriv* mp) {
   return TMC_OK;
 }
 
-tmc_status finish_mesh(tmc_ctx* ctx, uint32_t flags, tmc_mesh* out, MeshPriv* mp) {
+tmc_status finish_mesh(tmc_ctx* ctx, uint32_t flags, tmc_mesh* out, MeshPriv* mp, EarlyCopies* early = nullptr) {
   tmc_status s = TMC_OK;
   if (flags & TMC_OUT_HOST) {
     const size_t nv = (size_t)out->nr_v, nq = (size_t)out->nr_q, nt = (size_t)out->nr_t, nh = (size_t)out->nr_he;
-    if ((s = to_host(ctx, &out->v, 3 * nv, mp))) return s;
-    if ((s = to_host(ctx, &out->n, 3 * nv, mp))) return s;
-    if ((s = to_host(ctx, &out->v64, 3 * nv, mp))) return s;
-    if ((s = to_host(ctx, &out->quads, 4 * nq, mp))) return s;
-    if ((s = to_host(ctx, &out->tris, 3 * nt, mp))) return s;
-    if ((s = to_host(ctx, &out->he, 4 * nh, mp))) return s;
-    if ((s = to_host(ctx, &out->he_v, nv, mp))) return s;
-    if ((s = to_host(ctx, &out->he_f, out->nr_q ? nq : nt, mp))) return s;
-    if ((s = to_host(ctx, &out->vcell, nv, mp))) return s;
-    if ((s = to_host(ctx, &out->vuvw, 3 * nv, mp))) return s;
+    if ((s = to_host(ctx, &out->v, 3 * nv, mp, early))) return s;
+    if ((s = to_host(ctx, &out->n, 3 * nv, mp, early))) return s;
+    if ((s = to_host(ctx, &out->v64, 3 * nv, mp, early))) return s;
+    if ((s = to_host(ctx, &out->quads, 4 * nq, mp, early))) return s;
+    if ((s = to_host(ctx, &out->tris, 3 * nt, mp, early))) return s;
+    if ((s = to_host(ctx, &out->he, 4 * nh, mp, early))) return s;
+    if ((s = to_host(ctx, &out->he_v, nv, mp, early))) return s;
+    if ((s = to_host(ctx, &out->he_f, out->nr_q ? nq : nt, mp, early))) return s;
+    if ((s = to_host(ctx, &out->vcell, nv, mp, early))) return s;
+    if ((s = to_host(ctx, &out->vuvw, 3 * nv, mp, early))) return s;
+    if (early) TMC_CUDA(ctx, early->join());
     TMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     for (void* p : mp->dev) cudaFreeAsync(p, ctx->stream);
     mp->dev.clear();
@@ -255,7 +381,12 @@ tmc_status tmc_ctx_create(int device, const tmc_ctx_opts* opts, tmc_ctx** out) {
   }
   cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
   ctx->tune = tmc::Tuning::defaults(ctx->sms);
-  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  {
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    ctx->priority = std::min(least, std::max(greatest, (int)ctx->opts.priority));
+  }
+  if (cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, ctx->priority) != cudaSuccess) {
     delete ctx;
     return TMC_ERR_CUDA;
   }
@@ -280,6 +411,12 @@ tmc_status tmc_ctx_destroy(tmc_ctx* ctx) {
   if (ctx->d_stats) cudaFree(ctx->d_stats);
   for (auto& kv : ctx->pinned_size) cudaFreeHost(kv.first);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  if (ctx->copy_stream) {
+    cudaStreamSynchronize(ctx->copy_stream);
+    cudaStreamDestroy(ctx->copy_stream);
+  }
+  if (ctx->copy_event) cudaEventDestroy(ctx->copy_event);
+  for (cudaEvent_t e : ctx->slab_events) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return TMC_OK;
@@ -387,7 +524,8 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   cudaStream_t st = ctx->stream;
   Allocs al(ctx);
   const float* field = nullptr;
-  if ((s = field_on_device(ctx, vol, al, &field))) return s;
+  std::vector<tmc::TileGate> gates;
+  if ((s = field_slabs(ctx, vol, al, &field, gates))) return s;
   tmc::Grid g = make_grid(vol, field, iso);
   g.flags = ((flags & TMC_GRAD_FLIP) ? tmc::kGridFlip : 0) | (simplify ? tmc::kGridNormal64 : 0);
   const tmc::CellSpace space = tmc::single_space(g);
@@ -401,7 +539,7 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   TMC_CUDA(ctx, al.get(&sc.totals, 2));
   sc.stats = ctx->d_stats;
   TMC_CUDA(ctx, cudaMemsetAsync(sc.stats, 0, 8 * sizeof(unsigned long long), st));
-  ctx->launches += tmc::dmc_front_count(space, sc, st, &ctx->prof);
+  ctx->launches += tmc::dmc_front_count(space, sc, st, &ctx->prof, gates.data(), (int)gates.size());
   unsigned long long* h = (unsigned long long*)ctx->h_pinned;
   TMC_CUDA(ctx, cudaMemcpyAsync(h, sc.totals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   TMC_CUDA(ctx, cudaStreamSynchronize(st));
@@ -462,9 +600,15 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   mesh.quads = quads;
   mesh.colors = colors;
   tmc::DmcPostOut post{};
+  EarlyCopies early{ctx, mp};
+  const tmc::ReadyFn ready = [&early](const void* dev, size_t bytes) { early.issue(dev, bytes); };
   tmc::DmcPostStatus ps =
-      tmc::dmc_postprocess(mesh, flags, ctx->sms, st, &post, (unsigned long long*)ctx->h_pinned + 64, &ctx->prof);
+      tmc::dmc_postprocess(mesh, flags, ctx->sms, st, &post, (unsigned long long*)ctx->h_pinned + 64, &ctx->prof,
+                           false, (flags & TMC_OUT_HOST) ? &ready : nullptr);
+  if (ps.err == cudaSuccess) ps.err = early.err;
   if (ps.err != cudaSuccess) {
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    for (void* p : mp->host) ctx->pinned_put(p);
     delete mp;
     TMC_CUDA(ctx, ps.err);
   }
@@ -518,7 +662,7 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   out->stats[4] = post.non_manifold;
   out->stats[6] = ncell;
 #undef TMC_GET
-  return finish_mesh(ctx, flags, out, mp);
+  return finish_mesh(ctx, flags, out, mp, &early);
 }
 
 }  // extern "C"
@@ -539,7 +683,8 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   cudaStream_t st = ctx->stream;
   Allocs al(ctx);
   const float* field = nullptr;
-  if ((s = field_on_device(ctx, vol, al, &field))) return s;
+  std::vector<tmc::TileGate> gates;
+  if ((s = field_slabs(ctx, vol, al, &field, gates))) return s;
   tmc::Grid g = make_grid(vol, field, iso);
   g.flags = (flags & TMC_OUT_POS_F64) ? tmc::kGridPos64 : 0;
   const int64_t ncell = g.ncells();
@@ -553,7 +698,7 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   TMC_CUDA(ctx, al.get(&sc.amb_n, 1));
   sc.stats = ctx->d_stats;
   TMC_CUDA(ctx, cudaMemsetAsync(sc.stats, 0, 8 * sizeof(unsigned long long), st));
-  ctx->launches += tmc::tmc_count(space, sc, st, &ctx->prof);
+  ctx->launches += tmc::tmc_count(space, sc, st, &ctx->prof, gates.data(), (int)gates.size());
   unsigned long long* h = (unsigned long long*)ctx->h_pinned;
   TMC_CUDA(ctx, cudaMemcpyAsync(h, sc.totals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   TMC_CUDA(ctx, cudaMemcpyAsync(h + 1, sc.stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
@@ -591,6 +736,20 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   out->v64 = vo.v64;
   out->tris = tris;
   int64_t non_manifold = 0;
+  EarlyCopies early{ctx, mp};
+  if ((flags & TMC_OUT_HOST) && (flags & TMC_OUT_HALFEDGES)) {
+    // the vertices and triangles are final: copy them out while the halfedges are built
+    early.issue(vo.v, (size_t)nv * 3 * sizeof(float));
+    early.issue(vo.n, (size_t)nv * 3 * sizeof(float));
+    early.issue(vo.v64, (size_t)nv * 3 * sizeof(double));
+    early.issue(tris, (size_t)nt * 3 * sizeof(int32_t));
+    if (early.err != cudaSuccess) {
+      if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+      for (void* p : mp->host) ctx->pinned_put(p);
+      delete mp;
+      TMC_CUDA(ctx, early.err);
+    }
+  }
   if (flags & TMC_OUT_HALFEDGES) {
     const int64_t nh = 3 * nt;
     int32_t *twin = nullptr, *he4 = nullptr, *hv = nullptr, *hf = nullptr;
@@ -630,7 +789,7 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   ctx->prof.collect();
   out->stats[4] = non_manifold;
   out->stats[6] = ncell;
-  return finish_mesh(ctx, flags, out, mp);
+  return finish_mesh(ctx, flags, out, mp, &early);
 }
 
 // One batch of requests of one algorithm: all volumes share one cell space, so every stage is one

@@ -454,13 +454,14 @@ __device__ void load_amb_cell(const Grid& g, int i, int j, int k, const float u[
 // kernels
 // ------------------------------------------------------------------------------------------
 // Ambiguous cells are listed (amb_list, warp-aggregated appends) for the float64 counting pass.
-__global__ void __launch_bounds__(kScanThreads) tmc_classify_kernel(CellSpace space, uint32_t* rec,
+__global__ void __launch_bounds__(kScanThreads) tmc_classify_kernel(CellSpace space, int64_t tile0, uint32_t* rec,
                                                                    unsigned long long* tile_sums,
                                                                    unsigned long long* stats, uint32_t* amb_list,
                                                                    unsigned* amb_n) {
-  const Grid g = space.grid_of_tile(blockIdx.x);
+  const int64_t tile = tile0 + blockIdx.x;
+  const Grid g = space.grid_of_tile(tile);
   const int64_t n = g.ncells();
-  const int64_t vbase = (int64_t)blockIdx.x * kScanTile;
+  const int64_t vbase = tile * kScanTile;
   unsigned long long local = 0, act = 0, amb = 0;
   for (int s = 0; s < kScanItems; s++) {
     const int64_t vc = vbase + (int64_t)s * kScanThreads + threadIdx.x;
@@ -504,7 +505,7 @@ __global__ void __launch_bounds__(kScanThreads) tmc_classify_kernel(CellSpace sp
   }
   unsigned long long tot;
   block_exclusive_scan<unsigned long long>(local, &tot);
-  if (threadIdx.x == 0) tile_sums[blockIdx.x] = tot;
+  if (threadIdx.x == 0) tile_sums[tile] = tot;
   for (int o = 16; o; o >>= 1) {
     act += __shfl_down_sync(0xffffffffu, act, o);
     amb += __shfl_down_sync(0xffffffffu, amb, o);
@@ -849,16 +850,29 @@ __global__ void __launch_bounds__(kEmitThreads, 4) tmc_emit_kernel(CellSpace spa
 // ------------------------------------------------------------------------------------------
 int64_t tmc_tiles(const CellSpace& space) { return ceil_div(space.n, kScanTile); }
 
-int tmc_count(const CellSpace& space, TmcScratch& s, cudaStream_t st, Prof* prof) {
+int tmc_count(const CellSpace& space, TmcScratch& s, cudaStream_t st, Prof* prof, const TileGate* gates, int ngates) {
   const int64_t n = space.n;
   const int64_t tiles = tmc_tiles(space);
   // the ambiguous-cell list lives in toff until the offsets kernel overwrites it
   uint32_t* amb_cells = reinterpret_cast<uint32_t*>(s.toff);
+  int k = 0;
   {
     Stage t(prof, "tmc_classify", st);
     cudaMemsetAsync(s.amb_n, 0, sizeof(unsigned), st);
-    tmc_classify_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(space, s.rec, s.tile_sums, s.stats, amb_cells,
-                                                                  s.amb_n);
+    auto classify = [&](int64_t t0, int64_t t1) {
+      if (t1 <= t0) return;
+      tmc_classify_kernel<<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(space, t0, s.rec, s.tile_sums, s.stats,
+                                                                        amb_cells, s.amb_n);
+      k++;
+    };
+    if (ngates == 0) classify(0, tiles);
+    int64_t t0 = 0;
+    for (int q = 0; q < ngates; q++) {
+      cudaStreamWaitEvent(st, gates[q].ready, 0);
+      const int64_t t1 = (q == ngates - 1) ? tiles : std::min(gates[q].tile_end, tiles);
+      classify(t0, t1);
+      t0 = std::max(t0, t1);
+    }
   }
   {
     Stage ta(prof, "tmc_amb_count", st);
@@ -868,7 +882,7 @@ int tmc_count(const CellSpace& space, TmcScratch& s, cudaStream_t st, Prof* prof
   Stage t(prof, "tmc_scan", st);
   scan_tile_sums_kernel<<<1, 1024, 0, st>>>(s.tile_sums, tiles, s.totals);
   tmc_offsets_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(n, s.rec, s.tile_sums, s.voff, s.toff);
-  return 4;
+  return k + 3;
 }
 
 int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tris, const Tuning& tu, cudaStream_t st,

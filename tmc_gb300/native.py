@@ -17,6 +17,9 @@ TMC_OK = 0
 TMC_ERR_INVALID_ARG = 1
 TMC_ERR_OOM = 2
 TMC_ERR_CAPACITY = 3
+TMC_ERR_CUDA = 4
+TMC_ERR_TIMEOUT = 5
+TMC_ERR_NUMERIC = 6
 STATUS = {0: "TMC_OK", 1: "TMC_ERR_INVALID_ARG", 2: "TMC_ERR_OOM", 3: "TMC_ERR_CAPACITY", 4: "TMC_ERR_CUDA",
           5: "TMC_ERR_TIMEOUT", 6: "TMC_ERR_NUMERIC", 7: "TMC_ERR_INTERNAL"}
 
@@ -70,7 +73,7 @@ class TmcError(RuntimeError):
 
 
 class CtxOpts(ctypes.Structure):
-    _fields_ = [("reserve_bytes", ctypes.c_size_t), ("check_numeric", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+    _fields_ = [("reserve_bytes", ctypes.c_size_t), ("check_numeric", ctypes.c_int32), ("priority", ctypes.c_int32)]
 
 
 class Volume(ctypes.Structure):
@@ -239,10 +242,10 @@ def _host_array(ptr, count, dtype):
 class Context:
     """One CUDA stream, pooled device memory; mirrors a reference extraction object."""
 
-    def __init__(self, device: int = 0, reserve_bytes: int = 0, check_numeric: bool = False):
+    def __init__(self, device: int = 0, reserve_bytes: int = 0, check_numeric: bool = False, priority: int = 0):
         self.lib = load()
         self.h = ctypes.c_void_p()
-        opts = CtxOpts(reserve_bytes, 1 if check_numeric else 0, 0)
+        opts = CtxOpts(reserve_bytes, 1 if check_numeric else 0, priority)
         st = self.lib.tmc_ctx_create(device, ctypes.byref(opts), ctypes.byref(self.h))
         if st != TMC_OK:
             raise TmcError(st, "tmc_ctx_create failed (is a CUDA device visible?)")
