@@ -202,12 +202,13 @@ __global__ void merge_claim_kernel(HeView he, int64_t nq, const uint8_t* p, cons
   }
 }
 
-__device__ __forceinline__ void midpoint(double* v64, float* v, double* n64, float* n, int dst, int a, int b) {
+// float64 only: the float32 outputs are their roundings, written once after the last pass
+// (float_outputs_kernel)
+__device__ __forceinline__ void midpoint(double* v64, double* n64, int dst, int a, int b) {
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     const double x = v64[3 * (int64_t)a + d] + 0.5 * (v64[3 * (int64_t)b + d] - v64[3 * (int64_t)a + d]);
     v64[3 * (int64_t)dst + d] = x;
-    v[3 * (int64_t)dst + d] = (float)x;
   }
   double m[3];
 #pragma unroll
@@ -217,11 +218,7 @@ __device__ __forceinline__ void midpoint(double* v64, float* v, double* n64, flo
   }
   const double s = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
 #pragma unroll
-  for (int d = 0; d < 3; d++) {
-    const double x = m[d] / s;
-    n64[3 * (int64_t)dst + d] = x;
-    n[3 * (int64_t)dst + d] = (float)x;
-  }
+  for (int d = 0; d < 3; d++) n64[3 * (int64_t)dst + d] = m[d] / s;
 }
 
 // Marks the removed vertices and lists the midpoint merges (destination, two sources); the
@@ -269,12 +266,21 @@ __global__ void merge_apply_kernel(HeView he, int64_t nq, const uint8_t* branch,
   }
 }
 
-__global__ void midpoint_kernel(const int4* jobs, const unsigned* njobs, double* v64, float* v, double* n64,
-                                float* n) {
+__global__ void midpoint_kernel(const int4* jobs, const unsigned* njobs, double* v64, double* n64) {
   const int64_t nj = *njobs;
   FOR_EACH(a, nj) {
     const int4 j = jobs[a];
-    midpoint(v64, v, n64, n, j.x, j.y, j.z);
+    midpoint(v64, n64, j.x, j.y, j.z);
+  }
+}
+
+// The float32 positions and normals of the simplified mesh: the roundings of its float64 ones (the
+// front end writes float32 values that are the same roundings, so that the passes only carry the
+// float64 arrays).
+__global__ void float_outputs_kernel(const double* v64, const double* n64, int64_t n, float* v, float* nf) {
+  FOR_EACH(e, n) {
+    v[e] = (float)v64[e];
+    nf[e] = (float)n64[e];
   }
 }
 
@@ -286,11 +292,11 @@ __global__ void invert_flags_kernel(const uint8_t* in, int64_t n, uint8_t* out) 
 }
 
 // removeVertices3X3Y / removeVertices3333 (:1096-1112, :1324-1338): kept vertices move to their
-// new index, which becomes their map entry.  One thread per vertex component (x, y or z of all four
-// arrays): every load and store is unit-stride across the warp.
+// new index, which becomes their map entry.  One thread per vertex component (x, y or z of the
+// float64 positions and normals): every load and store is unit-stride across the warp.
 __global__ void gather_vertices_kernel(const uint8_t* keep, const int32_t* idx, int64_t nv, const double* v64,
-                                       const float* v, const double* n64, const float* n, double* v64o, float* vo,
-                                       double* n64o, float* no, int32_t* map, int64_t cap, unsigned* overflow) {
+                                       const double* n64, double* v64o, double* n64o, int32_t* map, int64_t cap,
+                                       unsigned* overflow) {
   FOR_EACH(e, 3 * nv) {
     const int64_t i = e / 3;
     if (!keep[i]) continue;
@@ -301,9 +307,7 @@ __global__ void gather_vertices_kernel(const uint8_t* keep, const int32_t* idx, 
       continue;
     }
     v64o[3 * o + d] = v64[e];
-    vo[3 * o + d] = v[e];
     n64o[3 * o + d] = n64[e];
-    no[3 * o + d] = n[e];
     if (d == 0) map[i] = (int32_t)o;
   }
 }
@@ -713,7 +717,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     cudaMemsetAsync(njobs, 0, sizeof(unsigned), st);
     merge_apply_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.nq, branch, own_pos, own_rm, vm_first, vm_second, em, jobs,
                                            njobs);
-    midpoint_kernel<<<gq, 256, 0, st>>>(jobs, njobs, cur.v64, cur.v, cur.n64, cur.n);
+    midpoint_kernel<<<gq, 256, 0, st>>>(jobs, njobs, cur.v64, cur.n64);
     s.launches += 9;
     // remove vertices
     invert_flags_kernel<<<gv, 256, 0, st>>>(vm_first, cur.nv, keep);
@@ -735,8 +739,8 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     adopt(nx.v);
     adopt(nx.n);
     adopt(nx.n64);
-    gather_vertices_kernel<<<grid_for(3 * cur.nv, sms), 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.v, cur.n64, cur.n, nx.v64, nx.v,
-                                                nx.n64, nx.n, vm_second, nv2, hw.ovf);
+    gather_vertices_kernel<<<grid_for(3 * cur.nv, sms), 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.n64, nx.v64,
+                                                                       nx.n64, vm_second, nv2, hw.ovf);
     // remove quads
     invert_flags_kernel<<<gq, 256, 0, st>>>(em, cur.nq, keep);
     s.launches += 2 + scan_flags(keep, cur.nq, idx, tiles, total, st);
@@ -797,8 +801,8 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
       adopt(nx.v);
       adopt(nx.n);
       adopt(nx.n64);
-      gather_vertices_kernel<<<grid_for(3 * cur.nv, sms), 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.v, cur.n64, cur.n, nx.v64, nx.v,
-                                                  nx.n64, nx.n, vm2, nv2, hw.ovf);
+      gather_vertices_kernel<<<grid_for(3 * cur.nv, sms), 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.n64, nx.v64,
+                                                                         nx.n64, vm2, nv2, hw.ovf);
       invert_flags_kernel<<<gq, 256, 0, st>>>(rflag, cur.nq, keep);
       s.launches += 2 + scan_flags(keep, cur.nq, idx, tiles, total, st);
       const int64_t nq2 = read_total();
@@ -820,6 +824,11 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
         mesh_version++;
       }
     }
+  }
+  // the float32 outputs of the simplified mesh
+  if (s.err == cudaSuccess && simplify && cur.nv > 0) {
+    float_outputs_kernel<<<grid_for(3 * cur.nv, sms), 256, 0, st>>>(cur.v64, cur.n64, 3 * cur.nv, cur.v, cur.n);
+    s.launches += 1;
   }
   // ---- final halfedges and triangles ----
   if (s.err == cudaSuccess && ready) {

@@ -17,6 +17,8 @@
 // the entries of a's list with target b and of b's list with target a.  Vertex lists are short
 // (valence ~4) and spatially coherent, so the pairing pass reads mostly from L2.  Sorting the few
 // ids of an edge restores the reference's insertion order.
+#include <climits>
+
 #include "halfedges.h"
 #include "scan.cuh"
 
@@ -57,34 +59,48 @@ __global__ void he_scatter_kernel(const int32_t* faces, int P, int64_t nf, const
   }
 }
 
-// ids of all halfedges of the undirected edge {a, b} (sorted); returns their number (capped at 8)
-__device__ __forceinline__ int edge_halfedges(const int2* list, const int32_t* off, const int32_t* deg, int a, int b,
-                                              int id[8]) {
-  int c = 0;
-  for (int q = off[a], e = off[a] + deg[a]; q < e; q++) {
+// The halfedges of the undirected edge {a, b}: returns their number, and the four lowest ids in
+// ascending order in id[0..3] (all of them when there are at most four; an edge with more pairs
+// none).  Registers only: each id is inserted into the sorted four with fixed compare-swaps.
+struct EdgeIds {
+  int id[4];
+  int c;
+};
+__device__ __forceinline__ void edge_ids_insert(EdgeIds& e, int x) {
+  e.c++;
+  if (x >= e.id[3]) return;
+  e.id[3] = x;
+  if (e.id[3] < e.id[2]) { const int t = e.id[2]; e.id[2] = e.id[3]; e.id[3] = t; }
+  if (e.id[2] < e.id[1]) { const int t = e.id[1]; e.id[1] = e.id[2]; e.id[2] = t; }
+  if (e.id[1] < e.id[0]) { const int t = e.id[0]; e.id[0] = e.id[1]; e.id[1] = t; }
+}
+// The list of vertex v is list[off[v] .. off[v + 1]), the last one ends at nh (every halfedge has
+// one origin, so the degrees sum to nh): one cache line holds both bounds.
+__device__ __forceinline__ int list_end(const int32_t* off, int v, int nv, int nh) {
+  return v + 1 < nv ? off[v + 1] : nh;
+}
+__device__ __forceinline__ EdgeIds edge_halfedges(const int2* list, const int32_t* off, int nv, int nh, int a, int b) {
+  EdgeIds e;
+  e.c = 0;
+  e.id[0] = e.id[1] = e.id[2] = e.id[3] = INT_MAX;
+  for (int q = off[a], end = list_end(off, a, nv, nh); q < end; q++) {
     const int2 x = list[q];
-    if (x.y == b && c < 8) id[c++] = x.x;
+    if (x.y == b) edge_ids_insert(e, x.x);
   }
   if (a != b) {
-    for (int q = off[b], e = off[b] + deg[b]; q < e; q++) {
+    for (int q = off[b], end = list_end(off, b, nv, nh); q < end; q++) {
       const int2 x = list[q];
-      if (x.y == a && c < 8) id[c++] = x.x;
+      if (x.y == a) edge_ids_insert(e, x.x);
     }
   }
-  for (int x = 1; x < c; x++)
-    for (int y = x; y > 0 && id[y - 1] > id[y]; y--) {
-      const int tmp = id[y];
-      id[y] = id[y - 1];
-      id[y - 1] = tmp;
-    }
-  return c;
+  return e;
 }
 
 // one thread per halfedge: two-halfedge edges pair without coordination; 3 or 4 are resolved by
 // the edge's lowest halfedge, which writes the twins and flags of all of them; every other
 // halfedge writes its own (each entry is written exactly once)
 __global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const int2* list, const int32_t* off,
-                               const int32_t* deg, int32_t* twin, uint8_t* flag, unsigned long long* hv_key,
+                               int nv, int32_t* twin, uint8_t* flag, unsigned long long* hv_key,
                                unsigned long long* non_manifold, int32_t* lone, unsigned long long* lone_count) {
   const int64_t nh = nf * P;
   unsigned long long nm = 0;
@@ -92,8 +108,9 @@ __global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const in
     const int64_t f = h / P;
     const int r = (int)(h - f * P);
     const int v0 = faces[h], v1 = faces[f * P + (r + 1) % P];
-    int id[8];
-    const int c = edge_halfedges(list, off, deg, v0, v1, id);
+    const EdgeIds e = edge_halfedges(list, off, nv, (int)nh, v0, v1);
+    const int c = e.c;
+    const int* id = e.id;
     if (c == 2) {
       twin[h] = (id[0] == (int)h) ? id[1] : id[0];
       flag[h] = 0;
@@ -179,7 +196,7 @@ int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& 
   he_build_kernel<<<grid(nh), 256, 0, st>>>(faces, nh, w.deg, w.rank, o.hv);
   k += 2 + scan_i32(w.deg, nv, w.off, w.tiles, w.total, st);
   he_scatter_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.off, w.rank, w.list);
-  he_twin_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.list, w.off, w.deg, o.twin, o.flag, w.hv_key,
+  he_twin_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.list, w.off, (int)nv, o.twin, o.flag, w.hv_key,
                                            w.non_manifold, w.rank, lone_count);
   he_override_kernel<<<(unsigned)std::max(1, sms), 256, 0, st>>>(faces, P, w.rank, lone_count, o.hv, w.hv_key);
   return k + 3;
