@@ -252,7 +252,7 @@ struct Tuning {
   int sms = 1;
   int64_t group_lanes = 0;        // lanes the projection pass may fill with lane groups (0: one thread per vertex)
   int64_t warp_list_max = 0;      // float64 fallback lists up to this length run one warp per vertex
-  int vertex_blocks_per_sm = 32;  // grid cap of the per-vertex passes
+  int vertex_blocks_per_sm = 32;  // grid cap of the per-vertex passes (rounded to whole waves)
   int emit_blocks_per_sm = 8;     // grid cap of the TMC emission kernel
   static Tuning defaults(int sms) {
     Tuning t;
@@ -262,6 +262,25 @@ struct Tuning {
     return t;
   }
 };
+
+// Blocks of `kernel` that fit on one SM at `threads` threads per block (the occupancy calculator;
+// registers and shared memory decide).
+template <typename K>
+inline int resident_blocks(K kernel, int threads) {
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, threads, 0) != cudaSuccess || b < 1) b = 1;
+  return b;
+}
+
+// Grid of a grid-stride launch: a whole number of waves (resident blocks per SM x SMs), the one
+// nearest to `per_sm` blocks per SM, and no more blocks than `threads`-item groups.  A grid of
+// 1.3 waves would run its last 0.3 wave alone, as long as a full one.
+inline int64_t wave_grid(int resident, int sms, int64_t per_sm, int64_t items, int threads) {
+  const int64_t waves = per_sm <= resident ? 1 : (per_sm + resident / 2) / resident;
+  const int64_t g = waves * resident * (int64_t)sms;
+  const int64_t need = (items + threads - 1) / threads;
+  return need < 1 ? 1 : (need < g ? need : g);
+}
 
 // Classification may start before the whole field is on the device (a host field copied in z
 // slabs): the scan tiles below tile_end may run once `ready` has completed.  Gates come in order,

@@ -852,12 +852,21 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
     dmc_offsets_kernel<<<(unsigned)ceil_div(n, kScanTile), kScanThreads, 0, st>>>(n, s.rec, s.tile_sums, s.voff,
                                                                                   s.qoff, s.vwork);
   }
-  const int64_t vb = std::max<int64_t>(1, std::min<int64_t>(ceil_div(nv, kVertexThreads), (int64_t)sms * tu.vertex_blocks_per_sm));
+  // per-vertex grids: whole waves of each kernel's resident blocks
+  static const int r_setup = resident_blocks(dmc_vertex_setup_kernel, kVertexThreads);
+  static const int r_project = resident_blocks(dmc_project_kernel, kVertexThreads);
+  static const int r_finish = resident_blocks(dmc_vertex_finish_kernel<true>, kVertexThreads);
+  static const int r_finish32 = resident_blocks(dmc_vertex_finish_kernel<false>, kVertexThreads);
+  static const int r_quad = resident_blocks(dmc_quad_kernel<false>, kQuadThreads);
+  static const int r_quad_batch = resident_blocks(dmc_quad_kernel<true>, kQuadThreads);
+  auto vgrid = [&](int resident) {
+    return (unsigned)wave_grid(resident, sms, tu.vertex_blocks_per_sm, nv, kVertexThreads);
+  };
   {
     Stage t(prof, "dmc_vertex_setup", st);
     cudaMemsetAsync(s.fb_count, 0, 2 * sizeof(unsigned), st);
-    dmc_vertex_setup_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(space, s.voff, s.vwork, nv, s.proj, s.fb_list,
-                                                                     s.fb_count, s.stats);
+    dmc_vertex_setup_kernel<<<vgrid(r_setup), kVertexThreads, 0, st>>>(space, s.voff, s.vwork, nv, s.proj, s.fb_list,
+                                                                       s.fb_count, s.stats);
   }
   {
     Stage t(prof, "dmc_project", st);
@@ -868,34 +877,38 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
       dmc_project_group_kernel<<<(unsigned)std::max<int64_t>(1, ceil_div(nv * G, kVertexThreads)), kVertexThreads, 0,
                                  st>>>(s.proj, nv, G, s.vp, s.fb_list, s.fb_count, s.stats);
     else
-      dmc_project_kernel<<<(unsigned)vb, kVertexThreads, 0, st>>>(s.proj, nv, s.vp, s.fb_list, s.fb_count, s.stats);
+      dmc_project_kernel<<<vgrid(r_project), kVertexThreads, 0, st>>>(s.proj, nv, s.vp, s.fb_list, s.fb_count, s.stats);
   }
   {
     Stage t(prof, "dmc_vertex_finish", st);
     // the float-float normals only when some volume keeps float64 normals (simplification)
     if (vo.n64)
-      dmc_vertex_finish_kernel<true><<<(unsigned)vb, kVertexThreads, 0, st>>>(space, s.vwork, nv, s.vp, vo, flip, s.stats);
+      dmc_vertex_finish_kernel<true><<<vgrid(r_finish), kVertexThreads, 0, st>>>(space, s.vwork, nv, s.vp, vo, flip,
+                                                                                 s.stats);
     else
-      dmc_vertex_finish_kernel<false><<<(unsigned)vb, kVertexThreads, 0, st>>>(space, s.vwork, nv, s.vp, vo, flip, s.stats);
+      dmc_vertex_finish_kernel<false><<<vgrid(r_finish32), kVertexThreads, 0, st>>>(space, s.vwork, nv, s.vp, vo, flip,
+                                                                                    s.stats);
   }
   {
     // the listed vertices: one thread each with every float64 fallback, the 26x26 retries one warp
     // each; a short list (small calls) entirely one warp per vertex
     Stage t(prof, "dmc_vertex", st);
     const unsigned warp_max = (unsigned)std::min<int64_t>(tu.warp_list_max, 0x7fffffff);
-    const unsigned fb = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nv, kVertexThreads), (int64_t)sms * 8));
+    static const int r_vertex = resident_blocks(dmc_vertex_kernel, kVertexThreads);
+    const unsigned fb = (unsigned)wave_grid(r_vertex, sms, 8, nv, kVertexThreads);
     dmc_vertex_kernel<<<fb, kVertexThreads, 0, st>>>(space, s.voff, s.vwork, s.fb_list, s.fb_count, s.tail_list,
                                                       s.fb_count + 1, warp_max, vo, flip, s.stats);
     dmc_vertex_warp_kernel<<<(unsigned)std::max(1, sms * 3), kVertexThreads, 0, st>>>(
         space, s.voff, s.vwork, s.fb_list, s.fb_count, s.tail_list, s.fb_count + 1, warp_max, vo, flip, s.stats);
   }
   Stage t(prof, "dmc_quad", st);
-  const unsigned qb = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 32 * (kQuadThreads / 32)),
-                                                                       (int64_t)sms * 8));
+  // one wave: the kernel takes 32-cell chunks until none are left
   if (space.grids)
-    dmc_quad_kernel<true><<<qb, kQuadThreads, 0, st>>>(space, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
+    dmc_quad_kernel<true><<<(unsigned)wave_grid(r_quad_batch, sms, 1, ceil_div(n, 32), kQuadThreads / 32), kQuadThreads,
+                            0, st>>>(space, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
   else
-    dmc_quad_kernel<false><<<qb, kQuadThreads, 0, st>>>(space, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
+    dmc_quad_kernel<false><<<(unsigned)wave_grid(r_quad, sms, 1, ceil_div(n, 32), kQuadThreads / 32), kQuadThreads, 0,
+                             st>>>(space, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
   return 7;
 }
 

@@ -48,7 +48,8 @@ __global__ void he_build_kernel(const int32_t* faces, int64_t nh, int32_t* deg, 
   }
 }
 
-__global__ void he_scatter_kernel(const int32_t* faces, int P, int64_t nf, const int32_t* off, const int32_t* rank,
+// (at most 32 registers: 8 blocks of 256 threads fit on an SM, the grid's 8 per SM in one wave)
+__global__ void __launch_bounds__(256, 8) he_scatter_kernel(const int32_t* faces, int P, int64_t nf, const int32_t* off, const int32_t* rank,
                                   int2* list) {
   const int64_t nh = nf * P;
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
@@ -171,7 +172,7 @@ __global__ void he_override_kernel(const int32_t* faces, int P, const int32_t* l
   }
 }
 
-__global__ void he_pack4_kernel(const int32_t* faces, int P, const int32_t* twin, int64_t nh, int32_t* he4,
+__global__ void __launch_bounds__(256, 8) he_pack4_kernel(const int32_t* faces, int P, const int32_t* twin, int64_t nh, int32_t* he4,
                                 int32_t* hf) {
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
     const int64_t f = h / P;

@@ -698,7 +698,7 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   TMC_CUDA(ctx, al.get(&sc.amb_n, 1));
   sc.stats = ctx->d_stats;
   TMC_CUDA(ctx, cudaMemsetAsync(sc.stats, 0, 8 * sizeof(unsigned long long), st));
-  ctx->launches += tmc::tmc_count(space, sc, st, &ctx->prof, gates.data(), (int)gates.size());
+  ctx->launches += tmc::tmc_count(space, sc, ctx->sms, st, &ctx->prof, gates.data(), (int)gates.size());
   unsigned long long* h = (unsigned long long*)ctx->h_pinned;
   TMC_CUDA(ctx, cudaMemcpyAsync(h, sc.totals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   TMC_CUDA(ctx, cudaMemcpyAsync(h + 1, sc.stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
@@ -876,7 +876,7 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
   } else {
     tsc = tmc::TmcScratch{rec, voff, qoff, tile_sums, totals, ctx->d_stats, nullptr, nullptr, nullptr};
     TMC_CUDA(ctx, al.get(&tsc.amb_n, 1));
-    ctx->launches += tmc::tmc_count(space, tsc, st, &ctx->prof);
+    ctx->launches += tmc::tmc_count(space, tsc, ctx->sms, st, &ctx->prof);
   }
   std::vector<unsigned long long> toff((size_t)tiles + 1);
   unsigned long long* h = (unsigned long long*)ctx->h_pinned;

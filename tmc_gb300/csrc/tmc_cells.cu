@@ -850,7 +850,8 @@ __global__ void __launch_bounds__(kEmitThreads, 4) tmc_emit_kernel(CellSpace spa
 // ------------------------------------------------------------------------------------------
 int64_t tmc_tiles(const CellSpace& space) { return ceil_div(space.n, kScanTile); }
 
-int tmc_count(const CellSpace& space, TmcScratch& s, cudaStream_t st, Prof* prof, const TileGate* gates, int ngates) {
+int tmc_count(const CellSpace& space, TmcScratch& s, int sms, cudaStream_t st, Prof* prof, const TileGate* gates,
+              int ngates) {
   const int64_t n = space.n;
   const int64_t tiles = tmc_tiles(space);
   // the ambiguous-cell list lives in toff until the offsets kernel overwrites it
@@ -876,7 +877,9 @@ int tmc_count(const CellSpace& space, TmcScratch& s, cudaStream_t st, Prof* prof
   }
   {
     Stage ta(prof, "tmc_amb_count", st);
-    tmc_amb_count_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 128 * 64), 152 * 16)), 128, 0,
+    // whole waves; the list length is only known on the device, so the grid follows the cell count
+    static const int r_amb = resident_blocks(tmc_amb_count_kernel, 128);
+    tmc_amb_count_kernel<<<(unsigned)wave_grid(r_amb, sms, 16, ceil_div(n, 64), 128), 128, 0,
                            st>>>(space, s.rec, s.tile_sums, s.stats, amb_cells, s.amb_n);
   }
   Stage t(prof, "tmc_scan", st);

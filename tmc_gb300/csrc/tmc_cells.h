@@ -30,7 +30,7 @@ struct TmcScratch {
 // volume, and the volumes' vertices and triangles follow one another in the outputs.
 int64_t tmc_tiles(const CellSpace& space);
 // gates: as dmc_front_count's (classification of a host field arriving in slabs)
-int tmc_count(const CellSpace& space, TmcScratch& s, cudaStream_t st, Prof* prof = nullptr,
+int tmc_count(const CellSpace& space, TmcScratch& s, int sms, cudaStream_t st, Prof* prof = nullptr,
               const TileGate* gates = nullptr, int ngates = 0);
 int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tris, const Tuning& tu, cudaStream_t st,
              Prof* prof = nullptr);
