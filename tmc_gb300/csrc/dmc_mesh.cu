@@ -615,14 +615,17 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   }
   // The mesh changes only where a pass merges or removes something; a pass that changes nothing
   // keeps `cur` as it is, and the halfedges (and out-degrees) built for it stay valid.
+  // Vertex handles are built only for the output (the passes never read them).
   int mesh_version = 0, he_version = -1;
-  auto halfedges = [&](const DmcMesh& m) {
-    if (he_version == mesh_version) return;
+  bool he_handles = false;
+  auto halfedges = [&](const DmcMesh& m, bool handles) {
+    if (he_version == mesh_version && (he_handles || !handles)) return;
     Stage tm(prof, "dmc_halfedges", st);
     cudaMemsetAsync(hw.nm, 0, 2 * sizeof(unsigned long long), st);
     HeOut ho{hw.twin, hw.flag, hw.hv};
-    s.launches += build_halfedges(m.quads, 4, m.nq, m.nv, ho, hw.w, sms, st);
+    s.launches += build_halfedges(m.quads, 4, m.nq, m.nv, ho, hw.w, sms, st, handles);
     he_version = mesh_version;
+    he_handles = handles;
   };
   auto read_total = [&]() -> int64_t {
     cudaMemcpyAsync(h_cnt, total, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
@@ -687,7 +690,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   for (int pass = 0; pass < 2; pass++) {
     if ((pass == 0 && !c3x3y) || (pass == 1 && !i3x3y)) continue;
     if (cur.nq == 0) break;
-    halfedges(cur);
+    halfedges(cur, false);
     if (pass == 0) {
       Stage tm(prof, "dmc_color", st);
       int32_t* cnt = pool.get<int32_t>(24);
@@ -765,7 +768,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   }
   // ---- P3333 (simplify3333, :1362-1385) ----
   if (s.err == cudaSuccess && p3333 && cur.nq > 0) {
-    halfedges(cur);
+    halfedges(cur, false);
     Stage tm(prof, "dmc_p3333", st);
     uint8_t* p3 = p;
     uint8_t* rflag = em;
@@ -838,7 +841,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     (*ready)(cur.quads, (size_t)cur.nq * 4 * sizeof(int32_t));
   }
   if (s.err == cudaSuccess && want_he) {
-    halfedges(cur);
+    halfedges(cur, true);
     void *he4 = nullptr, *hv = nullptr, *hf = nullptr;
     if ((s.err = cudaMallocAsync(&he4, std::max<int64_t>(4 * cur.nq, 1) * 4 * sizeof(int32_t), st)) == cudaSuccess &&
         (s.err = cudaMallocAsync(&hv, std::max<int64_t>(cur.nv, 1) * sizeof(int32_t), st)) == cudaSuccess &&

@@ -40,11 +40,12 @@ __global__ void he_vertex_init_kernel(unsigned long long* hv_key, int32_t* deg, 
 // atomic per halfedge).  The vertex handle is the highest halfedge with that origin (the
 // reference's last insertion): a fire-and-forget atomic maximum.  Twins and flags are written by
 // he_twin_kernel, every entry once.
+template <bool kHandles>
 __global__ void he_build_kernel(const int32_t* faces, int64_t nh, int32_t* deg, int32_t* rank, int32_t* hv) {
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
     const int v = faces[h];
     rank[h] = atomicAdd(deg + v, 1);
-    atomicMax(hv + v, (int32_t)h);
+    if (kHandles) atomicMax(hv + v, (int32_t)h);
   }
 }
 
@@ -99,7 +100,9 @@ __device__ __forceinline__ EdgeIds edge_halfedges(const int2* list, const int32_
 
 // one thread per halfedge: two-halfedge edges pair without coordination; 3 or 4 are resolved by
 // the edge's lowest halfedge, which writes the twins and flags of all of them; every other
-// halfedge writes its own (each entry is written exactly once)
+// halfedge writes its own (each entry is written exactly once).  kHandles: list the lone halfedges
+// of three-halfedge edges and their keys for the vertex handle override.
+template <bool kHandles>
 __global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const int2* list, const int32_t* off,
                                int nv, int32_t* twin, uint8_t* flag, unsigned long long* hv_key,
                                unsigned long long* non_manifold, int32_t* lone, unsigned long long* lone_count) {
@@ -137,10 +140,12 @@ __global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const in
       } else {
         twin[e1] = e2; twin[e2] = e1; twin[e0] = -1; lone_v = a0; lone_h = e0;
       }
-      lone[atomicAdd(lone_count, 1ull)] = lone_h;  // for the handle override
-      // the last override in key order wins: remember the largest key (+1 so that 0 = none)
-      const unsigned long long key = ((unsigned long long)(unsigned)min(v0, v1) << 32) | (unsigned)max(v0, v1);
-      atomicMax(hv_key + lone_v, key + 1ull);
+      if (kHandles) {
+        lone[atomicAdd(lone_count, 1ull)] = lone_h;  // for the handle override
+        // the last override in key order wins: remember the largest key (+1 so that 0 = none)
+        const unsigned long long key = ((unsigned long long)(unsigned)min(v0, v1) << 32) | (unsigned)max(v0, v1);
+        atomicMax(hv_key + lone_v, key + 1ull);
+      }
       nm++;
     } else {
       const int e0 = id[0], e1 = id[1], e2 = id[2], e3 = id[3];
@@ -185,7 +190,7 @@ __global__ void __launch_bounds__(256, 8) he_pack4_kernel(const int32_t* faces, 
 }  // namespace
 
 int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& o, HeWork& w, int sms,
-                    cudaStream_t st) {
+                    cudaStream_t st, bool handles) {
   const int64_t nh = nf * P;
   auto grid = [&](int64_t n) {
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)sms * 8));
@@ -193,14 +198,26 @@ int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& 
   int k = 0;
   // the lone-halfedge list reuses the slot array, which is dead once the lists are scattered
   unsigned long long* lone_count = w.total + 1;
-  he_vertex_init_kernel<<<grid(nv), 256, 0, st>>>(w.hv_key, w.deg, o.hv, nv, lone_count);
-  he_build_kernel<<<grid(nh), 256, 0, st>>>(faces, nh, w.deg, w.rank, o.hv);
-  k += 2 + scan_i32(w.deg, nv, w.off, w.tiles, w.total, st);
+  if (handles) {
+    he_vertex_init_kernel<<<grid(nv), 256, 0, st>>>(w.hv_key, w.deg, o.hv, nv, lone_count);
+    he_build_kernel<true><<<grid(nh), 256, 0, st>>>(faces, nh, w.deg, w.rank, o.hv);
+    k += 2;
+  } else {
+    cudaMemsetAsync(w.deg, 0, (size_t)nv * sizeof(int32_t), st);
+    he_build_kernel<false><<<grid(nh), 256, 0, st>>>(faces, nh, w.deg, w.rank, nullptr);
+    k += 1;
+  }
+  k += scan_i32(w.deg, nv, w.off, w.tiles, w.total, st);
   he_scatter_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.off, w.rank, w.list);
-  he_twin_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.list, w.off, (int)nv, o.twin, o.flag, w.hv_key,
-                                           w.non_manifold, w.rank, lone_count);
-  he_override_kernel<<<(unsigned)std::max(1, sms), 256, 0, st>>>(faces, P, w.rank, lone_count, o.hv, w.hv_key);
-  return k + 3;
+  if (handles) {
+    he_twin_kernel<true><<<grid(nh), 256, 0, st>>>(faces, P, nf, w.list, w.off, (int)nv, o.twin, o.flag, w.hv_key,
+                                                   w.non_manifold, w.rank, lone_count);
+    he_override_kernel<<<(unsigned)std::max(1, sms), 256, 0, st>>>(faces, P, w.rank, lone_count, o.hv, w.hv_key);
+    return k + 3;
+  }
+  he_twin_kernel<false><<<grid(nh), 256, 0, st>>>(faces, P, nf, w.list, w.off, (int)nv, o.twin, o.flag, nullptr,
+                                                  w.non_manifold, nullptr, nullptr);
+  return k + 2;
 }
 
 int pack_halfedges4(const int32_t* faces, int P, const int32_t* twin, int64_t nh, int32_t* he4, int32_t* hf, int sms,

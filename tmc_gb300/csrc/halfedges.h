@@ -29,8 +29,10 @@ struct HeWork {
 };
 
 // Returns the number of kernels launched.
+// handles = false: twins, flags and out-degrees only (o.hv, w.hv_key and the lone list untouched),
+// for the simplification passes, which never read the vertex handles.
 int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& o, HeWork& w, int sms,
-                    cudaStream_t st);
+                    cudaStream_t st, bool handles = true);
 // {origin, face, next, twin} int4 records and the face handles (first halfedge of each face) of the
 // public output
 int pack_halfedges4(const int32_t* faces, int P, const int32_t* twin, int64_t nh, int32_t* he4, int32_t* hf, int sms,

@@ -426,7 +426,7 @@ extern "C" tmc_status tmc_mesh_check(tmc_ctx* ctx, const tmc_mesh* mesh, int32_t
   if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, 64, st);
   unsigned long long h_counts[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (e == cudaSuccess) {
-    int k = build_halfedges(d.faces, P, nf, nv, ho, w, sms, st);
+    int k = build_halfedges(d.faces, P, nf, nv, ho, w, sms, st, false);  // twins and flags only
     iota_kernel<<<grid_of(nf, sms), 256, 0, st>>>(parent, nf);
     check_edges_kernel<<<grid_of(nh, sms), 256, 0, st>>>(d.faces, P, nf, ho.twin, ho.flag, parent, vbound, counts);
     count_roots_kernel<<<grid_of(std::max(nf, nv), sms), 256, 0, st>>>(parent, nf, vbound, nv, counts);
