@@ -135,31 +135,32 @@ __global__ void __launch_bounds__(kScanThreads, 4) dmc_classify_kernel(CellSpace
   if (threadIdx.x == 0) tile_sums[tile] = tile_sum;
 }
 
-// In-tile exclusive scan of the records -> per-cell vertex and quad offsets (striped: coalesced
-// record loads and offset stores), and one work item per vertex: the cell that generates it.
+// In-tile exclusive scan of the records -> per-cell vertex and quad offsets (blocked: 16-byte record
+// loads and offset stores, one block scan of the thread totals), and one work item per vertex: the
+// cell that generates it.
 __global__ void __launch_bounds__(kScanThreads) dmc_offsets_kernel(int64_t n, const uint32_t* rec,
                                                                   const unsigned long long* tile_off,
                                                                   int32_t* voff, int32_t* qoff, uint32_t* vwork) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t seg = (int64_t)blockIdx.x * kScanTile + (int64_t)w * 32 * kScanItems;
+  const int64_t first = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
   uint32_t r[kScanItems];
-  unsigned long long v[kScanItems];
+  load8(rec, first, n, r);
+  unsigned long long sum = 0;
+#pragma unroll
+  for (int s = 0; s < kScanItems; s++) sum += ((unsigned long long)rec_nv(r[s]) << 32) | rec_nq(r[s]);
+  unsigned long long tot;
+  unsigned long long pre = tile_off[blockIdx.x] + block_exclusive_scan(sum, &tot);
+  int32_t vo[kScanItems], qo[kScanItems];
 #pragma unroll
   for (int s = 0; s < kScanItems; s++) {
-    const int64_t c = seg + 32 * s + lane;
-    r[s] = c < n ? rec[c] : 0u;
-    v[s] = ((unsigned long long)rec_nv(r[s]) << 32) | (unsigned long long)rec_nq(r[s]);
+    vo[s] = (int32_t)(pre >> 32);
+    qo[s] = (int32_t)(pre & 0xffffffffull);
+    pre += ((unsigned long long)rec_nv(r[s]) << 32) | rec_nq(r[s]);
   }
-  tile_striped_exclusive_scan(v, tile_off[blockIdx.x]);
+  store8(voff, first, n, vo);
+  store8(qoff, first, n, qo);
 #pragma unroll
-  for (int s = 0; s < kScanItems; s++) {
-    const int64_t c = seg + 32 * s + lane;
-    if (c < n) {
-      voff[c] = (int32_t)(v[s] >> 32);
-      qoff[c] = (int32_t)(v[s] & 0xffffffffull);
-      for (int q = 0; q < rec_nv(r[s]); q++) vwork[(v[s] >> 32) + q] = (uint32_t)c;
-    }
-  }
+  for (int s = 0; s < kScanItems; s++)
+    for (int q = 0; q < rec_nv(r[s]); q++) vwork[vo[s] + q] = (uint32_t)(first + s);  // empty beyond n
 }
 
 // ------------------------------------------------------------------------------------------

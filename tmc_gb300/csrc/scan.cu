@@ -69,20 +69,21 @@ __global__ void __launch_bounds__(kScanThreads) flag_tile_sum_kernel(const uint8
 
 __global__ void __launch_bounds__(kScanThreads) flag_offsets_kernel(const uint8_t* flags, int64_t n,
                                                                    const unsigned long long* tile_off, int32_t* out) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t seg = (int64_t)blockIdx.x * kScanTile + (int64_t)w * 32 * kScanItems;
-  unsigned long long v[kScanItems];
+  const int64_t first = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  uint32_t f[kScanItems];
+  load8(flags, first, n, f);
+  int32_t sum = 0;
 #pragma unroll
-  for (int q = 0; q < kScanItems; q++) {
-    const int64_t i = seg + 32 * q + lane;
-    v[q] = (i < n && flags[i] != 0) ? 1ull : 0ull;
-  }
-  tile_striped_exclusive_scan(v, tile_off[blockIdx.x]);
+  for (int s = 0; s < kScanItems; s++) sum += f[s] != 0;
+  int32_t tot;
+  int32_t pre = (int32_t)tile_off[blockIdx.x] + block_exclusive_scan(sum, &tot);
+  int32_t o[kScanItems];
 #pragma unroll
-  for (int q = 0; q < kScanItems; q++) {
-    const int64_t i = seg + 32 * q + lane;
-    if (i < n) out[i] = (int32_t)v[q];
+  for (int s = 0; s < kScanItems; s++) {
+    o[s] = pre;
+    pre += f[s] != 0;
   }
+  store8(out, first, n, o);
 }
 int64_t scan_tiles(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
 
@@ -119,20 +120,21 @@ __global__ void __launch_bounds__(kScanThreads) i32_tile_sum_kernel(const int32_
 
 __global__ void __launch_bounds__(kScanThreads) i32_offsets_kernel(const int32_t* in, int64_t n,
                                                                   const unsigned long long* tile_off, int32_t* out) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t seg = (int64_t)blockIdx.x * kScanTile + (int64_t)w * 32 * kScanItems;
-  unsigned long long v[kScanItems];
+  const int64_t first = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  uint32_t x[kScanItems];
+  load8(reinterpret_cast<const uint32_t*>(in), first, n, x);
+  unsigned long long sum = 0;
 #pragma unroll
-  for (int q = 0; q < kScanItems; q++) {
-    const int64_t i = seg + 32 * q + lane;
-    v[q] = i < n ? (unsigned long long)in[i] : 0ull;
-  }
-  tile_striped_exclusive_scan(v, tile_off[blockIdx.x]);
+  for (int s = 0; s < kScanItems; s++) sum += x[s];
+  unsigned long long tot;
+  unsigned long long pre = tile_off[blockIdx.x] + block_exclusive_scan(sum, &tot);
+  int32_t o[kScanItems];
 #pragma unroll
-  for (int q = 0; q < kScanItems; q++) {
-    const int64_t i = seg + 32 * q + lane;
-    if (i < n) out[i] = (int32_t)v[q];
+  for (int s = 0; s < kScanItems; s++) {
+    o[s] = (int32_t)pre;
+    pre += x[s];
   }
+  store8(out, first, n, o);
 }
 
 int scan_i32(const int32_t* in, int64_t n, int32_t* out, unsigned long long* tile_sums, unsigned long long* total,

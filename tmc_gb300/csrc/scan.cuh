@@ -41,34 +41,47 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T* total) {
   return warp_prefix + x - v;
 }
 
-// Striped in-tile exclusive scan: warp w of the block owns the tile's cells 256w .. 256w + 255, in
-// kScanItems rounds of 32 consecutive cells (lane l takes cell 256w + 32s + l in round s), so that
-// the loads of the values and the stores of the offsets are coalesced.  v[s] is the lane's value in
-// round s; on return v[s] holds its exclusive prefix within the tile (plus `base`).
-__device__ __forceinline__ void tile_striped_exclusive_scan(unsigned long long v[kScanItems],
-                                                            unsigned long long base) {
-  __shared__ unsigned long long wsum[kScanThreads / 32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  unsigned long long run = 0;
+// Blocked tile layout: thread t of tile b owns the kScanItems consecutive elements from
+// b * kScanTile + t * kScanItems, read and written as 16-byte vectors (contiguous across the warp,
+// so the accesses stay coalesced), and scans them serially; one block scan of the thread totals
+// then gives every element its offset.  Elements at n and beyond read as 0 and are not written;
+// a range that is not 16-byte aligned falls back to scalar accesses.
+static_assert(kScanItems == 8, "the blocked accessors move 8 elements per thread");
+__device__ __forceinline__ void load8(const uint32_t* p, int64_t first, int64_t n, uint32_t r[8]) {
+  const uint32_t* q = p + first;
+  if (first + 8 <= n && ((uintptr_t)q & 15) == 0) {
+    const uint4 a = *reinterpret_cast<const uint4*>(q), b = *reinterpret_cast<const uint4*>(q + 4);
+    r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+    r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
+  } else {
 #pragma unroll
-  for (int s = 0; s < kScanItems; s++) {
-    unsigned long long x = v[s];
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    const unsigned long long tot = __shfl_sync(0xffffffffu, x, 31);
-    v[s] = run + x - v[s];
-    run += tot;
+    for (int s = 0; s < 8; s++) r[s] = first + s < n ? q[s] : 0u;
   }
-  if (lane == 0) wsum[w] = run;
-  __syncthreads();
-  unsigned long long pre = base;
-  for (int q = 0; q < w; q++) pre += wsum[q];
+}
+__device__ __forceinline__ void load8(const uint8_t* p, int64_t first, int64_t n, uint32_t r[8]) {
+  const uint8_t* q = p + first;
+  if (first + 8 <= n && ((uintptr_t)q & 7) == 0) {
+    const uint2 a = *reinterpret_cast<const uint2*>(q);
 #pragma unroll
-  for (int s = 0; s < kScanItems; s++) v[s] += pre;
-  __syncthreads();  // wsum is reused by the block's next tile
+    for (int s = 0; s < 4; s++) {
+      r[s] = (a.x >> (8 * s)) & 0xffu;
+      r[4 + s] = (a.y >> (8 * s)) & 0xffu;
+    }
+  } else {
+#pragma unroll
+    for (int s = 0; s < 8; s++) r[s] = first + s < n ? q[s] : 0u;
+  }
+}
+__device__ __forceinline__ void store8(int32_t* p, int64_t first, int64_t n, const int32_t v[8]) {
+  int32_t* q = p + first;
+  if (first + 8 <= n && ((uintptr_t)q & 15) == 0) {
+    *reinterpret_cast<int4*>(q) = make_int4(v[0], v[1], v[2], v[3]);
+    *reinterpret_cast<int4*>(q + 4) = make_int4(v[4], v[5], v[6], v[7]);
+  } else {
+#pragma unroll
+    for (int s = 0; s < 8; s++)
+      if (first + s < n) q[s] = v[s];
+  }
 }
 
 // Two counters packed in one 64-bit word (high: a, low: b) scan together: both stay far below

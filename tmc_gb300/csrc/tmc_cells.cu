@@ -589,28 +589,27 @@ __global__ void __launch_bounds__(128) tmc_amb_count_kernel(CellSpace space, uin
   if (sing) atomicAdd(stats + 5, sing);
 }
 
+// In-tile exclusive scan of the records -> per-cell vertex and triangle offsets (blocked layout).
 __global__ void __launch_bounds__(kScanThreads) tmc_offsets_kernel(int64_t n, const uint32_t* rec,
                                                                   const unsigned long long* tile_off,
                                                                   int32_t* voff, int32_t* toff) {
-  // striped in-tile scan: coalesced record loads and offset stores
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t seg = (int64_t)blockIdx.x * kScanTile + (int64_t)w * 32 * kScanItems;
-  unsigned long long v[kScanItems];
+  const int64_t first = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  uint32_t r[kScanItems];
+  load8(rec, first, n, r);
+  unsigned long long sum = 0;
+#pragma unroll
+  for (int s = 0; s < kScanItems; s++) sum += ((unsigned long long)trec_nv(r[s]) << 32) | trec_ntri(r[s]);
+  unsigned long long tot;
+  unsigned long long pre = tile_off[blockIdx.x] + block_exclusive_scan(sum, &tot);
+  int32_t vo[kScanItems], to[kScanItems];
 #pragma unroll
   for (int s = 0; s < kScanItems; s++) {
-    const int64_t c = seg + 32 * s + lane;
-    const uint32_t r = c < n ? rec[c] : 0u;
-    v[s] = ((unsigned long long)trec_nv(r) << 32) | (unsigned long long)trec_ntri(r);
+    vo[s] = (int32_t)(pre >> 32);
+    to[s] = (int32_t)(pre & 0xffffffffull);
+    pre += ((unsigned long long)trec_nv(r[s]) << 32) | trec_ntri(r[s]);
   }
-  tile_striped_exclusive_scan(v, tile_off[blockIdx.x]);
-#pragma unroll
-  for (int s = 0; s < kScanItems; s++) {
-    const int64_t c = seg + 32 * s + lane;
-    if (c < n) {
-      voff[c] = (int32_t)(v[s] >> 32);
-      toff[c] = (int32_t)(v[s] & 0xffffffffull);
-    }
-  }
+  store8(voff, first, n, vo);
+  store8(toff, first, n, to);
 }
 
 // corner value v of a cell's eight (selects, so that a run-time index keeps u in registers)
