@@ -627,16 +627,19 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     he_version = mesh_version;
     he_handles = handles;
   };
-  auto read_total = [&]() -> int64_t {
-    cudaMemcpyAsync(h_cnt, total, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+  // both compaction totals of a pass (kept vertices in total[0], kept quads in total[1]), one host
+  // synchronisation
+  auto read_totals = [&](int64_t& nv2, int64_t& nq2) {
+    cudaMemcpyAsync(h_cnt, total, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
-    return (int64_t)h_cnt[0];
+    nv2 = (int64_t)h_cnt[0];
+    nq2 = (int64_t)h_cnt[1];
   };
 
   const bool simplify = c3x3y || i3x3y || p3333;
   int32_t* val = nullptr;
-  uint8_t *p = nullptr, *branch = nullptr, *vm_first = nullptr, *em = nullptr, *keep = nullptr;
-  int32_t *own_pos = nullptr, *own_rm = nullptr, *vm_second = nullptr, *idx = nullptr;
+  uint8_t *p = nullptr, *branch = nullptr, *vm_first = nullptr, *em = nullptr, *keep = nullptr, *keep_q = nullptr;
+  int32_t *own_pos = nullptr, *own_rm = nullptr, *vm_second = nullptr, *idx = nullptr, *idx_q = nullptr;
   int4* jobs = nullptr;
   unsigned* njobs = nullptr;
   if (simplify) {
@@ -645,13 +648,15 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     branch = pool.get<uint8_t>(NQ);
     vm_first = pool.get<uint8_t>(NV);
     em = pool.get<uint8_t>(NQ);
-    keep = pool.get<uint8_t>(std::max(NV, NQ));
+    keep = pool.get<uint8_t>(NV);
+    keep_q = pool.get<uint8_t>(NQ);
+    idx_q = pool.get<int32_t>(NQ);
     own_pos = pool.get<int32_t>(NV);
     own_rm = pool.get<int32_t>(NV);
     vm_second = pool.get<int32_t>(NV);
     jobs = pool.get<int4>(NQ);
     njobs = pool.get<unsigned>(2);
-    idx = pool.get<int32_t>(std::max(NV, NQ));
+    idx = pool.get<int32_t>(NV);
     if (pool.err) {
       s.err = pool.err;
         return s;
@@ -720,22 +725,18 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     cudaMemsetAsync(njobs, 0, sizeof(unsigned), st);
     merge_apply_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.nq, branch, own_pos, own_rm, vm_first, vm_second, em, jobs,
                                            njobs);
-    midpoint_kernel<<<gq, 256, 0, st>>>(jobs, njobs, cur.v64, cur.n64);
+    static const int r_mid = resident_blocks(midpoint_kernel, 256);  // one wave over the merge list
+    midpoint_kernel<<<(unsigned)wave_grid(r_mid, sms, 1, cur.nq, 256), 256, 0, st>>>(jobs, njobs, cur.v64, cur.n64);
     s.launches += 9;
-    // remove vertices
+    // kept vertices and kept quads: new indices of both, one host read of the two counts
     invert_flags_kernel<<<gv, 256, 0, st>>>(vm_first, cur.nv, keep);
     s.launches += 1 + scan_flags(keep, cur.nv, idx, tiles, total, st);
-    int64_t nv2 = read_total();
-    if (nv2 == cur.nv) {
-      // no vertex merged: if no quad was removed either the pass changed nothing (only the merged
-      // pair's midpoints are written), and the mesh stays as it is
-      invert_flags_kernel<<<gq, 256, 0, st>>>(em, cur.nq, keep);
-      s.launches += 1 + scan_flags(keep, cur.nq, idx, tiles, total, st);
-      if (read_total() == cur.nq) continue;
-      invert_flags_kernel<<<gv, 256, 0, st>>>(vm_first, cur.nv, keep);
-      s.launches += 1 + scan_flags(keep, cur.nv, idx, tiles, total, st);
-      nv2 = read_total();
-    }
+    invert_flags_kernel<<<gq, 256, 0, st>>>(em, cur.nq, keep_q);
+    s.launches += 1 + scan_flags(keep_q, cur.nq, idx_q, tiles, total + 1, st);
+    int64_t nv2 = 0, nq2 = 0;
+    read_totals(nv2, nq2);
+    // nothing merged and nothing removed: the pass changed nothing, and the mesh stays as it is
+    if (nv2 == cur.nv && nq2 == cur.nq) continue;
     DmcMesh nx = cur;
     if ((s.err = new_vertices(nv2, nx)) != cudaSuccess) break;
     adopt(nx.v64);
@@ -745,15 +746,12 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     gather_vertices_kernel<<<grid_for(3 * cur.nv, sms), 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.n64, nx.v64,
                                                                        nx.n64, vm_second, nv2, hw.ovf);
     // remove quads
-    invert_flags_kernel<<<gq, 256, 0, st>>>(em, cur.nq, keep);
-    s.launches += 2 + scan_flags(keep, cur.nq, idx, tiles, total, st);
-    const int64_t nq2 = read_total();
     void* qn = nullptr;
     if ((s.err = cudaMallocAsync(&qn, std::max<int64_t>(nq2, 1) * 4 * sizeof(int32_t), st)) != cudaSuccess) break;
     adopt(qn);
-    gather_quads_3x3y_kernel<<<gq, 256, 0, st>>>(em, idx, cur.nq, cur.quads, vm_first, vm_second, (int32_t*)qn,
+    gather_quads_3x3y_kernel<<<gq, 256, 0, st>>>(em, idx_q, cur.nq, cur.quads, vm_first, vm_second, (int32_t*)qn,
                                                   nq2, hw.ovf);
-    s.launches += 1;
+    s.launches += 2;
     // the inherited colours are only read by the colour pass; they are not carried along
     retire(cur.v64);
     retire(cur.v);
@@ -785,19 +783,12 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     mark3333_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.nq, val, p3, rflag, vm0, vm1);
     invert_flags_kernel<<<gv, 256, 0, st>>>(vm0, cur.nv, keep);
     s.launches += 5 + scan_flags(keep, cur.nv, idx, tiles, total, st);
-    int64_t nv2 = read_total();
-    bool unchanged = false;
-    if (nv2 == cur.nv) {
-      // no vertex removed: with no quad removed either, the mesh stays as it is
-      invert_flags_kernel<<<gq, 256, 0, st>>>(rflag, cur.nq, keep);
-      s.launches += 1 + scan_flags(keep, cur.nq, idx, tiles, total, st);
-      unchanged = read_total() == cur.nq;
-      if (!unchanged) {
-        invert_flags_kernel<<<gv, 256, 0, st>>>(vm0, cur.nv, keep);
-        s.launches += 1 + scan_flags(keep, cur.nv, idx, tiles, total, st);
-        nv2 = read_total();
-      }
-    }
+    invert_flags_kernel<<<gq, 256, 0, st>>>(rflag, cur.nq, keep_q);
+    s.launches += 1 + scan_flags(keep_q, cur.nq, idx_q, tiles, total + 1, st);
+    int64_t nv2 = 0, nq2 = 0;
+    read_totals(nv2, nq2);
+    // no vertex and no quad removed: the mesh stays as it is
+    const bool unchanged = nv2 == cur.nv && nq2 == cur.nq;
     DmcMesh nx = cur;
     if (!unchanged && (s.err = new_vertices(nv2, nx)) == cudaSuccess) {
       adopt(nx.v64);
@@ -806,13 +797,11 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
       adopt(nx.n64);
       gather_vertices_kernel<<<grid_for(3 * cur.nv, sms), 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.n64, nx.v64,
                                                                          nx.n64, vm2, nv2, hw.ovf);
-      invert_flags_kernel<<<gq, 256, 0, st>>>(rflag, cur.nq, keep);
-      s.launches += 2 + scan_flags(keep, cur.nq, idx, tiles, total, st);
-      const int64_t nq2 = read_total();
+      s.launches += 1;
       void* qn = nullptr;
       if ((s.err = cudaMallocAsync(&qn, std::max<int64_t>(nq2, 1) * 4 * sizeof(int32_t), st)) == cudaSuccess) {
         adopt(qn);
-        gather_quads_3333_kernel<<<gq, 256, 0, st>>>(rflag, idx, cur.nq, cur.quads, p3, vm1, vm2, (int32_t*)qn, nq2,
+        gather_quads_3333_kernel<<<gq, 256, 0, st>>>(rflag, idx_q, cur.nq, cur.quads, p3, vm1, vm2, (int32_t*)qn, nq2,
                                                       hw.ovf);
         s.launches += 1;
         retire(cur.v64);

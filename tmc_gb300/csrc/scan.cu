@@ -56,12 +56,11 @@ namespace tmc {
 // Generic compaction scan of 0/1 flags (one byte each): out[i] = number of set flags before i.
 __global__ void __launch_bounds__(kScanThreads) flag_tile_sum_kernel(const uint8_t* flags, int64_t n,
                                                                     unsigned long long* tile_sums) {
-  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  uint32_t f[kScanItems];
+  load8(flags, (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems, n, f);
   unsigned long long s = 0;
-  for (int q = 0; q < kScanItems; q++) {
-    const int64_t i = base + (int64_t)q * kScanThreads + threadIdx.x;
-    if (i < n) s += flags[i] != 0;
-  }
+#pragma unroll
+  for (int q = 0; q < kScanItems; q++) s += f[q] != 0;
   unsigned long long tot;
   block_exclusive_scan<unsigned long long>(s, &tot);
   if (threadIdx.x == 0) tile_sums[blockIdx.x] = tot;
@@ -107,12 +106,12 @@ namespace tmc {
 // Exclusive scan of non-negative int32 values: out[i] = sum of in[0..i).
 __global__ void __launch_bounds__(kScanThreads) i32_tile_sum_kernel(const int32_t* in, int64_t n,
                                                                    unsigned long long* tile_sums) {
-  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  uint32_t x[kScanItems];
+  load8(reinterpret_cast<const uint32_t*>(in), (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems, n,
+        x);
   unsigned long long s = 0;
-  for (int q = 0; q < kScanItems; q++) {
-    const int64_t i = base + (int64_t)q * kScanThreads + threadIdx.x;
-    if (i < n) s += (unsigned long long)in[i];
-  }
+#pragma unroll
+  for (int q = 0; q < kScanItems; q++) s += x[q];
   unsigned long long tot;
   block_exclusive_scan<unsigned long long>(s, &tot);
   if (threadIdx.x == 0) tile_sums[blockIdx.x] = tot;
