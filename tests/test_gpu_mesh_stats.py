@@ -145,3 +145,23 @@ def test_mesh_check_against_numpy(ctx, name):
                     assert got["orientation_defects"] == 0
         finally:
             ctx.free(m)
+
+
+def test_mesh_check_unaligned_device_faces(ctx):
+    """A caller's device mesh whose quads start 4 bytes into a buffer (not 16-byte aligned) gets
+    the counts of the same mesh from host arrays: the per-face twin pass then reads and writes
+    without 16-byte vectors."""
+    torch = pytest.importorskip("torch")
+    vol = V.blobs_volume(40, seed=9)
+    d = ctx.dmc(vol, native.OUT_TRIANGLES)
+    q, v, n = d["q"], d["v"], d["n"]
+    assert q.size > 0
+    want = ctx.check(native.host_mesh(v, n, quads=q), native.FACES_QUADS)
+    buf = torch.zeros(q.size + 1, dtype=torch.int32, device="cuda")
+    buf[1:] = torch.from_numpy(q).cuda()
+    vd, nd = torch.from_numpy(v).cuda(), torch.from_numpy(n).cuda()
+    m = native.Mesh()
+    m.nr_v, m.nr_q, m.on_device = v.size // 3, q.size // 4, 1
+    m.v, m.n, m.quads = vd.data_ptr(), nd.data_ptr(), buf.data_ptr() + 4
+    assert m.quads % 16 != 0
+    assert ctx.check(m, native.FACES_QUADS) == want

@@ -81,81 +81,113 @@ __device__ __forceinline__ void edge_ids_insert(EdgeIds& e, int x) {
 __device__ __forceinline__ int list_end(const int32_t* off, int v, int nv, int nh) {
   return v + 1 < nv ? off[v + 1] : nh;
 }
-__device__ __forceinline__ EdgeIds edge_halfedges(const int2* list, const int32_t* off, int nv, int nh, int a, int b) {
-  EdgeIds e;
-  e.c = 0;
-  e.id[0] = e.id[1] = e.id[2] = e.id[3] = INT_MAX;
-  for (int q = off[a], end = list_end(off, a, nv, nh); q < end; q++) {
-    const int2 x = list[q];
-    if (x.y == b) edge_ids_insert(e, x.x);
-  }
-  if (a != b) {
-    for (int q = off[b], end = list_end(off, b, nv, nh); q < end; q++) {
-      const int2 x = list[q];
-      if (x.y == a) edge_ids_insert(e, x.x);
+
+// The twins and flags of a three- or four-halfedge edge {v0, v1} (ids ascending in e), written by
+// its lowest halfedge's thread.  kHandles: list the lone halfedge of a three-halfedge edge and its
+// key for the vertex handle override.
+template <bool kHandles>
+__device__ __forceinline__ void resolve_group(const int32_t* faces, const EdgeIds& e, int v0, int v1, int32_t* twin,
+                                              uint8_t* flag, unsigned long long* hv_key, int32_t* lone,
+                                              unsigned long long* lone_count) {
+  if (e.c == 3) {
+    const int e0 = e.id[0], e1 = e.id[1], e2 = e.id[2];
+    const int a0 = faces[e0], a1 = faces[e1], a2 = faces[e2];
+    flag[e0] = 2;
+    flag[e1] = 2;
+    flag[e2] = 2;
+    int lone_v, lone_h;
+    if (a0 != a1) {
+      twin[e0] = e1; twin[e1] = e0; twin[e2] = -1; lone_v = a2; lone_h = e2;
+    } else if (a0 != a2) {
+      twin[e0] = e2; twin[e2] = e0; twin[e1] = -1; lone_v = a1; lone_h = e1;
+    } else {
+      twin[e1] = e2; twin[e2] = e1; twin[e0] = -1; lone_v = a0; lone_h = e0;
     }
+    if (kHandles) {
+      lone[atomicAdd(lone_count, 1ull)] = lone_h;  // for the handle override
+      // the last override in key order wins: remember the largest key (+1 so that 0 = none)
+      const unsigned long long key = ((unsigned long long)(unsigned)min(v0, v1) << 32) | (unsigned)max(v0, v1);
+      atomicMax(hv_key + lone_v, key + 1ull);
+    }
+  } else {
+    const int e0 = e.id[0], e1 = e.id[1], e2 = e.id[2], e3 = e.id[3];
+    if (faces[e0] != faces[e1]) {
+      twin[e0] = e1; twin[e1] = e0; twin[e2] = e3; twin[e3] = e2;
+    } else {
+      twin[e0] = e2; twin[e2] = e0; twin[e1] = e3; twin[e3] = e1;
+    }
+    flag[e0] = 1; flag[e1] = 1; flag[e2] = 1; flag[e3] = 1;
   }
-  return e;
 }
 
-// one thread per halfedge: two-halfedge edges pair without coordination; 3 or 4 are resolved by
-// the edge's lowest halfedge, which writes the twins and flags of all of them; every other
-// halfedge writes its own (each entry is written exactly once).  kHandles: list the lone halfedges
-// of three-halfedge edges and their keys for the vertex handle override.
-template <bool kHandles>
-__global__ void he_twin_kernel(const int32_t* faces, int P, int64_t nf, const int2* list, const int32_t* off,
-                               int nv, int32_t* twin, uint8_t* flag, unsigned long long* hv_key,
+// One thread per face.  The list of corner r's vertex a is read once and serves the face's two
+// edges at a: the edge leaving a (halfedges a -> next, forward) and the edge arriving at a (the
+// opposite halfedges a -> prev, unless the edge is degenerate, prev == a, whose halfedges are all
+// in a's list and counted once as forward).  Per edge the result is the set edge {v_r, v_r+1}
+// has, however the face repeats vertices.  Two-halfedge edges pair without coordination; 3 or 4
+// are resolved by the edge's lowest halfedge, which writes the twins and flags of all of them;
+// every other halfedge is written by its own face (each entry exactly once, as one 16-byte store
+// for a quad whose four entries are its own).
+template <int P, bool kHandles>
+__global__ void he_twin_kernel(const int32_t* faces, int64_t nf, const int2* list, const int32_t* off, int nv,
+                               int32_t* twin, uint8_t* flag, unsigned long long* hv_key,
                                unsigned long long* non_manifold, int32_t* lone, unsigned long long* lone_count) {
-  const int64_t nh = nf * P;
+  const int nh = (int)(nf * P);
+  // 16-byte face loads and twin stores only on aligned arrays (a caller's mesh may be a slice)
+  const bool vec = P == 4 && ((reinterpret_cast<uintptr_t>(faces) | reinterpret_cast<uintptr_t>(twin)) & 15) == 0 &&
+                   (reinterpret_cast<uintptr_t>(flag) & 3) == 0;
   unsigned long long nm = 0;
-  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t f = h / P;
-    const int r = (int)(h - f * P);
-    const int v0 = faces[h], v1 = faces[f * P + (r + 1) % P];
-    const EdgeIds e = edge_halfedges(list, off, nv, (int)nh, v0, v1);
-    const int c = e.c;
-    const int* id = e.id;
-    if (c == 2) {
-      twin[h] = (id[0] == (int)h) ? id[1] : id[0];
-      flag[h] = 0;
-      continue;
-    }
-    if (c < 3 || c > 4) {  // boundary, or more halfedges than the rules pair: no twin
-      twin[h] = -1;
-      flag[h] = 0;
-      continue;
-    }
-    if (id[0] != (int)h) continue;  // resolved by the edge's lowest halfedge
-    if (c == 3) {
-      const int e0 = id[0], e1 = id[1], e2 = id[2];
-      const int a0 = faces[e0], a1 = faces[e1], a2 = faces[e2];
-      flag[e0] = 2;
-      flag[e1] = 2;
-      flag[e2] = 2;
-      int lone_v, lone_h;
-      if (a0 != a1) {
-        twin[e0] = e1; twin[e1] = e0; twin[e2] = -1; lone_v = a2; lone_h = e2;
-      } else if (a0 != a2) {
-        twin[e0] = e2; twin[e2] = e0; twin[e1] = -1; lone_v = a1; lone_h = e1;
-      } else {
-        twin[e1] = e2; twin[e2] = e1; twin[e0] = -1; lone_v = a0; lone_h = e0;
-      }
-      if (kHandles) {
-        lone[atomicAdd(lone_count, 1ull)] = lone_h;  // for the handle override
-        // the last override in key order wins: remember the largest key (+1 so that 0 = none)
-        const unsigned long long key = ((unsigned long long)(unsigned)min(v0, v1) << 32) | (unsigned)max(v0, v1);
-        atomicMax(hv_key + lone_v, key + 1ull);
-      }
-      nm++;
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += (int64_t)gridDim.x * blockDim.x) {
+    int v[P];
+    if (vec) {
+      const int4 q = reinterpret_cast<const int4*>(faces)[f];
+      v[0] = q.x; v[1] = q.y; v[2] = q.z; v[P - 1] = q.w;
     } else {
-      const int e0 = id[0], e1 = id[1], e2 = id[2], e3 = id[3];
-      if (faces[e0] != faces[e1]) {
-        twin[e0] = e1; twin[e1] = e0; twin[e2] = e3; twin[e3] = e2;
-      } else {
-        twin[e0] = e2; twin[e2] = e0; twin[e1] = e3; twin[e3] = e1;
+#pragma unroll
+      for (int r = 0; r < P; r++) v[r] = faces[P * f + r];
+    }
+    EdgeIds E[P];
+#pragma unroll
+    for (int r = 0; r < P; r++) {
+      E[r].c = 0;
+      E[r].id[0] = E[r].id[1] = E[r].id[2] = E[r].id[3] = INT_MAX;
+    }
+#pragma unroll
+    for (int r = 0; r < P; r++) {
+      const int a = v[r], next = v[(r + 1) % P], prev = v[(r + P - 1) % P];
+      for (int q = off[a], end = list_end(off, a, nv, nh); q < end; q++) {
+        const int2 x = list[q];
+        if (x.y == next) edge_ids_insert(E[r], x.x);
+        if (x.y == prev && prev != a) edge_ids_insert(E[(r + P - 1) % P], x.x);
       }
-      flag[e0] = 1; flag[e1] = 1; flag[e2] = 1; flag[e3] = 1;
-      nm++;
+    }
+    int tw[P];
+    unsigned fl = 0, mine = 0;
+#pragma unroll
+    for (int r = 0; r < P; r++) {
+      const int h = (int)(P * f) + r;
+      const EdgeIds& e = E[r];
+      tw[r] = -1;
+      if (e.c == 2) {
+        tw[r] = (e.id[0] == h) ? e.id[1] : e.id[0];
+        mine |= 1u << r;
+      } else if (e.c < 3 || e.c > 4) {  // boundary, or more halfedges than the rules pair: no twin
+        mine |= 1u << r;
+      } else if (e.id[0] == h) {
+        resolve_group<kHandles>(faces, e, v[r], v[(r + 1) % P], twin, flag, hv_key, lone, lone_count);
+        nm++;
+      }
+    }
+    if (vec && mine == 0xfu) {
+      reinterpret_cast<int4*>(twin)[f] = make_int4(tw[0], tw[1], tw[2], tw[P - 1]);
+      reinterpret_cast<uint32_t*>(flag)[f] = fl;
+    } else {
+#pragma unroll
+      for (int r = 0; r < P; r++)
+        if (mine & (1u << r)) {
+          twin[P * f + r] = tw[r];
+          flag[P * f + r] = 0;
+        }
     }
   }
   for (int o = 16; o; o >>= 1) nm += __shfl_down_sync(0xffffffffu, nm, o);
@@ -209,14 +241,24 @@ int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& 
   }
   k += scan_i32(w.deg, nv, w.off, w.tiles, w.total, st);
   he_scatter_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.off, w.rank, w.list);
+  // one thread per face, whole waves of the kernel's resident blocks
+#define HE_TWIN(PP, HH)                                                                                     \
+  {                                                                                                         \
+    static const int res = resident_blocks(he_twin_kernel<PP, HH>, 256);                                    \
+    he_twin_kernel<PP, HH><<<(unsigned)wave_grid(res, sms, 8, nf, 256), 256, 0, st>>>(                       \
+        faces, nf, w.list, w.off, (int)nv, o.twin, o.flag, HH ? w.hv_key : nullptr, w.non_manifold,          \
+        HH ? w.rank : nullptr, HH ? lone_count : nullptr);                                                  \
+  }
+  if (P == 4) {
+    if (handles) HE_TWIN(4, true) else HE_TWIN(4, false)
+  } else {
+    if (handles) HE_TWIN(3, true) else HE_TWIN(3, false)
+  }
+#undef HE_TWIN
   if (handles) {
-    he_twin_kernel<true><<<grid(nh), 256, 0, st>>>(faces, P, nf, w.list, w.off, (int)nv, o.twin, o.flag, w.hv_key,
-                                                   w.non_manifold, w.rank, lone_count);
     he_override_kernel<<<(unsigned)std::max(1, sms), 256, 0, st>>>(faces, P, w.rank, lone_count, o.hv, w.hv_key);
     return k + 3;
   }
-  he_twin_kernel<false><<<grid(nh), 256, 0, st>>>(faces, P, nf, w.list, w.off, (int)nv, o.twin, o.flag, nullptr,
-                                                  w.non_manifold, nullptr, nullptr);
   return k + 2;
 }
 
