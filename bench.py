@@ -736,8 +736,13 @@ def run_serve(args, rank, world, local):
     def srv_collect(t):
         srv.release(srv.wait_raw(t))
 
-    # warm-up: every request once (the plain loop's capacity run warmed its context the same way)
+    # warm-up: every request once in large batches (the plain loop's capacity run warmed its context
+    # the same way), then once at a low arrival rate, where requests run alone: the workers' pinned
+    # host blocks are pooled by size class, and a class first seen inside the timed runs would pay
+    # for pinning new host memory there
     _drive(srv_submit, srv.poll, srv_collect, [0.0] * n)
+    gaps = rng.exponential(1.0 / (0.5 * capacity), size=n)
+    _drive(srv_submit, srv.poll, srv_collect, list(np.cumsum(gaps) - gaps[0]))
     results = []
     with ClockSampler(local) as clk:
         for mult in [float(x) for x in args.rates.split(",")]:
