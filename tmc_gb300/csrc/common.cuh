@@ -17,6 +17,30 @@ namespace tmc {
 // ------------------------------------------------------------------------------------------
 // grid view
 // ------------------------------------------------------------------------------------------
+// Division of a 32-bit unsigned integer by an invariant divisor d >= 1 with one multiply-high, an
+// add and two shifts, exact for every 32-bit dividend: the unsigned method with the correction term
+// of Granlund & Montgomery, "Division by Invariant Integers using Multiplication" (PLDI 1994, sec. 4):
+// l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1, t = mulhi(m, n), q = (t + ((n - t) >> 1)) >> (l - 1)
+// (shifts 0 / 0 for d = 1).  Every cell kernel splits cell indices into (i, j, k) with two of these.
+struct Div32 {
+  uint32_t m = 1, s1 = 0, s2 = 0;  // d = 1
+  __host__ void init(uint32_t d) {
+    uint32_t l = 0;
+    while (l < 32 && (1ull << l) < d) l++;
+    m = (uint32_t)((((1ull << l) - d) << 32) / d + 1);
+    s1 = l < 1 ? l : 1;
+    s2 = l > 1 ? l - 1 : 0;
+  }
+  __host__ __device__ __forceinline__ uint32_t div(uint32_t n) const {
+#ifdef __CUDA_ARCH__
+    const uint32_t t = __umulhi(m, n);
+#else
+    const uint32_t t = (uint32_t)(((uint64_t)m * n) >> 32);
+#endif
+    return (t + ((n - t) >> s1)) >> s2;
+  }
+};
+
 struct Grid {
   const float* f;
   int nx, ny, nz;     // points
@@ -28,6 +52,11 @@ struct Grid {
   int64_t vbase;      // index of cell 0 in the launch's cell space (0 for a single volume)
   double inv2[3];     // 1 / (2 * spacing), for the central-difference gradients
   float inv2f[3];     // the same rounded to float
+  Div32 div_cx, div_cy;  // division by nx - 1 and ny - 1 (cell index -> i, j, k); set_divisors()
+  __host__ void set_divisors() {
+    div_cx.init((uint32_t)(nx - 1));
+    div_cy.init((uint32_t)(ny - 1));
+  }
   __host__ __device__ int cx() const { return nx - 1; }
   __host__ __device__ int cy() const { return ny - 1; }
   __host__ __device__ int cz() const { return nz - 1; }

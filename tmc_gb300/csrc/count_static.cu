@@ -156,6 +156,7 @@ extern "C" tmc_status tmc_dmc_count_static(tmc_ctx* ctx, const tmc_volume* vol, 
   float up = (float)iso;
   if ((double)up < iso) up = std::nextafter(up, INFINITY);
   g.iso_up = up;
+  g.set_divisors();
 
   const cudaStream_t st = ctx_stream(ctx);
   const int64_t tiles = ceil_div(cells, kScanTile);

@@ -48,10 +48,10 @@ __device__ __forceinline__ unsigned mc_case(const float u[8], float iso_up) {
 // Linear cell index -> (i, j, k); cell counts stay below 2^32 (checked by the runtime)
 __device__ __forceinline__ void cell_ijk(const Grid& g, int64_t c, int& i, int& j, int& k) {
   const uint32_t cx = (uint32_t)(g.nx - 1), cy = (uint32_t)(g.ny - 1);
-  const uint32_t cc = (uint32_t)c;
-  const uint32_t r = cc / cx;
+  const uint32_t cc = (uint32_t)c;  // cell indices of a volume stay below 2^32
+  const uint32_t r = g.div_cx.div(cc);
   i = (int)(cc - r * cx);
-  const uint32_t kk = r / cy;
+  const uint32_t kk = g.div_cy.div(r);
   j = (int)(r - kk * cy);
   k = (int)kk;
 }

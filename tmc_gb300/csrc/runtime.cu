@@ -257,6 +257,7 @@ tmc::Grid make_grid(const tmc_volume* vol, const float* dev, double iso) {
   g.inv2[1] = 1.0 / (2 * g.dy);
   g.inv2[2] = 1.0 / (2 * g.dz);
   for (int d = 0; d < 3; d++) g.inv2f[d] = (float)g.inv2[d];
+  g.set_divisors();
   return g;
 }
 

@@ -38,10 +38,10 @@ __device__ __forceinline__ int trec_nv(uint32_t r) { return __popc(trec_owned(r)
 // cell counts stay below 2^32 (checked by the runtime), so 32-bit division suffices
 __device__ __forceinline__ void tcell_ijk(const Grid& g, int64_t c, int& i, int& j, int& k) {
   const uint32_t cx = (uint32_t)(g.nx - 1), cy = (uint32_t)(g.ny - 1);
-  const uint32_t cc = (uint32_t)c;
-  const uint32_t r = cc / cx;
+  const uint32_t cc = (uint32_t)c;  // cell indices of a volume stay below 2^32
+  const uint32_t r = g.div_cx.div(cc);
   i = (int)(cc - r * cx);
-  const uint32_t kk = r / cy;
+  const uint32_t kk = g.div_cy.div(r);
   j = (int)(r - kk * cy);
   k = (int)kk;
 }
