@@ -50,8 +50,9 @@ __global__ void he_build_kernel(const int32_t* faces, int64_t nh, int32_t* deg, 
 }
 
 // (at most 32 registers: 8 blocks of 256 threads fit on an SM, the grid's 8 per SM in one wave)
-__global__ void __launch_bounds__(256, 8) he_scatter_kernel(const int32_t* faces, int P, int64_t nf, const int32_t* off, const int32_t* rank,
-                                  int2* list) {
+template <int P>  // a compile-time face size: h / P without a run-time 64-bit division
+__global__ void __launch_bounds__(256, 8) he_scatter_kernel(const int32_t* faces, int64_t nf, const int32_t* off,
+                                                            const int32_t* rank, int2* list) {
   const int64_t nh = nf * P;
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
     const int64_t f = h / P;
@@ -209,8 +210,9 @@ __global__ void he_override_kernel(const int32_t* faces, int P, const int32_t* l
   }
 }
 
-__global__ void __launch_bounds__(256, 8) he_pack4_kernel(const int32_t* faces, int P, const int32_t* twin, int64_t nh, int32_t* he4,
-                                int32_t* hf) {
+template <int P>
+__global__ void __launch_bounds__(256, 8) he_pack4_kernel(const int32_t* faces, const int32_t* twin, int64_t nh,
+                                                          int32_t* he4, int32_t* hf) {
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
     const int64_t f = h / P;
     const int r = (int)(h - f * P);
@@ -240,7 +242,8 @@ int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& 
     k += 1;
   }
   k += scan_i32(w.deg, nv, w.off, w.tiles, w.total, st);
-  he_scatter_kernel<<<grid(nh), 256, 0, st>>>(faces, P, nf, w.off, w.rank, w.list);
+  if (P == 4) he_scatter_kernel<4><<<grid(nh), 256, 0, st>>>(faces, nf, w.off, w.rank, w.list);
+  else he_scatter_kernel<3><<<grid(nh), 256, 0, st>>>(faces, nf, w.off, w.rank, w.list);
   // one thread per face, whole waves of the kernel's resident blocks
 #define HE_TWIN(PP, HH)                                                                                     \
   {                                                                                                         \
@@ -265,7 +268,8 @@ int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& 
 int pack_halfedges4(const int32_t* faces, int P, const int32_t* twin, int64_t nh, int32_t* he4, int32_t* hf, int sms,
                     cudaStream_t st) {
   const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nh, 256), (int64_t)sms * 8));
-  he_pack4_kernel<<<g, 256, 0, st>>>(faces, P, twin, nh, he4, hf);
+  if (P == 4) he_pack4_kernel<4><<<g, 256, 0, st>>>(faces, twin, nh, he4, hf);
+  else he_pack4_kernel<3><<<g, 256, 0, st>>>(faces, twin, nh, he4, hf);
   return 1;
 }
 
