@@ -58,10 +58,8 @@ def parse():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    from tmc_gb300.replicas import dist_env as env
+    return env()
 
 
 # ------------------------------------------------------------------------------------------------
@@ -163,12 +161,11 @@ def run_ours(args, rank, world, local):
     except RuntimeError:
         from tmc_gb300 import build
         build.build()
+    from tmc_gb300.replicas import Replicas, replica_seed, reports, throughput
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    rep = Replicas(world, "nccl", local)  # replicas: no collective on the data path
     n = args.grid
-    vol = volumes.noise_volume(n, seed=SEED + rank)
+    vol = volumes.noise_volume(n, seed=replica_seed(SEED, rank))
     cells = vol.cells
     voxels = vol.data.size
     ctx = native.Context(local)
@@ -196,17 +193,9 @@ def run_ours(args, rank, world, local):
 
     def barrier():
         torch.cuda.synchronize()
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        rep.barrier()
 
-    def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    max_over_ranks = rep.max_over_ranks
 
     sizes = {}
     for _ in range(args.warmup):
@@ -234,7 +223,7 @@ def run_ours(args, rank, world, local):
     launches = ctx.launches() + ctx_t.launches() - l0
     ms = max_over_ranks(e0.elapsed_time(e1))
     ms_step = ms / args.steps
-    value = world * cells * args.steps / (ms * 1e-3) / 1e9
+    value = throughput(world, cells, args.steps, ms * 1e-3)
     # ---- end to end through the C ABI with host buffers (W untimed steps first) ----
     for _ in range(max(1, args.warmup)):
         mt, md = step(vhost, native.OUT_HOST)
@@ -251,7 +240,7 @@ def run_ours(args, rank, world, local):
         ctx.free(md)
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e = world * cells * args.steps / e2e_s / 1e9
+    e2e = throughput(world, cells, args.steps, e2e_s)
     # ---- per-stage profile (separate pass, not timed above) ----
     ctx.set_profiling(True)
     m = ctx.dmc_raw(vdev, vol.iso, native.OUT_LOCAL)  # front end alone, for its mesh sizes
@@ -321,15 +310,13 @@ def run_ours(args, rank, world, local):
         "stages": stages,
         "clocks": clk.summary(),
     }
-    if rank == 0 and not args.no_cpu_baseline:
+    if reports(rank) and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_port(vol)
     helper.shutdown()
     ctx_t.close()
     ctx.close()
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
-    return out if rank == 0 else None
+    rep.close()
+    return out if reports(rank) else None
 
 
 def _sample_slab(vol, z0, nz):
