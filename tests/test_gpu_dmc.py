@@ -31,6 +31,14 @@ def _cases():
         "noise48": V.small_noise_volume(48, seed=5, coarse=7),
         "saddle33": V.Volume(sad, spacing=(2 / 32,) * 3, iso=0.0),
         "batch3": V.batch_volumes(4, seed=2)[3],
+        # edge cases: corners exactly at the isovalue (integer field, integer isovalue), a slab one cell
+        # thick with uneven spacing, and values near 1000 (float32 steps of 6e-5 around the isovalue)
+        "iso_on_grid": V.Volume(np.round(V.gaussian_blobs(20, 18, 22, np.random.Generator(np.random.PCG64(8))) * 8)
+                                .astype(np.float32), spacing=(0.5, 0.25, 0.75), iso=3.0),
+        "slab2": V.Volume(V.gaussian_blobs(40, 33, 2, np.random.Generator(np.random.PCG64(9))), spacing=(0.1, 0.3, 2.0),
+                          iso=0.3),
+        "offset1000": V.Volume(V.small_noise_volume(24, seed=4).data + np.float32(1000.0), spacing=(1.0, 1.0, 1.0),
+                               iso=1000.0),
         "tiny2": V.Volume(np.array([[[0.0, 1.0], [1.0, 0.0]], [[1.0, 0.0], [0.0, 1.0]]], np.float32),
                           spacing=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0), iso=0.5),
     }
