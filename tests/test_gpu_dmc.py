@@ -37,6 +37,9 @@ def _cases():
                                 .astype(np.float32), spacing=(0.5, 0.25, 0.75), iso=3.0),
         "slab2": V.Volume(V.gaussian_blobs(40, 33, 2, np.random.Generator(np.random.PCG64(9))), spacing=(0.1, 0.3, 2.0),
                           iso=0.3),
+        # long thin grids: cell indices split by large and small divisors
+        "long_x": V.Volume(V.periodic(20000, 3, 4, 900.0), spacing=(1e-3, 0.5, 0.5), iso=0.05),
+        "long_y": V.Volume(V.periodic(3, 9000, 5, 400.0), spacing=(0.5, 1e-3, 0.5), iso=-0.1),
         "offset1000": V.Volume(V.small_noise_volume(24, seed=4).data + np.float32(1000.0), spacing=(1.0, 1.0, 1.0),
                                iso=1000.0),
         "tiny2": V.Volume(np.array([[[0.0, 1.0], [1.0, 0.0]], [[1.0, 0.0], [0.0, 1.0]]], np.float32),

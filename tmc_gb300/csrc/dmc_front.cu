@@ -380,15 +380,28 @@ __device__ __forceinline__ void vertex_outputs(const GridCache& G, int i, int j,
     float nv3[3];
     const float uu = p[0], vv = p[1], ww = p[2];
     const float sgn = flip ? -1.0f : 1.0f;
+    float scale = 0;  // largest corner gradient component: the size of the interpolation's inputs
 #pragma unroll
     for (int d = 0; d < 3; d++) {
+#pragma unroll
+      for (int q = 0; q < 8; q++) scale = fmaxf(scale, fabsf(Gq[q][d]));
       const float a0 = fmaf(uu, Gq[1][d] - Gq[0][d], Gq[0][d]), a1 = fmaf(uu, Gq[3][d] - Gq[2][d], Gq[2][d]);
       const float a2 = fmaf(uu, Gq[5][d] - Gq[4][d], Gq[4][d]), a3 = fmaf(uu, Gq[7][d] - Gq[6][d], Gq[6][d]);
       const float b0 = fmaf(vv, a1 - a0, a0), b1 = fmaf(vv, a3 - a2, a2);
       nv3[d] = sgn * fmaf(ww, b1 - b0, b0);
     }
-    const float rn = rsqrtf(nv3[0] * nv3[0] + nv3[1] * nv3[1] + nv3[2] * nv3[2]);
-    for (int d = 0; d < 3; d++) out.n[o + d] = nv3[d] * rn;
+    const float dot = nv3[0] * nv3[0] + nv3[1] * nv3[1] + nv3[2] * nv3[2];
+    // The float32 interpolation errs by a few ulps of `scale`; where the gradients cancel to below
+    // 1/16 of it (strongly uneven spacing, near critical points) that would exceed ~4e-6 of the
+    // unit normal: the reference's float64 normal instead.
+    if (scale <= 16.0f * sqrtf(dot)) {
+      const float rn = rsqrtf(dot);
+      for (int d = 0; d < 3; d++) out.n[o + d] = nv3[d] * rn;
+    } else {
+      const Normal64 nf = normal_f64(g, i, j, k, (double)p[0], (double)p[1], (double)p[2], flip);
+      for (int d = 0; d < 3; d++) out.n[o + d] = (float)nf.n[d];
+      st.normal_f64++;
+    }
   }
   if (out.vcell) {
     out.vcell[vidx] = cell;
