@@ -50,6 +50,10 @@ def _cases():
                                 .astype(np.float32), spacing=(0.5, 0.25, 0.75), iso=3.0),
         "slab2": V.Volume(V.gaussian_blobs(40, 33, 2, np.random.Generator(np.random.PCG64(9))), spacing=(0.1, 0.3, 2.0),
                           iso=0.3),
+        # a far origin (positions rounded from float64 once) and micro spacing (gradients scaled by ~5e5)
+        "origin_far": V.Volume(V.blobs_volume(24, seed=6).data, spacing=(0.25, 0.5, 0.125),
+                               origin=(12345.5, -6789.25, 3.0), iso=0.5),
+        "tiny_spacing": V.Volume(V.small_noise_volume(20, seed=9).data, spacing=(1e-6, 1.5e-6, 2e-6), iso=0.0),
         # long thin grids: cell indices split by large and small divisors
         "long_x": V.Volume(V.periodic(20000, 3, 4, 900.0), spacing=(1e-3, 0.5, 0.5), iso=0.05),
         "long_y": V.Volume(V.periodic(3, 9000, 5, 400.0), spacing=(0.5, 1e-3, 0.5), iso=-0.1),
