@@ -101,3 +101,28 @@ def test_batch_rejects_bad_requests(ctx):
         ctx.batch(vols, [native.ALGO_DMC, 7], [0, 0])
     with pytest.raises(native.TmcError):
         ctx.batch(vols, [native.ALGO_TMC, native.ALGO_TMC], [native.DMC_SIMPLIFY, 0])
+
+
+def _edge_vols():
+    rng = np.random.Generator(np.random.PCG64(8))
+    return [
+        V.Volume(np.round(V.gaussian_blobs(20, 18, 22, rng) * 8).astype(np.float32), spacing=(0.5, 0.25, 0.75),
+                 iso=3.0),  # corners exactly at the isovalue
+        V.Volume(V.periodic(20000, 3, 4, 900.0), spacing=(1e-3, 0.5, 0.5), iso=0.05),  # long in x
+        V.Volume(V.periodic(3, 9000, 5, 400.0), spacing=(0.5, 1e-3, 0.5), iso=-0.1),  # long in y
+        V.Volume(V.blobs_volume(24, seed=6).data, spacing=(0.25, 0.5, 0.125), origin=(12345.5, -6789.25, 3.0),
+                 iso=0.5),  # far origin
+        V.Volume(V.small_noise_volume(24, seed=4).data + np.float32(1000.0), spacing=(1.0, 1.0, 1.0), iso=1000.0),
+    ]
+
+
+@pytest.mark.parametrize("algo,flags", [(native.ALGO_DMC, native.DMC_SIMPLIFY | native.OUT_TRIANGLES | native.OUT_HALFEDGES),
+                                        (native.ALGO_DMC, native.OUT_POS_F64 | native.OUT_LOCAL),
+                                        (native.ALGO_TMC, native.OUT_POS_F64 | native.OUT_HALFEDGES)])
+def test_batch_of_edge_cases_equals_single_calls(ctx, algo, flags):
+    """Grids of very different shapes in one cell space (long thin axes, a far origin, corners at
+    the isovalue, values near 1000) give each volume the mesh it gets alone."""
+    vols = _edge_vols()
+    got = ctx.batch(vols, [algo] * len(vols), [flags] * len(vols))
+    for q, vol in enumerate(vols):
+        _same(got[q], _single(ctx, vol, algo, flags), f"edge volume {q} algo {algo} flags {flags:#x}")
