@@ -118,14 +118,14 @@ class ClockSampler:
 # ------------------------------------------------------------------------------------------------
 # Kernel groups of the roofline: the profiler stages of one piece of work, and the DRAM traffic per
 # algorithmic byte that ncu measured for them on the 320^3 case of this workload (profiles/
-# dmc_vertex_noise320.md: 2,822 MB for 5.49 M vertices; tmc_emit_noise320.md: 1,207 MB for 267.7 MB of
-# mesh; dmc_classify_noise320.md: 224.0 MB for a 131.1 MB field), scaled to the full launch by the units
+# dmc_vertex_noise320.md: 2,772 MB for 5.49 M vertices; tmc_emit_noise320.md: 1,189 MB for 267.7 MB of
+# mesh; classify_noise320.md: 218.2 MB for a 131.1 MB field), scaled to the full launch by the units
 # it processes (traffic grows with the vertex / cell count).
 ROOFLINE_GROUPS = {
-    "dmc_vertex": (("dmc_vertex_setup", "dmc_project", "dmc_vertex_finish", "dmc_vertex"), 2822.1 / 131.6),
+    "dmc_vertex": (("dmc_vertex_setup", "dmc_project", "dmc_vertex_finish", "dmc_vertex"), 2771.6 / 131.6),
     "dmc_halfedges": (("dmc_halfedges",), None),
-    "tmc_emit": (("tmc_emit",), 1207.3 / 267.7),
-    "dmc_classify": (("dmc_classify",), 224.0 / 131.1),
+    "tmc_emit": (("tmc_emit",), 1188.9 / 267.7),
+    "dmc_classify": (("dmc_classify",), 218.2 / 131.1),
     "tmc_classify": (("tmc_classify",), None),
     "dmc_quad": (("dmc_quad",), None),
     "dmc_triangles": (("dmc_triangles",), None),
