@@ -109,3 +109,21 @@ def test_check_numeric(bad):
         assert strict.tmc(vol)["t"].size > 0
     finally:
         strict.close()
+
+
+def test_check_numeric_in_a_batch():
+    """A batch that holds one field with NaN fails as a whole with TMC_ERR_NUMERIC on a context that
+    checks fields; the same context then runs a clean batch."""
+    good = V.blobs_volume(24, seed=1)
+    data = good.data.copy()
+    data[3, 4, 5] = np.nan
+    bad = V.Volume(data, spacing=good.spacing, iso=good.iso)
+    strict = native.Context(0, check_numeric=True)
+    try:
+        with pytest.raises(native.TmcError) as e:
+            strict.batch([good, bad], [native.ALGO_DMC, native.ALGO_TMC], [0, 0])
+        assert e.value.status == native.TMC_ERR_NUMERIC
+        out = strict.batch([good, good], [native.ALGO_DMC, native.ALGO_TMC], [0, 0])
+        assert out[0]["q"].size > 0 and out[1]["t"].size > 0
+    finally:
+        strict.close()
