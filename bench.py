@@ -15,6 +15,9 @@ larger than L2, so no L2 flush is needed between steps.
 
 Prints one JSON line.  `value` is device-resident throughput (field already in HBM); `e2e` is the
 same metric through the C ABI with host buffers (field copied in, mesh copied out every step).
+The default line also carries `batch` (the 256-volume batched workload: one batched call against
+256 plain calls) and `serve` (Poisson arrivals at 0.5x and 1.5x the plain loop's capacity: the
+server's p50/p99 latency and Gcells/s against one call per request); --no-extras leaves them out.
 Cells per step = 511^3: each step extracts the one volume with both algorithms, and its cells are
 counted once (the CPU baseline and the reference arm count the same way).
 """
@@ -54,6 +57,8 @@ def parse():
     p.add_argument("--requests", type=int, default=256, help="requests per arrival rate of the serve workload")
     p.add_argument("--rates", default="0.5,0.8,1.0,1.5",
                    help="arrival rates of the serve workload, as multiples of the plain loop's capacity")
+    p.add_argument("--no-extras", action="store_true",
+                   help="default workload only, without the batch and serve keys")
     return p.parse_args()
 
 
@@ -856,11 +861,44 @@ def run_plain64(args, rank, world, local):
     return out if rank == 0 else None
 
 
+def headline_extras(args, rank, world, local):
+    """The batched and served workloads, measured beside the default one so that one bench line
+    carries the whole headline metric: `batch` (256 uneven volumes in one batched call against 256
+    plain calls) and `serve` (Poisson arrivals at two rates, the server against one call per request)."""
+    if world > 1:
+        note = "measured at one GPU only (each replica would run the same independent workload)"
+        return {"batch": {"note": note}, "serve": {"note": note}}
+    extras = {}
+    bargs = argparse.Namespace(**vars(args))
+    bargs.steps, bargs.warmup, bargs.volumes = 3, 3, 256
+    b = run_batch(bargs, rank, world, local)
+    extras["batch"] = {
+        "value": b["value"], "unit": "Gcells/s", "ms_per_batch": b["ms_per_step"], "volumes": bargs.volumes,
+        "cells_per_batch": b["config"]["cells_per_step"], "gpu_launches_per_batch": b["gpu_launches"],
+        "plain_calls": {"value": b["plain_calls"]["value"], "ms": b["plain_calls"]["ms_per_step"],
+                        "gpu_launches": b["plain_calls"]["gpu_launches"]},
+        "batched_over_plain": b["batched_over_plain"], "e2e": b["e2e"],
+        "roofline": {k: b["roofline"][k] for k in ("achieved", "peak", "unit", "frac", "algorithmic_bytes_per_launch")},
+        "workload": b["config"]["workload"], "steps": bargs.steps, "warmup": bargs.warmup, "clocks": b["clocks"]}
+    sargs = argparse.Namespace(**vars(args))
+    sargs.requests, sargs.rates = 256, "0.5,1.5"
+    sv = run_serve(sargs, rank, world, local)
+    extras["serve"] = {"rates": sv["rates"], "plain_capacity_req_s": sv["config"]["plain_capacity_req_s"],
+                       "requests_per_rate": sargs.requests, "workload": sv["config"]["workload"],
+                       "server_stats": sv["server_stats"], "clocks": sv["clocks"]}
+    return extras
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         out = run_reference(args, rank, world)
+    elif args.workload == "single" and args.grid == N and not args.no_extras:
+        out = run_ours(args, rank, world, local)
+        extra = headline_extras(args, rank, world, local)
+        if out is not None:
+            out.update(extra)
     elif args.workload == "batch":
         out = run_batch(args, rank, world, local)
     elif args.workload == "precision":

@@ -11,6 +11,7 @@
  *   tmc_batch_extract      (no single reference call: many dualMC / mc_sharedvertex calls in one launch)
  *   tmc_server_*           (no reference counterpart: request loop around the calls above)
  *   tmc_dmc_count_static   (no reference counterpart: DMC mesh sizes without allocating)
+ *   tmc_dmc_color_valence  colorFaces + vertexValence                cpp_dmc/DualMarchingCubes.cpp:714-871
  *   tmc_ctx_*_tuning, tmc_ctx_autotune  (no reference counterpart: launch shapes and their tuner)
  *   tmc_field_load         dmc::UniformGrid::init(file)              cpp_dmc/UniformGrid.cpp:3-45
  *                          readFromFile<T> / readDataFromFile<T>     cpp_dmc/Volumes.h:47, dmc/UniformGrid.h:431
@@ -148,9 +149,20 @@ tmc_status tmc_mesh_free(tmc_ctx* ctx, tmc_mesh* mesh);
  * before admitting the request against a fixed memory budget.  The field must be device memory.
  * Scratch is one static 512 KiB device array per device: grids above 134,217,728 cells (513^3
  * points) fail with TMC_ERR_CAPACITY; calls overlapping in time on one device race on the array
- * and must be serialised; the first call on a device does a one-time set-up
- * (cudaGetSymbolAddress) and should precede any stream capture on that device. */
+ * and must be serialised; every call looks up the array's address (cudaGetSymbolAddress), and
+ * the first call on a device may load the library's device code there, so it should precede any
+ * stream capture on that device.  Volumes are checked as tmc_dmc_extract checks them. */
 tmc_status tmc_dmc_count_static(tmc_ctx* ctx, const tmc_volume* vol, double iso, int64_t counts[4]);
+
+/* The face colouring and vertex valence stage of the DMC simplification on its own: the
+ * reference's colorFaces + vertexValence (cpp_dmc/DualMarchingCubes.cpp:714-871; GPU counterparts
+ * p_mc::FaceColoring::colorFaces, dmc/FaceColoring.cu:121-145, and vertexValence,
+ * dmc/MeshSimplification.cu:45-59).  quads: 4*nr_q vertex ids of a quad mesh; colors: nr_q
+ * inherited colours (3*parity + axis of the dual grid edge, 0..23) on entry, the reduced colours
+ * (0..4) on return; valence: nr_v counts out.  All three are device arrays; the call returns when
+ * they are written. */
+tmc_status tmc_dmc_color_valence(tmc_ctx* ctx, int64_t nr_v, int64_t nr_q, const int32_t* quads, uint8_t* colors,
+                                 int32_t* valence);
 
 /* volume files and mesh files --------------------------------------------------------------- */
 /* The reference's volume file layouts (origin 0; the data x fastest):

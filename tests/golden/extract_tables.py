@@ -1,7 +1,7 @@
 """Extract the reference's Marching Cubes lookup tables into tests/golden/ref_tables.json.
 
-Runs only where the reference checkout is present (default /root/reference, override with the
-REF environment variable).  The JSON is a golden fixture: tests compare the tables this library
+Runs only where the reference checkout is present: its path is the REF environment variable
+(required).  The JSON is a golden fixture: tests compare the tables this library
 generates (tmc_gb300/csrc/mc_tables.h) against it, and tmc_gb300/csrc/gen_tables.py packs the
 two tables that are arbitrary data (the contour start edges of cpp_dmc/LookupTables.h r_pattern
 and the triangle list mc/MarchingCubes.h t_pattern) from it.
@@ -15,7 +15,7 @@ import os
 import re
 import sys
 
-REF = os.environ.get("REF", "/root/reference")
+REF = os.environ.get("REF", "")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 

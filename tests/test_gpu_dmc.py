@@ -66,6 +66,13 @@ def _close32(a32, b64, ulps=2, abs_tol=1e-300):
 NORMAL_ABS_TOL = 2.0 ** -40
 
 
+def split_differences(got_t, want_t):
+    """Number of quads whose two triangles differ from the oracle's (the split decision)."""
+    gt, wt = got_t.reshape(-1, 6), want_t.reshape(-1, 6)
+    assert gt.shape == wt.shape
+    return int(np.count_nonzero(np.any(gt != wt, axis=1)))
+
+
 @pytest.mark.parametrize("name", sorted(CASES))
 @pytest.mark.parametrize("flip", [0, 1])
 def test_dmc_front_matches_oracle(ctx, oracle, name, flip):
@@ -149,11 +156,8 @@ def test_dmc_full_pipeline_matches_oracle(ctx, oracle, name, simplify):
     np.testing.assert_array_equal(got["he"].reshape(-1, 4), he5[:, :4])
     np.testing.assert_array_equal(got["hv"], want["hv"])
     np.testing.assert_array_equal(got["hf"], want["hf"])
-    # quad -> triangle split: identical except where the reference's decision is a float32 tie
-    # that its libm acosf rounds differently from a correctly rounded acos
-    gt, wt = got["t"].reshape(-1, 6), want["t"].reshape(-1, 6)
-    diff = np.nonzero(np.any(gt != wt, axis=1))[0]
-    assert diff.size <= max(1, gt.shape[0] // 100000), f"{diff.size} quads split differently"
+    # quad -> triangle split: bit-exact (the host library's float acos restated on the GPU)
+    assert split_differences(got["t"], want["t"]) == 0
 
 
 def test_dmc_saddle_crops_float64_mean_point(ctx):
@@ -169,3 +173,11 @@ def test_dmc_saddle_crops_float64_mean_point(ctx):
         np.testing.assert_array_equal(got["q"], z[f"q{q}"])
         np.testing.assert_array_equal(got["v64"], z[f"v{q}"])
         assert got["stats"][3] >= 1  # the reference's 26x26 failure counter
+
+
+def test_host_acosf_is_the_restated_one(tmp_path):
+    """The split parity above rests on the GPU's float acos being this host C library's acosf
+    (what the reference's std::acos calls here): bit-equal on every float of [-1, 1]."""
+    from test_acos_cpu import run_acos_check
+    out = run_acos_check(tmp_path)
+    assert out.returncode == 0 and out.stdout.startswith("ok 2130706434"), out.stdout + out.stderr

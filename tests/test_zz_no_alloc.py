@@ -106,6 +106,21 @@ def test_count_static_rejects_oversized_and_host_fields(torch_cuda):
     with pytest.raises(native.TmcError) as e:
         ctx.dmc_count_static(host, 0.5)
     assert e.value.status == native.TMC_ERR_INVALID_ARG
+    # spacing and origin are checked as tmc_dmc_extract checks them
+    for spacing, origin in (((0.0, 1.0, 1.0), (0, 0, 0)), ((1.0, -1.0, 1.0), (0, 0, 0)),
+                            ((1.0, 1.0, float("nan")), (0, 0, 0)), ((1.0, 1.0, 1.0), (0, float("inf"), 0))):
+        bad = native.Volume()
+        bad.nx = bad.ny = bad.nz = 2
+        bad.origin = (ctypes.c_double * 3)(*origin)
+        bad.spacing = (ctypes.c_double * 3)(*spacing)
+        bad.data = small.data_ptr()
+        bad.on_device = 1
+        with pytest.raises(native.TmcError) as e:
+            ctx.dmc_count_static(bad, 0.5)
+        assert e.value.status == native.TMC_ERR_INVALID_ARG
+        with pytest.raises(native.TmcError) as e:
+            ctx.dmc_raw(bad, 0.5, 0)
+        assert e.value.status == native.TMC_ERR_INVALID_ARG
     # the largest accepted grid: 513^3 points
     ok = native.Volume()
     ok.nx = ok.ny = ok.nz = 513

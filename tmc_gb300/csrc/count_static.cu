@@ -15,9 +15,9 @@
 // Limits and sharing.
 //  * The static array holds kStaticMaxTiles tile sums: at most 134,217,728 cells (a 513^3-point
 //    grid).  Larger grids are rejected with TMC_ERR_CAPACITY before anything is launched.
-//  * The first call on each device does a one-time set-up (cudaGetSymbolAddress of the array, which
-//    may load this library's device code); make that first call before any stream capture on the
-//    device.
+//  * Every call looks up the array's device address (cudaGetSymbolAddress, with the context's device
+//    current); the first call on a device may load this library's device code there, so make that
+//    first call before any stream capture on the device.
 //  * Every call on a device uses the same array.  Calls that overlap in time on one device (two
 //    host threads, or two contexts whose streams are not ordered) race on it and return wrong
 //    counts: serialise them.  Each call clears the two cell counters it accumulates atomically;
@@ -45,7 +45,6 @@ constexpr int64_t kTotalWord = kStaticMaxTiles;
 constexpr int64_t kActiveWord = kTotalWord + 1;
 constexpr int64_t kAmbiguousWord = kTotalWord + 2;
 constexpr int64_t kScratchWords = kStaticMaxTiles + 8;  // 512 KiB + 64 B
-constexpr int kMaxDevices = 64;
 }  // namespace
 }  // namespace tmc
 
@@ -88,24 +87,23 @@ __global__ void __launch_bounds__(kScanThreads) dmc_count_static_kernel(Grid g, 
   }
 }
 
+// Device address of the scratch on the current device.  Looked up on every call: the lookup
+// allocates nothing once the module is loaded, and a cudaDeviceReset by the host application (which
+// reloads the module, possibly at another address) then cannot leave a stale pointer behind.  The
+// mutex serialises the first lookups, which may load this library's device code.
 std::mutex g_setup_mutex;
-unsigned long long* g_scratch_ptr[kMaxDevices] = {};
 
-// Device address of the scratch on `dev` (the current device), looked up once per device.
-tmc_status scratch_on_device(tmc_ctx* ctx, int dev, unsigned long long** out) {
+tmc_status scratch_on_device(tmc_ctx* ctx, unsigned long long** out) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, tmc_count_scratch);
-    if (e != cudaSuccess || !p) {
-      char msg[256];
-      snprintf(msg, sizeof msg, "tmc_dmc_count_static: cudaGetSymbolAddress of the static scratch failed: %s",
-               cudaGetErrorString(e));
-      return ctx_fail(ctx, TMC_ERR_CUDA, msg);
-    }
-    g_scratch_ptr[dev] = static_cast<unsigned long long*>(p);
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, tmc_count_scratch);
+  if (e != cudaSuccess || !p) {
+    char msg[256];
+    snprintf(msg, sizeof msg, "tmc_dmc_count_static: cudaGetSymbolAddress of the static scratch failed: %s",
+             cudaGetErrorString(e));
+    return ctx_fail(ctx, TMC_ERR_CUDA, msg);
   }
-  *out = g_scratch_ptr[dev];
+  *out = static_cast<unsigned long long*>(p);
   return TMC_OK;
 }
 
@@ -129,6 +127,10 @@ extern "C" tmc_status tmc_dmc_count_static(tmc_ctx* ctx, const tmc_volume* vol, 
                     "copying a host field would allocate");
   if (vol->nx < 2 || vol->ny < 2 || vol->nz < 2 || vol->nx > 65535 || vol->ny > 65535 || vol->nz > 65535)
     return ctx_fail(ctx, TMC_ERR_INVALID_ARG, "tmc_dmc_count_static: every axis needs 2 to 65535 points");
+  for (int d = 0; d < 3; d++)
+    if (!(vol->spacing[d] > 0) || !std::isfinite(vol->spacing[d]) || !std::isfinite(vol->origin[d]))
+      return ctx_fail(ctx, TMC_ERR_INVALID_ARG,
+                      "tmc_dmc_count_static: spacing must be positive and finite, the origin finite");
   if (!std::isfinite(iso)) return ctx_fail(ctx, TMC_ERR_INVALID_ARG, "tmc_dmc_count_static: iso is not finite");
   const int64_t cells = (int64_t)(vol->nx - 1) * (vol->ny - 1) * (vol->nz - 1);
   if (cells > kStaticMaxCells) {
@@ -140,12 +142,10 @@ extern "C" tmc_status tmc_dmc_count_static(tmc_ctx* ctx, const tmc_volume* vol, 
     return ctx_fail(ctx, TMC_ERR_CAPACITY, msg);
   }
   const int dev = ctx_device(ctx);
-  if (dev < 0 || dev >= kMaxDevices)
-    return ctx_fail(ctx, TMC_ERR_INVALID_ARG, "tmc_dmc_count_static: device index above 63");
   cudaError_t e = cudaSetDevice(dev);
   if (e != cudaSuccess) return cuda_fail(ctx, "cudaSetDevice", e);
   unsigned long long* scratch = nullptr;
-  if (tmc_status s = scratch_on_device(ctx, dev, &scratch)) return s;
+  if (tmc_status s = scratch_on_device(ctx, &scratch)) return s;
 
   Grid g{};
   g.f = vol->data;

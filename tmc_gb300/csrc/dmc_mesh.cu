@@ -19,6 +19,7 @@
 #include "../../include/tmc_gb300.h"
 #include "dmc_mesh.h"
 #include "halfedges.h"
+#include "libm_acosf.h"
 #include "scan.cuh"
 
 namespace tmc {
@@ -392,28 +393,14 @@ __global__ void fill_i32_kernel(int32_t* p, int64_t n, int32_t v) {
 // ---------------------------------------------------------------------------------------------
 // quad -> triangles (collectTriangles, :1387-1460; minAngle, DualMarchingCubes.h:746-756)
 // ---------------------------------------------------------------------------------------------
-// float acos rounded once from the float64 result: correctly rounded in all but vanishingly rare
-// cases (the host library's acosf is not, so splits decided by a 1-ulp tie may differ)
-__device__ __forceinline__ float acos_f(float x) { return (float)acos((double)x); }
-
-// minAngle exactly as the reference (three acos, float min)
+// minAngle exactly as the reference: three float arc cosines of the host C library (restated in
+// libm_acosf.h, bit for bit), float minimum in the reference's std::min order
 __device__ __forceinline__ float min_angle_full(float a, float b, float c) {
-  const float A = acos_f((b * b + c * c - a * a) / (2 * b * c));
-  const float B = acos_f((a * a + c * c - b * b) / (2 * a * c));
-  const float C = acos_f((b * b + a * a - c * c) / (2 * b * a));
+  const float A = libm::acosf((b * b + c * c - a * a) / (2 * b * c));
+  const float B = libm::acosf((a * a + c * c - b * b) / (2 * a * c));
+  const float C = libm::acosf((b * b + a * a - c * c) / (2 * b * a));
   const float mAB = (B < A) ? B : A;
   return (C < mAB) ? C : mAB;
-}
-
-// The smallest angle is the acos of the largest cosine (acos is monotone); false when a cosine is
-// not a number in [-1, 1], where the reference's min of NaNs is replayed instead.
-__device__ __forceinline__ bool max_cosine(float a, float b, float c, float& m) {
-  const float cA = (b * b + c * c - a * a) / (2 * b * c);
-  const float cB = (a * a + c * c - b * b) / (2 * a * c);
-  const float cC = (b * b + a * a - c * c) / (2 * b * a);
-  if (!(cA >= -1.f && cA <= 1.f && cB >= -1.f && cB <= 1.f && cC >= -1.f && cC <= 1.f)) return false;
-  m = fmaxf(cA, fmaxf(cB, cC));
-  return true;
 }
 
 __device__ __forceinline__ float side(const double* p, const double* q) {
@@ -484,9 +471,12 @@ __global__ void triangles_fast_kernel(const int32_t* q, int64_t nq, const float*
     if (sure) {
       // smallest angle of a split = acos of its largest cosine (acos decreasing): the first split
       // (along v1-v3) wins when its largest cosine is smaller
+      // The bounds place the reference's largest cosines; a further 2^-20 between them keeps its
+      // angles (acos has slope at least 1 in magnitude, and the library's float acos is within one
+      // ulp, at most 2^-22 below pi) strictly ordered the same way.
       const float xb = fmaxf(m1, m2), eb = fmaxf(x1, x2), xc = fmaxf(m3, m4), ec = fmaxf(x3, x4);
-      if (xb + eb < xc - ec) first = false;       // b1 > c1
-      else if (xb - eb > xc + ec) first = true;  // b1 < c1
+      if (xb + eb + 0x1p-20f < xc - ec) first = false;       // b1 > c1
+      else if (xb - eb > xc + ec + 0x1p-20f) first = true;  // b1 < c1
       else sure = false;
     }
     if (sure) write_split(t, i, v0, v1, v2, v3, first);
@@ -502,9 +492,9 @@ __global__ void triangles_fast_kernel(const int32_t* q, int64_t nq, const float*
   }
 }
 
-// collectTriangles (:1387-1460), exact pass over the listed quads.  Six distinct side lengths
-// (float of a float64 distance, as the reference), four largest cosines in float32; acos only where
-// two candidate angles are within a few ulps of each other.
+// collectTriangles (:1387-1460), exact pass over the listed quads: the reference's arithmetic
+// step by step.  Six side lengths (float of a float64 distance), minAngle of the four triangles with
+// the host library's float acos (libm_acosf.h), float64 comparisons of the two splits.
 __global__ void triangles_kernel(const int32_t* q, const uint32_t* list, const unsigned* count, const double* v64,
                                  int32_t* t) {
   const int64_t nl = *count;
@@ -515,32 +505,13 @@ __global__ void triangles_kernel(const int32_t* q, const uint32_t* list, const u
                  *P3 = v64 + 3 * (int64_t)v3;
     const float d01 = side(P0, P1), d12 = side(P1, P2), d20 = side(P2, P0), d23 = side(P2, P3), d30 = side(P3, P0),
                 d13 = side(P1, P3);
-    // triangles (v0,v1,v2), (v0,v2,v3) | (v1,v3,v0), (v1,v2,v3); sides a = |p0p1|, b = |p1p2|, c = |p2p0|
-    float m1, m2, m3, m4;
-    bool ok = max_cosine(d01, d12, d20, m1) && max_cosine(d20, d23, d30, m2) && max_cosine(d13, d30, d01, m3) &&
-              max_cosine(d12, d23, d13, m4);
-    bool first;  // true: split along v1-v3
-    if (ok) {
-      // b1 = min angle of the first split, b2 = max; c1, c2 for the second
-      const float xb1 = fmaxf(m1, m2), xb2 = fminf(m1, m2), xc1 = fmaxf(m3, m4), xc2 = fminf(m3, m4);
-      float b1 = acosf(xb1), c1 = acosf(xc1);
-      const float tol = 4.0f * 1.2e-7f * fmaxf(fabsf(b1), fabsf(c1)) + 1e-30f;
-      if (fabsf(b1 - c1) > tol) {
-        first = b1 < c1;
-      } else {
-        b1 = acos_f(xb1);
-        c1 = acos_f(xc1);
-        if (b1 != c1) first = b1 < c1;
-        else first = acos_f(xb2) <= acos_f(xc2);
-      }
-    } else {
-      const double a1 = min_angle_full(d01, d12, d20), a2 = min_angle_full(d20, d23, d30);
-      const double b1 = a2 < a1 ? a2 : a1, b2 = a1 < a2 ? a2 : a1;
-      const double a3 = min_angle_full(d13, d30, d01), a4 = min_angle_full(d12, d23, d13);
-      const double c1 = a4 < a3 ? a4 : a3, c2 = a3 < a4 ? a4 : a3;
-      first = (b1 < c1 || (b1 == c1 && b2 <= c2));
-    }
-    write_split(t, i, v0, v1, v2, v3, first);
+    // triangles (v0,v1,v2), (v0,v2,v3) | (v1,v3,v0), (v1,v2,v3); minAngle(a, b, c) takes the sides
+    // |p0p1|, |p1p2|, |p2p0| of its triangle (p0, p1, p2)
+    const double a1 = min_angle_full(d01, d12, d20), a2 = min_angle_full(d20, d23, d30);
+    const double b1 = a2 < a1 ? a2 : a1, b2 = a1 < a2 ? a2 : a1;
+    const double a3 = min_angle_full(d13, d30, d01), a4 = min_angle_full(d12, d23, d13);
+    const double c1 = a4 < a3 ? a4 : a3, c2 = a3 < a4 ? a4 : a3;
+    write_split(t, i, v0, v1, v2, v3, b1 < c1 || (b1 == c1 && b2 <= c2));
   }
 }
 
@@ -578,20 +549,35 @@ struct HeBufs {
   unsigned* ovf = nullptr;
 };
 
-}  // namespace
+// colorFaces (:714-844) on a mesh whose halfedges are built: the inherited colours in `col` become
+// the reduced ones, class by class (colours 5..23 to the lowest of 0..4 free among the neighbours,
+// then colour 4 to the lowest of 0..3).  Returns the number of kernels launched.
+int color_faces(const HeView& he, uint8_t* col, int64_t nq, Pool& pool, int sms, cudaStream_t st) {
+  int32_t* cnt = pool.get<int32_t>(24);
+  int32_t* off = pool.get<int32_t>(24);
+  int32_t* cursor = pool.get<int32_t>(24);
+  int32_t* list = pool.get<int32_t>(std::max<int64_t>(nq, 1));
+  if (pool.err) return 0;
+  cudaMemsetAsync(cnt, 0, 24 * sizeof(int32_t), st);
+  const unsigned gc = (unsigned)std::max<int64_t>(1, ceil_div(nq, kColorTile));
+  color_count_kernel<<<gc, kColorThreads, 0, st>>>(col, nq, cnt);
+  color_offsets_kernel<<<1, 32, 0, st>>>(cnt, off, cursor);
+  color_scatter_kernel<<<gc, kColorThreads, 0, st>>>(col, nq, cursor, list);
+  const unsigned gq = grid_for(std::max<int64_t>(nq, 1), sms);
+  for (int k = 0; k < 19; k++) color_reduce_kernel<<<gq, 256, 0, st>>>(he, col, list, off, k, 4);
+  color_reduce_kernel<<<gq, 256, 0, st>>>(he, col, list, off, 19, 3);
+  return 23;
+}
 
-DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaStream_t st, DmcPostOut* out,
-                              unsigned long long* h_cnt, Prof* prof, bool borrowed, const ReadyFn* ready) {
-  DmcPostStatus s;
-  out->mesh = in;
-  const bool c3x3y = flags & TMC_DMC_P3X3Y_COLOR, i3x3y = flags & TMC_DMC_P3X3Y_ISOLATED,
-             p3333 = flags & TMC_DMC_P3333, want_t = flags & TMC_OUT_TRIANGLES, want_he = flags & TMC_OUT_HALFEDGES;
-  if (!(c3x3y || i3x3y || p3333 || want_t || want_he)) return s;
-  Pool pool{st};
-  const int64_t NV = std::max<int64_t>(in.nv, 1), NQ = std::max<int64_t>(in.nq, 1);
+// vertexValence (:847-871): the out-degrees of the halfedge build plus the boundary corrections
+int vertex_valence(const HeView& he, const int32_t* deg, int64_t nv, int64_t nq, int32_t* val, int sms,
+                   cudaStream_t st) {
+  cudaMemcpyAsync(val, deg, nv * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+  valence_boundary_kernel<<<grid_for(std::max<int64_t>(4 * nq, 1), sms), 256, 0, st>>>(he, 4 * nq, val);
+  return 1;
+}
 
-  // working mesh (double buffered)
-  DmcMesh cur = in;
+HeBufs halfedge_buffers(Pool& pool, int64_t NV, int64_t NQ) {
   HeBufs hw;
   hw.twin = pool.get<int32_t>(4 * NQ);
   hw.flag = pool.get<uint8_t>(4 * NQ);
@@ -606,6 +592,45 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   hw.nm = pool.get<unsigned long long>(2);
   hw.w.non_manifold = hw.nm;
   hw.ovf = pool.get<unsigned>(2);
+  return hw;
+}
+
+}  // namespace
+
+DmcPostStatus dmc_color_valence(const int32_t* quads, int64_t nq, int64_t nv, uint8_t* colors, int32_t* valence,
+                                int sms, cudaStream_t st) {
+  DmcPostStatus s;
+  if (nq == 0) {
+    if (nv > 0) s.err = cudaMemsetAsync(valence, 0, nv * sizeof(int32_t), st);
+    return s;
+  }
+  Pool pool{st};
+  HeBufs hw = halfedge_buffers(pool, std::max<int64_t>(nv, 1), nq);
+  if ((s.err = pool.err) != cudaSuccess) return s;
+  cudaMemsetAsync(hw.nm, 0, 2 * sizeof(unsigned long long), st);
+  HeOut ho{hw.twin, hw.flag, hw.hv};
+  s.launches += build_halfedges(quads, 4, nq, nv, ho, hw.w, sms, st, false);
+  const HeView he{quads, hw.twin, hw.flag};
+  s.launches += color_faces(he, colors, nq, pool, sms, st);
+  if ((s.err = pool.err) != cudaSuccess) return s;
+  s.launches += vertex_valence(he, hw.w.deg, nv, nq, valence, sms, st);
+  s.err = cudaGetLastError();
+  return s;
+}
+
+DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaStream_t st, DmcPostOut* out,
+                              unsigned long long* h_cnt, Prof* prof, bool borrowed, const ReadyFn* ready) {
+  DmcPostStatus s;
+  out->mesh = in;
+  const bool c3x3y = flags & TMC_DMC_P3X3Y_COLOR, i3x3y = flags & TMC_DMC_P3X3Y_ISOLATED,
+             p3333 = flags & TMC_DMC_P3333, want_t = flags & TMC_OUT_TRIANGLES, want_he = flags & TMC_OUT_HALFEDGES;
+  if (!(c3x3y || i3x3y || p3333 || want_t || want_he)) return s;
+  Pool pool{st};
+  const int64_t NV = std::max<int64_t>(in.nv, 1), NQ = std::max<int64_t>(in.nq, 1);
+
+  // working mesh (double buffered)
+  DmcMesh cur = in;
+  HeBufs hw = halfedge_buffers(pool, NV, NQ);
   unsigned long long* tiles = pool.get<unsigned long long>(scan_tiles(4 * NQ) + 2);
   if (hw.ovf) cudaMemsetAsync(hw.ovf, 0, 2 * sizeof(unsigned), st);
   unsigned long long* total = pool.get<unsigned long long>(2);
@@ -698,24 +723,11 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     halfedges(cur, false);
     if (pass == 0) {
       Stage tm(prof, "dmc_color", st);
-      int32_t* cnt = pool.get<int32_t>(24);
-      int32_t* off = pool.get<int32_t>(24);
-      int32_t* cursor = pool.get<int32_t>(24);
-      int32_t* list = pool.get<int32_t>(NQ);
+      s.launches += color_faces(HeView{cur.quads, hw.twin, hw.flag}, cur.colors, cur.nq, pool, sms, st);
       if (pool.err) break;
-      cudaMemsetAsync(cnt, 0, 24 * sizeof(int32_t), st);
-      const unsigned gc = (unsigned)std::max<int64_t>(1, ceil_div(cur.nq, kColorTile));
-      color_count_kernel<<<gc, kColorThreads, 0, st>>>(cur.colors, cur.nq, cnt);
-      color_offsets_kernel<<<1, 32, 0, st>>>(cnt, off, cursor);
-      color_scatter_kernel<<<gc, kColorThreads, 0, st>>>(cur.colors, cur.nq, cursor, list);
-      s.launches += 3;
-      for (int k = 0; k < 19; k++) color_reduce_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.colors, list, off, k, 4);
-      color_reduce_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.colors, list, off, 19, 3);
-      s.launches += 20;
     }
     Stage tm(prof, "dmc_p3x3y", st);
-    cudaMemcpyAsync(val, hw.w.deg, cur.nv * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
-    valence_boundary_kernel<<<grid_for(4 * cur.nq, sms), 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, 4 * cur.nq, val);
+    s.launches += vertex_valence(HeView{cur.quads, hw.twin, hw.flag}, hw.w.deg, cur.nv, cur.nq, val, sms, st);
     mark3x3y_kernel<<<gq, 256, 0, st>>>(cur.quads, cur.nq, val, p);
     fill_i32_kernel<<<gv, 256, 0, st>>>(own_pos, cur.nv, -1);
     fill_i32_kernel<<<gv, 256, 0, st>>>(own_rm, cur.nv, -1);

@@ -50,4 +50,10 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
                               unsigned long long* h_staging, Prof* prof = nullptr, bool borrowed = false,
                               const ReadyFn* ready = nullptr);
 
+// The face colouring and vertex valence stage alone (colorFaces + vertexValence,
+// cpp_dmc/DualMarchingCubes.cpp:714-871): colors holds the inherited colours on entry and the reduced
+// ones on return; valence receives one count per vertex.  Device arrays, stream-ordered on `st`.
+DmcPostStatus dmc_color_valence(const int32_t* quads, int64_t nq, int64_t nv, uint8_t* colors, int32_t* valence,
+                                int sms, cudaStream_t st);
+
 }  // namespace tmc

@@ -666,6 +666,23 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   return finish_mesh(ctx, flags, out, mp, &early);
 }
 
+// colorFaces + vertexValence as a stage of their own (cpp_dmc/DualMarchingCubes.cpp:714-871): the
+// P3X3Y colour pass of tmc_dmc_extract runs the same code on its front-end mesh.
+tmc_status tmc_dmc_color_valence(tmc_ctx* ctx, int64_t nr_v, int64_t nr_q, const int32_t* quads, uint8_t* colors,
+                                 int32_t* valence) {
+  if (!ctx) return TMC_ERR_INVALID_ARG;
+  if (nr_v < 0 || nr_q < 0 || nr_v > INT32_MAX || 4 * nr_q > INT32_MAX)
+    return fail(ctx, TMC_ERR_INVALID_ARG, "vertex or quad count out of range");
+  if ((nr_q > 0 && (!quads || !colors)) || (nr_v > 0 && !valence))
+    return fail(ctx, TMC_ERR_INVALID_ARG, "quads, colors or valence is NULL");
+  TMC_CUDA(ctx, cudaSetDevice(ctx->device));
+  const tmc::DmcPostStatus ps = tmc::dmc_color_valence(quads, nr_q, nr_v, colors, valence, ctx->sms, ctx->stream);
+  ctx->launches += ps.launches;
+  TMC_CUDA(ctx, ps.err);
+  TMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return TMC_OK;
+}
+
 }  // extern "C"
 
 namespace {

@@ -44,7 +44,7 @@ EXPORTS = ["tmc_ctx_create", "tmc_ctx_destroy", "tmc_last_error", "tmc_ctx_strea
            "tmc_server_submit", "tmc_server_poll", "tmc_server_wait", "tmc_server_release", "tmc_server_last_error",
            "tmc_server_stats", "tmc_ctx_set_tuning", "tmc_ctx_get_tuning", "tmc_ctx_autotune",
            "tmc_volume_file_info", "tmc_field_load", "tmc_field_free", "tmc_mesh_write_obj", "tmc_mesh_write_off",
-           "tmc_mesh_quality", "tmc_mesh_valence", "tmc_mesh_check", "tmc_field_generate"]
+           "tmc_mesh_quality", "tmc_mesh_valence", "tmc_mesh_check", "tmc_field_generate", "tmc_dmc_color_valence"]
 
 SURFACES = ("sphere", "torus", "two_holed_torus", "four_holed_torus", "genus_two", "iwp", "pw_hybrid", "neovius",
             "goursat", "steiner_roman")
@@ -135,6 +135,9 @@ def load(path: str = LIB_PATH):
     lib.tmc_dmc_count_static.argtypes = [ctypes.c_void_p, ctypes.POINTER(Volume), ctypes.c_double,
                                          ctypes.POINTER(ctypes.c_int64)]
     lib.tmc_dmc_count_static.restype = ctypes.c_int
+    lib.tmc_dmc_color_valence.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p]
+    lib.tmc_dmc_color_valence.restype = ctypes.c_int
     lib.tmc_server_create.argtypes = [ctypes.c_int, ctypes.POINTER(ServerOpts), ctypes.POINTER(ctypes.c_void_p)]
     lib.tmc_server_destroy.argtypes = [ctypes.c_void_p]
     lib.tmc_server_submit.argtypes = [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_int64)]
@@ -244,6 +247,7 @@ class Context:
 
     def __init__(self, device: int = 0, reserve_bytes: int = 0, check_numeric: bool = False, priority: int = 0):
         self.lib = load()
+        self.device = device
         self.h = ctypes.c_void_p()
         opts = CtxOpts(reserve_bytes, 1 if check_numeric else 0, priority)
         st = self.lib.tmc_ctx_create(device, ctypes.byref(opts), ctypes.byref(self.h))
@@ -312,6 +316,19 @@ class Context:
         counts = (ctypes.c_int64 * 4)()
         self._check(self.lib.tmc_dmc_count_static(self.h, ctypes.byref(volume), float(iso), counts))
         return tuple(counts)
+
+    def dmc_color_valence(self, nr_v: int, quads, inherited):
+        """tmc_dmc_color_valence on host arrays (copied to the device and back): the reduced face
+        colours and the vertex valences of a quad mesh with its inherited colours."""
+        import numpy as np
+        import torch
+        q = torch.from_numpy(np.ascontiguousarray(quads, dtype=np.int32)).cuda(self.device)
+        col = torch.from_numpy(np.ascontiguousarray(inherited).astype(np.uint8)).cuda(self.device)
+        val = torch.zeros(max(int(nr_v), 1), dtype=torch.int32, device=f"cuda:{self.device}")
+        torch.cuda.synchronize(self.device)
+        self._check(self.lib.tmc_dmc_color_valence(self.h, int(nr_v), q.numel() // 4, q.data_ptr(), col.data_ptr(),
+                                                   val.data_ptr()))
+        return col.cpu().numpy().astype(np.int32), val[:int(nr_v)].cpu().numpy()
 
     def batch_raw(self, volumes: list, isos: list, algos: list, flags: list) -> list:
         """tmc_batch_extract over prepared tmc_volume structs; returns the meshes (caller frees)."""

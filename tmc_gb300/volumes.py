@@ -60,15 +60,18 @@ def gaussian_blobs(nx: int, ny: int, nz: int, rng: np.random.Generator, nblobs: 
     return out.astype(np.float32)
 
 
-def periodic(nx: int, ny: int, nz: int, k: float, zslab: int = 64) -> np.ndarray:
-    """sin(kx)cos(ky) + sin(ky)cos(kz) + sin(kz)cos(kx), evaluated slab by slab."""
+def periodic(nx: int, ny: int, nz: int, k: float, zslab: int = 64, planes: tuple | None = None) -> np.ndarray:
+    """sin(kx)cos(ky) + sin(ky)cos(kz) + sin(kz)cos(kx), evaluated slab by slab.  `planes` = (z0, z1)
+    returns only those z-planes of the nz-plane grid (the same values, element for element)."""
     x, y, z = _axis(nx), _axis(ny), _axis(nz)
+    p0, p1 = planes if planes is not None else (0, nz)
+    z = z[p0:p1]
     sx, cx = np.sin(k * x), np.cos(k * x)
     sy, cy = np.sin(k * y), np.cos(k * y)
     sz, cz = np.sin(k * z), np.cos(k * z)
-    out = np.empty((nz, ny, nx), dtype=np.float32)
-    for z0 in range(0, nz, zslab):
-        z1 = min(nz, z0 + zslab)
+    out = np.empty((p1 - p0, ny, nx), dtype=np.float32)
+    for z0 in range(0, p1 - p0, zslab):
+        z1 = min(p1 - p0, z0 + zslab)
         a = sx[None, None, :] * cy[None, :, None]
         b = sy[None, :, None] * cz[z0:z1, None, None]
         c = sz[z0:z1, None, None] * cx[None, None, :]
@@ -98,20 +101,26 @@ def upsampled_noise(n: int, rng: np.random.Generator, coarse: int = 33, noise: f
 
 
 def seed_saddles(data: np.ndarray, rng: np.random.Generator, frac: float = 0.2, iso: float = 0.0,
-                 zslab: int = 64) -> int:
+                 zslab: int = 64, first_plane: int = 0, total_planes: int | None = None) -> int:
     """Overwrite the four corners of a random subset of a disjoint family of cell faces with a
     bilinear saddle whose asymptotic-decider value (f0 f3 - f1 f2)/(f0 + f3 - f1 - f2) lies within
     1e-6 of `iso` (in practice within a few 1e-8).
 
     The family is every xy-face whose lower corner has even i and even j: no two of them share a
     grid point, so every overwrite is independent.  Each face of the family is taken with
-    probability `frac`.  Returns the number of faces written."""
+    probability `frac`.  Returns the number of faces written.
+
+    `data` may hold only the planes first_plane .. first_plane + data.shape[0] of a grid of
+    `total_planes` planes: the random draws of the whole grid are replayed and the faces in those
+    planes written, so the slab equals the same planes of the whole seeded grid."""
     nz, ny, nx = data.shape
+    if total_planes is None:
+        total_planes = first_plane + nz
     fi = np.arange(0, nx - 1, 2)
     fj = np.arange(0, ny - 1, 2)
     total = 0
-    for z0 in range(0, nz, zslab):
-        z1 = min(nz, z0 + zslab)
+    for z0 in range(0, total_planes, zslab):
+        z1 = min(total_planes, z0 + zslab)
         m = rng.random(size=(z1 - z0, fj.size, fi.size)) < frac
         kk, jj, ii = np.nonzero(m)
         if kk.size == 0:
@@ -123,7 +132,10 @@ def seed_saddles(data: np.ndarray, rng: np.random.Generator, frac: float = 0.2, 
         d32 = (a32.astype(np.float64) * b32 / c32).astype(np.float32)
         flip = rng.random(size=kk.size) < 0.5
         s = np.where(flip, -1.0, 1.0).astype(np.float32)
-        k = kk + z0
+        k = kk + z0 - first_plane
+        inside = (k >= 0) & (k < nz)
+        if not inside.all():
+            k, jj, ii, a32, b32, c32, d32, s = (x[inside] for x in (k, jj, ii, a32, b32, c32, d32, s))
         j = fj[jj]
         i = fi[ii]
         # diagonal sign pattern: corners 0 and 3 on one side, 1 and 2 on the other
@@ -131,7 +143,7 @@ def seed_saddles(data: np.ndarray, rng: np.random.Generator, frac: float = 0.2, 
         data[k, j + 1, i + 1] = iso + s * b32
         data[k, j, i + 1] = iso - s * c32
         data[k, j + 1, i] = iso - s * d32
-        total += kk.size
+        total += k.size
     return total
 
 
@@ -182,6 +194,24 @@ def saddle_volume(n: int = 1024, seed: int = 3, frac: float = 0.2) -> Volume:
     faces = seed_saddles(d, rng, frac=frac)
     return Volume(d, spacing=_spacing(n, n, n), iso=0.0, kind="saddle",
                   meta={"seed": seed, "saddle_faces": faces})
+
+
+def saddle_slab(n: int = 1024, z0: int = 0, planes: int = 16, seed: int = 3, frac: float = 0.2) -> Volume:
+    """The z-planes z0 .. z0 + planes of saddle_volume(n, seed, frac), bit for bit, without building
+    the whole grid: a volume of its own whose origin is the first plane's position."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    d = periodic(n, n, n, 6 * math.pi, planes=(z0, z0 + planes))
+    faces = seed_saddles(d, rng, frac=frac, first_plane=z0, total_planes=n)
+    sp = _spacing(n, n, n)
+    return Volume(d, origin=(-1.0, -1.0, -1.0 + z0 * sp[2]), spacing=sp, iso=0.0, kind="saddle",
+                  meta={"seed": seed, "saddle_faces": faces, "z0": z0, "n": n})
+
+
+def z_slab(vol: Volume, z0: int, planes: int) -> Volume:
+    """Planes z0 .. z0 + planes of a volume, as a volume of its own (origin moved to the first plane)."""
+    d = np.ascontiguousarray(vol.data[z0:z0 + planes])
+    return Volume(d, origin=(vol.origin[0], vol.origin[1], vol.origin[2] + z0 * vol.spacing[2]),
+                  spacing=vol.spacing, iso=vol.iso, kind=vol.kind, meta=dict(vol.meta, z0=z0))
 
 
 def serve_request(rng: np.random.Generator, median: int = 128, sigma: float = 0.5,
