@@ -1,6 +1,7 @@
 """The float arc cosine the GPU triangle split uses (tmc_gb300/csrc/libm_acosf.h) against the
-platform C library's acosf, which the reference's minAngle calls through std::acos: bit-equal on
-every float of [-1, 1] (tests/cpp/acos_check.cpp, built as host code with contraction off)."""
+platform C library's acosf, which the reference's minAngle calls through std::acos: one of the two
+restated fdlibm kinds (separate roundings on x86-64, fused multiply-adds on aarch64) is bit-equal to
+it on every float of [-1, 1] (tests/cpp/acos_check.cpp, built as host code with contraction off)."""
 import os
 import shutil
 import subprocess
@@ -24,4 +25,5 @@ def run_acos_check(tmp_path, stride=1):
 
 def test_acosf_restatement_equals_host_library(tmp_path):
     out = run_acos_check(tmp_path)
-    assert out.returncode == 0 and out.stdout.startswith("ok 2130706434"), out.stdout + out.stderr
+    assert out.returncode == 0 and out.stdout.startswith("ok ") and out.stdout.split()[2] == "2130706434", \
+        out.stdout + out.stderr

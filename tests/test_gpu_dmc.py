@@ -177,7 +177,21 @@ def test_dmc_saddle_crops_float64_mean_point(ctx):
 
 def test_host_acosf_is_the_restated_one(tmp_path):
     """The split parity above rests on the GPU's float acos being this host C library's acosf
-    (what the reference's std::acos calls here): bit-equal on every float of [-1, 1]."""
-    from test_acos_cpu import run_acos_check
+    (what the reference's std::acos calls here).  On the host: one restated kind is bit-equal to it
+    on every float of [-1, 1].  On the GPU: the kind the library selects at run time, evaluated by the
+    device for every float of [-1, 1], is bit-equal to it (tests/cpp/acos_device_check.cu, built with
+    the library's floating-point flags)."""
+    import os
+    import shutil
+    import subprocess
+    from test_acos_cpu import ROOT, run_acos_check
     out = run_acos_check(tmp_path)
-    assert out.returncode == 0 and out.stdout.startswith("ok 2130706434"), out.stdout + out.stderr
+    assert out.returncode == 0 and out.stdout.startswith("ok "), out.stdout + out.stderr
+    host_kind = out.stdout.split()[1]
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    exe = tmp_path / "acos_device_check"
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-fmad=false", "-Xcompiler",
+                    "-ffp-contract=off", "-o", str(exe), os.path.join(ROOT, "tests", "cpp", "acos_device_check.cu")],
+                   check=True, capture_output=True)
+    dev = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
+    assert dev.returncode == 0 and dev.stdout.startswith("ok " + host_kind + " 2130706434"), dev.stdout + dev.stderr

@@ -1,9 +1,9 @@
 """Build the CUDA library in-tree: tmc_gb300/libtmc_gb300.so (sm_103a only).
 
 Each translation unit compiles in parallel with `nvcc -c`, then one link step.  The library is
-compiled with -fmad=false: the kernels restate the reference's CPU arithmetic operation by
-operation, and fused multiply-adds would round differently; hot loops that want FMAs use explicit
-intrinsics.
+compiled with -fmad=false (device code) and -ffp-contract=off (host code): the kernels restate the
+reference's CPU arithmetic operation by operation, and fused multiply-adds would round differently;
+hot loops that want FMAs use explicit intrinsics.
 """
 import concurrent.futures as cf
 import os
@@ -17,8 +17,8 @@ OUT = os.path.join(HERE, "libtmc_gb300.so")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["runtime.cu", "dmc_front.cu", "dmc_mesh.cu", "tmc_cells.cu", "halfedges.cu", "scan.cu", "count_static.cu", "server.cu", "volume_io.cu", "mesh_stats.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-         "-diag-suppress", "177"]
+FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+         "--expt-relaxed-constexpr", "-diag-suppress", "177"]
 
 
 def nvcc():

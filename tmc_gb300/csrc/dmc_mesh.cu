@@ -393,12 +393,12 @@ __global__ void fill_i32_kernel(int32_t* p, int64_t n, int32_t v) {
 // ---------------------------------------------------------------------------------------------
 // quad -> triangles (collectTriangles, :1387-1460; minAngle, DualMarchingCubes.h:746-756)
 // ---------------------------------------------------------------------------------------------
-// minAngle exactly as the reference: three float arc cosines of the host C library (restated in
-// libm_acosf.h, bit for bit), float minimum in the reference's std::min order
-__device__ __forceinline__ float min_angle_full(float a, float b, float c) {
-  const float A = libm::acosf((b * b + c * c - a * a) / (2 * b * c));
-  const float B = libm::acosf((a * a + c * c - b * b) / (2 * a * c));
-  const float C = libm::acosf((b * b + a * a - c * c) / (2 * b * a));
+// minAngle exactly as the reference: three float arc cosines of the host C library (the restated
+// kind of libm_acosf.h that the host's acosf is, bit for bit), float minimum in std::min's order
+__device__ __forceinline__ float min_angle_full(float a, float b, float c, int acos_kind) {
+  const float A = libm::acosf_kind((b * b + c * c - a * a) / (2 * b * c), acos_kind);
+  const float B = libm::acosf_kind((a * a + c * c - b * b) / (2 * a * c), acos_kind);
+  const float C = libm::acosf_kind((b * b + a * a - c * c) / (2 * b * a), acos_kind);
   const float mAB = (B < A) ? B : A;
   return (C < mAB) ? C : mAB;
 }
@@ -494,9 +494,9 @@ __global__ void triangles_fast_kernel(const int32_t* q, int64_t nq, const float*
 
 // collectTriangles (:1387-1460), exact pass over the listed quads: the reference's arithmetic
 // step by step.  Six side lengths (float of a float64 distance), minAngle of the four triangles with
-// the host library's float acos (libm_acosf.h), float64 comparisons of the two splits.
+// the host library's float acos (libm_acosf.h, acos_kind), float64 comparisons of the two splits.
 __global__ void triangles_kernel(const int32_t* q, const uint32_t* list, const unsigned* count, const double* v64,
-                                 int32_t* t) {
+                                 int32_t* t, int acos_kind) {
   const int64_t nl = *count;
   FOR_EACH(a, nl) {
     const int64_t i = list[a];
@@ -507,9 +507,9 @@ __global__ void triangles_kernel(const int32_t* q, const uint32_t* list, const u
                 d13 = side(P1, P3);
     // triangles (v0,v1,v2), (v0,v2,v3) | (v1,v3,v0), (v1,v2,v3); minAngle(a, b, c) takes the sides
     // |p0p1|, |p1p2|, |p2p0| of its triangle (p0, p1, p2)
-    const double a1 = min_angle_full(d01, d12, d20), a2 = min_angle_full(d20, d23, d30);
+    const double a1 = min_angle_full(d01, d12, d20, acos_kind), a2 = min_angle_full(d20, d23, d30, acos_kind);
     const double b1 = a2 < a1 ? a2 : a1, b2 = a1 < a2 ? a2 : a1;
-    const double a3 = min_angle_full(d13, d30, d01), a4 = min_angle_full(d12, d23, d13);
+    const double a3 = min_angle_full(d13, d30, d01, acos_kind), a4 = min_angle_full(d12, d23, d13, acos_kind);
     const double c1 = a4 < a3 ? a4 : a3, c2 = a3 < a4 ? a4 : a3;
     write_split(t, i, v0, v1, v2, v3, b1 < c1 || (b1 == c1 && b2 <= c2));
   }
@@ -877,7 +877,8 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
         cudaMemsetAsync(tcount, 0, sizeof(unsigned), st);
         triangles_fast_kernel<<<grid_for(cur.nq, sms), 256, 0, st>>>(cur.quads, cur.nq, cur.v, (int32_t*)tr, tlist,
                                                                       tcount);
-        triangles_kernel<<<grid_for(cur.nq, sms), 256, 0, st>>>(cur.quads, tlist, tcount, cur.v64, (int32_t*)tr);
+        triangles_kernel<<<grid_for(cur.nq, sms), 256, 0, st>>>(cur.quads, tlist, tcount, cur.v64, (int32_t*)tr,
+                                                                libm::host_acosf_kind());
         s.launches += 2;
         if (ready) (*ready)(tr, (size_t)cur.nq * 6 * sizeof(int32_t));
       }
