@@ -91,6 +91,32 @@ struct CellSpace {
   }
 };
 
+// Listed cells.  The classification lists, per scan tile, the cells whose MC case is neither 0 nor
+// 255 (12 % of the cells of the 512^3 dense-ambiguity field, 3 % of a smooth one); every per-cell
+// array after it (records, in-tile cell offsets, vertex and face offsets) holds only those, in cell
+// order, at slot = tile * kScanTile + rank in the tile, so the passes read and write 4 to 16 bytes
+// per listed cell instead of per cell.  CellMask, one per 32 cells, says which cells are listed and
+// how many listed cells of the tile come before the word; a cell's slot is one 8-byte load and a
+// population count away.
+struct CellMask {
+  uint32_t bits;  // listed cells among the word's 32
+  uint32_t pre;   // listed cells of the tile before the word
+};
+constexpr int kTileShift = 11;  // kScanTile = 2048 cells per scan tile
+__device__ __forceinline__ uint32_t listed_slot(const CellMask* mask, uint32_t vc) {
+  const uint2 a = __ldg(reinterpret_cast<const uint2*>(mask) + (vc >> 5));
+  return ((vc >> kTileShift) << kTileShift) + a.y + __popc(a.x & ((1u << (vc & 31)) - 1u));
+}
+// number of listed cells of a tile
+__device__ __forceinline__ uint32_t tile_listed(const CellMask* mask, int64_t tile) {
+  const uint2 a = __ldg(reinterpret_cast<const uint2*>(mask) + (tile << (kTileShift - 5)) + 63);
+  return a.y + __popc(a.x);
+}
+// the cell behind a slot (cell: in-tile cell offsets of the listed cells)
+__device__ __forceinline__ uint32_t slot_cell(const uint16_t* cell, uint32_t slot) {
+  return ((slot >> kTileShift) << kTileShift) + __ldg(cell + slot);
+}
+
 inline CellSpace single_space(const Grid& g) {
   CellSpace cs;
   cs.one = g;

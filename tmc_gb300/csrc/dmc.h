@@ -22,10 +22,10 @@ struct ProjRecord;
 }
 
 struct DmcScratch {
-  uint32_t* rec;                  // per cell
-  int32_t* voff;                  // per cell
-  int32_t* qoff;                  // per cell
-  uint32_t* vwork;                // per vertex: generating cell
+  uint32_t* rec;                  // per listed cell (slot)
+  int32_t* voff;                  // per listed cell (slot)
+  int32_t* qoff;                  // per listed cell (slot)
+  uint32_t* vwork;                // per vertex: slot of the generating cell
   unsigned long long* tile_sums;  // per scan tile
   unsigned long long* totals;     // [0] = (vertices << 32) | quads
   unsigned long long* stats;      // 8 counters
@@ -35,6 +35,10 @@ struct DmcScratch {
   uint32_t* fb_list;
   unsigned* fb_count;             // [0] fb_list entries, [1] tail_list entries
   uint32_t* tail_list;            // vertices without a valid 7x7 sample (26x26 retry)
+  // listed cells (common.cuh): rec, voff and qoff hold one entry per listed cell at its slot
+  CellMask* mask;                 // per 32 cells of the space
+  uint16_t* cellof;               // per slot: in-tile offset of the listed cell
+  uint8_t* vrank;                 // per vertex: rank among its cell's vertices (vwork: the cell's slot)
 };
 constexpr size_t kProjRecordBytes = 144;  // sizeof(repr::ProjRecord)
 

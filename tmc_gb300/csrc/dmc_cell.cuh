@@ -3,6 +3,7 @@
 // static-scratch counting kernel.
 #pragma once
 #include "common.cuh"
+#include "listing.cuh"
 
 namespace tmc {
 

@@ -40,19 +40,20 @@ __constant__ uint64_t c_case_contour[256] = TMC_CASE_CONTOUR_INIT;
 // ------------------------------------------------------------------------------------------
 // classification (per-cell helpers in dmc_cell.cuh)
 // ------------------------------------------------------------------------------------------
-// One block handles kScanTile consecutive cells (linear order), writes their records and the
-// tile's packed (vertices << 32 | quads) sum.  Pass 1 computes every cell's MC case (cheap, the
-// eight corner loads coalesced across the block) and compacts the active cells (12 % on the 512^3
-// workload) into shared memory with warp scans; pass 2 builds their contours densely, so that the
-// polygon and edge work does not keep mostly-inactive warps busy.
-__global__ void __launch_bounds__(kScanThreads, 4) dmc_classify_kernel(CellSpace space, int64_t tile0, uint32_t* rec,
+// One block per kScanTile consecutive cells (linear order).  Pass 1: every cell's MC case from the
+// warp-ballot corner rows (warp_cases: one coalesced load per corner row and warp, no per-cell
+// gather); the cells with a case other than 0 and 255 are listed in cell order (list_tile).  Pass 2:
+// contours and records of the listed cells only, written densely at their slots with their in-tile
+// offsets, and the tile's packed (vertices << 32 | quads) sum.
+__global__ void __launch_bounds__(kScanThreads, 3) dmc_classify_kernel(CellSpace space, int64_t tile0, uint32_t* rec,
+                                                                   uint16_t* cellof, CellMask* mask,
                                                                    unsigned long long* tile_sums,
                                                                    unsigned long long* stats) {
   const int64_t tile = tile0 + blockIdx.x;
   __shared__ uint64_t cc[256];
   __shared__ uint16_t act_list[kScanTile];
   __shared__ uint8_t case_of[kScanTile];
-  __shared__ int wcount[kScanThreads / 32];
+  __shared__ uint32_t wmask[kScanTile / 32], wpre[kScanTile / 32];
   __shared__ int total;
   __shared__ unsigned long long tile_sum;
   for (int c = threadIdx.x; c < 256; c += blockDim.x) cc[c] = c_case_contour[c];
@@ -60,54 +61,23 @@ __global__ void __launch_bounds__(kScanThreads, 4) dmc_classify_kernel(CellSpace
   const Grid g = space.grid_of_tile(tile);
   const int64_t n = g.ncells();
   const int64_t vbase = tile * kScanTile;  // first cell of the tile in the space
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  // pass 1: cases; inactive records are final here
-  bool act[kScanItems];
-  int mine = 0;
-#pragma unroll
+  const int lane = threadIdx.x & 31;
+  // pass 1: cases
+  unsigned actbits = 0;
+#pragma unroll 2
   for (int s = 0; s < kScanItems; s++) {
     const int off = s * kScanThreads + threadIdx.x;
     const int64_t vc = vbase + off;
     const int64_t c = vc - g.vbase;  // cell of the volume (beyond its last cell: padding)
-    unsigned cs = 0;
-    if (vc < space.n && c < n) {
-      int i, j, k;
-      cell_ijk(g, c, i, j, k);
-      float u[8];
-      load_corners(g, i, j, k, u);
-      cs = mc_case(u, g.iso_up);
-    }
-    act[s] = cs != 0 && cs != 255;
+    const bool valid = vc < space.n && c < n;
+    int i = 0, j = 0, k = 0;
+    if (valid) cell_ijk(g, c, i, j, k);
+    const unsigned cs = warp_cases(g, valid, i, j, k);
     case_of[off] = (uint8_t)cs;
-    if (!act[s] && vc < space.n) rec[vc] = 0;
-    mine += act[s];
+    actbits |= (unsigned)(cs != 0 && cs != 255) << s;
   }
-  // block compaction of the active cells
-  int pre = mine;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, pre, o);
-    if (lane >= o) pre += y;
-  }
-  if (lane == 31) wcount[wid] = pre;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int s = 0;
-    for (int w = 0; w < kScanThreads / 32; w++) {
-      const int x = wcount[w];
-      wcount[w] = s;
-      s += x;
-    }
-    total = s;
-  }
-  __syncthreads();
-  int pos = wcount[wid] + pre - mine;
-#pragma unroll
-  for (int s = 0; s < kScanItems; s++)
-    if (act[s]) act_list[pos++] = (uint16_t)(s * kScanThreads + threadIdx.x);
-  __syncthreads();
-  // pass 2: records of the active cells
-  const int na = total;
+  const int na = list_tile(actbits, tile, mask, wmask, wpre, act_list, &total);
+  // pass 2: records of the listed cells
   unsigned long long local = 0, amb = 0, nact = 0;
   for (int a = threadIdx.x; a < na; a += blockDim.x) {
     const int off = act_list[a];
@@ -118,10 +88,11 @@ __global__ void __launch_bounds__(kScanThreads, 4) dmc_classify_kernel(CellSpace
     float u[8];
     if (case_ambiguous(cs)) load_corners(g, i, j, k, u);
     const uint32_t r = classify_active(g, i, j, k, cs, u, cc);
-    rec[vc] = r;
+    rec[vbase + a] = r;
+    cellof[vbase + a] = (uint16_t)off;
     local += ((unsigned long long)rec_nv(r) << 32) | (unsigned long long)rec_nq(r);
     amb += (r >> 29) & 1;
-    nact += r != 0;  // active: the cell emits a vertex or owns a quad
+    nact += r != 0;  // active: a record (a used contour, an owned quad or the ambiguous flag)
   }
   for (int o = 16; o; o >>= 1) {
     local += __shfl_down_sync(0xffffffffu, local, o);
@@ -135,15 +106,18 @@ __global__ void __launch_bounds__(kScanThreads, 4) dmc_classify_kernel(CellSpace
   if (threadIdx.x == 0) tile_sums[tile] = tile_sum;
 }
 
-// In-tile exclusive scan of the records -> per-cell vertex and quad offsets (blocked: 16-byte record
-// loads and offset stores, one block scan of the thread totals), and one work item per vertex: the
-// cell that generates it.
-__global__ void __launch_bounds__(kScanThreads) dmc_offsets_kernel(int64_t n, const uint32_t* rec,
+// In-tile exclusive scan of the listed cells' records -> their vertex and quad offsets (blocked:
+// 16-byte record loads and offset stores over the tile's slots, one block scan of the thread
+// totals), and two entries per vertex: the slot of the cell that generates it and its rank there.
+__global__ void __launch_bounds__(kScanThreads) dmc_offsets_kernel(const CellMask* mask, const uint32_t* rec,
                                                                   const unsigned long long* tile_off,
-                                                                  int32_t* voff, int32_t* qoff, uint32_t* vwork) {
-  const int64_t first = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+                                                                  int32_t* voff, int32_t* qoff, uint32_t* vwork,
+                                                                  uint8_t* vrank) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  const int64_t end = base + tile_listed(mask, blockIdx.x);
+  const int64_t first = base + (int64_t)threadIdx.x * kScanItems;
   uint32_t r[kScanItems];
-  load8(rec, first, n, r);
+  load8(rec, first, end, r);
   unsigned long long sum = 0;
 #pragma unroll
   for (int s = 0; s < kScanItems; s++) sum += ((unsigned long long)rec_nv(r[s]) << 32) | rec_nq(r[s]);
@@ -156,11 +130,14 @@ __global__ void __launch_bounds__(kScanThreads) dmc_offsets_kernel(int64_t n, co
     qo[s] = (int32_t)(pre & 0xffffffffull);
     pre += ((unsigned long long)rec_nv(r[s]) << 32) | rec_nq(r[s]);
   }
-  store8(voff, first, n, vo);
-  store8(qoff, first, n, qo);
+  store8(voff, first, end, vo);
+  store8(qoff, first, end, qo);
 #pragma unroll
   for (int s = 0; s < kScanItems; s++)
-    for (int q = 0; q < rec_nv(r[s]); q++) vwork[vo[s] + q] = (uint32_t)(first + s);  // empty beyond n
+    for (int q = 0; q < rec_nv(r[s]); q++) {  // empty beyond the listed cells
+      vwork[vo[s] + q] = (uint32_t)(first + s);
+      vrank[vo[s] + q] = (uint8_t)q;
+    }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -423,7 +400,7 @@ __device__ __forceinline__ void flush_stats(const repr::Stats& st, unsigned long
 // without a valid 7x7 sample go on to the tail list (the reference's 26x26 retry, one warp each).
 // A list of at most `warp_max` entries is left whole to the warp kernel: one thread's serial
 // projection (~0.1 ms) would set the latency of a small call.
-__global__ void __launch_bounds__(kVertexThreads) dmc_vertex_kernel(CellSpace space, const int32_t* voff,
+__global__ void __launch_bounds__(kVertexThreads) dmc_vertex_kernel(CellSpace space, const uint16_t* cellof, const uint8_t* vrank,
                                                                      const uint32_t* vwork, const uint32_t* list,
                                                                      const unsigned* count, uint32_t* tail_list,
                                                                      unsigned* tail_count, unsigned warp_max,
@@ -439,8 +416,8 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_kernel(CellSpace sp
   GridCache G;
   for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
     const int64_t vidx = (int64_t)list[a];
-    const uint32_t vcell = vwork[vidx];
-    const int rank = (int)(vidx - voff[vcell]);
+    const uint32_t vcell = slot_cell(cellof, vwork[vidx]);
+    const int rank = vrank[vidx];
     G.load(space, vcell);
     const Grid& g = G.g;
     const int64_t cell = vcell - g.vbase;
@@ -479,7 +456,7 @@ __device__ __forceinline__ repr::LaneBest warp_best(repr::LaneBest b) {
 // ~2 samples per lane for its 7x7 projection and ~22 for the reference's 26x26 retry, instead of up
 // to 725 on one thread.  Work: the whole one-pass list when it has at most `warp_max` entries
 // (the one-pass kernel then does nothing), otherwise the one-pass kernel's tail list.
-__global__ void __launch_bounds__(kVertexThreads) dmc_vertex_warp_kernel(CellSpace space, const int32_t* voff,
+__global__ void __launch_bounds__(kVertexThreads) dmc_vertex_warp_kernel(CellSpace space, const uint16_t* cellof, const uint8_t* vrank,
                                                                           const uint32_t* vwork, const uint32_t* list,
                                                                           const unsigned* count,
                                                                           const uint32_t* tail_list,
@@ -503,8 +480,8 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_warp_kernel(CellSpa
   int f64 = 0;
   for (int64_t a = (int64_t)blockIdx.x * kWarps + wib; a < n; a += (int64_t)gridDim.x * kWarps) {
     const int64_t vidx = (int64_t)L[a];
-    const uint32_t vcell = vwork[vidx];
-    const int rank = (int)(vidx - voff[vcell]);
+    const uint32_t vcell = slot_cell(cellof, vwork[vidx]);
+    const int rank = vrank[vidx];
     G.load(space, vcell);
     const Grid& g = G.g;
     const int64_t cell = vcell - g.vbase;
@@ -569,7 +546,7 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_warp_kernel(CellSpa
 // vertex.  Only the vertex's own contour is evaluated: its edge points are summed and boxed as they
 // are computed (no point array, nothing in local memory).  Contours with neighbour-contour
 // exclusion go to the one-pass kernel's list.
-__global__ void __launch_bounds__(kVertexThreads, 5) dmc_vertex_setup_kernel(CellSpace space, const int32_t* voff,
+__global__ void __launch_bounds__(kVertexThreads, 5) dmc_vertex_setup_kernel(CellSpace space, const uint16_t* cellof, const uint8_t* vrank,
                                                                               const uint32_t* vwork, int64_t nv,
                                                                               repr::ProjRecord* recs, uint32_t* list,
                                                                               unsigned* count,
@@ -581,8 +558,8 @@ __global__ void __launch_bounds__(kVertexThreads, 5) dmc_vertex_setup_kernel(Cel
   int f64 = 0;
   for (int64_t vidx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vidx < nv;
        vidx += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t vcell = vwork[vidx];
-    const int rank = (int)(vidx - voff[vcell]);
+    const uint32_t vcell = slot_cell(cellof, vwork[vidx]);
+    const int rank = vrank[vidx];
     G.load(space, vcell);
     const Grid& g = G.g;
     int i, j, k;
@@ -699,7 +676,8 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_project_group_kernel(const
 
 // Two-pass vertices, pass 3: positions, normals and local coordinates of the projected vertices.
 template <bool kFF>
-__global__ void __launch_bounds__(kVertexThreads, 4) dmc_vertex_finish_kernel(CellSpace space, const uint32_t* vwork,
+__global__ void __launch_bounds__(kVertexThreads, 4) dmc_vertex_finish_kernel(CellSpace space, const uint16_t* cellof,
+                                                                            const uint32_t* vwork,
                                                                             int64_t nv, const float4* vp,
                                                                             DmcVertexOut out, int flip_all,
                                                                             unsigned long long* stats) {
@@ -709,7 +687,7 @@ __global__ void __launch_bounds__(kVertexThreads, 4) dmc_vertex_finish_kernel(Ce
        vidx += (int64_t)gridDim.x * blockDim.x) {
     const float4 q = vp[vidx];
     if (q.w != 0.0f) continue;  // done by the one-pass kernel
-    const uint32_t vcell = vwork[vidx];
+    const uint32_t vcell = slot_cell(cellof, vwork[vidx]);
     G.load(space, vcell);
     const Grid& g = G.g;
     const int64_t cell = vcell - g.vbase;
@@ -729,10 +707,10 @@ __global__ void __launch_bounds__(kVertexThreads, 4) dmc_vertex_finish_kernel(Ce
 // Quad corners are vertex indices within the quad's own volume: the space-wide offsets minus the
 // volume's first vertex (the scanned tile offset of its first tile; 0 for a single volume).
 // The quads a cell owns (one per crossed interior edge 0, 3, 8), from the records of the four
-// cells around each edge.
-__device__ __forceinline__ void cell_quads(const Grid& g, int32_t vfirst, int64_t vc, const uint32_t* rec,
-                                           const int32_t* voff, const int32_t* qoff, int32_t* quads,
-                                           uint8_t* colors) {
+// cells around each edge (listed cells: a crossed edge makes every cell around it listed).
+__device__ __forceinline__ void cell_quads(const Grid& g, int32_t vfirst, uint32_t slot, int64_t vc,
+                                           const CellMask* mask, const uint32_t* rec, const int32_t* voff,
+                                           const int32_t* qoff, int32_t* quads, uint8_t* colors) {
   // cell offsets (di, dj, dk) and local edge of the four cells around the owned edges 0, 3, 8
   // x edge: (0,-1,-1) e6, (0,0,-1) e4, (0,-1,0) e2, (0,0,0) e0
   // y edge: (-1,0,-1) e5, (0,0,-1) e7, (-1,0,0) e1, (0,0,0) e3
@@ -745,7 +723,7 @@ __device__ __forceinline__ void cell_quads(const Grid& g, int32_t vfirst, int64_
   const float fx = g.at(i + 1, j, k), fy = g.at(i, j + 1, k), fz = g.at(i, j, k + 1);
   const bool s0 = f0 >= g.iso_up;
   const bool crossed[3] = {s0 != (fx >= g.iso_up), s0 != (fy >= g.iso_up), s0 != (fz >= g.iso_up)};
-  int32_t q = qoff[vc];
+  int32_t q = qoff[slot];
   const int par = (i & 1) | ((j & 1) << 1) | ((k & 1) << 2);
 #pragma unroll
   for (int a = 0; a < 3; a++) {
@@ -770,9 +748,9 @@ __device__ __forceinline__ void cell_quads(const Grid& g, int32_t vfirst, int64_
     int32_t qv[4];
 #pragma unroll
     for (int s = 0; s < 4; s++) {
-      const int64_t nc = g.vcell(i + di[s], j + dj[s], k + dk[s]);
-      const uint32_t rn = rec[nc];
-      qv[quad_slot(le[s], neg)] = voff[nc] - vfirst + rec_rank(rn, le[s]);
+      const uint32_t ns = s == 3 ? slot : listed_slot(mask, (uint32_t)g.vcell(i + di[s], j + dj[s], k + dk[s]));
+      const uint32_t rn = rec[ns];
+      qv[quad_slot(le[s], neg)] = voff[ns] - vfirst + rec_rank(rn, le[s]);
     }
     reinterpret_cast<int4*>(quads)[q] = make_int4(qv[0], qv[1], qv[2], qv[3]);
     if (colors) colors[q] = (uint8_t)(3 * par + a);
@@ -780,12 +758,13 @@ __device__ __forceinline__ void cell_quads(const Grid& g, int32_t vfirst, int64_
   }
 }
 
-// Each warp walks chunks of 32 consecutive cells, queues those that own quads (ballot) in shared
-// memory and processes the queue 32 cells at a time, one per lane: ~12 % of the cells own quads,
-// so a plain cell loop would leave most lanes idle.  No block barrier.
+// Each warp walks chunks of 32 consecutive slots of the listed cells, queues those that own quads
+// (ballot) in shared memory and processes the queue 32 cells at a time, one per lane.  No block
+// barrier.
 constexpr int kQuadThreads = 256;
 template <bool kBatch>
-__global__ void __launch_bounds__(kQuadThreads) dmc_quad_kernel(CellSpace space, const uint32_t* rec,
+__global__ void __launch_bounds__(kQuadThreads) dmc_quad_kernel(CellSpace space, const CellMask* mask,
+                                                                const uint16_t* cellof, const uint32_t* rec,
                                                                 const int32_t* voff, const int32_t* qoff,
                                                                 const unsigned long long* tile_off, int32_t* quads,
                                                                 uint8_t* colors) {
@@ -793,26 +772,28 @@ __global__ void __launch_bounds__(kQuadThreads) dmc_quad_kernel(CellSpace space,
   __shared__ uint32_t queue[kWarps][64];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   uint32_t* Q = queue[wid];
-  const int64_t n = space.n;
-  const int64_t chunks = ceil_div(n, 32);
+  const int64_t chunks = ceil_div(space.n, kScanTile) * (kScanTile / 32);
   int qn = 0;  // queued cells (the same on every lane)
   for (int64_t chunk = (int64_t)blockIdx.x * kWarps + wid;; chunk += (int64_t)gridDim.x * kWarps) {
     const bool more = chunk < chunks;
     if (more) {
-      const int64_t c = chunk * 32 + lane;
-      const bool own = c < n && rec_nq(rec[c]) != 0;  // padding records are empty
+      const int64_t tile = chunk >> (kTileShift - 5);
+      const uint32_t r = (uint32_t)(chunk & (kScanTile / 32 - 1)) * 32 + lane;
+      const uint32_t slot = (uint32_t)(tile << kTileShift) + r;
+      const bool own = r < tile_listed(mask, tile) && rec_nq(rec[slot]) != 0;
       const unsigned bal = __ballot_sync(0xffffffffu, own);
-      if (own) Q[qn + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)c;
+      if (own) Q[qn + __popc(bal & ((1u << lane) - 1u))] = slot;
       qn += __popc(bal);
       __syncwarp();
     }
     while (qn >= 32 || (!more && qn > 0)) {
       const int take = qn < 32 ? qn : 32;
       if (lane < take) {
-        const int64_t vc = Q[lane];
+        const uint32_t slot = Q[lane];
+        const uint32_t vc = slot_cell(cellof, slot);
         const Grid& g = kBatch ? space.grids[__ldg(space.tile_vol + vc / kScanTile)] : space.one;
         const int32_t vfirst = kBatch ? (int32_t)(tile_off[g.vbase / kScanTile] >> 32) : 0;
-        cell_quads(g, vfirst, vc, rec, voff, qoff, quads, colors);
+        cell_quads(g, vfirst, slot, vc, mask, rec, voff, qoff, quads, colors);
       }
       __syncwarp();
       const int rest = qn - take;  // at most 31: move them to the front
@@ -837,7 +818,8 @@ int dmc_front_count(const CellSpace& space, DmcScratch& s, cudaStream_t st, Prof
     Stage t(prof, "dmc_classify", st);
     auto classify = [&](int64_t t0, int64_t t1) {
       if (t1 <= t0) return;
-      dmc_classify_kernel<<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(space, t0, s.rec, s.tile_sums, s.stats);
+      dmc_classify_kernel<<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(space, t0, s.rec, s.cellof, s.mask,
+                                                                         s.tile_sums, s.stats);
       k++;
     };
     if (ngates == 0) classify(0, tiles);
@@ -863,8 +845,8 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
   {
     // per-cell offsets and the vertex work list (needs the vertex count for its size)
     Stage t(prof, "dmc_scan", st);
-    dmc_offsets_kernel<<<(unsigned)ceil_div(n, kScanTile), kScanThreads, 0, st>>>(n, s.rec, s.tile_sums, s.voff,
-                                                                                  s.qoff, s.vwork);
+    dmc_offsets_kernel<<<(unsigned)ceil_div(n, kScanTile), kScanThreads, 0, st>>>(s.mask, s.rec, s.tile_sums, s.voff,
+                                                                                  s.qoff, s.vwork, s.vrank);
   }
   // per-vertex grids: whole waves of each kernel's resident blocks
   static const int r_setup = resident_blocks(dmc_vertex_setup_kernel, kVertexThreads);
@@ -879,7 +861,7 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
   {
     Stage t(prof, "dmc_vertex_setup", st);
     cudaMemsetAsync(s.fb_count, 0, 2 * sizeof(unsigned), st);
-    dmc_vertex_setup_kernel<<<vgrid(r_setup), kVertexThreads, 0, st>>>(space, s.voff, s.vwork, nv, s.proj, s.fb_list,
+    dmc_vertex_setup_kernel<<<vgrid(r_setup), kVertexThreads, 0, st>>>(space, s.cellof, s.vrank, s.vwork, nv, s.proj, s.fb_list,
                                                                        s.fb_count, s.stats);
   }
   {
@@ -897,10 +879,10 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
     Stage t(prof, "dmc_vertex_finish", st);
     // the float-float normals only when some volume keeps float64 normals (simplification)
     if (vo.n64)
-      dmc_vertex_finish_kernel<true><<<vgrid(r_finish), kVertexThreads, 0, st>>>(space, s.vwork, nv, s.vp, vo, flip,
+      dmc_vertex_finish_kernel<true><<<vgrid(r_finish), kVertexThreads, 0, st>>>(space, s.cellof, s.vwork, nv, s.vp, vo, flip,
                                                                                  s.stats);
     else
-      dmc_vertex_finish_kernel<false><<<vgrid(r_finish32), kVertexThreads, 0, st>>>(space, s.vwork, nv, s.vp, vo, flip,
+      dmc_vertex_finish_kernel<false><<<vgrid(r_finish32), kVertexThreads, 0, st>>>(space, s.cellof, s.vwork, nv, s.vp, vo, flip,
                                                                                     s.stats);
   }
   {
@@ -910,19 +892,20 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
     const unsigned warp_max = (unsigned)std::min<int64_t>(tu.warp_list_max, 0x7fffffff);
     static const int r_vertex = resident_blocks(dmc_vertex_kernel, kVertexThreads);
     const unsigned fb = (unsigned)wave_grid(r_vertex, sms, 8, nv, kVertexThreads);
-    dmc_vertex_kernel<<<fb, kVertexThreads, 0, st>>>(space, s.voff, s.vwork, s.fb_list, s.fb_count, s.tail_list,
+    dmc_vertex_kernel<<<fb, kVertexThreads, 0, st>>>(space, s.cellof, s.vrank, s.vwork, s.fb_list, s.fb_count, s.tail_list,
                                                       s.fb_count + 1, warp_max, vo, flip, s.stats);
     dmc_vertex_warp_kernel<<<(unsigned)std::max(1, sms * 3), kVertexThreads, 0, st>>>(
-        space, s.voff, s.vwork, s.fb_list, s.fb_count, s.tail_list, s.fb_count + 1, warp_max, vo, flip, s.stats);
+        space, s.cellof, s.vrank, s.vwork, s.fb_list, s.fb_count, s.tail_list, s.fb_count + 1, warp_max, vo, flip,
+        s.stats);
   }
   Stage t(prof, "dmc_quad", st);
   // one wave: the kernel takes 32-cell chunks until none are left
   if (space.grids)
     dmc_quad_kernel<true><<<(unsigned)wave_grid(r_quad_batch, sms, 1, ceil_div(n, 32), kQuadThreads / 32), kQuadThreads,
-                            0, st>>>(space, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
+                            0, st>>>(space, s.mask, s.cellof, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
   else
     dmc_quad_kernel<false><<<(unsigned)wave_grid(r_quad, sms, 1, ceil_div(n, 32), kQuadThreads / 32), kQuadThreads, 0,
-                             st>>>(space, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
+                             st>>>(space, s.mask, s.cellof, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
   return 7;
 }
 

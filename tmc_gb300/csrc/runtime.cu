@@ -536,6 +536,8 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   TMC_CUDA(ctx, al.get(&sc.rec, ncell));
   TMC_CUDA(ctx, al.get(&sc.voff, ncell));
   TMC_CUDA(ctx, al.get(&sc.qoff, ncell));
+  TMC_CUDA(ctx, al.get(&sc.cellof, ncell));
+  TMC_CUDA(ctx, al.get(&sc.mask, tmc::dmc_tiles(space) * (tmc::kScanTile / 32)));
   TMC_CUDA(ctx, al.get(&sc.tile_sums, tmc::dmc_tiles(space)));
   TMC_CUDA(ctx, al.get(&sc.totals, 2));
   sc.stats = ctx->d_stats;
@@ -582,6 +584,7 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
     TMC_CUDA(ctx, ce);
   }
   ce = al.get(&sc.vwork, nv);
+  if (ce == cudaSuccess) ce = al.get(&sc.vrank, nv);
   if (ce == cudaSuccess) ce = dmc_vertex_scratch(al, sc, nv);
   if (ce != cudaSuccess) {
     delete mp;
@@ -710,7 +713,9 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   TMC_CUDA(ctx, al.get(&sc.rec, ncell));
   TMC_CUDA(ctx, al.get(&sc.voff, ncell));
   TMC_CUDA(ctx, al.get(&sc.toff, ncell));
+  TMC_CUDA(ctx, al.get(&sc.cellof, ncell));
   const tmc::CellSpace space = tmc::single_space(g);
+  TMC_CUDA(ctx, al.get(&sc.mask, tmc::tmc_tiles(space) * (tmc::kScanTile / 32)));
   TMC_CUDA(ctx, al.get(&sc.tile_sums, tmc::tmc_tiles(space)));
   TMC_CUDA(ctx, al.get(&sc.totals, 2));
   TMC_CUDA(ctx, al.get(&sc.amb_n, 1));
@@ -880,9 +885,13 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
   uint32_t* rec = nullptr;
   int32_t *voff = nullptr, *qoff = nullptr;
   unsigned long long *tile_sums = nullptr, *totals = nullptr;
+  tmc::CellMask* mask = nullptr;
+  uint16_t* cellof = nullptr;
   TMC_CUDA(ctx, al.get(&rec, ncell));
   TMC_CUDA(ctx, al.get(&voff, ncell));
   TMC_CUDA(ctx, al.get(&qoff, ncell));
+  TMC_CUDA(ctx, al.get(&cellof, ncell));
+  TMC_CUDA(ctx, al.get(&mask, tiles * (tmc::kScanTile / 32)));
   TMC_CUDA(ctx, al.get(&tile_sums, tiles));
   TMC_CUDA(ctx, al.get(&totals, 2));
   TMC_CUDA(ctx, cudaMemsetAsync(ctx->d_stats, 0, 8 * sizeof(unsigned long long), st));
@@ -890,9 +899,13 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
   tmc::TmcScratch tsc{};
   if (dmc) {
     dsc = tmc::DmcScratch{rec, voff, qoff, nullptr, tile_sums, totals, ctx->d_stats};
+    dsc.mask = mask;
+    dsc.cellof = cellof;
     ctx->launches += tmc::dmc_front_count(space, dsc, st, &ctx->prof);
   } else {
     tsc = tmc::TmcScratch{rec, voff, qoff, tile_sums, totals, ctx->d_stats, nullptr, nullptr, nullptr};
+    tsc.mask = mask;
+    tsc.cellof = cellof;
     TMC_CUDA(ctx, al.get(&tsc.amb_n, 1));
     ctx->launches += tmc::tmc_count(space, tsc, ctx->sms, st, &ctx->prof);
   }
@@ -943,6 +956,7 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
     TMC_CUDA(ctx, get_shared(&faces, 4 * NF));
     TMC_CUDA(ctx, get_shared(&colors, NF));
     TMC_CUDA(ctx, al.get(&dsc.vwork, NV));
+    TMC_CUDA(ctx, al.get(&dsc.vrank, NV));
     TMC_CUDA(ctx, dmc_vertex_scratch(al, dsc, NV));
     tmc::DmcVertexOut vo{v, nn, v64, n64, vcell, vuvw};
     ctx->launches += tmc::dmc_front_emit(space, dsc, vo, NV, faces, colors, 0, ctx->tune, st, &ctx->prof);

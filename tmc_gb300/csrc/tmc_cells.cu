@@ -17,6 +17,7 @@
 //   tmc_offsets_kernel   in-tile scan -> per-cell vertex / triangle offsets
 //   tmc_emit_kernel      vertices (edge and inner) and triangles
 #include "ffloat.cuh"
+#include "listing.cuh"
 #include "scan.cuh"
 #include "tmc_cells.h"
 
@@ -453,121 +454,88 @@ __device__ void load_amb_cell(const Grid& g, int i, int j, int k, const float u[
 // ------------------------------------------------------------------------------------------
 // kernels
 // ------------------------------------------------------------------------------------------
-// Ambiguous cells are listed (amb_list, warp-aggregated appends) for the float64 counting pass.
-// 8 blocks per SM (32 registers, a few spilled): the kernel is issue-bound, and full occupancy
-// hides its corner loads (0.96 ms against 1.00 ms at 48 registers on the 512^3 step).
-__global__ void __launch_bounds__(kScanThreads, 8) tmc_classify_kernel(CellSpace space, int64_t tile0, uint32_t* rec,
+// One block per kScanTile consecutive cells.  Pass 1: MC cases from the warp-ballot corner rows
+// (warp_cases) and the listing of the crossed cells in cell order (list_tile).  Pass 2: the records
+// of the listed cells at their slots (owned crossed edges, table triangle counts); ambiguous cells are
+// listed by slot (amb_list, warp-aggregated appends) for the float64 counting pass.
+__global__ void __launch_bounds__(kScanThreads, 4) tmc_classify_kernel(CellSpace space, int64_t tile0, uint32_t* rec,
+                                                                   uint16_t* cellof, CellMask* mask,
                                                                    unsigned long long* tile_sums,
                                                                    unsigned long long* stats, uint32_t* amb_list,
                                                                    unsigned* amb_n) {
   const int64_t tile = tile0 + blockIdx.x;
+  __shared__ uint16_t act_list[kScanTile];
+  __shared__ uint8_t case_of[kScanTile];
+  __shared__ uint32_t wmask[kScanTile / 32], wpre[kScanTile / 32];
+  __shared__ int total;
+  __shared__ unsigned long long tile_sum;
+  if (threadIdx.x == 0) tile_sum = 0;
   const Grid g = space.grid_of_tile(tile);
   const int64_t n = g.ncells();
   const int64_t vbase = tile * kScanTile;
-  unsigned long long local = 0, act = 0, amb = 0;
+  const int lane = threadIdx.x & 31;
+  unsigned actbits = 0;
+#pragma unroll 2
   for (int s = 0; s < kScanItems; s++) {
-    const int64_t vc = vbase + (int64_t)s * kScanThreads + threadIdx.x;
-    if (vc >= space.n) break;
+    const int off = s * kScanThreads + threadIdx.x;
+    const int64_t vc = vbase + off;
     const int64_t c = vc - g.vbase;  // cell of the volume (beyond its last cell: padding)
-    uint32_t r = 0;
-    bool listed = false;
-    if (c < n) {
-      int i, j, k;
-      tcell_ijk(g, c, i, j, k);
-      float u[8];
-      tload_corners(g, i, j, k, u);
-      unsigned cs = 0;
-#pragma unroll
-      for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
-      if (cs != 0 && cs != 255) {
-        const uint32_t em = case_edge_mask(cs);
-        r = em & owned_edges(i, j, k);
-        if (!case_ambiguous(cs)) {
-          r |= (uint32_t)(c_tmc_tris[cs] & 0xF) << 15;
-        } else {
-          // counted by tmc_amb_count_kernel (float64), which adds to this tile's sums
-          r |= 1u << 21;
-          amb++;
-          listed = true;
-        }
-        act++;
-      }
-    }
-    rec[vc] = r;
+    const bool valid = vc < space.n && c < n;
+    int i = 0, j = 0, k = 0;
+    if (valid) tcell_ijk(g, c, i, j, k);
+    const unsigned cs = warp_cases(g, valid, i, j, k);
+    case_of[off] = (uint8_t)cs;
+    actbits |= (unsigned)(cs != 0 && cs != 255) << s;
+  }
+  const int na = list_tile(actbits, tile, mask, wmask, wpre, act_list, &total);
+  unsigned long long local = 0, amb = 0;
+  for (int a = threadIdx.x; a < na; a += blockDim.x) {
+    const int off = act_list[a];
+    const uint32_t slot = (uint32_t)(vbase + a);
+    int i, j, k;
+    tcell_ijk(g, vbase + off - g.vbase, i, j, k);
+    const unsigned cs = case_of[off];
+    uint32_t r = case_edge_mask(cs) & owned_edges(i, j, k);
+    const bool listed = case_ambiguous(cs);
+    // ambiguous: counted by tmc_amb_count_kernel (float64), which adds to this tile's sums
+    r |= listed ? (1u << 21) : (uint32_t)(c_tmc_tris[cs] & 0xF) << 15;
+    amb += listed;
+    rec[slot] = r;
+    cellof[slot] = (uint16_t)off;
     local += ((unsigned long long)trec_nv(r) << 32) | (unsigned long long)trec_ntri(r);
     const unsigned am = __activemask();
     const unsigned bal = __ballot_sync(am, listed);
     if (bal) {
-      const int lane = threadIdx.x & 31, leader = __ffs(bal) - 1;
+      const int leader = __ffs(bal) - 1;
       unsigned base = 0;
       if (lane == leader) base = atomicAdd(amb_n, (unsigned)__popc(bal));
       base = __shfl_sync(am, base, leader);
-      if (listed) amb_list[base + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)vc;
+      if (listed) amb_list[base + __popc(bal & ((1u << lane) - 1u))] = slot;
     }
   }
-  unsigned long long tot;
-  block_exclusive_scan<unsigned long long>(local, &tot);
-  if (threadIdx.x == 0) tile_sums[tile] = tot;
   for (int o = 16; o; o >>= 1) {
-    act += __shfl_down_sync(0xffffffffu, act, o);
+    local += __shfl_down_sync(0xffffffffu, local, o);
     amb += __shfl_down_sync(0xffffffffu, amb, o);
   }
-  if ((threadIdx.x & 31) == 0 && (act | amb)) {
-    atomicAdd(stats + 0, act);
-    atomicAdd(stats + 1, amb);
-  }
-}
-
-// Block-wide compaction of the cells of one tile that satisfy `pred` into list[0..return).
-template <typename Pred>
-__device__ __forceinline__ int compact_tile(const uint32_t* rec, int64_t base, int64_t n, Pred pred, uint32_t* list,
-                                            int* wcount, int* total) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  bool act[kScanItems];
-  int mine = 0;
-#pragma unroll
-  for (int s = 0; s < kScanItems; s++) {
-    const int64_t c = base + (int64_t)s * kScanThreads + threadIdx.x;
-    act[s] = (c < n) && pred(rec[c]);
-    mine += act[s];
-  }
-  int pre = mine;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, pre, o);
-    if (lane >= o) pre += y;
-  }
-  if (lane == 31) wcount[wid] = pre;
+  if (lane == 0 && local) atomicAdd(&tile_sum, local);
+  if (lane == 0 && amb) atomicAdd(stats + 1, amb);
+  if (threadIdx.x == 0 && na) atomicAdd(stats + 0, (unsigned long long)na);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int s = 0;
-    for (int w = 0; w < kScanThreads / 32; w++) {
-      const int x = wcount[w];
-      wcount[w] = s;
-      s += x;
-    }
-    *total = s;
-  }
-  __syncthreads();
-  int pos = wcount[wid] + pre - mine;
-#pragma unroll
-  for (int s = 0; s < kScanItems; s++)
-    if (act[s]) list[pos++] = (uint32_t)(s * kScanThreads + threadIdx.x);
-  __syncthreads();
-  return *total;
+  if (threadIdx.x == 0) tile_sums[tile] = tile_sum;
 }
 
 // Ambiguous cells from the classification's list: p_slice in counting mode (float64); the counts go
 // into the cell record and, atomically, into the cell's tile sum (one thread per listed cell, no
 // tile barrier to wait on).
-__global__ void __launch_bounds__(128) tmc_amb_count_kernel(CellSpace space, uint32_t* rec,
+__global__ void __launch_bounds__(128) tmc_amb_count_kernel(CellSpace space, const uint16_t* cellof, uint32_t* rec,
                                                             unsigned long long* tile_sums,
                                                             unsigned long long* stats, const uint32_t* list,
                                                             const unsigned* count) {
   const unsigned na = *count;
   unsigned long long sing = 0;
   for (unsigned a = blockIdx.x * blockDim.x + threadIdx.x; a < na; a += gridDim.x * blockDim.x) {
-    const int64_t vcell = list[a];
+    const uint32_t slot = list[a];
+    const int64_t vcell = slot_cell(cellof, slot);
     const Grid g = space.grid_of_tile(vcell / kScanTile);
     const int64_t cell = vcell - g.vbase;
     int i, j, k;
@@ -583,21 +551,24 @@ __global__ void __launch_bounds__(128) tmc_amb_count_kernel(CellSpace space, uin
     for (int e = 0; e < 12; e++) vid[e] = 0;
     TriSink ts{nullptr, 0};
     const AmbResult ar = p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, 0, ts, amb.P, amb.N, nullptr);
-    rec[vcell] |= (uint32_t)ar.inner << 12 | (uint32_t)ts.n << 15 | (ar.error ? (1u << 22) : 0u);
+    rec[slot] |= (uint32_t)ar.inner << 12 | (uint32_t)ts.n << 15 | (ar.error ? (1u << 22) : 0u);
     const unsigned long long add = ((unsigned long long)ar.inner << 32) | (unsigned long long)ts.n;
-    if (add) atomicAdd(tile_sums + vcell / kScanTile, add);
+    if (add) atomicAdd(tile_sums + (slot >> kTileShift), add);
     sing += ar.error;
   }
   if (sing) atomicAdd(stats + 5, sing);
 }
 
-// In-tile exclusive scan of the records -> per-cell vertex and triangle offsets (blocked layout).
-__global__ void __launch_bounds__(kScanThreads) tmc_offsets_kernel(int64_t n, const uint32_t* rec,
+// In-tile exclusive scan of the listed cells' records -> their vertex and triangle offsets (blocked
+// layout over the tile's slots).
+__global__ void __launch_bounds__(kScanThreads) tmc_offsets_kernel(const CellMask* mask, const uint32_t* rec,
                                                                   const unsigned long long* tile_off,
                                                                   int32_t* voff, int32_t* toff) {
-  const int64_t first = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  const int64_t end = base + tile_listed(mask, blockIdx.x);
+  const int64_t first = base + (int64_t)threadIdx.x * kScanItems;
   uint32_t r[kScanItems];
-  load8(rec, first, n, r);
+  load8(rec, first, end, r);
   unsigned long long sum = 0;
 #pragma unroll
   for (int s = 0; s < kScanItems; s++) sum += ((unsigned long long)trec_nv(r[s]) << 32) | trec_ntri(r[s]);
@@ -610,8 +581,8 @@ __global__ void __launch_bounds__(kScanThreads) tmc_offsets_kernel(int64_t n, co
     to[s] = (int32_t)(pre & 0xffffffffull);
     pre += ((unsigned long long)trec_nv(r[s]) << 32) | trec_ntri(r[s]);
   }
-  store8(voff, first, n, vo);
-  store8(toff, first, n, to);
+  store8(voff, first, end, vo);
+  store8(toff, first, end, to);
 }
 
 // corner value v of a cell's eight (selects, so that a run-time index keeps u in registers)
@@ -697,8 +668,8 @@ __device__ __forceinline__ void edge_vertex_f32(const Grid& g, int i, int j, int
 // Vertex index of each crossed edge of a cell, within the cell's volume (vfirst: the volume's first
 // vertex in the space-wide numbering; vbase: the cell's first vertex, space-wide).
 __device__ __forceinline__ void tmc_vertex_ids(const Grid& g, int i, int j, int k, uint32_t em, uint32_t own,
-                                               int32_t vbase, int32_t vfirst, const uint32_t* rec,
-                                               const int32_t* voff, int32_t vid[12]) {
+                                               int32_t vbase, int32_t vfirst, const CellMask* mask,
+                                               const uint32_t* rec, const int32_t* voff, int32_t vid[12]) {
 #pragma unroll
   for (int e = 0; e < 12; e++) vid[e] = -1;
   // crossed edges as a mask, lowest first: the lanes of a warp resolve their k-th edges together
@@ -709,22 +680,24 @@ __device__ __forceinline__ void tmc_vertex_ids(const Grid& g, int i, int j, int 
     } else {
       int oi, oj, ok, oe = 0;
       edge_owner(i, j, k, e, oi, oj, ok, oe);
-      const int64_t oc = g.vcell(oi, oj, ok);
-      vid[e] = voff[oc] - vfirst + __popc(trec_owned(rec[oc]) & ((1u << oe) - 1u));
+      const uint32_t os = listed_slot(mask, (uint32_t)g.vcell(oi, oj, ok));  // crossed edge: listed owner
+      vid[e] = voff[os] - vfirst + __popc(trec_owned(rec[os]) & ((1u << oe) - 1u));
     }
   }
 }
 
 // Ambiguous cells (listed by the emit kernel): p_slice triangles and inner vertices, float64.
-__global__ void __launch_bounds__(128) tmc_ambiguous_kernel(CellSpace space, const uint32_t* rec,
+__global__ void __launch_bounds__(128) tmc_ambiguous_kernel(CellSpace space, const CellMask* mask,
+                                                            const uint16_t* cellof, const uint32_t* rec,
                                                             const int32_t* voff, const int32_t* toff,
                                                             const unsigned long long* tile_off, TmcVertexOut out,
                                                             int32_t* tris, const uint32_t* list,
                                                             const unsigned* count) {
   const unsigned na = *count;
   for (unsigned a = blockIdx.x * blockDim.x + threadIdx.x; a < na; a += gridDim.x * blockDim.x) {
-    const int64_t vcell = list[a];
-    const uint32_t r = rec[vcell];
+    const uint32_t slot = list[a];
+    const int64_t vcell = slot_cell(cellof, slot);
+    const uint32_t r = rec[slot];
     const Grid g = space.grid_of_tile(vcell / kScanTile);
     const int32_t vfirst = (int32_t)(tile_off[g.vbase / kScanTile] >> 32);
     const int64_t cell = vcell - g.vbase;
@@ -738,25 +711,26 @@ __global__ void __launch_bounds__(128) tmc_ambiguous_kernel(CellSpace space, con
     const uint32_t em = case_edge_mask(cs);
     const uint32_t own = trec_owned(r);
     int32_t vid[12];
-    tmc_vertex_ids(g, i, j, k, em, own, voff[vcell], vfirst, rec, voff, vid);
-    TriSink ts{tris + 3 * (int64_t)toff[vcell], 0};
+    tmc_vertex_ids(g, i, j, k, em, own, voff[slot], vfirst, mask, rec, voff, vid);
+    TriSink ts{tris + 3 * (int64_t)toff[slot], 0};
     AmbCell amb;
     // corner positions and gradients serve only inner vertices, which the counting pass recorded
     load_amb_cell(g, i, j, k, u, em, amb, trec_inner(r) > 0);
     // inner vertices are numbered within the volume: shift the outputs to its first vertex
     InnerOut io{out.v + 3 * (int64_t)vfirst, out.n + 3 * (int64_t)vfirst, out.v64 ? out.v64 + 3 * (int64_t)vfirst : nullptr};
-    p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, voff[vcell] - vfirst + __popc(own), ts, amb.P, amb.N, &io);
+    p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, voff[slot] - vfirst + __popc(own), ts, amb.P, amb.N, &io);
   }
 }
 
 // One active cell: its owned edge vertices and (unambiguous case) its table triangles; ambiguous
 // cells go to the list of the float64 pass.
 template <bool kPos64>
-__device__ __forceinline__ void emit_cell(const Grid& g, int32_t vfirst, int64_t vcell, const uint32_t* rec,
-                                          const int32_t* voff, const int32_t* toff, const TmcVertexOut& out,
-                                          int32_t* tris, uint32_t* amb_list, unsigned* amb_count) {
+__device__ __forceinline__ void emit_cell(const Grid& g, int32_t vfirst, uint32_t slot, int64_t vcell,
+                                          const CellMask* mask, const uint32_t* rec, const int32_t* voff,
+                                          const int32_t* toff, const TmcVertexOut& out, int32_t* tris,
+                                          uint32_t* amb_list, unsigned* amb_count) {
   const int64_t cell = vcell - g.vbase;
-  const uint32_t r = rec[vcell];
+  const uint32_t r = rec[slot];
   int i, j, k;
   tcell_ijk(g, cell, i, j, k);
   float u[8];
@@ -766,7 +740,7 @@ __device__ __forceinline__ void emit_cell(const Grid& g, int32_t vfirst, int64_t
   for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
   const uint32_t em = case_edge_mask(cs);
   const uint32_t own = trec_owned(r);
-  const int32_t vbase = voff[vcell];
+  const int32_t vbase = voff[slot];
   // owned edge vertices, in edge order (the crossed owned edges as a mask, lowest first)
   int rank = 0;
   for (uint32_t mo = em & own; mo; mo &= mo - 1, rank++) {
@@ -780,12 +754,12 @@ __device__ __forceinline__ void emit_cell(const Grid& g, int32_t vfirst, int64_t
   }
   if ((r >> 21) & 1) {
     // ambiguous: triangles and inner vertices in a separate float64 pass
-    if (!((r >> 22) & 1)) amb_list[atomicAdd(amb_count, 1u)] = (uint32_t)vcell;
+    if (!((r >> 22) & 1)) amb_list[atomicAdd(amb_count, 1u)] = slot;
     return;
   }
   int32_t vid[12];
-  tmc_vertex_ids(g, i, j, k, em, own, vbase, vfirst, rec, voff, vid);
-  TriSink ts{tris + 3 * (int64_t)toff[vcell], 0};
+  tmc_vertex_ids(g, i, j, k, em, own, vbase, vfirst, mask, rec, voff, vid);
+  TriSink ts{tris + 3 * (int64_t)toff[slot], 0};
   // unambiguous: table triangles with reversed winding (t_mc, mc/MarchingCubes.cpp:276-294)
   const uint64_t tw = c_tmc_tris[cs];
   const int nt = (int)(tw & 0xF);
@@ -796,14 +770,15 @@ __device__ __forceinline__ void emit_cell(const Grid& g, int32_t vfirst, int64_t
   }
 }
 
-// Each warp walks chunks of 32 consecutive cells, appends the active ones to its own queue in
-// shared memory (ballot + popcount), and processes the queue 32 cells at a time, one per lane: all
-// lanes busy, and no block barrier (warps never wait for one another).
+// Each warp walks chunks of 32 consecutive slots of the listed cells, appends the cells with a
+// record to its own queue in shared memory (ballot + popcount), and processes the queue 32 cells at
+// a time, one per lane: all lanes busy, and no block barrier (warps never wait for one another).
 constexpr int kEmitThreads = 256;
 // kPos64: some volume of the launch wants float64 positions (the float64 edge-vertex path is
 // compiled only into that instantiation, which keeps the common one's code small)
 template <bool kBatch, bool kPos64>
-__global__ void __launch_bounds__(kEmitThreads, 4) tmc_emit_kernel(CellSpace space, const uint32_t* rec,
+__global__ void __launch_bounds__(kEmitThreads, 4) tmc_emit_kernel(CellSpace space, const CellMask* mask,
+                                                                   const uint16_t* cellof, const uint32_t* rec,
                                                                    const int32_t* voff, const int32_t* toff,
                                                                    const unsigned long long* tile_off,
                                                                    TmcVertexOut out, int32_t* tris,
@@ -812,27 +787,29 @@ __global__ void __launch_bounds__(kEmitThreads, 4) tmc_emit_kernel(CellSpace spa
   __shared__ uint32_t queue[kWarps][64];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   uint32_t* Q = queue[wid];
-  const int64_t n = space.n;
-  const int64_t chunks = ceil_div(n, 32);
+  const int64_t chunks = ceil_div(space.n, kScanTile) * (kScanTile / 32);
   int qn = 0;  // queued cells (the same on every lane)
   for (int64_t chunk = (int64_t)blockIdx.x * kWarps + wid;; chunk += (int64_t)gridDim.x * kWarps) {
     const bool more = chunk < chunks;
     if (more) {
-      const int64_t c = chunk * 32 + lane;
-      const bool act = c < n && rec[c] != 0;
+      const int64_t tile = chunk >> (kTileShift - 5);
+      const uint32_t r = (uint32_t)(chunk & (kScanTile / 32 - 1)) * 32 + lane;
+      const uint32_t slot = (uint32_t)(tile << kTileShift) + r;
+      const bool act = r < tile_listed(mask, tile) && rec[slot] != 0;
       const unsigned bal = __ballot_sync(0xffffffffu, act);
-      if (act) Q[qn + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)c;
+      if (act) Q[qn + __popc(bal & ((1u << lane) - 1u))] = slot;
       qn += __popc(bal);
       __syncwarp();
     }
     while (qn >= 32 || (!more && qn > 0)) {
       const int take = qn < 32 ? qn : 32;
       if (lane < take) {
-        const int64_t vcell = Q[lane];
+        const uint32_t slot = Q[lane];
+        const uint32_t vcell = slot_cell(cellof, slot);
         // the cell's volume: read in place (a batch's grid table, or the launch parameter)
         const Grid& g = kBatch ? space.grids[__ldg(space.tile_vol + vcell / kScanTile)] : space.one;
         const int32_t vfirst = kBatch ? (int32_t)(tile_off[g.vbase / kScanTile] >> 32) : 0;
-        emit_cell<kPos64>(g, vfirst, vcell, rec, voff, toff, out, tris, amb_list, amb_count);
+        emit_cell<kPos64>(g, vfirst, slot, vcell, mask, rec, voff, toff, out, tris, amb_list, amb_count);
       }
       __syncwarp();
       const int rest = qn - take;  // at most 31: move them to the front
@@ -863,8 +840,8 @@ int tmc_count(const CellSpace& space, TmcScratch& s, int sms, cudaStream_t st, P
     cudaMemsetAsync(s.amb_n, 0, sizeof(unsigned), st);
     auto classify = [&](int64_t t0, int64_t t1) {
       if (t1 <= t0) return;
-      tmc_classify_kernel<<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(space, t0, s.rec, s.tile_sums, s.stats,
-                                                                        amb_cells, s.amb_n);
+      tmc_classify_kernel<<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(space, t0, s.rec, s.cellof, s.mask,
+                                                                        s.tile_sums, s.stats, amb_cells, s.amb_n);
       k++;
     };
     if (ngates == 0) classify(0, tiles);
@@ -881,11 +858,11 @@ int tmc_count(const CellSpace& space, TmcScratch& s, int sms, cudaStream_t st, P
     // whole waves; the list length is only known on the device, so the grid follows the cell count
     static const int r_amb = resident_blocks(tmc_amb_count_kernel, 128);
     tmc_amb_count_kernel<<<(unsigned)wave_grid(r_amb, sms, 16, ceil_div(n, 64), 128), 128, 0,
-                           st>>>(space, s.rec, s.tile_sums, s.stats, amb_cells, s.amb_n);
+                           st>>>(space, s.cellof, s.rec, s.tile_sums, s.stats, amb_cells, s.amb_n);
   }
   Stage t(prof, "tmc_scan", st);
   scan_tile_sums_kernel<<<1, 1024, 0, st>>>(s.tile_sums, tiles, s.totals);
-  tmc_offsets_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(n, s.rec, s.tile_sums, s.voff, s.toff);
+  tmc_offsets_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(s.mask, s.rec, s.tile_sums, s.voff, s.toff);
   return k + 3;
 }
 
@@ -898,8 +875,8 @@ int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tr
         1, std::min<int64_t>(ceil_div(space.n, 32 * (kEmitThreads / 32)), (int64_t)sms * tu.emit_blocks_per_sm));
     cudaMemsetAsync(s.amb_count, 0, sizeof(unsigned), st);
 #define TMC_EMIT(B, P)                                                                                       \
-  tmc_emit_kernel<B, P><<<(unsigned)blocks, kEmitThreads, 0, st>>>(space, s.rec, s.voff, s.toff, s.tile_sums, vo, \
-                                                                  tris, s.amb_list, s.amb_count)
+  tmc_emit_kernel<B, P><<<(unsigned)blocks, kEmitThreads, 0, st>>>(space, s.mask, s.cellof, s.rec, s.voff, s.toff, \
+                                                                  s.tile_sums, vo, tris, s.amb_list, s.amb_count)
     const bool pos64 = vo.v64 != nullptr;
     if (space.grids) {
       if (pos64) TMC_EMIT(true, true);
@@ -912,7 +889,7 @@ int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tr
   }
   Stage t2(prof, "tmc_ambiguous", st);
   tmc_ambiguous_kernel<<<(unsigned)std::max<int64_t>(1, (int64_t)sms * 8), 128, 0, st>>>(
-      space, s.rec, s.voff, s.toff, s.tile_sums, vo, tris, s.amb_list, s.amb_count);
+      space, s.mask, s.cellof, s.rec, s.voff, s.toff, s.tile_sums, vo, tris, s.amb_list, s.amb_count);
   return 2;
 }
 

@@ -24,6 +24,10 @@ struct TmcScratch {
   uint32_t* amb_list;   // ambiguous cells with triangles, filled by the emit kernel
   unsigned* amb_count;
   unsigned* amb_n;      // ambiguous cells listed by the classification (count)
+  // listed cells (common.cuh): rec, voff and toff hold one entry per listed cell at its slot, the
+  // ambiguous lists hold slots
+  CellMask* mask;       // per 32 cells of the space
+  uint16_t* cellof;     // per slot: in-tile offset of the listed cell
 };
 
 // Per-cell scratch is indexed in the cell space; triangles hold vertex indices within their own
