@@ -112,6 +112,16 @@ __device__ __forceinline__ uint32_t tile_listed(const CellMask* mask, int64_t ti
   const uint2 a = __ldg(reinterpret_cast<const uint2*>(mask) + (tile << (kTileShift - 5)) + 63);
   return a.y + __popc(a.x);
 }
+// Chunk q of 32 slots for the kernels that walk the listed cells: chunks run over the tiles first
+// (chunk q covers slots 32 * (q / tiles) .. + 31 of tile q % tiles), so that consecutive warps take the
+// front slots of consecutive tiles, where every tile's listed cells sit; numbered the other way, the
+// warps whose index is a multiple of 64 apart would take the same part of every tile and a few of
+// them would get all the work.
+__device__ __forceinline__ void slot_chunk(int64_t q, int64_t tiles, int64_t& tile, uint32_t& first) {
+  const int64_t part = q / tiles;
+  tile = q - part * tiles;
+  first = (uint32_t)(tile << kTileShift) + (uint32_t)part * 32u;
+}
 // the cell behind a slot (cell: in-tile cell offsets of the listed cells)
 __device__ __forceinline__ uint32_t slot_cell(const uint16_t* cell, uint32_t slot) {
   return ((slot >> kTileShift) << kTileShift) + __ldg(cell + slot);

@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(kScanThreads, 3) dmc_classify_kernel(CellSpace
   const int lane = threadIdx.x & 31;
   // pass 1: cases
   unsigned actbits = 0;
-#pragma unroll 2
+#pragma unroll
   for (int s = 0; s < kScanItems; s++) {
     const int off = s * kScanThreads + threadIdx.x;
     const int64_t vc = vbase + off;
@@ -772,14 +772,15 @@ __global__ void __launch_bounds__(kQuadThreads) dmc_quad_kernel(CellSpace space,
   __shared__ uint32_t queue[kWarps][64];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   uint32_t* Q = queue[wid];
-  const int64_t chunks = ceil_div(space.n, kScanTile) * (kScanTile / 32);
+  const int64_t tiles = ceil_div(space.n, kScanTile), chunks = tiles * (kScanTile / 32);
   int qn = 0;  // queued cells (the same on every lane)
   for (int64_t chunk = (int64_t)blockIdx.x * kWarps + wid;; chunk += (int64_t)gridDim.x * kWarps) {
     const bool more = chunk < chunks;
     if (more) {
-      const int64_t tile = chunk >> (kTileShift - 5);
-      const uint32_t r = (uint32_t)(chunk & (kScanTile / 32 - 1)) * 32 + lane;
-      const uint32_t slot = (uint32_t)(tile << kTileShift) + r;
+      int64_t tile;
+      uint32_t first;
+      slot_chunk(chunk, tiles, tile, first);
+      const uint32_t slot = first + lane, r = slot & (kScanTile - 1);
       const bool own = r < tile_listed(mask, tile) && rec_nq(rec[slot]) != 0;
       const unsigned bal = __ballot_sync(0xffffffffu, own);
       if (own) Q[qn + __popc(bal & ((1u << lane) - 1u))] = slot;

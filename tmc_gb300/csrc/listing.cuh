@@ -19,27 +19,30 @@ __device__ __forceinline__ unsigned warp_cases(const Grid& g, bool valid, int i,
   const int lane = threadIdx.x & 31;
   const int64_t sy = g.nx, sz = (int64_t)g.nx * g.ny;
   const float* p = g.f + (valid ? ((int64_t)k * g.ny + j) * g.nx + i : 0);
-  bool b0 = false, b1 = false, b2 = false, b3 = false;
+  // the next lane holds cell (i + 1, j, k) unless this is the warp's last lane or the row's last cell;
+  // those lanes load their x+1 points together with the others' loads (no second round trip)
+  const bool own_next = valid && (lane == 31 || i >= g.nx - 2);
+  bool b0 = false, b1 = false, b2 = false, b3 = false, n0 = false, n1 = false, n2 = false, n3 = false;
   if (valid) {
     b0 = __ldg(p) >= g.iso_up;
     b1 = __ldg(p + sy) >= g.iso_up;
     b2 = __ldg(p + sz) >= g.iso_up;
     b3 = __ldg(p + sz + sy) >= g.iso_up;
   }
-  const unsigned m0 = __ballot_sync(0xffffffffu, b0), m1 = __ballot_sync(0xffffffffu, b1),
-                 m2 = __ballot_sync(0xffffffffu, b2), m3 = __ballot_sync(0xffffffffu, b3);
-  if (!valid) return 0;
-  bool n0, n1, n2, n3;
-  if (lane < 31 && i < g.nx - 2) {  // the next lane holds cell (i + 1, j, k)
-    n0 = (m0 >> (lane + 1)) & 1u;
-    n1 = (m1 >> (lane + 1)) & 1u;
-    n2 = (m2 >> (lane + 1)) & 1u;
-    n3 = (m3 >> (lane + 1)) & 1u;
-  } else {
+  if (own_next) {
     n0 = __ldg(p + 1) >= g.iso_up;
     n1 = __ldg(p + sy + 1) >= g.iso_up;
     n2 = __ldg(p + sz + 1) >= g.iso_up;
     n3 = __ldg(p + sz + sy + 1) >= g.iso_up;
+  }
+  const unsigned m0 = __ballot_sync(0xffffffffu, b0), m1 = __ballot_sync(0xffffffffu, b1),
+                 m2 = __ballot_sync(0xffffffffu, b2), m3 = __ballot_sync(0xffffffffu, b3);
+  if (!valid) return 0;
+  if (!own_next) {
+    n0 = (m0 >> (lane + 1)) & 1u;
+    n1 = (m1 >> (lane + 1)) & 1u;
+    n2 = (m2 >> (lane + 1)) & 1u;
+    n3 = (m3 >> (lane + 1)) & 1u;
   }
   return (unsigned)b0 | (unsigned)n0 << 1 | (unsigned)b1 << 2 | (unsigned)n1 << 3 | (unsigned)b2 << 4 |
          (unsigned)n2 << 5 | (unsigned)b3 << 6 | (unsigned)n3 << 7;
