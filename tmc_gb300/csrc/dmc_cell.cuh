@@ -66,11 +66,13 @@ __device__ __forceinline__ uint32_t classify_active(const Grid& g, int i, int j,
   const uint64_t c = amb ? dmc_polygon(cs, u, g.iso, cc) : table_contour(cc[cs]);
   const int ncnt = cnt_count(c);
   uint32_t rec = amb ? (1u << 29) : 0u;
+  // a cell at least one cell away from every border has only interior edges (most listed cells)
+  const bool inner = i >= 1 && j >= 1 && k >= 1 && i <= g.nx - 3 && j <= g.ny - 3 && k <= g.nz - 3;
   int nv = 0, flat = 0;
   for (int t = 0; t < ncnt; t++) {
     const int sz = cnt_size(c, t);
-    bool used = false;
-    for (int q = 0; q < sz; q++) used = used || edge_interior(g, i, j, k, cnt_edge(c, flat + q));
+    bool used = inner;
+    for (int q = 0; q < sz && !used; q++) used = edge_interior(g, i, j, k, cnt_edge(c, flat + q));
     if (used) {
       for (int q = 0; q < sz; q++) rec |= (uint32_t)nv << (5 + 2 * cnt_edge(c, flat + q));
       nv++;
@@ -80,9 +82,9 @@ __device__ __forceinline__ uint32_t classify_active(const Grid& g, int i, int j,
   // owned quads: crossed interior edges 0 (x), 3 (y), 8 (z) at the cell's lower corner
   const uint32_t em = case_edge_mask(cs);
   int nq = 0;
-  nq += ((em >> 0) & 1) && edge_interior(g, i, j, k, 0);
-  nq += ((em >> 3) & 1) && edge_interior(g, i, j, k, 3);
-  nq += ((em >> 8) & 1) && edge_interior(g, i, j, k, 8);
+  nq += ((em >> 0) & 1) && (inner || edge_interior(g, i, j, k, 0));
+  nq += ((em >> 3) & 1) && (inner || edge_interior(g, i, j, k, 3));
+  nq += ((em >> 8) & 1) && (inner || edge_interior(g, i, j, k, 8));
   rec |= (uint32_t)nv | ((uint32_t)nq << 3);
   return rec;
 }

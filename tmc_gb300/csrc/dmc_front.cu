@@ -64,14 +64,31 @@ __global__ void __launch_bounds__(kScanThreads, 3) dmc_classify_kernel(CellSpace
   const int lane = threadIdx.x & 31;
   // pass 1: cases
   unsigned actbits = 0;
+  // coordinates of the thread's first cell, then advanced by kScanThreads cells per step (one row
+  // wrap at most when rows hold kScanThreads cells or more, a division otherwise)
+  const int cx = g.nx - 1, cy = g.ny - 1;
+  int i, j, k;
+  cell_ijk(g, vbase + threadIdx.x - g.vbase, i, j, k);
 #pragma unroll
   for (int s = 0; s < kScanItems; s++) {
     const int off = s * kScanThreads + threadIdx.x;
     const int64_t vc = vbase + off;
     const int64_t c = vc - g.vbase;  // cell of the volume (beyond its last cell: padding)
     const bool valid = vc < space.n && c < n;
-    int i = 0, j = 0, k = 0;
-    if (valid) cell_ijk(g, c, i, j, k);
+    if (s > 0) {
+      if (cx >= kScanThreads) {
+        i += kScanThreads;
+        if (i >= cx) {
+          i -= cx;
+          if (++j >= cy) {
+            j = 0;
+            ++k;
+          }
+        }
+      } else if (valid) {
+        cell_ijk(g, c, i, j, k);
+      }
+    }
     const unsigned cs = warp_cases(g, valid, i, j, k);
     case_of[off] = (uint8_t)cs;
     actbits |= (unsigned)(cs != 0 && cs != 255) << s;

@@ -475,14 +475,31 @@ __global__ void __launch_bounds__(kScanThreads, 4) tmc_classify_kernel(CellSpace
   const int64_t vbase = tile * kScanTile;
   const int lane = threadIdx.x & 31;
   unsigned actbits = 0;
+  // coordinates of the thread's first cell, then advanced by kScanThreads cells per step (one row
+  // wrap at most when rows hold kScanThreads cells or more, a division otherwise)
+  const int cx = g.nx - 1, cy = g.ny - 1;
+  int i, j, k;
+  tcell_ijk(g, vbase + threadIdx.x - g.vbase, i, j, k);
 #pragma unroll
   for (int s = 0; s < kScanItems; s++) {
     const int off = s * kScanThreads + threadIdx.x;
     const int64_t vc = vbase + off;
     const int64_t c = vc - g.vbase;  // cell of the volume (beyond its last cell: padding)
     const bool valid = vc < space.n && c < n;
-    int i = 0, j = 0, k = 0;
-    if (valid) tcell_ijk(g, c, i, j, k);
+    if (s > 0) {
+      if (cx >= kScanThreads) {
+        i += kScanThreads;
+        if (i >= cx) {
+          i -= cx;
+          if (++j >= cy) {
+            j = 0;
+            ++k;
+          }
+        }
+      } else if (valid) {
+        tcell_ijk(g, c, i, j, k);
+      }
+    }
     const unsigned cs = warp_cases(g, valid, i, j, k);
     case_of[off] = (uint8_t)cs;
     actbits |= (unsigned)(cs != 0 && cs != 255) << s;
@@ -495,7 +512,8 @@ __global__ void __launch_bounds__(kScanThreads, 4) tmc_classify_kernel(CellSpace
     int i, j, k;
     tcell_ijk(g, vbase + off - g.vbase, i, j, k);
     const unsigned cs = case_of[off];
-    uint32_t r = case_edge_mask(cs) & owned_edges(i, j, k);
+    // away from the lower borders a cell owns a fixed set of edges (folded at compile time)
+    uint32_t r = case_edge_mask(cs) & ((i > 0 && j > 0 && k > 0) ? owned_edges(1, 1, 1) : owned_edges(i, j, k));
     const bool listed = case_ambiguous(cs);
     // ambiguous: counted by tmc_amb_count_kernel (float64), which adds to this tile's sums
     r |= listed ? (1u << 21) : (uint32_t)(c_tmc_tris[cs] & 0xF) << 15;
