@@ -39,6 +39,7 @@ struct DmcScratch {
   CellMask* mask;                 // per 32 cells of the space
   uint16_t* cellof;               // per slot: in-tile offset of the listed cell
   uint8_t* vrank;                 // per vertex: rank among its cell's vertices (vwork: the cell's slot)
+  unsigned* amb_n;                // listed cells with an ambiguous case (their slots wait in qoff)
 };
 constexpr size_t kProjRecordBytes = 144;  // sizeof(repr::ProjRecord)
 

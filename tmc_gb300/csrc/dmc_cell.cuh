@@ -57,13 +57,10 @@ __device__ __forceinline__ void cell_ijk(const Grid& g, int64_t c, int& i, int& 
   k = (int)kk;
 }
 
-// Record of one cell (0 for an inactive cell); cc: the 256 packed case contours.
-// Record of an active cell (case cs, neither 0 nor 255); u, the corners, are read only for the
-// ambiguous cases (the decider).
-__device__ __forceinline__ uint32_t classify_active(const Grid& g, int i, int j, int k, unsigned cs, const float* u,
-                                                    const uint64_t* cc) {
-  const bool amb = case_ambiguous(cs);
-  const uint64_t c = amb ? dmc_polygon(cs, u, g.iso, cc) : table_contour(cc[cs]);
+// Record of a listed cell (case cs, neither 0 nor 255) from its contour word c (at most four
+// contours); amb: the case is ambiguous (record bit 29).
+__device__ __forceinline__ uint32_t record_from_contours(const Grid& g, int i, int j, int k, unsigned cs, uint64_t c,
+                                                         bool amb) {
   const int ncnt = cnt_count(c);
   uint32_t rec = amb ? (1u << 29) : 0u;
   // a cell at least one cell away from every border has only interior edges (most listed cells)
@@ -87,6 +84,15 @@ __device__ __forceinline__ uint32_t classify_active(const Grid& g, int i, int j,
   nq += ((em >> 8) & 1) && (inner || edge_interior(g, i, j, k, 8));
   rec |= (uint32_t)nv | ((uint32_t)nq << 3);
   return rec;
+}
+
+// Record of a listed cell; cc: the 256 packed case contours; u, the corners, are read only for the
+// ambiguous cases (the decider).
+__device__ __forceinline__ uint32_t classify_active(const Grid& g, int i, int j, int k, unsigned cs, const float* u,
+                                                    const uint64_t* cc) {
+  const bool amb = case_ambiguous(cs);
+  const uint64_t c = amb ? dmc_polygon(cs, u, g.iso, cc) : table_contour(cc[cs]);
+  return record_from_contours(g, i, j, k, cs, c, amb);
 }
 
 __device__ __forceinline__ uint32_t classify_cell(const Grid& g, int i, int j, int k, const uint64_t* cc,

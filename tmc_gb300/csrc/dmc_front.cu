@@ -41,14 +41,17 @@ __constant__ uint64_t c_case_contour[256] = TMC_CASE_CONTOUR_INIT;
 // classification (per-cell helpers in dmc_cell.cuh)
 // ------------------------------------------------------------------------------------------
 // One block per kScanTile consecutive cells (linear order).  Pass 1: every cell's MC case from the
-// warp-ballot corner rows (warp_cases: one coalesced load per corner row and warp, no per-cell
+// warp-ballot corner rows (tile_cases: one coalesced load per corner row and warp, no per-cell
 // gather); the cells with a case other than 0 and 255 are listed in cell order (list_tile).  Pass 2:
-// contours and records of the listed cells only, written densely at their slots with their in-tile
-// offsets, and the tile's packed (vertices << 32 | quads) sum.
-__global__ void __launch_bounds__(kScanThreads, 3) dmc_classify_kernel(CellSpace space, int64_t tile0, uint32_t* rec,
+// the contours and records of the listed cells with an unambiguous case, written densely at their
+// slots with their in-tile offsets, and the tile's packed (vertices << 32 | quads) sum.  Listed cells
+// with an ambiguous case (the asymptotic decider, ~1 % of the cells) go by slot to amb_list for
+// dmc_amb_kernel, which runs them densely instead of stalling every warp here on a few lanes.
+__global__ void __launch_bounds__(kScanThreads, 6) dmc_classify_kernel(CellSpace space, int64_t tile0, uint32_t* rec,
                                                                    uint16_t* cellof, CellMask* mask,
                                                                    unsigned long long* tile_sums,
-                                                                   unsigned long long* stats) {
+                                                                   unsigned long long* stats, uint32_t* amb_list,
+                                                                   unsigned* amb_n) {
   const int64_t tile = tile0 + blockIdx.x;
   __shared__ uint64_t cc[256];
   __shared__ uint16_t act_list[kScanTile];
@@ -59,57 +62,36 @@ __global__ void __launch_bounds__(kScanThreads, 3) dmc_classify_kernel(CellSpace
   for (int c = threadIdx.x; c < 256; c += blockDim.x) cc[c] = c_case_contour[c];
   if (threadIdx.x == 0) tile_sum = 0;
   const Grid g = space.grid_of_tile(tile);
-  const int64_t n = g.ncells();
   const int64_t vbase = tile * kScanTile;  // first cell of the tile in the space
   const int lane = threadIdx.x & 31;
-  // pass 1: cases
-  unsigned actbits = 0;
-  // coordinates of the thread's first cell, then advanced by kScanThreads cells per step (one row
-  // wrap at most when rows hold kScanThreads cells or more, a division otherwise)
-  const int cx = g.nx - 1, cy = g.ny - 1;
-  int i, j, k;
-  cell_ijk(g, vbase + threadIdx.x - g.vbase, i, j, k);
-#pragma unroll
-  for (int s = 0; s < kScanItems; s++) {
-    const int off = s * kScanThreads + threadIdx.x;
-    const int64_t vc = vbase + off;
-    const int64_t c = vc - g.vbase;  // cell of the volume (beyond its last cell: padding)
-    const bool valid = vc < space.n && c < n;
-    if (s > 0) {
-      if (cx >= kScanThreads) {
-        i += kScanThreads;
-        if (i >= cx) {
-          i -= cx;
-          if (++j >= cy) {
-            j = 0;
-            ++k;
-          }
-        }
-      } else if (valid) {
-        cell_ijk(g, c, i, j, k);
-      }
-    }
-    const unsigned cs = warp_cases(g, valid, i, j, k);
-    case_of[off] = (uint8_t)cs;
-    actbits |= (unsigned)(cs != 0 && cs != 255) << s;
-  }
+  const unsigned actbits = tile_cases(g, space.n, vbase, case_of);
   const int na = list_tile(actbits, tile, mask, wmask, wpre, act_list, &total);
   // pass 2: records of the listed cells
   unsigned long long local = 0, amb = 0, nact = 0;
   for (int a = threadIdx.x; a < na; a += blockDim.x) {
     const int off = act_list[a];
-    const int64_t vc = vbase + off;
-    int i, j, k;
-    cell_ijk(g, vc - g.vbase, i, j, k);
+    const uint32_t slot = (uint32_t)(vbase + a);
     const unsigned cs = case_of[off];
-    float u[8];
-    if (case_ambiguous(cs)) load_corners(g, i, j, k, u);
-    const uint32_t r = classify_active(g, i, j, k, cs, u, cc);
-    rec[vbase + a] = r;
-    cellof[vbase + a] = (uint16_t)off;
-    local += ((unsigned long long)rec_nv(r) << 32) | (unsigned long long)rec_nq(r);
-    amb += (r >> 29) & 1;
-    nact += r != 0;  // active: a record (a used contour, an owned quad or the ambiguous flag)
+    const bool ambiguous = case_ambiguous(cs);
+    cellof[slot] = (uint16_t)off;
+    if (!ambiguous) {
+      int i, j, k;
+      cell_ijk(g, vbase + off - g.vbase, i, j, k);
+      const uint32_t r = record_from_contours(g, i, j, k, cs, table_contour(cc[cs]), false);
+      rec[slot] = r;
+      local += ((unsigned long long)rec_nv(r) << 32) | (unsigned long long)rec_nq(r);
+      nact += r != 0;
+    }
+    amb += ambiguous;
+    const unsigned am = __activemask();
+    const unsigned bal = __ballot_sync(am, ambiguous);
+    if (bal) {
+      const int leader = __ffs(bal) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(amb_n, (unsigned)__popc(bal));
+      base = __shfl_sync(am, base, leader);
+      if (ambiguous) amb_list[base + __popc(bal & ((1u << lane) - 1u))] = slot;
+    }
   }
   for (int o = 16; o; o >>= 1) {
     local += __shfl_down_sync(0xffffffffu, local, o);
@@ -117,10 +99,36 @@ __global__ void __launch_bounds__(kScanThreads, 3) dmc_classify_kernel(CellSpace
     nact += __shfl_down_sync(0xffffffffu, nact, o);
   }
   if (lane == 0 && local) atomicAdd(&tile_sum, local);
+  // stats[0]: cells with a record (a used contour, an owned quad or the ambiguous flag); the
+  // ambiguous cells' records are never empty, so they count here too
   if (lane == 0 && amb) atomicAdd(stats + 1, amb);
-  if (lane == 0 && nact) atomicAdd(stats + 0, nact);
+  if (lane == 0 && (nact | amb)) atomicAdd(stats + 0, nact + amb);
   __syncthreads();
   if (threadIdx.x == 0) tile_sums[tile] = tile_sum;
+}
+
+// The ambiguous listed cells: MC polygon with the asymptotic decider (float-float, float64 near the
+// isovalue), record, and their counts added to their tile's sum (after the classification wrote it).
+__global__ void __launch_bounds__(128) dmc_amb_kernel(CellSpace space, const uint16_t* cellof, uint32_t* rec,
+                                                      unsigned long long* tile_sums, const uint32_t* list,
+                                                      const unsigned* count) {
+  __shared__ uint64_t cc[256];
+  for (int c = threadIdx.x; c < 256; c += blockDim.x) cc[c] = c_case_contour[c];
+  __syncthreads();
+  const unsigned na = *count;
+  for (unsigned a = blockIdx.x * blockDim.x + threadIdx.x; a < na; a += gridDim.x * blockDim.x) {
+    const uint32_t slot = list[a];
+    const int64_t tile = slot >> kTileShift;
+    const Grid g = space.grid_of_tile(tile);
+    int i, j, k;
+    cell_ijk(g, slot_cell(cellof, slot) - g.vbase, i, j, k);
+    float u[8];
+    load_corners(g, i, j, k, u);
+    const uint32_t r = classify_active(g, i, j, k, mc_case(u, g.iso_up), u, cc);
+    rec[slot] = r;
+    const unsigned long long add = ((unsigned long long)rec_nv(r) << 32) | (unsigned long long)rec_nq(r);
+    if (add) atomicAdd(tile_sums + tile, add);
+  }
 }
 
 // In-tile exclusive scan of the listed cells' records -> their vertex and quad offsets (blocked:
@@ -831,13 +839,17 @@ __global__ void __launch_bounds__(kQuadThreads) dmc_quad_kernel(CellSpace space,
 int dmc_front_count(const CellSpace& space, DmcScratch& s, cudaStream_t st, Prof* prof, const TileGate* gates,
                     int ngates) {
   const int64_t tiles = ceil_div(space.n, kScanTile);
-  int k = 0;
+  int k = 0, dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   {
     Stage t(prof, "dmc_classify", st);
+    // the ambiguous cells' list lives in qoff until the offsets kernel writes the quad offsets
+    cudaMemsetAsync(s.amb_n, 0, sizeof(unsigned), st);
     auto classify = [&](int64_t t0, int64_t t1) {
       if (t1 <= t0) return;
-      dmc_classify_kernel<<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(space, t0, s.rec, s.cellof, s.mask,
-                                                                         s.tile_sums, s.stats);
+      dmc_classify_kernel<<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(
+          space, t0, s.rec, s.cellof, s.mask, s.tile_sums, s.stats, reinterpret_cast<uint32_t*>(s.qoff), s.amb_n);
       k++;
     };
     if (ngates == 0) classify(0, tiles);
@@ -848,6 +860,11 @@ int dmc_front_count(const CellSpace& space, DmcScratch& s, cudaStream_t st, Prof
       classify(t0, t1);
       t0 = std::max(t0, t1);
     }
+    // one wave; the list length is only known on the device, so the grid follows the cell count
+    static const int r_amb = resident_blocks(dmc_amb_kernel, 128);
+    dmc_amb_kernel<<<(unsigned)wave_grid(r_amb, sms, 16, ceil_div(space.n, 128), 128), 128, 0, st>>>(
+        space, s.cellof, s.rec, s.tile_sums, reinterpret_cast<const uint32_t*>(s.qoff), s.amb_n);
+    k++;
   }
   Stage t(prof, "dmc_scan", st);
   scan_tile_sums_kernel<<<1, 1024, 0, st>>>(s.tile_sums, tiles, s.totals);

@@ -9,43 +9,86 @@ namespace tmc {
 
 static_assert(kScanTile == 1 << kTileShift, "listed-cell slots assume 2048-cell scan tiles");
 
-// MC cases of 32 consecutive cells of a volume, one per lane of a warp (every lane must call it):
-// each lane loads the point at its own cell's lower x on the four corner rows (y,z), (y+1,z),
-// (y,z+1), (y+1,z+1) -- one coalesced 128-byte load per row for the warp -- and takes the points at
-// x+1 from the next lane's ballot bits when that lane holds the next cell of the same row (every lane
-// but the last of the warp and the last cell of a row); those few lanes load their x+1 points.
-// `valid`: the lane has a cell (i, j, k); invalid lanes return 0.
-__device__ __forceinline__ unsigned warp_cases(const Grid& g, bool valid, int i, int j, int k) {
+// Pass 1 of both classifications: the MC case of each of the tile's kScanTile cells (linear order,
+// thread t takes cells t, t + 256, ..., so that at each step the 32 lanes of a warp hold 32
+// consecutive cells), stored in case_of; returns the thread's listed bits (bit s: the cell of step s
+// has a case other than 0 and 255).
+//
+// Per step each lane loads the point at its cell's lower x on the four corner rows (y,z), (y+1,z),
+// (y,z+1), (y+1,z+1) -- one coalesced 128-byte load per row and warp -- and the warp's ballots of the
+// comparisons give every lane the bits at x and x+1 at once ((mask >> lane) & 3) when the next lane
+// holds the next cell of the same row.  The warp's last lane and a row's last cell load their x+1
+// points too, in the same round trip.  Coordinates and the point index advance by 256 cells per step
+// (one row wrap at most on rows of 256 cells or more, a division otherwise).
+__device__ __forceinline__ unsigned tile_cases(const Grid& g, int64_t space_n, int64_t vbase, uint8_t* case_of) {
   const int lane = threadIdx.x & 31;
-  const int64_t sy = g.nx, sz = (int64_t)g.nx * g.ny;
-  const float* p = g.f + (valid ? ((int64_t)k * g.ny + j) * g.nx + i : 0);
-  // the next lane holds cell (i + 1, j, k) unless this is the warp's last lane or the row's last cell;
-  // those lanes load their x+1 points together with the others' loads (no second round trip)
-  const bool own_next = valid && (lane == 31 || i >= g.nx - 2);
-  bool b0 = false, b1 = false, b2 = false, b3 = false, n0 = false, n1 = false, n2 = false, n3 = false;
-  if (valid) {
-    b0 = __ldg(p) >= g.iso_up;
-    b1 = __ldg(p + sy) >= g.iso_up;
-    b2 = __ldg(p + sz) >= g.iso_up;
-    b3 = __ldg(p + sz + sy) >= g.iso_up;
+  const int64_t n = g.ncells();
+  const int cx = g.nx - 1, cy = g.ny - 1;
+  const int64_t sy = g.nx, sz = (int64_t)g.nx * g.ny, szy = sz + sy;
+  const int64_t c0 = vbase + threadIdx.x - g.vbase;  // the thread's first cell in its volume
+  // cells of the volume in this tile, from the thread's first: c0 + 256 s < lim
+  const int64_t lim = (space_n - g.vbase < n ? space_n - g.vbase : n);
+  int i = 0, j = 0, k = 0;
+  if (c0 < lim) {
+    const uint32_t cc = (uint32_t)c0;
+    const uint32_t r = g.div_cx.div(cc);
+    i = (int)(cc - r * (uint32_t)cx);
+    const uint32_t kk = g.div_cy.div(r);
+    j = (int)(r - kk * (uint32_t)cy);
+    k = (int)kk;
   }
-  if (own_next) {
-    n0 = __ldg(p + 1) >= g.iso_up;
-    n1 = __ldg(p + sy + 1) >= g.iso_up;
-    n2 = __ldg(p + sz + 1) >= g.iso_up;
-    n3 = __ldg(p + sz + sy + 1) >= g.iso_up;
+  int64_t pi = ((int64_t)k * g.ny + j) * g.nx + i;  // point (i, j, k)
+  const float iso = g.iso_up;
+  unsigned actbits = 0;
+#pragma unroll
+  for (int s = 0; s < kScanItems; s++) {
+    const bool valid = c0 + (int64_t)s * kScanThreads < lim;
+    if (s > 0 && valid) {
+      if (cx >= kScanThreads) {
+        i += kScanThreads;
+        pi += kScanThreads;
+        if (i >= cx) {  // next row: skip the row's last point
+          i -= cx;
+          pi += 1;
+          if (++j >= cy) {  // next plane: skip the plane's last row
+            j = 0;
+            ++k;
+            pi += g.nx;
+          }
+        }
+      } else {
+        const uint32_t cc = (uint32_t)(c0 + (int64_t)s * kScanThreads);
+        const uint32_t r = g.div_cx.div(cc);
+        i = (int)(cc - r * (uint32_t)cx);
+        const uint32_t kk = g.div_cy.div(r);
+        j = (int)(r - kk * (uint32_t)cy);
+        k = (int)kk;
+        pi = ((int64_t)k * g.ny + j) * g.nx + i;
+      }
+    }
+    const float* p = g.f + pi;
+    const bool own_next = valid && (lane == 31 || i == cx - 1);
+    bool b0 = false, b1 = false, b2 = false, b3 = false;
+    if (valid) {
+      b0 = __ldg(p) >= iso;
+      b1 = __ldg(p + sy) >= iso;
+      b2 = __ldg(p + sz) >= iso;
+      b3 = __ldg(p + szy) >= iso;
+    }
+    unsigned nx_bits = 0;
+    if (own_next) {
+      nx_bits = (unsigned)(__ldg(p + 1) >= iso) << 1 | (unsigned)(__ldg(p + sy + 1) >= iso) << 3 |
+                (unsigned)(__ldg(p + sz + 1) >= iso) << 5 | (unsigned)(__ldg(p + szy + 1) >= iso) << 7;
+    }
+    const unsigned m0 = __ballot_sync(0xffffffffu, b0), m1 = __ballot_sync(0xffffffffu, b1),
+                   m2 = __ballot_sync(0xffffffffu, b2), m3 = __ballot_sync(0xffffffffu, b3);
+    unsigned cs = ((m0 >> lane) & 3u) | ((m1 >> lane) & 3u) << 2 | ((m2 >> lane) & 3u) << 4 | ((m3 >> lane) & 3u) << 6;
+    if (own_next) cs = (cs & 0x55u) | nx_bits;
+    if (!valid) cs = 0;
+    case_of[s * kScanThreads + threadIdx.x] = (uint8_t)cs;
+    actbits |= (unsigned)(cs - 1u < 254u) << s;
   }
-  const unsigned m0 = __ballot_sync(0xffffffffu, b0), m1 = __ballot_sync(0xffffffffu, b1),
-                 m2 = __ballot_sync(0xffffffffu, b2), m3 = __ballot_sync(0xffffffffu, b3);
-  if (!valid) return 0;
-  if (!own_next) {
-    n0 = (m0 >> (lane + 1)) & 1u;
-    n1 = (m1 >> (lane + 1)) & 1u;
-    n2 = (m2 >> (lane + 1)) & 1u;
-    n3 = (m3 >> (lane + 1)) & 1u;
-  }
-  return (unsigned)b0 | (unsigned)n0 << 1 | (unsigned)b1 << 2 | (unsigned)n1 << 3 | (unsigned)b2 << 4 |
-         (unsigned)n2 << 5 | (unsigned)b3 << 6 | (unsigned)n3 << 7;
+  return actbits;
 }
 
 // Tile-wide listing of the cells whose `act` bit is set, in cell order: each warp's ballot masks of

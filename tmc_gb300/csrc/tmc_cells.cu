@@ -458,7 +458,7 @@ __device__ void load_amb_cell(const Grid& g, int i, int j, int k, const float u[
 // (warp_cases) and the listing of the crossed cells in cell order (list_tile).  Pass 2: the records
 // of the listed cells at their slots (owned crossed edges, table triangle counts); ambiguous cells are
 // listed by slot (amb_list, warp-aggregated appends) for the float64 counting pass.
-__global__ void __launch_bounds__(kScanThreads, 4) tmc_classify_kernel(CellSpace space, int64_t tile0, uint32_t* rec,
+__global__ void __launch_bounds__(kScanThreads, 6) tmc_classify_kernel(CellSpace space, int64_t tile0, uint32_t* rec,
                                                                    uint16_t* cellof, CellMask* mask,
                                                                    unsigned long long* tile_sums,
                                                                    unsigned long long* stats, uint32_t* amb_list,
@@ -474,36 +474,7 @@ __global__ void __launch_bounds__(kScanThreads, 4) tmc_classify_kernel(CellSpace
   const int64_t n = g.ncells();
   const int64_t vbase = tile * kScanTile;
   const int lane = threadIdx.x & 31;
-  unsigned actbits = 0;
-  // coordinates of the thread's first cell, then advanced by kScanThreads cells per step (one row
-  // wrap at most when rows hold kScanThreads cells or more, a division otherwise)
-  const int cx = g.nx - 1, cy = g.ny - 1;
-  int i, j, k;
-  tcell_ijk(g, vbase + threadIdx.x - g.vbase, i, j, k);
-#pragma unroll
-  for (int s = 0; s < kScanItems; s++) {
-    const int off = s * kScanThreads + threadIdx.x;
-    const int64_t vc = vbase + off;
-    const int64_t c = vc - g.vbase;  // cell of the volume (beyond its last cell: padding)
-    const bool valid = vc < space.n && c < n;
-    if (s > 0) {
-      if (cx >= kScanThreads) {
-        i += kScanThreads;
-        if (i >= cx) {
-          i -= cx;
-          if (++j >= cy) {
-            j = 0;
-            ++k;
-          }
-        }
-      } else if (valid) {
-        tcell_ijk(g, c, i, j, k);
-      }
-    }
-    const unsigned cs = warp_cases(g, valid, i, j, k);
-    case_of[off] = (uint8_t)cs;
-    actbits |= (unsigned)(cs != 0 && cs != 255) << s;
-  }
+  const unsigned actbits = tile_cases(g, space.n, vbase, case_of);
   const int na = list_tile(actbits, tile, mask, wmask, wpre, act_list, &total);
   unsigned long long local = 0, amb = 0;
   for (int a = threadIdx.x; a < na; a += blockDim.x) {
