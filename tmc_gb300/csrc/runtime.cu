@@ -14,6 +14,7 @@
 
 #include "../../include/tmc_gb300.h"
 #include "common.cuh"
+#include "ctx_access.h"
 #include "dmc.h"
 #include "dmc_mesh.h"
 #include "halfedges.h"
@@ -39,30 +40,11 @@ struct tmc_ctx {
   unsigned long long* d_stats = nullptr;  // 8 counters, reused per call
   void* h_pinned = nullptr;               // small pinned staging area (totals, stats)
   tmc::Prof prof;                         // stage timings (off unless enabled)
-  // pinned host blocks for TMC_OUT_HOST results, reused across calls (size -> block)
-  std::multimap<size_t, void*> pinned_free;
-  std::map<void*, size_t> pinned_size;
-  void* pinned_get(size_t bytes) {
-    // power-of-two size classes (from 4 KiB): varied request sizes still reuse blocks
-    size_t cls = 4096;
-    while (cls < bytes) cls <<= 1;
-    bytes = cls;
-    auto it = pinned_free.lower_bound(bytes);
-    if (it != pinned_free.end() && it->first <= 2 * bytes) {
-      void* p = it->second;
-      pinned_free.erase(it);
-      return p;
-    }
-    void* p = nullptr;
-    if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
-    pinned_size[p] = bytes;
-    return p;
-  }
-  void pinned_put(void* p) {
-    auto it = pinned_size.find(p);
-    if (it == pinned_size.end()) return;
-    pinned_free.emplace(it->second, p);
-  }
+  // pinned host blocks for TMC_OUT_HOST results, reused across calls; shared by the worker contexts
+  // of a request server (tmc::ctx_share_pinned)
+  std::shared_ptr<tmc::PinnedPool> pinned = std::make_shared<tmc::PinnedPool>();
+  void* pinned_get(size_t bytes) { return pinned->get(bytes); }
+  void pinned_put(void* p) { pinned->put(p); }
 };
 
 namespace {
@@ -410,7 +392,7 @@ tmc_status tmc_ctx_destroy(tmc_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->d_stats) cudaFree(ctx->d_stats);
-  for (auto& kv : ctx->pinned_size) cudaFreeHost(kv.first);
+  ctx->pinned.reset();  // the last context using the pool frees its blocks
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   if (ctx->copy_stream) {
     cudaStreamSynchronize(ctx->copy_stream);
@@ -1196,4 +1178,5 @@ int ctx_device(const tmc_ctx* ctx) { return ctx->device; }
 cudaStream_t ctx_stream(const tmc_ctx* ctx) { return ctx->stream; }
 tmc_status ctx_fail(tmc_ctx* ctx, tmc_status s, const char* msg) { return fail(ctx, s, "%s", msg); }
 void ctx_count_launches(tmc_ctx* ctx, int64_t n) { ctx->launches += n; }
+void ctx_share_pinned(tmc_ctx* ctx, tmc_ctx* from) { ctx->pinned = from->pinned; }
 }  // namespace tmc

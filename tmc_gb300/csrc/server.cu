@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "../../include/tmc_gb300.h"
+#include "ctx_access.h"
 
 namespace {
 
@@ -206,6 +207,9 @@ tmc_status tmc_server_create(int device, const tmc_server_opts* opts, tmc_server
       tmc_server_destroy(s);
       return st;
     }
+    // one pool of pinned result blocks for all workers: a request's result block comes from any
+    // earlier request's, whichever worker ran it (no first-use pinning inside a request's latency)
+    if (w > 0) tmc::ctx_share_pinned(W->ctx, s->workers[0]->ctx);
     s->workers.push_back(W);
   }
   for (int w = 0; w < nworkers; w++) s->workers[(size_t)w]->thread = std::thread([s, w] { s->run(w); });
