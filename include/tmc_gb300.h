@@ -17,6 +17,8 @@
  *                          readFromFile<T> / readDataFromFile<T>     cpp_dmc/Volumes.h:47, dmc/UniformGrid.h:431
  *                          p_mc::MarchingCubes::readDataFromFile    cuda_tmc/MarchingCubes.cu:3363
  *   tmc_field_generate     p_mc::UniformGrid::generateVolume         dmc/UniformGrid.cu:177-217
+ *   tmc_field_generate_ex, tmc_*_extract_generated  (no reference counterpart: parameterised fields,
+ *                          generation fused into the extraction)
  *   tmc_mesh_write_obj/off the OBJ / OFF writers                     cpp_dmc/main.cpp:33-87, mc/MarchingCubes.cpp:98-141
  *   tmc_mesh_quality       p_mc::EstimateElementQuality::q           dmc/EstimateElementQuality.cu:39-56
  *   tmc_mesh_valence       p_mc::VertexValence::vertexValence        dmc/VertexValence.cu:79-170
@@ -195,6 +197,31 @@ enum {
   TMC_SURF_STEINER_ROMAN = 9
 };
 tmc_status tmc_field_generate(tmc_ctx* ctx, int32_t surface, int32_t nx, int32_t ny, int32_t nz, tmc_field* out);
+/* Generated fields with parameters (no counterpart in the reference's API: the two field families of
+ * the batched workloads, evaluated in float32 on the same grid):
+ *   TMC_SURF_PERIODIC  sin(kx)cos(ky) + sin(ky)cos(kz) + sin(kz)cos(kx), k = params[0]
+ *   TMC_SURF_BLOBS     sum over `count` (1..16) blobs of exp(-|p - c|^2 / (2 sigma^2)), blob b:
+ *                      params[4b .. 4b+2] = centre, params[4b+3] = sigma
+ * and the ten surfaces above (params unused). */
+enum { TMC_SURF_PERIODIC = 10, TMC_SURF_BLOBS = 11 };
+typedef struct tmc_generator {
+  int32_t surface;     /* TMC_SURF_* */
+  int32_t nx, ny, nz;  /* points on [-1, 1]^3, spacing 2 / (n - 1) in float32 */
+  int32_t count;       /* TMC_SURF_BLOBS: number of blobs */
+  int32_t reserved;
+  double params[64];
+} tmc_generator;
+/* The generator's field written to device memory (the stored path); free with tmc_field_free. */
+tmc_status tmc_field_generate_ex(tmc_ctx* ctx, const tmc_generator* gen, tmc_field* out);
+/* Extraction with the field generation fused into the classification: the classification kernels
+ * evaluate the field instead of reading it (each point once) and keep the values for the passes
+ * that follow, which touch only the crossed cells' neighbourhoods; no generation pass and no field
+ * read.  The meshes equal those of tmc_field_generate_ex followed by tmc_dmc_extract /
+ * tmc_tmc_sharedvertex / tmc_tmc_halfedge (halfedge != 0) on the same field, bit for bit. */
+tmc_status tmc_dmc_extract_generated(tmc_ctx* ctx, const tmc_generator* gen, double iso, uint32_t flags,
+                                     tmc_mesh* out);
+tmc_status tmc_tmc_extract_generated(tmc_ctx* ctx, const tmc_generator* gen, double iso, uint32_t flags,
+                                     int32_t halfedge, tmc_mesh* out);
 /* OBJ output in the reference's layouts: TMC_OBJ_DMC_TRIS / TMC_OBJ_DMC_QUADS as cpp_dmc/main.cpp:33-87
  * (the triangle or the quad file), TMC_OBJ_TMC as mc/MarchingCubes.cpp:98-118 (including its use of
  * the second vertex's index as the third normal index).  OFF output as mc/MarchingCubes.cpp:123-141

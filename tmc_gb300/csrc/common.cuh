@@ -41,6 +41,8 @@ struct Div32 {
   }
 };
 
+struct GenParams;  // generators.cuh
+
 struct Grid {
   const float* f;
   int nx, ny, nz;     // points
@@ -53,6 +55,12 @@ struct Grid {
   double inv2[3];     // 1 / (2 * spacing), for the central-difference gradients
   float inv2f[3];     // the same rounded to float
   Div32 div_cx, div_cy;  // division by nx - 1 and ny - 1 (cell index -> i, j, k); set_divisors()
+  // fused generation (single-volume launches): the classification evaluates the field from `gen` at
+  // the float32 spacing gd instead of reading f, and writes each point once to gen_out (== f), which
+  // the later passes read
+  const GenParams* gen;
+  float* gen_out;
+  float gd[3];
   __host__ void set_divisors() {
     div_cx.init((uint32_t)(nx - 1));
     div_cy.init((uint32_t)(ny - 1));

@@ -47,6 +47,7 @@ __constant__ uint64_t c_case_contour[256] = TMC_CASE_CONTOUR_INIT;
 // slots with their in-tile offsets, and the tile's packed (vertices << 32 | quads) sum.  Listed cells
 // with an ambiguous case (the asymptotic decider, ~1 % of the cells) go by slot to amb_list for
 // dmc_amb_kernel, which runs them densely instead of stalling every warp here on a few lanes.
+template <bool kGen>
 __global__ void __launch_bounds__(kScanThreads, 6) dmc_classify_kernel(CellSpace space, int64_t tile0, uint32_t* rec,
                                                                    uint16_t* cellof, CellMask* mask,
                                                                    unsigned long long* tile_sums,
@@ -64,7 +65,7 @@ __global__ void __launch_bounds__(kScanThreads, 6) dmc_classify_kernel(CellSpace
   const Grid g = space.grid_of_tile(tile);
   const int64_t vbase = tile * kScanTile;  // first cell of the tile in the space
   const int lane = threadIdx.x & 31;
-  const unsigned actbits = tile_cases(g, space.n, vbase, case_of);
+  const unsigned actbits = tile_cases<kGen>(g, space.n, vbase, case_of);
   const int na = list_tile(actbits, tile, mask, wmask, wpre, act_list, &total);
   // pass 2: records of the listed cells
   unsigned long long local = 0, amb = 0, nact = 0;
@@ -848,8 +849,12 @@ int dmc_front_count(const CellSpace& space, DmcScratch& s, cudaStream_t st, Prof
     cudaMemsetAsync(s.amb_n, 0, sizeof(unsigned), st);
     auto classify = [&](int64_t t0, int64_t t1) {
       if (t1 <= t0) return;
-      dmc_classify_kernel<<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(
-          space, t0, s.rec, s.cellof, s.mask, s.tile_sums, s.stats, reinterpret_cast<uint32_t*>(s.qoff), s.amb_n);
+      if (space.one.gen)  // fused generation (single volumes)
+        dmc_classify_kernel<true><<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(
+            space, t0, s.rec, s.cellof, s.mask, s.tile_sums, s.stats, reinterpret_cast<uint32_t*>(s.qoff), s.amb_n);
+      else
+        dmc_classify_kernel<false><<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(
+            space, t0, s.rec, s.cellof, s.mask, s.tile_sums, s.stats, reinterpret_cast<uint32_t*>(s.qoff), s.amb_n);
       k++;
     };
     if (ngates == 0) classify(0, tiles);

@@ -3,6 +3,7 @@
 // common.cuh).
 #pragma once
 #include "common.cuh"
+#include "generators.cuh"
 #include "scan.cuh"
 
 namespace tmc {
@@ -20,6 +21,10 @@ static_assert(kScanTile == 1 << kTileShift, "listed-cell slots assume 2048-cell 
 // holds the next cell of the same row.  The warp's last lane and a row's last cell load their x+1
 // points too, in the same round trip.  Coordinates and the point index advance by 256 cells per step
 // (one row wrap at most on rows of 256 cells or more, a division otherwise).
+// kGen: the field is generated (Grid::gen) instead of read: every lane evaluates its points, and the
+// points whose lower cell it holds (at the upper borders also the border points next to it) are
+// written once to Grid::gen_out for the passes that follow.
+template <bool kGen = false>
 __device__ __forceinline__ unsigned tile_cases(const Grid& g, int64_t space_n, int64_t vbase, uint8_t* case_of) {
   const int lane = threadIdx.x & 31;
   const int64_t n = g.ncells();
@@ -69,16 +74,46 @@ __device__ __forceinline__ unsigned tile_cases(const Grid& g, int64_t space_n, i
     const float* p = g.f + pi;
     const bool own_next = valid && (lane == 31 || i == cx - 1);
     bool b0 = false, b1 = false, b2 = false, b3 = false;
-    if (valid) {
-      b0 = __ldg(p) >= iso;
-      b1 = __ldg(p + sy) >= iso;
-      b2 = __ldg(p + sz) >= iso;
-      b3 = __ldg(p + szy) >= iso;
-    }
     unsigned nx_bits = 0;
-    if (own_next) {
-      nx_bits = (unsigned)(__ldg(p + 1) >= iso) << 1 | (unsigned)(__ldg(p + sy + 1) >= iso) << 3 |
-                (unsigned)(__ldg(p + sz + 1) >= iso) << 5 | (unsigned)(__ldg(p + szy + 1) >= iso) << 7;
+    if (kGen) {
+      if (valid) {
+        const GenParams& P = *g.gen;
+        float* o = g.gen_out + pi;
+        const bool lj = j == cy - 1, lk = k == g.nz - 2;  // the cell touches the upper y / z border
+        const float v0 = generated_at(P, g.gd, i, j, k), v1 = generated_at(P, g.gd, i, j + 1, k),
+                    v2 = generated_at(P, g.gd, i, j, k + 1), v3 = generated_at(P, g.gd, i, j + 1, k + 1);
+        b0 = v0 >= iso;
+        b1 = v1 >= iso;
+        b2 = v2 >= iso;
+        b3 = v3 >= iso;
+        o[0] = v0;
+        if (lj) o[sy] = v1;
+        if (lk) o[sz] = v2;
+        if (lj && lk) o[szy] = v3;
+        if (own_next) {
+          const float w0 = generated_at(P, g.gd, i + 1, j, k), w1 = generated_at(P, g.gd, i + 1, j + 1, k),
+                      w2 = generated_at(P, g.gd, i + 1, j, k + 1), w3 = generated_at(P, g.gd, i + 1, j + 1, k + 1);
+          nx_bits = (unsigned)(w0 >= iso) << 1 | (unsigned)(w1 >= iso) << 3 | (unsigned)(w2 >= iso) << 5 |
+                    (unsigned)(w3 >= iso) << 7;
+          if (i == cx - 1) {  // the row's last cell also writes the row's last points
+            o[1] = w0;
+            if (lj) o[sy + 1] = w1;
+            if (lk) o[sz + 1] = w2;
+            if (lj && lk) o[szy + 1] = w3;
+          }
+        }
+      }
+    } else {
+      if (valid) {
+        b0 = __ldg(p) >= iso;
+        b1 = __ldg(p + sy) >= iso;
+        b2 = __ldg(p + sz) >= iso;
+        b3 = __ldg(p + szy) >= iso;
+      }
+      if (own_next) {
+        nx_bits = (unsigned)(__ldg(p + 1) >= iso) << 1 | (unsigned)(__ldg(p + sy + 1) >= iso) << 3 |
+                  (unsigned)(__ldg(p + sz + 1) >= iso) << 5 | (unsigned)(__ldg(p + szy + 1) >= iso) << 7;
+      }
     }
     const unsigned m0 = __ballot_sync(0xffffffffu, b0), m1 = __ballot_sync(0xffffffffu, b1),
                    m2 = __ballot_sync(0xffffffffu, b2), m3 = __ballot_sync(0xffffffffu, b3);

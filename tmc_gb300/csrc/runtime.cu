@@ -17,6 +17,7 @@
 #include "ctx_access.h"
 #include "dmc.h"
 #include "dmc_mesh.h"
+#include "generators.cuh"
 #include "halfedges.h"
 #include "scan.cuh"
 #include "profiler.h"
@@ -341,6 +342,50 @@ tmc_status finish_mesh(tmc_ctx* ctx, uint32_t flags, tmc_mesh* out, MeshPriv* mp
   return TMC_OK;
 }
 
+// Fused generation: the field buffer comes from the call's pool and the classification writes it
+// (Grid::gen_out) while it evaluates the generator; vol describes the generated grid (no data).
+struct FusedGen {
+  tmc::GenParams params;
+  float d[3];
+};
+
+// The volume of a generator's grid (origin -1, the float32 spacing), checked
+tmc_status gen_volume(tmc_ctx* ctx, const tmc_generator* gen, FusedGen& fg, tmc_volume& vol) {
+  if (!gen || !tmc::gen_params(*gen, fg.params, fg.d))
+    return fail(ctx, TMC_ERR_INVALID_ARG, "invalid generator (surface, grid or parameters)");
+  vol = tmc_volume{};
+  vol.nx = gen->nx;
+  vol.ny = gen->ny;
+  vol.nz = gen->nz;
+  for (int a = 0; a < 3; a++) {
+    vol.origin[a] = -1.0;
+    vol.spacing[a] = (double)fg.d[a];
+  }
+  vol.on_device = 1;
+  const int64_t cells = (int64_t)(vol.nx - 1) * (vol.ny - 1) * (vol.nz - 1);
+  if (cells > (int64_t)1 << 32) return fail(ctx, TMC_ERR_INVALID_ARG, "more than 2^32 cells");
+  return TMC_OK;
+}
+
+// The generated field's buffer (written by the classification) and the grid's generator fields.
+tmc_status fused_field(tmc_ctx* ctx, const tmc_volume* vol, const FusedGen& fg, Allocs& al, const float** field,
+                       tmc::GenParams** dev_params) {
+  float* buf = nullptr;
+  TMC_CUDA(ctx, al.get(&buf, (int64_t)vol->nx * vol->ny * vol->nz));
+  TMC_CUDA(ctx, al.get(dev_params, 1));
+  TMC_CUDA(ctx, cudaMemcpyAsync(*dev_params, &fg.params, sizeof(tmc::GenParams), cudaMemcpyHostToDevice, ctx->stream));
+  *field = buf;
+  return TMC_OK;
+}
+void set_fused(tmc::Grid& g, const FusedGen& fg, tmc::GenParams* dev_params) {
+  g.gen = dev_params;
+  g.gen_out = const_cast<float*>(g.f);
+  for (int a = 0; a < 3; a++) g.gd[a] = fg.d[a];
+}
+
+tmc_status dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t flags, tmc_mesh* out,
+                       const FusedGen* fg);
+
 }  // namespace
 
 // ============================================================================================
@@ -494,9 +539,45 @@ tmc_status tmc_mesh_free(tmc_ctx* ctx, tmc_mesh* mesh) {
 }
 
 tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t flags, tmc_mesh* out) {
+  return dmc_extract(ctx, vol, iso, flags, out, nullptr);
+}
+
+tmc_status tmc_dmc_extract_generated(tmc_ctx* ctx, const tmc_generator* gen, double iso, uint32_t flags,
+                                                tmc_mesh* out) {
   if (!ctx || !out) return fail(ctx, TMC_ERR_INVALID_ARG, "context or output is NULL");
   mesh_reset(out);
-  tmc_status s = check_volume(ctx, vol);
+  FusedGen fg;
+  tmc_volume vol;
+  if (tmc_status s = gen_volume(ctx, gen, fg, vol)) return s;
+  return dmc_extract(ctx, &vol, iso, flags, out, &fg);
+}
+
+// colorFaces + vertexValence as a stage of their own (cpp_dmc/DualMarchingCubes.cpp:714-871): the
+// P3X3Y colour pass of tmc_dmc_extract runs the same code on its front-end mesh.
+tmc_status tmc_dmc_color_valence(tmc_ctx* ctx, int64_t nr_v, int64_t nr_q, const int32_t* quads, uint8_t* colors,
+                                 int32_t* valence) {
+  if (!ctx) return TMC_ERR_INVALID_ARG;
+  if (nr_v < 0 || nr_q < 0 || nr_v > INT32_MAX || 4 * nr_q > INT32_MAX)
+    return fail(ctx, TMC_ERR_INVALID_ARG, "vertex or quad count out of range");
+  if ((nr_q > 0 && (!quads || !colors)) || (nr_v > 0 && !valence))
+    return fail(ctx, TMC_ERR_INVALID_ARG, "quads, colors or valence is NULL");
+  TMC_CUDA(ctx, cudaSetDevice(ctx->device));
+  const tmc::DmcPostStatus ps = tmc::dmc_color_valence(quads, nr_q, nr_v, colors, valence, ctx->sms, ctx->stream);
+  ctx->launches += ps.launches;
+  TMC_CUDA(ctx, ps.err);
+  TMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return TMC_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+tmc_status dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t flags, tmc_mesh* out,
+                       const FusedGen* fg) {
+  if (!ctx || !out) return fail(ctx, TMC_ERR_INVALID_ARG, "context or output is NULL");
+  mesh_reset(out);
+  tmc_status s = fg ? TMC_OK : check_volume(ctx, vol);
   if (s) return s;
   if (!std::isfinite(iso)) return fail(ctx, TMC_ERR_INVALID_ARG, "isovalue must be finite");
   if (flags & TMC_DMC_SIMPLIFY) flags |= TMC_DMC_P3X3Y_COLOR | TMC_DMC_P3X3Y_ISOLATED | TMC_DMC_P3333;
@@ -508,8 +589,11 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   Allocs al(ctx);
   const float* field = nullptr;
   std::vector<tmc::TileGate> gates;
-  if ((s = field_slabs(ctx, vol, al, &field, gates))) return s;
+  tmc::GenParams* dev_params = nullptr;
+  if ((s = fg ? fused_field(ctx, vol, *fg, al, &field, &dev_params) : field_slabs(ctx, vol, al, &field, gates)))
+    return s;
   tmc::Grid g = make_grid(vol, field, iso);
+  if (fg) set_fused(g, *fg, dev_params);
   g.flags = ((flags & TMC_GRAD_FLIP) ? tmc::kGridFlip : 0) | (simplify ? tmc::kGridNormal64 : 0);
   const tmc::CellSpace space = tmc::single_space(g);
   const int64_t ncell = g.ncells();
@@ -652,32 +736,12 @@ tmc_status tmc_dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint
   return finish_mesh(ctx, flags, out, mp, &early);
 }
 
-// colorFaces + vertexValence as a stage of their own (cpp_dmc/DualMarchingCubes.cpp:714-871): the
-// P3X3Y colour pass of tmc_dmc_extract runs the same code on its front-end mesh.
-tmc_status tmc_dmc_color_valence(tmc_ctx* ctx, int64_t nr_v, int64_t nr_q, const int32_t* quads, uint8_t* colors,
-                                 int32_t* valence) {
-  if (!ctx) return TMC_ERR_INVALID_ARG;
-  if (nr_v < 0 || nr_q < 0 || nr_v > INT32_MAX || 4 * nr_q > INT32_MAX)
-    return fail(ctx, TMC_ERR_INVALID_ARG, "vertex or quad count out of range");
-  if ((nr_q > 0 && (!quads || !colors)) || (nr_v > 0 && !valence))
-    return fail(ctx, TMC_ERR_INVALID_ARG, "quads, colors or valence is NULL");
-  TMC_CUDA(ctx, cudaSetDevice(ctx->device));
-  const tmc::DmcPostStatus ps = tmc::dmc_color_valence(quads, nr_q, nr_v, colors, valence, ctx->sms, ctx->stream);
-  ctx->launches += ps.launches;
-  TMC_CUDA(ctx, ps.err);
-  TMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  return TMC_OK;
-}
-
-}  // extern "C"
-
-namespace {
-
 // TMC extraction driver shared by the shared-vertex and halfedge entry points.
-tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t flags, tmc_mesh* out, bool halfedge) {
+tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t flags, tmc_mesh* out, bool halfedge,
+                       const FusedGen* fg = nullptr) {
   if (!ctx || !out) return fail(ctx, TMC_ERR_INVALID_ARG, "context or output is NULL");
   mesh_reset(out);
-  tmc_status s = check_volume(ctx, vol);
+  tmc_status s = fg ? TMC_OK : check_volume(ctx, vol);
   if (s) return s;
   if (!std::isfinite(iso)) return fail(ctx, TMC_ERR_INVALID_ARG, "isovalue must be finite");
   if (flags & (TMC_DMC_SIMPLIFY | TMC_DMC_P3X3Y_COLOR | TMC_DMC_P3X3Y_ISOLATED | TMC_DMC_P3333 | TMC_OUT_LOCAL))
@@ -688,8 +752,11 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   Allocs al(ctx);
   const float* field = nullptr;
   std::vector<tmc::TileGate> gates;
-  if ((s = field_slabs(ctx, vol, al, &field, gates))) return s;
+  tmc::GenParams* dev_params = nullptr;
+  if ((s = fg ? fused_field(ctx, vol, *fg, al, &field, &dev_params) : field_slabs(ctx, vol, al, &field, gates)))
+    return s;
   tmc::Grid g = make_grid(vol, field, iso);
+  if (fg) set_fused(g, *fg, dev_params);
   g.flags = (flags & TMC_OUT_POS_F64) ? tmc::kGridPos64 : 0;
   const int64_t ncell = g.ncells();
   tmc::TmcScratch sc{};
@@ -1081,6 +1148,15 @@ tmc_status tmc_tmc_sharedvertex(tmc_ctx* ctx, const tmc_volume* vol, double iso,
 }
 tmc_status tmc_tmc_halfedge(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t flags, tmc_mesh* out) {
   return tmc_extract(ctx, vol, iso, flags, out, true);
+}
+tmc_status tmc_tmc_extract_generated(tmc_ctx* ctx, const tmc_generator* gen, double iso, uint32_t flags,
+                                     int32_t halfedge, tmc_mesh* out) {
+  if (!ctx || !out) return fail(ctx, TMC_ERR_INVALID_ARG, "context or output is NULL");
+  mesh_reset(out);
+  FusedGen fg;
+  tmc_volume vol;
+  if (tmc_status s = gen_volume(ctx, gen, fg, vol)) return s;
+  return tmc_extract(ctx, &vol, iso, flags, out, halfedge != 0, &fg);
 }
 tmc_status tmc_batch_extract(tmc_ctx* ctx, int32_t n, const tmc_request* reqs, tmc_mesh* outs) {
   if (!ctx) return TMC_ERR_INVALID_ARG;

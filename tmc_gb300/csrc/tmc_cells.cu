@@ -458,6 +458,7 @@ __device__ void load_amb_cell(const Grid& g, int i, int j, int k, const float u[
 // (warp_cases) and the listing of the crossed cells in cell order (list_tile).  Pass 2: the records
 // of the listed cells at their slots (owned crossed edges, table triangle counts); ambiguous cells are
 // listed by slot (amb_list, warp-aggregated appends) for the float64 counting pass.
+template <bool kGen>
 __global__ void __launch_bounds__(kScanThreads, 6) tmc_classify_kernel(CellSpace space, int64_t tile0, uint32_t* rec,
                                                                    uint16_t* cellof, CellMask* mask,
                                                                    unsigned long long* tile_sums,
@@ -474,7 +475,7 @@ __global__ void __launch_bounds__(kScanThreads, 6) tmc_classify_kernel(CellSpace
   const int64_t n = g.ncells();
   const int64_t vbase = tile * kScanTile;
   const int lane = threadIdx.x & 31;
-  const unsigned actbits = tile_cases(g, space.n, vbase, case_of);
+  const unsigned actbits = tile_cases<kGen>(g, space.n, vbase, case_of);
   const int na = list_tile(actbits, tile, mask, wmask, wpre, act_list, &total);
   unsigned long long local = 0, amb = 0;
   for (int a = threadIdx.x; a < na; a += blockDim.x) {
@@ -830,8 +831,12 @@ int tmc_count(const CellSpace& space, TmcScratch& s, int sms, cudaStream_t st, P
     cudaMemsetAsync(s.amb_n, 0, sizeof(unsigned), st);
     auto classify = [&](int64_t t0, int64_t t1) {
       if (t1 <= t0) return;
-      tmc_classify_kernel<<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(space, t0, s.rec, s.cellof, s.mask,
-                                                                        s.tile_sums, s.stats, amb_cells, s.amb_n);
+      if (space.one.gen)  // fused generation (single volumes)
+        tmc_classify_kernel<true><<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(
+            space, t0, s.rec, s.cellof, s.mask, s.tile_sums, s.stats, amb_cells, s.amb_n);
+      else
+        tmc_classify_kernel<false><<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(
+            space, t0, s.rec, s.cellof, s.mask, s.tile_sums, s.stats, amb_cells, s.amb_n);
       k++;
     };
     if (ngates == 0) classify(0, tiles);

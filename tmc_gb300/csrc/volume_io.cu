@@ -35,6 +35,7 @@
 #include "../../include/tmc_gb300.h"
 #include "common.cuh"
 #include "ctx_access.h"
+#include "generators.cuh"
 
 namespace tmc {
 namespace {
@@ -345,68 +346,48 @@ tmc_status tmc_mesh_write_off(tmc_ctx* ctx, const tmc_mesh* mesh, const char* pa
 namespace tmc {
 namespace {
 
-__device__ __forceinline__ float sqf(float x) { return x * x; }
-// torus around the z axis (horizontal) or the y axis (vertical): ring radius R, tube radius r
-__device__ __forceinline__ float torus_field(float x, float y, float z, float cx, float cy, float cz, bool vertical) {
-  const float R2 = sqf(0.3f), r2 = sqf(0.15f);
-  const float X = sqf(x - cx), Y = sqf(y - cy), Z = sqf(z - cz);
-  return sqf(X + Y + Z + R2 - r2) - 4 * R2 * (X + (vertical ? Z : Y));
-}
-
-__device__ float surface_value(int sc, float x, float y, float z) {
-  const float pi = 3.14159265358979323846f;
-  switch (sc) {
-    case TMC_SURF_SPHERE:
-      return x * x + y * y + z * z - 0.16f;
-    case TMC_SURF_TORUS:
-      return torus_field(x, y, z, 0, 0, 0, false);
-    case TMC_SURF_TWO_HOLED_TORUS:
-      return fminf(torus_field(x, y, z, -0.38f, 0, 0, false), torus_field(x, y, z, 0.2f, 0.38f, 0, false));
-    case TMC_SURF_FOUR_HOLED_TORUS: {
-      const float a = fminf(torus_field(x, y, z, -0.38f, 0, 0, false), torus_field(x, y, z, 0.38f, 0, 0, false));
-      const float b = fminf(torus_field(x, y, z, 0, 0, -0.38f, true), torus_field(x, y, z, 0, 0, 0.38f, true));
-      return fminf(a, b);
-    }
-    case TMC_SURF_IWP: {
-      const float s = 5.01f * pi;
-      const float cx = cosf(s * (x + 1)), cy = cosf(s * (y + 1)), cz = cosf(s * (z + 1));
-      return cx * cy + cy * cz + cz * cx - cx * cy * cz;
-    }
-    case TMC_SURF_PW_HYBRID: {
-      const float s = 1.01f * pi;
-      const float cx = cosf(s * (x + 1)), cy = cosf(s * (y + 1)), cz = cosf(s * (z + 1));
-      return 4.0f * (cx * cy + cy * cz + cz * cx) - 3 * cx * cy * cz + 0.8f;
-    }
-    case TMC_SURF_NEOVIUS: {
-      const float cx = cosf(pi * (x + 1)), cy = cosf(pi * (y + 1)), cz = cosf(pi * (z + 1));
-      return 3 * (cx + cy + cz) + 4 * cx * cy * cz;
-    }
-    case TMC_SURF_GOURSAT: {
-      const float r2 = x * x + y * y + z * z;
-      return sqf(sqf(x)) + sqf(sqf(y)) + sqf(sqf(z)) - r2 + 0.5f;
-    }
-    case TMC_SURF_STEINER_ROMAN: {
-      const float X = 1.5f * x, Y = 1.5f * y, Z = 1.5f * z;
-      return sqf(X * X + Y * Y + Z * Z - 1.0f) - (sqf(Z - 1) - 2.0f * X * X) * (sqf(Z + 1) - 2 * Y * Y);
-    }
-    default: {  // TMC_SURF_GENUS_TWO: the domain mapped to [-2, 2]^3
-      const float X = 4.0f * ((x + 1.0f) / 2.0f) - 2.0f;
-      const float Y = 4.0f * ((y + 1.0f) / 2.0f) - 2.0f;
-      const float Z = 4.0f * ((z + 1.0f) / 2.0f) - 2.0f;
-      float t = 2 * Y * (Y * Y - 3 * X * X) * (1 - Z * Z);
-      t += (X * X + Y * Y) * (X * X + Y * Y);
-      t -= (9 * Z * Z - 1) * (1 - Z * Z);
-      return t;
-    }
-  }
-}
-
-__global__ void generate_kernel(int sc, int nx, int ny, int nz, float dx, float dy, float dz, float* out) {
+__global__ void generate_kernel(GenParams P, int nx, int ny, int nz, float dx, float dy, float dz, float* out) {
   const int64_t n = (int64_t)nx * ny * nz;
+  const float d[3] = {dx, dy, dz};
   for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(g % nx), j = (int)((g / nx) % ny), k = (int)(g / ((int64_t)nx * ny));
-    out[g] = surface_value(sc, -1.0f + i * dx, -1.0f + j * dy, -1.0f + k * dz);
+    out[g] = generated_at(P, d, i, j, k);
   }
+}
+
+// The generator's field into new device memory (the stored path of both generation entry points).
+tmc_status generate_field(tmc_ctx* ctx, const tmc_generator& gen, tmc_field* out) {
+  GenParams P;
+  float d[3];
+  if (!gen_params(gen, P, d)) return ctx_fail(ctx, TMC_ERR_INVALID_ARG, "invalid generator (surface, grid or parameters)");
+  const int64_t n = (int64_t)gen.nx * gen.ny * gen.nz;
+  float* field = nullptr;
+  cudaError_t e = cudaSetDevice(ctx_device(ctx));
+  if (e == cudaSuccess) e = cudaMalloc(&field, (size_t)n * sizeof(float));
+  if (e == cudaSuccess) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx_device(ctx));
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)sms * 16));
+    generate_kernel<<<(unsigned)blocks, 256, 0, ctx_stream(ctx)>>>(P, gen.nx, gen.ny, gen.nz, d[0], d[1], d[2], field);
+    e = cudaGetLastError();
+    ctx_count_launches(ctx, 1);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx_stream(ctx));
+  if (e != cudaSuccess) {
+    if (field) cudaFree(field);
+    return ctx_fail(ctx, TMC_ERR_CUDA, cudaGetErrorString(e));
+  }
+  out->vol.nx = gen.nx;
+  out->vol.ny = gen.ny;
+  out->vol.nz = gen.nz;
+  for (int a = 0; a < 3; a++) {
+    out->vol.origin[a] = -1.0;
+    out->vol.spacing[a] = (double)d[a];
+  }
+  out->vol.data = field;
+  out->vol.on_device = 1;
+  out->priv = field;
+  return TMC_OK;
 }
 
 }  // namespace
@@ -419,34 +400,16 @@ extern "C" tmc_status tmc_field_generate(tmc_ctx* ctx, int32_t surface, int32_t 
   if (surface < TMC_SURF_SPHERE || surface > TMC_SURF_STEINER_ROMAN)
     return ctx_fail(ctx, TMC_ERR_INVALID_ARG, "unknown surface");
   if (nx < 2 || ny < 2 || nz < 2) return ctx_fail(ctx, TMC_ERR_INVALID_ARG, "at least 2 points per axis");
-  const int64_t n = (int64_t)nx * ny * nz;
-  // the reference's spacing, in float32: (xmax - xmin) / (n - 1.0f)
-  const float d[3] = {2.0f / (nx - 1.0f), 2.0f / (ny - 1.0f), 2.0f / (nz - 1.0f)};
-  float* field = nullptr;
-  cudaError_t e = cudaSetDevice(ctx_device(ctx));
-  if (e == cudaSuccess) e = cudaMalloc(&field, (size_t)n * sizeof(float));
-  if (e == cudaSuccess) {
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx_device(ctx));
-    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)sms * 16));
-    generate_kernel<<<(unsigned)blocks, 256, 0, ctx_stream(ctx)>>>(surface, nx, ny, nz, d[0], d[1], d[2], field);
-    e = cudaGetLastError();
-    ctx_count_launches(ctx, 1);
-  }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx_stream(ctx));
-  if (e != cudaSuccess) {
-    if (field) cudaFree(field);
-    return ctx_fail(ctx, TMC_ERR_CUDA, cudaGetErrorString(e));
-  }
-  out->vol.nx = nx;
-  out->vol.ny = ny;
-  out->vol.nz = nz;
-  for (int a = 0; a < 3; a++) {
-    out->vol.origin[a] = -1.0;
-    out->vol.spacing[a] = (double)d[a];
-  }
-  out->vol.data = field;
-  out->vol.on_device = 1;
-  out->priv = field;
-  return TMC_OK;
+  tmc_generator gen{};
+  gen.surface = surface;
+  gen.nx = nx;
+  gen.ny = ny;
+  gen.nz = nz;
+  return tmc::generate_field(ctx, gen, out);
+}
+
+extern "C" tmc_status tmc_field_generate_ex(tmc_ctx* ctx, const tmc_generator* gen, tmc_field* out) {
+  if (!ctx || !out || !gen) return TMC_ERR_INVALID_ARG;
+  std::memset(out, 0, sizeof(*out));
+  return tmc::generate_field(ctx, *gen, out);
 }

@@ -44,7 +44,8 @@ EXPORTS = ["tmc_ctx_create", "tmc_ctx_destroy", "tmc_last_error", "tmc_ctx_strea
            "tmc_server_submit", "tmc_server_poll", "tmc_server_wait", "tmc_server_release", "tmc_server_last_error",
            "tmc_server_stats", "tmc_ctx_set_tuning", "tmc_ctx_get_tuning", "tmc_ctx_autotune",
            "tmc_volume_file_info", "tmc_field_load", "tmc_field_free", "tmc_mesh_write_obj", "tmc_mesh_write_off",
-           "tmc_mesh_quality", "tmc_mesh_valence", "tmc_mesh_check", "tmc_field_generate", "tmc_dmc_color_valence"]
+           "tmc_mesh_quality", "tmc_mesh_valence", "tmc_mesh_check", "tmc_field_generate", "tmc_dmc_color_valence",
+           "tmc_field_generate_ex", "tmc_dmc_extract_generated", "tmc_tmc_extract_generated"]
 
 SURFACES = ("sphere", "torus", "two_holed_torus", "four_holed_torus", "genus_two", "iwp", "pw_hybrid", "neovius",
             "goursat", "steiner_roman")
@@ -95,6 +96,27 @@ class Field(ctypes.Structure):
     _fields_ = [("vol", Volume), ("priv", ctypes.c_void_p)]
 
 
+SURF_PERIODIC = 10
+SURF_BLOBS = 11
+
+
+class Generator(ctypes.Structure):
+    _fields_ = [("surface", ctypes.c_int32), ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+                ("count", ctypes.c_int32), ("reserved", ctypes.c_int32), ("params", ctypes.c_double * 64)]
+
+
+def make_generator(surface: int, dims, params=(), count: int = 0) -> Generator:
+    """A tmc_generator: surface id (SURFACES index, SURF_PERIODIC or SURF_BLOBS), (nx, ny, nz),
+    parameters (periodic: (k,); blobs: (cx, cy, cz, sigma) per blob)."""
+    g = Generator()
+    g.surface = int(surface)
+    g.nx, g.ny, g.nz = (int(d) for d in dims)
+    g.count = int(count)
+    for i, x in enumerate(params):
+        g.params[i] = float(x)
+    return g
+
+
 class Request(ctypes.Structure):
     _fields_ = [("vol", Volume), ("iso", ctypes.c_double), ("algo", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
 
@@ -138,6 +160,11 @@ def load(path: str = LIB_PATH):
     lib.tmc_dmc_color_valence.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_void_p]
     lib.tmc_dmc_color_valence.restype = ctypes.c_int
+    lib.tmc_field_generate_ex.argtypes = [ctypes.c_void_p, ctypes.POINTER(Generator), ctypes.POINTER(Field)]
+    lib.tmc_dmc_extract_generated.argtypes = [ctypes.c_void_p, ctypes.POINTER(Generator), ctypes.c_double,
+                                              ctypes.c_uint32, ctypes.POINTER(Mesh)]
+    lib.tmc_tmc_extract_generated.argtypes = [ctypes.c_void_p, ctypes.POINTER(Generator), ctypes.c_double,
+                                              ctypes.c_uint32, ctypes.c_int32, ctypes.POINTER(Mesh)]
     lib.tmc_server_create.argtypes = [ctypes.c_int, ctypes.POINTER(ServerOpts), ctypes.POINTER(ctypes.c_void_p)]
     lib.tmc_server_destroy.argtypes = [ctypes.c_void_p]
     lib.tmc_server_submit.argtypes = [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_int64)]
@@ -377,6 +404,26 @@ class Context:
         f = Field()
         self._check(self.lib.tmc_field_generate(self.h, int(surface), nx, ny, nz, ctypes.byref(f)))
         return f
+
+    def field_generate_ex(self, gen: Generator) -> Field:
+        """tmc_field_generate_ex: a parameterised generated field written to device memory."""
+        f = Field()
+        self._check(self.lib.tmc_field_generate_ex(self.h, ctypes.byref(gen), ctypes.byref(f)))
+        return f
+
+    def dmc_generated_raw(self, gen: Generator, iso: float, flags: int) -> Mesh:
+        """tmc_dmc_extract_generated: DMC with the field generation fused into the classification."""
+        m = Mesh()
+        self._check(self.lib.tmc_dmc_extract_generated(self.h, ctypes.byref(gen), float(iso), int(flags),
+                                                       ctypes.byref(m)))
+        return m
+
+    def tmc_generated_raw(self, gen: Generator, iso: float, flags: int, halfedge: bool = False) -> Mesh:
+        """tmc_tmc_extract_generated: TMC with the field generation fused into the classification."""
+        m = Mesh()
+        self._check(self.lib.tmc_tmc_extract_generated(self.h, ctypes.byref(gen), float(iso), int(flags),
+                                                       1 if halfedge else 0, ctypes.byref(m)))
+        return m
 
     def field_free(self, f: Field):
         self._check(self.lib.tmc_field_free(self.h, ctypes.byref(f)))
