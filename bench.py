@@ -12,6 +12,7 @@ larger than L2, so no L2 flush is needed between steps.
     python bench.py --workload precision      # 1024^3 seeded saddles: topology vs the oracle, position error
     python bench.py --workload serve          # Poisson request stream: server vs one call per request
     python bench.py --workload plain64        # the 64^3 Gaussian-blob plain DMC call (latency-bound)
+    python bench.py --workload fused          # generated 512^3 fields: stored vs fused generation
 
 Prints one JSON line.  `value` is device-resident throughput (field already in HBM); `e2e` is the
 same metric through the C ABI with host buffers (field copied in, mesh copied out every step).
@@ -50,7 +51,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--grid", type=int, default=N, help="points per axis of the noise field (profiling cases)")
-    p.add_argument("--workload", default="single", choices=["single", "batch", "precision", "serve", "plain64"],
+    p.add_argument("--workload", default="single", choices=["single", "batch", "precision", "serve", "plain64", "fused"],
                    help="single: the 512^3 volume (TMC + DMC); batch: 256 uneven volumes, DMC; "
                         "precision: 1024^3 periodic field with seeded near-singular saddles")
     p.add_argument("--volumes", type=int, default=256, help="volumes of the batch workload")
@@ -861,6 +862,96 @@ def run_plain64(args, rank, world, local):
     return out if rank == 0 else None
 
 
+# ------------------------------------------------------------------------------------------------
+# fused generation: the field evaluated inside the classification instead of generated and read
+# ------------------------------------------------------------------------------------------------
+def run_fused(args, rank, world, local, steps=None, warmup=None):
+    """Generated 512^3 fields (the periodic field with k = 6 pi, isovalue 0, and the reference's sphere):
+    per step one DMC (shared-vertex quads) and one TMC (shared-vertex triangles) extraction, either
+    stored (tmc_field_generate_ex writes the field, then the extractions read it) or fused
+    (tmc_*_extract_generated: the classification evaluates the field).  The fused classification's
+    ALU roofline is its rate of field evaluations against the rate of the standalone generation
+    kernel, which does nothing but evaluate and store (one evaluation per point)."""
+    import torch
+
+    from tmc_gb300 import native
+    try:
+        native.load()
+    except RuntimeError:
+        from tmc_gb300 import build
+        build.build()
+    torch.cuda.set_device(local)
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
+    n = args.grid
+    ctx = native.Context(local)
+    cells = (n - 1) ** 3
+    gens = {"periodic_k6pi": (native.make_generator(native.SURF_PERIODIC, (n, n, n), (6 * math.pi,)), 0.0),
+            "sphere": (native.make_generator(0, (n, n, n)), 0.0)}
+    results = {}
+    for name, (gen, iso) in gens.items():
+        def stored():
+            f = ctx.field_generate_ex(gen)
+            ctx.free(ctx.dmc_raw(f.vol, iso, 0))
+            ctx.free(ctx.tmc_raw(f.vol, iso, 0))
+            ctx.field_free(f)
+
+        def fused():
+            ctx.free(ctx.dmc_generated_raw(gen, iso, 0))
+            ctx.free(ctx.tmc_generated_raw(gen, iso, 0))
+
+        def generate_only():
+            ctx.field_free(ctx.field_generate_ex(gen))
+
+        def timed(fn, k):
+            for _ in range(warmup):
+                fn()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(k):
+                fn()
+            ctx.synchronize()
+            return (time.perf_counter() - t0) / k * 1e3
+
+        with ClockSampler(local) as clk:
+            ms_stored = timed(stored, steps)
+            ms_fused = timed(fused, steps)
+            ms_gen = timed(generate_only, steps)
+        # the fused classification alone (stage timing on the context stream)
+        ctx.set_profiling(True)
+        ctx.free(ctx.dmc_generated_raw(gen, iso, 0))
+        ctx.free(ctx.tmc_generated_raw(gen, iso, 0))
+        prof = ctx.profile()
+        ctx.set_profiling(False)
+        # evaluations of the fused classification: four corner rows per cell, four more on the lanes
+        # that load their x+1 points themselves (a warp's last lane and a row's last cell)
+        evals = 4 * cells * (1 + 1 / 32 + 1 / (n - 1))
+        gen_rate = n ** 3 / (ms_gen * 1e-3)
+        cls = {}
+        for st in ("dmc_classify", "tmc_classify"):
+            if st in prof:
+                ms = prof[st][0] / max(prof[st][1], 1)
+                rate = evals / (ms * 1e-3)
+                cls[st] = {"ms": round(ms, 4), "evals_per_s": round(rate / 1e9, 2),
+                           "frac_of_generation_rate": round(rate / gen_rate, 3)}
+        results[name] = {
+            "stored_ms_per_step": round(ms_stored, 3), "fused_ms_per_step": round(ms_fused, 3),
+            "stored_gcells_s": round(cells / (ms_stored * 1e-3) / 1e9, 4),
+            "fused_gcells_s": round(cells / (ms_fused * 1e-3) / 1e9, 4),
+            "fused_over_stored": round(ms_stored / ms_fused, 3),
+            "generation_call_ms": round(ms_gen, 3), "generation_gevals_s": round(gen_rate / 1e9, 2),
+            "fused_classify": cls, "clocks": clk.summary()}
+    ctx.close()
+    return {"workload": f"generated {n}^3 fields, isovalue 0: DMC shared-vertex + TMC shared-vertex per step; "
+                        "stored = generate the field then extract, fused = the classification evaluates the field",
+            "steps": steps, "warmup": warmup, "fields": results,
+            "roofline": "ALU: the fused classification's field evaluations per second against the generation "
+                        "kernel's (one evaluation and one 4-byte store per point; for the periodic field its "
+                        "six float32 sin/cos bound it, for the sphere the store)",
+            "note": "timed on the host clock with a synchronisation per step (the stored path allocates and frees "
+                    "its field each step)"}
+
+
 def headline_extras(args, rank, world, local):
     """The batched and served workloads, measured beside the default one so that one bench line
     carries the whole headline metric: `batch` (256 uneven volumes in one batched call against 256
@@ -883,6 +974,8 @@ def headline_extras(args, rank, world, local):
     sargs = argparse.Namespace(**vars(args))
     sargs.requests, sargs.rates = 256, "0.5,1.5"
     sv = run_serve(sargs, rank, world, local)
+    fargs = argparse.Namespace(**vars(args))
+    extras["fused_generation"] = run_fused(fargs, rank, world, local, steps=5, warmup=3)
     extras["serve"] = {"rates": sv["rates"], "plain_capacity_req_s": sv["config"]["plain_capacity_req_s"],
                        "requests_per_rate": sargs.requests, "workload": sv["config"]["workload"],
                        "server_stats": sv["server_stats"], "clocks": sv["clocks"]}
@@ -907,6 +1000,8 @@ def main():
         out = run_serve(args, rank, world, local)
     elif args.workload == "plain64":
         out = run_plain64(args, rank, world, local)
+    elif args.workload == "fused":
+        out = run_fused(args, rank, world, local)
     else:
         out = run_ours(args, rank, world, local)
     if out is not None and rank == 0:
