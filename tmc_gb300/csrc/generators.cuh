@@ -25,7 +25,53 @@ struct GenParams {
   float k;               // TMC_SURF_PERIODIC: wave number
   float c[kMaxBlobs][3];  // blob centres
   float inv2s2[kMaxBlobs];  // 1 / (2 sigma^2)
+  // fused path, separable surfaces (axis_separable): per-axis terms of every grid index, built by
+  // axis_terms (so the values are those the stored path computes per point); null otherwise
+  const float2* tab[3];
 };
+
+// The surfaces whose transcendental parts depend on one coordinate each: the periodic field
+// (sin and cos of k x) and the reference's IWP, P-W hybrid and Neovius surfaces (cos of s (x + 1)).
+__host__ __device__ __forceinline__ bool axis_separable(int surface) {
+  return surface == TMC_SURF_PERIODIC || surface == TMC_SURF_IWP || surface == TMC_SURF_PW_HYBRID ||
+         surface == TMC_SURF_NEOVIUS;
+}
+
+// The per-axis terms of a separable surface at coordinate x: (sin kx, cos kx) for the periodic field,
+// (cos s(x + 1), 0) for the cosine surfaces.
+__device__ __forceinline__ float2 axis_terms(const GenParams& P, float x) {
+  const float pi = 3.14159265358979323846f;
+  switch (P.surface) {
+    case TMC_SURF_PERIODIC:
+      return make_float2(sinf(P.k * x), cosf(P.k * x));
+    case TMC_SURF_IWP:
+      return make_float2(cosf(5.01f * pi * (x + 1)), 0.0f);
+    case TMC_SURF_PW_HYBRID:
+      return make_float2(cosf(1.01f * pi * (x + 1)), 0.0f);
+    default:  // TMC_SURF_NEOVIUS
+      return make_float2(cosf(pi * (x + 1)), 0.0f);
+  }
+}
+
+// A separable surface from its three per-axis terms
+__device__ __forceinline__ float combine_terms(int surface, float2 X, float2 Y, float2 Z) {
+  switch (surface) {
+    case TMC_SURF_PERIODIC:  // sin(kx)cos(ky) + sin(ky)cos(kz) + sin(kz)cos(kx)
+      return X.x * Y.y + Y.x * Z.y + Z.x * X.y;
+    case TMC_SURF_IWP: {
+      const float cx = X.x, cy = Y.x, cz = Z.x;
+      return cx * cy + cy * cz + cz * cx - cx * cy * cz;
+    }
+    case TMC_SURF_PW_HYBRID: {
+      const float cx = X.x, cy = Y.x, cz = Z.x;
+      return 4.0f * (cx * cy + cy * cz + cz * cx) - 3 * cx * cy * cz + 0.8f;
+    }
+    default: {  // TMC_SURF_NEOVIUS
+      const float cx = X.x, cy = Y.x, cz = Z.x;
+      return 3 * (cx + cy + cz) + 4 * cx * cy * cz;
+    }
+  }
+}
 
 __device__ __forceinline__ float gsq(float x) { return x * x; }
 // torus around the z axis (horizontal) or the y axis (vertical): ring radius R, tube radius r
@@ -49,20 +95,11 @@ static __device__ __noinline__ float surface_value(const GenParams& P, float x, 
       const float b = fminf(torus_field(x, y, z, 0, 0, -0.38f, true), torus_field(x, y, z, 0, 0, 0.38f, true));
       return fminf(a, b);
     }
-    case TMC_SURF_IWP: {
-      const float s = 5.01f * pi;
-      const float cx = cosf(s * (x + 1)), cy = cosf(s * (y + 1)), cz = cosf(s * (z + 1));
-      return cx * cy + cy * cz + cz * cx - cx * cy * cz;
-    }
-    case TMC_SURF_PW_HYBRID: {
-      const float s = 1.01f * pi;
-      const float cx = cosf(s * (x + 1)), cy = cosf(s * (y + 1)), cz = cosf(s * (z + 1));
-      return 4.0f * (cx * cy + cy * cz + cz * cx) - 3 * cx * cy * cz + 0.8f;
-    }
-    case TMC_SURF_NEOVIUS: {
-      const float cx = cosf(pi * (x + 1)), cy = cosf(pi * (y + 1)), cz = cosf(pi * (z + 1));
-      return 3 * (cx + cy + cz) + 4 * cx * cy * cz;
-    }
+    case TMC_SURF_IWP:
+    case TMC_SURF_PW_HYBRID:
+    case TMC_SURF_NEOVIUS:
+    case TMC_SURF_PERIODIC:
+      return combine_terms(P.surface, axis_terms(P, x), axis_terms(P, y), axis_terms(P, z));
     case TMC_SURF_GOURSAT: {
       const float r2 = x * x + y * y + z * z;
       return gsq(gsq(x)) + gsq(gsq(y)) + gsq(gsq(z)) - r2 + 0.5f;
@@ -70,11 +107,6 @@ static __device__ __noinline__ float surface_value(const GenParams& P, float x, 
     case TMC_SURF_STEINER_ROMAN: {
       const float X = 1.5f * x, Y = 1.5f * y, Z = 1.5f * z;
       return gsq(X * X + Y * Y + Z * Z - 1.0f) - (gsq(Z - 1) - 2.0f * X * X) * (gsq(Z + 1) - 2 * Y * Y);
-    }
-    case TMC_SURF_PERIODIC: {  // sin(kx)cos(ky) + sin(ky)cos(kz) + sin(kz)cos(kx)
-      const float sx = sinf(P.k * x), cx = cosf(P.k * x), sy = sinf(P.k * y), cy = cosf(P.k * y);
-      const float sz = sinf(P.k * z), cz = cosf(P.k * z);
-      return sx * cy + sy * cz + sz * cx;
     }
     case TMC_SURF_BLOBS: {  // sum of exp(-|p - c|^2 / (2 sigma^2))
       float f = 0;
@@ -99,6 +131,26 @@ static __device__ __noinline__ float surface_value(const GenParams& P, float x, 
 // The value at grid point (i, j, k): coordinates -1 + i * dx in float32, as the reference forms them.
 __device__ __forceinline__ float generated_at(const GenParams& P, const float d[3], int i, int j, int k) {
   return surface_value(P, -1.0f + i * d[0], -1.0f + j * d[1], -1.0f + k * d[2]);
+}
+
+// The same value from the per-axis tables where the surface has them (the fused classification:
+// a few loads from L1-resident tables and a few products instead of six transcendentals per point).
+__device__ __forceinline__ float generated_at_fused(const GenParams& P, const float d[3], int i, int j, int k) {
+  if (P.tab[0])
+    return combine_terms(P.surface, __ldg(P.tab[0] + i), __ldg(P.tab[1] + j), __ldg(P.tab[2] + k));
+  return generated_at(P, d, i, j, k);
+}
+
+// Per-axis tables of a separable surface: tab[a][i] = axis_terms at the i-th coordinate of axis a
+// (the three axes one after another, n[a] entries each).
+static __global__ void axis_terms_kernel(GenParams P, int nx, int ny, int nz, float dx, float dy, float dz, float2* out) {
+  const int total = nx + ny + nz;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+    const int a = q < nx ? 0 : (q < nx + ny ? 1 : 2);
+    const int i = q - (a == 0 ? 0 : (a == 1 ? nx : nx + ny));
+    const float d = a == 0 ? dx : (a == 1 ? dy : dz);
+    out[q] = axis_terms(P, -1.0f + i * d);
+  }
 }
 
 // Host side: parameters and spacing of a generator, checked.  Returns false for a bad descriptor.

@@ -80,8 +80,8 @@ __device__ __forceinline__ unsigned tile_cases(const Grid& g, int64_t space_n, i
         const GenParams& P = *g.gen;
         float* o = g.gen_out + pi;
         const bool lj = j == cy - 1, lk = k == g.nz - 2;  // the cell touches the upper y / z border
-        const float v0 = generated_at(P, g.gd, i, j, k), v1 = generated_at(P, g.gd, i, j + 1, k),
-                    v2 = generated_at(P, g.gd, i, j, k + 1), v3 = generated_at(P, g.gd, i, j + 1, k + 1);
+        const float v0 = generated_at_fused(P, g.gd, i, j, k), v1 = generated_at_fused(P, g.gd, i, j + 1, k),
+                    v2 = generated_at_fused(P, g.gd, i, j, k + 1), v3 = generated_at_fused(P, g.gd, i, j + 1, k + 1);
         b0 = v0 >= iso;
         b1 = v1 >= iso;
         b2 = v2 >= iso;
@@ -91,8 +91,8 @@ __device__ __forceinline__ unsigned tile_cases(const Grid& g, int64_t space_n, i
         if (lk) o[sz] = v2;
         if (lj && lk) o[szy] = v3;
         if (own_next) {
-          const float w0 = generated_at(P, g.gd, i + 1, j, k), w1 = generated_at(P, g.gd, i + 1, j + 1, k),
-                      w2 = generated_at(P, g.gd, i + 1, j, k + 1), w3 = generated_at(P, g.gd, i + 1, j + 1, k + 1);
+          const float w0 = generated_at_fused(P, g.gd, i + 1, j, k), w1 = generated_at_fused(P, g.gd, i + 1, j + 1, k),
+                      w2 = generated_at_fused(P, g.gd, i + 1, j, k + 1), w3 = generated_at_fused(P, g.gd, i + 1, j + 1, k + 1);
           nx_bits = (unsigned)(w0 >= iso) << 1 | (unsigned)(w1 >= iso) << 3 | (unsigned)(w2 >= iso) << 5 |
                     (unsigned)(w3 >= iso) << 7;
           if (i == cx - 1) {  // the row's last cell also writes the row's last points

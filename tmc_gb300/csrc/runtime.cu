@@ -372,8 +372,22 @@ tmc_status fused_field(tmc_ctx* ctx, const tmc_volume* vol, const FusedGen& fg, 
                        tmc::GenParams** dev_params) {
   float* buf = nullptr;
   TMC_CUDA(ctx, al.get(&buf, (int64_t)vol->nx * vol->ny * vol->nz));
+  tmc::GenParams P = fg.params;
+  if (tmc::axis_separable(P.surface)) {
+    float2* tab = nullptr;
+    const int total = vol->nx + vol->ny + vol->nz;
+    TMC_CUDA(ctx, al.get(&tab, total));
+    tmc::axis_terms_kernel<<<(unsigned)tmc::ceil_div(total, 256), 256, 0, ctx->stream>>>(P, vol->nx, vol->ny, vol->nz,
+                                                                                   fg.d[0], fg.d[1], fg.d[2], tab);
+    ctx->launches += 1;
+    TMC_CUDA(ctx, cudaGetLastError());
+    P.tab[0] = tab;
+    P.tab[1] = tab + vol->nx;
+    P.tab[2] = tab + vol->nx + vol->ny;
+  }
   TMC_CUDA(ctx, al.get(dev_params, 1));
-  TMC_CUDA(ctx, cudaMemcpyAsync(*dev_params, &fg.params, sizeof(tmc::GenParams), cudaMemcpyHostToDevice, ctx->stream));
+  // pageable source: the copy is staged before the call returns, so P may go out of scope
+  TMC_CUDA(ctx, cudaMemcpyAsync(*dev_params, &P, sizeof(tmc::GenParams), cudaMemcpyHostToDevice, ctx->stream));
   *field = buf;
   return TMC_OK;
 }
