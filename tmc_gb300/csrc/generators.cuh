@@ -133,14 +133,6 @@ __device__ __forceinline__ float generated_at(const GenParams& P, const float d[
   return surface_value(P, -1.0f + i * d[0], -1.0f + j * d[1], -1.0f + k * d[2]);
 }
 
-// The same value from the per-axis tables where the surface has them (the fused classification:
-// a few loads from L1-resident tables and a few products instead of six transcendentals per point).
-__device__ __forceinline__ float generated_at_fused(const GenParams& P, const float d[3], int i, int j, int k) {
-  if (P.tab[0])
-    return combine_terms(P.surface, __ldg(P.tab[0] + i), __ldg(P.tab[1] + j), __ldg(P.tab[2] + k));
-  return generated_at(P, d, i, j, k);
-}
-
 // Per-axis tables of a separable surface: tab[a][i] = axis_terms at the i-th coordinate of axis a
 // (the three axes one after another, n[a] entries each).
 static __global__ void axis_terms_kernel(GenParams P, int nx, int ny, int nz, float dx, float dy, float dz, float2* out) {

@@ -44,6 +44,16 @@ __device__ __forceinline__ unsigned tile_cases(const Grid& g, int64_t space_n, i
   }
   int64_t pi = ((int64_t)k * g.ny + j) * g.nx + i;  // point (i, j, k)
   const float iso = g.iso_up;
+  // fused generation: the generator's per-axis tables and kind, read once (the field stores below
+  // could otherwise alias them and force a reload per point)
+  const float2 *tx = nullptr, *ty = nullptr, *tz = nullptr;
+  int surf = 0;
+  if (kGen) {
+    tx = (const float2*)__ldg((const unsigned long long*)&g.gen->tab[0]);
+    ty = (const float2*)__ldg((const unsigned long long*)&g.gen->tab[1]);
+    tz = (const float2*)__ldg((const unsigned long long*)&g.gen->tab[2]);
+    surf = __ldg(&g.gen->surface);
+  }
   unsigned actbits = 0;
 #pragma unroll
   for (int s = 0; s < kScanItems; s++) {
@@ -80,8 +90,20 @@ __device__ __forceinline__ unsigned tile_cases(const Grid& g, int64_t space_n, i
         const GenParams& P = *g.gen;
         float* o = g.gen_out + pi;
         const bool lj = j == cy - 1, lk = k == g.nz - 2;  // the cell touches the upper y / z border
-        const float v0 = generated_at_fused(P, g.gd, i, j, k), v1 = generated_at_fused(P, g.gd, i, j + 1, k),
-                    v2 = generated_at_fused(P, g.gd, i, j, k + 1), v3 = generated_at_fused(P, g.gd, i, j + 1, k + 1);
+        float v0, v1, v2, v3;
+        if (tx) {  // separable: the four corner rows share the x term, pairs of rows the y and z terms
+          const float2 X = __ldg(tx + i), Y0 = __ldg(ty + j), Y1 = __ldg(ty + j + 1), Z0 = __ldg(tz + k),
+                       Z1 = __ldg(tz + k + 1);
+          v0 = combine_terms(surf, X, Y0, Z0);
+          v1 = combine_terms(surf, X, Y1, Z0);
+          v2 = combine_terms(surf, X, Y0, Z1);
+          v3 = combine_terms(surf, X, Y1, Z1);
+        } else {
+          v0 = generated_at(P, g.gd, i, j, k);
+          v1 = generated_at(P, g.gd, i, j + 1, k);
+          v2 = generated_at(P, g.gd, i, j, k + 1);
+          v3 = generated_at(P, g.gd, i, j + 1, k + 1);
+        }
         b0 = v0 >= iso;
         b1 = v1 >= iso;
         b2 = v2 >= iso;
@@ -91,8 +113,20 @@ __device__ __forceinline__ unsigned tile_cases(const Grid& g, int64_t space_n, i
         if (lk) o[sz] = v2;
         if (lj && lk) o[szy] = v3;
         if (own_next) {
-          const float w0 = generated_at_fused(P, g.gd, i + 1, j, k), w1 = generated_at_fused(P, g.gd, i + 1, j + 1, k),
-                      w2 = generated_at_fused(P, g.gd, i + 1, j, k + 1), w3 = generated_at_fused(P, g.gd, i + 1, j + 1, k + 1);
+          float w0, w1, w2, w3;
+          if (tx) {
+            const float2 X = __ldg(tx + i + 1), Y0 = __ldg(ty + j), Y1 = __ldg(ty + j + 1), Z0 = __ldg(tz + k),
+                         Z1 = __ldg(tz + k + 1);
+            w0 = combine_terms(surf, X, Y0, Z0);
+            w1 = combine_terms(surf, X, Y1, Z0);
+            w2 = combine_terms(surf, X, Y0, Z1);
+            w3 = combine_terms(surf, X, Y1, Z1);
+          } else {
+            w0 = generated_at(P, g.gd, i + 1, j, k);
+            w1 = generated_at(P, g.gd, i + 1, j + 1, k);
+            w2 = generated_at(P, g.gd, i + 1, j, k + 1);
+            w3 = generated_at(P, g.gd, i + 1, j + 1, k + 1);
+          }
           nx_bits = (unsigned)(w0 >= iso) << 1 | (unsigned)(w1 >= iso) << 3 | (unsigned)(w2 >= iso) << 5 |
                     (unsigned)(w3 >= iso) << 7;
           if (i == cx - 1) {  // the row's last cell also writes the row's last points
