@@ -129,7 +129,12 @@ enum {
   TMC_TUNE_WARP_LIST_MAX = 2,        /* DMC float64-fallback lists up to this length run one warp
                                         per vertex (0 = one thread per vertex, retries by warp) */
   TMC_TUNE_VERTEX_BLOCKS_PER_SM = 3, /* grid cap of the per-vertex DMC passes, 1..64 */
-  TMC_TUNE_EMIT_BLOCKS_PER_SM = 4    /* grid cap of the TMC emission kernel, 1..64 */
+  TMC_TUNE_EMIT_BLOCKS_PER_SM = 4,   /* grid cap of the TMC emission kernel, 1..64 */
+  /* the slab pipeline of a host field (copy of slab q+1 beside the classification of slab q):
+   * slab depth in MiB (4..1024) and the most slabs per field (2..64) */
+  TMC_TUNE_SLAB_MIB = 5,
+  TMC_TUNE_MAX_SLABS = 6,
+  TMC_TUNE_QUAD_BLOCKS_PER_SM = 7    /* grid of the DMC quad pass over the listed cells, 1..64 */
 };
 tmc_status tmc_ctx_set_tuning(tmc_ctx* ctx, int32_t key, int64_t value);
 tmc_status tmc_ctx_get_tuning(const tmc_ctx* ctx, int32_t key, int64_t* value);
@@ -263,7 +268,9 @@ typedef struct tmc_request {
 tmc_status tmc_batch_extract(tmc_ctx* ctx, int32_t n, const tmc_request* reqs, tmc_mesh* outs);
 /* Autotuner (no reference counterpart): times `rounds` batched extractions of the given requests
  * for each candidate launch shape (coordinate descent over the TMC_TUNE_* keys) and keeps the
- * fastest in the context; *best_ms (optional) receives the time of one batch with the result. */
+ * fastest in the context; *best_ms (optional) receives the time of one batch with the result.  With
+ * one request the single-volume entry point is timed instead, and a host field there also tunes the
+ * slab pipeline (TMC_TUNE_SLAB_MIB, TMC_TUNE_MAX_SLABS). */
 tmc_status tmc_ctx_autotune(tmc_ctx* ctx, int32_t n, const tmc_request* reqs, int32_t rounds, double* best_ms);
 
 /* request server (no reference counterpart) ------------------------------------------------------

@@ -2,7 +2,8 @@
 
 The settings choose between kernels that compute the same values: one thread per vertex or a group
 of lanes per vertex for the DMC projection, one thread or one warp per float64-fallback vertex, and
-the grid sizes of the per-vertex and TMC emission passes.  Every setting must give bit-identical
+the grid sizes of the per-vertex, quad and TMC emission passes, and the slab depth and count of a
+host field's copy/classification pipeline.  Every setting must give bit-identical
 meshes and the same counters; the oracle parity of the default settings is checked in
 test_gpu_dmc.py and test_gpu_tmc.py.
 """
@@ -19,13 +20,15 @@ pytestmark = pytest.mark.gpu
 
 KEYS = ("v", "n", "v64", "q", "t", "he", "hv", "hf", "vcell", "vuvw")
 TUNE_KEYS = (native.TUNE_GROUP_LANES, native.TUNE_WARP_LIST_MAX, native.TUNE_VERTEX_BLOCKS_PER_SM,
-             native.TUNE_EMIT_BLOCKS_PER_SM)
+             native.TUNE_EMIT_BLOCKS_PER_SM, native.TUNE_QUAD_BLOCKS_PER_SM, native.TUNE_SLAB_MIB,
+             native.TUNE_MAX_SLABS)
 
-# (group lanes, warp list max, vertex blocks per SM, emit blocks per SM)
+# (group lanes, warp list max, vertex blocks per SM, emit blocks per SM, quad blocks per SM,
+#  slab MiB, max slabs)
 SETTINGS = {
-    "threads": (0, 0, 32, 8),              # one thread per vertex everywhere, 26x26 retries by warp
-    "lanes": (1 << 40, 1 << 30, 32, 8),    # lane groups and whole lists by warp wherever possible
-    "small_grids": (0, 1 << 30, 1, 1),     # minimal grids: every grid-stride loop takes many turns
+    "threads": (0, 0, 32, 8, 1, 32, 16),              # one thread per vertex, 26x26 retries by warp
+    "lanes": (1 << 40, 1 << 30, 32, 8, 4, 128, 4),    # lane groups and whole lists by warp wherever possible
+    "small_grids": (0, 1 << 30, 1, 1, 1, 4, 64),      # minimal grids, thin slabs: every loop takes many turns
 }
 
 
@@ -118,6 +121,46 @@ def test_tmc_identical_under_every_setting(ctx, name):
         ctx.set_tuning(native.TUNE_EMIT_BLOCKS_PER_SM, default)
 
 
+def test_host_field_slab_shapes(ctx):
+    """A host field copied in slabs of every tuned depth and count (4 MiB to one slab per field, 2 to
+    64 slabs) extracts the same meshes as the same field on the device."""
+    vol = V.small_noise_volume(160, seed=4, coarse=9)  # 16 MiB
+    default = tuple(ctx.get_tuning(k) for k in (native.TUNE_SLAB_MIB, native.TUNE_MAX_SLABS))
+    want_d = ctx.dmc(vol, native.OUT_POS_F64 | native.OUT_TRIANGLES | native.OUT_HALFEDGES | native.DMC_SIMPLIFY)
+    want_t = ctx.tmc(vol, native.OUT_POS_F64)
+    try:
+        for mib, slabs in ((4, 2), (4, 64), (8, 3), (16, 16), (1024, 64)):
+            ctx.set_tuning(native.TUNE_SLAB_MIB, mib)
+            ctx.set_tuning(native.TUNE_MAX_SLABS, slabs)
+            got = ctx.dmc(vol, native.OUT_POS_F64 | native.OUT_TRIANGLES | native.OUT_HALFEDGES | native.DMC_SIMPLIFY)
+            _same(got, want_d, f"slabs {mib} MiB x {slabs}")
+            _same(ctx.tmc(vol, native.OUT_POS_F64), want_t, f"TMC slabs {mib} MiB x {slabs}")
+    finally:
+        ctx.set_tuning(native.TUNE_SLAB_MIB, default[0])
+        ctx.set_tuning(native.TUNE_MAX_SLABS, default[1])
+
+
+def test_autotune_single_host_volume_tunes_slabs():
+    """One request with a host field: the autotuner times the single-volume path and reports the
+    slab depth and count it chose; the meshes stay the same."""
+    import torch
+    c = native.Context(0)
+    try:
+        vol = V.small_noise_volume(192, seed=6, coarse=9)  # 27 MiB
+        pin = torch.from_numpy(vol.data).pin_memory()
+        tv = native.make_volume(vol, pin.data_ptr(), on_device=False)
+        before = c.dmc(vol, 0)
+        ms = c.autotune([tv], [vol.iso], [native.ALGO_DMC], [0], rounds=2)
+        assert ms > 0
+        assert 4 <= c.get_tuning(native.TUNE_SLAB_MIB) <= 1024
+        assert 2 <= c.get_tuning(native.TUNE_MAX_SLABS) <= 64
+        after = c.dmc(vol, 0)
+        for k in KEYS:
+            np.testing.assert_array_equal(before[k], after[k], err_msg=k)
+    finally:
+        c.close()
+
+
 def test_tuning_keys_are_checked(ctx):
     with pytest.raises(native.TmcError):
         ctx.set_tuning(99, 1)
@@ -125,6 +168,10 @@ def test_tuning_keys_are_checked(ctx):
         ctx.set_tuning(native.TUNE_VERTEX_BLOCKS_PER_SM, 0)
     with pytest.raises(native.TmcError):
         ctx.set_tuning(native.TUNE_GROUP_LANES, -1)
+    with pytest.raises(native.TmcError):
+        ctx.set_tuning(native.TUNE_SLAB_MIB, 3)
+    with pytest.raises(native.TmcError):
+        ctx.set_tuning(native.TUNE_MAX_SLABS, 1)
     old = ctx.get_tuning(native.TUNE_WARP_LIST_MAX)
     ctx.set_tuning(native.TUNE_WARP_LIST_MAX, 123)
     assert ctx.get_tuning(native.TUNE_WARP_LIST_MAX) == 123

@@ -327,6 +327,9 @@ struct Tuning {
   int64_t warp_list_max = 0;      // float64 fallback lists up to this length run one warp per vertex
   int vertex_blocks_per_sm = 32;  // grid cap of the per-vertex passes (rounded to whole waves)
   int emit_blocks_per_sm = 8;     // grid cap of the TMC emission kernel
+  int quad_blocks_per_sm = 1;     // grid of the DMC quad pass (whole waves)
+  int64_t slab_bytes = (int64_t)32 << 20;  // host-field slab depth
+  int max_slabs = 16;             // host-field slabs per field
   static Tuning defaults(int sms) {
     Tuning t;
     t.sms = sms;

@@ -941,10 +941,12 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
   Stage t(prof, "dmc_quad", st);
   // one wave: the kernel takes 32-cell chunks until none are left
   if (space.grids)
-    dmc_quad_kernel<true><<<(unsigned)wave_grid(r_quad_batch, sms, 1, ceil_div(n, 32), kQuadThreads / 32), kQuadThreads,
+    dmc_quad_kernel<true><<<(unsigned)wave_grid(r_quad_batch, sms, tu.quad_blocks_per_sm, ceil_div(n, 32),
+                                                kQuadThreads / 32), kQuadThreads,
                             0, st>>>(space, s.mask, s.cellof, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
   else
-    dmc_quad_kernel<false><<<(unsigned)wave_grid(r_quad, sms, 1, ceil_div(n, 32), kQuadThreads / 32), kQuadThreads, 0,
+    dmc_quad_kernel<false><<<(unsigned)wave_grid(r_quad, sms, tu.quad_blocks_per_sm, ceil_div(n, 32),
+                                                 kQuadThreads / 32), kQuadThreads, 0,
                              st>>>(space, s.mask, s.cellof, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
   return 7;
 }

@@ -188,13 +188,13 @@ tmc_status field_on_device(tmc_ctx* ctx, const tmc_volume* vol, Allocs& al, cons
 // cells lie in the planes of slabs 0..q (a cell needs its planes z and z + 1) and the event that
 // slab q has arrived.  A device field, a small one, or a context that checks the field for NaN/Inf
 // (which needs the whole field first) takes field_on_device and no gates.
-constexpr size_t kSlabBytes = (size_t)32 << 20;
-constexpr int kMaxSlabs = 16;
+// Slab depth and count: the context's tuning (TMC_TUNE_SLAB_MIB, TMC_TUNE_MAX_SLABS).
 tmc_status field_slabs(tmc_ctx* ctx, const tmc_volume* vol, Allocs& al, const float** out,
                        std::vector<tmc::TileGate>& gates) {
   gates.clear();
   const size_t plane = (size_t)vol->nx * vol->ny, n = plane * vol->nz;
-  const int slabs = (int)std::min<size_t>({(size_t)kMaxSlabs, n * sizeof(float) / kSlabBytes, (size_t)vol->nz / 2});
+  const int slabs = (int)std::min<size_t>(
+      {(size_t)ctx->tune.max_slabs, n * sizeof(float) / (size_t)ctx->tune.slab_bytes, (size_t)vol->nz / 2});
   if (vol->on_device || ctx->opts.check_numeric || slabs < 2) return field_on_device(ctx, vol, al, out);
   float* d = nullptr;
   TMC_CUDA(ctx, al.get(&d, n));
@@ -502,6 +502,18 @@ tmc_status tmc_ctx_set_tuning(tmc_ctx* ctx, int32_t key, int64_t value) {
       if (value < 1 || value > 64) break;
       ctx->tune.emit_blocks_per_sm = (int)value;
       return TMC_OK;
+    case TMC_TUNE_SLAB_MIB:
+      if (value < 4 || value > 1024) break;
+      ctx->tune.slab_bytes = value << 20;
+      return TMC_OK;
+    case TMC_TUNE_MAX_SLABS:
+      if (value < 2 || value > 64) break;
+      ctx->tune.max_slabs = (int)value;
+      return TMC_OK;
+    case TMC_TUNE_QUAD_BLOCKS_PER_SM:
+      if (value < 1 || value > 64) break;
+      ctx->tune.quad_blocks_per_sm = (int)value;
+      return TMC_OK;
     default:
       return fail(ctx, TMC_ERR_INVALID_ARG, "unknown tuning key %d", key);
   }
@@ -515,6 +527,9 @@ tmc_status tmc_ctx_get_tuning(const tmc_ctx* ctx, int32_t key, int64_t* value) {
     case TMC_TUNE_WARP_LIST_MAX: *value = ctx->tune.warp_list_max; return TMC_OK;
     case TMC_TUNE_VERTEX_BLOCKS_PER_SM: *value = ctx->tune.vertex_blocks_per_sm; return TMC_OK;
     case TMC_TUNE_EMIT_BLOCKS_PER_SM: *value = ctx->tune.emit_blocks_per_sm; return TMC_OK;
+    case TMC_TUNE_SLAB_MIB: *value = ctx->tune.slab_bytes >> 20; return TMC_OK;
+    case TMC_TUNE_MAX_SLABS: *value = ctx->tune.max_slabs; return TMC_OK;
+    case TMC_TUNE_QUAD_BLOCKS_PER_SM: *value = ctx->tune.quad_blocks_per_sm; return TMC_OK;
     default: return TMC_ERR_INVALID_ARG;
   }
 }
@@ -1213,7 +1228,15 @@ extern "C" tmc_status tmc_ctx_autotune(tmc_ctx* ctx, int32_t n, const tmc_reques
     const int reps = timed ? rounds : 1;
     cudaEventRecord(e0, ctx->stream);
     for (int r = 0; r < reps; r++) {
-      tmc_status st = tmc_batch_extract(ctx, n, reqs, outs.data());
+      tmc_status st;
+      if (n == 1) {  // one request: the single-volume entry point (slab pipeline for a host field)
+        const tmc_request& q = reqs[0];
+        if (q.algo == TMC_ALGO_DMC) st = tmc_dmc_extract(ctx, &q.vol, q.iso, q.flags, outs.data());
+        else if (q.flags & TMC_OUT_HALFEDGES) st = tmc_tmc_halfedge(ctx, &q.vol, q.iso, q.flags, outs.data());
+        else st = tmc_tmc_sharedvertex(ctx, &q.vol, q.iso, q.flags, outs.data());
+      } else {
+        st = tmc_batch_extract(ctx, n, reqs, outs.data());
+      }
       if (st) return st;
       for (auto& m : outs) tmc_mesh_free(ctx, &m);
     }
@@ -1229,12 +1252,18 @@ extern "C" tmc_status tmc_ctx_autotune(tmc_ctx* ctx, int32_t n, const tmc_reques
     int32_t key;
     std::vector<int64_t> values;
   };
-  const Axis axes[] = {
+  const bool host_field = n == 1 && !reqs[0].vol.on_device;
+  std::vector<Axis> axes = {
       {TMC_TUNE_GROUP_LANES, {0, sm * 12 * 32, sm * 24 * 32, sm * 48 * 32}},
       {TMC_TUNE_WARP_LIST_MAX, {0, sm * 8, sm * 32, sm * 128}},
       {TMC_TUNE_VERTEX_BLOCKS_PER_SM, {8, 16, 32}},
       {TMC_TUNE_EMIT_BLOCKS_PER_SM, {4, 8, 16}},
+      {TMC_TUNE_QUAD_BLOCKS_PER_SM, {1, 2, 4}},
   };
+  if (host_field) {
+    axes.push_back({TMC_TUNE_SLAB_MIB, {8, 16, 32, 64, 128}});
+    axes.push_back({TMC_TUNE_MAX_SLABS, {4, 8, 16, 32}});
+  }
   double best = 0, ms = 0;
   tmc_status st = run(false, ms);  // warm-up: pools, pinned blocks
   if (!st) st = run(true, best);

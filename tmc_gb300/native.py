@@ -65,6 +65,9 @@ TUNE_GROUP_LANES = 1
 TUNE_WARP_LIST_MAX = 2
 TUNE_VERTEX_BLOCKS_PER_SM = 3
 TUNE_EMIT_BLOCKS_PER_SM = 4
+TUNE_SLAB_MIB = 5
+TUNE_MAX_SLABS = 6
+TUNE_QUAD_BLOCKS_PER_SM = 7
 
 
 class TmcError(RuntimeError):
