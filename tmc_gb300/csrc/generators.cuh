@@ -30,15 +30,16 @@ struct GenParams {
   const float2* tab[3];
 };
 
-// The surfaces whose transcendental parts depend on one coordinate each: the periodic field
-// (sin and cos of k x) and the reference's IWP, P-W hybrid and Neovius surfaces (cos of s (x + 1)).
+// The surfaces that are sums and products of terms of one coordinate each, combined in the order
+// the formula rounds them: the periodic field (sin and cos of k x), the reference's IWP, P-W hybrid
+// and Neovius surfaces (cos of s (x + 1)), its sphere (x^2) and its Goursat surface (x^4, x^2).
 __host__ __device__ __forceinline__ bool axis_separable(int surface) {
   return surface == TMC_SURF_PERIODIC || surface == TMC_SURF_IWP || surface == TMC_SURF_PW_HYBRID ||
-         surface == TMC_SURF_NEOVIUS;
+         surface == TMC_SURF_NEOVIUS || surface == TMC_SURF_SPHERE || surface == TMC_SURF_GOURSAT;
 }
 
 // The per-axis terms of a separable surface at coordinate x: (sin kx, cos kx) for the periodic field,
-// (cos s(x + 1), 0) for the cosine surfaces.
+// (cos s(x + 1), 0) for the cosine surfaces, (x^2, 0) for the sphere, (x^4, x^2) for Goursat's.
 __device__ __forceinline__ float2 axis_terms(const GenParams& P, float x) {
   const float pi = 3.14159265358979323846f;
   switch (P.surface) {
@@ -48,6 +49,10 @@ __device__ __forceinline__ float2 axis_terms(const GenParams& P, float x) {
       return make_float2(cosf(5.01f * pi * (x + 1)), 0.0f);
     case TMC_SURF_PW_HYBRID:
       return make_float2(cosf(1.01f * pi * (x + 1)), 0.0f);
+    case TMC_SURF_SPHERE:
+      return make_float2(x * x, 0.0f);
+    case TMC_SURF_GOURSAT:
+      return make_float2(gsq(gsq(x)), x * x);
     default:  // TMC_SURF_NEOVIUS
       return make_float2(cosf(pi * (x + 1)), 0.0f);
   }
@@ -56,6 +61,12 @@ __device__ __forceinline__ float2 axis_terms(const GenParams& P, float x) {
 // A separable surface from its three per-axis terms
 __device__ __forceinline__ float combine_terms(int surface, float2 X, float2 Y, float2 Z) {
   switch (surface) {
+    case TMC_SURF_SPHERE:  // x^2 + y^2 + z^2 - 0.16
+      return X.x + Y.x + Z.x - 0.16f;
+    case TMC_SURF_GOURSAT: {  // x^4 + y^4 + z^4 - (x^2 + y^2 + z^2) + 0.5
+      const float r2 = X.y + Y.y + Z.y;
+      return X.x + Y.x + Z.x - r2 + 0.5f;
+    }
     case TMC_SURF_PERIODIC:  // sin(kx)cos(ky) + sin(ky)cos(kz) + sin(kz)cos(kx)
       return X.x * Y.y + Y.x * Z.y + Z.x * X.y;
     case TMC_SURF_IWP: {
@@ -84,8 +95,6 @@ __device__ __forceinline__ float torus_field(float x, float y, float z, float cx
 static __device__ __noinline__ float surface_value(const GenParams& P, float x, float y, float z) {
   const float pi = 3.14159265358979323846f;
   switch (P.surface) {
-    case TMC_SURF_SPHERE:
-      return x * x + y * y + z * z - 0.16f;
     case TMC_SURF_TORUS:
       return torus_field(x, y, z, 0, 0, 0, false);
     case TMC_SURF_TWO_HOLED_TORUS:
@@ -99,11 +108,9 @@ static __device__ __noinline__ float surface_value(const GenParams& P, float x, 
     case TMC_SURF_PW_HYBRID:
     case TMC_SURF_NEOVIUS:
     case TMC_SURF_PERIODIC:
+    case TMC_SURF_SPHERE:
+    case TMC_SURF_GOURSAT:
       return combine_terms(P.surface, axis_terms(P, x), axis_terms(P, y), axis_terms(P, z));
-    case TMC_SURF_GOURSAT: {
-      const float r2 = x * x + y * y + z * z;
-      return gsq(gsq(x)) + gsq(gsq(y)) + gsq(gsq(z)) - r2 + 0.5f;
-    }
     case TMC_SURF_STEINER_ROMAN: {
       const float X = 1.5f * x, Y = 1.5f * y, Z = 1.5f * z;
       return gsq(X * X + Y * Y + Z * Z - 1.0f) - (gsq(Z - 1) - 2.0f * X * X) * (gsq(Z + 1) - 2 * Y * Y);
