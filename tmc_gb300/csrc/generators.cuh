@@ -30,6 +30,8 @@ struct GenParams {
   const float2* tab[3];
 };
 
+__device__ __forceinline__ float gsq(float x) { return x * x; }
+
 // The surfaces that are sums and products of terms of one coordinate each, combined in the order
 // the formula rounds them: the periodic field (sin and cos of k x), the reference's IWP, P-W hybrid
 // and Neovius surfaces (cos of s (x + 1)), its sphere (x^2) and its Goursat surface (x^4, x^2).
@@ -84,7 +86,6 @@ __device__ __forceinline__ float combine_terms(int surface, float2 X, float2 Y, 
   }
 }
 
-__device__ __forceinline__ float gsq(float x) { return x * x; }
 // torus around the z axis (horizontal) or the y axis (vertical): ring radius R, tube radius r
 __device__ __forceinline__ float torus_field(float x, float y, float z, float cx, float cy, float cz, bool vertical) {
   const float R2 = gsq(0.3f), r2 = gsq(0.15f);
