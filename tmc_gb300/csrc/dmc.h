@@ -38,6 +38,7 @@ struct DmcScratch {
   // listed cells (common.cuh): rec, voff and qoff hold one entry per listed cell at its slot
   CellMask* mask;                 // per 32 cells of the space
   uint16_t* cellof;               // per slot: in-tile offset of the listed cell
+  uint8_t* ccase;                 // per slot: the listed cell's MC case
   uint8_t* vrank;                 // per vertex: rank among its cell's vertices (vwork: the cell's slot)
   unsigned* amb_n;                // listed cells with an ambiguous case (their slots wait in qoff)
 };

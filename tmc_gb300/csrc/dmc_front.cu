@@ -49,7 +49,7 @@ __constant__ uint64_t c_case_contour[256] = TMC_CASE_CONTOUR_INIT;
 // dmc_amb_kernel, which runs them densely instead of stalling every warp here on a few lanes.
 template <bool kGen>
 __global__ void __launch_bounds__(kScanThreads, 6) dmc_classify_kernel(CellSpace space, int64_t tile0, uint32_t* rec,
-                                                                   uint16_t* cellof, CellMask* mask,
+                                                                   uint16_t* cellof, uint8_t* ccase, CellMask* mask,
                                                                    unsigned long long* tile_sums,
                                                                    unsigned long long* stats, uint32_t* amb_list,
                                                                    unsigned* amb_n) {
@@ -75,6 +75,7 @@ __global__ void __launch_bounds__(kScanThreads, 6) dmc_classify_kernel(CellSpace
     const unsigned cs = case_of[off];
     const bool ambiguous = case_ambiguous(cs);
     cellof[slot] = (uint16_t)off;
+    ccase[slot] = (uint8_t)cs;
     if (!ambiguous) {
       int i, j, k;
       cell_ijk(g, vbase + off - g.vbase, i, j, k);
@@ -734,7 +735,7 @@ __global__ void __launch_bounds__(kVertexThreads, 4) dmc_vertex_finish_kernel(Ce
 // volume's first vertex (the scanned tile offset of its first tile; 0 for a single volume).
 // The quads a cell owns (one per crossed interior edge 0, 3, 8), from the records of the four
 // cells around each edge (listed cells: a crossed edge makes every cell around it listed).
-__device__ __forceinline__ void cell_quads(const Grid& g, int32_t vfirst, uint32_t slot, int64_t vc,
+__device__ __forceinline__ void cell_quads(const Grid& g, int32_t vfirst, uint32_t slot, int64_t vc, unsigned cs,
                                            const CellMask* mask, const uint32_t* rec, const int32_t* voff,
                                            const int32_t* qoff, int32_t* quads, uint8_t* colors) {
   // cell offsets (di, dj, dk) and local edge of the four cells around the owned edges 0, 3, 8
@@ -744,11 +745,10 @@ __device__ __forceinline__ void cell_quads(const Grid& g, int32_t vfirst, uint32
   const int64_t cell = vc - g.vbase;
   int i, j, k;
   cell_ijk(g, cell, i, j, k);
-  const float f0 = g.at(i, j, k);
-  const int neg = !(f0 >= g.iso_up);  // first end vertex below the isovalue
-  const float fx = g.at(i + 1, j, k), fy = g.at(i, j + 1, k), fz = g.at(i, j, k + 1);
-  const bool s0 = f0 >= g.iso_up;
-  const bool crossed[3] = {s0 != (fx >= g.iso_up), s0 != (fy >= g.iso_up), s0 != (fz >= g.iso_up)};
+  // from the cell's MC case (bit v: corner v at or above the isovalue): corner 0's side, and the
+  // crossings of edges 0 (corners 0-1), 3 (0-2) and 8 (0-4)
+  const int neg = !(cs & 1u);  // first end vertex below the isovalue
+  const bool crossed[3] = {((cs ^ (cs >> 1)) & 1u) != 0, ((cs ^ (cs >> 2)) & 1u) != 0, ((cs ^ (cs >> 4)) & 1u) != 0};
   int32_t q = qoff[slot];
   const int par = (i & 1) | ((j & 1) << 1) | ((k & 1) << 2);
 #pragma unroll
@@ -790,7 +790,8 @@ __device__ __forceinline__ void cell_quads(const Grid& g, int32_t vfirst, uint32
 constexpr int kQuadThreads = 256;
 template <bool kBatch>
 __global__ void __launch_bounds__(kQuadThreads) dmc_quad_kernel(CellSpace space, const CellMask* mask,
-                                                                const uint16_t* cellof, const uint32_t* rec,
+                                                                const uint16_t* cellof, const uint8_t* ccase,
+                                                                const uint32_t* rec,
                                                                 const int32_t* voff, const int32_t* qoff,
                                                                 const unsigned long long* tile_off, int32_t* quads,
                                                                 uint8_t* colors) {
@@ -820,7 +821,7 @@ __global__ void __launch_bounds__(kQuadThreads) dmc_quad_kernel(CellSpace space,
         const uint32_t vc = slot_cell(cellof, slot);
         const Grid& g = kBatch ? space.grids[__ldg(space.tile_vol + vc / kScanTile)] : space.one;
         const int32_t vfirst = kBatch ? (int32_t)(tile_off[g.vbase / kScanTile] >> 32) : 0;
-        cell_quads(g, vfirst, slot, vc, mask, rec, voff, qoff, quads, colors);
+        cell_quads(g, vfirst, slot, vc, __ldg(ccase + slot), mask, rec, voff, qoff, quads, colors);
       }
       __syncwarp();
       const int rest = qn - take;  // at most 31: move them to the front
@@ -851,10 +852,10 @@ int dmc_front_count(const CellSpace& space, DmcScratch& s, cudaStream_t st, Prof
       if (t1 <= t0) return;
       if (space.one.gen)  // fused generation (single volumes)
         dmc_classify_kernel<true><<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(
-            space, t0, s.rec, s.cellof, s.mask, s.tile_sums, s.stats, reinterpret_cast<uint32_t*>(s.qoff), s.amb_n);
+            space, t0, s.rec, s.cellof, s.ccase, s.mask, s.tile_sums, s.stats, reinterpret_cast<uint32_t*>(s.qoff), s.amb_n);
       else
         dmc_classify_kernel<false><<<(unsigned)(t1 - t0), kScanThreads, 0, st>>>(
-            space, t0, s.rec, s.cellof, s.mask, s.tile_sums, s.stats, reinterpret_cast<uint32_t*>(s.qoff), s.amb_n);
+            space, t0, s.rec, s.cellof, s.ccase, s.mask, s.tile_sums, s.stats, reinterpret_cast<uint32_t*>(s.qoff), s.amb_n);
       k++;
     };
     if (ngates == 0) classify(0, tiles);
@@ -943,11 +944,12 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
   if (space.grids)
     dmc_quad_kernel<true><<<(unsigned)wave_grid(r_quad_batch, sms, tu.quad_blocks_per_sm, ceil_div(n, 32),
                                                 kQuadThreads / 32), kQuadThreads,
-                            0, st>>>(space, s.mask, s.cellof, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
+                            0, st>>>(space, s.mask, s.cellof, s.ccase, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
   else
     dmc_quad_kernel<false><<<(unsigned)wave_grid(r_quad, sms, tu.quad_blocks_per_sm, ceil_div(n, 32),
                                                  kQuadThreads / 32), kQuadThreads, 0,
-                             st>>>(space, s.mask, s.cellof, s.rec, s.voff, s.qoff, s.tile_sums, quads, colors);
+                             st>>>(space, s.mask, s.cellof, s.ccase, s.rec, s.voff, s.qoff, s.tile_sums, quads,
+                                   colors);
   return 7;
 }
 

@@ -632,6 +632,7 @@ tmc_status dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   TMC_CUDA(ctx, al.get(&sc.voff, ncell));
   TMC_CUDA(ctx, al.get(&sc.qoff, ncell));
   TMC_CUDA(ctx, al.get(&sc.cellof, ncell));
+  TMC_CUDA(ctx, al.get(&sc.ccase, ncell));
   TMC_CUDA(ctx, al.get(&sc.amb_n, 1));
   TMC_CUDA(ctx, al.get(&sc.mask, tmc::dmc_tiles(space) * (tmc::kScanTile / 32)));
   TMC_CUDA(ctx, al.get(&sc.tile_sums, tmc::dmc_tiles(space)));
@@ -981,6 +982,7 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
     dsc.mask = mask;
     dsc.cellof = cellof;
     TMC_CUDA(ctx, al.get(&dsc.amb_n, 1));
+    TMC_CUDA(ctx, al.get(&dsc.ccase, ncell));
     ctx->launches += tmc::dmc_front_count(space, dsc, st, &ctx->prof);
   } else {
     tsc = tmc::TmcScratch{rec, voff, qoff, tile_sums, totals, ctx->d_stats, nullptr, nullptr, nullptr};
