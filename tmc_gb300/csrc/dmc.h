@@ -41,8 +41,6 @@ struct DmcScratch {
   uint8_t* ccase;                 // per slot: the listed cell's MC case
   uint8_t* vrank;                 // per vertex: rank among its cell's vertices (vwork: the cell's slot)
   unsigned* amb_n;                // listed cells with an ambiguous case (their slots wait in qoff)
-  uint32_t* order;                // 4 * nv: the vertices of each set-up class (vertex_order_classes)
-  unsigned* order_count;          // 4 class sizes
 };
 constexpr size_t kProjRecordBytes = 144;  // sizeof(repr::ProjRecord)
 

@@ -135,18 +135,11 @@ __global__ void __launch_bounds__(128) dmc_amb_kernel(CellSpace space, const uin
 
 // In-tile exclusive scan of the listed cells' records -> their vertex and quad offsets (blocked:
 // 16-byte record loads and offset stores over the tile's slots, one block scan of the thread
-// totals), two entries per vertex (the slot of the cell that generates it and its rank there), and
-// the vertex's class for the set-up pass: ambiguous case or not, contour of six edges or more (the
-// gradient-plane path) or not.  Each class gets its own list (order + class * nv_cap, counts in
-// order_count[class]), so that the set-up pass's warps follow one code path.
+// totals), and two entries per vertex: the slot of the cell that generates it and its rank there.
 __global__ void __launch_bounds__(kScanThreads) dmc_offsets_kernel(const CellMask* mask, const uint32_t* rec,
-                                                                  const uint8_t* ccase,
                                                                   const unsigned long long* tile_off,
                                                                   int32_t* voff, int32_t* qoff, uint32_t* vwork,
-                                                                  uint8_t* vrank, uint32_t* order,
-                                                                  unsigned* order_count, int64_t nv_cap) {
-  __shared__ unsigned cls_n[4], cls_base[4];
-  if (threadIdx.x < 4) cls_n[threadIdx.x] = 0;
+                                                                  uint8_t* vrank) {
   const int64_t base = (int64_t)blockIdx.x * kScanTile;
   const int64_t end = base + tile_listed(mask, blockIdx.x);
   const int64_t first = base + (int64_t)threadIdx.x * kScanItems;
@@ -156,7 +149,7 @@ __global__ void __launch_bounds__(kScanThreads) dmc_offsets_kernel(const CellMas
 #pragma unroll
   for (int s = 0; s < kScanItems; s++) sum += ((unsigned long long)rec_nv(r[s]) << 32) | rec_nq(r[s]);
   unsigned long long tot;
-  unsigned long long pre = tile_off[blockIdx.x] + block_exclusive_scan(sum, &tot);  // synchronises
+  unsigned long long pre = tile_off[blockIdx.x] + block_exclusive_scan(sum, &tot);
   int32_t vo[kScanItems], qo[kScanItems];
 #pragma unroll
   for (int s = 0; s < kScanItems; s++) {
@@ -166,36 +159,11 @@ __global__ void __launch_bounds__(kScanThreads) dmc_offsets_kernel(const CellMas
   }
   store8(voff, first, end, vo);
   store8(qoff, first, end, qo);
-  // vertex entries and classes; a vertex's place in its class list: its block-local rank (shared
-  // atomics), then one global reservation per class and block.  Per cell and vertex q, 16 bits of
-  // ranks[s]: the class (2 bits) over the local rank (14 bits; a block has at most 4 * 2048 vertices)
-  uint64_t ranks[kScanItems];
-#pragma unroll
-  for (int s = 0; s < kScanItems; s++) {
-    ranks[s] = 0;
-    const int nvs = rec_nv(r[s]);
-    if (nvs == 0) continue;
-    const uint32_t em = case_edge_mask(__ldg(ccase + first + s));
-    const unsigned amb = (r[s] >> 29) & 1u;
-    for (int q = 0; q < nvs; q++) {
-      vwork[vo[s] + q] = (uint32_t)(first + s);
-      vrank[vo[s] + q] = (uint8_t)q;
-      int size = 0;
-      for (uint32_t m = em; m; m &= m - 1) size += rec_rank(r[s], __ffs(m) - 1) == q;
-      const unsigned c = amb << 1 | (unsigned)(size >= 6);
-      const unsigned lr = atomicAdd(&cls_n[c], 1u);
-      ranks[s] |= (uint64_t)(c << 14 | lr) << (16 * q);
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x < 4)
-    cls_base[threadIdx.x] = cls_n[threadIdx.x] ? atomicAdd(order_count + threadIdx.x, cls_n[threadIdx.x]) : 0u;
-  __syncthreads();
 #pragma unroll
   for (int s = 0; s < kScanItems; s++)
-    for (int q = 0; q < rec_nv(r[s]); q++) {
-      const unsigned e = (unsigned)(ranks[s] >> (16 * q)) & 0xffffu, c = e >> 14;
-      order[(int64_t)c * nv_cap + cls_base[c] + (e & 0x3fffu)] = (uint32_t)(vo[s] + q);
+    for (int q = 0; q < rec_nv(r[s]); q++) {  // empty beyond the listed cells
+      vwork[vo[s] + q] = (uint32_t)(first + s);
+      vrank[vo[s] + q] = (uint8_t)q;
     }
 }
 
@@ -607,25 +575,16 @@ __global__ void __launch_bounds__(kVertexThreads) dmc_vertex_warp_kernel(CellSpa
 // exclusion go to the one-pass kernel's list.
 __global__ void __launch_bounds__(kVertexThreads, 5) dmc_vertex_setup_kernel(CellSpace space, const uint16_t* cellof, const uint8_t* vrank,
                                                                               const uint32_t* vwork, int64_t nv,
-                                                                              const uint32_t* order,
-                                                                              const unsigned* order_count,
                                                                               repr::ProjRecord* recs, uint32_t* list,
                                                                               unsigned* count,
                                                                               unsigned long long* stats) {
   __shared__ uint64_t cc[256];
-  __shared__ int64_t cls_end[4];
   for (int c = threadIdx.x; c < 256; c += blockDim.x) cc[c] = c_case_contour[c];
-  if (threadIdx.x == 0) {
-    int64_t e = 0;
-    for (int c = 0; c < 4; c++) cls_end[c] = (e += order_count[c]);
-  }
   __syncthreads();
   GridCache G;
   int f64 = 0;
-  // the vertices class by class (offsets kernel): a = position in the concatenated class lists
-  for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < nv; a += (int64_t)gridDim.x * blockDim.x) {
-    const int cls = a < cls_end[0] ? 0 : (a < cls_end[1] ? 1 : (a < cls_end[2] ? 2 : 3));
-    const int64_t vidx = order[cls * nv + (a - (cls ? cls_end[cls - 1] : 0))];
+  for (int64_t vidx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; vidx < nv;
+       vidx += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t vcell = slot_cell(cellof, vwork[vidx]);
     const int rank = vrank[vidx];
     G.load(space, vcell);
@@ -927,9 +886,8 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
   {
     // per-cell offsets and the vertex work list (needs the vertex count for its size)
     Stage t(prof, "dmc_scan", st);
-    cudaMemsetAsync(s.order_count, 0, 4 * sizeof(unsigned), st);
-    dmc_offsets_kernel<<<(unsigned)ceil_div(n, kScanTile), kScanThreads, 0, st>>>(
-        s.mask, s.rec, s.ccase, s.tile_sums, s.voff, s.qoff, s.vwork, s.vrank, s.order, s.order_count, nv);
+    dmc_offsets_kernel<<<(unsigned)ceil_div(n, kScanTile), kScanThreads, 0, st>>>(s.mask, s.rec, s.tile_sums, s.voff,
+                                                                                  s.qoff, s.vwork, s.vrank);
   }
   // per-vertex grids: whole waves of each kernel's resident blocks
   static const int r_setup = resident_blocks(dmc_vertex_setup_kernel, kVertexThreads);
@@ -944,8 +902,7 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
   {
     Stage t(prof, "dmc_vertex_setup", st);
     cudaMemsetAsync(s.fb_count, 0, 2 * sizeof(unsigned), st);
-    dmc_vertex_setup_kernel<<<vgrid(r_setup), kVertexThreads, 0, st>>>(space, s.cellof, s.vrank, s.vwork, nv,
-                                                                       s.order, s.order_count, s.proj, s.fb_list,
+    dmc_vertex_setup_kernel<<<vgrid(r_setup), kVertexThreads, 0, st>>>(space, s.cellof, s.vrank, s.vwork, nv, s.proj, s.fb_list,
                                                                        s.fb_count, s.stats);
   }
   {

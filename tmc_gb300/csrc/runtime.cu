@@ -252,8 +252,6 @@ cudaError_t dmc_vertex_scratch(Allocs& al, tmc::DmcScratch& sc, int64_t nv) {
   cudaError_t e = al.get(&rec, nv * (int64_t)tmc::kProjRecordBytes);
   sc.proj = reinterpret_cast<tmc::repr::ProjRecord*>(rec);
   if (e == cudaSuccess) e = al.get(&sc.vp, nv);
-  if (e == cudaSuccess) e = al.get(&sc.order, 4 * nv);
-  if (e == cudaSuccess) e = al.get(&sc.order_count, 4);
   if (e == cudaSuccess) e = al.get(&sc.fb_list, nv);
   if (e == cudaSuccess) e = al.get(&sc.fb_count, 2);
   if (e == cudaSuccess) e = al.get(&sc.tail_list, nv);
