@@ -153,13 +153,25 @@ __global__ void he_twin_kernel(const int32_t* faces, int64_t nf, const int2* lis
       E[r].c = 0;
       E[r].id[0] = E[r].id[1] = E[r].id[2] = E[r].id[3] = INT_MAX;
     }
+    // the P corner lists walked in lockstep: P independent loads in flight per step instead of one
+    // list after another (the pass is bound by the latency of these gathers)
+    int beg[P], len[P], maxlen = 0;
 #pragma unroll
     for (int r = 0; r < P; r++) {
-      const int a = v[r], next = v[(r + 1) % P], prev = v[(r + P - 1) % P];
-      for (int q = off[a], end = list_end(off, a, nv, nh); q < end; q++) {
-        const int2 x = list[q];
-        if (x.y == next) edge_ids_insert(E[r], x.x);
-        if (x.y == prev && prev != a) edge_ids_insert(E[(r + P - 1) % P], x.x);
+      beg[r] = off[v[r]];
+      len[r] = list_end(off, v[r], nv, nh) - beg[r];
+      maxlen = len[r] > maxlen ? len[r] : maxlen;
+    }
+    for (int t = 0; t < maxlen; t++) {
+      int2 x[P];
+#pragma unroll
+      for (int r = 0; r < P; r++) x[r] = t < len[r] ? list[beg[r] + t] : make_int2(-1, -1);
+#pragma unroll
+      for (int r = 0; r < P; r++) {
+        if (t >= len[r]) continue;
+        const int a = v[r], next = v[(r + 1) % P], prev = v[(r + P - 1) % P];
+        if (x[r].y == next) edge_ids_insert(E[r], x[r].x);
+        if (x[r].y == prev && prev != a) edge_ids_insert(E[(r + P - 1) % P], x[r].x);
       }
     }
     int tw[P];
