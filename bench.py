@@ -138,6 +138,28 @@ ROOFLINE_GROUPS = {
 }
 
 
+def link_bandwidth(torch) -> dict:
+    """Host link bandwidth right now: a pinned 256 MiB buffer copied in and out (best of three each,
+    CUDA events), in GB/s.  The link is shared with the other GPUs of the machine, so the end-to-end
+    figure is read against it."""
+    n = 64 << 20
+    h = torch.empty(n, dtype=torch.float32).pin_memory()
+    d = torch.empty(n, dtype=torch.float32, device="cuda")
+    out = {}
+    for name, dst, src in (("h2d", d, h), ("d2h", h, d)):
+        best = 0.0
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            best = max(best, 4 * n / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+        out[name] = round(best, 1)
+    del h, d
+    return out
+
+
 def algorithmic_bytes(group: str, sizes: dict, cells: int, voxels: int) -> float:
     """Algorithmic bytes of one launch of a kernel group: the field read once (4 B/voxel) for the
     classifying kernels, the mesh bytes a group emits for the others (24 B/vertex, 16 B/quad,
@@ -245,19 +267,24 @@ def run_ours(args, rank, world, local):
         mt, md = step_e(vhost, native.OUT_HOST)
         ctx_e.free(mt)
         ctx.free(md)
+    link_before = link_bandwidth(torch)
     barrier()
     d2h = 0
+    step_ms = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
+        ts = time.perf_counter()
         mt, md = step_e(vhost, native.OUT_HOST)
         d2h = (24 * mt.nr_v + 12 * mt.nr_t) + (24 * md.nr_v + 16 * md.nr_q + 12 * md.nr_t + 16 * md.nr_he +
                                                  4 * md.nr_v + 4 * md.nr_q)
         ctx_e.free(mt)
         ctx.free(md)
+        step_ms.append(round((time.perf_counter() - ts) * 1e3, 2))
     barrier()
     ctx_e.close()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e = throughput(world, cells, args.steps, e2e_s)
+    link_after = link_bandwidth(torch)
     # ---- per-stage profile (separate pass, not timed above) ----
     ctx.set_profiling(True)
     m = ctx.dmc_raw(vdev, vol.iso, native.OUT_LOCAL)  # front end alone, for its mesh sizes
@@ -316,7 +343,10 @@ def run_ours(args, rank, world, local):
                               "come from a separate sequential pass"},
         "mesh": sizes,
         "e2e": {"value": round(e2e, 4), "unit": "Gcells/s", "h2d_bytes_per_step": 2 * 4 * voxels,
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h), "step_ms": step_ms,
+                "host_link_gbs": {"before": link_before, "after": link_after,
+                                  "note": "pinned 256 MiB copies each way, measured just before and after the "
+                                          "end-to-end steps; the link is shared with the machine's other GPUs"}},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
