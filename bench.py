@@ -1003,12 +1003,17 @@ def headline_extras(args, rank, world, local):
         "workload": b["config"]["workload"], "steps": bargs.steps, "warmup": bargs.warmup, "clocks": b["clocks"]}
     sargs = argparse.Namespace(**vars(args))
     sargs.requests, sargs.rates = 256, "0.5,1.5"
+    import torch
+    link = link_bandwidth(torch)
     sv = run_serve(sargs, rank, world, local)
     fargs = argparse.Namespace(**vars(args))
     extras["fused_generation"] = run_fused(fargs, rank, world, local, steps=5, warmup=3)
     extras["serve"] = {"rates": sv["rates"], "plain_capacity_req_s": sv["config"]["plain_capacity_req_s"],
                        "requests_per_rate": sargs.requests, "workload": sv["config"]["workload"],
-                       "server_stats": sv["server_stats"], "clocks": sv["clocks"]}
+                       "server_stats": sv["server_stats"], "clocks": sv["clocks"],
+                       "host_link_gbs": link,
+                       "note": "every request's field crosses the host link in and its mesh out, on both arms; the link "
+                               "is shared with the machine's other GPUs, so both arms' latencies vary between runs"}
     return extras
 
 
