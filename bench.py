@@ -513,6 +513,13 @@ def run_batch(args, rank, world, local):
     with ClockSampler(local) as clk:
         ms_batch, launches_batch, _ = timed(batched)
         ms_plain, launches_plain, _ = timed(plain)
+    # per-stage device time of one batched call (separate pass, not timed above)
+    ctx.set_profiling(True)
+    for m in batched():
+        ctx.free(m)
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    batch_stages = {k: round(v[0], 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
     # sizes and the output bytes of one batch
     ms = batched()
     nv = sum(m.nr_v for m in ms)
@@ -550,6 +557,7 @@ def run_batch(args, rank, world, local):
                         "ms_per_step": round(ms_plain, 3), "gpu_launches": int(launches_plain),
                         "note": f"{n} sequential tmc_dmc_extract calls"},
         "batched_over_plain": round(ms_plain / ms_batch, 3),
+        "stages_ms": batch_stages,
         "e2e": {"value": round(cells / e2e_s / 1e9, 4), "unit": "Gcells/s", "h2d_bytes_per_step": 4 * voxels,
                 "d2h_bytes_per_step": int(24 * nv + 16 * nq)},
         "gpu_launches": int(launches_batch),
@@ -998,7 +1006,7 @@ def headline_extras(args, rank, world, local):
         "cells_per_batch": b["config"]["cells_per_step"], "gpu_launches_per_batch": b["gpu_launches"],
         "plain_calls": {"value": b["plain_calls"]["value"], "ms": b["plain_calls"]["ms_per_step"],
                         "gpu_launches": b["plain_calls"]["gpu_launches"]},
-        "batched_over_plain": b["batched_over_plain"], "e2e": b["e2e"],
+        "batched_over_plain": b["batched_over_plain"], "e2e": b["e2e"], "stages_ms": b["stages_ms"],
         "roofline": {k: b["roofline"][k] for k in ("achieved", "peak", "unit", "frac", "algorithmic_bytes_per_launch")},
         "workload": b["config"]["workload"], "steps": bargs.steps, "warmup": bargs.warmup, "clocks": b["clocks"]}
     sargs = argparse.Namespace(**vars(args))
