@@ -226,9 +226,11 @@ __device__ __forceinline__ void midpoint(double* v64, double* n64, int dst, int 
 // float64 midpoints run densely in midpoint_kernel (a few merging faces per warp would otherwise
 // pay the float64 pipe for the whole warp).  Each destination has one owner, and the sources are
 // never destinations (valence >= 5 vs valence 3), so the merges are independent.
+// dold: the valence-3 corners of the removed faces (merge targets and removed vertices), whose
+// images are the vertices the halfedge update re-pairs around.
 __global__ void merge_apply_kernel(HeView he, int64_t nq, const uint8_t* branch, const int32_t* own_pos,
                                    const int32_t* own_rm, uint8_t* vm_first, int32_t* vm_second, uint8_t* em,
-                                   int4* jobs, unsigned* njobs) {
+                                   int4* jobs, unsigned* njobs, uint8_t* dold) {
   const int lane = threadIdx.x & 31;
   FOR_EACH(f, nq) {
     const uint8_t br = branch[f];
@@ -243,6 +245,8 @@ __global__ void merge_apply_kernel(HeView he, int64_t nq, const uint8_t* branch,
           job = true;
           jv = make_int4(v0, v1, v3, 0);
         }
+        dold[v0] = 1;
+        dold[v2] = 1;
         vm_first[v2] = 1;
         if (own_rm[v2] == f) vm_second[v2] = v0;
       } else {
@@ -250,6 +254,8 @@ __global__ void merge_apply_kernel(HeView he, int64_t nq, const uint8_t* branch,
           job = true;
           jv = make_int4(v1, v0, v2, 0);
         }
+        dold[v1] = 1;
+        dold[v3] = 1;
         vm_first[v3] = 1;
         if (own_rm[v3] == f) vm_second[v3] = v1;
       }
@@ -313,27 +319,44 @@ __global__ void gather_vertices_kernel(const uint8_t* keep, const int32_t* idx, 
   }
 }
 
+// What the halfedge update needs from a face compaction: the removed faces' clean corners lose one
+// outgoing halfedge each (deg_old), a kept face records its old index (src) and marks the images of
+// its corners in dold as dirty (dnew).
+__device__ __forceinline__ void removed_face_degrees(const int32_t* q, int64_t f, const uint8_t* dold, int32_t* deg_old) {
+  for (int r = 0; r < 4; r++) {
+    const int x = q[4 * f + r];
+    if (!dold[x]) atomicSub(deg_old + x, 1);
+  }
+}
+
 // removeQuadrilaterals3X3Y (:1114-1137)
 __global__ void gather_quads_3x3y_kernel(const uint8_t* em, const int32_t* idx, int64_t nq, const int32_t* q,
                                          const uint8_t* vm_first, const int32_t* vm_second, int32_t* qo, int64_t cap,
-                                         unsigned* overflow) {
+                                         unsigned* overflow, const uint8_t* dold, uint8_t* dnew, int32_t* src,
+                                         int32_t* deg_old) {
   FOR_EACH(f, nq) {
-    if (em[f]) continue;
+    if (em[f]) {
+      removed_face_degrees(q, f, dold, deg_old);
+      continue;
+    }
     const int64_t o = idx[f];
     if (o < 0 || o >= cap) {
       atomicAdd(overflow, 1u);
       continue;
     }
+    src[o] = (int32_t)f;
     for (int r = 0; r < 4; r++) {
       const int x = q[4 * f + r];
-      qo[4 * o + r] = vm_first[x] ? vm_second[vm_second[x]] : vm_second[x];
+      const int y = vm_first[x] ? vm_second[vm_second[x]] : vm_second[x];
+      qo[4 * o + r] = y;
+      if (dold[x] && y >= 0) dnew[y] = 1;
     }
   }
 }
 
 // mark3333 (:1189-1322)
 __global__ void mark3333_kernel(HeView he, int64_t nq, const int32_t* val, uint8_t* p3, uint8_t* rflag,
-                                uint8_t* vm0, int32_t* vm1) {
+                                uint8_t* vm0, int32_t* vm1, uint8_t* dold) {
   FOR_EACH(f, nq) {
     if (non_manifold(he, f)) continue;
     int vq[4], fo[4], vo[4];
@@ -362,6 +385,8 @@ __global__ void mark3333_kernel(HeView he, int64_t nq, const int32_t* val, uint8
     for (int r = 0; r < 4; r++) {
       vm0[vq[r]] = 1;
       vm1[vq[r]] = vo[r];
+      dold[vq[r]] = 1;
+      dold[vo[r]] = 1;
     }
     p3[f] = 1;
     for (int r = 0; r < 4; r++) rflag[fo[r]] = 1;
@@ -371,18 +396,36 @@ __global__ void mark3333_kernel(HeView he, int64_t nq, const int32_t* val, uint8
 // removeQuadrilaterals3333 (:1340-1382)
 __global__ void gather_quads_3333_kernel(const uint8_t* rflag, const int32_t* idx, int64_t nq, const int32_t* q,
                                          const uint8_t* p3, const int32_t* vm1, const int32_t* vm2, int32_t* qo,
-                                         int64_t cap, unsigned* overflow) {
+                                         int64_t cap, unsigned* overflow, const uint8_t* dold, uint8_t* dnew,
+                                         int32_t* src, int32_t* deg_old) {
   FOR_EACH(f, nq) {
-    if (rflag[f]) continue;
+    if (rflag[f]) {
+      removed_face_degrees(q, f, dold, deg_old);
+      continue;
+    }
     const int64_t o = idx[f];
     if (o < 0 || o >= cap) {
       atomicAdd(overflow, 1u);
       continue;
     }
+    src[o] = (int32_t)f;
     for (int r = 0; r < 4; r++) {
       const int x = q[4 * f + r];
-      qo[4 * o + r] = p3[f] ? vm2[vm1[x]] : vm2[x];
+      const int y = p3[f] ? vm2[vm1[x]] : vm2[x];
+      qo[4 * o + r] = y;
+      if (dold[x] && y >= 0) dnew[y] = 1;
     }
+  }
+}
+
+// Out-degrees of the kept vertices at their new indices: carried over for the clean ones, zero for
+// the dirty ones (update_halfedges counts those).
+__global__ void carry_degrees_kernel(const uint8_t* keep, const int32_t* idx, int64_t nv, const int32_t* deg_old,
+                                     const uint8_t* dnew, int32_t* deg_new, int64_t cap) {
+  FOR_EACH(x, nv) {
+    if (!keep[x]) continue;
+    const int64_t y = idx[x];
+    if (y >= 0 && y < cap) deg_new[y] = dnew[y] ? 0 : deg_old[x];
   }
 }
 
@@ -547,6 +590,16 @@ struct HeBufs {
   HeWork w{};
   unsigned long long* nm = nullptr;
   unsigned* ovf = nullptr;
+  // incremental updates: the second set of twins, flags and degrees (swapped after each update),
+  // dirty marks before and after a pass, the new faces' old indices, handle counters
+  int32_t* twin2 = nullptr;
+  uint8_t* flag2 = nullptr;
+  int32_t* deg2 = nullptr;
+  uint8_t* dold = nullptr;
+  uint8_t* dnew = nullptr;
+  int32_t* src = nullptr;
+  HeUpdateWork u{};
+  unsigned long long* hcount = nullptr;
 };
 
 // colorFaces (:714-844) on a mesh whose halfedges are built: the inherited colours in `col` become
@@ -592,7 +645,25 @@ HeBufs halfedge_buffers(Pool& pool, int64_t NV, int64_t NQ) {
   hw.nm = pool.get<unsigned long long>(2);
   hw.w.non_manifold = hw.nm;
   hw.ovf = pool.get<unsigned>(2);
+  hw.hcount = pool.get<unsigned long long>(4);
   return hw;
+}
+
+// buffers of the incremental halfedge updates (meshes that a simplification pass changes)
+void update_buffers(Pool& pool, HeBufs& hw, int64_t NV, int64_t NQ) {
+  hw.twin2 = pool.get<int32_t>(4 * NQ);
+  hw.flag2 = pool.get<uint8_t>(4 * NQ);
+  hw.deg2 = pool.get<int32_t>(NV);
+  hw.dold = pool.get<uint8_t>(NV);
+  hw.dnew = pool.get<uint8_t>(NV);
+  hw.src = pool.get<int32_t>(NQ);
+  hw.u.drank = pool.get<int32_t>(4 * NQ);
+  hw.u.dmask = pool.get<uint8_t>(NQ);
+  hw.u.bcnt = pool.get<int32_t>(NV);
+  hw.u.boff = hw.w.off;    // the build's scratch is idle between builds
+  hw.u.blist = hw.w.list;
+  hw.u.tiles = hw.w.tiles;
+  hw.u.total = hw.w.total;
 }
 
 }  // namespace
@@ -639,13 +710,19 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     return s;
   }
   // The mesh changes only where a pass merges or removes something; a pass that changes nothing
-  // keeps `cur` as it is, and the halfedges (and out-degrees) built for it stay valid.
-  // Vertex handles are built only for the output (the passes never read them).
+  // keeps `cur` as it is, and the halfedges (and out-degrees) built for it stay valid.  A pass that
+  // changes it updates them (update_he).  Vertex handles are made only for the output (the passes
+  // never read them).
   int mesh_version = 0, he_version = -1;
   bool he_handles = false;
   auto halfedges = [&](const DmcMesh& m, bool handles) {
     if (he_version == mesh_version && (he_handles || !handles)) return;
     Stage tm(prof, "dmc_halfedges", st);
+    if (he_version == mesh_version) {  // twins and flags current: the handles alone
+      s.launches += halfedge_handles(m.quads, 4, m.nq, m.nv, hw.twin, hw.flag, hw.hv, hw.w, hw.hcount, sms, st);
+      he_handles = true;
+      return;
+    }
     cudaMemsetAsync(hw.nm, 0, 2 * sizeof(unsigned long long), st);
     HeOut ho{hw.twin, hw.flag, hw.hv};
     s.launches += build_halfedges(m.quads, 4, m.nq, m.nv, ho, hw.w, sms, st, handles);
@@ -662,6 +739,23 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   };
 
   const bool simplify = c3x3y || i3x3y || p3333;
+  if (simplify) update_buffers(pool, hw, NV, NQ);
+  // after a pass that changed the mesh (old `cur`, new `nx`; kept vertex x -> keep_idx[x], kept face
+  // g -> idx_q[g]): out-degrees, twins and flags of the new mesh from those of the old one
+  auto update_he = [&](const DmcMesh& old, const DmcMesh& nx, const uint8_t* keep_v, const int32_t* keep_idx,
+                       const int32_t* idx_q) {
+    Stage tm(prof, "dmc_halfedges", st);
+    carry_degrees_kernel<<<grid_for(old.nv, sms), 256, 0, st>>>(keep_v, keep_idx, old.nv, hw.w.deg, hw.dnew, hw.deg2,
+                                                                nx.nv);
+    HeOut ho{hw.twin2, hw.flag2, nullptr};
+    s.launches += 1 + update_halfedges(nx.quads, nx.nq, nx.nv, hw.src, idx_q, hw.dnew, hw.twin, hw.flag, ho, hw.deg2,
+                                       hw.u, sms, st);
+    std::swap(hw.twin, hw.twin2);
+    std::swap(hw.flag, hw.flag2);
+    std::swap(hw.w.deg, hw.deg2);
+    he_version = mesh_version;
+    he_handles = false;
+  };
   int32_t* val = nullptr;
   uint8_t *p = nullptr, *branch = nullptr, *vm_first = nullptr, *em = nullptr, *keep = nullptr, *keep_q = nullptr;
   int32_t *own_pos = nullptr, *own_rm = nullptr, *vm_second = nullptr, *idx = nullptr, *idx_q = nullptr;
@@ -735,8 +829,9 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     cudaMemsetAsync(vm_first, 0, cur.nv, st);
     merge_claim_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.nq, p, val, cur.colors, pass == 0, branch, own_pos, own_rm);
     cudaMemsetAsync(njobs, 0, sizeof(unsigned), st);
-    merge_apply_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.nq, branch, own_pos, own_rm, vm_first, vm_second, em, jobs,
-                                           njobs);
+    cudaMemsetAsync(hw.dold, 0, cur.nv, st);
+    merge_apply_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.nq, branch, own_pos, own_rm,
+                                           vm_first, vm_second, em, jobs, njobs, hw.dold);
     static const int r_mid = resident_blocks(midpoint_kernel, 256);  // one wave over the merge list
     midpoint_kernel<<<(unsigned)wave_grid(r_mid, sms, 1, cur.nq, 256), 256, 0, st>>>(jobs, njobs, cur.v64, cur.n64);
     s.launches += 9;
@@ -761,8 +856,9 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     void* qn = nullptr;
     if ((s.err = cudaMallocAsync(&qn, std::max<int64_t>(nq2, 1) * 4 * sizeof(int32_t), st)) != cudaSuccess) break;
     adopt(qn);
+    cudaMemsetAsync(hw.dnew, 0, std::max<int64_t>(nv2, 1), st);
     gather_quads_3x3y_kernel<<<gq, 256, 0, st>>>(em, idx_q, cur.nq, cur.quads, vm_first, vm_second, (int32_t*)qn,
-                                                  nq2, hw.ovf);
+                                                  nq2, hw.ovf, hw.dold, hw.dnew, hw.src, hw.w.deg);
     s.launches += 2;
     // the inherited colours are only read by the colour pass; they are not carried along
     retire(cur.v64);
@@ -773,8 +869,10 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     nx.nv = nv2;
     nx.nq = nq2;
     nx.quads = (int32_t*)qn;
+    const DmcMesh old = cur;
     cur = nx;
     mesh_version++;
+    update_he(old, cur, keep, idx, idx_q);
   }
   // ---- P3333 (simplify3333, :1362-1385) ----
   if (s.err == cudaSuccess && p3333 && cur.nq > 0) {
@@ -790,9 +888,11 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     cudaMemsetAsync(p3, 0, cur.nq, st);
     cudaMemsetAsync(rflag, 0, cur.nq, st);
     cudaMemsetAsync(vm0, 0, cur.nv, st);
+    cudaMemsetAsync(hw.dold, 0, cur.nv, st);
     fill_i32_kernel<<<gv, 256, 0, st>>>(vm1, cur.nv, -1);
     fill_i32_kernel<<<gv, 256, 0, st>>>(vm2, cur.nv, -1);
-    mark3333_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.nq, val, p3, rflag, vm0, vm1);
+    mark3333_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.nq, val, p3, rflag, vm0, vm1,
+                                        hw.dold);
     invert_flags_kernel<<<gv, 256, 0, st>>>(vm0, cur.nv, keep);
     s.launches += 5 + scan_flags(keep, cur.nv, idx, tiles, total, st);
     invert_flags_kernel<<<gq, 256, 0, st>>>(rflag, cur.nq, keep_q);
@@ -813,8 +913,9 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
       void* qn = nullptr;
       if ((s.err = cudaMallocAsync(&qn, std::max<int64_t>(nq2, 1) * 4 * sizeof(int32_t), st)) == cudaSuccess) {
         adopt(qn);
+        cudaMemsetAsync(hw.dnew, 0, std::max<int64_t>(nv2, 1), st);
         gather_quads_3333_kernel<<<gq, 256, 0, st>>>(rflag, idx_q, cur.nq, cur.quads, p3, vm1, vm2, (int32_t*)qn, nq2,
-                                                      hw.ovf);
+                                                      hw.ovf, hw.dold, hw.dnew, hw.src, hw.w.deg);
         s.launches += 1;
         retire(cur.v64);
         retire(cur.v);
@@ -824,8 +925,10 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
         nx.nv = nv2;
         nx.nq = nq2;
         nx.quads = (int32_t*)qn;
+        const DmcMesh old = cur;
         cur = nx;
         mesh_version++;
+        update_he(old, cur, keep, idx, idx_q);
       }
     }
   }

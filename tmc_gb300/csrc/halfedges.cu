@@ -222,6 +222,199 @@ __global__ void he_override_kernel(const int32_t* faces, int P, const int32_t* l
   }
 }
 
+// ---- incremental update after a simplification pass (quad meshes) ----
+// A pass removes quads and re-targets the corners of some kept quads.  Call a new vertex dirty when
+// it is the image of a removed vertex, of a merge target, or of a re-targeted corner: every removed
+// quad has a dirty end on each of its edges, and every re-targeted corner lands on a dirty vertex.
+// So an edge whose two ends are clean has the same halfedges before and after the pass (their
+// faces kept, in the same order), and keeps its pairing and flag; its twins only move with the
+// face compaction.  The halfedges with a dirty end are bucketed by that end (the lower one when
+// both are dirty), so all halfedges of such an edge share one bucket, and re-paired there with the
+// build's rules.  Out-degrees of clean vertices carry over (less the removed quads' corners, done
+// by the caller); those of dirty vertices are counted here.
+
+// Own twin and flag of halfedge h from its edge's halfedges (ids ascending in e): the rules of
+// he_twin_kernel and resolve_group, evaluated by every member for itself.
+__device__ __forceinline__ void group_member(const int32_t* faces, const EdgeIds& e, int h, int& tw, int& fl) {
+  tw = -1;
+  fl = 0;
+  if (e.c == 2) {
+    tw = (e.id[0] == h) ? e.id[1] : e.id[0];
+  } else if (e.c == 3) {
+    const int e0 = e.id[0], e1 = e.id[1], e2 = e.id[2];
+    const int a0 = faces[e0], a1 = faces[e1], a2 = faces[e2];
+    int p = e0, q = e1;  // the twin pair; the third member is the lone boundary halfedge
+    if (a0 != a1) {
+      p = e0; q = e1;
+    } else if (a0 != a2) {
+      p = e0; q = e2;
+    } else {
+      p = e1; q = e2;
+    }
+    fl = 2;
+    tw = (h == p) ? q : (h == q) ? p : -1;
+  } else if (e.c == 4) {
+    const int e0 = e.id[0], e1 = e.id[1], e2 = e.id[2], e3 = e.id[3];
+    // pairs (e0, e1) and (e2, e3), or (e0, e2) and (e1, e3) when e0 and e1 have one origin
+    const bool cross = faces[e0] == faces[e1];
+    const int a = cross ? e2 : e1, b = cross ? e1 : e2;
+    fl = 1;
+    tw = (h == e0) ? a : (h == a) ? e0 : (h == b) ? e3 : b;
+  }
+}
+
+// bucket of a halfedge with a dirty end (origin dirty: dout, target dirty: din)
+__device__ __forceinline__ int bucket_of(int o, int t, bool dout, bool din) {
+  return (dout && din) ? min(o, t) : (dout ? o : t);
+}
+
+// One thread per face of the new mesh (new face f comes from old face src[f]); the four halfedges'
+// loads are independent, so each thread keeps four in flight.  Halfedges whose ends are clean take
+// their twin and flag from the old mesh; the others get a rank in their bucket (drank), and the face
+// a mask of them (dmask).  Quad arrays are 16-byte aligned (pool allocations).
+__global__ void __launch_bounds__(256) he_update_kernel(const int4* faces, int64_t nf, const int32_t* src,
+                                                        const int32_t* fidx, const uint8_t* dirty,
+                                                        const int4* twin_old, const uint32_t* flag_old, int4* twin,
+                                                        uint32_t* flag, int32_t* deg, int32_t* bcnt, int32_t* drank,
+                                                        uint8_t* dmask) {
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += (int64_t)gridDim.x * blockDim.x) {
+    const int4 q = faces[f];
+    const int v[4] = {q.x, q.y, q.z, q.w};
+    bool d[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) d[r] = dirty[v[r]] != 0;
+    unsigned m = 0;
+#pragma unroll
+    for (int r = 0; r < 4; r++) m |= (unsigned)(d[r] || d[(r + 1) & 3]) << r;
+    dmask[f] = (uint8_t)m;
+    if (m != 0xFu) {
+      const int64_t s = src[f];
+      const int4 T4 = twin_old[s];
+      const uint32_t F4 = flag_old[s];
+      const int T[4] = {T4.x, T4.y, T4.z, T4.w};
+      int o[4];
+#pragma unroll
+      for (int r = 0; r < 4; r++) o[r] = (m >> r & 1) || T[r] < 0 ? -1 : 4 * fidx[T[r] >> 2] + (T[r] & 3);
+      if (m == 0) {
+        twin[f] = make_int4(o[0], o[1], o[2], o[3]);
+        flag[f] = F4;
+      } else {
+        int32_t* tw = reinterpret_cast<int32_t*>(twin + f);
+        uint8_t* fl = reinterpret_cast<uint8_t*>(flag + f);
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+          if (!(m >> r & 1)) {
+            tw[r] = o[r];
+            fl[r] = (uint8_t)(F4 >> (8 * r));
+          }
+      }
+    }
+    if (m) {
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        if (d[r]) atomicAdd(deg + v[r], 1);
+        if (m >> r & 1) drank[4 * f + r] = atomicAdd(bcnt + bucket_of(v[r], v[(r + 1) & 3], d[r], d[(r + 1) & 3]), 1);
+      }
+    }
+  }
+}
+
+// bucket entries: (halfedge, the edge's other end)
+__global__ void he_bucket_scatter_kernel(const int4* faces, int64_t nf, const uint8_t* dirty, const uint8_t* dmask,
+                                         const int32_t* drank, const int32_t* boff, int2* blist) {
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned m = dmask[f];
+    if (!m) continue;
+    const int4 q = faces[f];
+    const int v[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      if (!(m >> r & 1)) continue;
+      const int o = v[r], t = v[(r + 1) & 3];
+      const int key = bucket_of(o, t, dirty[o] != 0, dirty[t] != 0);
+      blist[boff[key] + drank[4 * f + r]] = make_int2((int)(4 * f + r), o == key ? t : o);
+    }
+  }
+}
+
+__global__ void he_pair_kernel(const int4* faces, int64_t nf, const uint8_t* dirty, const uint8_t* dmask,
+                               const int32_t* boff, int nv, const unsigned long long* total, const int2* blist,
+                               int32_t* twin, uint8_t* flag) {
+  const int n = (int)*total;
+  const int32_t* fv = reinterpret_cast<const int32_t*>(faces);
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned m = dmask[f];
+    if (!m) continue;
+    const int4 q = faces[f];
+    const int v[4] = {q.x, q.y, q.z, q.w};
+    for (int r = 0; r < 4; r++) {
+      if (!(m >> r & 1)) continue;
+      const int o = v[r], t = v[(r + 1) & 3];
+      const int key = bucket_of(o, t, dirty[o] != 0, dirty[t] != 0);
+      const int other = o == key ? t : o;
+      const int b = boff[key], end = list_end(boff, key, nv, n);
+      EdgeIds e;
+      e.c = 0;
+      e.id[0] = e.id[1] = e.id[2] = e.id[3] = INT_MAX;
+      for (int x = b; x < end; x++) {
+        const int2 y = blist[x];
+        if (y.y == other) edge_ids_insert(e, y.x);
+      }
+      const int h = (int)(4 * f + r);
+      int tw, fl;
+      group_member(fv, e, h, tw, fl);
+      twin[h] = tw;
+      flag[h] = (uint8_t)fl;
+    }
+  }
+}
+
+// Vertex handles and the count of three- and four-halfedge edges from built twins and flags: the
+// handle is the highest halfedge with the vertex as origin, overridden by the lone (twinless)
+// member of a three-halfedge edge in edge-key order (he_override_kernel).
+__global__ void he_handles_init_kernel(int32_t* hv, unsigned long long* hv_key, int64_t nv,
+                                       unsigned long long* counts) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (int64_t)gridDim.x * blockDim.x) {
+    hv[i] = -1;
+    hv_key[i] = 0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x < 3) counts[threadIdx.x] = 0;
+}
+
+template <int P>
+__global__ void he_handles_kernel(const int32_t* faces, int64_t nh, const int32_t* twin, const uint8_t* flag,
+                                  int32_t* hv, unsigned long long* hv_key, int32_t* lone,
+                                  unsigned long long* counts) {
+  unsigned long long n1 = 0, n2 = 0;
+  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
+    const int v = faces[h];
+    atomicMax(hv + v, (int32_t)h);
+    const int fl = flag[h];
+    n1 += fl == 1;
+    n2 += fl == 2;
+    if (fl == 2 && twin[h] == -1) {
+      const int64_t f = h / P;
+      const int w = faces[f * P + (h - f * P + 1) % P];
+      const unsigned long long key = ((unsigned long long)(unsigned)min(v, w) << 32) | (unsigned)max(v, w);
+      atomicMax(hv_key + v, key + 1ull);
+      lone[atomicAdd(counts + 2, 1ull)] = (int32_t)h;
+    }
+  }
+  for (int o = 16; o; o >>= 1) {
+    n1 += __shfl_down_sync(0xffffffffu, n1, o);
+    n2 += __shfl_down_sync(0xffffffffu, n2, o);
+  }
+  if ((threadIdx.x & 31) == 0 && (n1 | n2)) {
+    atomicAdd(counts + 0, n1);
+    atomicAdd(counts + 1, n2);
+  }
+}
+
+// edges with four halfedges (flag 1 on each) and with three (flag 2 on each)
+__global__ void he_group_count_kernel(const unsigned long long* counts, unsigned long long* non_manifold) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) *non_manifold = counts[0] / 4 + counts[1] / 3;
+}
+
 template <int P>
 __global__ void __launch_bounds__(256, 8) he_pack4_kernel(const int32_t* faces, const int32_t* twin, int64_t nh,
                                                           int32_t* he4, int32_t* hf) {
@@ -275,6 +468,40 @@ int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& 
     return k + 3;
   }
   return k + 2;
+}
+
+int update_halfedges(const int32_t* faces, int64_t nf, int64_t nv, const int32_t* src, const int32_t* fidx,
+                     const uint8_t* dirty, const int32_t* twin_old, const uint8_t* flag_old, HeOut& o, int32_t* deg,
+                     HeUpdateWork& w, int sms, cudaStream_t st) {
+  if (nf == 0) return 0;
+  const int4* q4 = reinterpret_cast<const int4*>(faces);
+  cudaMemsetAsync(w.bcnt, 0, (size_t)nv * sizeof(int32_t), st);
+  static const int r_upd = resident_blocks(he_update_kernel, 256);
+  he_update_kernel<<<(unsigned)wave_grid(r_upd, sms, 8, nf, 256), 256, 0, st>>>(
+      q4, nf, src, fidx, dirty, reinterpret_cast<const int4*>(twin_old), reinterpret_cast<const uint32_t*>(flag_old),
+      reinterpret_cast<int4*>(o.twin), reinterpret_cast<uint32_t*>(o.flag), deg, w.bcnt, w.drank, w.dmask);
+  int k = 1 + scan_i32(w.bcnt, nv, w.boff, w.tiles, w.total, st);
+  static const int r_sc = resident_blocks(he_bucket_scatter_kernel, 256);
+  he_bucket_scatter_kernel<<<(unsigned)wave_grid(r_sc, sms, 8, nf, 256), 256, 0, st>>>(q4, nf, dirty, w.dmask, w.drank,
+                                                                                      w.boff, w.blist);
+  static const int r_pair = resident_blocks(he_pair_kernel, 256);
+  he_pair_kernel<<<(unsigned)wave_grid(r_pair, sms, 8, nf, 256), 256, 0, st>>>(q4, nf, dirty, w.dmask, w.boff, (int)nv,
+                                                                              w.total, w.blist, o.twin, o.flag);
+  return k + 2;
+}
+
+int halfedge_handles(const int32_t* faces, int P, int64_t nf, int64_t nv, const int32_t* twin, const uint8_t* flag,
+                     int32_t* hv, HeWork& w, unsigned long long* counts, int sms, cudaStream_t st) {
+  const int64_t nh = nf * P;
+  auto grid = [&](int64_t n) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)sms * 8));
+  };
+  he_handles_init_kernel<<<grid(nv), 256, 0, st>>>(hv, w.hv_key, nv, counts);
+  if (P == 4) he_handles_kernel<4><<<grid(nh), 256, 0, st>>>(faces, nh, twin, flag, hv, w.hv_key, w.rank, counts);
+  else he_handles_kernel<3><<<grid(nh), 256, 0, st>>>(faces, nh, twin, flag, hv, w.hv_key, w.rank, counts);
+  he_override_kernel<<<(unsigned)std::max(1, sms), 256, 0, st>>>(faces, P, w.rank, counts + 2, hv, w.hv_key);
+  he_group_count_kernel<<<1, 32, 0, st>>>(counts, w.non_manifold);
+  return 4;
 }
 
 int pack_halfedges4(const int32_t* faces, int P, const int32_t* twin, int64_t nh, int32_t* he4, int32_t* hf, int sms,
