@@ -112,6 +112,17 @@ struct Allocs {
   }
 };
 
+// The ambiguous cells the TMC classification listed (one host read) and their records for the
+// counting pass to fill.
+cudaError_t tmc_ambiguous_records(tmc_ctx* ctx, Allocs& al, tmc::TmcScratch& sc, int64_t& n_amb) {
+  unsigned* h = (unsigned*)ctx->h_pinned + 320;
+  cudaError_t e = cudaMemcpyAsync(h, sc.amb_n, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return e;
+  n_amb = (int64_t)*h;
+  return al.get(&sc.amb_rec, (size_t)std::max<int64_t>(n_amb, 1) * tmc::kTmcAmbRecWords);
+}
+
 float iso_up(double iso) {
   float f = (float)iso;
   if ((double)f < iso) f = std::nextafter(f, INFINITY);
@@ -801,15 +812,15 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   TMC_CUDA(ctx, al.get(&sc.amb_n, 1));
   sc.stats = ctx->d_stats;
   TMC_CUDA(ctx, cudaMemsetAsync(sc.stats, 0, 8 * sizeof(unsigned long long), st));
-  ctx->launches += tmc::tmc_count(space, sc, ctx->sms, st, &ctx->prof, gates.data(), (int)gates.size());
+  ctx->launches += tmc::tmc_classify(space, sc, st, &ctx->prof, gates.data(), (int)gates.size());
   unsigned long long* h = (unsigned long long*)ctx->h_pinned;
+  int64_t n_amb = 0;
+  TMC_CUDA(ctx, tmc_ambiguous_records(ctx, al, sc, n_amb));
+  ctx->launches += tmc::tmc_count(space, sc, n_amb, ctx->sms, st, &ctx->prof);
   TMC_CUDA(ctx, cudaMemcpyAsync(h, sc.totals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   TMC_CUDA(ctx, cudaMemcpyAsync(h + 1, sc.stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   TMC_CUDA(ctx, cudaStreamSynchronize(st));
   const int64_t nv = (int64_t)(h[0] >> 32), nt = (int64_t)(h[0] & 0xffffffffull);
-  const int64_t n_amb = (int64_t)h[2];
-  TMC_CUDA(ctx, al.get(&sc.amb_list, n_amb));
-  TMC_CUDA(ctx, al.get(&sc.amb_count, 1));
 
   MeshPriv* mp = new (std::nothrow) MeshPriv();
   if (!mp) return fail(ctx, TMC_ERR_OOM, "host allocation failed");
@@ -830,7 +841,7 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   TMC_OWN(vo.n, 3 * nv);
   if (flags & TMC_OUT_POS_F64) TMC_OWN(vo.v64, 3 * nv);
   TMC_OWN(tris, 3 * nt);
-  ctx->launches += tmc::tmc_emit(space, sc, vo, tris, ctx->tune, st, &ctx->prof);
+  ctx->launches += tmc::tmc_emit(space, sc, n_amb, vo, tris, ctx->tune, st, &ctx->prof);
   TMC_CUDA(ctx, cudaGetLastError());
   out->nr_v = nv;
   out->nr_t = nt;
@@ -977,6 +988,7 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
   TMC_CUDA(ctx, cudaMemsetAsync(ctx->d_stats, 0, 8 * sizeof(unsigned long long), st));
   tmc::DmcScratch dsc{};
   tmc::TmcScratch tsc{};
+  int64_t n_amb_rec = 0;
   if (dmc) {
     dsc = tmc::DmcScratch{rec, voff, qoff, nullptr, tile_sums, totals, ctx->d_stats};
     dsc.mask = mask;
@@ -985,11 +997,13 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
     TMC_CUDA(ctx, al.get(&dsc.ccase, ncell));
     ctx->launches += tmc::dmc_front_count(space, dsc, st, &ctx->prof);
   } else {
-    tsc = tmc::TmcScratch{rec, voff, qoff, tile_sums, totals, ctx->d_stats, nullptr, nullptr, nullptr};
+    tsc = tmc::TmcScratch{rec, voff, qoff, tile_sums, totals, ctx->d_stats, nullptr, nullptr};
     tsc.mask = mask;
     tsc.cellof = cellof;
     TMC_CUDA(ctx, al.get(&tsc.amb_n, 1));
-    ctx->launches += tmc::tmc_count(space, tsc, ctx->sms, st, &ctx->prof);
+    ctx->launches += tmc::tmc_classify(space, tsc, st, &ctx->prof);
+    TMC_CUDA(ctx, tmc_ambiguous_records(ctx, al, tsc, n_amb_rec));
+    ctx->launches += tmc::tmc_count(space, tsc, n_amb_rec, ctx->sms, st, &ctx->prof);
   }
   std::vector<unsigned long long> toff((size_t)tiles + 1);
   unsigned long long* h = (unsigned long long*)ctx->h_pinned;
@@ -999,7 +1013,6 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
   TMC_CUDA(ctx, cudaStreamSynchronize(st));
   toff[(size_t)tiles] = h[0];
   const int64_t NV = (int64_t)(h[0] >> 32), NF = (int64_t)(h[0] & 0xffffffffull);
-  const int64_t n_amb = (int64_t)h[2];
   if (NV >= ((int64_t)1 << 31) || NF >= ((int64_t)1 << 31))
     return fail(ctx, TMC_ERR_CAPACITY, "batch output above 2^31 vertices or faces; split the batch");
   std::vector<int64_t> vb(nb + 1), fb(nb + 1);
@@ -1044,10 +1057,8 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
     ctx->launches += tmc::dmc_front_emit(space, dsc, vo, NV, faces, colors, 0, ctx->tune, st, &ctx->prof);
   } else {
     TMC_CUDA(ctx, get_shared(&faces, 3 * NF));
-    TMC_CUDA(ctx, al.get(&tsc.amb_list, n_amb));
-    TMC_CUDA(ctx, al.get(&tsc.amb_count, 1));
     tmc::TmcVertexOut vo{v, nn, v64};
-    ctx->launches += tmc::tmc_emit(space, tsc, vo, faces, ctx->tune, st, &ctx->prof);
+    ctx->launches += tmc::tmc_emit(space, tsc, n_amb_rec, vo, faces, ctx->tune, st, &ctx->prof);
   }
   TMC_CUDA(ctx, cudaGetLastError());
 

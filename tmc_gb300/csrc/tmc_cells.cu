@@ -118,18 +118,41 @@ __device__ __forceinline__ double e_vert(const double ecoord[12], int e, int d) 
   return (edge_axis(e) == d) ? ecoord[e] : (double)((edge_off(e) >> d) & 1);
 }
 
+// Triangles of p_slice: written out (3 vertex indices each), or, in the counting pass, kept as local
+// vertex codes (0..11 the crossed edges, 12..17 the inner vertices; 5 bits each) in the cell's
+// ambiguous-cell record, the first kAmbRecTris of them.  n counts them all.
+constexpr int kAmbRecTris = 36;
 struct TriSink {
-  int32_t* out;  // 3 per triangle, NULL when counting
+  int32_t* out;     // 3 per triangle, or NULL
+  uint16_t* codes;  // packed codes, or NULL
   int n;
   __device__ __forceinline__ void put(int a, int b, int c) {
     if (out) {
       out[3 * n] = a;
       out[3 * n + 1] = b;
       out[3 * n + 2] = c;
+    } else if (codes && n < kAmbRecTris) {
+      codes[n] = (uint16_t)(a | b << 5 | c << 10);
     }
     n++;
   }
 };
+
+// The record the counting pass keeps of an ambiguous cell, so that the emission pass does not run
+// p_slice again (32 words, 16-byte aligned):
+//   w[0]     slot of the cell
+//   w[1]     bits 0-7 MC case, 8-13 triangles, 14-16 inner vertices, 17 triangles beyond the record
+//            (emission runs p_slice again), 18 a singular face the reference cannot triangulate
+//   w[2..13] six float64 parameters of the inner vertices: (u, v, w) of the single inner vertex, or
+//            (u0, u1, v0, v1, w0, w1) of the six hexagon corners
+//   w[14..31] kAmbRecTris triangles as packed local codes (TriSink)
+constexpr int kAmbRecWords = 32;
+struct __align__(16) AmbRec {
+  uint32_t slot, info;
+  double prm[6];
+  uint16_t tri[kAmbRecTris];
+};
+static_assert(sizeof(AmbRec) == 4 * kAmbRecWords && kAmbRecWords == kTmcAmbRecWords, "ambiguous-cell record size");
 
 struct AmbResult {
   int inner;     // inner vertices created
@@ -138,16 +161,44 @@ struct AmbResult {
 
 // p_slice after the edge vertices (mc/MarchingCubes.cpp:418-1296), float64 throughout.
 // vid[e]: global index of the vertex on crossed edge e; ibase: index of the first inner vertex.
-// When `geo` is set, inner vertices are written there (positions/normals).
+// When `geo` is set, inner vertices are written there (positions/normals); when `prm` is set, the
+// parameters they are made from (AmbRec::prm).
 struct InnerOut {
   float* v;
   float* n;
   double* v64;
 };
 
+// Corners (u, v, w) of the inner hexagon (:831-840) from the quadratic's two roots per axis
+__device__ __forceinline__ void hex_corners(const double ui[2], const double vi[2], const double wi[2],
+                                            double hvt[6][3]) {
+  const double c[6][3] = {{ui[0], vi[0], wi[0]}, {ui[0], vi[0], wi[1]}, {ui[1], vi[0], wi[1]},
+                          {ui[1], vi[1], wi[1]}, {ui[1], vi[1], wi[0]}, {ui[0], vi[1], wi[0]}};
+#pragma unroll
+  for (int s = 0; s < 6; s++)
+#pragma unroll
+    for (int d = 0; d < 3; d++) hvt[s][d] = c[s][d];
+}
+
+// One inner vertex at local parameters (u, v, w): trilinear position and normal of the cell's corners,
+// the normal normalised (the reference's arithmetic, :1073-1083 and :1283-1293).
+__device__ __forceinline__ void inner_vertex(const double (*P)[3], const double (*N)[3], double u, double v, double w,
+                                             const InnerOut& geo, int64_t index) {
+  double ip[3], in[3];
+  cell_trilinear3(P, u, v, w, ip);
+  cell_trilinear3(N, u, v, w, in);
+  const double factor = sqrt(in[0] * in[0] + in[1] * in[1] + in[2] * in[2]);
+  const int64_t o = 3 * index;
+  for (int q = 0; q < 3; q++) {
+    geo.v[o + q] = (float)ip[q];
+    geo.n[o + q] = (float)(in[q] / factor);
+    if (geo.v64) geo.v64[o + q] = ip[q];
+  }
+}
+
 __device__ AmbResult p_slice_dev(unsigned ic, const double F[8], double iso, const double ecoord[12],
                                  const int32_t vid[12], int32_t ibase, TriSink& tri, const double (*P)[3],
-                                 const double (*N)[3], const InnerOut* geo) {
+                                 const double (*N)[3], const InnerOut* geo, double* prm) {
   AmbResult res{0, false};
   uint64_t to = ~0ull;
   int f_flag = 0;
@@ -228,8 +279,8 @@ __device__ AmbResult p_slice_dev(unsigned ic, const double F[8], double iso, con
 
   if (__popc(q_sol) == 6) {
     // tunnel or 12-vertex contour: inner hexagon (:831-1083)
-    const double hvt[6][3] = {{ui[0], vi[0], wi[0]}, {ui[0], vi[0], wi[1]}, {ui[1], vi[0], wi[1]},
-                              {ui[1], vi[1], wi[1]}, {ui[1], vi[1], wi[0]}, {ui[0], vi[1], wi[0]}};
+    double hvt[6][3];
+    hex_corners(ui, vi, wi, hvt);
     int not_tunnel = 0xF;
     if (cnt == 3) {
       const double uc_min = (ui[0] < ui[1]) ? ui[0] : ui[1];
@@ -255,19 +306,10 @@ __device__ AmbResult p_slice_dev(unsigned ic, const double F[8], double iso, con
         flat += sz;
       }
     }
-    if (geo) {
-      for (int s = 0; s < 6; s++) {
-        double hp[3], hn[3];
-        cell_trilinear3(P, hvt[s][0], hvt[s][1], hvt[s][2], hp);
-        cell_trilinear3(N, hvt[s][0], hvt[s][1], hvt[s][2], hn);
-        const double factor = sqrt(hn[0] * hn[0] + hn[1] * hn[1] + hn[2] * hn[2]);
-        const int64_t o = 3 * (int64_t)(ibase + s);
-        for (int q = 0; q < 3; q++) {
-          geo->v[o + q] = (float)hp[q];
-          geo->n[o + q] = (float)(hn[q] / factor);
-          if (geo->v64) geo->v64[o + q] = hp[q];
-        }
-      }
+    if (geo)
+      for (int s = 0; s < 6; s++) inner_vertex(P, N, hvt[s][0], hvt[s][1], hvt[s][2], *geo, (int64_t)ibase + s);
+    if (prm) {
+      prm[0] = ui[0]; prm[1] = ui[1]; prm[2] = vi[0]; prm[3] = vi[1]; prm[4] = wi[0]; prm[5] = wi[1];
     }
     res.inner = 6;
     unsigned char tcon[12];
@@ -405,17 +447,9 @@ __device__ AmbResult p_slice_dev(unsigned ic, const double F[8], double iso, con
   }
   if (pt_used) {
     res.inner = 1;
-    if (geo) {
-      double ip[3], in[3];
-      cell_trilinear3(P, uc, vc, wc, ip);
-      cell_trilinear3(N, uc, vc, wc, in);
-      const double factor = sqrt(in[0] * in[0] + in[1] * in[1] + in[2] * in[2]);
-      const int64_t o = 3 * (int64_t)ibase;
-      for (int q = 0; q < 3; q++) {
-        geo->v[o + q] = (float)ip[q];
-        geo->n[o + q] = (float)(in[q] / factor);
-        if (geo->v64) geo->v64[o + q] = ip[q];
-      }
+    if (geo) inner_vertex(P, N, uc, vc, wc, *geo, ibase);
+    if (prm) {
+      prm[0] = uc; prm[1] = vc; prm[2] = wc;
     }
   }
   return res;
@@ -429,6 +463,17 @@ struct AmbCell {
   double ec[12];
 };
 
+// corner positions and gradients (the inner vertices' trilinear sources)
+__device__ __forceinline__ void amb_geometry(const Grid& g, int i, int j, int k, double P[8][3], double N[8][3]) {
+  for (int q = 0; q < 8; q++) {
+    const int ii = i + (q & 1), jj = j + ((q >> 1) & 1), kk = k + ((q >> 2) & 1);
+    P[q][0] = g.ox + ii * g.dx;
+    P[q][1] = g.oy + jj * g.dy;
+    P[q][2] = g.oz + kk * g.dz;
+    tmc_point_gradient(g, ii, jj, kk, N[q]);
+  }
+}
+
 __device__ void load_amb_cell(const Grid& g, int i, int j, int k, const float u[8], uint32_t emask, AmbCell& a,
                               bool geometry) {
 #pragma unroll
@@ -440,15 +485,7 @@ __device__ void load_amb_cell(const Grid& g, int i, int j, int k, const float u[
       a.ec[e] = (g.iso - a.F[v0]) / (a.F[v1] - a.F[v0]);
     }
   }
-  if (geometry) {
-    for (int q = 0; q < 8; q++) {
-      const int ii = i + (q & 1), jj = j + ((q >> 1) & 1), kk = k + ((q >> 2) & 1);
-      a.P[q][0] = g.ox + ii * g.dx;
-      a.P[q][1] = g.oy + jj * g.dy;
-      a.P[q][2] = g.oz + kk * g.dz;
-      tmc_point_gradient(g, ii, jj, kk, a.N[q]);
-    }
-  }
+  if (geometry) amb_geometry(g, i, j, k, a.P, a.N);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -516,11 +553,12 @@ __global__ void __launch_bounds__(kScanThreads, 6) tmc_classify_kernel(CellSpace
 
 // Ambiguous cells from the classification's list: p_slice in counting mode (float64); the counts go
 // into the cell record and, atomically, into the cell's tile sum (one thread per listed cell, no
-// tile barrier to wait on).
+// tile barrier to wait on).  The triangles (as local codes) and the inner vertices' parameters go
+// into the cell's ambiguous-cell record, which the emission pass reads instead of running p_slice.
 __global__ void __launch_bounds__(128) tmc_amb_count_kernel(CellSpace space, const uint16_t* cellof, uint32_t* rec,
                                                             unsigned long long* tile_sums,
                                                             unsigned long long* stats, const uint32_t* list,
-                                                            const unsigned* count) {
+                                                            const unsigned* count, AmbRec* recs) {
   const unsigned na = *count;
   unsigned long long sing = 0;
   for (unsigned a = blockIdx.x * blockDim.x + threadIdx.x; a < na; a += gridDim.x * blockDim.x) {
@@ -538,9 +576,13 @@ __global__ void __launch_bounds__(128) tmc_amb_count_kernel(CellSpace space, con
     AmbCell amb;
     load_amb_cell(g, i, j, k, u, case_edge_mask(cs), amb, false);
     int32_t vid[12];
-    for (int e = 0; e < 12; e++) vid[e] = 0;
-    TriSink ts{nullptr, 0};
-    const AmbResult ar = p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, 0, ts, amb.P, amb.N, nullptr);
+    for (int e = 0; e < 12; e++) vid[e] = e;  // local codes: edges 0..11, inner vertices from 12
+    AmbRec& R = recs[a];
+    TriSink ts{nullptr, R.tri, 0};
+    const AmbResult ar = p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, 12, ts, amb.P, amb.N, nullptr, R.prm);
+    R.slot = slot;
+    R.info = cs | (uint32_t)ts.n << 8 | (uint32_t)ar.inner << 14 | (ts.n > kAmbRecTris ? (1u << 17) : 0u) |
+             (ar.error ? (1u << 18) : 0u);
     rec[slot] |= (uint32_t)ar.inner << 12 | (uint32_t)ts.n << 15 | (ar.error ? (1u << 22) : 0u);
     const unsigned long long add = ((unsigned long long)ar.inner << 32) | (unsigned long long)ts.n;
     if (add) atomicAdd(tile_sums + (slot >> kTileShift), add);
@@ -676,49 +718,73 @@ __device__ __forceinline__ void tmc_vertex_ids(const Grid& g, int i, int j, int 
   }
 }
 
-// Ambiguous cells (listed by the emit kernel): p_slice triangles and inner vertices, float64.
+// Ambiguous cells, one thread per record of the counting pass: the recorded triangles with the
+// cell's vertex indices, and the inner vertices from the recorded parameters (float64 trilinear
+// position and normal).  A cell with more triangles than its record holds runs p_slice again.
 __global__ void __launch_bounds__(128) tmc_ambiguous_kernel(CellSpace space, const CellMask* mask,
                                                             const uint16_t* cellof, const uint32_t* rec,
                                                             const int32_t* voff, const int32_t* toff,
                                                             const unsigned long long* tile_off, TmcVertexOut out,
-                                                            int32_t* tris, const uint32_t* list,
-                                                            const unsigned* count) {
+                                                            int32_t* tris, const AmbRec* recs, const unsigned* count) {
   const unsigned na = *count;
   for (unsigned a = blockIdx.x * blockDim.x + threadIdx.x; a < na; a += gridDim.x * blockDim.x) {
-    const uint32_t slot = list[a];
+    const AmbRec& R = recs[a];
+    const uint32_t info = R.info;
+    if ((info >> 18) & 1) continue;  // singular face: the reference emits nothing for the cell
+    const uint32_t slot = R.slot;
     const int64_t vcell = slot_cell(cellof, slot);
     const uint32_t r = rec[slot];
     const Grid g = space.grid_of_tile(vcell / kScanTile);
     const int32_t vfirst = (int32_t)(tile_off[g.vbase / kScanTile] >> 32);
-    const int64_t cell = vcell - g.vbase;
     int i, j, k;
-    tcell_ijk(g, cell, i, j, k);
-    float u[8];
-    tload_corners(g, i, j, k, u);
-    unsigned cs = 0;
-#pragma unroll
-    for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
+    tcell_ijk(g, vcell - g.vbase, i, j, k);
+    const unsigned cs = info & 0xFF;
     const uint32_t em = case_edge_mask(cs);
     const uint32_t own = trec_owned(r);
     int32_t vid[12];
     tmc_vertex_ids(g, i, j, k, em, own, voff[slot], vfirst, mask, rec, voff, vid);
-    TriSink ts{tris + 3 * (int64_t)toff[slot], 0};
-    AmbCell amb;
-    // corner positions and gradients serve only inner vertices, which the counting pass recorded
-    load_amb_cell(g, i, j, k, u, em, amb, trec_inner(r) > 0);
+    const int32_t ibase = voff[slot] - vfirst + __popc(own);
     // inner vertices are numbered within the volume: shift the outputs to its first vertex
     InnerOut io{out.v + 3 * (int64_t)vfirst, out.n + 3 * (int64_t)vfirst, out.v64 ? out.v64 + 3 * (int64_t)vfirst : nullptr};
-    p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, voff[slot] - vfirst + __popc(own), ts, amb.P, amb.N, &io);
+    const int nt = (int)((info >> 8) & 63), ni = (int)((info >> 14) & 7);
+    int32_t* t = tris + 3 * (int64_t)toff[slot];
+    if ((info >> 17) & 1) {
+      float u[8];
+      tload_corners(g, i, j, k, u);
+      AmbCell amb;
+      load_amb_cell(g, i, j, k, u, em, amb, ni > 0);
+      TriSink ts{t, nullptr, 0};
+      p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, ibase, ts, amb.P, amb.N, &io, nullptr);
+      continue;
+    }
+    for (int q = 0; q < nt; q++) {
+      const unsigned code = R.tri[q];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const int x = (int)((code >> (5 * c)) & 31u);
+        t[3 * q + c] = x < 12 ? vid[x] : ibase + (x - 12);
+      }
+    }
+    if (ni) {
+      double P[8][3], N[8][3];
+      amb_geometry(g, i, j, k, P, N);
+      if (ni == 1) {
+        inner_vertex(P, N, R.prm[0], R.prm[1], R.prm[2], io, ibase);
+      } else {
+        const double ui[2] = {R.prm[0], R.prm[1]}, vi[2] = {R.prm[2], R.prm[3]}, wi[2] = {R.prm[4], R.prm[5]};
+        double hvt[6][3];
+        hex_corners(ui, vi, wi, hvt);
+        for (int q = 0; q < 6; q++) inner_vertex(P, N, hvt[q][0], hvt[q][1], hvt[q][2], io, (int64_t)ibase + q);
+      }
+    }
   }
 }
 
-// One active cell: its owned edge vertices and (unambiguous case) its table triangles; ambiguous
-// cells go to the list of the float64 pass.
+// One active cell: its owned edge vertices and (unambiguous case) its table triangles.
 template <bool kPos64>
 __device__ __forceinline__ void emit_cell(const Grid& g, int32_t vfirst, uint32_t slot, int64_t vcell,
                                           const CellMask* mask, const uint32_t* rec, const int32_t* voff,
-                                          const int32_t* toff, const TmcVertexOut& out, int32_t* tris,
-                                          uint32_t* amb_list, unsigned* amb_count) {
+                                          const int32_t* toff, const TmcVertexOut& out, int32_t* tris) {
   const int64_t cell = vcell - g.vbase;
   const uint32_t r = rec[slot];
   int i, j, k;
@@ -742,11 +808,8 @@ __device__ __forceinline__ void emit_cell(const Grid& g, int32_t vfirst, uint32_
       edge_vertex_f32(g, i, j, k, e, u, out, vbase + rank, inv, inv2);
     }
   }
-  if ((r >> 21) & 1) {
-    // ambiguous: triangles and inner vertices in a separate float64 pass
-    if (!((r >> 22) & 1)) amb_list[atomicAdd(amb_count, 1u)] = slot;
-    return;
-  }
+  // ambiguous: triangles and inner vertices from the cell's ambiguous-cell record (tmc_ambiguous_kernel)
+  if ((r >> 21) & 1) return;
   int32_t vid[12];
   tmc_vertex_ids(g, i, j, k, em, own, vbase, vfirst, mask, rec, voff, vid);
   TriSink ts{tris + 3 * (int64_t)toff[slot], 0};
@@ -771,8 +834,7 @@ __global__ void __launch_bounds__(kEmitThreads, 4) tmc_emit_kernel(CellSpace spa
                                                                    const uint16_t* cellof, const uint32_t* rec,
                                                                    const int32_t* voff, const int32_t* toff,
                                                                    const unsigned long long* tile_off,
-                                                                   TmcVertexOut out, int32_t* tris,
-                                                                   uint32_t* amb_list, unsigned* amb_count) {
+                                                                   TmcVertexOut out, int32_t* tris) {
   constexpr int kWarps = kEmitThreads / 32;
   __shared__ uint32_t queue[kWarps][64];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -800,7 +862,7 @@ __global__ void __launch_bounds__(kEmitThreads, 4) tmc_emit_kernel(CellSpace spa
         // the cell's volume: read in place (a batch's grid table, or the launch parameter)
         const Grid& g = kBatch ? space.grids[__ldg(space.tile_vol + vcell / kScanTile)] : space.one;
         const int32_t vfirst = kBatch ? (int32_t)(tile_off[g.vbase / kScanTile] >> 32) : 0;
-        emit_cell<kPos64>(g, vfirst, slot, vcell, mask, rec, voff, toff, out, tris, amb_list, amb_count);
+        emit_cell<kPos64>(g, vfirst, slot, vcell, mask, rec, voff, toff, out, tris);
       }
       __syncwarp();
       const int rest = qn - take;  // at most 31: move them to the front
@@ -819,9 +881,8 @@ __global__ void __launch_bounds__(kEmitThreads, 4) tmc_emit_kernel(CellSpace spa
 // ------------------------------------------------------------------------------------------
 int64_t tmc_tiles(const CellSpace& space) { return ceil_div(space.n, kScanTile); }
 
-int tmc_count(const CellSpace& space, TmcScratch& s, int sms, cudaStream_t st, Prof* prof, const TileGate* gates,
-              int ngates) {
-  const int64_t n = space.n;
+int tmc_classify(const CellSpace& space, TmcScratch& s, cudaStream_t st, Prof* prof, const TileGate* gates,
+                 int ngates) {
   const int64_t tiles = tmc_tiles(space);
   // the ambiguous-cell list lives in toff until the offsets kernel overwrites it
   uint32_t* amb_cells = reinterpret_cast<uint32_t*>(s.toff);
@@ -848,30 +909,36 @@ int tmc_count(const CellSpace& space, TmcScratch& s, int sms, cudaStream_t st, P
       t0 = std::max(t0, t1);
     }
   }
-  {
+  return k;
+}
+
+int tmc_count(const CellSpace& space, TmcScratch& s, int64_t n_amb, int sms, cudaStream_t st, Prof* prof) {
+  const int64_t tiles = tmc_tiles(space);
+  const uint32_t* amb_cells = reinterpret_cast<const uint32_t*>(s.toff);
+  int k = 0;
+  if (n_amb > 0) {
     Stage ta(prof, "tmc_amb_count", st);
-    // whole waves; the list length is only known on the device, so the grid follows the cell count
     static const int r_amb = resident_blocks(tmc_amb_count_kernel, 128);
-    tmc_amb_count_kernel<<<(unsigned)wave_grid(r_amb, sms, 16, ceil_div(n, 64), 128), 128, 0,
-                           st>>>(space, s.cellof, s.rec, s.tile_sums, s.stats, amb_cells, s.amb_n);
+    tmc_amb_count_kernel<<<(unsigned)wave_grid(r_amb, sms, 16, n_amb, 128), 128, 0, st>>>(
+        space, s.cellof, s.rec, s.tile_sums, s.stats, amb_cells, s.amb_n, reinterpret_cast<AmbRec*>(s.amb_rec));
+    k++;
   }
   Stage t(prof, "tmc_scan", st);
   scan_tile_sums_kernel<<<1, 1024, 0, st>>>(s.tile_sums, tiles, s.totals);
   tmc_offsets_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(s.mask, s.rec, s.tile_sums, s.voff, s.toff);
-  return k + 3;
+  return k + 2;
 }
 
-int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tris, const Tuning& tu, cudaStream_t st,
-             Prof* prof) {
+int tmc_emit(const CellSpace& space, TmcScratch& s, int64_t n_amb, TmcVertexOut vo, int32_t* tris, const Tuning& tu,
+             cudaStream_t st, Prof* prof) {
   const int sms = tu.sms;
   {
     Stage t(prof, "tmc_emit", st);
     const int64_t blocks = std::max<int64_t>(
         1, std::min<int64_t>(ceil_div(space.n, 32 * (kEmitThreads / 32)), (int64_t)sms * tu.emit_blocks_per_sm));
-    cudaMemsetAsync(s.amb_count, 0, sizeof(unsigned), st);
 #define TMC_EMIT(B, P)                                                                                       \
   tmc_emit_kernel<B, P><<<(unsigned)blocks, kEmitThreads, 0, st>>>(space, s.mask, s.cellof, s.rec, s.voff, s.toff, \
-                                                                  s.tile_sums, vo, tris, s.amb_list, s.amb_count)
+                                                                  s.tile_sums, vo, tris)
     const bool pos64 = vo.v64 != nullptr;
     if (space.grids) {
       if (pos64) TMC_EMIT(true, true);
@@ -882,9 +949,12 @@ int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tr
     }
 #undef TMC_EMIT
   }
+  if (n_amb == 0) return 1;
   Stage t2(prof, "tmc_ambiguous", st);
-  tmc_ambiguous_kernel<<<(unsigned)std::max<int64_t>(1, (int64_t)sms * 8), 128, 0, st>>>(
-      space, s.mask, s.cellof, s.rec, s.voff, s.toff, s.tile_sums, vo, tris, s.amb_list, s.amb_count);
+  static const int r_amb = resident_blocks(tmc_ambiguous_kernel, 128);
+  tmc_ambiguous_kernel<<<(unsigned)wave_grid(r_amb, sms, 8, n_amb, 128), 128, 0, st>>>(
+      space, s.mask, s.cellof, s.rec, s.voff, s.toff, s.tile_sums, vo, tris, reinterpret_cast<const AmbRec*>(s.amb_rec),
+      s.amb_n);
   return 2;
 }
 

@@ -14,6 +14,8 @@ struct TmcVertexOut {
   double* v64;  // optional
 };
 
+constexpr int kTmcAmbRecWords = 32;
+
 struct TmcScratch {
   uint32_t* rec;
   int32_t* voff;
@@ -21,11 +23,11 @@ struct TmcScratch {
   unsigned long long* tile_sums;
   unsigned long long* totals;
   unsigned long long* stats;
-  uint32_t* amb_list;   // ambiguous cells with triangles, filled by the emit kernel
-  unsigned* amb_count;
-  unsigned* amb_n;      // ambiguous cells listed by the classification (count)
+  unsigned* amb_n;      // ambiguous cells listed by the classification
+  uint32_t* amb_rec;    // kTmcAmbRecWords words per ambiguous cell: what the counting pass keeps of
+                        // its p_slice for the emission pass (tmc_cells.cu, AmbRec)
   // listed cells (common.cuh): rec, voff and toff hold one entry per listed cell at its slot, the
-  // ambiguous lists hold slots
+  // ambiguous-cell list holds slots
   CellMask* mask;       // per 32 cells of the space
   uint16_t* cellof;     // per slot: in-tile offset of the listed cell
 };
@@ -33,10 +35,14 @@ struct TmcScratch {
 // Per-cell scratch is indexed in the cell space; triangles hold vertex indices within their own
 // volume, and the volumes' vertices and triangles follow one another in the outputs.
 int64_t tmc_tiles(const CellSpace& space);
-// gates: as dmc_front_count's (classification of a host field arriving in slabs)
-int tmc_count(const CellSpace& space, TmcScratch& s, int sms, cudaStream_t st, Prof* prof = nullptr,
-              const TileGate* gates = nullptr, int ngates = 0);
-int tmc_emit(const CellSpace& space, TmcScratch& s, TmcVertexOut vo, int32_t* tris, const Tuning& tu, cudaStream_t st,
-             Prof* prof = nullptr);
+// Classification: records of the crossed cells and the list of the ambiguous ones, whose number it
+// leaves in *s.amb_n.  gates: as dmc_front_count's (classification of a host field arriving in slabs).
+int tmc_classify(const CellSpace& space, TmcScratch& s, cudaStream_t st, Prof* prof = nullptr,
+                 const TileGate* gates = nullptr, int ngates = 0);
+// The ambiguous cells' counts (p_slice, float64) into their records and s.amb_rec (n_amb records,
+// n_amb = *s.amb_n), then the vertex and triangle offsets.
+int tmc_count(const CellSpace& space, TmcScratch& s, int64_t n_amb, int sms, cudaStream_t st, Prof* prof = nullptr);
+int tmc_emit(const CellSpace& space, TmcScratch& s, int64_t n_amb, TmcVertexOut vo, int32_t* tris, const Tuning& tu,
+             cudaStream_t st, Prof* prof = nullptr);
 
 }  // namespace tmc
