@@ -145,15 +145,32 @@ __global__ void color_reduce_kernel(HeView he, uint8_t* col, const int32_t* list
 // vertexValence (:847-871): outgoing halfedges, +1 at the origin of a boundary halfedge's next.
 // The outgoing count is the out-degree the halfedge build just counted; only boundary halfedges
 // (rare) add with atomics.
-__global__ void valence_boundary_kernel(HeView he, int64_t nh, int32_t* val) {
-  FOR_EACH(h, nh) {
-    if (he_twin(he, h) == -1) atomicAdd(val + he_origin(he, he_next(h)), 1);
+// One thread per face (16-byte twin loads; the corners only for a face with a boundary halfedge);
+// alive: the live faces (all when NULL).  A caller's quads need not be 16-byte aligned.
+__global__ void valence_boundary_kernel(HeView he, int64_t nq, int32_t* val, const uint8_t* alive) {
+  const bool vec = ((reinterpret_cast<uintptr_t>(he.q) | reinterpret_cast<uintptr_t>(he.twin)) & 15) == 0;
+  FOR_EACH(f, nq) {
+    if (alive && !alive[f]) continue;
+    const int4 t = vec ? reinterpret_cast<const int4*>(he.twin)[f]
+                       : make_int4(he.twin[4 * f], he.twin[4 * f + 1], he.twin[4 * f + 2], he.twin[4 * f + 3]);
+    if (t.x != -1 && t.y != -1 && t.z != -1 && t.w != -1) continue;
+    const int4 q = vec ? reinterpret_cast<const int4*>(he.q)[f]
+                       : make_int4(he.q[4 * f], he.q[4 * f + 1], he.q[4 * f + 2], he.q[4 * f + 3]);
+    // a boundary halfedge adds one at the origin of its next, the following corner
+    if (t.x == -1) atomicAdd(val + q.y, 1);
+    if (t.y == -1) atomicAdd(val + q.z, 1);
+    if (t.z == -1) atomicAdd(val + q.w, 1);
+    if (t.w == -1) atomicAdd(val + q.x, 1);
   }
 }
 
 // mark3X3Y (:889-913)
-__global__ void mark3x3y_kernel(const int32_t* q, int64_t nq, const int32_t* val, uint8_t* p) {
+__global__ void mark3x3y_kernel(const int32_t* q, int64_t nq, const int32_t* val, uint8_t* p, const uint8_t* alive) {
   FOR_EACH(f, nq) {
+    if (!alive[f]) {
+      p[f] = 0;
+      continue;
+    }
     const int a = val[q[4 * f]], b = val[q[4 * f + 1]], c = val[q[4 * f + 2]], d = val[q[4 * f + 3]];
     p[f] = (a == 3 && b >= 5 && c == 3 && d >= 5) || (a >= 5 && b == 3 && c >= 5 && d == 3);
   }
@@ -226,11 +243,11 @@ __device__ __forceinline__ void midpoint(double* v64, double* n64, int dst, int 
 // float64 midpoints run densely in midpoint_kernel (a few merging faces per warp would otherwise
 // pay the float64 pipe for the whole warp).  Each destination has one owner, and the sources are
 // never destinations (valence >= 5 vs valence 3), so the merges are independent.
-// dold: the valence-3 corners of the removed faces (merge targets and removed vertices), whose
-// images are the vertices the halfedge update re-pairs around.
+// dold: the valence-3 corners of the removed faces (merge targets and removed vertices), the
+// vertices the halfedge repair re-pairs around; valive: the removed vertices die.
 __global__ void merge_apply_kernel(HeView he, int64_t nq, const uint8_t* branch, const int32_t* own_pos,
                                    const int32_t* own_rm, uint8_t* vm_first, int32_t* vm_second, uint8_t* em,
-                                   int4* jobs, unsigned* njobs, uint8_t* dold) {
+                                   int4* jobs, unsigned* njobs, uint8_t* dold, uint8_t* valive) {
   const int lane = threadIdx.x & 31;
   FOR_EACH(f, nq) {
     const uint8_t br = branch[f];
@@ -248,6 +265,7 @@ __global__ void merge_apply_kernel(HeView he, int64_t nq, const uint8_t* branch,
         dold[v0] = 1;
         dold[v2] = 1;
         vm_first[v2] = 1;
+        valive[v2] = 0;
         if (own_rm[v2] == f) vm_second[v2] = v0;
       } else {
         if (own_pos[v1] == f) {
@@ -257,6 +275,7 @@ __global__ void merge_apply_kernel(HeView he, int64_t nq, const uint8_t* branch,
         dold[v1] = 1;
         dold[v3] = 1;
         vm_first[v3] = 1;
+        valive[v3] = 0;
         if (own_rm[v3] == f) vm_second[v3] = v1;
       }
     }
@@ -294,9 +313,6 @@ __global__ void float_outputs_kernel(const double* v64, const double* n64, int64
 // ---------------------------------------------------------------------------------------------
 // compaction helpers
 // ---------------------------------------------------------------------------------------------
-__global__ void invert_flags_kernel(const uint8_t* in, int64_t n, uint8_t* out) {
-  FOR_EACH(i, n) out[i] = !in[i];
-}
 
 // removeVertices3X3Y / removeVertices3333 (:1096-1112, :1324-1338): kept vertices move to their
 // new index, which becomes their map entry.  One thread per vertex component (x, y or z of the
@@ -319,46 +335,50 @@ __global__ void gather_vertices_kernel(const uint8_t* keep, const int32_t* idx, 
   }
 }
 
-// What the halfedge update needs from a face compaction: the removed faces' clean corners lose one
-// outgoing halfedge each (deg_old), a kept face records its old index (src) and marks the images of
-// its corners in dold as dirty (dnew).
-__device__ __forceinline__ void removed_face_degrees(const int32_t* q, int64_t f, const uint8_t* dold, int32_t* deg_old) {
+// A killed face's corners that stay clean lose one outgoing halfedge each.
+__device__ __forceinline__ void killed_face_degrees(const int32_t* q, int64_t f, const uint8_t* dold, int32_t* deg) {
   for (int r = 0; r < 4; r++) {
     const int x = q[4 * f + r];
-    if (!dold[x]) atomicSub(deg_old + x, 1);
+    if (!dold[x]) atomicSub(deg + x, 1);
   }
 }
 
-// removeQuadrilaterals3X3Y (:1114-1137)
-__global__ void gather_quads_3x3y_kernel(const uint8_t* em, const int32_t* idx, int64_t nq, const int32_t* q,
-                                         const uint8_t* vm_first, const int32_t* vm_second, int32_t* qo, int64_t cap,
-                                         unsigned* overflow, const uint8_t* dold, uint8_t* dnew, int32_t* src,
-                                         int32_t* deg_old) {
+// Marks a live face's corner x, now y, for the halfedge repair: y is dirty when x was touched by the
+// pass (dold), and then its out-degree is recounted from zero.
+__device__ __forceinline__ void touch_corner(int x, int y, const uint8_t* dold, uint8_t* dirty, int32_t* deg) {
+  if (dold[x] && y >= 0) {
+    dirty[y] = 1;
+    deg[y] = 0;
+  }
+}
+
+// removeVertices3X3Y + removeQuadrilaterals3X3Y (:1096-1137) in place: the merged faces die, the
+// corners on removed vertices move to their merge target (which a merge always keeps: the faces
+// around a valence-3 vertex are pairwise adjacent and no two adjacent faces merge in one pass).
+// Faces and vertices keep their indices; the compaction runs once after the last pass.
+__global__ void apply_3x3y_kernel(int32_t* q, int64_t nq, uint8_t* alive, const uint8_t* em, const uint8_t* vm_first,
+                                  const int32_t* vm_second, const uint8_t* dold, uint8_t* dirty, int32_t* deg) {
   FOR_EACH(f, nq) {
+    if (!alive[f]) continue;
     if (em[f]) {
-      removed_face_degrees(q, f, dold, deg_old);
+      alive[f] = 0;
+      killed_face_degrees(q, f, dold, deg);
       continue;
     }
-    const int64_t o = idx[f];
-    if (o < 0 || o >= cap) {
-      atomicAdd(overflow, 1u);
-      continue;
-    }
-    src[o] = (int32_t)f;
     for (int r = 0; r < 4; r++) {
       const int x = q[4 * f + r];
-      const int y = vm_first[x] ? vm_second[vm_second[x]] : vm_second[x];
-      qo[4 * o + r] = y;
-      if (dold[x] && y >= 0) dnew[y] = 1;
+      const int y = vm_first[x] ? vm_second[x] : x;
+      if (y != x) q[4 * f + r] = y;
+      touch_corner(x, y, dold, dirty, deg);
     }
   }
 }
 
 // mark3333 (:1189-1322)
 __global__ void mark3333_kernel(HeView he, int64_t nq, const int32_t* val, uint8_t* p3, uint8_t* rflag,
-                                uint8_t* vm0, int32_t* vm1, uint8_t* dold) {
+                                uint8_t* vm0, int32_t* vm1, uint8_t* dold, const uint8_t* alive, uint8_t* valive) {
   FOR_EACH(f, nq) {
-    if (non_manifold(he, f)) continue;
+    if (!alive[f] || non_manifold(he, f)) continue;
     int vq[4], fo[4], vo[4];
     for (int r = 0; r < 4; r++) vq[r] = he_origin(he, 4 * f + r);
     if (val[vq[0]] != 3 || val[vq[1]] != 3 || val[vq[2]] != 3 || val[vq[3]] != 3) continue;
@@ -387,45 +407,48 @@ __global__ void mark3333_kernel(HeView he, int64_t nq, const int32_t* val, uint8
       vm1[vq[r]] = vo[r];
       dold[vq[r]] = 1;
       dold[vo[r]] = 1;
+      valive[vq[r]] = 0;
     }
     p3[f] = 1;
     for (int r = 0; r < 4; r++) rflag[fo[r]] = 1;
   }
 }
 
-// removeQuadrilaterals3333 (:1340-1382)
-__global__ void gather_quads_3333_kernel(const uint8_t* rflag, const int32_t* idx, int64_t nq, const int32_t* q,
-                                         const uint8_t* p3, const int32_t* vm1, const int32_t* vm2, int32_t* qo,
-                                         int64_t cap, unsigned* overflow, const uint8_t* dold, uint8_t* dnew,
-                                         int32_t* src, int32_t* deg_old) {
+// removeVertices3333 + removeQuadrilaterals3333 (:1324-1382) in place: the four neighbours of a
+// marked face die and its corners move to the neighbours' far vertices (kept: their valence is not 3).
+__global__ void apply_3333_kernel(int32_t* q, int64_t nq, uint8_t* alive, const uint8_t* rflag, const uint8_t* p3,
+                                  const int32_t* vm1, const uint8_t* dold, uint8_t* dirty, int32_t* deg) {
   FOR_EACH(f, nq) {
+    if (!alive[f]) continue;
     if (rflag[f]) {
-      removed_face_degrees(q, f, dold, deg_old);
+      alive[f] = 0;
+      killed_face_degrees(q, f, dold, deg);
       continue;
     }
+    const bool moved = p3[f] != 0;
+    for (int r = 0; r < 4; r++) {
+      const int x = q[4 * f + r];
+      const int y = moved ? vm1[x] : x;
+      if (y != x) q[4 * f + r] = y;
+      touch_corner(x, y, dold, dirty, deg);
+    }
+  }
+}
+
+// The live faces at their compacted indices, corners renumbered (vertex x -> vmap[x]); src[o]: the
+// face's index before.
+__global__ void gather_live_quads_kernel(const uint8_t* alive, const int32_t* idx, int64_t nq, const int32_t* q,
+                                         const int32_t* vmap, int32_t* qo, int32_t* src, int64_t cap,
+                                         unsigned* overflow) {
+  FOR_EACH(f, nq) {
+    if (!alive[f]) continue;
     const int64_t o = idx[f];
     if (o < 0 || o >= cap) {
       atomicAdd(overflow, 1u);
       continue;
     }
     src[o] = (int32_t)f;
-    for (int r = 0; r < 4; r++) {
-      const int x = q[4 * f + r];
-      const int y = p3[f] ? vm2[vm1[x]] : vm2[x];
-      qo[4 * o + r] = y;
-      if (dold[x] && y >= 0) dnew[y] = 1;
-    }
-  }
-}
-
-// Out-degrees of the kept vertices at their new indices: carried over for the clean ones, zero for
-// the dirty ones (update_halfedges counts those).
-__global__ void carry_degrees_kernel(const uint8_t* keep, const int32_t* idx, int64_t nv, const int32_t* deg_old,
-                                     const uint8_t* dnew, int32_t* deg_new, int64_t cap) {
-  FOR_EACH(x, nv) {
-    if (!keep[x]) continue;
-    const int64_t y = idx[x];
-    if (y >= 0 && y < cap) deg_new[y] = dnew[y] ? 0 : deg_old[x];
+    for (int r = 0; r < 4; r++) qo[4 * o + r] = vmap[q[4 * f + r]];
   }
 }
 
@@ -590,11 +613,8 @@ struct HeBufs {
   HeWork w{};
   unsigned long long* nm = nullptr;
   unsigned* ovf = nullptr;
-  // incremental updates: the second set of twins, flags and degrees (swapped after each update),
-  // dirty marks before and after a pass, the new faces' old indices, handle counters
-  int32_t* twin2 = nullptr;
-  uint8_t* flag2 = nullptr;
-  int32_t* deg2 = nullptr;
+  // repairs after the simplification passes: vertices a pass touched (dold) and the dirty ones
+  // (dnew); the compacted faces' indices before (src); handle counters
   uint8_t* dold = nullptr;
   uint8_t* dnew = nullptr;
   int32_t* src = nullptr;
@@ -623,10 +643,11 @@ int color_faces(const HeView& he, uint8_t* col, int64_t nq, Pool& pool, int sms,
 }
 
 // vertexValence (:847-871): the out-degrees of the halfedge build plus the boundary corrections
+// (alive: the live faces, all when NULL)
 int vertex_valence(const HeView& he, const int32_t* deg, int64_t nv, int64_t nq, int32_t* val, int sms,
-                   cudaStream_t st) {
+                   cudaStream_t st, const uint8_t* alive = nullptr) {
   cudaMemcpyAsync(val, deg, nv * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
-  valence_boundary_kernel<<<grid_for(std::max<int64_t>(4 * nq, 1), sms), 256, 0, st>>>(he, 4 * nq, val);
+  valence_boundary_kernel<<<grid_for(std::max<int64_t>(nq, 1), sms), 256, 0, st>>>(he, nq, val, alive);
   return 1;
 }
 
@@ -649,19 +670,17 @@ HeBufs halfedge_buffers(Pool& pool, int64_t NV, int64_t NQ) {
   return hw;
 }
 
-// buffers of the incremental halfedge updates (meshes that a simplification pass changes)
+// buffers of the halfedge repairs and of the final compaction
 void update_buffers(Pool& pool, HeBufs& hw, int64_t NV, int64_t NQ) {
-  hw.twin2 = pool.get<int32_t>(4 * NQ);
-  hw.flag2 = pool.get<uint8_t>(4 * NQ);
-  hw.deg2 = pool.get<int32_t>(NV);
   hw.dold = pool.get<uint8_t>(NV);
   hw.dnew = pool.get<uint8_t>(NV);
   hw.src = pool.get<int32_t>(NQ);
   hw.u.drank = pool.get<int32_t>(4 * NQ);
   hw.u.dmask = pool.get<uint8_t>(NQ);
   hw.u.bcnt = pool.get<int32_t>(NV);
-  hw.u.boff = hw.w.off;    // the build's scratch is idle between builds
+  hw.u.boff = hw.w.off;    // the build's scratch is idle after the one build
   hw.u.blist = hw.w.list;
+  hw.u.bkey = pool.get<int32_t>(4 * NQ);
   hw.u.tiles = hw.w.tiles;
   hw.u.total = hw.w.total;
 }
@@ -696,105 +715,30 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   const bool c3x3y = flags & TMC_DMC_P3X3Y_COLOR, i3x3y = flags & TMC_DMC_P3X3Y_ISOLATED,
              p3333 = flags & TMC_DMC_P3333, want_t = flags & TMC_OUT_TRIANGLES, want_he = flags & TMC_OUT_HALFEDGES;
   if (!(c3x3y || i3x3y || p3333 || want_t || want_he)) return s;
+  // the repairs and handles read quads and flags 4 at a time: front-end meshes are 16-byte aligned
+  if (reinterpret_cast<uintptr_t>(in.quads) & 15) {
+    s.err = cudaErrorInvalidValue;
+    return s;
+  }
   Pool pool{st};
   const int64_t NV = std::max<int64_t>(in.nv, 1), NQ = std::max<int64_t>(in.nq, 1);
 
-  // working mesh (double buffered)
   DmcMesh cur = in;
   HeBufs hw = halfedge_buffers(pool, NV, NQ);
-  unsigned long long* tiles = pool.get<unsigned long long>(scan_tiles(4 * NQ) + 2);
-  if (hw.ovf) cudaMemsetAsync(hw.ovf, 0, 2 * sizeof(unsigned), st);
+  unsigned long long* tiles = pool.get<unsigned long long>(scan_tiles(std::max(NV, NQ)) + 2);
   unsigned long long* total = pool.get<unsigned long long>(2);
   if (pool.err) {
     s.err = pool.err;
     return s;
   }
-  // The mesh changes only where a pass merges or removes something; a pass that changes nothing
-  // keeps `cur` as it is, and the halfedges (and out-degrees) built for it stay valid.  A pass that
-  // changes it updates them (update_he).  Vertex handles are made only for the output (the passes
-  // never read them).
-  int mesh_version = 0, he_version = -1;
-  bool he_handles = false;
-  auto halfedges = [&](const DmcMesh& m, bool handles) {
-    if (he_version == mesh_version && (he_handles || !handles)) return;
+  if (hw.ovf) cudaMemsetAsync(hw.ovf, 0, 2 * sizeof(unsigned), st);
+  const unsigned gq = grid_for(NQ, sms), gv = grid_for(NV, sms);
+  const bool simplify = (c3x3y || i3x3y || p3333) && in.nq > 0;
+  auto build_he = [&](bool handles) {
     Stage tm(prof, "dmc_halfedges", st);
-    if (he_version == mesh_version) {  // twins and flags current: the handles alone
-      s.launches += halfedge_handles(m.quads, 4, m.nq, m.nv, hw.twin, hw.flag, hw.hv, hw.w, hw.hcount, sms, st);
-      he_handles = true;
-      return;
-    }
     cudaMemsetAsync(hw.nm, 0, 2 * sizeof(unsigned long long), st);
     HeOut ho{hw.twin, hw.flag, hw.hv};
-    s.launches += build_halfedges(m.quads, 4, m.nq, m.nv, ho, hw.w, sms, st, handles);
-    he_version = mesh_version;
-    he_handles = handles;
-  };
-  // both compaction totals of a pass (kept vertices in total[0], kept quads in total[1]), one host
-  // synchronisation
-  auto read_totals = [&](int64_t& nv2, int64_t& nq2) {
-    cudaMemcpyAsync(h_cnt, total, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
-    cudaStreamSynchronize(st);
-    nv2 = (int64_t)h_cnt[0];
-    nq2 = (int64_t)h_cnt[1];
-  };
-
-  const bool simplify = c3x3y || i3x3y || p3333;
-  if (simplify) update_buffers(pool, hw, NV, NQ);
-  // after a pass that changed the mesh (old `cur`, new `nx`; kept vertex x -> keep_idx[x], kept face
-  // g -> idx_q[g]): out-degrees, twins and flags of the new mesh from those of the old one
-  auto update_he = [&](const DmcMesh& old, const DmcMesh& nx, const uint8_t* keep_v, const int32_t* keep_idx,
-                       const int32_t* idx_q) {
-    Stage tm(prof, "dmc_halfedges", st);
-    carry_degrees_kernel<<<grid_for(old.nv, sms), 256, 0, st>>>(keep_v, keep_idx, old.nv, hw.w.deg, hw.dnew, hw.deg2,
-                                                                nx.nv);
-    HeOut ho{hw.twin2, hw.flag2, nullptr};
-    s.launches += 1 + update_halfedges(nx.quads, nx.nq, nx.nv, hw.src, idx_q, hw.dnew, hw.twin, hw.flag, ho, hw.deg2,
-                                       hw.u, sms, st);
-    std::swap(hw.twin, hw.twin2);
-    std::swap(hw.flag, hw.flag2);
-    std::swap(hw.w.deg, hw.deg2);
-    he_version = mesh_version;
-    he_handles = false;
-  };
-  int32_t* val = nullptr;
-  uint8_t *p = nullptr, *branch = nullptr, *vm_first = nullptr, *em = nullptr, *keep = nullptr, *keep_q = nullptr;
-  int32_t *own_pos = nullptr, *own_rm = nullptr, *vm_second = nullptr, *idx = nullptr, *idx_q = nullptr;
-  int4* jobs = nullptr;
-  unsigned* njobs = nullptr;
-  if (simplify) {
-    val = pool.get<int32_t>(NV);
-    p = pool.get<uint8_t>(NQ);
-    branch = pool.get<uint8_t>(NQ);
-    vm_first = pool.get<uint8_t>(NV);
-    em = pool.get<uint8_t>(NQ);
-    keep = pool.get<uint8_t>(NV);
-    keep_q = pool.get<uint8_t>(NQ);
-    idx_q = pool.get<int32_t>(NQ);
-    own_pos = pool.get<int32_t>(NV);
-    own_rm = pool.get<int32_t>(NV);
-    vm_second = pool.get<int32_t>(NV);
-    jobs = pool.get<int4>(NQ);
-    njobs = pool.get<unsigned>(2);
-    idx = pool.get<int32_t>(NV);
-    if (pool.err) {
-      s.err = pool.err;
-        return s;
-    }
-  }
-  // new output buffers replace the input ones after each compaction
-  auto new_vertices = [&](int64_t nv, DmcMesh& m) {
-    m.v64 = nullptr;
-    cudaError_t e;
-    void *a = nullptr, *b = nullptr, *c = nullptr, *d = nullptr;
-    if ((e = cudaMallocAsync(&a, std::max<int64_t>(nv, 1) * 3 * sizeof(double), st)) != cudaSuccess) return e;
-    if ((e = cudaMallocAsync(&b, std::max<int64_t>(nv, 1) * 3 * sizeof(float), st)) != cudaSuccess) return e;
-    if ((e = cudaMallocAsync(&c, std::max<int64_t>(nv, 1) * 3 * sizeof(float), st)) != cudaSuccess) return e;
-    if ((e = cudaMallocAsync(&d, std::max<int64_t>(nv, 1) * 3 * sizeof(double), st)) != cudaSuccess) return e;
-    m.v64 = (double*)a;
-    m.v = (float*)b;
-    m.n = (float*)c;
-    m.n64 = (double*)d;
-    return cudaSuccess;
+    s.launches += build_halfedges(cur.quads, 4, cur.nq, cur.nv, ho, hw.w, sms, st, handles);
   };
   auto retire = [&](void* ptr) {
     if (!ptr) return;
@@ -809,127 +753,140 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
   };
   auto adopt = [&](void* ptr) { out->owned.push_back(ptr); };
 
-  const unsigned gq = grid_for(NQ, sms), gv = grid_for(NV, sms);
-  // ---- P3X3Y: colour pass, then isolated pass (simplify3X3Y, :1139-1182) ----
-  for (int pass = 0; pass < 2; pass++) {
-    if ((pass == 0 && !c3x3y) || (pass == 1 && !i3x3y)) continue;
-    if (cur.nq == 0) break;
-    halfedges(cur, false);
-    if (pass == 0) {
-      Stage tm(prof, "dmc_color", st);
-      s.launches += color_faces(HeView{cur.quads, hw.twin, hw.flag}, cur.colors, cur.nq, pool, sms, st);
-      if (pool.err) break;
-    }
-    Stage tm(prof, "dmc_p3x3y", st);
-    s.launches += vertex_valence(HeView{cur.quads, hw.twin, hw.flag}, hw.w.deg, cur.nv, cur.nq, val, sms, st);
-    mark3x3y_kernel<<<gq, 256, 0, st>>>(cur.quads, cur.nq, val, p);
-    fill_i32_kernel<<<gv, 256, 0, st>>>(own_pos, cur.nv, -1);
-    fill_i32_kernel<<<gv, 256, 0, st>>>(own_rm, cur.nv, -1);
-    fill_i32_kernel<<<gv, 256, 0, st>>>(vm_second, cur.nv, -1);
-    cudaMemsetAsync(vm_first, 0, cur.nv, st);
-    merge_claim_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.nq, p, val, cur.colors, pass == 0, branch, own_pos, own_rm);
-    cudaMemsetAsync(njobs, 0, sizeof(unsigned), st);
-    cudaMemsetAsync(hw.dold, 0, cur.nv, st);
-    merge_apply_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.nq, branch, own_pos, own_rm,
-                                           vm_first, vm_second, em, jobs, njobs, hw.dold);
-    static const int r_mid = resident_blocks(midpoint_kernel, 256);  // one wave over the merge list
-    midpoint_kernel<<<(unsigned)wave_grid(r_mid, sms, 1, cur.nq, 256), 256, 0, st>>>(jobs, njobs, cur.v64, cur.n64);
-    s.launches += 9;
-    // kept vertices and kept quads: new indices of both, one host read of the two counts
-    invert_flags_kernel<<<gv, 256, 0, st>>>(vm_first, cur.nv, keep);
-    s.launches += 1 + scan_flags(keep, cur.nv, idx, tiles, total, st);
-    invert_flags_kernel<<<gq, 256, 0, st>>>(em, cur.nq, keep_q);
-    s.launches += 1 + scan_flags(keep_q, cur.nq, idx_q, tiles, total + 1, st);
-    int64_t nv2 = 0, nq2 = 0;
-    read_totals(nv2, nq2);
-    // nothing merged and nothing removed: the pass changed nothing, and the mesh stays as it is
-    if (nv2 == cur.nv && nq2 == cur.nq) continue;
-    DmcMesh nx = cur;
-    if ((s.err = new_vertices(nv2, nx)) != cudaSuccess) break;
-    adopt(nx.v64);
-    adopt(nx.v);
-    adopt(nx.n);
-    adopt(nx.n64);
-    gather_vertices_kernel<<<grid_for(3 * cur.nv, sms), 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.n64, nx.v64,
-                                                                       nx.n64, vm_second, nv2, hw.ovf);
-    // remove quads
-    void* qn = nullptr;
-    if ((s.err = cudaMallocAsync(&qn, std::max<int64_t>(nq2, 1) * 4 * sizeof(int32_t), st)) != cudaSuccess) break;
-    adopt(qn);
-    cudaMemsetAsync(hw.dnew, 0, std::max<int64_t>(nv2, 1), st);
-    gather_quads_3x3y_kernel<<<gq, 256, 0, st>>>(em, idx_q, cur.nq, cur.quads, vm_first, vm_second, (int32_t*)qn,
-                                                  nq2, hw.ovf, hw.dold, hw.dnew, hw.src, hw.w.deg);
-    s.launches += 2;
-    // the inherited colours are only read by the colour pass; they are not carried along
-    retire(cur.v64);
-    retire(cur.v);
-    retire(cur.n);
-    retire(cur.n64);
-    retire(cur.quads);
-    nx.nv = nv2;
-    nx.nq = nq2;
-    nx.quads = (int32_t*)qn;
-    const DmcMesh old = cur;
-    cur = nx;
-    mesh_version++;
-    update_he(old, cur, keep, idx, idx_q);
-  }
-  // ---- P3333 (simplify3333, :1362-1385) ----
-  if (s.err == cudaSuccess && p3333 && cur.nq > 0) {
-    halfedges(cur, false);
-    Stage tm(prof, "dmc_p3333", st);
-    uint8_t* p3 = p;
-    uint8_t* rflag = em;
-    uint8_t* vm0 = vm_first;
-    int32_t* vm1 = own_pos;
-    int32_t* vm2 = vm_second;
-    cudaMemcpyAsync(val, hw.w.deg, cur.nv * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
-    valence_boundary_kernel<<<grid_for(4 * cur.nq, sms), 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, 4 * cur.nq, val);
-    cudaMemsetAsync(p3, 0, cur.nq, st);
-    cudaMemsetAsync(rflag, 0, cur.nq, st);
-    cudaMemsetAsync(vm0, 0, cur.nv, st);
-    cudaMemsetAsync(hw.dold, 0, cur.nv, st);
-    fill_i32_kernel<<<gv, 256, 0, st>>>(vm1, cur.nv, -1);
-    fill_i32_kernel<<<gv, 256, 0, st>>>(vm2, cur.nv, -1);
-    mark3333_kernel<<<gq, 256, 0, st>>>(HeView{cur.quads, hw.twin, hw.flag}, cur.nq, val, p3, rflag, vm0, vm1,
-                                        hw.dold);
-    invert_flags_kernel<<<gv, 256, 0, st>>>(vm0, cur.nv, keep);
-    s.launches += 5 + scan_flags(keep, cur.nv, idx, tiles, total, st);
-    invert_flags_kernel<<<gq, 256, 0, st>>>(rflag, cur.nq, keep_q);
-    s.launches += 1 + scan_flags(keep_q, cur.nq, idx_q, tiles, total + 1, st);
-    int64_t nv2 = 0, nq2 = 0;
-    read_totals(nv2, nq2);
-    // no vertex and no quad removed: the mesh stays as it is
-    const bool unchanged = nv2 == cur.nv && nq2 == cur.nq;
-    DmcMesh nx = cur;
-    if (!unchanged && (s.err = new_vertices(nv2, nx)) == cudaSuccess) {
-      adopt(nx.v64);
-      adopt(nx.v);
-      adopt(nx.n);
-      adopt(nx.n64);
-      gather_vertices_kernel<<<grid_for(3 * cur.nv, sms), 256, 0, st>>>(keep, idx, cur.nv, cur.v64, cur.n64, nx.v64,
-                                                                         nx.n64, vm2, nv2, hw.ovf);
-      s.launches += 1;
-      void* qn = nullptr;
-      if ((s.err = cudaMallocAsync(&qn, std::max<int64_t>(nq2, 1) * 4 * sizeof(int32_t), st)) == cudaSuccess) {
-        adopt(qn);
-        cudaMemsetAsync(hw.dnew, 0, std::max<int64_t>(nv2, 1), st);
-        gather_quads_3333_kernel<<<gq, 256, 0, st>>>(rflag, idx_q, cur.nq, cur.quads, p3, vm1, vm2, (int32_t*)qn, nq2,
-                                                      hw.ovf, hw.dold, hw.dnew, hw.src, hw.w.deg);
-        s.launches += 1;
-        retire(cur.v64);
-        retire(cur.v);
-        retire(cur.n);
-        retire(cur.n64);
-        retire(cur.quads);
-        nx.nv = nv2;
-        nx.nq = nq2;
-        nx.quads = (int32_t*)qn;
-        const DmcMesh old = cur;
-        cur = nx;
-        mesh_version++;
-        update_he(old, cur, keep, idx, idx_q);
+  // ---- simplification (simplify3X3Y :1139-1182, simplify3333 :1362-1385) ----
+  // In place: faces and vertices keep their indices through the passes (alive / valive flags), the
+  // halfedges are built once and repaired after each pass, and one order-preserving compaction after
+  // the last pass gives the reference's numbering (each of its per-pass compactions keeps the order
+  // of what remains, and every rule that compares indices compares them in the same order).
+  bool compacted = false;
+  uint8_t *alive = nullptr, *valive = nullptr;
+  int32_t *idx = nullptr, *idx_q = nullptr;
+  int64_t nv0 = cur.nv, nq0 = cur.nq;  // the uncompacted mesh
+  int32_t* q0 = cur.quads;
+  if (simplify) {
+    update_buffers(pool, hw, NV, NQ);
+    int32_t* val = pool.get<int32_t>(NV);
+    uint8_t* p = pool.get<uint8_t>(NQ);
+    uint8_t* branch = pool.get<uint8_t>(NQ);
+    uint8_t* vm_first = pool.get<uint8_t>(NV);
+    uint8_t* em = pool.get<uint8_t>(NQ);
+    int32_t* own_pos = pool.get<int32_t>(NV);
+    int32_t* own_rm = pool.get<int32_t>(NV);
+    int32_t* vm_second = pool.get<int32_t>(NV);
+    int4* jobs = pool.get<int4>(NQ);
+    unsigned* njobs = pool.get<unsigned>(2);
+    alive = pool.get<uint8_t>(NQ);
+    valive = pool.get<uint8_t>(NV);
+    idx = pool.get<int32_t>(NV);
+    idx_q = pool.get<int32_t>(NQ);
+    if ((s.err = pool.err) != cudaSuccess) return s;
+    cudaMemsetAsync(alive, 1, nq0, st);
+    cudaMemsetAsync(valive, 1, nv0, st);
+    build_he(false);
+    const HeView he{q0, hw.twin, hw.flag};
+    auto repair = [&]() {
+      Stage tm(prof, "dmc_halfedges", st);
+      HeOut ho{hw.twin, hw.flag, nullptr};
+      s.launches += repair_halfedges(q0, nq0, nv0, alive, hw.dnew, ho, hw.w.deg, hw.u, sms, st);
+    };
+    // P3X3Y: colour pass, then isolated pass
+    for (int pass = 0; pass < 2; pass++) {
+      if ((pass == 0 && !c3x3y) || (pass == 1 && !i3x3y)) continue;
+      if (pass == 0) {
+        Stage tm(prof, "dmc_color", st);
+        s.launches += color_faces(he, cur.colors, nq0, pool, sms, st);
+        if ((s.err = pool.err) != cudaSuccess) return s;
       }
+      {
+        Stage tm(prof, "dmc_p3x3y", st);
+        s.launches += vertex_valence(he, hw.w.deg, nv0, nq0, val, sms, st, alive);
+        mark3x3y_kernel<<<gq, 256, 0, st>>>(q0, nq0, val, p, alive);
+        fill_i32_kernel<<<gv, 256, 0, st>>>(own_pos, nv0, -1);
+        fill_i32_kernel<<<gv, 256, 0, st>>>(own_rm, nv0, -1);
+        fill_i32_kernel<<<gv, 256, 0, st>>>(vm_second, nv0, -1);
+        cudaMemsetAsync(vm_first, 0, nv0, st);
+        cudaMemsetAsync(hw.dold, 0, nv0, st);
+        cudaMemsetAsync(hw.dnew, 0, nv0, st);
+        merge_claim_kernel<<<gq, 256, 0, st>>>(he, nq0, p, val, cur.colors, pass == 0, branch, own_pos, own_rm);
+        cudaMemsetAsync(njobs, 0, sizeof(unsigned), st);
+        merge_apply_kernel<<<gq, 256, 0, st>>>(he, nq0, branch, own_pos, own_rm, vm_first, vm_second, em, jobs, njobs,
+                                               hw.dold, valive);
+        static const int r_mid = resident_blocks(midpoint_kernel, 256);  // one wave over the merge list
+        midpoint_kernel<<<(unsigned)wave_grid(r_mid, sms, 1, nq0, 256), 256, 0, st>>>(jobs, njobs, cur.v64, cur.n64);
+        apply_3x3y_kernel<<<gq, 256, 0, st>>>(q0, nq0, alive, em, vm_first, vm_second, hw.dold, hw.dnew, hw.w.deg);
+        s.launches += 11;
+      }
+      repair();
+    }
+    // P3333
+    if (p3333) {
+      {
+        Stage tm(prof, "dmc_p3333", st);
+        uint8_t* p3 = p;
+        uint8_t* rflag = em;
+        uint8_t* vm0 = vm_first;
+        int32_t* vm1 = own_pos;
+        s.launches += vertex_valence(he, hw.w.deg, nv0, nq0, val, sms, st, alive);
+        cudaMemsetAsync(p3, 0, nq0, st);
+        cudaMemsetAsync(rflag, 0, nq0, st);
+        cudaMemsetAsync(vm0, 0, nv0, st);
+        cudaMemsetAsync(hw.dold, 0, nv0, st);
+        cudaMemsetAsync(hw.dnew, 0, nv0, st);
+        fill_i32_kernel<<<gv, 256, 0, st>>>(vm1, nv0, -1);
+        mark3333_kernel<<<gq, 256, 0, st>>>(he, nq0, val, p3, rflag, vm0, vm1, hw.dold, alive, valive);
+        apply_3333_kernel<<<gq, 256, 0, st>>>(q0, nq0, alive, rflag, p3, vm1, hw.dold, hw.dnew, hw.w.deg);
+        s.launches += 3;
+      }
+      repair();
+    }
+    // the output's vertex handles and edge counts, on the uncompacted mesh (before it is released)
+    if (want_he) {
+      Stage tm(prof, "dmc_halfedges", st);
+      s.launches += halfedge_handles(q0, 4, nq0, nv0, alive, hw.twin, hw.flag, hw.hv, hw.w, hw.hcount, sms, st);
+    }
+    // ---- the one compaction: live vertices and faces, in order ----
+    Stage tm(prof, "dmc_compact", st);
+    s.launches += scan_flags(valive, nv0, idx, tiles, total, st);
+    s.launches += scan_flags(alive, nq0, idx_q, tiles, total + 1, st);
+    cudaMemcpyAsync(h_cnt, total, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    const int64_t nv2 = (int64_t)h_cnt[0], nq2 = (int64_t)h_cnt[1];
+    // nothing died: no pass changed the mesh, and it stays as it is (with its halfedges)
+    if (nv2 != nv0 || nq2 != nq0) {
+      DmcMesh nx = cur;
+      void *a = nullptr, *b = nullptr, *c = nullptr, *d = nullptr, *qn = nullptr;
+      const size_t nvb = (size_t)std::max<int64_t>(nv2, 1) * 3;
+      if ((s.err = cudaMallocAsync(&a, nvb * sizeof(double), st)) != cudaSuccess) return s;
+      adopt(a);
+      if ((s.err = cudaMallocAsync(&b, nvb * sizeof(float), st)) != cudaSuccess) return s;
+      adopt(b);
+      if ((s.err = cudaMallocAsync(&c, nvb * sizeof(float), st)) != cudaSuccess) return s;
+      adopt(c);
+      if ((s.err = cudaMallocAsync(&d, nvb * sizeof(double), st)) != cudaSuccess) return s;
+      adopt(d);
+      if ((s.err = cudaMallocAsync(&qn, (size_t)std::max<int64_t>(nq2, 1) * 4 * sizeof(int32_t), st)) != cudaSuccess)
+        return s;
+      adopt(qn);
+      nx.v64 = (double*)a;
+      nx.v = (float*)b;
+      nx.n = (float*)c;
+      nx.n64 = (double*)d;
+      nx.quads = (int32_t*)qn;
+      nx.nv = nv2;
+      nx.nq = nq2;
+      // vertex map into vm_second (free after the passes)
+      gather_vertices_kernel<<<grid_for(3 * nv0, sms), 256, 0, st>>>(valive, idx, nv0, cur.v64, cur.n64, nx.v64,
+                                                                     nx.n64, vm_second, nv2, hw.ovf);
+      gather_live_quads_kernel<<<gq, 256, 0, st>>>(alive, idx_q, nq0, q0, vm_second, nx.quads, hw.src, nq2, hw.ovf);
+      s.launches += 2;
+      // the inherited colours are only read by the colour pass; they are not carried along
+      retire(cur.v64);
+      retire(cur.v);
+      retire(cur.n);
+      retire(cur.n64);
+      retire(cur.quads);
+      cur = nx;
+      compacted = true;
     }
   }
   // the float32 outputs of the simplified mesh
@@ -945,7 +902,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     (*ready)(cur.quads, (size_t)cur.nq * 4 * sizeof(int32_t));
   }
   if (s.err == cudaSuccess && want_he) {
-    halfedges(cur, true);
+    if (!simplify) build_he(true);  // the front-end mesh as it is: one build with the handles
     void *he4 = nullptr, *hv = nullptr, *hf = nullptr;
     if ((s.err = cudaMallocAsync(&he4, std::max<int64_t>(4 * cur.nq, 1) * 4 * sizeof(int32_t), st)) == cudaSuccess &&
         (s.err = cudaMallocAsync(&hv, std::max<int64_t>(cur.nv, 1) * sizeof(int32_t), st)) == cudaSuccess &&
@@ -953,8 +910,14 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
       adopt(he4);
       adopt(hv);
       adopt(hf);
-      s.launches += pack_halfedges4(cur.quads, 4, hw.twin, 4 * cur.nq, (int32_t*)he4, (int32_t*)hf, sms, st);
-      cudaMemcpyAsync(hv, hw.hv, cur.nv * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+      Stage tm(prof, "dmc_halfedges", st);
+      if (compacted) {
+        s.launches += pack_compacted_halfedges(cur.quads, cur.nq, hw.src, idx_q, hw.twin, (int32_t*)he4, (int32_t*)hf,
+                                               valive, idx, nv0, hw.hv, (int32_t*)hv, sms, st);
+      } else {
+        s.launches += pack_halfedges4(cur.quads, 4, hw.twin, 4 * cur.nq, (int32_t*)he4, (int32_t*)hf, sms, st);
+        cudaMemcpyAsync(hv, hw.hv, cur.nv * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+      }
       if (ready) {
         (*ready)(he4, (size_t)cur.nq * 16 * sizeof(int32_t));
         (*ready)(hv, (size_t)cur.nv * sizeof(int32_t));

@@ -222,16 +222,15 @@ __global__ void he_override_kernel(const int32_t* faces, int P, const int32_t* l
   }
 }
 
-// ---- incremental update after a simplification pass (quad meshes) ----
-// A pass removes quads and re-targets the corners of some kept quads.  Call a new vertex dirty when
-// it is the image of a removed vertex, of a merge target, or of a re-targeted corner: every removed
-// quad has a dirty end on each of its edges, and every re-targeted corner lands on a dirty vertex.
-// So an edge whose two ends are clean has the same halfedges before and after the pass (their
-// faces kept, in the same order), and keeps its pairing and flag; its twins only move with the
-// face compaction.  The halfedges with a dirty end are bucketed by that end (the lower one when
-// both are dirty), so all halfedges of such an edge share one bucket, and re-paired there with the
-// build's rules.  Out-degrees of clean vertices carry over (less the removed quads' corners, done
-// by the caller); those of dirty vertices are counted here.
+// ---- repair after a simplification pass (quad meshes, faces and vertices keep their indices) ----
+// A pass kills faces and re-targets corners of some live faces.  Call a vertex dirty when a
+// re-targeted corner lands on it or it is a corner of a killed face that is still in use: every
+// killed face has a dirty or dead end on each of its edges, and every re-targeted corner lands on a
+// dirty vertex.  So an edge whose two ends are clean has the same halfedges before and after the
+// pass, and keeps its twins and flags as they are.  The live halfedges with a dirty end are bucketed
+// by that end (the lower one when both are dirty), so all halfedges of such an edge share one
+// bucket, and re-paired there with the build's rules.  Out-degrees of clean vertices are kept (less
+// the killed faces' corners, done by the pass); those of dirty vertices are counted here.
 
 // Own twin and flag of halfedge h from its edge's halfedges (ids ascending in e): the rules of
 // he_twin_kernel and resolve_group, evaluated by every member for itself.
@@ -268,60 +267,38 @@ __device__ __forceinline__ int bucket_of(int o, int t, bool dout, bool din) {
   return (dout && din) ? min(o, t) : (dout ? o : t);
 }
 
-// One thread per face of the new mesh (new face f comes from old face src[f]); the four halfedges'
-// loads are independent, so each thread keeps four in flight.  Halfedges whose ends are clean take
-// their twin and flag from the old mesh; the others get a rank in their bucket (drank), and the face
-// a mask of them (dmask).  Quad arrays are 16-byte aligned (pool allocations).
-__global__ void __launch_bounds__(256) he_update_kernel(const int4* faces, int64_t nf, const int32_t* src,
-                                                        const int32_t* fidx, const uint8_t* dirty,
-                                                        const int4* twin_old, const uint32_t* flag_old, int4* twin,
-                                                        uint32_t* flag, int32_t* deg, int32_t* bcnt, int32_t* drank,
-                                                        uint8_t* dmask) {
+// One thread per face: the mask of the live face's halfedges with a dirty end (dmask), their ranks
+// in their buckets (drank), and the out-degrees of the dirty vertices (zero on entry).  Quad arrays
+// are 16-byte aligned (pool allocations).
+__global__ void __launch_bounds__(256) he_repair_mark_kernel(const int4* faces, int64_t nf, const uint8_t* alive,
+                                                             const uint8_t* dirty, int32_t* deg, int32_t* bcnt,
+                                                             int32_t* drank, uint8_t* dmask) {
   for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += (int64_t)gridDim.x * blockDim.x) {
-    const int4 q = faces[f];
-    const int v[4] = {q.x, q.y, q.z, q.w};
-    bool d[4];
-#pragma unroll
-    for (int r = 0; r < 4; r++) d[r] = dirty[v[r]] != 0;
     unsigned m = 0;
+    if (alive[f]) {
+      const int4 q = faces[f];
+      const int v[4] = {q.x, q.y, q.z, q.w};
+      bool d[4];
 #pragma unroll
-    for (int r = 0; r < 4; r++) m |= (unsigned)(d[r] || d[(r + 1) & 3]) << r;
+      for (int r = 0; r < 4; r++) d[r] = dirty[v[r]] != 0;
+#pragma unroll
+      for (int r = 0; r < 4; r++) m |= (unsigned)(d[r] || d[(r + 1) & 3]) << r;
+      if (m) {
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+          if (d[r]) atomicAdd(deg + v[r], 1);
+          if (m >> r & 1)
+            drank[4 * f + r] = atomicAdd(bcnt + bucket_of(v[r], v[(r + 1) & 3], d[r], d[(r + 1) & 3]), 1);
+        }
+      }
+    }
     dmask[f] = (uint8_t)m;
-    if (m != 0xFu) {
-      const int64_t s = src[f];
-      const int4 T4 = twin_old[s];
-      const uint32_t F4 = flag_old[s];
-      const int T[4] = {T4.x, T4.y, T4.z, T4.w};
-      int o[4];
-#pragma unroll
-      for (int r = 0; r < 4; r++) o[r] = (m >> r & 1) || T[r] < 0 ? -1 : 4 * fidx[T[r] >> 2] + (T[r] & 3);
-      if (m == 0) {
-        twin[f] = make_int4(o[0], o[1], o[2], o[3]);
-        flag[f] = F4;
-      } else {
-        int32_t* tw = reinterpret_cast<int32_t*>(twin + f);
-        uint8_t* fl = reinterpret_cast<uint8_t*>(flag + f);
-#pragma unroll
-        for (int r = 0; r < 4; r++)
-          if (!(m >> r & 1)) {
-            tw[r] = o[r];
-            fl[r] = (uint8_t)(F4 >> (8 * r));
-          }
-      }
-    }
-    if (m) {
-#pragma unroll
-      for (int r = 0; r < 4; r++) {
-        if (d[r]) atomicAdd(deg + v[r], 1);
-        if (m >> r & 1) drank[4 * f + r] = atomicAdd(bcnt + bucket_of(v[r], v[(r + 1) & 3], d[r], d[(r + 1) & 3]), 1);
-      }
-    }
   }
 }
 
 // bucket entries: (halfedge, the edge's other end)
 __global__ void he_bucket_scatter_kernel(const int4* faces, int64_t nf, const uint8_t* dirty, const uint8_t* dmask,
-                                         const int32_t* drank, const int32_t* boff, int2* blist) {
+                                         const int32_t* drank, const int32_t* boff, int2* blist, int32_t* bkey) {
   for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += (int64_t)gridDim.x * blockDim.x) {
     const unsigned m = dmask[f];
     if (!m) continue;
@@ -332,40 +309,33 @@ __global__ void he_bucket_scatter_kernel(const int4* faces, int64_t nf, const ui
       if (!(m >> r & 1)) continue;
       const int o = v[r], t = v[(r + 1) & 3];
       const int key = bucket_of(o, t, dirty[o] != 0, dirty[t] != 0);
-      blist[boff[key] + drank[4 * f + r]] = make_int2((int)(4 * f + r), o == key ? t : o);
+      const int at = boff[key] + drank[4 * f + r];
+      blist[at] = make_int2((int)(4 * f + r), o == key ? t : o);
+      bkey[at] = key;
     }
   }
 }
 
-__global__ void he_pair_kernel(const int4* faces, int64_t nf, const uint8_t* dirty, const uint8_t* dmask,
-                               const int32_t* boff, int nv, const unsigned long long* total, const int2* blist,
-                               int32_t* twin, uint8_t* flag) {
+// One thread per bucket entry: its edge is the entries of its bucket with the same other end.  The
+// lanes of one bucket load the same entries (one broadcast load per step), all from L1.
+__global__ void he_pair_kernel(const int32_t* faces, int nv, const unsigned long long* total, const int32_t* boff,
+                               const int2* blist, const int32_t* bkey, int32_t* twin, uint8_t* flag) {
   const int n = (int)*total;
-  const int32_t* fv = reinterpret_cast<const int32_t*>(faces);
-  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += (int64_t)gridDim.x * blockDim.x) {
-    const unsigned m = dmask[f];
-    if (!m) continue;
-    const int4 q = faces[f];
-    const int v[4] = {q.x, q.y, q.z, q.w};
-    for (int r = 0; r < 4; r++) {
-      if (!(m >> r & 1)) continue;
-      const int o = v[r], t = v[(r + 1) & 3];
-      const int key = bucket_of(o, t, dirty[o] != 0, dirty[t] != 0);
-      const int other = o == key ? t : o;
-      const int b = boff[key], end = list_end(boff, key, nv, n);
-      EdgeIds e;
-      e.c = 0;
-      e.id[0] = e.id[1] = e.id[2] = e.id[3] = INT_MAX;
-      for (int x = b; x < end; x++) {
-        const int2 y = blist[x];
-        if (y.y == other) edge_ids_insert(e, y.x);
-      }
-      const int h = (int)(4 * f + r);
-      int tw, fl;
-      group_member(fv, e, h, tw, fl);
-      twin[h] = tw;
-      flag[h] = (uint8_t)fl;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
+    const int2 x = blist[a];
+    const int key = bkey[a];
+    const int b = boff[key], end = list_end(boff, key, nv, n);
+    EdgeIds e;
+    e.c = 0;
+    e.id[0] = e.id[1] = e.id[2] = e.id[3] = INT_MAX;
+    for (int j = b; j < end; j++) {
+      const int2 y = blist[j];
+      if (y.y == x.y) edge_ids_insert(e, y.x);
     }
+    int tw, fl;
+    group_member(faces, e, x.x, tw, fl);
+    twin[x.x] = tw;
+    flag[x.x] = (uint8_t)fl;
   }
 }
 
@@ -382,11 +352,12 @@ __global__ void he_handles_init_kernel(int32_t* hv, unsigned long long* hv_key, 
 }
 
 template <int P>
-__global__ void he_handles_kernel(const int32_t* faces, int64_t nh, const int32_t* twin, const uint8_t* flag,
-                                  int32_t* hv, unsigned long long* hv_key, int32_t* lone,
+__global__ void he_handles_kernel(const int32_t* faces, int64_t nh, const uint8_t* alive, const int32_t* twin,
+                                  const uint8_t* flag, int32_t* hv, unsigned long long* hv_key, int32_t* lone,
                                   unsigned long long* counts) {
   unsigned long long n1 = 0, n2 = 0;
   for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
+    if (alive && !alive[h / P]) continue;
     const int v = faces[h];
     atomicMax(hv + v, (int32_t)h);
     const int fl = flag[h];
@@ -410,9 +381,68 @@ __global__ void he_handles_kernel(const int32_t* faces, int64_t nh, const int32_
   }
 }
 
+// The same for quads, one thread per face (16-byte corner and twin loads, the four flags in one word).
+__global__ void he_handles4_kernel(const int4* faces, int64_t nf, const uint8_t* alive, const int32_t* twin,
+                                   const uint32_t* flag4, int32_t* hv, unsigned long long* hv_key, int32_t* lone,
+                                   unsigned long long* counts) {
+  unsigned long long n1 = 0, n2 = 0;
+  for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += (int64_t)gridDim.x * blockDim.x) {
+    if (alive && !alive[f]) continue;
+    const int4 q = faces[f];
+    const uint32_t fw = flag4[f];
+    const int v[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const int h = (int)(4 * f + r);
+      atomicMax(hv + v[r], h);
+      const uint32_t fl = (fw >> (8 * r)) & 0xFFu;
+      n1 += fl == 1;
+      n2 += fl == 2;
+      if (fl == 2 && twin[h] == -1) {
+        const int w = v[(r + 1) & 3];
+        const unsigned long long key = ((unsigned long long)(unsigned)min(v[r], w) << 32) | (unsigned)max(v[r], w);
+        atomicMax(hv_key + v[r], key + 1ull);
+        lone[atomicAdd(counts + 2, 1ull)] = h;
+      }
+    }
+  }
+  for (int o = 16; o; o >>= 1) {
+    n1 += __shfl_down_sync(0xffffffffu, n1, o);
+    n2 += __shfl_down_sync(0xffffffffu, n2, o);
+  }
+  if ((threadIdx.x & 31) == 0 && (n1 | n2)) {
+    atomicAdd(counts + 0, n1);
+    atomicAdd(counts + 1, n2);
+  }
+}
+
 // edges with four halfedges (flag 1 on each) and with three (flag 2 on each)
 __global__ void he_group_count_kernel(const unsigned long long* counts, unsigned long long* non_manifold) {
   if (blockIdx.x == 0 && threadIdx.x == 0) *non_manifold = counts[0] / 4 + counts[1] / 3;
+}
+
+// Output records of a compacted quad mesh from halfedges built on its uncompacted form: new face f
+// was face src[f], kept face g became fidx[g]; twins move with their faces.
+__global__ void he_pack_compacted_kernel(const int32_t* faces, int64_t nh, const int32_t* src, const int32_t* fidx,
+                                         const int32_t* twin, int32_t* he4, int32_t* hf) {
+  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = h >> 2;
+    const int r = (int)(h & 3);
+    const int T = twin[4 * (int64_t)src[f] + r];
+    const int t = T < 0 ? -1 : 4 * fidx[T >> 2] + (T & 3);
+    reinterpret_cast<int4*>(he4)[h] = make_int4(faces[h], (int)f, (int)(4 * f + ((r + 1) & 3)), t);
+    if (r == 0 && hf) hf[f] = (int32_t)h;
+  }
+}
+
+// handles of the kept vertices in the compacted numbering (vertex x became vidx[x])
+__global__ void he_handles_compacted_kernel(const uint8_t* vkeep, const int32_t* vidx, int64_t nv, const int32_t* hv,
+                                            const int32_t* fidx, int32_t* hv_out) {
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < nv; x += (int64_t)gridDim.x * blockDim.x) {
+    if (!vkeep[x]) continue;
+    const int h = hv[x];
+    hv_out[vidx[x]] = h < 0 ? -1 : 4 * fidx[h >> 2] + (h & 3);
+  }
 }
 
 template <int P>
@@ -470,38 +500,55 @@ int build_halfedges(const int32_t* faces, int P, int64_t nf, int64_t nv, HeOut& 
   return k + 2;
 }
 
-int update_halfedges(const int32_t* faces, int64_t nf, int64_t nv, const int32_t* src, const int32_t* fidx,
-                     const uint8_t* dirty, const int32_t* twin_old, const uint8_t* flag_old, HeOut& o, int32_t* deg,
-                     HeUpdateWork& w, int sms, cudaStream_t st) {
+int repair_halfedges(const int32_t* faces, int64_t nf, int64_t nv, const uint8_t* alive, const uint8_t* dirty,
+                     HeOut& o, int32_t* deg, HeUpdateWork& w, int sms, cudaStream_t st) {
   if (nf == 0) return 0;
   const int4* q4 = reinterpret_cast<const int4*>(faces);
   cudaMemsetAsync(w.bcnt, 0, (size_t)nv * sizeof(int32_t), st);
-  static const int r_upd = resident_blocks(he_update_kernel, 256);
-  he_update_kernel<<<(unsigned)wave_grid(r_upd, sms, 8, nf, 256), 256, 0, st>>>(
-      q4, nf, src, fidx, dirty, reinterpret_cast<const int4*>(twin_old), reinterpret_cast<const uint32_t*>(flag_old),
-      reinterpret_cast<int4*>(o.twin), reinterpret_cast<uint32_t*>(o.flag), deg, w.bcnt, w.drank, w.dmask);
+  static const int r_mark = resident_blocks(he_repair_mark_kernel, 256);
+  he_repair_mark_kernel<<<(unsigned)wave_grid(r_mark, sms, 8, nf, 256), 256, 0, st>>>(q4, nf, alive, dirty, deg, w.bcnt,
+                                                                                      w.drank, w.dmask);
   int k = 1 + scan_i32(w.bcnt, nv, w.boff, w.tiles, w.total, st);
   static const int r_sc = resident_blocks(he_bucket_scatter_kernel, 256);
   he_bucket_scatter_kernel<<<(unsigned)wave_grid(r_sc, sms, 8, nf, 256), 256, 0, st>>>(q4, nf, dirty, w.dmask, w.drank,
-                                                                                      w.boff, w.blist);
+                                                                                      w.boff, w.blist, w.bkey);
+  // the entries are counted on the device: whole waves, as many as the halfedges could need
   static const int r_pair = resident_blocks(he_pair_kernel, 256);
-  he_pair_kernel<<<(unsigned)wave_grid(r_pair, sms, 8, nf, 256), 256, 0, st>>>(q4, nf, dirty, w.dmask, w.boff, (int)nv,
-                                                                              w.total, w.blist, o.twin, o.flag);
+  he_pair_kernel<<<(unsigned)wave_grid(r_pair, sms, 8, 4 * nf, 256), 256, 0, st>>>(faces, (int)nv, w.total, w.boff,
+                                                                                  w.blist, w.bkey, o.twin, o.flag);
   return k + 2;
 }
 
-int halfedge_handles(const int32_t* faces, int P, int64_t nf, int64_t nv, const int32_t* twin, const uint8_t* flag,
-                     int32_t* hv, HeWork& w, unsigned long long* counts, int sms, cudaStream_t st) {
+int halfedge_handles(const int32_t* faces, int P, int64_t nf, int64_t nv, const uint8_t* alive, const int32_t* twin,
+                     const uint8_t* flag, int32_t* hv, HeWork& w, unsigned long long* counts, int sms,
+                     cudaStream_t st) {
   const int64_t nh = nf * P;
   auto grid = [&](int64_t n) {
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)sms * 8));
   };
   he_handles_init_kernel<<<grid(nv), 256, 0, st>>>(hv, w.hv_key, nv, counts);
-  if (P == 4) he_handles_kernel<4><<<grid(nh), 256, 0, st>>>(faces, nh, twin, flag, hv, w.hv_key, w.rank, counts);
-  else he_handles_kernel<3><<<grid(nh), 256, 0, st>>>(faces, nh, twin, flag, hv, w.hv_key, w.rank, counts);
+  if (P == 4) {  // quad arrays are 16-byte aligned (pool allocations)
+    static const int r4 = resident_blocks(he_handles4_kernel, 256);
+    he_handles4_kernel<<<(unsigned)wave_grid(r4, sms, 8, nf, 256), 256, 0, st>>>(
+        reinterpret_cast<const int4*>(faces), nf, alive, twin, reinterpret_cast<const uint32_t*>(flag), hv, w.hv_key,
+        w.rank, counts);
+  } else {
+    he_handles_kernel<3><<<grid(nh), 256, 0, st>>>(faces, nh, alive, twin, flag, hv, w.hv_key, w.rank, counts);
+  }
   he_override_kernel<<<(unsigned)std::max(1, sms), 256, 0, st>>>(faces, P, w.rank, counts + 2, hv, w.hv_key);
   he_group_count_kernel<<<1, 32, 0, st>>>(counts, w.non_manifold);
   return 4;
+}
+
+int pack_compacted_halfedges(const int32_t* faces, int64_t nf, const int32_t* src, const int32_t* fidx,
+                             const int32_t* twin, int32_t* he4, int32_t* hf, const uint8_t* vkeep, const int32_t* vidx,
+                             int64_t nv, const int32_t* hv, int32_t* hv_out, int sms, cudaStream_t st) {
+  auto grid = [&](int64_t n) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)sms * 8));
+  };
+  if (nf > 0) he_pack_compacted_kernel<<<grid(4 * nf), 256, 0, st>>>(faces, 4 * nf, src, fidx, twin, he4, hf);
+  he_handles_compacted_kernel<<<grid(nv), 256, 0, st>>>(vkeep, vidx, nv, hv, fidx, hv_out);
+  return 2;
 }
 
 int pack_halfedges4(const int32_t* faces, int P, const int32_t* twin, int64_t nh, int32_t* he4, int32_t* hf, int sms,
