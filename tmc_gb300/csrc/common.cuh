@@ -120,14 +120,23 @@ __device__ __forceinline__ uint32_t tile_listed(const CellMask* mask, int64_t ti
   const uint2 a = __ldg(reinterpret_cast<const uint2*>(mask) + (tile << (kTileShift - 5)) + 63);
   return a.y + __popc(a.x);
 }
-// Chunk q of 32 slots for the kernels that walk the listed cells: chunks run over the tiles first
-// (chunk q covers slots 32 * (q / tiles) .. + 31 of tile q % tiles), so that consecutive warps take the
-// front slots of consecutive tiles, where every tile's listed cells sit; numbered the other way, the
-// warps whose index is a multiple of 64 apart would take the same part of every tile and a few of
-// them would get all the work.
+// Chunk q of 32 slots for the kernels that walk the listed cells.  Every tile's listed cells sit in
+// its front slots, so the chunks run over the tiles first (chunk r of a run covers slots
+// 32 * (r / W) .. + 31 of the run's tile r % W): consecutive warps take the front slots of
+// consecutive tiles.  Numbered tile by tile instead, the warps whose index is a multiple of 64 apart
+// would take the same part of every tile and a few of them would get all the work.  The runs are
+// windows of kChunkWindow consecutive tiles (a few z-planes of a volume), taken in order, so that the
+// cells processed at any moment, and the field around them, stay within a narrow band that the L2
+// holds.
+constexpr int64_t kChunkWindow = 512;
 __device__ __forceinline__ void slot_chunk(int64_t q, int64_t tiles, int64_t& tile, uint32_t& first) {
-  const int64_t part = q / tiles;
-  tile = q - part * tiles;
+  const int64_t per = kChunkWindow << (kTileShift - 5);  // chunks of a full window (32 slots each)
+  const int64_t win = q / per;
+  const int64_t t0 = win * kChunkWindow;
+  const int64_t w = tiles - t0 < kChunkWindow ? tiles - t0 : kChunkWindow;  // tiles in this window
+  const int64_t r = q - win * per;
+  const int64_t part = r / w;
+  tile = t0 + (r - part * w);
   first = (uint32_t)(tile << kTileShift) + (uint32_t)part * 32u;
 }
 // the cell behind a slot (cell: in-tile cell offsets of the listed cells)
