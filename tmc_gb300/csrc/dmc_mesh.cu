@@ -245,50 +245,58 @@ __device__ __forceinline__ void midpoint(double* v64, double* n64, int dst, int 
 // never destinations (valence >= 5 vs valence 3), so the merges are independent.
 // dold: the valence-3 corners of the removed faces (merge targets and removed vertices), the
 // vertices the halfedge repair re-pairs around; valive: the removed vertices die.
-__global__ void merge_apply_kernel(HeView he, int64_t nq, const uint8_t* branch, const int32_t* own_pos,
-                                   const int32_t* own_rm, uint8_t* vm_first, int32_t* vm_second, uint8_t* em,
-                                   int4* jobs, unsigned* njobs, uint8_t* dold, uint8_t* valive) {
-  const int lane = threadIdx.x & 31;
-  FOR_EACH(f, nq) {
-    const uint8_t br = branch[f];
-    em[f] = br != 0;
-    bool job = false;
-    int4 jv = make_int4(0, 0, 0, 0);
-    if (br) {
-      const int v0 = he_origin(he, 4 * f), v1 = he_origin(he, 4 * f + 1), v2 = he_origin(he, 4 * f + 2),
-                v3 = he_origin(he, 4 * f + 3);
-      if (br == 1) {
-        if (own_pos[v0] == f) {
-          job = true;
-          jv = make_int4(v0, v1, v3, 0);
+// The jobs of a block's faces are gathered in shared memory and appended with one global atomic
+// per block and iteration (per-warp appends to the one counter serialise on it).
+constexpr int kMergeThreads = 256;
+__global__ void __launch_bounds__(kMergeThreads) merge_apply_kernel(HeView he, int64_t nq, const uint8_t* branch,
+                                                                   const int32_t* own_pos, const int32_t* own_rm,
+                                                                   uint8_t* vm_first, int32_t* vm_second, uint8_t* em,
+                                                                   int4* jobs, unsigned* njobs, uint8_t* dold,
+                                                                   uint8_t* valive) {
+  __shared__ int4 s_jobs[kMergeThreads];
+  __shared__ unsigned s_n, s_base;
+  // block-uniform loop: every thread reaches the barriers
+  for (int64_t f0 = (int64_t)blockIdx.x * kMergeThreads; f0 < nq; f0 += (int64_t)gridDim.x * kMergeThreads) {
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    const int64_t f = f0 + threadIdx.x;
+    if (f < nq) {
+      const uint8_t br = branch[f];
+      em[f] = br != 0;
+      if (br) {
+        const int v0 = he_origin(he, 4 * f), v1 = he_origin(he, 4 * f + 1), v2 = he_origin(he, 4 * f + 2),
+                  v3 = he_origin(he, 4 * f + 3);
+        bool job = false;
+        int4 jv = make_int4(0, 0, 0, 0);
+        if (br == 1) {
+          if (own_pos[v0] == f) {
+            job = true;
+            jv = make_int4(v0, v1, v3, 0);
+          }
+          dold[v0] = 1;
+          dold[v2] = 1;
+          vm_first[v2] = 1;
+          valive[v2] = 0;
+          if (own_rm[v2] == f) vm_second[v2] = v0;
+        } else {
+          if (own_pos[v1] == f) {
+            job = true;
+            jv = make_int4(v1, v0, v2, 0);
+          }
+          dold[v1] = 1;
+          dold[v3] = 1;
+          vm_first[v3] = 1;
+          valive[v3] = 0;
+          if (own_rm[v3] == f) vm_second[v3] = v1;
         }
-        dold[v0] = 1;
-        dold[v2] = 1;
-        vm_first[v2] = 1;
-        valive[v2] = 0;
-        if (own_rm[v2] == f) vm_second[v2] = v0;
-      } else {
-        if (own_pos[v1] == f) {
-          job = true;
-          jv = make_int4(v1, v0, v2, 0);
-        }
-        dold[v1] = 1;
-        dold[v3] = 1;
-        vm_first[v3] = 1;
-        valive[v3] = 0;
-        if (own_rm[v3] == f) vm_second[v3] = v1;
+        if (job) s_jobs[atomicAdd(&s_n, 1u)] = jv;
       }
     }
-    // warp-aggregated append
-    const unsigned act = __activemask();
-    const unsigned bal = __ballot_sync(act, job);
-    if (bal) {
-      const int leader = __ffs(bal) - 1;
-      unsigned base = 0;
-      if (lane == leader) base = atomicAdd(njobs, (unsigned)__popc(bal));
-      base = __shfl_sync(act, base, leader);
-      if (job) jobs[base + __popc(bal & ((1u << lane) - 1u))] = jv;
-    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_base = s_n ? atomicAdd(njobs, s_n) : 0u;
+    __syncthreads();
+    if (threadIdx.x < s_n) jobs[s_base + threadIdx.x] = s_jobs[threadIdx.x];
+    __syncthreads();  // s_n and s_jobs are read before the next iteration resets them
   }
 }
 
@@ -809,8 +817,8 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
         cudaMemsetAsync(hw.dnew, 0, nv0, st);
         merge_claim_kernel<<<gq, 256, 0, st>>>(he, nq0, p, val, cur.colors, pass == 0, branch, own_pos, own_rm);
         cudaMemsetAsync(njobs, 0, sizeof(unsigned), st);
-        merge_apply_kernel<<<gq, 256, 0, st>>>(he, nq0, branch, own_pos, own_rm, vm_first, vm_second, em, jobs, njobs,
-                                               hw.dold, valive);
+        merge_apply_kernel<<<gq, kMergeThreads, 0, st>>>(he, nq0, branch, own_pos, own_rm, vm_first, vm_second, em,
+                                                         jobs, njobs, hw.dold, valive);
         static const int r_mid = resident_blocks(midpoint_kernel, 256);  // one wave over the merge list
         midpoint_kernel<<<(unsigned)wave_grid(r_mid, sms, 1, nq0, 256), 256, 0, st>>>(jobs, njobs, cur.v64, cur.n64);
         apply_3x3y_kernel<<<gq, 256, 0, st>>>(q0, nq0, alive, em, vm_first, vm_second, hw.dold, hw.dnew, hw.w.deg);
