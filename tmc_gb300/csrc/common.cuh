@@ -54,6 +54,11 @@ struct Grid {
   int64_t vbase;      // index of cell 0 in the launch's cell space (0 for a single volume)
   double inv2[3];     // 1 / (2 * spacing), for the central-difference gradients
   float inv2f[3];     // the same rounded to float
+  // float forms for the float32 paths, made once on the host (a float64 conversion per vertex runs
+  // on the float64 pipe): origin and spacing as float pairs (hi + lo within 2^-48 relative of the
+  // double), the isovalue rounded to float
+  float org_hi[3], org_lo[3], sp_hi[3], sp_lo[3];
+  float iso_f;
   Div32 div_cx, div_cy;  // division by nx - 1 and ny - 1 (cell index -> i, j, k); set_divisors()
   // fused generation (single-volume launches): the classification evaluates the field from `gen` at
   // the float32 spacing gd instead of reading f, and writes each point once to gen_out (== f), which

@@ -872,6 +872,7 @@ struct alignas(16) ProjRecord {
   double iso;
   int32_t prj;         // projection plane (0..2)
   int32_t pad;
+  float iso_hi, iso_lo;  // iso as a float pair (ffx::ff_from_double), made once per volume
 };
 
 // Set-up pass of one contour.  Returns false when the contour needs the one-pass kernel.
@@ -890,6 +891,8 @@ TMC_HD bool projection_record(const float u[8], double iso, uint64_t c, int t, c
   R.iso = iso;
   R.prj = prj;
   R.pad = 0;
+  R.iso_hi = P.iso_ff.hi;
+  R.iso_lo = P.iso_ff.lo;
   return true;
 }
 
@@ -910,6 +913,8 @@ TMC_HD bool projection_record_acc(const float u[8], double iso, uint64_t c, int 
   R.iso = iso;
   R.prj = prj;
   R.pad = 0;
+  R.iso_hi = P.iso_ff.hi;
+  R.iso_lo = P.iso_ff.lo;
   return true;
 }
 
@@ -927,7 +932,7 @@ TMC_HD void ctx_from_record(const ProjRecord& R, ProjCtx& P) {
     P.pff[d] = ff{R.pff[2 * d], R.pff[2 * d + 1]};
     P.pf[d] = R.pff[2 * d];
   }
-  P.iso_ff = ffx::ff_from_double(R.iso);
+  P.iso_ff = ff{R.iso_hi, R.iso_lo};  // no float64 conversion per vertex
   P.iso_d = R.iso;
   P.iso_f = P.iso_ff.hi;
   P.iso_err = fabsf(P.iso_ff.lo) + fabsf(P.iso_ff.hi) * 0x1p-30f;

@@ -17,6 +17,7 @@
 #include "ctx_access.h"
 #include "dmc.h"
 #include "dmc_mesh.h"
+#include "ffloat.cuh"
 #include "generators.cuh"
 #include "halfedges.h"
 #include "scan.cuh"
@@ -251,6 +252,15 @@ tmc::Grid make_grid(const tmc_volume* vol, const float* dev, double iso) {
   g.inv2[1] = 1.0 / (2 * g.dy);
   g.inv2[2] = 1.0 / (2 * g.dz);
   for (int d = 0; d < 3; d++) g.inv2f[d] = (float)g.inv2[d];
+  const double org[3] = {g.ox, g.oy, g.oz}, sp[3] = {g.dx, g.dy, g.dz};
+  for (int d = 0; d < 3; d++) {
+    const tmc::ffx::ff a = tmc::ffx::ff_from_double(org[d]), b = tmc::ffx::ff_from_double(sp[d]);
+    g.org_hi[d] = a.hi;
+    g.org_lo[d] = a.lo;
+    g.sp_hi[d] = b.hi;
+    g.sp_lo[d] = b.lo;
+  }
+  g.iso_f = (float)iso;
   g.set_divisors();
   return g;
 }

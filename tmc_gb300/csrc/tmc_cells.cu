@@ -673,17 +673,16 @@ __device__ __forceinline__ void edge_vertex_f32(const Grid& g, int i, int j, int
                                                 const float inv2[3]) {
   const int v0 = edge_v0(e), v1 = edge_v1(e), ax = edge_axis(e);
   const float F0 = pick8(u, v0), F1 = pick8(u, v1);
-  const float l = ((float)g.iso - F0) / (F1 - F0);
+  const float l = (g.iso_f - F0) / (F1 - F0);
   const int i0 = i + (v0 & 1), j0 = j + ((v0 >> 1) & 1), k0 = k + ((v0 >> 2) & 1);
   const int i1 = i + (v1 & 1), j1 = j + ((v1 >> 1) & 1), k1 = k + ((v1 >> 2) & 1);
   const int gi[3] = {i0, j0, k0};
-  const double o[3] = {g.ox, g.oy, g.oz}, dd[3] = {g.dx, g.dy, g.dz};
   const int64_t base = 3 * (int64_t)idx;
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     // origin + (index + l) * spacing, with index + l exact as a float pair
     const ffx::ff t = (d == ax) ? ffx::two_sum((float)gi[d], l) : ffx::ff_from((float)gi[d]);
-    const ffx::ff x = ffx::ff_add(ffx::ff_from_double(o[d]), ffx::ff_mul(t, ffx::ff_from_double(dd[d])));
+    const ffx::ff x = ffx::ff_add(ffx::ff{g.org_hi[d], g.org_lo[d]}, ffx::ff_mul(t, ffx::ff{g.sp_hi[d], g.sp_lo[d]}));
     out.v[base + d] = x.hi + x.lo;
   }
   float n0[3], n1[3];
