@@ -12,7 +12,7 @@ struct DmcVertexOut {
   float* v;        // 3 per vertex
   float* n;        // 3 per vertex
   double* v64;     // optional
-  double* n64;     // optional: float64 normals (kept while the mesh is simplified)
+  double* n64;     // optional: normals kept while the mesh is simplified, as float pairs (hi, lo) per 8-byte slot
   int64_t* vcell;  // optional (with vuvw)
   float* vuvw;
 };

@@ -313,14 +313,20 @@ __device__ __forceinline__ void vertex_outputs(const GridCache& G, int i, int j,
                                                const DmcVertexOut& out, int flip, repr::Stats& st) {
   const Grid& g = G.g;
   const int64_t o = 3 * vidx;
+  // a simplified volume: its float32 positions and normals are written after the passes, from the
+  // float64 positions and the float-pair normals kept here
+  const bool keep64 = out.n64 && (g.flags & kGridNormal64);
+  float2* n2 = reinterpret_cast<float2*>(out.n64);
   // position: UniformGrid::position (cpp_dmc/UniformGrid.h:300-305)
   const double lx = p64 ? p64[0] : (double)p[0], ly = p64 ? p64[1] : (double)p[1], lz = p64 ? p64[2] : (double)p[2];
   const double px = g.ox + (i + lx) * g.dx;
   const double py = g.oy + (j + ly) * g.dy;
   const double pz = g.oz + (k + lz) * g.dz;
-  out.v[o] = (float)px;
-  out.v[o + 1] = (float)py;
-  out.v[o + 2] = (float)pz;
+  if (!keep64) {
+    out.v[o] = (float)px;
+    out.v[o + 1] = (float)py;
+    out.v[o + 2] = (float)pz;
+  }
   if (out.v64) {
     out.v64[o] = px;
     out.v64[o + 1] = py;
@@ -333,11 +339,15 @@ __device__ __forceinline__ void vertex_outputs(const GridCache& G, int i, int j,
     // float64 local coordinates: the reference's float64 normal at them
     const Normal64 nf = normal_f64(g, i, j, k, lx, ly, lz, flip);
     for (int d = 0; d < 3; d++) {
-      if (out.n64 && (g.flags & kGridNormal64)) out.n64[o + d] = nf.n[d];
-      out.n[o + d] = (float)nf.n[d];
+      if (keep64) {
+        const ffx::ff x = ffx::ff_from_double(nf.n[d]);
+        n2[o + d] = make_float2(x.hi, x.lo);
+      } else {
+        out.n[o + d] = (float)nf.n[d];
+      }
     }
     st.normal_f64++;
-  } else if (kFF && out.n64 && (g.flags & kGridNormal64)) {
+  } else if (kFF && keep64) {
     ffx::ff Gq[8][3];
 #pragma unroll
     for (int q = 0; q < 8; q++) point_diff_ff(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), Gq[q]);
@@ -364,15 +374,14 @@ __device__ __forceinline__ void vertex_outputs(const GridCache& G, int i, int j,
     if (scale <= 0x1p10f * sqrtf(dot.hi)) {
       for (int d = 0; d < 3; d++) {
         const ffx::ff x = ffx::ff_mul(nv3[d], r);
-        out.n64[o + d] = (double)x.hi + (double)x.lo;
-        out.n[o + d] = x.hi;
+        n2[o + d] = make_float2(x.hi, x.lo);
       }
     } else {
       // the gradients cancel to below 2^-10 of their size: float64, as the reference
       const Normal64 nf = normal_f64(g, i, j, k, p[0], p[1], p[2], flip);
       for (int d = 0; d < 3; d++) {
-        out.n64[o + d] = nf.n[d];
-        out.n[o + d] = (float)nf.n[d];
+        const ffx::ff x = ffx::ff_from_double(nf.n[d]);
+        n2[o + d] = make_float2(x.hi, x.lo);
       }
       st.normal_f64++;
     }

@@ -18,6 +18,7 @@
 
 #include "../../include/tmc_gb300.h"
 #include "dmc_mesh.h"
+#include "ffloat.cuh"
 #include "halfedges.h"
 #include "libm_acosf.h"
 #include "scan.cuh"
@@ -220,8 +221,16 @@ __global__ void merge_claim_kernel(HeView he, int64_t nq, const uint8_t* p, cons
   }
 }
 
-// float64 only: the float32 outputs are their roundings, written once after the last pass
-// (float_outputs_kernel)
+// The normals kept while simplifying are float pairs (hi, lo) in the 8-byte slots of n64: the front
+// end computes them in float-float (within ~2^-40 of the reference's float64 normals), and only their
+// float32 roundings leave the library, so they are stored as computed.
+__device__ __forceinline__ double pair_to_double(const double* n64, int64_t e) {
+  const float2 x = reinterpret_cast<const float2*>(n64)[e];
+  return (double)x.x + (double)x.y;
+}
+
+// float64 positions and normals: the float32 outputs are their roundings, written once after the
+// last pass (float_outputs_kernel)
 __device__ __forceinline__ void midpoint(double* v64, double* n64, int dst, int a, int b) {
 #pragma unroll
   for (int d = 0; d < 3; d++) {
@@ -231,12 +240,16 @@ __device__ __forceinline__ void midpoint(double* v64, double* n64, int dst, int 
   double m[3];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    const double na = n64[3 * (int64_t)a + d], nb = n64[3 * (int64_t)b + d];
+    const double na = pair_to_double(n64, 3 * (int64_t)a + d), nb = pair_to_double(n64, 3 * (int64_t)b + d);
     m[d] = na + 0.5 * (nb - na);
   }
   const double s = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+  float2* n2 = reinterpret_cast<float2*>(n64);
 #pragma unroll
-  for (int d = 0; d < 3; d++) n64[3 * (int64_t)dst + d] = m[d] / s;
+  for (int d = 0; d < 3; d++) {
+    const ffx::ff x = ffx::ff_from_double(m[d] / s);
+    n2[3 * (int64_t)dst + d] = make_float2(x.hi, x.lo);
+  }
 }
 
 // Marks the removed vertices and lists the midpoint merges (destination, two sources); the
@@ -312,9 +325,10 @@ __global__ void midpoint_kernel(const int4* jobs, const unsigned* njobs, double*
 // front end writes float32 values that are the same roundings, so that the passes only carry the
 // float64 arrays).
 __global__ void float_outputs_kernel(const double* v64, const double* n64, int64_t n, float* v, float* nf) {
+  const float2* n2 = reinterpret_cast<const float2*>(n64);
   FOR_EACH(e, n) {
     v[e] = (float)v64[e];
-    nf[e] = (float)n64[e];
+    nf[e] = n2[e].x;  // a normalised pair's high part is its float32 rounding
   }
 }
 

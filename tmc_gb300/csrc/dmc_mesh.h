@@ -15,7 +15,7 @@ struct DmcMesh {
   float* v = nullptr;
   float* n = nullptr;
   double* v64 = nullptr;
-  double* n64 = nullptr;  // float64 normals while simplifying (merges average them as the reference)
+  double* n64 = nullptr;  // normals while simplifying, float pairs (hi, lo) per 8-byte slot (merges average them in float64)
   int32_t* quads = nullptr;
   uint8_t* colors = nullptr;
 };
