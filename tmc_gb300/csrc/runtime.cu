@@ -121,7 +121,11 @@ cudaError_t tmc_ambiguous_records(tmc_ctx* ctx, Allocs& al, tmc::TmcScratch& sc,
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return e;
   n_amb = (int64_t)*h;
-  return al.get(&sc.amb_rec, (size_t)std::max<int64_t>(n_amb, 1) * tmc::kTmcAmbRecWords);
+  const size_t na = (size_t)std::max<int64_t>(n_amb, 1);
+  if ((e = al.get(&sc.amb_rec, na * tmc::kTmcAmbRecWords)) != cudaSuccess) return e;
+  if ((e = al.get(&sc.amb_sorted, na)) != cudaSuccess) return e;
+  if ((e = al.get(&sc.amb_key, na)) != cudaSuccess) return e;
+  return al.get(&sc.amb_hist, 512);
 }
 
 float iso_up(double iso) {
@@ -1007,7 +1011,7 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
     TMC_CUDA(ctx, al.get(&dsc.ccase, ncell));
     ctx->launches += tmc::dmc_front_count(space, dsc, st, &ctx->prof);
   } else {
-    tsc = tmc::TmcScratch{rec, voff, qoff, tile_sums, totals, ctx->d_stats, nullptr, nullptr};
+    tsc = tmc::TmcScratch{rec, voff, qoff, tile_sums, totals, ctx->d_stats};
     tsc.mask = mask;
     tsc.cellof = cellof;
     TMC_CUDA(ctx, al.get(&tsc.amb_n, 1));

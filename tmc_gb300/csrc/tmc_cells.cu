@@ -551,6 +551,52 @@ __global__ void __launch_bounds__(kScanThreads, 6) tmc_classify_kernel(CellSpace
   if (threadIdx.x == 0) tile_sums[tile] = tile_sum;
 }
 
+// The classification lists the ambiguous cells in no useful order; p_slice's branches follow the MC
+// case, so the list is sorted by case (counting sort over the 256 cases) before the float64 passes:
+// the lanes of a warp then mostly take the same branches (the float64 pipe issues for the whole warp
+// whatever its active lanes).  Key pass: each cell's case and the per-case counts.
+__global__ void __launch_bounds__(256) tmc_amb_key_kernel(CellSpace space, const uint16_t* cellof, const uint32_t* list,
+                                                          int64_t n, uint8_t* key, unsigned* hist) {
+  __shared__ unsigned h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t vcell = slot_cell(cellof, list[a]);
+    const Grid g = space.grid_of_tile(vcell / kScanTile);
+    int i, j, k;
+    tcell_ijk(g, vcell - g.vbase, i, j, k);
+    float u[8];
+    tload_corners(g, i, j, k, u);
+    unsigned cs = 0;
+#pragma unroll
+    for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
+    key[a] = (uint8_t)cs;
+    atomicAdd(&h[cs], 1u);
+  }
+  __syncthreads();
+  if (h[threadIdx.x]) atomicAdd(hist + threadIdx.x, h[threadIdx.x]);
+}
+
+// exclusive scan of the 256 counts into the scatter cursors (one block of 256 threads)
+__global__ void tmc_amb_cursor_kernel(const unsigned* hist, unsigned* cursor) {
+  __shared__ unsigned x[256];
+  x[threadIdx.x] = hist[threadIdx.x];
+  __syncthreads();
+  for (int o = 1; o < 256; o <<= 1) {
+    const unsigned y = threadIdx.x >= (unsigned)o ? x[threadIdx.x - o] : 0u;
+    __syncthreads();
+    x[threadIdx.x] += y;
+    __syncthreads();
+  }
+  cursor[threadIdx.x] = x[threadIdx.x] - hist[threadIdx.x];
+}
+
+__global__ void tmc_amb_sort_kernel(const uint32_t* list, const uint8_t* key, int64_t n, unsigned* cursor,
+                                    uint32_t* sorted) {
+  for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x)
+    sorted[atomicAdd(cursor + key[a], 1u)] = list[a];
+}
+
 // Ambiguous cells from the classification's list: p_slice in counting mode (float64); the counts go
 // into the cell record and, atomically, into the cell's tile sum (one thread per listed cell, no
 // tile barrier to wait on).  The triangles (as local codes) and the inner vertices' parameters go
@@ -917,10 +963,16 @@ int tmc_count(const CellSpace& space, TmcScratch& s, int64_t n_amb, int sms, cud
   int k = 0;
   if (n_amb > 0) {
     Stage ta(prof, "tmc_amb_count", st);
+    // the list sorted by MC case (the records follow its order, so the emission pass is sorted too)
+    const unsigned gs = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n_amb, 256), (int64_t)sms * 8));
+    cudaMemsetAsync(s.amb_hist, 0, 256 * sizeof(unsigned), st);
+    tmc_amb_key_kernel<<<gs, 256, 0, st>>>(space, s.cellof, amb_cells, n_amb, s.amb_key, s.amb_hist);
+    tmc_amb_cursor_kernel<<<1, 256, 0, st>>>(s.amb_hist, s.amb_hist + 256);
+    tmc_amb_sort_kernel<<<gs, 256, 0, st>>>(amb_cells, s.amb_key, n_amb, s.amb_hist + 256, s.amb_sorted);
     static const int r_amb = resident_blocks(tmc_amb_count_kernel, 128);
     tmc_amb_count_kernel<<<(unsigned)wave_grid(r_amb, sms, 16, n_amb, 128), 128, 0, st>>>(
-        space, s.cellof, s.rec, s.tile_sums, s.stats, amb_cells, s.amb_n, reinterpret_cast<AmbRec*>(s.amb_rec));
-    k++;
+        space, s.cellof, s.rec, s.tile_sums, s.stats, s.amb_sorted, s.amb_n, reinterpret_cast<AmbRec*>(s.amb_rec));
+    k += 4;
   }
   Stage t(prof, "tmc_scan", st);
   scan_tile_sums_kernel<<<1, 1024, 0, st>>>(s.tile_sums, tiles, s.totals);

@@ -26,6 +26,9 @@ struct TmcScratch {
   unsigned* amb_n;      // ambiguous cells listed by the classification
   uint32_t* amb_rec;    // kTmcAmbRecWords words per ambiguous cell: what the counting pass keeps of
                         // its p_slice for the emission pass (tmc_cells.cu, AmbRec)
+  uint32_t* amb_sorted; // the ambiguous cells' slots sorted by MC case (one per ambiguous cell)
+  uint8_t* amb_key;     // their cases, in list order (one per ambiguous cell)
+  unsigned* amb_hist;   // 512: per-case counts, then scatter cursors
   // listed cells (common.cuh): rec, voff and toff hold one entry per listed cell at its slot, the
   // ambiguous-cell list holds slots
   CellMask* mask;       // per 32 cells of the space
