@@ -58,6 +58,7 @@ struct Grid {
   // on the float64 pipe): origin and spacing as float pairs (hi + lo within 2^-48 relative of the
   // double), the isovalue rounded to float
   float org_hi[3], org_lo[3], sp_hi[3], sp_lo[3];
+  float inv2_hi[3], inv2_lo[3];  // 1 / (2 * spacing)
   float iso_f;
   Div32 div_cx, div_cy;  // division by nx - 1 and ny - 1 (cell index -> i, j, k); set_divisors()
   // fused generation (single-volume launches): the classification evaluates the field from `gen` at

@@ -263,6 +263,9 @@ tmc::Grid make_grid(const tmc_volume* vol, const float* dev, double iso) {
     g.org_lo[d] = a.lo;
     g.sp_hi[d] = b.hi;
     g.sp_lo[d] = b.lo;
+    const tmc::ffx::ff c = tmc::ffx::ff_from_double(g.inv2[d]);
+    g.inv2_hi[d] = c.hi;
+    g.inv2_lo[d] = c.lo;
   }
   g.iso_f = (float)iso;
   g.set_divisors();

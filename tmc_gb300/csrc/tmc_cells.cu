@@ -474,6 +474,73 @@ __device__ __forceinline__ void amb_geometry(const Grid& g, int i, int j, int k,
   }
 }
 
+// Corner positions alone (float64, as amb_geometry).
+__device__ __forceinline__ void amb_positions(const Grid& g, int i, int j, int k, double P[8][3]) {
+  const double x[2] = {g.ox + i * g.dx, g.ox + (i + 1) * g.dx};
+  const double y[2] = {g.oy + j * g.dy, g.oy + (j + 1) * g.dy};
+  const double z[2] = {g.oz + k * g.dz, g.oz + (k + 1) * g.dz};
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    P[q][0] = x[q & 1];
+    P[q][1] = y[(q >> 1) & 1];
+    P[q][2] = z[(q >> 2) & 1];
+  }
+}
+
+// tmc_point_gradient in float-float: the exact float difference times 1/(2 spacing) (1/spacing on
+// the border), within ~2^-46 of the reference's float64 quotient.
+__device__ __forceinline__ ffx::ff grad_axis_ff(float hi_v, float lo_v, bool border, float s_hi, float s_lo) {
+  const float m = border ? 2.0f : 1.0f;  // 1/spacing = 2 * 1/(2 spacing), exactly
+  return ffx::ff_mul(ffx::two_sum(hi_v, -lo_v), ffx::ff{s_hi * m, s_lo * m});
+}
+__device__ __forceinline__ void tmc_gradient_ff(const Grid& g, int i, int j, int k, ffx::ff out[3]) {
+  const int i1 = i == g.nx - 1 ? i : i + 1, i0 = i == 0 ? 0 : i - 1;
+  const int j1 = j == g.ny - 1 ? j : j + 1, j0 = j == 0 ? 0 : j - 1;
+  const int k1 = k == g.nz - 1 ? k : k + 1, k0 = k == 0 ? 0 : k - 1;
+  out[0] = grad_axis_ff(g.at(i1, j, k), g.at(i0, j, k), i == 0 || i == g.nx - 1, g.inv2_hi[0], g.inv2_lo[0]);
+  out[1] = grad_axis_ff(g.at(i, j1, k), g.at(i, j0, k), j == 0 || j == g.ny - 1, g.inv2_hi[1], g.inv2_lo[1]);
+  out[2] = grad_axis_ff(g.at(i, j, k1), g.at(i, j, k0), k == 0 || k == g.nz - 1, g.inv2_hi[2], g.inv2_lo[2]);
+}
+
+// a + t (b - a), all float pairs
+__device__ __forceinline__ ffx::ff ff_lerp_ff(ffx::ff a, ffx::ff b, ffx::ff t) {
+  return ffx::ff_add(a, ffx::ff_mul(ffx::ff_sub(b, a), t));
+}
+
+// One inner vertex of the emission pass: the float64 position as inner_vertex forms it, the normal
+// from the float-float corner gradients N (trilinear at (u, v, w), normalised; within a few 2^-40 of
+// the reference's float64 normal).  Only the float32 rounding of the normal is output, so the float
+// pairs serve wherever the gradients do not cancel to below 2^-10 of their size; there it returns
+// false and the caller computes the normal in float64.
+__device__ __forceinline__ bool inner_vertex_ff(const double (*P)[3], const ffx::ff (*N)[3], float scale, double u,
+                                                double v, double w, const InnerOut& geo, int64_t index) {
+  double ip[3];
+  cell_trilinear3(P, u, v, w, ip);
+  const ffx::ff U = ffx::ff_from_double(u), V = ffx::ff_from_double(v), W = ffx::ff_from_double(w);
+  ffx::ff in[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const ffx::ff a0 = ff_lerp_ff(N[0][d], N[1][d], U), a1 = ff_lerp_ff(N[2][d], N[3][d], U);
+    const ffx::ff a2 = ff_lerp_ff(N[4][d], N[5][d], U), a3 = ff_lerp_ff(N[6][d], N[7][d], U);
+    in[d] = ff_lerp_ff(ff_lerp_ff(a0, a1, V), ff_lerp_ff(a2, a3, V), W);
+  }
+  const ffx::ff dot =
+      ffx::ff_add(ffx::ff_add(ffx::ff_mul(in[0], in[0]), ffx::ff_mul(in[1], in[1])), ffx::ff_mul(in[2], in[2]));
+  if (!(dot.hi > 0.0f) || !(scale <= 0x1p10f * sqrtf(dot.hi))) return false;
+  // 1/sqrt(dot): float estimate and one Newton step in float-float
+  const float r0 = rsqrtf(dot.hi);
+  const ffx::ff h = ffx::ff_mul_f(ffx::ff_mul_f(dot, r0), r0);
+  const ffx::ff r = ffx::ff_mul_f(ffx::ff_sub(ffx::ff_from(1.5f), ffx::ff_mul_f(h, 0.5f)), r0);
+  const int64_t o = 3 * index;
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    geo.v[o + q] = (float)ip[q];
+    geo.n[o + q] = ffx::ff_mul(in[q], r).hi;
+    if (geo.v64) geo.v64[o + q] = ip[q];
+  }
+  return true;
+}
+
 __device__ void load_amb_cell(const Grid& g, int i, int j, int k, const float u[8], uint32_t emask, AmbCell& a,
                               bool geometry) {
 #pragma unroll
@@ -734,12 +801,31 @@ __device__ __forceinline__ void edge_vertex_f32(const Grid& g, int i, int j, int
   float n0[3], n1[3];
   tmc_gradient_f(g, i0, j0, k0, inv, inv2, n0);
   tmc_gradient_f(g, i1, j1, k1, inv, inv2, n1);
-  float in[3];
+  float in[3], scale = 0;
 #pragma unroll
-  for (int d = 0; d < 3; d++) in[d] = fmaf(l, n1[d] - n0[d], n0[d]);
-  const float rn = rsqrtf(in[0] * in[0] + in[1] * in[1] + in[2] * in[2]);
+  for (int d = 0; d < 3; d++) {
+    in[d] = fmaf(l, n1[d] - n0[d], n0[d]);
+    scale = fmaxf(scale, fmaxf(fabsf(n0[d]), fabsf(n1[d])));
+  }
+  const float dot = in[0] * in[0] + in[1] * in[1] + in[2] * in[2];
+  // The float32 interpolation errs by a few ulps of `scale`; where the gradients cancel to below
+  // 1/16 of it that would exceed ~4e-6 of the unit normal: the reference's float64 normal instead.
+  if (scale <= 16.0f * sqrtf(dot)) {
+    const float rn = rsqrtf(dot);
 #pragma unroll
-  for (int d = 0; d < 3; d++) out.n[base + d] = in[d] * rn;
+    for (int d = 0; d < 3; d++) out.n[base + d] = in[d] * rn;
+    return;
+  }
+  double m0[3], m1[3];
+  tmc_point_gradient(g, i0, j0, k0, m0);
+  tmc_point_gradient(g, i1, j1, k1, m1);
+  const double F0d = F0, F1d = F1, ld = (g.iso - F0d) / (F1d - F0d);
+  double md[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) md[d] = (1 - ld) * m0[d] + ld * m1[d];
+  const double nl = sqrt(md[0] * md[0] + md[1] * md[1] + md[2] * md[2]);
+#pragma unroll
+  for (int d = 0; d < 3; d++) out.n[base + d] = (float)(md[d] / nl);
 }
 
 // Vertex index of each crossed edge of a cell, within the cell's volume (vfirst: the volume's first
@@ -811,15 +897,37 @@ __global__ void __launch_bounds__(128) tmc_ambiguous_kernel(CellSpace space, con
       }
     }
     if (ni) {
-      double P[8][3], N[8][3];
-      amb_geometry(g, i, j, k, P, N);
+      // positions in float64 (the output's), normals (float32 outputs only) from float-float
+      // gradients; the float64 gradients for float64 outputs and where the gradients cancel
+      double P[8][3];
+      amb_positions(g, i, j, k, P);
+      ffx::ff N[8][3];
+      float scale = 0;
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        tmc_gradient_ff(g, i + (q & 1), j + ((q >> 1) & 1), k + ((q >> 2) & 1), N[q]);
+        scale = fmaxf(scale, fmaxf(fabsf(N[q][0].hi), fmaxf(fabsf(N[q][1].hi), fabsf(N[q][2].hi))));
+      }
+      double uvw[6][3];
+      int nv = 1;
       if (ni == 1) {
-        inner_vertex(P, N, R.prm[0], R.prm[1], R.prm[2], io, ibase);
+        uvw[0][0] = R.prm[0];
+        uvw[0][1] = R.prm[1];
+        uvw[0][2] = R.prm[2];
       } else {
         const double ui[2] = {R.prm[0], R.prm[1]}, vi[2] = {R.prm[2], R.prm[3]}, wi[2] = {R.prm[4], R.prm[5]};
-        double hvt[6][3];
-        hex_corners(ui, vi, wi, hvt);
-        for (int q = 0; q < 6; q++) inner_vertex(P, N, hvt[q][0], hvt[q][1], hvt[q][2], io, (int64_t)ibase + q);
+        hex_corners(ui, vi, wi, uvw);
+        nv = 6;
+      }
+      for (int q = 0; q < nv; q++) {
+        // float64 outputs requested for this volume: the reference's float64 normal (and its
+        // float32 rounding), as its edge vertices have
+        if (!(g.flags & kGridPos64) &&
+            inner_vertex_ff(P, N, scale, uvw[q][0], uvw[q][1], uvw[q][2], io, (int64_t)ibase + q))
+          continue;
+        double Pd[8][3], Nd[8][3];
+        amb_geometry(g, i, j, k, Pd, Nd);
+        inner_vertex(Pd, Nd, uvw[q][0], uvw[q][1], uvw[q][2], io, (int64_t)ibase + q);
       }
     }
   }
