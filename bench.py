@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--requests", type=int, default=256, help="requests per arrival rate of the serve workload")
     p.add_argument("--rates", default="0.5,0.8,1.0,1.5",
                    help="arrival rates of the serve workload, as multiples of the plain loop's capacity")
+    p.add_argument("--in-flight", type=int, default=2,
+                   help="end-to-end steps in flight at once (each on its own pair of contexts)")
     p.add_argument("--no-extras", action="store_true",
                    help="default workload only, without the batch and serve keys")
     return p.parse_args()
@@ -255,35 +257,58 @@ def run_ours(args, rank, world, local):
     # ---- end to end through the C ABI with host buffers (W untimed steps first) ----
     # With results going to host memory the link, not the GPU, sets the end of a step: the TMC
     # extraction runs on a context of higher stream priority (tmc_ctx_opts.priority), so that it
-    # finishes early and its output crosses the link while DMC still computes.
-    ctx_e = native.Context(local, priority=-1)
+    # finishes early and its output crosses the link while DMC still computes.  A step's DMC meshes
+    # exist only after its last pass, so their copy (about 10 ms of link time) is a tail that one
+    # step cannot hide; with `--in-flight` steps in flight, each on its own pair of contexts driven
+    # by its own thread (what a caller of the C ABI does from several threads), one step's meshes
+    # cross the link while the next step computes.  Every step still copies its field in and its
+    # meshes out inside the timed region.
+    lanes = []
+    for li in range(max(1, args.in_flight)):
+        lanes.append({"dmc": ctx if li == 0 else native.Context(local), "tmc": native.Context(local, priority=-1),
+                      "helper": concurrent.futures.ThreadPoolExecutor(1),
+                      "runner": concurrent.futures.ThreadPoolExecutor(1)})
 
-    def step_e(v, extra):
-        ft = helper.submit(ctx_e.tmc_raw, v, vol.iso, extra)
-        md = ctx.dmc_raw(v, vol.iso, dmc_flags | extra)
-        return ft.result(), md
-
-    for _ in range(max(1, args.warmup)):
-        mt, md = step_e(vhost, native.OUT_HOST)
-        ctx_e.free(mt)
-        ctx.free(md)
-    link_before = link_bandwidth(torch)
-    barrier()
-    d2h = 0
-    step_ms = []
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
+    def step_lane(li):
+        ln = lanes[li]
         ts = time.perf_counter()
-        mt, md = step_e(vhost, native.OUT_HOST)
-        d2h = (24 * mt.nr_v + 12 * mt.nr_t) + (24 * md.nr_v + 16 * md.nr_q + 12 * md.nr_t + 16 * md.nr_he +
-                                                 4 * md.nr_v + 4 * md.nr_q)
-        ctx_e.free(mt)
-        ctx.free(md)
-        step_ms.append(round((time.perf_counter() - ts) * 1e3, 2))
+        ft = ln["helper"].submit(ln["tmc"].tmc_raw, vhost, vol.iso, native.OUT_HOST)
+        md = ln["dmc"].dmc_raw(vhost, vol.iso, dmc_flags | native.OUT_HOST)
+        mt = ft.result()
+        nbytes = (24 * mt.nr_v + 12 * mt.nr_t) + (24 * md.nr_v + 16 * md.nr_q + 12 * md.nr_t + 16 * md.nr_he +
+                                                  4 * md.nr_v + 4 * md.nr_q)
+        ln["tmc"].free(mt)
+        ln["dmc"].free(md)
+        return nbytes, round((time.perf_counter() - ts) * 1e3, 2)
+
+    def run_steps(k, in_flight):
+        futs = [lanes[q % in_flight]["runner"].submit(step_lane, q % in_flight) for q in range(k)]
+        return [f.result() for f in futs]
+
+    run_steps(max(1, args.warmup) * len(lanes), len(lanes))
+    link_before = link_bandwidth(torch)
+    # one step at a time (the latency of a step)
     barrier()
-    ctx_e.close()
+    t0 = time.perf_counter()
+    serial = run_steps(args.steps, 1)
+    barrier()
+    serial_s = max_over_ranks(time.perf_counter() - t0)
+    # steps in flight (the throughput)
+    barrier()
+    t0 = time.perf_counter()
+    res = run_steps(args.steps, len(lanes))
+    barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
+    d2h = res[-1][0]
+    step_ms = [r[1] for r in serial]
     e2e = throughput(world, cells, args.steps, e2e_s)
+    e2e_serial = throughput(world, cells, args.steps, serial_s)
+    for li, ln in enumerate(lanes):
+        ln["helper"].shutdown()
+        ln["runner"].shutdown()
+        ln["tmc"].close()
+        if li:
+            ln["dmc"].close()
     link_after = link_bandwidth(torch)
     # ---- per-stage profile (separate pass, not timed above) ----
     ctx.set_profiling(True)
@@ -339,11 +364,16 @@ def run_ours(args, rank, world, local):
                    "l2": f"inputs larger than L2 ({4 * voxels / 2**20:.0f} MiB field)", "parallelism": f"replicas x{world}",
                    "streams": "the TMC and the DMC extraction of a step run concurrently, one context (stream) each; "
                               "in the end-to-end steps the TMC context has the higher stream priority (its output "
-                              "then crosses the host link while DMC computes); the stage profile and the roofline "
-                              "come from a separate sequential pass"},
+                              "then crosses the host link while DMC computes), and `in_flight` steps run at once, "
+                              "each on its own pair of contexts and thread, so that one step's meshes cross the "
+                              "link while the next computes; the stage profile and the roofline come from a "
+                              "separate sequential pass"},
         "mesh": sizes,
         "e2e": {"value": round(e2e, 4), "unit": "Gcells/s", "h2d_bytes_per_step": 2 * 4 * voxels,
-                "d2h_bytes_per_step": int(d2h), "step_ms": step_ms,
+                "d2h_bytes_per_step": int(d2h), "in_flight": len(lanes),
+                "ms_per_step": round(e2e_s * 1e3 / args.steps, 3),
+                "one_at_a_time": {"value": round(e2e_serial, 4), "step_ms": step_ms,
+                                  "note": "the same steps one after another (each step's latency)"},
                 "host_link_gbs": {"before": link_before, "after": link_after,
                                   "note": "pinned 256 MiB copies each way, measured just before and after the "
                                           "end-to-end steps; the link is shared with the machine's other GPUs"}},
