@@ -113,6 +113,14 @@ __device__ __forceinline__ void cell_trilinear3(const double q[8][3], double u, 
              w * ((1 - v) * (q[4][d] + u * (q[5][d] - q[4][d])) + v * (q[6][d] + u * (q[7][d] - q[6][d])));
 }
 
+// The isovalue's parameter on crossed edge e (t_mc's edge coordinates, mc/MarchingCubes.cpp:241-254),
+// float64.  p_slice reads them only on a singular face and in the tunnel / hexagon branch, so they
+// are computed there, not for every ambiguous cell.
+__device__ __forceinline__ double edge_coord(const double F[8], double iso, int e) {
+  const int v0 = edge_v0(e), v1 = edge_v1(e);
+  return (iso - F[v0]) / (F[v1] - F[v0]);
+}
+
 // e_vert (mc/MarchingCubes.cpp:902-911): local coordinate d of the point on edge e
 __device__ __forceinline__ double e_vert(const double ecoord[12], int e, int d) {
   return (edge_axis(e) == d) ? ecoord[e] : (double)((edge_off(e) >> d) & 1);
@@ -196,9 +204,9 @@ __device__ __forceinline__ void inner_vertex(const double (*P)[3], const double 
   }
 }
 
-__device__ AmbResult p_slice_dev(unsigned ic, const double F[8], double iso, const double ecoord[12],
-                                 const int32_t vid[12], int32_t ibase, TriSink& tri, const double (*P)[3],
-                                 const double (*N)[3], const InnerOut* geo, double* prm) {
+__device__ AmbResult p_slice_dev(unsigned ic, const double F[8], double iso, const int32_t vid[12], int32_t ibase,
+                                 TriSink& tri, const double (*P)[3], const double (*N)[3], const InnerOut* geo,
+                                 double* prm) {
   AmbResult res{0, false};
   uint64_t to = ~0ull;
   int f_flag = 0;
@@ -219,7 +227,9 @@ __device__ AmbResult p_slice_dev(unsigned ic, const double F[8], double iso, con
       else {
         f_flag |= 1 << f;
         const unsigned e_flag = 0x218;
-        double ec0 = ecoord[nib(fe, 0)], ec1 = ecoord[nib(fe, 1)], ec2 = ecoord[nib(fe, 2)], ec3 = ecoord[nib(fe, 3)];
+        // an ambiguous face: its four edges are crossed
+        double ec0 = edge_coord(F, iso, nib(fe, 0)), ec1 = edge_coord(F, iso, nib(fe, 1)),
+               ec2 = edge_coord(F, iso, nib(fe, 2)), ec3 = edge_coord(F, iso, nib(fe, 3));
         if ((e_flag >> (f * 2)) & 1) { ec0 = 1 - ec0; ec2 = 1 - ec2; }
         if ((e_flag >> (f * 2)) & 2) { ec1 = 1 - ec1; ec3 = 1 - ec3; }
         const bool c1 = (ec1 < ec3 && ec0 > ec2), c2 = (ec1 > ec3 && ec0 < ec2);
@@ -279,6 +289,9 @@ __device__ AmbResult p_slice_dev(unsigned ic, const double F[8], double iso, con
 
   if (__popc(q_sol) == 6) {
     // tunnel or 12-vertex contour: inner hexagon (:831-1083)
+    double ecoord[12];
+    const uint32_t emask = case_edge_mask(ic);
+    for (int e = 0; e < 12; e++) ecoord[e] = (emask >> e) & 1 ? edge_coord(F, iso, e) : 0.0;
     double hvt[6][3];
     hex_corners(ui, vi, wi, hvt);
     int not_tunnel = 0xF;
@@ -455,12 +468,11 @@ __device__ AmbResult p_slice_dev(unsigned ic, const double F[8], double iso, con
   return res;
 }
 
-// corner data of an ambiguous cell in float64: values, positions, normals, edge parameters
+// corner data of an ambiguous cell in float64: values, positions, normals
 struct AmbCell {
   double F[8];
   double P[8][3];
   double N[8][3];
-  double ec[12];
 };
 
 // corner positions and gradients (the inner vertices' trilinear sources)
@@ -541,17 +553,9 @@ __device__ __forceinline__ bool inner_vertex_ff(const double (*P)[3], const ffx:
   return true;
 }
 
-__device__ void load_amb_cell(const Grid& g, int i, int j, int k, const float u[8], uint32_t emask, AmbCell& a,
-                              bool geometry) {
+__device__ void load_amb_cell(const Grid& g, int i, int j, int k, const float u[8], AmbCell& a, bool geometry) {
 #pragma unroll
   for (int q = 0; q < 8; q++) a.F[q] = u[q];
-  for (int e = 0; e < 12; e++) {
-    a.ec[e] = 0;
-    if (emask & (1u << e)) {
-      const int v0 = edge_v0(e), v1 = edge_v1(e);
-      a.ec[e] = (g.iso - a.F[v0]) / (a.F[v1] - a.F[v0]);
-    }
-  }
   if (geometry) amb_geometry(g, i, j, k, a.P, a.N);
 }
 
@@ -687,12 +691,12 @@ __global__ void __launch_bounds__(128) tmc_amb_count_kernel(CellSpace space, con
 #pragma unroll
     for (int v = 0; v < 8; v++) cs |= (unsigned)(u[v] >= g.iso_up) << v;
     AmbCell amb;
-    load_amb_cell(g, i, j, k, u, case_edge_mask(cs), amb, false);
+    load_amb_cell(g, i, j, k, u, amb, false);
     int32_t vid[12];
     for (int e = 0; e < 12; e++) vid[e] = e;  // local codes: edges 0..11, inner vertices from 12
     AmbRec& R = recs[a];
     TriSink ts{nullptr, R.tri, 0};
-    const AmbResult ar = p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, 12, ts, amb.P, amb.N, nullptr, R.prm);
+    const AmbResult ar = p_slice_dev(cs, amb.F, g.iso, vid, 12, ts, amb.P, amb.N, nullptr, R.prm);
     R.slot = slot;
     R.info = cs | (uint32_t)ts.n << 8 | (uint32_t)ar.inner << 14 | (ts.n > kAmbRecTris ? (1u << 17) : 0u) |
              (ar.error ? (1u << 18) : 0u);
@@ -883,9 +887,9 @@ __global__ void __launch_bounds__(128) tmc_ambiguous_kernel(CellSpace space, con
       float u[8];
       tload_corners(g, i, j, k, u);
       AmbCell amb;
-      load_amb_cell(g, i, j, k, u, em, amb, ni > 0);
+      load_amb_cell(g, i, j, k, u, amb, ni > 0);
       TriSink ts{t, nullptr, 0};
-      p_slice_dev(cs, amb.F, g.iso, amb.ec, vid, ibase, ts, amb.P, amb.N, &io, nullptr);
+      p_slice_dev(cs, amb.F, g.iso, vid, ibase, ts, amb.P, amb.N, &io, nullptr);
       continue;
     }
     for (int q = 0; q < nt; q++) {
