@@ -136,35 +136,42 @@ __global__ void __launch_bounds__(128) dmc_amb_kernel(CellSpace space, const uin
 // In-tile exclusive scan of the listed cells' records -> their vertex and quad offsets (blocked:
 // 16-byte record loads and offset stores over the tile's slots, one block scan of the thread
 // totals), and two entries per vertex: the slot of the cell that generates it and its rank there.
-__global__ void __launch_bounds__(kScanThreads) dmc_offsets_kernel(const CellMask* mask, const uint32_t* rec,
-                                                                  const unsigned long long* tile_off,
-                                                                  int32_t* voff, int32_t* qoff, uint32_t* vwork,
-                                                                  uint8_t* vrank) {
-  const int64_t base = (int64_t)blockIdx.x * kScanTile;
-  const int64_t end = base + tile_listed(mask, blockIdx.x);
-  const int64_t first = base + (int64_t)threadIdx.x * kScanItems;
-  uint32_t r[kScanItems];
-  load8(rec, first, end, r);
-  unsigned long long sum = 0;
+__global__ void __launch_bounds__(32 * kOffsetWarps) dmc_offsets_kernel(const CellMask* mask, const uint32_t* rec,
+                                                                       const unsigned long long* tile_off,
+                                                                       int64_t tiles, int32_t* voff, int32_t* qoff,
+                                                                       uint32_t* vwork, uint8_t* vrank) {
+  const int lane = threadIdx.x & 31;
+  const int64_t tile = (int64_t)blockIdx.x * kOffsetWarps + (threadIdx.x >> 5);
+  if (tile >= tiles) return;  // the whole warp
+  const int64_t base = tile * kScanTile;
+  const int64_t end = base + tile_listed(mask, tile);
+  unsigned long long carry = tile_off[tile];
+  for (int64_t step = base; step < end; step += kOffsetStep) {  // warp-uniform
+    const int64_t first = step + (int64_t)lane * kScanItems;
+    uint32_t r[kScanItems];
+    load8(rec, first, end, r);
+    unsigned long long sum = 0;
 #pragma unroll
-  for (int s = 0; s < kScanItems; s++) sum += ((unsigned long long)rec_nv(r[s]) << 32) | rec_nq(r[s]);
-  unsigned long long tot;
-  unsigned long long pre = tile_off[blockIdx.x] + block_exclusive_scan(sum, &tot);
-  int32_t vo[kScanItems], qo[kScanItems];
+    for (int s = 0; s < kScanItems; s++) sum += ((unsigned long long)rec_nv(r[s]) << 32) | rec_nq(r[s]);
+    const unsigned long long inc = warp_inclusive_scan(sum);
+    unsigned long long pre = carry + inc - sum;
+    carry += __shfl_sync(0xffffffffu, inc, 31);
+    int32_t vo[kScanItems], qo[kScanItems];
 #pragma unroll
-  for (int s = 0; s < kScanItems; s++) {
-    vo[s] = (int32_t)(pre >> 32);
-    qo[s] = (int32_t)(pre & 0xffffffffull);
-    pre += ((unsigned long long)rec_nv(r[s]) << 32) | rec_nq(r[s]);
-  }
-  store8(voff, first, end, vo);
-  store8(qoff, first, end, qo);
-#pragma unroll
-  for (int s = 0; s < kScanItems; s++)
-    for (int q = 0; q < rec_nv(r[s]); q++) {  // empty beyond the listed cells
-      vwork[vo[s] + q] = (uint32_t)(first + s);
-      vrank[vo[s] + q] = (uint8_t)q;
+    for (int s = 0; s < kScanItems; s++) {
+      vo[s] = (int32_t)(pre >> 32);
+      qo[s] = (int32_t)(pre & 0xffffffffull);
+      pre += ((unsigned long long)rec_nv(r[s]) << 32) | rec_nq(r[s]);
     }
+    store8(voff, first, end, vo);
+    store8(qoff, first, end, qo);
+#pragma unroll
+    for (int s = 0; s < kScanItems; s++)
+      for (int q = 0; q < rec_nv(r[s]); q++) {  // empty beyond the listed cells
+        vwork[vo[s] + q] = (uint32_t)(first + s);
+        vrank[vo[s] + q] = (uint8_t)q;
+      }
+  }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -895,8 +902,9 @@ int dmc_front_emit(const CellSpace& space, DmcScratch& s, DmcVertexOut vo, int64
   {
     // per-cell offsets and the vertex work list (needs the vertex count for its size)
     Stage t(prof, "dmc_scan", st);
-    dmc_offsets_kernel<<<(unsigned)ceil_div(n, kScanTile), kScanThreads, 0, st>>>(s.mask, s.rec, s.tile_sums, s.voff,
-                                                                                  s.qoff, s.vwork, s.vrank);
+    const int64_t tiles = ceil_div(n, kScanTile);
+    dmc_offsets_kernel<<<(unsigned)ceil_div(tiles, kOffsetWarps), 32 * kOffsetWarps, 0, st>>>(
+        s.mask, s.rec, s.tile_sums, tiles, s.voff, s.qoff, s.vwork, s.vrank);
   }
   // per-vertex grids: whole waves of each kernel's resident blocks
   static const int r_setup = resident_blocks(dmc_vertex_setup_kernel, kVertexThreads);

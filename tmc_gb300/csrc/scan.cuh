@@ -84,6 +84,23 @@ __device__ __forceinline__ void store8(int32_t* p, int64_t first, int64_t n, con
   }
 }
 
+// In-tile offsets with one warp per tile: the tile's listed slots are walked 256 at a time, each
+// lane owning 8 consecutive slots (the blocked accessors above), scanned with warp shuffles and a
+// carry from one step to the next; no block barrier, and a tile's few listed slots (a few hundred
+// of its 2048) cost a step or two.
+constexpr int kOffsetWarps = 8;  // tiles per block
+constexpr int kOffsetStep = 32 * kScanItems;
+// inclusive warp scan of a 64-bit value (all lanes of the warp take part)
+__device__ __forceinline__ unsigned long long warp_inclusive_scan(unsigned long long x) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  return x;
+}
+
 // Two counters packed in one 64-bit word (high: a, low: b) scan together: both stay far below
 // 2^32 per tile, so carries never cross.
 struct Pair {

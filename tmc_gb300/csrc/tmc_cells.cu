@@ -710,28 +710,35 @@ __global__ void __launch_bounds__(128) tmc_amb_count_kernel(CellSpace space, con
 
 // In-tile exclusive scan of the listed cells' records -> their vertex and triangle offsets (blocked
 // layout over the tile's slots).
-__global__ void __launch_bounds__(kScanThreads) tmc_offsets_kernel(const CellMask* mask, const uint32_t* rec,
-                                                                  const unsigned long long* tile_off,
-                                                                  int32_t* voff, int32_t* toff) {
-  const int64_t base = (int64_t)blockIdx.x * kScanTile;
-  const int64_t end = base + tile_listed(mask, blockIdx.x);
-  const int64_t first = base + (int64_t)threadIdx.x * kScanItems;
-  uint32_t r[kScanItems];
-  load8(rec, first, end, r);
-  unsigned long long sum = 0;
+__global__ void __launch_bounds__(32 * kOffsetWarps) tmc_offsets_kernel(const CellMask* mask, const uint32_t* rec,
+                                                                       const unsigned long long* tile_off,
+                                                                       int64_t tiles, int32_t* voff, int32_t* toff) {
+  const int lane = threadIdx.x & 31;
+  const int64_t tile = (int64_t)blockIdx.x * kOffsetWarps + (threadIdx.x >> 5);
+  if (tile >= tiles) return;  // the whole warp
+  const int64_t base = tile * kScanTile;
+  const int64_t end = base + tile_listed(mask, tile);
+  unsigned long long carry = tile_off[tile];
+  for (int64_t step = base; step < end; step += kOffsetStep) {  // warp-uniform
+    const int64_t first = step + (int64_t)lane * kScanItems;
+    uint32_t r[kScanItems];
+    load8(rec, first, end, r);
+    unsigned long long sum = 0;
 #pragma unroll
-  for (int s = 0; s < kScanItems; s++) sum += ((unsigned long long)trec_nv(r[s]) << 32) | trec_ntri(r[s]);
-  unsigned long long tot;
-  unsigned long long pre = tile_off[blockIdx.x] + block_exclusive_scan(sum, &tot);
-  int32_t vo[kScanItems], to[kScanItems];
+    for (int s = 0; s < kScanItems; s++) sum += ((unsigned long long)trec_nv(r[s]) << 32) | trec_ntri(r[s]);
+    const unsigned long long inc = warp_inclusive_scan(sum);
+    unsigned long long pre = carry + inc - sum;
+    carry += __shfl_sync(0xffffffffu, inc, 31);
+    int32_t vo[kScanItems], to[kScanItems];
 #pragma unroll
-  for (int s = 0; s < kScanItems; s++) {
-    vo[s] = (int32_t)(pre >> 32);
-    to[s] = (int32_t)(pre & 0xffffffffull);
-    pre += ((unsigned long long)trec_nv(r[s]) << 32) | trec_ntri(r[s]);
+    for (int s = 0; s < kScanItems; s++) {
+      vo[s] = (int32_t)(pre >> 32);
+      to[s] = (int32_t)(pre & 0xffffffffull);
+      pre += ((unsigned long long)trec_nv(r[s]) << 32) | trec_ntri(r[s]);
+    }
+    store8(voff, first, end, vo);
+    store8(toff, first, end, to);
   }
-  store8(voff, first, end, vo);
-  store8(toff, first, end, to);
 }
 
 // corner value v of a cell's eight (selects, so that a run-time index keeps u in registers)
@@ -1088,7 +1095,8 @@ int tmc_count(const CellSpace& space, TmcScratch& s, int64_t n_amb, int sms, cud
   }
   Stage t(prof, "tmc_scan", st);
   scan_tile_sums_kernel<<<1, 1024, 0, st>>>(s.tile_sums, tiles, s.totals);
-  tmc_offsets_kernel<<<(unsigned)tiles, kScanThreads, 0, st>>>(s.mask, s.rec, s.tile_sums, s.voff, s.toff);
+  tmc_offsets_kernel<<<(unsigned)ceil_div(tiles, kOffsetWarps), 32 * kOffsetWarps, 0, st>>>(s.mask, s.rec, s.tile_sums,
+                                                                                           tiles, s.voff, s.toff);
   return k + 2;
 }
 
