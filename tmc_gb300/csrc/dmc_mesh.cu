@@ -339,9 +339,10 @@ __global__ void float_outputs_kernel(const double* v64, const double* n64, int64
 // removeVertices3X3Y / removeVertices3333 (:1096-1112, :1324-1338): kept vertices move to their
 // new index, which becomes their map entry.  One thread per vertex component (x, y or z of the
 // float64 positions and normals): every load and store is unit-stride across the warp.
+// vo, no: the float32 outputs of the kept vertices (the roundings float_outputs_kernel makes), or null
 __global__ void gather_vertices_kernel(const uint8_t* keep, const int32_t* idx, int64_t nv, const double* v64,
                                        const double* n64, double* v64o, double* n64o, int32_t* map, int64_t cap,
-                                       unsigned* overflow) {
+                                       unsigned* overflow, float* vo, float* no) {
   FOR_EACH(e, 3 * nv) {
     const int64_t i = e / 3;
     if (!keep[i]) continue;
@@ -351,8 +352,13 @@ __global__ void gather_vertices_kernel(const uint8_t* keep, const int32_t* idx, 
       if (d == 0) atomicAdd(overflow, 1u);
       continue;
     }
-    v64o[3 * o + d] = v64[e];
-    n64o[3 * o + d] = n64[e];
+    const double x = v64[e], nn = n64[e];
+    v64o[3 * o + d] = x;
+    n64o[3 * o + d] = nn;
+    if (vo) {
+      vo[3 * o + d] = (float)x;
+      no[3 * o + d] = reinterpret_cast<const float2*>(n64)[e].x;
+    }
     if (d == 0) map[i] = (int32_t)o;
   }
 }
@@ -898,7 +904,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
       nx.nq = nq2;
       // vertex map into vm_second (free after the passes)
       gather_vertices_kernel<<<grid_for(3 * nv0, sms), 256, 0, st>>>(valive, idx, nv0, cur.v64, cur.n64, nx.v64,
-                                                                     nx.n64, vm_second, nv2, hw.ovf);
+                                                                     nx.n64, vm_second, nv2, hw.ovf, nx.v, nx.n);
       gather_live_quads_kernel<<<gq, 256, 0, st>>>(alive, idx_q, nq0, q0, vm_second, nx.quads, hw.src, nq2, hw.ovf);
       s.launches += 2;
       // the inherited colours are only read by the colour pass; they are not carried along
@@ -911,8 +917,8 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
       compacted = true;
     }
   }
-  // the float32 outputs of the simplified mesh
-  if (s.err == cudaSuccess && simplify && cur.nv > 0) {
+  // the float32 outputs of the simplified mesh (the compaction's gather writes them when it ran)
+  if (s.err == cudaSuccess && simplify && !compacted && cur.nv > 0) {
     float_outputs_kernel<<<grid_for(3 * cur.nv, sms), 256, 0, st>>>(cur.v64, cur.n64, 3 * cur.nv, cur.v, cur.n);
     s.launches += 1;
   }
