@@ -295,13 +295,13 @@ def run_ours(args, rank, world, local):
 
     run_steps(max(1, args.warmup) * len(lanes), len(lanes))
     link_before = link_bandwidth(torch)
-    # one step at a time (the latency of a step)
+    # one step at a time: the line's e2e value (steady across runs)
     barrier()
     t0 = time.perf_counter()
     serial = run_steps(args.steps, 1)
     barrier()
     serial_s = max_over_ranks(time.perf_counter() - t0)
-    # steps in flight (the throughput): every lane runs the same number of steps, at least four, so
+    # steps in flight (e2e.in_flight; host-load dependent): every lane runs the same number of steps, at least four, so
     # that the measurement covers the lanes' steady state rather than their start and a lone last step
     e2e_steps = len(lanes) * max(4, -(-args.steps // len(lanes)))
     barrier()
@@ -378,11 +378,15 @@ def run_ours(args, rank, world, local):
                               "link while the next computes; the stage profile and the roofline come from a "
                               "separate sequential pass"},
         "mesh": sizes,
-        "e2e": {"value": round(e2e, 4), "unit": "Gcells/s", "h2d_bytes_per_step": 2 * 4 * voxels,
-                "d2h_bytes_per_step": int(d2h), "in_flight": len(lanes), "steps": e2e_steps,
-                "ms_per_step": round(e2e_s * 1e3 / e2e_steps, 3),
-                "one_at_a_time": {"value": round(e2e_serial, 4), "step_ms": step_ms,
-                                  "note": "the same steps one after another (each step's latency)"},
+        "e2e": {"value": round(e2e_serial, 4), "unit": "Gcells/s", "h2d_bytes_per_step": 2 * 4 * voxels,
+                "d2h_bytes_per_step": int(d2h), "steps": args.steps,
+                "ms_per_step": round(serial_s * 1e3 / args.steps, 3), "step_ms": step_ms,
+                "in_flight": {"value": round(e2e, 4), "lanes": len(lanes), "steps": e2e_steps,
+                              "ms_per_step": round(e2e_s * 1e3 / e2e_steps, 3),
+                              "note": "the same steps with several in flight (lanes of contexts and threads at "
+                                      "different stream priorities): one step's meshes cross the link while "
+                                      "another computes; this throughput depends on the host's load (threads "
+                                      "driving the lanes), so the line's value is the one-step-at-a-time one"},
                 "host_link_gbs": {"before": link_before, "after": link_after,
                                   "note": "pinned 256 MiB copies each way, measured just before and after the "
                                           "end-to-end steps; the link is shared with the machine's other GPUs"}},

@@ -20,6 +20,7 @@
 #include "dmc_mesh.h"
 #include "ffloat.cuh"
 #include "halfedges.h"
+#include "host_wait.h"
 #include "libm_acosf.h"
 #include "scan.cuh"
 
@@ -877,7 +878,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
     s.launches += scan_flags(valive, nv0, idx, tiles, total, st);
     s.launches += scan_flags(alive, nq0, idx_q, tiles, total + 1, st);
     cudaMemcpyAsync(h_cnt, total, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
-    cudaStreamSynchronize(st);
+    host_wait(st);
     const int64_t nv2 = (int64_t)h_cnt[0], nq2 = (int64_t)h_cnt[1];
     // nothing died: no pass changed the mesh, and it stays as it is (with its halfedges)
     if (nv2 != nv0 || nq2 != nq0) {
@@ -952,7 +953,7 @@ DmcPostStatus dmc_postprocess(const DmcMesh& in, uint32_t flags, int sms, cudaSt
         (*ready)(hf, (size_t)cur.nq * sizeof(int32_t));
       }
       cudaMemcpyAsync(h_cnt + 1, hw.nm, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
-      cudaStreamSynchronize(st);
+      host_wait(st);
       out->non_manifold = (int64_t)h_cnt[1];
       out->nhe = 4 * cur.nq;
       out->he = (int32_t*)he4;

@@ -20,6 +20,7 @@
 #include "ffloat.cuh"
 #include "generators.cuh"
 #include "halfedges.h"
+#include "host_wait.h"
 #include "scan.cuh"
 #include "profiler.h"
 #include "tmc_cells.h"
@@ -118,7 +119,7 @@ struct Allocs {
 cudaError_t tmc_ambiguous_records(tmc_ctx* ctx, Allocs& al, tmc::TmcScratch& sc, int64_t& n_amb) {
   unsigned* h = (unsigned*)ctx->h_pinned + 320;
   cudaError_t e = cudaMemcpyAsync(h, sc.amb_n, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess) e = tmc::host_wait(ctx->stream);
   if (e != cudaSuccess) return e;
   n_amb = (int64_t)*h;
   const size_t na = (size_t)std::max<int64_t>(n_amb, 1);
@@ -180,7 +181,7 @@ tmc_status check_field_numeric(tmc_ctx* ctx, const float* field, const tmc_volum
   ctx->launches += 1;
   unsigned* h = (unsigned*)ctx->h_pinned + 256;
   TMC_CUDA(ctx, cudaMemcpyAsync(h, flag, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
-  TMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  TMC_CUDA(ctx, tmc::host_wait(ctx->stream));
   if (*h) return fail(ctx, TMC_ERR_NUMERIC, "the field holds NaN or Inf");
   return TMC_OK;
 }
@@ -358,7 +359,7 @@ tmc_status finish_mesh(tmc_ctx* ctx, uint32_t flags, tmc_mesh* out, MeshPriv* mp
     if ((s = to_host(ctx, &out->vcell, nv, mp, early))) return s;
     if ((s = to_host(ctx, &out->vuvw, 3 * nv, mp, early))) return s;
     if (early) TMC_CUDA(ctx, early->join());
-    TMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    TMC_CUDA(ctx, tmc::host_wait(ctx->stream));
     for (void* p : mp->dev) cudaFreeAsync(p, ctx->stream);
     mp->dev.clear();
     mp->shared.reset();
@@ -477,12 +478,12 @@ tmc_status tmc_ctx_create(int device, const tmc_ctx_opts* opts, tmc_ctx** out) {
 tmc_status tmc_ctx_destroy(tmc_ctx* ctx) {
   if (!ctx) return TMC_ERR_INVALID_ARG;
   cudaSetDevice(ctx->device);
-  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->stream) tmc::host_wait(ctx->stream);
   if (ctx->d_stats) cudaFree(ctx->d_stats);
   ctx->pinned.reset();  // the last context using the pool frees its blocks
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   if (ctx->copy_stream) {
-    cudaStreamSynchronize(ctx->copy_stream);
+    tmc::host_wait(ctx->copy_stream);
     cudaStreamDestroy(ctx->copy_stream);
   }
   if (ctx->copy_event) cudaEventDestroy(ctx->copy_event);
@@ -498,13 +499,13 @@ int64_t tmc_ctx_launch_count(const tmc_ctx* ctx) { return ctx ? ctx->launches.lo
 
 tmc_status tmc_ctx_synchronize(tmc_ctx* ctx) {
   if (!ctx) return TMC_ERR_INVALID_ARG;
-  TMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  TMC_CUDA(ctx, tmc::host_wait(ctx->stream));
   return TMC_OK;
 }
 
 tmc_status tmc_ctx_set_profiling(tmc_ctx* ctx, int on) {
   if (!ctx) return TMC_ERR_INVALID_ARG;
-  TMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  TMC_CUDA(ctx, tmc::host_wait(ctx->stream));
   ctx->prof.collect();
   ctx->prof.on = on != 0;
   ctx->prof.acc.clear();
@@ -564,7 +565,7 @@ tmc_status tmc_ctx_get_tuning(const tmc_ctx* ctx, int32_t key, int64_t* value) {
 
 int32_t tmc_ctx_profile_read(tmc_ctx* ctx, int32_t max, char* names, double* ms, int64_t* counts) {
   if (!ctx) return -1;
-  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return -1;
+  if (tmc::host_wait(ctx->stream) != cudaSuccess) return -1;
   ctx->prof.collect();
   int32_t i = 0;
   for (auto& kv : ctx->prof.acc) {
@@ -587,7 +588,7 @@ tmc_status tmc_mesh_free(tmc_ctx* ctx, tmc_mesh* mesh) {
     cudaSetDevice(ctx->device);
     for (void* p : mp->dev) cudaFreeAsync(p, ctx->stream);
     mp->shared.reset();
-    cudaStreamSynchronize(ctx->stream);  // the next call may reuse these pinned blocks
+    tmc::host_wait(ctx->stream);  // the next call may reuse these pinned blocks
     for (void* p : mp->host) ctx->pinned_put(p);
     delete mp;
   }
@@ -622,7 +623,7 @@ tmc_status tmc_dmc_color_valence(tmc_ctx* ctx, int64_t nr_v, int64_t nr_q, const
   const tmc::DmcPostStatus ps = tmc::dmc_color_valence(quads, nr_q, nr_v, colors, valence, ctx->sms, ctx->stream);
   ctx->launches += ps.launches;
   TMC_CUDA(ctx, ps.err);
-  TMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  TMC_CUDA(ctx, tmc::host_wait(ctx->stream));
   return TMC_OK;
 }
 
@@ -670,7 +671,7 @@ tmc_status dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   ctx->launches += tmc::dmc_front_count(space, sc, st, &ctx->prof, gates.data(), (int)gates.size());
   unsigned long long* h = (unsigned long long*)ctx->h_pinned;
   TMC_CUDA(ctx, cudaMemcpyAsync(h, sc.totals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-  TMC_CUDA(ctx, cudaStreamSynchronize(st));
+  TMC_CUDA(ctx, tmc::host_wait(st));
   const int64_t nv = (int64_t)(h[0] >> 32), nq = (int64_t)(h[0] & 0xffffffffull);
 
   MeshPriv* mp = new (std::nothrow) MeshPriv();
@@ -736,7 +737,7 @@ tmc_status dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
                            false, (flags & TMC_OUT_HOST) ? &ready : nullptr);
   if (ps.err == cudaSuccess) ps.err = early.err;
   if (ps.err != cudaSuccess) {
-    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    if (ctx->copy_stream) tmc::host_wait(ctx->copy_stream);
     for (void* p : mp->host) ctx->pinned_put(p);
     delete mp;
     TMC_CUDA(ctx, ps.err);
@@ -785,7 +786,7 @@ tmc_status dmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   out->vcell = vo.vcell;
   out->vuvw = vo.vuvw;
   TMC_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-  TMC_CUDA(ctx, cudaStreamSynchronize(st));
+  TMC_CUDA(ctx, tmc::host_wait(st));
   for (int q = 0; q < 8; q++) out->stats[q] = (int64_t)h[q];
   ctx->prof.collect();
   out->stats[4] = post.non_manifold;
@@ -836,7 +837,7 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   ctx->launches += tmc::tmc_count(space, sc, n_amb, ctx->sms, st, &ctx->prof);
   TMC_CUDA(ctx, cudaMemcpyAsync(h, sc.totals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   TMC_CUDA(ctx, cudaMemcpyAsync(h + 1, sc.stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-  TMC_CUDA(ctx, cudaStreamSynchronize(st));
+  TMC_CUDA(ctx, tmc::host_wait(st));
   const int64_t nv = (int64_t)(h[0] >> 32), nt = (int64_t)(h[0] & 0xffffffffull);
 
   MeshPriv* mp = new (std::nothrow) MeshPriv();
@@ -875,7 +876,7 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
     early.issue(vo.v64, (size_t)nv * 3 * sizeof(double));
     early.issue(tris, (size_t)nt * 3 * sizeof(int32_t));
     if (early.err != cudaSuccess) {
-      if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+      if (ctx->copy_stream) tmc::host_wait(ctx->copy_stream);
       for (void* p : mp->host) ctx->pinned_put(p);
       delete mp;
       TMC_CUDA(ctx, early.err);
@@ -906,7 +907,7 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
     ctx->launches += tmc::pack_halfedges4(tris, 3, twin, nh, he4, hf, ctx->sms, st);
     TMC_CUDA(ctx, cudaGetLastError());
     TMC_CUDA(ctx, cudaMemcpyAsync(h + 8, w.non_manifold, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-    TMC_CUDA(ctx, cudaStreamSynchronize(st));
+    TMC_CUDA(ctx, tmc::host_wait(st));
     non_manifold = (int64_t)h[8];
     out->nr_he = nh;
     out->he = he4;
@@ -915,7 +916,7 @@ tmc_status tmc_extract(tmc_ctx* ctx, const tmc_volume* vol, double iso, uint32_t
   }
 #undef TMC_OWN
   TMC_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-  TMC_CUDA(ctx, cudaStreamSynchronize(st));
+  TMC_CUDA(ctx, tmc::host_wait(st));
   for (int q = 0; q < 8; q++) out->stats[q] = (int64_t)h[q];
   ctx->prof.collect();
   out->stats[4] = non_manifold;
@@ -1027,7 +1028,7 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
   TMC_CUDA(ctx, cudaMemcpyAsync(toff.data(), tile_sums, tiles * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   TMC_CUDA(ctx, cudaMemcpyAsync(h, totals, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   TMC_CUDA(ctx, cudaMemcpyAsync(h + 1, ctx->d_stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-  TMC_CUDA(ctx, cudaStreamSynchronize(st));
+  TMC_CUDA(ctx, tmc::host_wait(st));
   toff[(size_t)tiles] = h[0];
   const int64_t NV = (int64_t)(h[0] >> 32), NF = (int64_t)(h[0] & 0xffffffffull);
   if (NV >= ((int64_t)1 << 31) || NF >= ((int64_t)1 << 31))
@@ -1185,7 +1186,7 @@ tmc_status batch_run(tmc_ctx* ctx, const std::vector<int>& idx, const tmc_reques
         ctx->launches += tmc::pack_halfedges4(out->tris, 3, twin, nh, he4, hf, ctx->sms, st);
         TMC_CUDA(ctx, cudaGetLastError());
         TMC_CUDA(ctx, cudaMemcpyAsync(h + 8, w.non_manifold, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-        TMC_CUDA(ctx, cudaStreamSynchronize(st));
+        TMC_CUDA(ctx, tmc::host_wait(st));
         out->stats[4] = (int64_t)h[8];
         out->nr_he = nh;
         out->he = he4;
