@@ -135,7 +135,7 @@ __device__ __forceinline__ uint32_t tile_listed(const CellMask* mask, int64_t ti
 // cells processed at any moment, and the field around them, stay within a narrow band that the L2
 // holds.
 constexpr int64_t kChunkWindow = 512;
-__device__ __forceinline__ void slot_chunk(int64_t q, int64_t tiles, int64_t& tile, uint32_t& first) {
+__host__ __device__ __forceinline__ void slot_chunk(int64_t q, int64_t tiles, int64_t& tile, uint32_t& first) {
   const int64_t per = kChunkWindow << (kTileShift - 5);  // chunks of a full window (32 slots each)
   const int64_t win = q / per;
   const int64_t t0 = win * kChunkWindow;
