@@ -9,26 +9,29 @@
 
 namespace tmc {
 
-// Waits for the work queued on `st` so far (the stream's device must be the current device).
+// Waits for the work queued on `st` so far.  The event belongs to the current device; when it
+// cannot be recorded on `st` (a stream of another device, or an event left from before a device
+// reset, which is replaced once) the wait falls back to cudaStreamSynchronize.
 inline cudaError_t host_wait(cudaStream_t st) {
   int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return cudaStreamSynchronize(st);
+  }
   thread_local std::vector<cudaEvent_t> events;  // by device
   if ((int)events.size() <= dev) events.resize(dev + 1, nullptr);
   for (int attempt = 0; attempt < 2; attempt++) {
     if (!events[dev] &&
-        (e = cudaEventCreateWithFlags(&events[dev], cudaEventBlockingSync | cudaEventDisableTiming)) != cudaSuccess) {
+        cudaEventCreateWithFlags(&events[dev], cudaEventBlockingSync | cudaEventDisableTiming) != cudaSuccess) {
+      (void)cudaGetLastError();
       events[dev] = nullptr;
-      return e;
+      break;
     }
-    e = cudaEventRecord(events[dev], st);
-    if (e == cudaSuccess) return cudaEventSynchronize(events[dev]);
-    // an event left from before a device reset: make a new one, once
+    if (cudaEventRecord(events[dev], st) == cudaSuccess) return cudaEventSynchronize(events[dev]);
     (void)cudaGetLastError();
     events[dev] = nullptr;
   }
-  return e;
+  return cudaStreamSynchronize(st);
 }
 
 }  // namespace tmc
