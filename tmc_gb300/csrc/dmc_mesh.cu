@@ -13,7 +13,11 @@
 //    highest face index (the reference's last write), via atomicMax claims.
 //  * mark3333 (:1189-1322): marked faces cannot be adjacent and their vertices have valence 3, so
 //    no vertex is written twice; the neighbour flags are idempotent.
-//  * removal passes: order-preserving compaction through prefix sums.
+//  * removals (removeVertices3X3Y / removeQuadrilaterals3X3Y, their 3333 pair): the passes run in
+//    place, killing faces and re-targeting corners while every index stays; the halfedges are built
+//    once and repaired around the touched vertices after each pass (halfedges.cu,
+//    repair_halfedges), and one order-preserving compaction after the last pass gives the
+//    reference's numbering, since each of its per-pass compactions keeps the order of what remains.
 #include <cmath>
 
 #include "../../include/tmc_gb300.h"

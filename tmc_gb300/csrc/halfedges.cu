@@ -16,7 +16,9 @@
 // count, exclusive scan, scatter of (halfedge, target) pairs), so the halfedges of edge {a, b} are
 // the entries of a's list with target b and of b's list with target a.  Vertex lists are short
 // (valence ~4) and spatially coherent, so the pairing pass reads mostly from L2.  Sorting the few
-// ids of an edge restores the reference's insertion order.
+// ids of an edge restores the reference's insertion order.  After a simplification pass the
+// structure is repaired in place around the vertices the pass touched (repair_halfedges) instead
+// of built again.
 #include <climits>
 
 #include "halfedges.h"
