@@ -12,10 +12,14 @@
 // that neighbour's record.  No hash table, no atomics, deterministic output.
 //
 // Kernels:
-//   tmc_classify_kernel  per-cell record: owned crossed edges, inner vertex and triangle counts
-//                        (ambiguous cells run the full p_slice logic in counting mode)
+//   tmc_classify_kernel  per-cell record: owned crossed edges, table triangle counts; ambiguous
+//                        cells listed
+//   tmc_amb_key/cursor/sort_kernel  the ambiguous list sorted by MC case
+//   tmc_amb_count_kernel the ambiguous cells' p_slice (float64), once: counts into the cell records,
+//                        triangles (local codes) and inner-vertex parameters into AmbRec records
 //   tmc_offsets_kernel   in-tile scan -> per-cell vertex / triangle offsets
-//   tmc_emit_kernel      vertices (edge and inner) and triangles
+//   tmc_emit_kernel      edge vertices and table triangles
+//   tmc_ambiguous_kernel the ambiguous cells' triangles and inner vertices from their records
 #include "ffloat.cuh"
 #include "listing.cuh"
 #include "scan.cuh"
